@@ -1,0 +1,303 @@
+/*
+ * gbfv.h -- C ABI of the GB300-native ECFV/TPFA linearizer and Newton linear
+ * solve (BiCGStab + block ILU0).
+ *
+ * Everything here is plain C: pointers, sizes and status codes.  Host arrays
+ * are in the reference's natural (grid index) order; device-side layouts are
+ * private to the library.
+ *
+ * Reference interfaces each group of entry points replaces (paths inside
+ * OPM/opm-models):
+ *   - problem description   : tests/problems/lensproblem.hh:227-627,
+ *                             tests/problems/reservoirproblem.hh:215-736
+ *                             (what Problem::intrinsicPermeability/porosity/
+ *                             materialLawParams/boundary/constraints return)
+ *   - gbfv_linearize & co.  : opm/models/discretization/common/
+ *                             fvbaselinearizer.hh:133-375 (FvBaseLinearizer)
+ *   - gbfv_solve & co.      : opm/simulators/linalg/parallelbasebackend.hh:
+ *                             137-290 (prepare/setResidual/setMatrix/solve)
+ *   - gbfv_newton_*         : opm/models/nonlinear/newtonmethod.hh:228-845,
+ *                             opm/models/blackoil/blackoilnewtonmethod.hh:
+ *                             176-427
+ *   - gbfv_time_integration : opm/models/discretization/common/
+ *                             fvbaseproblem.hh:512-606
+ */
+#ifndef GBFV_H
+#define GBFV_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ */
+/* status codes (the reference throws; every entry point here returns)  */
+/* ------------------------------------------------------------------ */
+enum gbfv_status {
+    GBFV_OK = 0,
+    GBFV_ERR_ARG = 1,           /* invalid argument / size                  */
+    GBFV_ERR_CUDA = 2,          /* CUDA runtime error                       */
+    GBFV_ERR_OOM = 3,           /* device allocation failed                 */
+    GBFV_ERR_NUMERICAL = 4,     /* Opm::NumericalProblem equivalent         */
+    GBFV_ERR_NONFINITE = 5,     /* non-finite residual / update             */
+    GBFV_ERR_BREAKDOWN = 6,     /* BiCGStab breakdown (bicgstabsolver.hh)   */
+    GBFV_ERR_NOT_CONVERGED = 7, /* linear solver returned false             */
+    GBFV_ERR_TIMEOUT = 8,       /* a bounded device-side wait expired       */
+    GBFV_ERR_UNSUPPORTED = 9,   /* input outside what the kernels handle    */
+    GBFV_ERR_SINGULAR = 10,     /* ILU0 pivot block could not be inverted   */
+    GBFV_ERR_NO_DEVICE = 11     /* no CUDA device visible                   */
+};
+
+/* models (Properties::Model of the reference's type tags) */
+enum gbfv_model {
+    GBFV_MODEL_IMMISCIBLE_2P = 0, /* opm/models/immiscible, 2 phases, b = 2 */
+    GBFV_MODEL_BLACKOIL_3P = 1    /* opm/models/blackoil, 3 phases,  b = 3  */
+};
+
+/* material laws (opm-common MaterialLaw of the problems) */
+enum gbfv_law {
+    GBFV_LAW_REG_VAN_GENUCHTEN = 0, /* EffToAbsLaw<RegularizedVanGenuchten> */
+    GBFV_LAW_REG_BROOKS_COREY = 1,  /* EffToAbsLaw<RegularizedBrooksCorey>  */
+    GBFV_LAW_COREY3P = 2            /* 3-phase Corey kr, zero p_c (black-oil)*/
+};
+
+/* boundary condition kinds (ImmiscibleBoundaryRateVector setters) */
+enum gbfv_bc {
+    GBFV_BC_NOFLOW = 0,   /* setNoFlow()                                    */
+    GBFV_BC_FREEFLOW = 1, /* setFreeFlow(fs): Dirichlet state (p_w, S_w)    */
+    GBFV_BC_MASSRATE = 2  /* setMassRate(rate) [kg/(m^2 s)] per equation    */
+};
+
+/* black-oil primary-variable meanings (blackoilprimaryvariables.hh) */
+enum gbfv_pv_meaning {
+    GBFV_WATER_SW = 0,
+    GBFV_PRESSURE_PO = 0,
+    GBFV_GAS_SG = 0,
+    GBFV_GAS_RS = 1,
+    GBFV_GAS_RV = 2
+};
+
+/* solve precision */
+enum gbfv_precision {
+    GBFV_PREC_FP64 = 0,  /* everything FP64 (plain form)                      */
+    GBFV_PREC_MIXED = 1  /* FP64 outer refinement around FP32 BiCGStab/ILU0    */
+};
+
+/* material-law parameter record: GBFV_MAT_STRIDE doubles per material */
+#define GBFV_MAT_STRIDE 8
+/*  [0] law (enum gbfv_law, stored as double)
+ *  two-phase laws:  [1] S_wr  [2] S_nr
+ *    van Genuchten: [3] alpha [1/Pa]   [4] n
+ *    Brooks-Corey:  [3] entry pressure p_e [Pa]   [4] lambda
+ *  3-phase Corey:   [4] exponent  (residual saturations zero)              */
+
+/* black-oil PVT (BlackOilFluidSystem with LiveOilPvt / DryGasPvt /
+ * ConstantCompressibilityWaterPvt, reservoirproblem.hh:223-327)          */
+typedef struct gbfv_blackoil_pvt {
+    double rho_ref_oil, rho_ref_water, rho_ref_gas; /* surface densities     */
+    int32_t n_oil;            /* rows of the saturated live-oil table        */
+    const double* oil_p;      /* [n_oil] pressure [Pa], increasing           */
+    const double* oil_rs;     /* [n_oil] saturated R_s, increasing           */
+    const double* oil_bo;     /* [n_oil] saturated B_o                       */
+    const double* oil_mu;     /* [n_oil] saturated viscosity [Pa s]          */
+    double oil_compressibility; /* undersaturated d(1/B_o)/dp / (1/B_o) [1/Pa]*/
+    int32_t n_gas;
+    const double* gas_p;      /* [n_gas] pressure [Pa], increasing           */
+    const double* gas_bg;     /* [n_gas] B_g                                 */
+    const double* gas_mu;     /* [n_gas] viscosity [Pa s]                    */
+    double water_p_ref, water_bw_ref, water_compressibility, water_mu;
+} gbfv_blackoil_pvt;
+
+/* The problem: geometry, rock, boundary and constraint data of one grid.
+ * Cells and faces follow the reference's element / intersection order
+ * (YaspGrid: x fastest; intersections -x,+x,-y,+y,-z,+z).                */
+typedef struct gbfv_problem {
+    int32_t model;            /* enum gbfv_model                             */
+    int32_t num_cells;
+    int32_t num_conn;         /* interior intersections (2 per interior face)*/
+    int32_t num_bfaces;       /* boundary intersections                      */
+    /* cells */
+    const double* center;     /* [num_cells*3] cell centre (z = 0 in 2D)     */
+    const double* volume;     /* [num_cells]                                 */
+    const double* porosity;   /* [num_cells]                                 */
+    const double* perm;       /* [num_cells*3] diagonal of K                 */
+    const int32_t* material;  /* [num_cells] index into material_params      */
+    /* interior intersections, grouped per cell, in intersection order     */
+    const int32_t* conn_ptr;  /* [num_cells+1]                               */
+    const int32_t* conn_nbr;  /* [num_conn] neighbour cell                   */
+    const int32_t* conn_dir;  /* [num_conn] local intersection index (0..5)  */
+    const double* conn_normal;/* [num_conn*3] unit outer normal              */
+    const double* conn_center;/* [num_conn*3] integration point              */
+    const double* conn_area;  /* [num_conn]                                  */
+    /* boundary intersections, grouped per cell, in intersection order     */
+    const int32_t* bface_ptr; /* [num_cells+1]                               */
+    const double* bface_normal;/* [num_bfaces*3]                             */
+    const double* bface_center;/* [num_bfaces*3]                             */
+    const double* bface_area; /* [num_bfaces]                                */
+    const int32_t* bface_type;/* [num_bfaces] enum gbfv_bc                   */
+    const double* bface_value;/* [num_bfaces*4] FREEFLOW: p_w, S_w;
+                                 MASSRATE: rate per equation                 */
+    /* constraints (FvBaseConstraints; wells of the reservoir problem)     */
+    const int32_t* constraint;/* [num_cells] -1 = free, else row of below     */
+    int32_t num_constraints;
+    const double* constraint_pv;        /* [num_constraints*3]               */
+    const int32_t* constraint_meaning;  /* [num_constraints] gas meaning      */
+    /* parameters */
+    double gravity[3];
+    int32_t num_materials;
+    const double* material_params;      /* [num_materials*GBFV_MAT_STRIDE]   */
+    double rho[2], mu[2];     /* immiscible: constant liquid density/visc.   */
+    const gbfv_blackoil_pvt* pvt; /* black-oil only, else NULL               */
+    double temperature;
+} gbfv_problem;
+
+/* run-time parameters; names and defaults follow the reference's
+ * Opm::Parameters (newtonmethodparameters.hh:31-53, linalgparameters.hh:
+ * 41-78, blackoilnewtonmethodparameters.hh, fvbaseparameters.hh)        */
+typedef struct gbfv_params {
+    double newton_tolerance;          /* NewtonTolerance            1e-8    */
+    int32_t newton_max_iterations;    /* NewtonMaxIterations        20      */
+    int32_t newton_target_iterations; /* NewtonTargetIterations     10      */
+    double newton_max_error;          /* NewtonMaxError             1e100   */
+    double linear_tolerance;          /* LinearSolverTolerance      1e-3    */
+    double linear_abs_tolerance;      /* LinearSolverAbsTolerance  -1       */
+    int32_t linear_max_iterations;    /* LinearSolverMaxIterations  1000    */
+    double linear_max_error;          /* LinearSolverMaxError       1e7     */
+    int32_t precision;                /* enum gbfv_precision                */
+    double inner_tolerance;           /* mixed: FP32 inner reduction  1e-3  */
+    int32_t max_refinements;          /* mixed: outer FP64 refinement steps */
+    double dp_max_rel;                /* DpMaxRel                   0.3     */
+    double ds_max;                    /* DsMax                      0.2     */
+    double pv_oscillation_threshold;  /* PriVarOscilationThreshold  1e-5    */
+    double pressure_min, pressure_max;/* PressureMin/PressureMax            */
+    double max_water_saturation;      /* MaximumWaterSaturation     1.0     */
+    double water_only_threshold;      /* WaterOnlyThreshold         1.0     */
+    double min_time_step;             /* MinTimeStepSize            0       */
+    double max_time_step;             /* MaxTimeStepSize            inf     */
+    int32_t max_time_step_divisions;  /* MaxTimeStepDivisions       10      */
+} gbfv_params;
+
+/* fill *p with the reference's defaults */
+void gbfv_default_params(gbfv_params* p);
+
+/* ------------------------------------------------------------------ */
+/* context: one grid (or a batch of grids, see gbfv_batch_*)            */
+/* ------------------------------------------------------------------ */
+typedef struct gbfv_ctx gbfv_ctx;
+
+/* Create a context on the current CUDA device and upload the problem.
+ * Mirrors FvBaseLinearizer::init + createMatrix_ (fvbaselinearizer.hh:
+ * 418-452): the sparsity pattern, level sets and block-slot maps are built
+ * once here.  *status receives the result; NULL is returned on error.    */
+gbfv_ctx* gbfv_create(const gbfv_problem* prob, const gbfv_params* params,
+                      int* status);
+int gbfv_destroy(gbfv_ctx* ctx);
+int gbfv_set_params(gbfv_ctx* ctx, const gbfv_params* params);
+/* equations per cell (2 or 3) and number of cells */
+int gbfv_dims(const gbfv_ctx* ctx, int* num_cells, int* block_size,
+              int* nnz_blocks);
+
+/* model().solution(timeIdx) (fvbasediscretization.hh): primary variables in
+ * natural order, [num_cells*b]; meanings [num_cells] (black-oil gas
+ * meaning, enum gbfv_pv_meaning; ignored for the immiscible model).       */
+int gbfv_set_solution(gbfv_ctx* ctx, const double* pv,
+                      const int32_t* meaning);
+int gbfv_get_solution(gbfv_ctx* ctx, double* pv, int32_t* meaning);
+
+/* simulator().timeStepSize() and newtonMethod().numIterations(), which the
+ * storage cache reads (fvbaselocalresidual.hh:535-571)                    */
+int gbfv_set_timestep(gbfv_ctx* ctx, double dt);
+int gbfv_set_newton_iteration(gbfv_ctx* ctx, int iteration);
+
+/* FvBaseLinearizer::linearizeDomain (fvbaselinearizer.hh:201-241):
+ * residual and Jacobian of the current solution, on the device.  Applies
+ * the constraints to the solution first and to the system afterwards
+ * (:630-666).                                                             */
+int gbfv_linearize(gbfv_ctx* ctx);
+/* linearizer.residual() -> [num_cells*b], natural order                   */
+int gbfv_get_residual(gbfv_ctx* ctx, double* residual);
+/* linearizer.jacobian().istlMatrix() as BCRS, natural order, columns sorted
+ * ascending in each row; blocks row-major b*b, entry [eq][pv].
+ * row_ptr[num_cells+1], col_idx[nnz], blocks[nnz*b*b]                     */
+int gbfv_get_jacobian(gbfv_ctx* ctx, int32_t* row_ptr, int32_t* col_idx,
+                      double* blocks);
+
+/* NewtonMethod::preSolve_ error: max_{dof,eq} |r * eqWeight| over
+ * unconstrained cells (newtonmethod.hh:572-607)                           */
+int gbfv_newton_error(gbfv_ctx* ctx, double* error);
+
+/* ParallelBiCGStabSolverBackend: prepare + setResidual + setMatrix + solve
+ * (parallelbasebackend.hh:182-284) on the current linearization.  Solves
+ * J dx = r; dx [num_cells*b] natural order (may be NULL to keep it on the
+ * device for gbfv_newton_update).  iterations: BiCGStab iterations (sum of
+ * inner iterations in mixed precision).  Returns GBFV_OK when converged,
+ * GBFV_ERR_NOT_CONVERGED / GBFV_ERR_BREAKDOWN otherwise.                  */
+int gbfv_solve(gbfv_ctx* ctx, double* dx, int* iterations);
+
+/* NewtonMethod::update_ / BlackOilNewtonMethod::updatePrimaryVariables_:
+ * x <- x - dx with chopping and primary-variable switching, using the dx
+ * of the last gbfv_solve.  num_switched may be NULL.                      */
+int gbfv_newton_update(gbfv_ctx* ctx, int* num_switched);
+
+/* NewtonMethod::apply (newtonmethod.hh:228-438) for one time step of size
+ * dt.  converged: 1/0.  iterations: numIterations() after the call
+ * (2*target on failure, as failed_()).  linear_iterations: total.         */
+typedef struct gbfv_newton_report {
+    int32_t converged;
+    int32_t iterations;
+    int32_t linear_iterations;
+    int32_t linearizations;
+    int32_t refinements;       /* mixed precision: outer refinement steps   */
+    int32_t status;            /* GBFV_OK or the error that ended it        */
+    double error;              /* last Newton error                         */
+} gbfv_newton_report;
+int gbfv_newton_apply(gbfv_ctx* ctx, double dt, gbfv_newton_report* rep);
+
+/* NewtonMethod::suggestTimeStepSize (newtonmethod.hh:448-465)              */
+double gbfv_suggest_time_step(const gbfv_ctx* ctx, double old_dt,
+                              int newton_iterations);
+
+/* FvBaseProblem::timeIntegration + Simulator time loop (fvbaseproblem.hh:
+ * 512-606): num_steps time steps starting at dt0 (dt halving on failure,
+ * dt control by Newton iterations unless fixed_dt != 0).  Per-step stats
+ * (each may be NULL): dt used, Newton iterations, linear iterations.      */
+int gbfv_time_integration(gbfv_ctx* ctx, int num_steps, double dt0,
+                          double end_time, int fixed_dt, double* step_dt,
+                          int32_t* step_newton, int32_t* step_linear,
+                          int32_t* total_linearizations);
+
+/* ------------------------------------------------------------------ */
+/* stand-alone linear-solver backend over a host BCRS matrix            */
+/* (ParallelBiCGStabSolverBackend used without the linearizer)          */
+/* ------------------------------------------------------------------ */
+typedef struct gbfv_linsolver gbfv_linsolver;
+/* prepare(M): pattern of an n x n block matrix, blocks b x b (b = 2, 3),
+ * columns sorted ascending per row, diagonal present.                     */
+gbfv_linsolver* gbfv_linsolver_create(int n, int b, const int32_t* row_ptr,
+                                      const int32_t* col_idx,
+                                      const gbfv_params* params, int* status);
+int gbfv_linsolver_destroy(gbfv_linsolver* s);
+/* setMatrix(M): values [nnz*b*b] row-major blocks                         */
+int gbfv_linsolver_set_matrix(gbfv_linsolver* s, const double* blocks);
+/* setResidual(b) + solve(x): x = A^-1 rhs, iterations as gbfv_solve       */
+int gbfv_linsolver_solve(gbfv_linsolver* s, const double* rhs, double* x,
+                         int* iterations);
+
+/* ------------------------------------------------------------------ */
+/* diagnostics                                                          */
+/* ------------------------------------------------------------------ */
+/* kernel launches issued by this library since load                       */
+int64_t gbfv_kernel_launches(void);
+/* last CUDA error string for the calling thread ("" if none)              */
+const char* gbfv_last_error(void);
+/* per-phase device time of the last gbfv_newton_apply, milliseconds:
+ * [0] linearize, [1] solver-format conversion + ILU0 factorization,
+ * [2] Krylov iterations, [3] Newton update + error                       */
+int gbfv_phase_times(const gbfv_ctx* ctx, double* ms4);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBFV_H */

@@ -1,0 +1,1310 @@
+// Host side of libgbfv: the C ABI declared in include/gbfv.h.
+//
+// Set-up (gbfv_create) does once what the reference does once per grid in
+// FvBaseLinearizer::createMatrix_ (fvbaselinearizer.hh:418-452) and
+// ParallelBaseBackend::prepare (parallelbasebackend.hh:182-210): it builds
+// the sparsity pattern, orders cells wavefront-major (see
+// gbfv_internal.cuh), precomputes per-face geometry and transmissibility
+// factors, boundary fluid states and the ILU(0) level sets, and uploads
+// everything.  The Newton driver (gbfv_newton_apply) follows
+// NewtonMethod::apply (newtonmethod.hh:228-438); each iteration reads back
+// two scalars (Newton error, solver status).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+
+#include "../../include/gbfv.h"
+#include "gbfv_internal.cuh"
+#include "solver.cuh"
+
+namespace gbfv {
+int64_t g_launches = 0;
+}
+
+using namespace gbfv;
+
+namespace {
+
+thread_local std::string t_lastError;
+
+void setError(const std::string& s) { t_lastError = s; }
+
+#define CK(call)                                                                        \
+    do {                                                                                \
+        cudaError_t e_ = (call);                                                        \
+        if (e_ != cudaSuccess) {                                                        \
+            setError(std::string(#call) + ": " + cudaGetErrorString(e_));              \
+            return e_ == cudaErrorMemoryAllocation ? GBFV_ERR_OOM : GBFV_ERR_CUDA;      \
+        }                                                                               \
+    } while (0)
+
+template <class T>
+int devAlloc(T** p, size_t n)
+{
+    *p = nullptr;
+    if (n == 0) n = 1;
+    CK(cudaMalloc((void**)p, n * sizeof(T)));
+    return GBFV_OK;
+}
+
+template <class T>
+int upload(T** p, const std::vector<T>& v)
+{
+    int st = devAlloc(p, v.size());
+    if (st) return st;
+    if (!v.empty()) CK(cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return GBFV_OK;
+}
+
+double harmonicMean(double x, double y)
+{
+    if (x * y <= 0) return 0.0;
+    return (2 * x * y) / (x + y);
+}
+
+// solver-side structure shared by the grid context and the stand-alone
+// linear solver: ELL columns, level sets, factor and Krylov storage
+struct SolverData {
+    int N = 0, b = 0, dim = 0, nslot = 0, ldN = 0;
+    std::vector<int> levPtr;  // host copy
+    int* col = nullptr;
+    int* levPtrD = nullptr;
+    double* FL64 = nullptr;
+    double* FD64 = nullptr;
+    float* A32 = nullptr;
+    float* FL32 = nullptr;
+    float* FD32 = nullptr;
+    double* v64[6] = {};  // x r p v y z
+    float* v32[7] = {};   // rhs x r p v y z
+    double* xref = nullptr;
+    double* rref = nullptr;
+    double* partial = nullptr;
+    unsigned* bar = nullptr;  // count, gen, abort
+    int nblocks64 = 1, nblocks32 = 1;
+    double lastMs[4] = {0, 0, 0, 0};
+};
+
+int allocSolver(SolverData& S, int maxBlocksOverride = 0)
+{
+    const size_t ld = S.ldN, bb = (size_t)S.b * S.b;
+    int st;
+    if ((st = devAlloc(&S.FL64, S.dim * bb * ld))) return st;
+    if ((st = devAlloc(&S.FD64, bb * ld))) return st;
+    if ((st = devAlloc(&S.A32, S.nslot * bb * ld))) return st;
+    if ((st = devAlloc(&S.FL32, S.dim * bb * ld))) return st;
+    if ((st = devAlloc(&S.FD32, bb * ld))) return st;
+    for (auto& p : S.v64)
+        if ((st = devAlloc(&p, (size_t)S.N * S.b))) return st;
+    for (auto& p : S.v32)
+        if ((st = devAlloc(&p, (size_t)S.N * S.b))) return st;
+    if ((st = devAlloc(&S.xref, (size_t)S.N * S.b))) return st;
+    if ((st = devAlloc(&S.rref, (size_t)S.N * S.b))) return st;
+    // persistent-kernel grid: one block for small systems (barriers are then
+    // __syncthreads), otherwise as many co-resident blocks as useful
+    const int smallN = 12288;
+    auto pick = [&](int maxb) {
+        if (maxBlocksOverride > 0) return std::min(maxBlocksOverride, maxb);
+        if (S.N <= smallN) return 1;
+        const int want = (S.N + SOLVER_THREADS - 1) / SOLVER_THREADS;
+        return std::max(1, std::min(maxb, want));
+    };
+    S.nblocks64 = pick(maxSolverBlocks<double>(S.b));
+    S.nblocks32 = pick(maxSolverBlocks<float>(S.b));
+    const int nbMax = std::max(S.nblocks64, S.nblocks32);
+    if ((st = devAlloc(&S.partial, 4 * (size_t)nbMax))) return st;
+    if ((st = devAlloc(&S.bar, 4))) return st;
+    CK(cudaMemset(S.bar, 0, 4 * sizeof(unsigned)));
+    return GBFV_OK;
+}
+
+void freeSolver(SolverData& S)
+{
+    cudaFree(S.col);
+    cudaFree(S.levPtrD);
+    cudaFree(S.FL64);
+    cudaFree(S.FD64);
+    cudaFree(S.A32);
+    cudaFree(S.FL32);
+    cudaFree(S.FD32);
+    for (auto p : S.v64) cudaFree(p);
+    for (auto p : S.v32) cudaFree(p);
+    cudaFree(S.xref);
+    cudaFree(S.rref);
+    cudaFree(S.partial);
+    cudaFree(S.bar);
+}
+
+
+
+}  // namespace
+
+// ===================================================================== ctx
+struct gbfv_ctx {
+    int N = 0, b = 0, dim = 0, model = 0, ldN = 0;
+    gbfv_params prm;
+    cudaStream_t stream = nullptr;
+    std::vector<int> perm, iperm;  // natural -> internal, internal -> natural
+    DevMesh mesh{};
+    DevPhysics hphys{};
+    DevPhysics* dphys = nullptr;
+    // device state
+    double *x = nullptr, *xOld = nullptr, *storageOld = nullptr, *residual = nullptr, *jval = nullptr;
+    int *meaning = nullptr, *meaningOld = nullptr, *wasSwitched = nullptr;
+    IqBuffers iq{};
+    double* dx = nullptr;
+    SolverData S;
+    DevStatus* st = nullptr;
+    DevStatus* hst = nullptr;  // pinned
+    // owned device arrays of the mesh
+    std::vector<void*> owned;
+    // natural BCRS view
+    std::vector<int> bcrsRowPtr, bcrsCol, bcrsSlot, bcrsRow;
+    double dt = 1.0;
+    int newtonIter = 0;
+    int numIterations = 0;
+    double error = 0, lastError = 0;
+    int haveDx = 0;
+    cudaEvent_t ev[6];
+    double phaseMs[4] = {0, 0, 0, 0};
+    int lastIterations = 0, lastRefinements = 0;
+};
+
+struct gbfv_linsolver {
+    int N = 0, b = 0;
+    gbfv_params prm;
+    cudaStream_t stream = nullptr;
+    SolverData S;
+    std::vector<int> perm, iperm;
+    std::vector<int> rowPtr, colN;
+    std::vector<int> entSlot, entRow;  // BCRS entry -> (slot, internal row)
+    double* A64 = nullptr;
+    double* A64host = nullptr;  // pinned staging
+    double* rhs = nullptr;
+    DevStatus* st = nullptr;
+    DevStatus* hst = nullptr;
+    double* stage = nullptr;    // pinned vector staging
+};
+
+namespace {
+
+int syncStatus(cudaStream_t s, DevStatus* d, DevStatus* h)
+{
+    CK(cudaMemcpyAsync(h, d, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return GBFV_OK;
+}
+
+int resetStatus(cudaStream_t s, DevStatus* d)
+{
+    CK(cudaMemsetAsync(d, 0, sizeof(DevStatus), s));
+    return GBFV_OK;
+}
+
+// levels and wavefront-major order from a lower-triangular dependency walk
+void buildOrder(int N, const std::vector<std::vector<int>>& lower, std::vector<int>& perm,
+                std::vector<int>& iperm, std::vector<int>& levPtr)
+{
+    std::vector<int> level(N, 0);
+    int maxLev = 0;
+    for (int i = 0; i < N; ++i) {
+        int l = 0;
+        for (int k : lower[i]) l = std::max(l, level[k] + 1);
+        level[i] = l;
+        maxLev = std::max(maxLev, l);
+    }
+    std::vector<int> cnt(maxLev + 2, 0);
+    for (int i = 0; i < N; ++i) cnt[level[i] + 1]++;
+    for (int l = 0; l <= maxLev; ++l) cnt[l + 1] += cnt[l];
+    levPtr.assign(cnt.begin(), cnt.end());
+    iperm.assign(N, 0);
+    perm.assign(N, 0);
+    std::vector<int> pos(cnt.begin(), cnt.end() - 1);
+    for (int i = 0; i < N; ++i) {  // natural order inside a level
+        const int p = pos[level[i]]++;
+        iperm[p] = i;
+        perm[i] = p;
+    }
+}
+
+// solver-precision iteration; returns status and fills iterations
+template <class T>
+int runKrylov(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hst, const T* A, T* FL, T* FD,
+              const T* rhs, T* const* vec, int factor, double redTol, double absTol, double maxRes,
+              int maxIter, int nblocks, int& iters)
+{
+    KArgs<T> a;
+    a.N = S.N;
+    a.ldN = S.ldN;
+    a.dim = S.dim;
+    a.nslot = S.nslot;
+    a.numLev = (int)S.levPtr.size() - 1;
+    a.col = S.col;
+    a.levPtr = S.levPtrD;
+    a.A = A;
+    a.FL = FL;
+    a.FD = FD;
+    a.rhs = rhs;
+    a.x = vec[0];
+    a.r = vec[1];
+    a.p = vec[2];
+    a.v = vec[3];
+    a.y = vec[4];
+    a.z = vec[5];
+    a.partial = S.partial;
+    a.gs.count = S.bar;
+    a.gs.gen = S.bar + 1;
+    a.gs.abort = (int*)(S.bar + 2);
+    a.st = st;
+    a.redTol = redTol;
+    a.absTol = absTol;
+    a.maxRes = maxRes;
+    a.maxIter = maxIter;
+    a.factor = factor;
+    int rs;
+    if ((rs = resetStatus(stream, st))) return rs;
+    CK(cudaMemsetAsync(S.bar, 0, 4 * sizeof(unsigned), stream));
+    const int ls = launchBicgstab<T>(a, S.b, nblocks, stream);
+    if (ls != GBFV_OK) {
+        setError(std::string("cooperative launch failed: ") + cudaGetErrorString(cudaGetLastError()));
+        return ls;
+    }
+    if ((rs = syncStatus(stream, st, hst))) return rs;
+    iters = hst->iterations;
+    if (hst->code) return hst->code;
+    return hst->converged ? GBFV_OK : GBFV_ERR_NOT_CONVERGED;
+}
+
+double absTolOf(const gbfv_params& p)
+{
+    return p.linear_abs_tolerance < 0 ? p.newton_tolerance / 100.0 : p.linear_abs_tolerance;
+}
+
+// FP64 BiCGStab + ILU0 (plain form): solves A x = rhs into S.v64[0]
+int solvePlain(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hst, const double* A,
+               const double* rhs, const gbfv_params& prm, int& iters)
+{
+    return runKrylov<double>(S, stream, st, hst, A, S.FL64, S.FD64, rhs, S.v64, 1, prm.linear_tolerance,
+                             absTolOf(prm), prm.linear_max_error, prm.linear_max_iterations, S.nblocks64,
+                             iters);
+}
+
+// FP32 BiCGStab + FP32 ILU0 under FP64 iterative refinement (mixed form):
+// solution in S.xref (FP64)
+int solveMixed(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hst, const double* A,
+               const double* rhs, const gbfv_params& prm, int& iters, int& refinements)
+{
+    const long nval = (long)S.nslot * S.b * S.b * S.ldN;
+    launchCastMatrix(A, S.A32, nval, stream);
+    const int n = S.N * S.b;
+    CK(cudaMemsetAsync(S.xref, 0, sizeof(double) * n, stream));
+    // r = b - A*0 = b, its max-norm and FP32 copy
+    int rs;
+    if ((rs = resetStatus(stream, st))) return rs;
+    launchResidual64(S.N, S.ldN, S.nslot, S.b, S.col, A, rhs, S.xref, S.rref, S.v32[0], st, stream);
+    if ((rs = syncStatus(stream, st, hst))) return rs;
+    const double eps = std::numeric_limits<double>::min() * 1e10;
+    double resErr;
+    {
+        unsigned long long bits = hst->errorBits;
+        std::memcpy(&resErr, &bits, sizeof(double));
+    }
+    resErr = std::max(resErr, eps);
+    const double resErr0 = resErr;
+    const double absTol = absTolOf(prm);
+    auto converged = [&](double re) {
+        return re / std::max(1e-20, resErr0) <= prm.linear_tolerance || re <= absTol;
+    };
+    iters = 0;
+    refinements = 0;
+    if (converged(resErr)) return GBFV_OK;
+    for (int ref = 0; ref < std::max(1, prm.max_refinements); ++ref) {
+        const double target = std::max(prm.linear_tolerance * resErr0, absTol);
+        const double need = target / resErr;
+        const double innerTol = std::min(0.5, std::max(0.5 * need, prm.inner_tolerance));
+        int it = 0;
+        float* vec[6] = {S.v32[1], S.v32[2], S.v32[3], S.v32[4], S.v32[5], S.v32[6]};
+        const int ks = runKrylov<float>(S, stream, st, hst, S.A32, S.FL32, S.FD32, S.v32[0], vec, ref == 0,
+                                        innerTol, 0.0, prm.linear_max_error * resErr0 / resErr,
+                                        prm.linear_max_iterations, S.nblocks32, it);
+        iters += it;
+        refinements++;
+        if (ks != GBFV_OK && ks != GBFV_ERR_NOT_CONVERGED) return ks;
+        launchAccumulate(n, S.xref, S.v32[1], stream);
+        if ((rs = resetStatus(stream, st))) return rs;
+        launchResidual64(S.N, S.ldN, S.nslot, S.b, S.col, A, rhs, S.xref, S.rref, S.v32[0], st, stream);
+        if ((rs = syncStatus(stream, st, hst))) return rs;
+        unsigned long long bits = hst->errorBits;
+        std::memcpy(&resErr, &bits, sizeof(double));
+        if (!std::isfinite(resErr)) return GBFV_ERR_NONFINITE;
+        if (converged(resErr)) return GBFV_OK;
+        if (resErr > prm.linear_max_error * resErr0) return GBFV_ERR_NOT_CONVERGED;
+        if (ks == GBFV_ERR_NOT_CONVERGED && it >= prm.linear_max_iterations) return GBFV_ERR_NOT_CONVERGED;
+    }
+    return GBFV_ERR_NOT_CONVERGED;
+}
+
+}  // namespace
+
+extern "C" {
+
+void gbfv_default_params(gbfv_params* p)
+{
+    std::memset(p, 0, sizeof(*p));
+    p->newton_tolerance = 1e-8;
+    p->newton_max_iterations = 20;
+    p->newton_target_iterations = 10;
+    p->newton_max_error = 1e100;
+    p->linear_tolerance = 1e-3;
+    p->linear_abs_tolerance = -1.0;
+    p->linear_max_iterations = 1000;
+    p->linear_max_error = 1e7;
+    p->precision = GBFV_PREC_FP64;
+    p->inner_tolerance = 1e-3;
+    p->max_refinements = 20;
+    p->dp_max_rel = 0.3;
+    p->ds_max = 0.2;
+    p->pv_oscillation_threshold = 1e-5;
+    p->pressure_min = -1e99;
+    p->pressure_max = 1e99;
+    p->max_water_saturation = 1.0;
+    p->water_only_threshold = 1.0;
+    p->min_time_step = 0.0;
+    p->max_time_step = std::numeric_limits<double>::infinity();
+    p->max_time_step_divisions = 10;
+}
+
+int64_t gbfv_kernel_launches(void) { return g_launches; }
+const char* gbfv_last_error(void) { return t_lastError.c_str(); }
+
+static int createImpl(gbfv_ctx* C, const gbfv_problem* P)
+{
+    const int N = P->num_cells;
+    if (N <= 0 || !P->center || !P->volume || !P->porosity || !P->perm || !P->material || !P->conn_ptr ||
+        !P->conn_nbr || !P->conn_normal || !P->conn_center || !P->conn_area || !P->bface_ptr) {
+        setError("incomplete problem description");
+        return GBFV_ERR_ARG;
+    }
+    if (P->model != GBFV_MODEL_IMMISCIBLE_2P && P->model != GBFV_MODEL_BLACKOIL_3P) return GBFV_ERR_ARG;
+    if (P->model == GBFV_MODEL_BLACKOIL_3P && !P->pvt) return GBFV_ERR_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        setError("no CUDA device");
+        return GBFV_ERR_NO_DEVICE;
+    }
+    C->N = N;
+    C->model = P->model;
+    C->b = P->model == GBFV_MODEL_BLACKOIL_3P ? 3 : 2;
+    const int b = C->b;
+    // dimension from the face normals
+    int dim = 2;
+    for (int c = 0; c < P->num_conn && dim == 2; ++c)
+        if (P->conn_normal[3 * c + 2] != 0.0) dim = 3;
+    for (int f = 0; f < P->num_bfaces && dim == 2; ++f)
+        if (P->bface_normal[3 * f + 2] != 0.0) dim = 3;
+    if (P->model == GBFV_MODEL_BLACKOIL_3P) dim = 3;
+    C->dim = dim;
+    const int ndir = 2 * dim;
+    // neighbour per (cell, direction); verify axis-aligned geometry
+    std::vector<int> nbrDir((size_t)N * ndir, -1), connOf((size_t)N * ndir, -1);
+    auto axisOf = [&](const double* n, int& axis, double& sgn) {
+        int cnt = 0;
+        for (int d = 0; d < 3; ++d)
+            if (n[d] != 0.0) { axis = d; sgn = n[d]; ++cnt; }
+        return cnt == 1 && (sgn == 1.0 || sgn == -1.0);
+    };
+    for (int I = 0; I < N; ++I) {
+        for (int c = P->conn_ptr[I]; c < P->conn_ptr[I + 1]; ++c) {
+            int axis = 0;
+            double sgn = 0;
+            if (!axisOf(&P->conn_normal[3 * c], axis, sgn) || axis >= dim) {
+                setError("only axis-aligned (Cartesian) faces are supported");
+                return GBFV_ERR_UNSUPPORTED;
+            }
+            const int J = P->conn_nbr[c];
+            if (J < 0 || J >= N) return GBFV_ERR_ARG;
+            for (int d = 0; d < 3; ++d) {
+                if (d == axis) continue;
+                if (P->center[3 * J + d] != P->center[3 * I + d] || P->conn_center[3 * c + d] != P->center[3 * I + d]) {
+                    setError("face centres must share the off-axis coordinates of the cell centres");
+                    return GBFV_ERR_UNSUPPORTED;
+                }
+            }
+            const int dir = 2 * axis + (sgn > 0 ? 1 : 0);
+            if (nbrDir[(size_t)I * ndir + dir] >= 0) {
+                setError("two neighbours in one direction");
+                return GBFV_ERR_UNSUPPORTED;
+            }
+            nbrDir[(size_t)I * ndir + dir] = J;
+            connOf[(size_t)I * ndir + dir] = c;
+        }
+    }
+    // symmetric pattern and natural column order matching the slot order
+    for (int I = 0; I < N; ++I) {
+        int prevLower = -1;
+        for (int s = 0; s < dim; ++s) {  // slots -z..-x: dirs 2(dim-1-s)
+            const int J = nbrDir[(size_t)I * ndir + 2 * (dim - 1 - s)];
+            if (J < 0) continue;
+            if (J >= I || J <= prevLower) {
+                setError("cell numbering is not the structured natural order");
+                return GBFV_ERR_UNSUPPORTED;
+            }
+            prevLower = J;
+        }
+        int prevUpper = I;
+        for (int a = 0; a < dim; ++a) {
+            const int J = nbrDir[(size_t)I * ndir + 2 * a + 1];
+            if (J < 0) continue;
+            if (J <= prevUpper) {
+                setError("cell numbering is not the structured natural order");
+                return GBFV_ERR_UNSUPPORTED;
+            }
+            prevUpper = J;
+            if (nbrDir[(size_t)J * ndir + 2 * a] != I) {
+                setError("asymmetric connectivity");
+                return GBFV_ERR_UNSUPPORTED;
+            }
+        }
+    }
+    // ILU(0) update structure: lower entry k of row i may only update (i,i)
+    for (int I = 0; I < N; ++I)
+        for (int a = 0; a < dim; ++a) {
+            const int K = nbrDir[(size_t)I * ndir + 2 * a];
+            if (K < 0) continue;
+            for (int a2 = 0; a2 < dim; ++a2) {
+                const int Kup = nbrDir[(size_t)K * ndir + 2 * a2 + 1];
+                if (Kup < 0 || Kup == I) continue;
+                for (int d = 0; d < ndir; ++d)
+                    if (nbrDir[(size_t)I * ndir + d] == Kup) {
+                        setError("pattern has ILU(0) fill interactions beyond the diagonal");
+                        return GBFV_ERR_UNSUPPORTED;
+                    }
+            }
+        }
+    // wavefront-major order
+    std::vector<std::vector<int>> lower(N);
+    for (int I = 0; I < N; ++I)
+        for (int a = 0; a < dim; ++a) {
+            const int K = nbrDir[(size_t)I * ndir + 2 * a];
+            if (K >= 0) lower[I].push_back(K);
+        }
+    std::vector<int> levPtr;
+    buildOrder(N, lower, C->perm, C->iperm, levPtr);
+    const int ld = ((N + 63) / 64) * 64;
+    C->ldN = ld;
+    const auto& perm = C->perm;
+    const auto& iperm = C->iperm;
+    // per-direction geometry in internal order
+    std::vector<int> hNbr((size_t)ndir * ld, -1);
+    std::vector<double> hDTot((size_t)ndir * ld, 0), hGIn((size_t)ndir * ld, 0), hGEx((size_t)ndir * ld, 0),
+        hKh((size_t)ndir * ld, 0), hArea((size_t)ndir * ld, 0);
+    const double* g = P->gravity;
+    for (int p = 0; p < N; ++p) {
+        const int I = iperm[p];
+        const double* xI = &P->center[3 * I];
+        for (int dir = 0; dir < ndir; ++dir) {
+            const int J = nbrDir[(size_t)I * ndir + dir];
+            if (J < 0) continue;
+            const int c = connOf[(size_t)I * ndir + dir];
+            const int axis = dir / 2;
+            const double* xJ = &P->center[3 * J];
+            const double* xf = &P->conn_center[3 * c];
+            const size_t o = (size_t)dir * ld + p;
+            hNbr[o] = perm[J];
+            hDTot[o] = xJ[axis] - xI[axis];
+            double gIn = 0.0, gEx = 0.0;
+            for (int d = 0; d < 3; ++d) gIn += g[d] * (xI[d] - xf[d]);
+            for (int d = 0; d < 3; ++d) gEx += g[d] * (xJ[d] - xf[d]);
+            hGIn[o] = gIn;
+            hGEx[o] = gEx;
+            hKh[o] = harmonicMean(P->perm[3 * I + axis], P->perm[3 * J + axis]);
+            hArea[o] = P->conn_area[c];
+        }
+    }
+    std::vector<double> hVol(ld, 1.0), hPor(ld, 0.0), hPerm((size_t)3 * ld, 0.0);
+    std::vector<int> hMat(ld, 0), hCflag(ld, -1);
+    for (int p = 0; p < N; ++p) {
+        const int I = iperm[p];
+        hVol[p] = P->volume[I];
+        hPor[p] = P->porosity[I];
+        for (int d = 0; d < 3; ++d) hPerm[(size_t)d * ld + p] = P->perm[3 * I + d];
+        hMat[p] = P->material[I];
+        if (hMat[p] < 0 || hMat[p] >= P->num_materials || P->num_materials > MAX_MATERIALS) {
+            setError("material index out of range");
+            return GBFV_ERR_ARG;
+        }
+        hCflag[p] = P->constraint ? P->constraint[I] : -1;
+    }
+    // physics parameters
+    DevPhysics& ph = C->hphys;
+    std::memset(&ph, 0, sizeof(ph));
+    ph.numMaterials = P->num_materials;
+    for (int m = 0; m < P->num_materials; ++m) {
+        const double* mp = P->material_params + m * GBFV_MAT_STRIDE;
+        const int law = (int)mp[0];
+        TwoPhaseLaw& L = ph.law[m];
+        std::memset(&L, 0, sizeof(L));
+        if (law == GBFV_LAW_REG_VAN_GENUCHTEN || law == GBFV_LAW_REG_BROOKS_COREY) {
+            L.law = law == GBFV_LAW_REG_VAN_GENUCHTEN ? 0 : 1;
+            L.Swr = mp[1];
+            L.Snr = mp[2];
+            if (L.law == 0) { L.alpha = mp[3]; L.n = mp[4]; }
+            else { L.pe = mp[3]; L.lambda = mp[4]; }
+            finalizeLaw(L);
+        }
+        ph.coreyN[m] = law == GBFV_LAW_COREY3P ? mp[4] : 2.0;
+    }
+    ph.rho[0] = P->rho[0];
+    ph.rho[1] = P->rho[1];
+    ph.mu[0] = P->mu[0];
+    ph.mu[1] = P->mu[1];
+    if (P->pvt) {
+        const gbfv_blackoil_pvt& t = *P->pvt;
+        if (t.n_oil < 2 || t.n_oil > GBFV_MAX_TABLE || t.n_gas < 2 || t.n_gas > GBFV_MAX_TABLE) {
+            setError("PVT table size outside [2, 32]");
+            return GBFV_ERR_ARG;
+        }
+        BlackOilPvt& v = ph.pvt;
+        v.rhoRefO = t.rho_ref_oil;
+        v.rhoRefW = t.rho_ref_water;
+        v.rhoRefG = t.rho_ref_gas;
+        v.rsSat.n = v.pBubble.n = v.invBoSat.n = v.muoSat.n = t.n_oil;
+        for (int i = 0; i < t.n_oil; ++i) {
+            v.rsSat.x[i] = t.oil_p[i]; v.rsSat.y[i] = t.oil_rs[i];
+            v.pBubble.x[i] = t.oil_rs[i]; v.pBubble.y[i] = t.oil_p[i];
+            v.invBoSat.x[i] = t.oil_p[i]; v.invBoSat.y[i] = 1.0 / t.oil_bo[i];
+            v.muoSat.x[i] = t.oil_p[i]; v.muoSat.y[i] = t.oil_mu[i];
+        }
+        v.oilComp = t.oil_compressibility;
+        v.invBg.n = v.mug.n = t.n_gas;
+        for (int i = 0; i < t.n_gas; ++i) {
+            v.invBg.x[i] = t.gas_p[i]; v.invBg.y[i] = 1.0 / t.gas_bg[i];
+            v.mug.x[i] = t.gas_p[i]; v.mug.y[i] = t.gas_mu[i];
+        }
+        v.pwRef = t.water_p_ref;
+        v.bwRef = t.water_bw_ref;
+        v.cw = t.water_compressibility;
+        v.muw = t.water_mu;
+    }
+    // boundary faces in internal order, free-flow states on the host
+    std::vector<int> hBfPtr(N + 1, 0);
+    std::vector<BFace> hBf;
+    for (int p = 0; p < N; ++p) {
+        const int I = iperm[p];
+        hBfPtr[p] = (int)hBf.size();
+        for (int f = P->bface_ptr[I]; f < P->bface_ptr[I + 1]; ++f) {
+            const int type = P->bface_type ? P->bface_type[f] : GBFV_BC_NOFLOW;
+            if (type == GBFV_BC_NOFLOW) continue;
+            BFace bf;
+            std::memset(&bf, 0, sizeof(bf));
+            bf.p = p;
+            bf.type = type;
+            int axis = 0;
+            double sgn = 0;
+            if (!axisOf(&P->bface_normal[3 * f], axis, sgn)) return GBFV_ERR_UNSUPPORTED;
+            bf.axis = axis;
+            bf.nrm = sgn;
+            const double* xI = &P->center[3 * I];
+            const double* xf = &P->bface_center[3 * f];
+            for (int d = 0; d < 3; ++d)
+                if (d != axis && xf[d] != xI[d]) return GBFV_ERR_UNSUPPORTED;
+            bf.tmpA = xf[axis] - xI[axis];
+            bf.dInA = xI[axis] - xf[axis];
+            double gtd = 0.0;
+            for (int d = 0; d < 3; ++d) gtd += g[d] * (xI[d] - xf[d]);
+            bf.gTimesDist = gtd;
+            bf.area = P->bface_area[f];
+            const double* val = &P->bface_value[4 * f];
+            if (type == GBFV_BC_MASSRATE) {
+                for (int e = 0; e < b; ++e) bf.rate[e] = val[e];
+            }
+            else if (type == GBFV_BC_FREEFLOW) {
+                if (P->model != GBFV_MODEL_IMMISCIBLE_2P) return GBFV_ERR_UNSUPPORTED;
+                const TwoPhaseLaw& L = ph.law[P->material[I]];
+                const double pw = val[0], Swb = val[1];
+                const double sumRes = L.Swr + L.Snr;
+                const double SwE = (Swb - L.Swr) / (1.0 - sumRes);
+                const double SnE = ((1 - Swb) - L.Snr) / (1.0 - sumRes);
+                const double pcn = pcnw(L, SwE);
+                bf.pb[0] = pw;
+                bf.pb[1] = pw + pcn - 0.0;
+                const double krb[2] = {krw(L, SwE), krn(L, 1.0 - SnE)};
+                for (int a = 0; a < 2; ++a) {
+                    bf.mobb[a] = krb[a] / P->mu[a];
+                    bf.rhob[a] = P->rho[a];
+                }
+            }
+            hBf.push_back(bf);
+        }
+    }
+    hBfPtr[N] = (int)hBf.size();
+    // constraints
+    std::vector<int> consCells, consOf;
+    for (int p = 0; p < N; ++p)
+        if (hCflag[p] >= 0) {
+            if (hCflag[p] >= P->num_constraints) return GBFV_ERR_ARG;
+            consCells.push_back(p);
+            consOf.push_back(hCflag[p]);
+        }
+    std::vector<double> consPv(P->constraint_pv, P->constraint_pv + 3 * (size_t)std::max(0, P->num_constraints));
+    std::vector<int> consMeaning(P->constraint_meaning,
+                                 P->constraint_meaning + std::max(0, P->num_constraints));
+    // ELL columns of the Jacobian / solver matrix
+    const int nslot = 2 * dim + 1;
+    std::vector<int> hCol((size_t)nslot * ld, -1);
+    int slotOfDir[6];
+    for (int dir = 0; dir < 6; ++dir) {
+        const int a = dir / 2;
+        slotOfDir[dir] = (dir & 1) ? dim + 1 + a : dim - 1 - a;
+    }
+    for (int p = 0; p < N; ++p) {
+        hCol[(size_t)dim * ld + p] = p;
+        for (int dir = 0; dir < ndir; ++dir) {
+            const int q = hNbr[(size_t)dir * ld + p];
+            if (q >= 0) hCol[(size_t)slotOfDir[dir] * ld + p] = q;
+        }
+    }
+    // natural BCRS view (columns ascending), entry -> (slot, internal row)
+    C->bcrsRowPtr.assign(N + 1, 0);
+    for (int I = 0; I < N; ++I) {
+        std::vector<std::pair<int, int>> ent;  // (col, slot)
+        ent.push_back({I, dim});
+        for (int dir = 0; dir < ndir; ++dir) {
+            const int J = nbrDir[(size_t)I * ndir + dir];
+            if (J >= 0) ent.push_back({J, slotOfDir[dir]});
+        }
+        std::sort(ent.begin(), ent.end());
+        for (auto& e : ent) {
+            C->bcrsCol.push_back(e.first);
+            C->bcrsSlot.push_back(e.second);
+            C->bcrsRow.push_back(perm[I]);
+        }
+        C->bcrsRowPtr[I + 1] = (int)C->bcrsCol.size();
+    }
+    // ---------------------------------------------------------- upload
+    CK(cudaStreamCreateWithFlags(&C->stream, cudaStreamNonBlocking));
+    for (auto& e : C->ev) CK(cudaEventCreate(&e));
+    DevMesh& m = C->mesh;
+    m.N = N;
+    m.ldN = ld;
+    m.dim = dim;
+    m.b = b;
+    m.model = C->model;
+    m.nslot = nslot;
+    for (int d = 0; d < 6; ++d) m.slotOfDir[d] = slotOfDir[d];
+    int st;
+    auto up = [&](auto** dst, const auto& vec) {
+        int s2 = upload(dst, vec);
+        if (!s2) C->owned.push_back((void*)*dst);
+        return s2;
+    };
+    int *dNbr, *dMat, *dCflag, *dBfPtr, *dConsCells, *dConsOf, *dConsMeaning;
+    double *dDTot, *dGIn, *dGEx, *dKh, *dArea, *dVol, *dPor, *dPerm, *dConsPv;
+    BFace* dBf;
+    if ((st = up(&dNbr, hNbr)) || (st = up(&dDTot, hDTot)) || (st = up(&dGIn, hGIn)) || (st = up(&dGEx, hGEx)) ||
+        (st = up(&dKh, hKh)) || (st = up(&dArea, hArea)) || (st = up(&dVol, hVol)) || (st = up(&dPor, hPor)) ||
+        (st = up(&dPerm, hPerm)) || (st = up(&dMat, hMat)) || (st = up(&dCflag, hCflag)) ||
+        (st = up(&dBfPtr, hBfPtr)) || (st = up(&dBf, hBf)) || (st = up(&dConsCells, consCells)) ||
+        (st = up(&dConsOf, consOf)) || (st = up(&dConsPv, consPv)) || (st = up(&dConsMeaning, consMeaning)))
+        return st;
+    m.nbr = dNbr;
+    m.dTot = dDTot;
+    m.gIn = dGIn;
+    m.gEx = dGEx;
+    m.Kh = dKh;
+    m.area = dArea;
+    m.volume = dVol;
+    m.porosity = dPor;
+    m.perm = dPerm;
+    m.material = dMat;
+    m.cflag = dCflag;
+    m.bfPtr = dBfPtr;
+    m.bfaces = dBf;
+    m.consCells = dConsCells;
+    m.consOf = dConsOf;
+    m.consPv = dConsPv;
+    m.consMeaning = dConsMeaning;
+    m.numConsCells = (int)consCells.size();
+    m.inst = nullptr;
+    if ((st = devAlloc(&C->dphys, 1))) return st;
+    CK(cudaMemcpy(C->dphys, &ph, sizeof(DevPhysics), cudaMemcpyHostToDevice));
+    // state
+    const size_t nb = (size_t)N * b;
+    if ((st = devAlloc(&C->x, nb)) || (st = devAlloc(&C->xOld, nb)) || (st = devAlloc(&C->residual, nb)) ||
+        (st = devAlloc(&C->dx, nb)) || (st = devAlloc(&C->storageOld, (size_t)b * ld)) ||
+        (st = devAlloc(&C->meaning, (size_t)N)) || (st = devAlloc(&C->meaningOld, (size_t)N)) ||
+        (st = devAlloc(&C->wasSwitched, (size_t)N)))
+        return st;
+    CK(cudaMemset(C->meaning, 0, sizeof(int) * N));
+    CK(cudaMemset(C->meaningOld, 0, sizeof(int) * N));
+    CK(cudaMemset(C->wasSwitched, 0, sizeof(int) * N));
+    CK(cudaMemset(C->x, 0, sizeof(double) * nb));
+    CK(cudaMemset(C->xOld, 0, sizeof(double) * nb));
+    const int nv = b == 2 ? 6 : 11;
+    const int nd = b == 2 ? 12 : 30;
+    const int ns = b * (b + 1);
+    if ((st = devAlloc(&C->iq.val, (size_t)nv * ld)) || (st = devAlloc(&C->iq.der, (size_t)nd * ld)) ||
+        (st = devAlloc(&C->iq.sto, (size_t)ns * ld)))
+        return st;
+    if ((st = devAlloc(&C->jval, (size_t)nslot * b * b * ld))) return st;
+    CK(cudaMemset(C->jval, 0, sizeof(double) * (size_t)nslot * b * b * ld));
+    // solver
+    SolverData& S = C->S;
+    S.N = N;
+    S.b = b;
+    S.dim = dim;
+    S.nslot = nslot;
+    S.ldN = ld;
+    S.levPtr = levPtr;
+    if ((st = upload(&S.col, hCol)) || (st = upload(&S.levPtrD, levPtr))) return st;
+    if ((st = allocSolver(S))) return st;
+    if ((st = devAlloc(&C->st, 1))) return st;
+    CK(cudaMallocHost((void**)&C->hst, sizeof(DevStatus)));
+    CK(cudaMemset(C->st, 0, sizeof(DevStatus)));
+    return GBFV_OK;
+}
+
+gbfv_ctx* gbfv_create(const gbfv_problem* prob, const gbfv_params* params, int* status)
+{
+    gbfv_ctx* C = new gbfv_ctx();
+    if (params) C->prm = *params;
+    else gbfv_default_params(&C->prm);
+    int st = GBFV_ERR_ARG;
+    try {
+        st = prob ? createImpl(C, prob) : GBFV_ERR_ARG;
+    }
+    catch (const std::bad_alloc&) {
+        st = GBFV_ERR_OOM;
+    }
+    if (status) *status = st;
+    if (st != GBFV_OK) {
+        gbfv_destroy(C);
+        return nullptr;
+    }
+    return C;
+}
+
+int gbfv_destroy(gbfv_ctx* C)
+{
+    if (!C) return GBFV_ERR_ARG;
+    for (void* p : C->owned) cudaFree(p);
+    cudaFree(C->dphys);
+    cudaFree(C->x);
+    cudaFree(C->xOld);
+    cudaFree(C->residual);
+    cudaFree(C->dx);
+    cudaFree(C->storageOld);
+    cudaFree(C->meaning);
+    cudaFree(C->meaningOld);
+    cudaFree(C->wasSwitched);
+    cudaFree(C->iq.val);
+    cudaFree(C->iq.der);
+    cudaFree(C->iq.sto);
+    cudaFree(C->jval);
+    freeSolver(C->S);
+    cudaFree(C->st);
+    if (C->hst) cudaFreeHost(C->hst);
+    if (C->stream) {
+        for (auto& e : C->ev) cudaEventDestroy(e);
+        cudaStreamDestroy(C->stream);
+    }
+    delete C;
+    return GBFV_OK;
+}
+
+int gbfv_set_params(gbfv_ctx* C, const gbfv_params* p)
+{
+    if (!C || !p) return GBFV_ERR_ARG;
+    C->prm = *p;
+    return GBFV_OK;
+}
+
+int gbfv_dims(const gbfv_ctx* C, int* n, int* b, int* nnz)
+{
+    if (!C) return GBFV_ERR_ARG;
+    if (n) *n = C->N;
+    if (b) *b = C->b;
+    if (nnz) *nnz = (int)C->bcrsCol.size();
+    return GBFV_OK;
+}
+
+int gbfv_set_solution(gbfv_ctx* C, const double* pv, const int32_t* meaning)
+{
+    if (!C || !pv) return GBFV_ERR_ARG;
+    const int N = C->N, b = C->b;
+    std::vector<double> h((size_t)N * b);
+    for (int I = 0; I < N; ++I)
+        for (int e = 0; e < b; ++e) h[(size_t)C->perm[I] * b + e] = pv[(size_t)I * b + e];
+    CK(cudaMemcpy(C->x, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(C->xOld, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice));
+    std::vector<int> hm(N, 0);
+    if (meaning)
+        for (int I = 0; I < N; ++I) hm[C->perm[I]] = meaning[I];
+    CK(cudaMemcpy(C->meaning, hm.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(C->meaningOld, hm.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
+    return GBFV_OK;
+}
+
+int gbfv_get_solution(gbfv_ctx* C, double* pv, int32_t* meaning)
+{
+    if (!C || !pv) return GBFV_ERR_ARG;
+    const int N = C->N, b = C->b;
+    std::vector<double> h((size_t)N * b);
+    CK(cudaStreamSynchronize(C->stream));
+    CK(cudaMemcpy(h.data(), C->x, sizeof(double) * h.size(), cudaMemcpyDeviceToHost));
+    for (int I = 0; I < N; ++I)
+        for (int e = 0; e < b; ++e) pv[(size_t)I * b + e] = h[(size_t)C->perm[I] * b + e];
+    if (meaning) {
+        std::vector<int> hm(N);
+        CK(cudaMemcpy(hm.data(), C->meaning, sizeof(int) * N, cudaMemcpyDeviceToHost));
+        for (int I = 0; I < N; ++I) meaning[I] = hm[C->perm[I]];
+    }
+    return GBFV_OK;
+}
+
+int gbfv_set_timestep(gbfv_ctx* C, double dt)
+{
+    if (!C || !(dt > 0)) return GBFV_ERR_ARG;
+    C->dt = dt;
+    return GBFV_OK;
+}
+
+int gbfv_set_newton_iteration(gbfv_ctx* C, int it)
+{
+    if (!C || it < 0) return GBFV_ERR_ARG;
+    C->newtonIter = it;
+    return GBFV_OK;
+}
+
+static int linearizeImpl(gbfv_ctx* C)
+{
+    launchApplyConstraints(C->mesh, C->x, C->xOld, C->meaning, C->meaningOld, C->stream);
+    launchIq(C->mesh, C->dphys, C->x, C->meaning, C->iq, C->stream);
+    launchAssemble(C->mesh, C->dphys, C->iq, C->storageOld, C->newtonIter == 0, C->dt, C->residual, C->jval,
+                   C->stream);
+    CK(cudaGetLastError());
+    return GBFV_OK;
+}
+
+int gbfv_linearize(gbfv_ctx* C)
+{
+    if (!C) return GBFV_ERR_ARG;
+    int st = linearizeImpl(C);
+    if (st) return st;
+    CK(cudaStreamSynchronize(C->stream));
+    return GBFV_OK;
+}
+
+int gbfv_get_residual(gbfv_ctx* C, double* r)
+{
+    if (!C || !r) return GBFV_ERR_ARG;
+    const int N = C->N, b = C->b;
+    std::vector<double> h((size_t)N * b);
+    CK(cudaStreamSynchronize(C->stream));
+    CK(cudaMemcpy(h.data(), C->residual, sizeof(double) * h.size(), cudaMemcpyDeviceToHost));
+    for (int I = 0; I < N; ++I)
+        for (int e = 0; e < b; ++e) r[(size_t)I * b + e] = h[(size_t)C->perm[I] * b + e];
+    return GBFV_OK;
+}
+
+int gbfv_get_jacobian(gbfv_ctx* C, int32_t* rowPtr, int32_t* colIdx, double* blocks)
+{
+    if (!C) return GBFV_ERR_ARG;
+    const int b = C->b, bb = b * b, ld = C->ldN;
+    const size_t nval = (size_t)C->mesh.nslot * bb * ld;
+    std::vector<double> h(nval);
+    CK(cudaStreamSynchronize(C->stream));
+    CK(cudaMemcpy(h.data(), C->jval, sizeof(double) * nval, cudaMemcpyDeviceToHost));
+    if (rowPtr) std::copy(C->bcrsRowPtr.begin(), C->bcrsRowPtr.end(), rowPtr);
+    if (colIdx) std::copy(C->bcrsCol.begin(), C->bcrsCol.end(), colIdx);
+    if (blocks)
+        for (size_t k = 0; k < C->bcrsCol.size(); ++k)
+            for (int e = 0; e < bb; ++e)
+                blocks[k * bb + e] = h[((size_t)C->bcrsSlot[k] * bb + e) * ld + C->bcrsRow[k]];
+    return GBFV_OK;
+}
+
+static int newtonErrorImpl(gbfv_ctx* C, double* err)
+{
+    int st;
+    if ((st = resetStatus(C->stream, C->st))) return st;
+    launchNewtonError(C->mesh, C->residual, C->st, C->stream);
+    if ((st = syncStatus(C->stream, C->st, C->hst))) return st;
+    unsigned long long bits = C->hst->errorBits;
+    std::memcpy(err, &bits, sizeof(double));
+    if (C->hst->nonfinite) {
+        *err = std::numeric_limits<double>::quiet_NaN();
+        return GBFV_ERR_NONFINITE;
+    }
+    return GBFV_OK;
+}
+
+int gbfv_newton_error(gbfv_ctx* C, double* err)
+{
+    if (!C || !err) return GBFV_ERR_ARG;
+    return newtonErrorImpl(C, err);
+}
+
+static int solveImpl(gbfv_ctx* C, int* iterations)
+{
+    int it = 0, ref = 0, st;
+    if (C->prm.precision == GBFV_PREC_MIXED) {
+        st = solveMixed(C->S, C->stream, C->st, C->hst, C->jval, C->residual, C->prm, it, ref);
+        if (st == GBFV_OK || st == GBFV_ERR_NOT_CONVERGED)
+            CK(cudaMemcpyAsync(C->dx, C->S.xref, sizeof(double) * C->N * C->b, cudaMemcpyDeviceToDevice,
+                               C->stream));
+    }
+    else {
+        st = solvePlain(C->S, C->stream, C->st, C->hst, C->jval, C->residual, C->prm, it);
+        if (st == GBFV_OK || st == GBFV_ERR_NOT_CONVERGED)
+            CK(cudaMemcpyAsync(C->dx, C->S.v64[0], sizeof(double) * C->N * C->b, cudaMemcpyDeviceToDevice,
+                               C->stream));
+    }
+    C->lastIterations = it;
+    C->lastRefinements = ref;
+    if (iterations) *iterations = it;
+    C->haveDx = 1;
+    return st;
+}
+
+int gbfv_solve(gbfv_ctx* C, double* dx, int* iterations)
+{
+    if (!C) return GBFV_ERR_ARG;
+    const int st = solveImpl(C, iterations);
+    if (dx) {
+        const int N = C->N, b = C->b;
+        std::vector<double> h((size_t)N * b);
+        CK(cudaStreamSynchronize(C->stream));
+        CK(cudaMemcpy(h.data(), C->dx, sizeof(double) * h.size(), cudaMemcpyDeviceToHost));
+        for (int I = 0; I < N; ++I)
+            for (int e = 0; e < b; ++e) dx[(size_t)I * b + e] = h[(size_t)C->perm[I] * b + e];
+    }
+    return st;
+}
+
+static int updateImpl(gbfv_ctx* C, int* switched)
+{
+    int st;
+    if ((st = resetStatus(C->stream, C->st))) return st;
+    launchCheckUpdate(C->N * C->b, C->dx, C->st, C->stream);
+    UpdateParams up;
+    up.dsMax = C->prm.ds_max;
+    up.dpMaxRel = C->prm.dp_max_rel;
+    up.oscThreshold = C->prm.pv_oscillation_threshold;
+    up.pMin = C->prm.pressure_min;
+    up.pMax = C->prm.pressure_max;
+    up.swMax = C->prm.max_water_saturation;
+    up.waterOnly = C->prm.water_only_threshold;
+    if ((st = syncStatus(C->stream, C->st, C->hst))) return st;
+    if (C->hst->nonfinite) {
+        setError("Non-finite update!");
+        return GBFV_ERR_NONFINITE;
+    }
+    launchNewtonUpdate(C->mesh, C->dphys, C->dx, C->x, C->meaning, C->wasSwitched, up, C->st, C->stream);
+    if (switched) {
+        if ((st = syncStatus(C->stream, C->st, C->hst))) return st;
+        *switched = C->hst->switched;
+    }
+    CK(cudaGetLastError());
+    return GBFV_OK;
+}
+
+int gbfv_newton_update(gbfv_ctx* C, int* switched)
+{
+    if (!C || !C->haveDx) return GBFV_ERR_ARG;
+    int st = updateImpl(C, switched);
+    if (st) return st;
+    CK(cudaStreamSynchronize(C->stream));
+    return GBFV_OK;
+}
+
+int gbfv_phase_times(const gbfv_ctx* C, double* ms4)
+{
+    if (!C || !ms4) return GBFV_ERR_ARG;
+    for (int i = 0; i < 4; ++i) ms4[i] = C->phaseMs[i];
+    return GBFV_OK;
+}
+
+int gbfv_newton_apply(gbfv_ctx* C, double dt, gbfv_newton_report* rep)
+{
+    if (!C || !(dt > 0)) return GBFV_ERR_ARG;
+    gbfv_newton_report r;
+    std::memset(&r, 0, sizeof(r));
+    C->dt = dt;
+    C->numIterations = 0;
+    C->error = 0;
+    C->lastError = 0;
+    const gbfv_params& prm = C->prm;
+    auto converged = [&]() { return C->error <= prm.newton_tolerance; };
+    auto proceed = [&]() {
+        if (C->numIterations < 1) return true;
+        if (converged()) return false;
+        if (C->numIterations >= prm.newton_max_iterations) return C->error * 4.0 < C->lastError;
+        return true;
+    };
+    for (int i = 0; i < 4; ++i) C->phaseMs[i] = 0;
+    int status = GBFV_OK;
+    bool failed = false;
+    while (proceed()) {
+        C->lastError = C->error;
+        C->newtonIter = C->numIterations;
+        cudaEventRecord(C->ev[0], C->stream);
+        if ((status = linearizeImpl(C))) { failed = true; break; }
+        cudaEventRecord(C->ev[1], C->stream);
+        r.linearizations++;
+        C->lastError = C->error;
+        double err = 0;
+        status = newtonErrorImpl(C, &err);
+        C->error = err;
+        if (status) { failed = true; break; }
+        if (C->error > prm.newton_max_error) { status = GBFV_ERR_NUMERICAL; failed = true; break; }
+        float ms = 0;
+        cudaEventElapsedTime(&ms, C->ev[0], C->ev[1]);
+        C->phaseMs[0] += ms;
+        if (!proceed()) { C->numIterations++; break; }
+        cudaEventRecord(C->ev[2], C->stream);
+        int it = 0;
+        status = solveImpl(C, &it);
+        cudaEventRecord(C->ev[3], C->stream);
+        r.linear_iterations += it;
+        r.refinements += C->lastRefinements;
+        if (status) { failed = true; break; }
+        status = updateImpl(C, nullptr);
+        cudaEventRecord(C->ev[4], C->stream);
+        if (status) { failed = true; break; }
+        cudaEventSynchronize(C->ev[4]);
+        cudaEventElapsedTime(&ms, C->ev[2], C->ev[3]);
+        C->phaseMs[2] += ms;
+        cudaEventElapsedTime(&ms, C->ev[3], C->ev[4]);
+        C->phaseMs[3] += ms;
+        C->numIterations++;
+    }
+    if (!failed && !converged()) {
+        failed = true;
+        status = GBFV_ERR_NOT_CONVERGED;
+    }
+    if (failed) {
+        C->numIterations = prm.newton_target_iterations * 2;
+        // FvBaseDiscretization::updateFailed: solution(0) = solution(1)
+        cudaMemcpyAsync(C->x, C->xOld, sizeof(double) * C->N * C->b, cudaMemcpyDeviceToDevice, C->stream);
+        cudaMemcpyAsync(C->meaning, C->meaningOld, sizeof(int) * C->N, cudaMemcpyDeviceToDevice, C->stream);
+        cudaStreamSynchronize(C->stream);
+    }
+    else
+        r.converged = 1;
+    r.iterations = C->numIterations;
+    r.status = failed ? status : GBFV_OK;
+    r.error = C->error;
+    if (rep) *rep = r;
+    return failed ? status : GBFV_OK;
+}
+
+double gbfv_suggest_time_step(const gbfv_ctx* C, double oldDt, int n)
+{
+    const int target = C->prm.newton_target_iterations;
+    if (n > target) {
+        const double percent = double(n - target) / target;
+        return std::max(C->prm.min_time_step, oldDt / (1.0 + percent));
+    }
+    const double percent = double(target - n) / target;
+    return std::max(C->prm.min_time_step, oldDt * (1.0 + percent / 1.2));
+}
+
+int gbfv_time_integration(gbfv_ctx* C, int numSteps, double dt0, double endTime, int fixedDt, double* stepDt,
+                          int32_t* stepNewton, int32_t* stepLinear, int32_t* totalLin)
+{
+    if (!C || numSteps < 0 || !(dt0 > 0)) return GBFV_ERR_ARG;
+    double dt = dt0, t = 0.0;
+    int lin = 0;
+    for (int step = 0; step < numSteps; ++step) {
+        if (t >= endTime) break;
+        bool ok = false;
+        gbfv_newton_report rep;
+        int linIt = 0;
+        const int maxFails = C->prm.max_time_step_divisions;
+        for (int i = 0; i < maxFails; ++i) {
+            const int st = gbfv_newton_apply(C, dt, &rep);
+            linIt += rep.linear_iterations;
+            lin += rep.linearizations;
+            ok = st == GBFV_OK;
+            if (ok) break;
+            if (st == GBFV_ERR_CUDA || st == GBFV_ERR_TIMEOUT || st == GBFV_ERR_OOM) return st;
+            double nextDt = dt / 2.0;
+            if (dt < C->prm.min_time_step * (1 + 1e-9)) return GBFV_ERR_NOT_CONVERGED;
+            if (nextDt < C->prm.min_time_step) nextDt = C->prm.min_time_step;
+            dt = nextDt;
+        }
+        if (!ok) return GBFV_ERR_NOT_CONVERGED;
+        if (stepDt) stepDt[step] = dt;
+        if (stepNewton) stepNewton[step] = C->numIterations;
+        if (stepLinear) stepLinear[step] = linIt;
+        // advanceTimeLevel: solution(1) = solution(0)
+        CK(cudaMemcpyAsync(C->xOld, C->x, sizeof(double) * C->N * C->b, cudaMemcpyDeviceToDevice, C->stream));
+        CK(cudaMemcpyAsync(C->meaningOld, C->meaning, sizeof(int) * C->N, cudaMemcpyDeviceToDevice, C->stream));
+        t += dt;
+        if (fixedDt) {
+            dt = dt0;
+            continue;
+        }
+        const double maxTs = std::max(0.0, endTime - t);
+        double dtNext = std::min(C->prm.max_time_step, gbfv_suggest_time_step(C, dt, C->numIterations));
+        if (dtNext < maxTs && maxTs < dtNext * 2) dtNext = maxTs / 2 * 1.01;
+        dt = std::min(maxTs, dtNext);
+    }
+    CK(cudaStreamSynchronize(C->stream));
+    if (totalLin) *totalLin = lin;
+    return GBFV_OK;
+}
+
+// ============================================================ linsolver
+gbfv_linsolver* gbfv_linsolver_create(int n, int b, const int32_t* rowPtr, const int32_t* col,
+                                      const gbfv_params* params, int* status)
+{
+    auto fail = [&](gbfv_linsolver* L, int st) -> gbfv_linsolver* {
+        if (status) *status = st;
+        if (L) gbfv_linsolver_destroy(L);
+        return nullptr;
+    };
+    if (n <= 0 || (b != 2 && b != 3) || !rowPtr || !col) return fail(nullptr, GBFV_ERR_ARG);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(nullptr, GBFV_ERR_NO_DEVICE);
+    gbfv_linsolver* L = new gbfv_linsolver();
+    if (params) L->prm = *params;
+    else gbfv_default_params(&L->prm);
+    L->N = n;
+    L->b = b;
+    L->rowPtr.assign(rowPtr, rowPtr + n + 1);
+    L->colN.assign(col, col + rowPtr[n]);
+    // slots from the distinct column offsets (symmetric, at most 7)
+    std::vector<int> offs;
+    for (int i = 0; i < n; ++i)
+        for (int k = rowPtr[i]; k < rowPtr[i + 1]; ++k) offs.push_back(col[k] - i);
+    std::sort(offs.begin(), offs.end());
+    offs.erase(std::unique(offs.begin(), offs.end()), offs.end());
+    const int nslot = (int)offs.size();
+    if (nslot > MAX_SLOTS || nslot % 2 == 0) { setError("pattern needs at most 7 symmetric offsets"); return fail(L, GBFV_ERR_UNSUPPORTED); }
+    const int dim = nslot / 2;
+    for (int s = 0; s < nslot; ++s)
+        if (offs[s] != -offs[nslot - 1 - s]) { setError("asymmetric pattern offsets"); return fail(L, GBFV_ERR_UNSUPPORTED); }
+    auto slotOf = [&](int off) { return (int)(std::lower_bound(offs.begin(), offs.end(), off) - offs.begin()); };
+    std::vector<std::vector<int>> lower(n);
+    for (int i = 0; i < n; ++i) {
+        bool diag = false;
+        for (int k = rowPtr[i]; k < rowPtr[i + 1]; ++k) {
+            if (col[k] < i) lower[i].push_back(col[k]);
+            if (col[k] == i) diag = true;
+            if (k > rowPtr[i] && col[k] <= col[k - 1]) { setError("columns must be sorted"); return fail(L, GBFV_ERR_ARG); }
+        }
+        if (!diag) { setError("diagonal entry missing"); return fail(L, GBFV_ERR_ARG); }
+    }
+    // ILU(0) update structure check
+    for (int i = 0; i < n; ++i)
+        for (int k : lower[i])
+            for (int kk = rowPtr[k]; kk < rowPtr[k + 1]; ++kk) {
+                const int j = col[kk];
+                if (j <= k || j == i) continue;
+                for (int q = rowPtr[i]; q < rowPtr[i + 1]; ++q)
+                    if (col[q] == j) { setError("pattern has ILU(0) fill interactions beyond the diagonal"); return fail(L, GBFV_ERR_UNSUPPORTED); }
+            }
+    std::vector<int> levPtr;
+    buildOrder(n, lower, L->perm, L->iperm, levPtr);
+    const int ld = ((n + 63) / 64) * 64;
+    std::vector<int> hCol((size_t)nslot * ld, -1);
+    L->entSlot.resize(L->colN.size());
+    L->entRow.resize(L->colN.size());
+    for (int i = 0; i < n; ++i)
+        for (int k = rowPtr[i]; k < rowPtr[i + 1]; ++k) {
+            const int s = slotOf(col[k] - i);
+            hCol[(size_t)s * ld + L->perm[i]] = L->perm[col[k]];
+            L->entSlot[k] = s;
+            L->entRow[k] = L->perm[i];
+        }
+    // every (i,k) lower entry must have its mirror (k,i)
+    for (int i = 0; i < n; ++i)
+        for (int k = rowPtr[i]; k < rowPtr[i + 1]; ++k) {
+            const int j = col[k];
+            bool found = false;
+            for (int q = rowPtr[j]; q < rowPtr[j + 1]; ++q) found |= col[q] == i;
+            if (!found) { setError("structurally asymmetric matrix"); return fail(L, GBFV_ERR_UNSUPPORTED); }
+        }
+    SolverData& S = L->S;
+    S.N = n;
+    S.b = b;
+    S.dim = dim;
+    S.nslot = nslot;
+    S.ldN = ld;
+    S.levPtr = levPtr;
+    int st;
+    if ((st = upload(&S.col, hCol)) || (st = upload(&S.levPtrD, levPtr)) || (st = allocSolver(S)))
+        return fail(L, st);
+    const size_t nval = (size_t)nslot * b * b * ld;
+    if ((st = devAlloc(&L->A64, nval)) || (st = devAlloc(&L->rhs, (size_t)n * b)) || (st = devAlloc(&L->st, 1)))
+        return fail(L, st);
+    if (cudaMallocHost((void**)&L->hst, sizeof(DevStatus)) != cudaSuccess ||
+        cudaMallocHost((void**)&L->A64host, sizeof(double) * nval) != cudaSuccess ||
+        cudaMallocHost((void**)&L->stage, sizeof(double) * (size_t)n * b) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return fail(L, GBFV_ERR_CUDA);
+    std::memset(L->A64host, 0, sizeof(double) * nval);
+    if (status) *status = GBFV_OK;
+    return L;
+}
+
+int gbfv_linsolver_destroy(gbfv_linsolver* L)
+{
+    if (!L) return GBFV_ERR_ARG;
+    freeSolver(L->S);
+    cudaFree(L->A64);
+    cudaFree(L->rhs);
+    cudaFree(L->st);
+    if (L->hst) cudaFreeHost(L->hst);
+    if (L->A64host) cudaFreeHost(L->A64host);
+    if (L->stage) cudaFreeHost(L->stage);
+    if (L->stream) cudaStreamDestroy(L->stream);
+    delete L;
+    return GBFV_OK;
+}
+
+int gbfv_linsolver_set_matrix(gbfv_linsolver* L, const double* blocks)
+{
+    if (!L || !blocks) return GBFV_ERR_ARG;
+    const int bb = L->b * L->b, ld = L->S.ldN;
+    for (size_t k = 0; k < L->colN.size(); ++k)
+        for (int e = 0; e < bb; ++e)
+            L->A64host[((size_t)L->entSlot[k] * bb + e) * ld + L->entRow[k]] = blocks[k * bb + e];
+    CK(cudaMemcpyAsync(L->A64, L->A64host, sizeof(double) * (size_t)L->S.nslot * bb * ld, cudaMemcpyHostToDevice,
+                       L->stream));
+    return GBFV_OK;
+}
+
+int gbfv_linsolver_solve(gbfv_linsolver* L, const double* rhs, double* x, int* iterations)
+{
+    if (!L || !rhs || !x) return GBFV_ERR_ARG;
+    const int n = L->N, b = L->b;
+    for (int i = 0; i < n; ++i)
+        for (int e = 0; e < b; ++e) L->stage[(size_t)L->perm[i] * b + e] = rhs[(size_t)i * b + e];
+    CK(cudaMemcpyAsync(L->rhs, L->stage, sizeof(double) * n * b, cudaMemcpyHostToDevice, L->stream));
+    int it = 0, ref = 0, st;
+    const double* out;
+    if (L->prm.precision == GBFV_PREC_MIXED) {
+        st = solveMixed(L->S, L->stream, L->st, L->hst, L->A64, L->rhs, L->prm, it, ref);
+        out = L->S.xref;
+    }
+    else {
+        st = solvePlain(L->S, L->stream, L->st, L->hst, L->A64, L->rhs, L->prm, it);
+        out = L->S.v64[0];
+    }
+    if (iterations) *iterations = it;
+    CK(cudaMemcpyAsync(L->stage, out, sizeof(double) * n * b, cudaMemcpyDeviceToHost, L->stream));
+    CK(cudaStreamSynchronize(L->stream));
+    for (int i = 0; i < n; ++i)
+        for (int e = 0; e < b; ++e) x[(size_t)i * b + e] = L->stage[(size_t)L->perm[i] * b + e];
+    return st;
+}
+
+}  // extern "C"

@@ -1,0 +1,607 @@
+// Linearization kernels: intensive quantities (K1), cell-centric TPFA
+// assembly (K2), constraints, Newton error and Newton update (K7).
+//
+// This translation unit is compiled with -fmad=false: the FP64 residual and
+// Jacobian follow the reference's operation order term by term, so they can
+// be compared with the CPU restatement at the 1e-12 level.
+//
+// K2 mirrors the reference's element loop (fvbaselinearizer.hh:510-626 with
+// FvBaseAdLocalLinearizer, fvbaseadlocallinearizer.hh:173-292): one thread
+// per cell I evaluates its faces with derivatives with respect to x_I only,
+// writes the residual row I, the diagonal block (I,I) and the column blocks
+// (J,I) of its neighbours.  Each block has exactly one writer, so there are
+// no atomics and the summation order inside a row is the reference's:
+// interior faces in intersection order, storage, boundary faces.  The
+// expensive intensive quantities (pow-heavy material laws, PVT tables) are
+// computed once per cell by K1 and read back -- FP64 arithmetic is the scarce
+// resource on this GPU, bytes are cheap.
+#include "../../include/gbfv.h"
+#include "gbfv_internal.cuh"
+
+namespace gbfv {
+
+using D2 = Dual<2>;
+using D3 = Dual<3>;
+
+// ------------------------------------------------------- constraints -----
+// FvBaseLinearizer::applyConstraintsToSolution_ (fvbaselinearizer.hh:630-645)
+__global__ void kApplyConstraints(DevMesh m, double* __restrict__ x, double* __restrict__ xOld,
+                                  int* __restrict__ meaning, int* __restrict__ meaningOld)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m.numConsCells) return;
+    const int p = m.consCells[k];
+    const int c = m.consOf[k];
+    for (int e = 0; e < m.b; ++e) {
+        x[p * m.b + e] = m.consPv[3 * c + e];
+        xOld[p * m.b + e] = m.consPv[3 * c + e];
+    }
+    meaning[p] = m.consMeaning[c];
+    meaningOld[p] = m.consMeaning[c];
+}
+
+void launchApplyConstraints(const DevMesh& m, double* x, double* xOld, int* meaning, int* meaningOld,
+                            cudaStream_t s)
+{
+    if (m.numConsCells == 0) return;
+    kApplyConstraints<<<(m.numConsCells + 127) / 128, 128, 0, s>>>(m, x, xOld, meaning, meaningOld);
+    countLaunch();
+}
+
+// ------------------------------------------------------------- K1 --------
+// ImmiscibleIntensiveQuantities::update (immiscibleintensivequantities.hh:93-151)
+// and ImmiscibleLocalResidual::computeStorage (immisciblelocalresidual.hh:75-109)
+__global__ void __launch_bounds__(256) kIqImmiscible(DevMesh m, const DevPhysics* __restrict__ phys,
+                                                     const double* __restrict__ x, IqBuffers iq)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= m.N) return;
+    const int ld = m.ldN;
+    const TwoPhaseLaw L = phys->law[m.material[p]];
+    const double pv0 = x[2 * p + 0], pv1 = x[2 * p + 1];
+    D2 sumSat(0.0);
+    D2 Sw = D2::var(pv1, 1);
+    D2 S[2];
+    S[0] = Sw;
+    sumSat = sumSat + Sw;
+    S[1] = 1.0 - sumSat;
+    const double sumRes = L.Swr + L.Snr;
+    D2 SwE = (S[0] - L.Swr) / (1.0 - sumRes);
+    D2 SnE = (S[1] - L.Snr) / (1.0 - sumRes);
+    D2 pc[2];
+    pc[0] = D2(0.0);
+    pc[1] = pcnw(L, SwE);
+    D2 kr[2];
+    kr[0] = krw(L, SwE);
+    kr[1] = krn(L, 1.0 - SnE);
+    D2 p0 = D2::var(pv0, 0);
+    D2 pr[2], rho[2], lam[2];
+    for (int a = 0; a < 2; ++a) pr[a] = p0 + (pc[a] - pc[0]);
+    for (int a = 0; a < 2; ++a) {
+        D2 mu(phys->mu[a]);
+        rho[a] = D2(phys->rho[a]);
+        lam[a] = kr[a] / mu;
+    }
+    const double phi = m.porosity[p];
+    const D2* q[6] = {&pr[0], &pr[1], &rho[0], &rho[1], &lam[0], &lam[1]};
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        iq.val[k * ld + p] = q[k]->v;
+        iq.der[(k * 2 + 0) * ld + p] = q[k]->d[0];
+        iq.der[(k * 2 + 1) * ld + p] = q[k]->d[1];
+    }
+#pragma unroll
+    for (int a = 0; a < 2; ++a) {
+        D2 st = (D2(phi) * S[a]) * rho[a];
+        iq.sto[(a * 3 + 0) * ld + p] = st.v;
+        iq.sto[(a * 3 + 1) * ld + p] = st.d[0];
+        iq.sto[(a * 3 + 2) * ld + p] = st.d[1];
+    }
+}
+
+// BlackOilIntensiveQuantities::update (blackoilintensivequantities.hh:179-462)
+// for water meaning Sw, pressure meaning Po, gas meaning Sg / Rs, zero p_c,
+// Corey relperm via updateRelperms; storage per blackoillocalresidual.hh:101-188
+__global__ void __launch_bounds__(256) kIqBlackoil(DevMesh m, const DevPhysics* __restrict__ phys,
+                                                   const double* __restrict__ x,
+                                                   const int* __restrict__ meaning, IqBuffers iq)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= m.N) return;
+    const int ld = m.ldN;
+    const BlackOilPvt& T = phys->pvt;
+    const double pv0 = x[3 * p + 0], pv1 = x[3 * p + 1], pv2 = x[3 * p + 2];
+    const int gm = meaning[p];
+    D3 Sw = D3::var(pv0, 0);
+    D3 Sg(0.0);
+    if (gm == GBFV_GAS_SG) Sg = D3::var(pv2, 2);
+    D3 So = 1.0 - Sw - Sg;
+    D3 S[3] = {Sw, So, Sg};
+    const double n = phys->coreyN[m.material[p]];
+    D3 kr[3];
+    for (int a = 0; a < 3; ++a) kr[a] = corey(S[a], n);
+    D3 po = D3::var(pv1, 1) * 1.0;
+    D3 pr = po + (D3(0.0) - D3(0.0));
+    D3 RsSat = tableEval(T.rsSat, pr);
+    D3 Rs = gm == GBFV_GAS_RS ? D3::var(pv2, 2) : RsSat;
+    D3 invB[3], mu[3];
+    invB[0] = waterInvB(T, pr);
+    mu[0] = D3(T.muw);
+    const bool sat = S[2].v > 0.0 && Rs.v >= (1.0 - 1e-10) * RsSat.v;
+    if (sat) {
+        invB[1] = tableEval(T.invBoSat, pr);
+        mu[1] = tableEval(T.muoSat, pr);
+    }
+    else {
+        D3 pb = tableEval(T.pBubble, Rs);
+        D3 ib = tableEval(T.invBoSat, pb);
+        invB[1] = ib * (1.0 + T.oilComp * (pr - pb));
+        mu[1] = tableEval(T.muoSat, pb);
+    }
+    invB[2] = tableEval(T.invBg, pr);
+    mu[2] = tableEval(T.mug, pr);
+    D3 lam[3], rho[3];
+    for (int a = 0; a < 3; ++a) lam[a] = kr[a] / mu[a];
+    rho[0] = invB[0] * T.rhoRefW;
+    rho[2] = invB[2] * T.rhoRefG;
+    rho[1] = invB[1] * T.rhoRefO;
+    rho[1] = rho[1] + invB[1] * Rs * T.rhoRefG;
+    const double phi = m.porosity[p];
+    // values: p, rho0..2, lam0..2, invB0..2, Rs ; derivatives for all but p
+    iq.val[0 * ld + p] = pr.v;
+    const D3* q[10] = {&rho[0], &rho[1], &rho[2], &lam[0], &lam[1], &lam[2],
+                       &invB[0], &invB[1], &invB[2], &Rs};
+#pragma unroll
+    for (int k = 0; k < 10; ++k) {
+        iq.val[(k + 1) * ld + p] = q[k]->v;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) iq.der[(k * 3 + j) * ld + p] = q[k]->d[j];
+    }
+    D3 tmp[3] = {D3(0.0), D3(0.0), D3(0.0)};
+    const int comp[3] = {1, 0, 2};
+    D3 dphi(phi);
+    for (int a = 0; a < 3; ++a) {
+        D3 sv = S[a] * invB[a] * dphi;
+        tmp[comp[a]] = tmp[comp[a]] + sv;
+        if (a == 1) tmp[2] = tmp[2] + Rs * sv;
+    }
+    tmp[1] = tmp[1] * T.rhoRefW;
+    tmp[2] = tmp[2] * T.rhoRefG;
+    tmp[0] = tmp[0] * T.rhoRefO;
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+        iq.sto[(e * 4 + 0) * ld + p] = tmp[e].v;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) iq.sto[(e * 4 + 1 + j) * ld + p] = tmp[e].d[j];
+    }
+}
+
+void launchIq(const DevMesh& m, const DevPhysics* phys, const double* x, const int* meaning,
+              IqBuffers iq, cudaStream_t s)
+{
+    const int bs = 256, nb = (m.N + bs - 1) / bs;
+    if (m.model == GBFV_MODEL_IMMISCIBLE_2P)
+        kIqImmiscible<<<nb, bs, 0, s>>>(m, phys, x, iq);
+    else
+        kIqBlackoil<<<nb, bs, 0, s>>>(m, phys, x, meaning, iq);
+    countLaunch();
+}
+
+// ------------------------------------------------------------- K2 --------
+// load a dual from the IQ buffers
+template <int B>
+__device__ __forceinline__ Dual<B> ldDual(const IqBuffers& iq, int ld, int qv, int qd, int p)
+{
+    Dual<B> r;
+    r.v = iq.val[qv * ld + p];
+#pragma unroll
+    for (int j = 0; j < B; ++j) r.d[j] = iq.der[(qd * B + j) * ld + p];
+    return r;
+}
+
+// write block (row q, slot s) = -flux.d / V_q (zero in constraint rows)
+template <int B>
+__device__ __forceinline__ void writeOffBlock(double* __restrict__ jval, int ld, int slot, int q,
+                                              const Dual<B>* flux, double Vq, bool zero)
+{
+#pragma unroll
+    for (int e = 0; e < B; ++e)
+#pragma unroll
+        for (int v = 0; v < B; ++v) {
+            const double d = zero ? 0.0 : (0.0 - flux[e].d[v]) / Vq;
+            jval[(slot * B * B + e * B + v) * ld + q] = d;
+        }
+}
+
+// Axis-aligned Darcy flux of one phase, focus = interior cell
+// (darcyfluxmodule.hh:183-322, 459-525).  Components of the gradient off the
+// face axis are exact zeros, so only the axis component is carried.
+template <int B>
+__device__ __forceinline__ Dual<B> darcyPhase(const Dual<B>& pI, double pJ, const Dual<B>& rhoI,
+                                              double rhoJ, const Dual<B>& lamI, double lamJ,
+                                              double dTot, double gIn, double gEx, double Kh,
+                                              double nrm, bool& upI)
+{
+    const double distSq = dTot * dTot;
+    Dual<B> deltay = pJ - pI;
+    Dual<B> pg = deltay * (dTot / distSq);
+    Dual<B> pStatIn = (-rhoI) * gIn;
+    const double pStatEx = (-rhoJ) * gEx;
+    Dual<B> fs = (pStatEx - pStatIn) / distSq;
+    pg = pg + dTot * fs;
+    const double t = pg.v * nrm;
+    upI = !(t > 0.0);
+    Dual<B> mob = upI ? lamI : Dual<B>(lamJ);
+    Dual<B> fv = Kh * pg;
+    fv = fv * (-mob);
+    return fv * nrm;
+}
+
+__global__ void __launch_bounds__(128) kAssembleImmiscible(DevMesh m, const DevPhysics* __restrict__ phys,
+                                                           IqBuffers iq, double* __restrict__ storageOld,
+                                                           int iter0, double dt,
+                                                           double* __restrict__ residual,
+                                                           double* __restrict__ jval)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= m.N) return;
+    const int ld = m.ldN;
+    D2 pI[2], rhoI[2], lamI[2];
+    for (int a = 0; a < 2; ++a) {
+        pI[a] = ldDual<2>(iq, ld, a, a, p);
+        rhoI[a] = ldDual<2>(iq, ld, 2 + a, 2 + a, p);
+        lamI[a] = ldDual<2>(iq, ld, 4 + a, 4 + a, p);
+    }
+    D2 res[2] = {D2(0.0), D2(0.0)};
+    const int ndir = 2 * m.dim;
+    for (int dir = 0; dir < ndir; ++dir) {
+        const int q = m.nbr[dir * ld + p];
+        if (q < 0) continue;
+        const double dTot = m.dTot[dir * ld + p];
+        const double gIn = m.gIn[dir * ld + p];
+        const double gEx = m.gEx[dir * ld + p];
+        const double Kh = m.Kh[dir * ld + p];
+        const double area = m.area[dir * ld + p];
+        const double nrm = (dir & 1) ? 1.0 : -1.0;
+        D2 flux[2];
+        for (int a = 0; a < 2; ++a) {
+            const double pJ = iq.val[a * ld + q];
+            const double rhoJ = iq.val[(2 + a) * ld + q];
+            const double lamJ = iq.val[(4 + a) * ld + q];
+            bool upI;
+            D2 vf = darcyPhase<2>(pI[a], pJ, rhoI[a], rhoJ, lamI[a], lamJ, dTot, gIn, gEx, Kh, nrm, upI);
+            flux[a] = D2(0.0) + (upI ? vf * rhoI[a] : vf * rhoJ);
+        }
+        double alpha = 1.0;
+        alpha *= area;
+        for (int e = 0; e < 2; ++e) flux[e] = flux[e] * alpha;
+        for (int e = 0; e < 2; ++e) res[e] = res[e] + flux[e];
+        writeOffBlock<2>(jval, ld, m.slotOfDir[dir ^ 1], q, flux, m.volume[q], m.cflag[q] >= 0);
+    }
+    const double V = m.volume[p];
+    {
+        const double scvVolume = V * 1.0;
+        for (int e = 0; e < 2; ++e) {
+            D2 tmp;
+            tmp.v = iq.sto[(e * 3 + 0) * ld + p];
+            tmp.d[0] = iq.sto[(e * 3 + 1) * ld + p];
+            tmp.d[1] = iq.sto[(e * 3 + 2) * ld + p];
+            double tmp2;
+            if (iter0) {
+                tmp2 = tmp.v;
+                storageOld[e * ld + p] = tmp2;
+            }
+            else
+                tmp2 = storageOld[e * ld + p];
+            tmp = tmp - tmp2;
+            tmp = tmp * (scvVolume / dt);
+            res[e] = res[e] + tmp;
+        }
+        for (int e = 0; e < 2; ++e) res[e] = res[e] - 0.0 * scvVolume;
+    }
+    for (int f = m.bfPtr[p]; f < m.bfPtr[p + 1]; ++f) {
+        const BFace bf = m.bfaces[f];
+        D2 values[2] = {D2(0.0), D2(0.0)};
+        if (bf.type == GBFV_BC_MASSRATE) {
+            for (int e = 0; e < 2; ++e) values[e] = D2(bf.rate[e]);
+        }
+        else if (bf.type == GBFV_BC_FREEFLOW) {
+            const double distSq = bf.tmpA * bf.tmpA;
+            const double absDist2 = bf.dInA * bf.dInA;
+            const double K = m.perm[bf.axis * ld + p];
+            for (int a = 0; a < 2; ++a) {
+                D2 deltay = bf.pb[a] - pI[a];
+                D2 pg = deltay * (bf.tmpA / distSq);
+                D2 pStatIn = (-bf.gTimesDist) * rhoI[a];
+                D2 fsc = pStatIn / absDist2;
+                pg = pg + bf.dInA * fsc;
+                const double t = pg.v * bf.nrm;
+                D2 mob = t > 0.0 ? D2(bf.mobb[a]) : lamI[a];
+                D2 fv = K * pg;
+                fv = fv * (-mob);
+                D2 vf = fv * bf.nrm;
+                D2 dens = bf.pb[a] > pI[a].v ? D2(bf.rhob[a]) : rhoI[a];
+                values[a] = values[a] + vf * dens;
+            }
+        }
+        const double aa = bf.area * 1.0;
+        for (int e = 0; e < 2; ++e) values[e] = values[e] * aa;
+        for (int e = 0; e < 2; ++e) res[e] = res[e] + values[e];
+    }
+    for (int e = 0; e < 2; ++e) res[e] = res[e] / V;
+    const bool cons = m.cflag[p] >= 0;
+    const int ds = m.dim;  // diagonal slot
+    for (int e = 0; e < 2; ++e) {
+        residual[2 * p + e] = cons ? 0.0 : res[e].v;
+        for (int v = 0; v < 2; ++v)
+            jval[(ds * 4 + e * 2 + v) * ld + p] = cons ? (e == v ? 1.0 : 0.0) : res[e].d[v];
+    }
+}
+
+__global__ void __launch_bounds__(128) kAssembleBlackoil(DevMesh m, const DevPhysics* __restrict__ phys,
+                                                         IqBuffers iq, double* __restrict__ storageOld,
+                                                         int iter0, double dt,
+                                                         double* __restrict__ residual,
+                                                         double* __restrict__ jval)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= m.N) return;
+    const int ld = m.ldN;
+    const BlackOilPvt& T = phys->pvt;
+    // own quantities: p as a seeded variable, the rest from K1
+    D3 pI = D3::var(iq.val[0 * ld + p], 1);
+    D3 rhoI[3], lamI[3], invBI[3], RsI;
+    for (int a = 0; a < 3; ++a) {
+        rhoI[a] = ldDual<3>(iq, ld, 1 + a, a, p);
+        lamI[a] = ldDual<3>(iq, ld, 4 + a, 3 + a, p);
+        invBI[a] = ldDual<3>(iq, ld, 7 + a, 6 + a, p);
+    }
+    RsI = ldDual<3>(iq, ld, 10, 9, p);
+    const double rhoRef[3] = {T.rhoRefW, T.rhoRefO, T.rhoRefG};
+    const int comp[3] = {1, 0, 2};
+    D3 res[3] = {D3(0.0), D3(0.0), D3(0.0)};
+    for (int dir = 0; dir < 6; ++dir) {
+        const int q = m.nbr[dir * ld + p];
+        if (q < 0) continue;
+        const double dTot = m.dTot[dir * ld + p];
+        const double gIn = m.gIn[dir * ld + p];
+        const double gEx = m.gEx[dir * ld + p];
+        const double Kh = m.Kh[dir * ld + p];
+        const double area = m.area[dir * ld + p];
+        const double nrm = (dir & 1) ? 1.0 : -1.0;
+        const double pJ = iq.val[0 * ld + q];
+        D3 flux[3] = {D3(0.0), D3(0.0), D3(0.0)};
+        for (int a = 0; a < 3; ++a) {
+            const double rhoJ = iq.val[(1 + a) * ld + q];
+            const double lamJ = iq.val[(4 + a) * ld + q];
+            bool upI;
+            D3 vf = darcyPhase<3>(pI, pJ, rhoI[a], rhoJ, lamI[a], lamJ, dTot, gIn, gEx, Kh, nrm, upI);
+            D3 invB = upI ? invBI[a] : D3(iq.val[(7 + a) * ld + q]);
+            D3 svf = invB * vf;
+            flux[comp[a]] = flux[comp[a]] + svf * rhoRef[a];
+            if (a == 1) {
+                D3 Rs = upI ? RsI : D3(iq.val[10 * ld + q]);
+                flux[2] = flux[2] + Rs * svf * T.rhoRefG;
+            }
+        }
+        double alpha = 1.0;
+        alpha *= area;
+        for (int e = 0; e < 3; ++e) flux[e] = flux[e] * alpha;
+        for (int e = 0; e < 3; ++e) res[e] = res[e] + flux[e];
+        writeOffBlock<3>(jval, ld, m.slotOfDir[dir ^ 1], q, flux, m.volume[q], m.cflag[q] >= 0);
+    }
+    const double V = m.volume[p];
+    {
+        const double scvVolume = V * 1.0;
+        for (int e = 0; e < 3; ++e) {
+            D3 tmp;
+            tmp.v = iq.sto[(e * 4 + 0) * ld + p];
+            for (int j = 0; j < 3; ++j) tmp.d[j] = iq.sto[(e * 4 + 1 + j) * ld + p];
+            double tmp2;
+            if (iter0) {
+                tmp2 = tmp.v;
+                storageOld[e * ld + p] = tmp2;
+            }
+            else
+                tmp2 = storageOld[e * ld + p];
+            tmp = tmp - tmp2;
+            tmp = tmp * (scvVolume / dt);
+            res[e] = res[e] + tmp;
+        }
+        for (int e = 0; e < 3; ++e) res[e] = res[e] - 0.0 * scvVolume;
+    }
+    for (int f = m.bfPtr[p]; f < m.bfPtr[p + 1]; ++f) {
+        const BFace& bf = m.bfaces[f];
+        if (bf.type != GBFV_BC_MASSRATE) continue;
+        const double aa = bf.area * 1.0;
+        for (int e = 0; e < 3; ++e) res[e] = res[e] + D3(bf.rate[e]) * aa;
+    }
+    for (int e = 0; e < 3; ++e) res[e] = res[e] / V;
+    const bool cons = m.cflag[p] >= 0;
+    const int ds = m.dim;
+    for (int e = 0; e < 3; ++e) {
+        residual[3 * p + e] = cons ? 0.0 : res[e].v;
+        for (int v = 0; v < 3; ++v)
+            jval[(ds * 9 + e * 3 + v) * ld + p] = cons ? (e == v ? 1.0 : 0.0) : res[e].d[v];
+    }
+}
+
+void launchAssemble(const DevMesh& m, const DevPhysics* phys, IqBuffers iq, double* storageOld,
+                    int iter0, double dt, double* residual, double* jval, cudaStream_t s)
+{
+    const int bs = 128, nb = (m.N + bs - 1) / bs;
+    if (m.model == GBFV_MODEL_IMMISCIBLE_2P)
+        kAssembleImmiscible<<<nb, bs, 0, s>>>(m, phys, iq, storageOld, iter0, dt, residual, jval);
+    else
+        kAssembleBlackoil<<<nb, bs, 0, s>>>(m, phys, iq, storageOld, iter0, dt, residual, jval);
+    countLaunch();
+}
+
+// ------------------------------------------------------- Newton error ----
+// NewtonMethod::preSolve_ (newtonmethod.hh:572-607): max |r| over
+// unconstrained cells; non-finite values are flagged.  The maximum of
+// non-negative doubles is order independent, so an atomicMax on the bit
+// pattern gives a deterministic result.
+__global__ void kNewtonError(DevMesh m, const double* __restrict__ r, DevStatus* st)
+{
+    __shared__ unsigned long long smax[8];
+    __shared__ int snf[8];
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    double e = 0.0;
+    int nf = 0;
+    if (p < m.N && m.cflag[p] < 0 && m.volume[p] > 0.0)
+        for (int k = 0; k < m.b; ++k) {
+            const double v = r[p * m.b + k];
+            if (!isfinite(v)) nf = 1;
+            else e = fmax(e, fabs(v));
+        }
+    unsigned long long bits = __double_as_longlong(e);
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long ob = __shfl_down_sync(0xffffffffu, bits, o);
+        bits = ob > bits ? ob : bits;
+        nf |= __shfl_down_sync(0xffffffffu, nf, o);
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) { smax[w] = bits; snf[w] = nf; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long b = 0;
+        int f = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) { b = smax[i] > b ? smax[i] : b; f |= snf[i]; }
+        atomicMax(&st->errorBits, b);
+        if (f) atomicOr(&st->nonfinite, 1);
+    }
+}
+
+void launchNewtonError(const DevMesh& m, const double* residual, DevStatus* st, cudaStream_t s)
+{
+    kNewtonError<<<(m.N + 255) / 256, 256, 0, s>>>(m, residual, st);
+    countLaunch();
+}
+
+// NewtonMethod::update_ guard: a non-finite update aborts the step
+__global__ void kCheckUpdate(int n, const double* __restrict__ dx, DevStatus* st)
+{
+    int bad = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        if (!isfinite(dx[i])) bad = 1;
+    bad = __syncthreads_or(bad);
+    if (bad && threadIdx.x == 0) atomicOr(&st->nonfinite, 1);
+}
+
+void launchCheckUpdate(int n, const double* dx, DevStatus* st, cudaStream_t s)
+{
+    int nb = (n + 255) / 256;
+    if (nb > 1024) nb = 1024;
+    kCheckUpdate<<<nb, 256, 0, s>>>(n, dx, st);
+    countLaunch();
+}
+
+// ----------------------------------------------------- Newton update -----
+__device__ __forceinline__ double signum(double v) { return (double)((v > 0) - (v < 0)); }
+
+// BlackOilPrimaryVariables::adaptPrimaryVariables (blackoilprimaryvariables.hh:549-910)
+__device__ bool adaptPv(const BlackOilPvt& T, const UpdateParams& prm, double* pv, int& meaning, double eps)
+{
+    const double sw = pv[0];
+    const double sg = meaning == GBFV_GAS_SG ? pv[2] : 0.0;
+    const double rsMax = 8.98846567431158e307;  // numeric_limits<double>::max()/2
+    if (sw >= prm.waterOnly) {
+        pv[0] = fmin(prm.swMax, sw);
+        pv[2] = 0.0;
+        const bool changed = meaning != GBFV_GAS_SG;
+        if (changed) meaning = GBFV_GAS_SG;
+        return changed;
+    }
+    bool changed = false;
+    if (meaning == GBFV_GAS_SG) {
+        const double s = 1.0 - sw - 0.0;
+        if (sg < -eps && s > 0.0) {
+            const double po = pv[1];
+            meaning = GBFV_GAS_RS;
+            const double rsSat = tableEval(T.rsSat, po);
+            pv[2] = fmin(rsMax, rsSat);
+            changed = true;
+        }
+    }
+    else if (meaning == GBFV_GAS_RS) {
+        const double po = pv[1];
+        const double rsSat = tableEval(T.rsSat, po);
+        const double rs = pv[2];
+        if (rs > fmin(rsMax, rsSat * (1.0 + eps))) {
+            meaning = GBFV_GAS_SG;
+            pv[2] = 0.0;
+            changed = true;
+        }
+    }
+    return changed;
+}
+
+// NewtonMethod::update_ / BlackOilNewtonMethod::updatePrimaryVariables_
+// (newtonmethod.hh:665-731, blackoilnewtonmethod.hh:226-427)
+__global__ void kNewtonUpdate(DevMesh m, const DevPhysics* __restrict__ phys, const double* __restrict__ dx,
+                              double* __restrict__ x, int* __restrict__ meaning,
+                              int* __restrict__ wasSwitched, UpdateParams prm, DevStatus* st)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    int sw = 0;
+    if (p < m.N) {
+        const int k = m.cflag[p];
+        const int b = m.b;
+        if (k >= 0) {
+            for (int e = 0; e < b; ++e) x[p * b + e] = m.consPv[3 * k + e];
+            meaning[p] = m.consMeaning[k];
+        }
+        else if (m.model == GBFV_MODEL_IMMISCIBLE_2P) {
+            for (int e = 0; e < b; ++e) x[p * b + e] = x[p * b + e] - dx[p * b + e];
+        }
+        else {
+            const double up[3] = {dx[3 * p], dx[3 * p + 1], dx[3 * p + 2]};
+            const double cv[3] = {x[3 * p], x[3 * p + 1], x[3 * p + 2]};
+            const int mg = meaning[p];
+            double dSw = 0, dSo = 0, dSg = 0;
+            dSw = up[0];
+            dSo -= dSw;
+            if (mg == GBFV_GAS_SG) { dSg = up[2]; dSo -= dSg; }
+            double maxSat = fmax(fabs(dSg), fabs(dSo));
+            maxSat = fmax(maxSat, fabs(dSw));
+            maxSat = fmax(maxSat, 0.0);
+            double satAlpha = 1.0;
+            if (maxSat > prm.dsMax) satAlpha = prm.dsMax / maxSat;
+            double nv[3];
+            for (int pvIdx = 0; pvIdx < 3; ++pvIdx) {
+                double delta = up[pvIdx];
+                if (pvIdx == 1) {
+                    if (fabs(delta) > prm.dpMaxRel * cv[1]) delta = signum(delta) * prm.dpMaxRel * cv[1];
+                }
+                else if (pvIdx == 0)
+                    delta *= satAlpha;
+                else {
+                    if (mg == GBFV_GAS_SG) delta *= satAlpha;
+                    else if (delta > cv[2]) delta = cv[2];
+                }
+                nv[pvIdx] = cv[pvIdx] - delta;
+                if (pvIdx == 1) nv[1] = fmin(fmax(nv[1], prm.pMin), prm.pMax);
+            }
+            int mm = mg;
+            const double eps = wasSwitched[p] ? prm.oscThreshold : 0.0;
+            const bool ch = adaptPv(phys->pvt, prm, nv, mm, eps);
+            wasSwitched[p] = ch ? 1 : 0;
+            sw = ch ? 1 : 0;
+            for (int e = 0; e < 3; ++e) x[3 * p + e] = nv[e];
+            meaning[p] = mm;
+        }
+    }
+    sw = __syncthreads_count(sw);
+    if (threadIdx.x == 0 && sw) atomicAdd(&st->switched, sw);
+}
+
+void launchNewtonUpdate(const DevMesh& m, const DevPhysics* phys, const double* dx, double* x,
+                        int* meaning, int* wasSwitched, UpdateParams prm, DevStatus* st,
+                        cudaStream_t s)
+{
+    kNewtonUpdate<<<(m.N + 255) / 256, 256, 0, s>>>(m, phys, dx, x, meaning, wasSwitched, prm, st);
+    countLaunch();
+}
+
+}  // namespace gbfv

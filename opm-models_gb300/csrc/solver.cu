@@ -1,0 +1,646 @@
+// Linear solver kernels: block ILU(0) factorization, level-scheduled
+// triangular sweeps and BiCGStab, all inside one persistent cooperative
+// kernel per solve; plus the FP64 kernels of the mixed-precision outer
+// iterative refinement.
+//
+// The algorithm is the reference's (ParallelBiCGStabSolverBackend ->
+// BiCGStabSolver with Dune::SeqILU<...,0> and CombinedCriterion;
+// bicgstabsolver.hh:120-330, combinedcriterion.hh:116-209,
+// istlpreconditionerwrappers.hh:151-190): zero initial guess, r0hat = b,
+// right preconditioning, max-norm criterion on the recursively updated
+// residual, breakdown threshold numeric_limits<double>::min()*1e10.
+//
+// ILU(0) of the 5/7-point TPFA pattern: every lower entry (i,k) only updates
+// the diagonal of row i (row k's upper entries other than (k,i) are outside
+// row i's pattern), so the factorization is
+//     L_ik = A_ik * D_k^-1 ;  D_i = A_ii - sum_k L_ik A_ki  (k ascending)
+// and the upper factor is A's own upper part.  Rows of one wavefront level
+// are independent; levels are separated by grid barriers.  Every wait on a
+// barrier is bounded: on timeout the kernel records GBFV_ERR_TIMEOUT and all
+// blocks leave.
+#include <cuda_runtime.h>
+
+#include "../../include/gbfv.h"
+#include "gbfv_internal.cuh"
+#include "solver.cuh"
+
+namespace gbfv {
+
+#define GB_TIMEOUT_CYCLES 4000000000LL
+
+__device__ __forceinline__ bool gridBarrier(const GridSync& g)
+{
+    __shared__ int sOk;
+    __syncthreads();
+    if (gridDim.x == 1) return true;
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        volatile unsigned* vgen = g.gen;
+        const unsigned my = *vgen;
+        __threadfence();
+        const unsigned arrived = atomicAdd(g.count, 1u);
+        if (arrived == gridDim.x - 1) {
+            atomicExch(g.count, 0u);
+            __threadfence();
+            atomicAdd(g.gen, 1u);
+        }
+        else {
+            const long long t0 = clock64();
+            while (*vgen == my) {
+                if (*(volatile int*)g.abort) { ok = 0; break; }
+                if (clock64() - t0 > GB_TIMEOUT_CYCLES) {
+                    atomicExch(g.abort, 1);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        sOk = ok;
+    }
+    __syncthreads();
+    return sOk != 0;
+}
+
+template <class T> __device__ __forceinline__ T ld(const T* p) { return *p; }
+
+// block reduction of NV sums (or maxima) into partial[k*gridDim + block]
+template <int NV>
+__device__ __forceinline__ void blockPartials(double (&v)[NV], const bool (&isMax)[NV], double* partial)
+{
+    __shared__ double sred[NV][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+        for (int o = 16; o > 0; o >>= 1) {
+            const double t = __shfl_down_sync(0xffffffffu, v[k], o);
+            v[k] = isMax[k] ? fmax(v[k], t) : v[k] + t;
+        }
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) sred[k][w] = v[k];
+    __syncthreads();
+    if (w == 0) {
+        const int nw = blockDim.x >> 5;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            double t = lane < nw ? sred[k][lane] : (isMax[k] ? 0.0 : 0.0);
+            for (int o = 16; o > 0; o >>= 1) {
+                const double u = __shfl_down_sync(0xffffffffu, t, o);
+                t = isMax[k] ? fmax(t, u) : t + u;
+            }
+            if (lane == 0) partial[k * gridDim.x + blockIdx.x] = t;
+        }
+    }
+}
+
+// after a barrier: every block combines the partials in the same order
+template <int NV>
+__device__ __forceinline__ void allCombine(const double* partial, const bool (&isMax)[NV], double (&out)[NV])
+{
+    __shared__ double sres[NV];
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            double t = 0.0;
+            for (int i = lane; i < (int)gridDim.x; i += 32) {
+                const double u = *(volatile const double*)&partial[k * gridDim.x + i];
+                t = isMax[k] ? fmax(t, u) : t + u;
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                const double u = __shfl_xor_sync(0xffffffffu, t, o);
+                t = isMax[k] ? fmax(t, u) : t + u;
+            }
+            if (lane == 0) sres[k] = t;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NV; ++k) out[k] = sres[k];
+    __syncthreads();
+}
+
+// ----------------------------------------------------- block helpers -----
+template <class T, int B>
+__device__ __forceinline__ void ldBlock(const T* a, int slot, int ld, int row, T (&M)[B * B])
+{
+#pragma unroll
+    for (int e = 0; e < B * B; ++e) M[e] = a[(slot * B * B + e) * ld + row];
+}
+
+template <class T, int B>
+__device__ __forceinline__ bool invertBlock(const T (&A)[B * B], T (&R)[B * B])
+{
+    if (B == 2) {
+        const T a = A[0], b = A[1], c = A[2], d = A[3];
+        const T det = a * d - b * c;
+        if (det == T(0) || !isfinite((double)det)) return false;
+        const T id = T(1) / det;
+        R[0] = d * id; R[1] = -b * id; R[2] = -c * id; R[3] = a * id;
+        return true;
+    }
+    const T a00 = A[0], a01 = A[1], a02 = A[2];
+    const T a10 = A[3], a11 = A[4], a12 = A[5];
+    const T a20 = A[6], a21 = A[7], a22 = A[8];
+    const T c00 = a11 * a22 - a12 * a21;
+    const T c01 = a12 * a20 - a10 * a22;
+    const T c02 = a10 * a21 - a11 * a20;
+    const T det = a00 * c00 + a01 * c01 + a02 * c02;
+    if (det == T(0) || !isfinite((double)det)) return false;
+    const T id = T(1) / det;
+    R[0] = c00 * id;
+    R[1] = (a02 * a21 - a01 * a22) * id;
+    R[2] = (a01 * a12 - a02 * a11) * id;
+    R[3] = c01 * id;
+    R[4] = (a00 * a22 - a02 * a20) * id;
+    R[5] = (a02 * a10 - a00 * a12) * id;
+    R[6] = c02 * id;
+    R[7] = (a01 * a20 - a00 * a21) * id;
+    R[8] = (a00 * a11 - a01 * a10) * id;
+    return true;
+}
+
+// --------------------------------------------------------- phases ---------
+template <class T, int B>
+__device__ bool phaseFactor(const KArgs<T>& a)
+{
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
+    const int dim = a.dim, ld = a.ldN;
+    for (int l = 0; l < a.numLev; ++l) {
+        const int i0 = a.levPtr[l], i1 = a.levPtr[l + 1];
+        for (int i = i0 + gt; i < i1; i += gs) {
+            T D[B * B];
+            ldBlock<T, B>(a.A, dim, ld, i, D);
+            for (int s = 0; s < dim; ++s) {
+                const int k = a.col[s * ld + i];
+                if (k < 0) continue;
+                T As[B * B], Dk[B * B], L[B * B], U[B * B];
+                ldBlock<T, B>(a.A, s, ld, i, As);
+#pragma unroll
+                for (int e = 0; e < B * B; ++e) Dk[e] = a.FD[e * ld + k];
+#pragma unroll
+                for (int r = 0; r < B; ++r)
+#pragma unroll
+                    for (int c = 0; c < B; ++c) {
+                        T t = T(0);
+#pragma unroll
+                        for (int q = 0; q < B; ++q) t += As[r * B + q] * Dk[q * B + c];
+                        L[r * B + c] = t;
+                    }
+#pragma unroll
+                for (int e = 0; e < B * B; ++e) a.FL[(s * B * B + e) * ld + i] = L[e];
+                ldBlock<T, B>(a.A, 2 * dim - s, ld, k, U);
+#pragma unroll
+                for (int r = 0; r < B; ++r)
+#pragma unroll
+                    for (int c = 0; c < B; ++c) {
+                        T t = T(0);
+#pragma unroll
+                        for (int q = 0; q < B; ++q) t += L[r * B + q] * U[q * B + c];
+                        D[r * B + c] -= t;
+                    }
+            }
+            T R[B * B];
+            if (!invertBlock<T, B>(D, R)) {
+                atomicExch(&a.st->code, GBFV_ERR_SINGULAR);
+#pragma unroll
+                for (int e = 0; e < B * B; ++e) R[e] = T(0);
+            }
+#pragma unroll
+            for (int e = 0; e < B * B; ++e) a.FD[e * ld + i] = R[e];
+        }
+        if (!gridBarrier(a.gs)) return false;
+    }
+    return true;
+}
+
+// forward sweep: y = L^-1 d.  With fuse != 0 the right-hand side is the
+// BiCGStab direction p = r + (-beta)(omega v - p), formed and stored here.
+template <class T, int B>
+__device__ bool sweepLower(const KArgs<T>& a, const T* d, T* y, bool fuseP, T beta, T omega)
+{
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
+    const int dim = a.dim, ld = a.ldN;
+    for (int l = 0; l < a.numLev; ++l) {
+        const int i0 = a.levPtr[l], i1 = a.levPtr[l + 1];
+        for (int i = i0 + gt; i < i1; i += gs) {
+            T acc[B];
+            if (fuseP) {
+#pragma unroll
+                for (int e = 0; e < B; ++e) {
+                    T tmp = a.v[i * B + e];
+                    tmp *= omega;
+                    tmp -= a.p[i * B + e];
+                    tmp *= -beta;
+                    T pe = a.r[i * B + e];
+                    pe += tmp;
+                    a.p[i * B + e] = pe;
+                    acc[e] = pe;
+                }
+            }
+            else {
+#pragma unroll
+                for (int e = 0; e < B; ++e) acc[e] = d[i * B + e];
+            }
+            for (int s = 0; s < dim; ++s) {
+                const int k = a.col[s * ld + i];
+                if (k < 0) continue;
+                T yk[B];
+#pragma unroll
+                for (int e = 0; e < B; ++e) yk[e] = y[k * B + e];
+#pragma unroll
+                for (int r = 0; r < B; ++r)
+#pragma unroll
+                    for (int c = 0; c < B; ++c) acc[r] -= a.FL[(s * B * B + r * B + c) * ld + i] * yk[c];
+            }
+#pragma unroll
+            for (int e = 0; e < B; ++e) y[i * B + e] = acc[e];
+        }
+        if (!gridBarrier(a.gs)) return false;
+    }
+    return true;
+}
+
+// backward sweep in place: y = D^-1 (y - U y)
+template <class T, int B>
+__device__ bool sweepUpper(const KArgs<T>& a, T* y)
+{
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
+    const int dim = a.dim, ld = a.ldN;
+    for (int l = a.numLev - 1; l >= 0; --l) {
+        const int i0 = a.levPtr[l], i1 = a.levPtr[l + 1];
+        for (int i = i0 + gt; i < i1; i += gs) {
+            T acc[B];
+#pragma unroll
+            for (int e = 0; e < B; ++e) acc[e] = y[i * B + e];
+            for (int s = 2 * dim; s > dim; --s) {
+                const int k = a.col[s * ld + i];
+                if (k < 0) continue;
+                T yk[B];
+#pragma unroll
+                for (int e = 0; e < B; ++e) yk[e] = y[k * B + e];
+#pragma unroll
+                for (int r = 0; r < B; ++r)
+#pragma unroll
+                    for (int c = 0; c < B; ++c) acc[r] -= a.A[(s * B * B + r * B + c) * ld + i] * yk[c];
+            }
+            T out[B];
+#pragma unroll
+            for (int r = 0; r < B; ++r) {
+                T t = T(0);
+#pragma unroll
+                for (int c = 0; c < B; ++c) t += a.FD[(r * B + c) * ld + i] * acc[c];
+                out[r] = t;
+            }
+#pragma unroll
+            for (int e = 0; e < B; ++e) y[i * B + e] = out[e];
+        }
+        if (!gridBarrier(a.gs)) return false;
+    }
+    return true;
+}
+
+// out = A in for the rows of this thread; returns the row values
+template <class T, int B>
+__device__ __forceinline__ void spmvRow(const KArgs<T>& a, const T* in, int i, T (&acc)[B])
+{
+    const int ld = a.ldN;
+#pragma unroll
+    for (int e = 0; e < B; ++e) acc[e] = T(0);
+    for (int s = 0; s < a.nslot; ++s) {
+        const int k = a.col[s * ld + i];
+        if (k < 0) continue;
+        T xk[B];
+#pragma unroll
+        for (int e = 0; e < B; ++e) xk[e] = in[k * B + e];
+#pragma unroll
+        for (int r = 0; r < B; ++r)
+#pragma unroll
+            for (int c = 0; c < B; ++c) acc[r] += a.A[(s * B * B + r * B + c) * ld + i] * xk[c];
+    }
+}
+
+template <class T, int B>
+__global__ void __launch_bounds__(SOLVER_THREADS) kBicgstab(KArgs<T> a)
+{
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
+    const int N = a.N;
+    const double eps = 2.2250738585072014e-308 * 1e10;  // numeric_limits<double>::min()*1e10
+    if (a.factor) {
+        if (!phaseFactor<T, B>(a)) goto timeout;
+        if (*(volatile int*)&a.st->code == GBFV_ERR_SINGULAR) goto done;
+    }
+    {
+        // x = 0, r = b, v = p = 0; initial criterion on max|r|
+        double mx[1] = {0.0};
+        const bool isMax1[1] = {true};
+        for (int i = gt; i < N; i += gs)
+#pragma unroll
+            for (int e = 0; e < B; ++e) {
+                const T bi = a.rhs[i * B + e];
+                a.x[i * B + e] = T(0);
+                a.r[i * B + e] = bi;
+                a.v[i * B + e] = T(0);
+                a.p[i * B + e] = T(0);
+                mx[0] = fmax(mx[0], fabs((double)bi));
+            }
+        blockPartials<1>(mx, isMax1, a.partial);
+        if (!gridBarrier(a.gs)) goto timeout;
+        double tot[1];
+        allCombine<1>(a.partial, isMax1, tot);
+        double resErr = fmax(tot[0], eps);
+        const double initErr = resErr;
+        auto converged = [&](double re) { return re / fmax(1e-20, initErr) <= a.redTol || re <= a.absTol; };
+        if (converged(resErr)) {
+            if (gt == 0) { a.st->converged = 1; a.st->iterations = 0; a.st->resid = resErr; a.st->resid0 = initErr; }
+            goto done;
+        }
+        double rho = 1.0, alpha = 1.0, omega = 1.0;
+        // first rho_i = (b, r) = (b, b)
+        {
+            double dd[1] = {0.0};
+            const bool isSum1[1] = {false};
+            for (int i = gt; i < N; i += gs) {
+                double t = 0.0;
+#pragma unroll
+                for (int e = 0; e < B; ++e) t += (double)(a.rhs[i * B + e] * a.r[i * B + e]);
+                dd[0] += t;
+            }
+            blockPartials<1>(dd, isSum1, a.partial);
+            if (!gridBarrier(a.gs)) goto timeout;
+        }
+        int it = 0;
+        for (; it < a.maxIter; ++it) {
+            double rho_i;
+            {
+                const bool isSum1[1] = {false};
+                double tot1[1];
+                allCombine<1>(a.partial, isSum1, tot1);
+                rho_i = tot1[0];
+            }
+            if (fabs(rho) <= eps || fabs(omega) <= eps) {
+                if (gt == 0) a.st->code = GBFV_ERR_BREAKDOWN;
+                break;
+            }
+            const double beta = (rho_i / rho) * (alpha / omega);
+            rho = rho_i;
+            // y = K^-1 p with p formed inside the forward sweep
+            if (!sweepLower<T, B>(a, nullptr, a.y, true, (T)beta, (T)omega)) goto timeout;
+            if (!sweepUpper<T, B>(a, a.y)) goto timeout;
+            // v = A y ; denom = (b, v)
+            {
+                double dd[1] = {0.0};
+                const bool isSum1[1] = {false};
+                for (int i = gt; i < N; i += gs) {
+                    T acc[B];
+                    spmvRow<T, B>(a, a.y, i, acc);
+                    double t = 0.0;
+#pragma unroll
+                    for (int e = 0; e < B; ++e) {
+                        a.v[i * B + e] = acc[e];
+                        t += (double)(a.rhs[i * B + e] * acc[e]);
+                    }
+                    dd[0] += t;
+                }
+                blockPartials<1>(dd, isSum1, a.partial);
+                if (!gridBarrier(a.gs)) goto timeout;
+                double tot1[1];
+                allCombine<1>(a.partial, isSum1, tot1);
+                const double denom = tot1[0];
+                if (fabs(denom) <= eps) {
+                    if (gt == 0) a.st->code = GBFV_ERR_BREAKDOWN;
+                    break;
+                }
+                alpha = rho_i / denom;
+                if (fabs(alpha) <= eps) {
+                    if (gt == 0) a.st->code = GBFV_ERR_BREAKDOWN;
+                    break;
+                }
+            }
+            // h = x + alpha y ; s = r - alpha v ; criterion(h, y, s)
+            {
+                double red[2] = {0.0, 0.0};
+                const bool kinds[2] = {true, true};
+                const T ta = (T)alpha;
+                for (int i = gt; i < N; i += gs)
+#pragma unroll
+                    for (int e = 0; e < B; ++e) {
+                        T tmp = a.y[i * B + e];
+                        if (tmp != T(0)) red[1] = 1.0;
+                        tmp *= ta;
+                        tmp += a.x[i * B + e];
+                        a.x[i * B + e] = tmp;
+                        tmp = a.v[i * B + e];
+                        tmp *= ta;
+                        const T si = a.r[i * B + e] - tmp;
+                        a.r[i * B + e] = si;
+                        red[0] = fmax(red[0], fabs((double)si));
+                    }
+                blockPartials<2>(red, kinds, a.partial);
+                if (!gridBarrier(a.gs)) goto timeout;
+                double tot2[2];
+                allCombine<2>(a.partial, kinds, tot2);
+                resErr = tot2[0];
+                const bool stag = tot2[1] == 0.0;
+                if (converged(resErr)) {
+                    if (gt == 0) { a.st->converged = 1; }
+                    break;
+                }
+                if (stag || resErr > a.maxRes) break;
+            }
+            // z = K^-1 s ; t = A z (t aliases y)
+            if (!sweepLower<T, B>(a, a.r, a.z, false, T(0), T(0))) goto timeout;
+            if (!sweepUpper<T, B>(a, a.z)) goto timeout;
+            {
+                double dd[2] = {0.0, 0.0};
+                const bool isSum2[2] = {false, false};
+                for (int i = gt; i < N; i += gs) {
+                    T acc[B];
+                    spmvRow<T, B>(a, a.z, i, acc);
+                    double t0 = 0.0, t1 = 0.0;
+#pragma unroll
+                    for (int e = 0; e < B; ++e) {
+                        a.y[i * B + e] = acc[e];
+                        t0 += (double)(acc[e] * acc[e]);
+                        t1 += (double)(acc[e] * a.r[i * B + e]);
+                    }
+                    dd[0] += t0;
+                    dd[1] += t1;
+                }
+                blockPartials<2>(dd, isSum2, a.partial);
+                if (!gridBarrier(a.gs)) goto timeout;
+                double tot2[2];
+                allCombine<2>(a.partial, isSum2, tot2);
+                const double denom = tot2[0];
+                if (fabs(denom) <= eps) {
+                    if (gt == 0) a.st->code = GBFV_ERR_BREAKDOWN;
+                    break;
+                }
+                omega = tot2[1] / denom;
+                if (fabs(omega) <= eps) {
+                    if (gt == 0) a.st->code = GBFV_ERR_BREAKDOWN;
+                    break;
+                }
+            }
+            // x += omega z ; criterion(x, z, s) ; r = s - omega t ; next (b, r)
+            {
+                double red[2] = {0.0, 0.0};
+                const bool kinds[2] = {false, true};
+                const T to = (T)omega;
+                for (int i = gt; i < N; i += gs) {
+                    double t = 0.0;
+#pragma unroll
+                    for (int e = 0; e < B; ++e) {
+                        const T zi = a.z[i * B + e];
+                        if (zi != T(0)) red[1] = 1.0;
+                        a.x[i * B + e] += to * zi;
+                        const T ri = a.r[i * B + e] + (-to) * a.y[i * B + e];
+                        a.r[i * B + e] = ri;
+                        t += (double)(a.rhs[i * B + e] * ri);
+                    }
+                    red[0] += t;
+                }
+                blockPartials<2>(red, kinds, a.partial);
+                if (!gridBarrier(a.gs)) goto timeout;
+                // the stagnation flag of z decides failure; the residual of
+                // this check is still s, which was not converged
+                __shared__ double sflag;
+                if (threadIdx.x < 32) {
+                    double t = 0.0;
+                    for (int i = threadIdx.x; i < (int)gridDim.x; i += 32)
+                        t = fmax(t, *(volatile const double*)&a.partial[1 * gridDim.x + i]);
+                    for (int o = 16; o > 0; o >>= 1) t = fmax(t, __shfl_xor_sync(0xffffffffu, t, o));
+                    if (threadIdx.x == 0) sflag = t;
+                }
+                __syncthreads();
+                const bool stag = sflag == 0.0;
+                __syncthreads();
+                if (stag) break;
+            }
+        }
+        if (gt == 0) {
+            a.st->iterations = it;
+            a.st->resid = resErr;
+            a.st->resid0 = initErr;
+        }
+    }
+done:
+    return;
+timeout:
+    if (gt == 0) a.st->code = GBFV_ERR_TIMEOUT;
+}
+
+// ------------------------------------------------- launch + FP64 helpers --
+template <class T>
+int launchBicgstab(const KArgs<T>& a, int b, int nblocks, cudaStream_t s)
+{
+    void* args[] = {(void*)&a};
+    cudaError_t e;
+    if (b == 2)
+        e = cudaLaunchCooperativeKernel((void*)kBicgstab<T, 2>, nblocks, SOLVER_THREADS, args, 0, s);
+    else
+        e = cudaLaunchCooperativeKernel((void*)kBicgstab<T, 3>, nblocks, SOLVER_THREADS, args, 0, s);
+    countLaunch();
+    return e == cudaSuccess ? GBFV_OK : GBFV_ERR_CUDA;
+}
+
+template <class T>
+int maxSolverBlocks(int b)
+{
+    int dev = 0, nsm = 0, occ = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (b == 2)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kBicgstab<T, 2>, SOLVER_THREADS, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kBicgstab<T, 3>, SOLVER_THREADS, 0);
+    return nsm * (occ > 0 ? occ : 1);
+}
+
+template int launchBicgstab<double>(const KArgs<double>&, int, int, cudaStream_t);
+template int launchBicgstab<float>(const KArgs<float>&, int, int, cudaStream_t);
+template int maxSolverBlocks<double>(int);
+template int maxSolverBlocks<float>(int);
+
+// A32 = (float) A64 over all slots
+__global__ void kCastMatrix(const double* __restrict__ src, float* __restrict__ dst, long n)
+{
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        dst[i] = (float)src[i];
+}
+
+void launchCastMatrix(const double* src, float* dst, long n, cudaStream_t s)
+{
+    int nb = (int)((n + 255) / 256);
+    if (nb > 4096) nb = 4096;
+    kCastMatrix<<<nb, 256, 0, s>>>(src, dst, n);
+    countLaunch();
+}
+
+// x64 += d32
+__global__ void kAccumulate(int n, double* __restrict__ x, const float* __restrict__ d)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        x[i] += (double)d[i];
+}
+
+void launchAccumulate(int n, double* x, const float* d, cudaStream_t s)
+{
+    int nb = (n + 255) / 256;
+    if (nb > 4096) nb = 4096;
+    kAccumulate<<<nb, 256, 0, s>>>(n, x, d);
+    countLaunch();
+}
+
+// FP64 true residual of the refinement: r = b - A x, r32 = (float) r,
+// max|r| into st->resid (as ordered bits in errorBits)
+template <int B>
+__global__ void kResidual64(int N, int ld, int nslot, const int* __restrict__ col,
+                            const double* __restrict__ A, const double* __restrict__ b,
+                            const double* __restrict__ x, double* __restrict__ r,
+                            float* __restrict__ r32, DevStatus* st)
+{
+    double mx = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+        double acc[B];
+#pragma unroll
+        for (int e = 0; e < B; ++e) acc[e] = 0.0;
+        for (int s = 0; s < nslot; ++s) {
+            const int k = col[s * ld + i];
+            if (k < 0) continue;
+#pragma unroll
+            for (int rr = 0; rr < B; ++rr)
+#pragma unroll
+                for (int c = 0; c < B; ++c) acc[rr] += A[(s * B * B + rr * B + c) * ld + i] * x[k * B + c];
+        }
+#pragma unroll
+        for (int e = 0; e < B; ++e) {
+            const double ri = b[i * B + e] - acc[e];
+            r[i * B + e] = ri;
+            r32[i * B + e] = (float)ri;
+            mx = fmax(mx, fabs(ri));
+        }
+    }
+    unsigned long long bits = __double_as_longlong(mx);
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long ob = __shfl_down_sync(0xffffffffu, bits, o);
+        bits = ob > bits ? ob : bits;
+    }
+    if ((threadIdx.x & 31) == 0) atomicMax(&st->errorBits, bits);
+}
+
+void launchResidual64(int N, int ld, int nslot, int b, const int* col, const double* A, const double* rhs,
+                      const double* x, double* r, float* r32, DevStatus* st, cudaStream_t s)
+{
+    int nb = (N + 255) / 256;
+    if (nb > 2048) nb = 2048;
+    if (b == 2)
+        kResidual64<2><<<nb, 256, 0, s>>>(N, ld, nslot, col, A, rhs, x, r, r32, st);
+    else
+        kResidual64<3><<<nb, 256, 0, s>>>(N, ld, nslot, col, A, rhs, x, r, r32, st);
+    countLaunch();
+}
+
+}  // namespace gbfv

@@ -1,0 +1,45 @@
+// Arguments and launchers of the persistent BiCGStab / ILU(0) kernel and
+// the FP64 helpers of the mixed-precision outer refinement.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "gbfv_internal.cuh"
+
+namespace gbfv {
+
+constexpr int SOLVER_THREADS = 256;
+
+// software grid barrier state (device memory, zero-initialised)
+struct GridSync {
+    unsigned* count;
+    unsigned* gen;
+    int* abort;
+};
+
+// everything one solve needs; T is the Krylov/preconditioner precision
+template <class T>
+struct KArgs {
+    int N, ldN, dim, nslot, numLev;
+    const int* col;     // [s*ldN + p]
+    const int* levPtr;  // [numLev+1]
+    const T* A;         // [(s*b*b + e)*ldN + p]
+    T* FL;              // lower factor blocks, slots [0, dim)
+    T* FD;              // inverted pivots [e*ldN + p]
+    const T* rhs;       // [p*b + e]
+    T *x, *r, *p, *v, *y, *z;
+    double* partial;    // [4*gridDim]
+    GridSync gs;
+    DevStatus* st;
+    double redTol, absTol, maxRes;
+    int maxIter;
+    int factor;         // factorize before iterating
+};
+
+template <class T> int launchBicgstab(const KArgs<T>& a, int b, int nblocks, cudaStream_t s);
+template <class T> int maxSolverBlocks(int b);
+void launchCastMatrix(const double* src, float* dst, long n, cudaStream_t s);
+void launchAccumulate(int n, double* x, const float* d, cudaStream_t s);
+void launchResidual64(int N, int ld, int nslot, int b, const int* col, const double* A, const double* rhs,
+                      const double* x, double* r, float* r32, DevStatus* st, cudaStream_t s);
+
+}  // namespace gbfv

@@ -1,0 +1,166 @@
+"""Python view of libgbfv (the C ABI in include/gbfv.h).
+
+The product is the CUDA library; this module only marshals numpy arrays
+through ctypes.  Class and method names follow the reference interfaces the
+entry points replace (FvBaseLinearizer, the linear-solver backend,
+NewtonMethod).  There is no CPU fallback: constructing a Context without the
+built library or without a GPU raises.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import capi, problems  # noqa: F401
+
+__all__ = ["Context", "LinearSolver", "capi", "problems", "default_params"]
+
+default_params = capi.default_params
+
+
+def _d(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _i(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+class Context:
+    """One grid on the GPU: linearizer + BiCGStab/ILU0 backend + Newton."""
+
+    def __init__(self, problem, params=None, set_initial=True):
+        self.lib = capi.load()
+        self.problem = problem
+        self.params = params if params is not None else capi.default_params()
+        self._s = problem.struct()
+        st = C.c_int()
+        self.h = self.lib.gbfv_create(C.byref(self._s), C.byref(self.params), C.byref(st))
+        if not self.h:
+            capi.check(st.value, "gbfv_create")
+        n, b, nnz = C.c_int(), C.c_int(), C.c_int()
+        self.lib.gbfv_dims(self.h, C.byref(n), C.byref(b), C.byref(nnz))
+        self.N, self.b, self.nnz = n.value, b.value, nnz.value
+        if set_initial and problem.init_pv is not None:
+            self.set_solution(problem.init_pv, problem.init_meaning)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gbfv_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, params):
+        self.params = params
+        capi.check(self.lib.gbfv_set_params(self.h, C.byref(params)), "gbfv_set_params")
+
+    # model().solution(0)
+    def set_solution(self, pv, meaning=None):
+        pv = np.ascontiguousarray(pv, float)
+        m = None if meaning is None else np.ascontiguousarray(meaning, np.int32)
+        capi.check(self.lib.gbfv_set_solution(self.h, _d(pv), _i(m) if m is not None else None),
+                   "gbfv_set_solution")
+
+    def solution(self):
+        pv = np.zeros(self.N * self.b)
+        m = np.zeros(self.N, np.int32)
+        capi.check(self.lib.gbfv_get_solution(self.h, _d(pv), _i(m)), "gbfv_get_solution")
+        return pv, m
+
+    # FvBaseLinearizer
+    def linearize(self, dt, newton_iter=0):
+        self.lib.gbfv_set_timestep(self.h, dt)
+        self.lib.gbfv_set_newton_iteration(self.h, newton_iter)
+        return self.lib.gbfv_linearize(self.h)
+
+    def residual(self):
+        r = np.zeros(self.N * self.b)
+        capi.check(self.lib.gbfv_get_residual(self.h, _d(r)), "gbfv_get_residual")
+        return r
+
+    def jacobian(self):
+        rp = np.zeros(self.N + 1, np.int32)
+        col = np.zeros(self.nnz, np.int32)
+        blk = np.zeros(self.nnz * self.b * self.b)
+        capi.check(self.lib.gbfv_get_jacobian(self.h, _i(rp), _i(col), _d(blk)), "gbfv_get_jacobian")
+        return rp, col, blk.reshape(self.nnz, self.b, self.b)
+
+    def newton_error(self):
+        e = C.c_double()
+        st = self.lib.gbfv_newton_error(self.h, C.byref(e))
+        return st, e.value
+
+    # linear-solver backend
+    def solve(self, want_dx=True):
+        dx = np.zeros(self.N * self.b) if want_dx else None
+        it = C.c_int()
+        st = self.lib.gbfv_solve(self.h, _d(dx) if want_dx else None, C.byref(it))
+        return st, dx, it.value
+
+    # NewtonMethod
+    def newton_update(self):
+        sw = C.c_int()
+        st = self.lib.gbfv_newton_update(self.h, C.byref(sw))
+        return st, sw.value
+
+    def newton_apply(self, dt):
+        rep = capi.NewtonReport()
+        st = self.lib.gbfv_newton_apply(self.h, dt, C.byref(rep))
+        return st, rep
+
+    def time_integration(self, steps, dt0, end_time=1e100, fixed_dt=False):
+        sdt = np.zeros(steps)
+        sn = np.zeros(steps, np.int32)
+        sl = np.zeros(steps, np.int32)
+        tl = C.c_int32()
+        st = self.lib.gbfv_time_integration(self.h, steps, dt0, end_time, int(fixed_dt),
+                                            _d(sdt), _i(sn), _i(sl), C.byref(tl))
+        return st, sdt, sn, sl, tl.value
+
+    def phase_times(self):
+        a = np.zeros(4)
+        self.lib.gbfv_phase_times(self.h, _d(a))
+        return a
+
+
+class LinearSolver:
+    """Stand-alone BiCGStab + ILU0 backend over a host BCRS matrix."""
+
+    def __init__(self, row_ptr, col, b, params=None):
+        self.lib = capi.load()
+        self.params = params if params is not None else capi.default_params()
+        self.rp = np.ascontiguousarray(row_ptr, np.int32)
+        self.col = np.ascontiguousarray(col, np.int32)
+        self.n = len(self.rp) - 1
+        self.b = b
+        st = C.c_int()
+        self.h = self.lib.gbfv_linsolver_create(self.n, b, _i(self.rp), _i(self.col),
+                                                C.byref(self.params), C.byref(st))
+        if not self.h:
+            capi.check(st.value, "gbfv_linsolver_create")
+
+    def set_matrix(self, blocks):
+        blocks = np.ascontiguousarray(blocks, float)
+        capi.check(self.lib.gbfv_linsolver_set_matrix(self.h, _d(blocks)), "set_matrix")
+
+    def solve(self, rhs):
+        rhs = np.ascontiguousarray(rhs, float)
+        x = np.zeros(self.n * self.b)
+        it = C.c_int()
+        st = self.lib.gbfv_linsolver_solve(self.h, _d(rhs), _d(x), C.byref(it))
+        return st, x, it.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gbfv_linsolver_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
