@@ -1,0 +1,351 @@
+#!/usr/bin/env python
+"""Benchmark: cell-Newton-iterations/s of the ECFV/TPFA linearization +
+BiCGStab/ILU0 Newton solve on the three-phase black-oil grid
+100x100x20 (200k cells, 3x3 blocks), 10 time steps of 1 day.
+
+One bench step = the whole 10-time-step run from the initial state (restored
+on the device before each step).  value = sum over time steps of Newton
+iterations x cells / device time, for the mixed-precision form (FP64
+residual/Jacobian/update/outer residual, FP32 ILU0 + FP32 BiCGStab inside
+FP64 iterative refinement, linear tolerance 1e-6 relative).  The plain FP64
+form is measured on the same workload and reported beside it.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+For N > 1 (torchrun, one rank per GPU) every rank runs its own replica: the
+path has no data-path collective, scaling is weak.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "opm-models_gb300"))
+
+import numpy as np  # noqa: E402
+
+WORKLOADS = {
+    "blackoil-100x100x20": dict(nx=100, ny=100, nz=20, steps=10, dt=86400.0),
+    "blackoil-100x100x100": dict(nx=100, ny=100, nz=100, steps=10, dt=86400.0),
+    "blackoil-50x50x20": dict(nx=50, ny=50, nz=20, steps=10, dt=86400.0),
+}
+METRIC = "cell-Newton-iters/s (mixed vs plain FP64, same tol); served solve p50/p99 ms"
+UNIT = "cell-Newton-iters/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="blackoil-100x100x20", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.file, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        if self.proc is None:
+            return out
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.file.flush()
+        self.file.seek(0)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.file.read().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        self.file.close()
+        os.unlink(self.file.name)
+        if sm:
+            out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                   "samples": len(sm)}
+        return out
+
+
+def build_problem(wl):
+    from gbfv import problems
+    w = WORKLOADS[wl]
+    return problems.blackoil(w["nx"], w["ny"], w["nz"])
+
+
+def params(precision):
+    from gbfv import capi
+    return capi.default_params(linear_tolerance=1e-6, newton_tolerance=1e-6, precision=precision,
+                               inner_tolerance=1e-5)
+
+
+def cpu_sample(prob, iters=2):
+    """The oracle (the reference algorithm restated on the CPU) on the first
+    `iters` Newton iterations of the first time step: OpenMP over elements in
+    the linearization, sequential BiCGStab/ILU0 (as the reference)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    orc = O.Oracle(prob, params(0))
+    t0 = time.perf_counter()
+    for it in range(iters):
+        st = orc.linearize(86400.0, it)
+        if st:
+            raise RuntimeError("oracle linearize failed %d" % st)
+        st, _, _ = orc.solve()
+        orc.newton_update()
+    dt = time.perf_counter() - t0
+    orc.close()
+    return iters * prob.num_cells / dt, dt, threads
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    prob = build_problem(args.workload)
+    for _ in range(args.warmup):
+        cpu_sample(prob)
+    vals, tot = [], 0.0
+    for _ in range(args.steps):
+        v, dt, threads = cpu_sample(prob)
+        vals.append(v)
+        tot += dt
+    value = args.steps * 2 * prob.num_cells / tot
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * tot / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded lognormal permeability, uniform porosity)",
+        "config": {"workload": args.workload + " black-oil, first 2 Newton iterations of time step 1",
+                   "cells": prob.num_cells, "precision": "fp64"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "2 Newton iterations (linearize + BiCGStab/ILU0 to 1e-6 + update) of "
+                                   "time step 1 of the %s workload, per step" % args.workload},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def timed_runs(ctx, w, steps, warmup, flush, torch, ext):
+    """Device-time K full runs (restore state on device, 10 time steps)."""
+    its = []
+    for _ in range(warmup):
+        ctx.restore_state()
+        st, sdt, sn, sl, tl = ctx.time_integration(w["steps"], w["dt"], fixed_dt=True)
+        if st:
+            raise RuntimeError("warm-up run failed %d" % st)
+    ms_tot, cells_its = 0.0, 0
+    launches0 = ctx.lib.gbfv_kernel_launches()
+    ctx.reset_kernel_stats()
+    for _ in range(steps):
+        with torch.cuda.stream(ext):
+            flush.zero_()  # write a buffer larger than L2 between timed steps
+        ctx.restore_state()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        st, sdt, sn, sl, tl = ctx.time_integration(w["steps"], w["dt"], fixed_dt=True)
+        e1.record(ext)
+        e1.synchronize()
+        if st:
+            raise RuntimeError("timed run failed %d" % st)
+        ms_tot += e0.elapsed_time(e1)
+        cells_its += int(sn.sum()) * ctx.N
+        its.append((sn.copy(), sl.copy()))
+    launches = ctx.lib.gbfv_kernel_launches() - launches0
+    return ms_tot, cells_its, its, launches, ctx.kernel_stats()
+
+
+def run_ours(args):
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    import __graft_entry__ as ge
+    if rank == 0 or world == 1:
+        ge.build()
+    if world > 1:
+        dist.barrier()
+        ge.build()
+    from gbfv import Context, capi
+    w = WORKLOADS[args.workload]
+    prob = build_problem(args.workload)
+    N = prob.num_cells
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    results = {}
+    for name, prec in (("mixed", capi.PREC_MIXED), ("fp64", capi.PREC_FP64)):
+        ctx = Context(prob, params(prec))
+        ctx.save_state()
+        ext = torch.cuda.ExternalStream(ctx.stream())
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        sampler = ClockSampler(local) if name == "mixed" and rank == 0 else None
+        if sampler:
+            sampler.start()
+        ms, cits, its, launches, kst = timed_runs(ctx, w, args.steps, args.warmup, flush, torch, ext)
+        torch.cuda.synchronize()
+        clocks = sampler.stop() if sampler else None
+        if world > 1:
+            t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+            c = torch.tensor([cits], dtype=torch.float64, device="cuda")
+            dist.all_reduce(c, op=dist.ReduceOp.SUM)
+            cits = float(c.item())
+        cfg = ctx.solver_config(prec)
+        results[name] = dict(ms=ms, cits=cits, its=its, launches=launches, kst=kst, clocks=clocks, ctx=ctx,
+                             cfg=cfg)
+    # end-to-end through the C ABI with host buffers (mixed form)
+    ctx = results["mixed"]["ctx"]
+    pv_host = torch.empty(N * 3, dtype=torch.float64, pin_memory=True).numpy()
+    m_host = torch.empty(N, dtype=torch.int32, pin_memory=True).numpy()
+    out_pv = torch.empty(N * 3, dtype=torch.float64, pin_memory=True).numpy()
+    out_m = torch.empty(N, dtype=torch.int32, pin_memory=True).numpy()
+    pv_host[:] = prob.init_pv
+    m_host[:] = prob.init_meaning
+    e2e_s, e2e_cits = 0.0, 0
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.set_solution(pv_host, m_host)
+        ctx.lib.gbfv_reset_kernel_stats(ctx.h)
+        st, sdt, sn, sl, tl = ctx.time_integration(w["steps"], w["dt"], fixed_dt=True)
+        out_pv[:], out_m[:] = ctx.solution()
+        e2e_s += time.perf_counter() - t0
+        e2e_cits += int(sn.sum()) * N
+    if world > 1:
+        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+        c = torch.tensor([e2e_cits], dtype=torch.float64, device="cuda")
+        dist.all_reduce(c, op=dist.ReduceOp.SUM)
+        e2e_cits = float(c.item())
+    if rank != 0:
+        if world > 1:
+            dist.barrier()
+            dist.destroy_process_group()
+        return 0
+    mixed, plain = results["mixed"], results["fp64"]
+    value = mixed["cits"] / (mixed["ms"] / 1000.0)
+    plain_value = plain["cits"] / (plain["ms"] / 1000.0)
+    peak, peak_kind = load_peaks()
+    kst = mixed["kst"]
+    achieved = kst["solve_bytes"] / (kst["solve_ms"] / 1000.0) / 1e9 if kst["solve_ms"] > 0 else 0.0
+    avg_launch_ms = kst["solve_ms"] / max(1, kst["solve_launches"])
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tfile):
+        try:
+            with open(tfile) as f:
+                traffic = json.load(f).get(args.workload)
+        except Exception:
+            traffic = None
+    lin_ach = kst["linearize_bytes"] / (kst["linearize_ms"] / 1000.0) / 1e9 if kst["linearize_ms"] > 0 else 0.0
+    sn0, sl0 = mixed["its"][0]
+    spn, spl = plain["its"][0]
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": mixed["ms"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64 residual/Jacobian/update + f32 ILU0/BiCGStab",
+        "data": "synthetic (seeded lognormal permeability sigma 1, uniform porosity [0.15,0.30])",
+        "config": {"workload": "%s three-phase black-oil, %d cells, 10 time steps x 1 day, "
+                               "BiCGStab+ILU0 to 1e-6, Newton tol 1e-6, mixed precision" % (args.workload, N),
+                   "cells": N, "time_steps": w["steps"], "precision": "mixed", "l2": "flushed (256 MiB write) "
+                   "between timed steps", "parallelism": "replicas" if world > 1 else "single GPU"},
+        "plain_fp64": {"value": plain_value, "ms_per_step": plain["ms"] / args.steps,
+                       "newton_iterations": spn.tolist(), "linear_iterations": spl.tolist()},
+        "mixed_over_plain": value / plain_value,
+        "newton_iterations": sn0.tolist(), "linear_iterations": sl0.tolist(),
+        "same_newton_iterations": bool(np.array_equal(sn0, spn)),
+        "e2e": {"value": e2e_cits / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(N * 3 * 8 + N * 4),
+                "d2h_bytes_per_step": int(N * 3 * 8 + N * 4)},
+        "gpu_launches": int(mixed["launches"] / args.steps),
+        "roofline": {"bound": "hbm", "kernel": "kBicgstab<float,3> (persistent ILU0 + BiCGStab)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_kind": peak_kind,
+                     "avg_launch_ms": avg_launch_ms, "bytes_per_launch": kst["solve_bytes"] / max(1, kst["solve_launches"])},
+        "solver_config": {"mixed": mixed["cfg"], "fp64": plain["cfg"]},
+        "linearize_roofline": {"achieved": lin_ach, "frac": lin_ach / peak, "ms": kst["linearize_ms"] / args.steps},
+        "clocks": mixed["clocks"],
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        v, dt, threads = cpu_sample(prob)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": "first 2 Newton iterations of time step 1 (%.1f s)" % dt}
+    print(json.dumps(line))
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

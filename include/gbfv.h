@@ -297,6 +297,42 @@ const char* gbfv_last_error(void);
  * [2] Krylov iterations, [3] Newton update + error                       */
 int gbfv_phase_times(const gbfv_ctx* ctx, double* ms4);
 
+/* the CUDA stream (cudaStream_t) all work of this context is issued on    */
+void* gbfv_stream(gbfv_ctx* ctx);
+
+/* device-side snapshot of the solution, its meanings and the switching
+ * flags, and its restore (keeps a run's inputs resident on the device)    */
+int gbfv_save_state(gbfv_ctx* ctx);
+int gbfv_restore_state(gbfv_ctx* ctx);
+
+/* cumulative kernel statistics since creation or the last reset.
+ * Durations are CUDA-event times on the context's stream.  Algorithmic
+ * bytes are what each kernel must move at least once for its work:
+ *   solve: per factorization  N*(S*b*b + (d+1)*b*b)*s + 4*N*d
+ *          per iteration      N*(2*S*b*b + 4*d*b*b + 2*b*b)*s
+ *                             + 4*N*(2*S + 4*d) + 30*N*b*s
+ *          (S = 2d+1 blocks per row, d = lower blocks, s = 4 or 8 bytes)
+ *   linearize: IQ pass (reads x, writes the intensive quantities) plus the
+ *          assembly pass (reads them, the face geometry and the storage
+ *          cache; writes residual and all S Jacobian blocks)            */
+typedef struct gbfv_kernel_stats {
+    double solve_ms;           /* persistent BiCGStab/ILU0 kernels        */
+    int64_t solve_launches;
+    int64_t solve_iterations;
+    int64_t solve_factorizations;
+    double solve_bytes;
+    double linearize_ms;       /* IQ + assembly kernels                   */
+    int64_t linearize_launches;
+    double linearize_bytes;
+} gbfv_kernel_stats;
+int gbfv_get_kernel_stats(const gbfv_ctx* ctx, gbfv_kernel_stats* out);
+/* launch configuration the autotuner chose for the persistent solve kernel
+ * of a precision (GBFV_PREC_FP64 / GBFV_PREC_MIXED): cluster (mode 1) or
+ * cooperative grid (mode 0), blocks, and the candidate timings [ms]       */
+int gbfv_solver_config(const gbfv_ctx* ctx, int precision, int* mode, int* blocks,
+                       double* tune_ms, int* num_tuned);
+int gbfv_reset_kernel_stats(gbfv_ctx* ctx);
+
 #ifdef __cplusplus
 }
 #endif

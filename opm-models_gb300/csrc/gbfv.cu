@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <string>
@@ -87,7 +88,18 @@ struct SolverData {
     double* partial = nullptr;
     unsigned* bar = nullptr;  // count, gen, abort
     int nblocks64 = 1, nblocks32 = 1;
-    double lastMs[4] = {0, 0, 0, 0};
+    // solver launch configuration per precision ([0] FP64, [1] FP32):
+    // SYNC_CLUSTER with a cluster of nblk blocks, or SYNC_GRID (cooperative)
+    int mode[2] = {SYNC_CLUSTER, SYNC_CLUSTER};
+    int nblk[2] = {1, 1};
+    int tuned[2] = {0, 0};
+    int maxGrid[2] = {1, 1};
+    int maxCluster[2] = {1, 1};
+    double tuneMs[2][16] = {};
+    // cumulative statistics of the persistent solve kernel
+    cudaEvent_t evA = nullptr, evB = nullptr;
+    double statMs = 0, statBytes = 0;
+    int64_t statLaunches = 0, statIters = 0, statFactor = 0;
 };
 
 int allocSolver(SolverData& S, int maxBlocksOverride = 0)
@@ -105,22 +117,41 @@ int allocSolver(SolverData& S, int maxBlocksOverride = 0)
         if ((st = devAlloc(&p, (size_t)S.N * S.b))) return st;
     if ((st = devAlloc(&S.xref, (size_t)S.N * S.b))) return st;
     if ((st = devAlloc(&S.rref, (size_t)S.N * S.b))) return st;
-    // persistent-kernel grid: one block for small systems (barriers are then
-    // __syncthreads), otherwise as many co-resident blocks as useful
-    const int smallN = 12288;
-    auto pick = [&](int maxb) {
-        if (maxBlocksOverride > 0) return std::min(maxBlocksOverride, maxb);
-        if (S.N <= smallN) return 1;
-        const int want = (S.N + SOLVER_THREADS - 1) / SOLVER_THREADS;
-        return std::max(1, std::min(maxb, want));
-    };
-    S.nblocks64 = pick(maxSolverBlocks<double>(S.b));
-    S.nblocks32 = pick(maxSolverBlocks<float>(S.b));
-    const int nbMax = std::max(S.nblocks64, S.nblocks32);
+    (void)maxBlocksOverride;
+    S.maxGrid[0] = maxSolverBlocks<double>(S.b);
+    S.maxGrid[1] = maxSolverBlocks<float>(S.b);
+    S.maxCluster[0] = std::min(16, maxClusterBlocks<double>(S.b));
+    S.maxCluster[1] = std::min(16, maxClusterBlocks<float>(S.b));
+    // default before tuning: one block for small systems, else a cluster of 8
+    for (int k = 0; k < 2; ++k) {
+        S.mode[k] = SYNC_CLUSTER;
+        S.nblk[k] = S.N <= 12288 ? 1 : std::min(8, S.maxCluster[k]);
+    }
+    // forced configuration, e.g. GBFV_SOLVER=cluster:16 or grid:152
+    if (const char* f = getenv("GBFV_SOLVER")) {
+        int n = 0;
+        if (sscanf(f, "cluster:%d", &n) == 1 && n > 0)
+            for (int k = 0; k < 2; ++k) { S.mode[k] = SYNC_CLUSTER; S.nblk[k] = std::min(n, S.maxCluster[k]); S.tuned[k] = 1; }
+        else if (sscanf(f, "grid:%d", &n) == 1 && n > 0)
+            for (int k = 0; k < 2; ++k) { S.mode[k] = SYNC_GRID; S.nblk[k] = std::min(n, S.maxGrid[k]); S.tuned[k] = 1; }
+    }
+    const int nbMax = std::max(std::max(S.maxGrid[0], S.maxGrid[1]), 16);
     if ((st = devAlloc(&S.partial, 4 * (size_t)nbMax))) return st;
     if ((st = devAlloc(&S.bar, 4))) return st;
     CK(cudaMemset(S.bar, 0, 4 * sizeof(unsigned)));
+    CK(cudaEventCreate(&S.evA));
+    CK(cudaEventCreate(&S.evB));
     return GBFV_OK;
+}
+
+// algorithmic bytes of one persistent solve launch (see gbfv.h)
+double solveBytes(const SolverData& S, int iters, int factor, int s)
+{
+    const double N = S.N, b = S.b, d = S.dim, Sl = S.nslot, bb = b * b;
+    double B = 5.0 * N * b * s;  // rhs read, x r v p initialised
+    if (factor) B += N * (Sl * bb + (d + 1) * bb) * s + 4.0 * N * d;
+    B += (double)iters * (N * (2 * Sl * bb + 4 * d * bb + 2 * bb) * s + 4.0 * N * (2 * Sl + 4 * d) + 30.0 * N * b * s);
+    return B;
 }
 
 void freeSolver(SolverData& S)
@@ -138,6 +169,8 @@ void freeSolver(SolverData& S)
     cudaFree(S.rref);
     cudaFree(S.partial);
     cudaFree(S.bar);
+    if (S.evA) cudaEventDestroy(S.evA);
+    if (S.evB) cudaEventDestroy(S.evB);
 }
 
 
@@ -173,6 +206,15 @@ struct gbfv_ctx {
     cudaEvent_t ev[6];
     double phaseMs[4] = {0, 0, 0, 0};
     int lastIterations = 0, lastRefinements = 0;
+    // snapshot
+    double* xSave = nullptr;
+    int* meaningSave = nullptr;
+    int* switchedSave = nullptr;
+    // linearization statistics
+    cudaEvent_t evL0 = nullptr, evL1 = nullptr;
+    int linPending = 0;
+    double linMs = 0, linBytes = 0, linBytesPer = 0;
+    int64_t linLaunches = 0;
 };
 
 struct gbfv_linsolver {
@@ -234,9 +276,9 @@ void buildOrder(int N, const std::vector<std::vector<int>>& lower, std::vector<i
 
 // solver-precision iteration; returns status and fills iterations
 template <class T>
-int runKrylov(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hst, const T* A, T* FL, T* FD,
-              const T* rhs, T* const* vec, int factor, double redTol, double absTol, double maxRes,
-              int maxIter, int nblocks, int& iters)
+int runKrylovCfg(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hst, const T* A, T* FL, T* FD,
+                 const T* rhs, T* const* vec, int factor, double redTol, double absTol, double maxRes,
+                 int maxIter, int mode, int nblocks, int& iters, float* msOut, bool stats)
 {
     KArgs<T> a;
     a.N = S.N;
@@ -266,18 +308,86 @@ int runKrylov(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hst,
     a.maxRes = maxRes;
     a.maxIter = maxIter;
     a.factor = factor;
+    {
+        int maxW = 0;
+        for (size_t l = 0; l + 1 < S.levPtr.size(); ++l) maxW = std::max(maxW, S.levPtr[l + 1] - S.levPtr[l]);
+        a.dsmem = (mode == SYNC_CLUSTER && maxW <= nblocks * clusterThreads<T>() && !getenv("GBFV_NO_DSMEM")) ? 1 : 0;
+    }
     int rs;
     if ((rs = resetStatus(stream, st))) return rs;
     CK(cudaMemsetAsync(S.bar, 0, 4 * sizeof(unsigned), stream));
-    const int ls = launchBicgstab<T>(a, S.b, nblocks, stream);
+    cudaEventRecord(S.evA, stream);
+    const int ls = launchBicgstab<T>(a, S.b, mode, nblocks, stream);
     if (ls != GBFV_OK) {
         setError(std::string("cooperative launch failed: ") + cudaGetErrorString(cudaGetLastError()));
         return ls;
     }
+    cudaEventRecord(S.evB, stream);
     if ((rs = syncStatus(stream, st, hst))) return rs;
     iters = hst->iterations;
+    {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, S.evA, S.evB);
+        if (msOut) *msOut = ms;
+        if (stats) {
+            S.statMs += ms;
+            S.statLaunches++;
+            S.statIters += iters;
+            S.statFactor += factor;
+            S.statBytes += solveBytes(S, iters, factor, (int)sizeof(T));
+        }
+    }
     if (hst->code) return hst->code;
     return hst->converged ? GBFV_OK : GBFV_ERR_NOT_CONVERGED;
+}
+
+// Autotuner: time a factorization + 12 iterations of every candidate launch
+// configuration on the system at hand and keep the fastest.
+template <class T>
+void tuneSolver(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hst, const T* A, T* FL, T* FD,
+                const T* rhs, T* const* vec)
+{
+    const int k = sizeof(T) == 4 ? 1 : 0;
+    if (S.tuned[k]) return;
+    S.tuned[k] = 1;
+    struct Cand { int mode, nb; };
+    std::vector<Cand> cands;
+    for (int c = 1; c <= S.maxCluster[k]; c *= 2) cands.push_back({SYNC_CLUSTER, c});
+    int dev = 0, nsm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (S.N > 4 * 4096) {
+        cands.push_back({SYNC_GRID, std::min(nsm, S.maxGrid[k])});
+        cands.push_back({SYNC_GRID, std::min(2 * nsm, S.maxGrid[k])});
+    }
+    double best = 1e300;
+    Cand pick = {S.mode[k], S.nblk[k]};
+    int idx = 0;
+    for (const Cand& c : cands) {
+        int it = 0;
+        float ms = 0;
+        const int rs = runKrylovCfg<T>(S, stream, st, hst, A, FL, FD, rhs, vec, 1, 0.0, 0.0, 1e300, 12, c.mode,
+                                       c.nb, it, &ms, false);
+        if (rs != GBFV_OK && rs != GBFV_ERR_NOT_CONVERGED) {
+            cudaGetLastError();
+            continue;
+        }
+        if (idx < 16) S.tuneMs[k][idx++] = ms;
+        if (ms < best) { best = ms; pick = c; }
+    }
+    S.mode[k] = pick.mode;
+    S.nblk[k] = pick.nb;
+}
+
+template <class T>
+int runKrylov(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hst, const T* A, T* FL, T* FD,
+              const T* rhs, T* const* vec, int factor, double redTol, double absTol, double maxRes,
+              int maxIter, int& iters)
+{
+    const int k = sizeof(T) == 4 ? 1 : 0;
+    if (!S.tuned[k]) tuneSolver<T>(S, stream, st, hst, A, FL, FD, rhs, vec);
+    return runKrylovCfg<T>(S, stream, st, hst, A, FL, FD, rhs, vec, factor, redTol, absTol, maxRes, maxIter,
+                           S.mode[k], S.nblk[k], iters, nullptr, true);
 }
 
 double absTolOf(const gbfv_params& p)
@@ -290,8 +400,7 @@ int solvePlain(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hst
                const double* rhs, const gbfv_params& prm, int& iters)
 {
     return runKrylov<double>(S, stream, st, hst, A, S.FL64, S.FD64, rhs, S.v64, 1, prm.linear_tolerance,
-                             absTolOf(prm), prm.linear_max_error, prm.linear_max_iterations, S.nblocks64,
-                             iters);
+                             absTolOf(prm), prm.linear_max_error, prm.linear_max_iterations, iters);
 }
 
 // FP32 BiCGStab + FP32 ILU0 under FP64 iterative refinement (mixed form):
@@ -330,8 +439,7 @@ int solveMixed(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hst
         int it = 0;
         float* vec[6] = {S.v32[1], S.v32[2], S.v32[3], S.v32[4], S.v32[5], S.v32[6]};
         const int ks = runKrylov<float>(S, stream, st, hst, S.A32, S.FL32, S.FD32, S.v32[0], vec, ref == 0,
-                                        innerTol, 0.0, prm.linear_max_error * resErr0 / resErr,
-                                        prm.linear_max_iterations, S.nblocks32, it);
+                                        innerTol, 0.0, prm.linear_max_error, prm.linear_max_iterations, it);
         iters += it;
         refinements++;
         if (ks != GBFV_OK && ks != GBFV_ERR_NOT_CONVERGED) return ks;
@@ -766,6 +874,20 @@ static int createImpl(gbfv_ctx* C, const gbfv_problem* P)
     if ((st = devAlloc(&C->st, 1))) return st;
     CK(cudaMallocHost((void**)&C->hst, sizeof(DevStatus)));
     CK(cudaMemset(C->st, 0, sizeof(DevStatus)));
+    if ((st = devAlloc(&C->xSave, nb)) || (st = devAlloc(&C->meaningSave, (size_t)N)) ||
+        (st = devAlloc(&C->switchedSave, (size_t)N)))
+        return st;
+    CK(cudaEventCreate(&C->evL0));
+    CK(cudaEventCreate(&C->evL1));
+    // algorithmic bytes per cell of the IQ + assembly passes
+    {
+        const double s8 = 8.0;
+        const double iqv = (b == 2 ? 6 : 11), iqd = (b == 2 ? 12 : 30), iqs = b * (b + 1);
+        const double k1 = b * s8 + 8 + 4 + (b == 3 ? 4 : 0) + (iqv + iqd + iqs) * s8;
+        const double k2 = (iqv + iqd + iqs) * s8 + ndir * (4 + 5 * s8) + 8 + 4 + b * s8 + b * s8 +
+                          nslot * b * b * s8;
+        C->linBytesPer = N * (k1 + k2);
+    }
     return GBFV_OK;
 }
 
@@ -808,6 +930,11 @@ int gbfv_destroy(gbfv_ctx* C)
     cudaFree(C->jval);
     freeSolver(C->S);
     cudaFree(C->st);
+    cudaFree(C->xSave);
+    cudaFree(C->meaningSave);
+    cudaFree(C->switchedSave);
+    if (C->evL0) cudaEventDestroy(C->evL0);
+    if (C->evL1) cudaEventDestroy(C->evL1);
     if (C->hst) cudaFreeHost(C->hst);
     if (C->stream) {
         for (auto& e : C->ev) cudaEventDestroy(e);
@@ -881,12 +1008,28 @@ int gbfv_set_newton_iteration(gbfv_ctx* C, int it)
     return GBFV_OK;
 }
 
+static void collectLinStats(gbfv_ctx* C)
+{
+    if (!C->linPending) return;
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, C->evL0, C->evL1) == cudaSuccess) {
+        C->linMs += ms;
+        C->linLaunches += 2;
+        C->linBytes += C->linBytesPer;
+    }
+    C->linPending = 0;
+}
+
 static int linearizeImpl(gbfv_ctx* C)
 {
+    collectLinStats(C);
     launchApplyConstraints(C->mesh, C->x, C->xOld, C->meaning, C->meaningOld, C->stream);
+    cudaEventRecord(C->evL0, C->stream);
     launchIq(C->mesh, C->dphys, C->x, C->meaning, C->iq, C->stream);
     launchAssemble(C->mesh, C->dphys, C->iq, C->storageOld, C->newtonIter == 0, C->dt, C->residual, C->jval,
                    C->stream);
+    cudaEventRecord(C->evL1, C->stream);
+    C->linPending = 1;
     CK(cudaGetLastError());
     return GBFV_OK;
 }
@@ -1020,6 +1163,74 @@ int gbfv_newton_update(gbfv_ctx* C, int* switched)
     int st = updateImpl(C, switched);
     if (st) return st;
     CK(cudaStreamSynchronize(C->stream));
+    return GBFV_OK;
+}
+
+void* gbfv_stream(gbfv_ctx* C) { return C ? (void*)C->stream : nullptr; }
+
+int gbfv_save_state(gbfv_ctx* C)
+{
+    if (!C) return GBFV_ERR_ARG;
+    CK(cudaMemcpyAsync(C->xSave, C->x, sizeof(double) * C->N * C->b, cudaMemcpyDeviceToDevice, C->stream));
+    CK(cudaMemcpyAsync(C->meaningSave, C->meaning, sizeof(int) * C->N, cudaMemcpyDeviceToDevice, C->stream));
+    CK(cudaMemcpyAsync(C->switchedSave, C->wasSwitched, sizeof(int) * C->N, cudaMemcpyDeviceToDevice, C->stream));
+    CK(cudaStreamSynchronize(C->stream));
+    return GBFV_OK;
+}
+
+int gbfv_restore_state(gbfv_ctx* C)
+{
+    if (!C) return GBFV_ERR_ARG;
+    const size_t nb = sizeof(double) * C->N * C->b;
+    CK(cudaMemcpyAsync(C->x, C->xSave, nb, cudaMemcpyDeviceToDevice, C->stream));
+    CK(cudaMemcpyAsync(C->xOld, C->xSave, nb, cudaMemcpyDeviceToDevice, C->stream));
+    CK(cudaMemcpyAsync(C->meaning, C->meaningSave, sizeof(int) * C->N, cudaMemcpyDeviceToDevice, C->stream));
+    CK(cudaMemcpyAsync(C->meaningOld, C->meaningSave, sizeof(int) * C->N, cudaMemcpyDeviceToDevice, C->stream));
+    CK(cudaMemcpyAsync(C->wasSwitched, C->switchedSave, sizeof(int) * C->N, cudaMemcpyDeviceToDevice, C->stream));
+    return GBFV_OK;
+}
+
+int gbfv_get_kernel_stats(const gbfv_ctx* Cc, gbfv_kernel_stats* out)
+{
+    if (!Cc || !out) return GBFV_ERR_ARG;
+    gbfv_ctx* C = const_cast<gbfv_ctx*>(Cc);
+    cudaStreamSynchronize(C->stream);
+    collectLinStats(C);
+    out->solve_ms = C->S.statMs;
+    out->solve_launches = C->S.statLaunches;
+    out->solve_iterations = C->S.statIters;
+    out->solve_factorizations = C->S.statFactor;
+    out->solve_bytes = C->S.statBytes;
+    out->linearize_ms = C->linMs;
+    out->linearize_launches = C->linLaunches;
+    out->linearize_bytes = C->linBytes;
+    return GBFV_OK;
+}
+
+int gbfv_solver_config(const gbfv_ctx* C, int precision, int* mode, int* blocks, double* tuneMs, int* nt)
+{
+    if (!C) return GBFV_ERR_ARG;
+    const int k = precision == GBFV_PREC_MIXED ? 1 : 0;
+    if (mode) *mode = C->S.mode[k];
+    if (blocks) *blocks = C->S.nblk[k];
+    int n = 0;
+    for (int i = 0; i < 16; ++i)
+        if (C->S.tuneMs[k][i] > 0) n = i + 1;
+    if (tuneMs)
+        for (int i = 0; i < n; ++i) tuneMs[i] = C->S.tuneMs[k][i];
+    if (nt) *nt = n;
+    return GBFV_OK;
+}
+
+int gbfv_reset_kernel_stats(gbfv_ctx* C)
+{
+    if (!C) return GBFV_ERR_ARG;
+    cudaStreamSynchronize(C->stream);
+    C->linPending = 0;
+    C->linMs = C->linBytes = 0;
+    C->linLaunches = 0;
+    C->S.statMs = C->S.statBytes = 0;
+    C->S.statLaunches = C->S.statIters = C->S.statFactor = 0;
     return GBFV_OK;
 }
 

@@ -24,9 +24,37 @@
 #include "gbfv_internal.cuh"
 #include "solver.cuh"
 
+#include <cooperative_groups.h>
+namespace cg = cooperative_groups;
+
 namespace gbfv {
 
 #define GB_TIMEOUT_CYCLES 4000000000LL
+
+// loads of data written inside the kernel by other blocks go to L2 directly
+// (ld.global.cg), so no block can hit a stale line in its own L1
+__device__ __forceinline__ float ldcg(const float* p) { return __ldcg(p); }
+__device__ __forceinline__ double ldcg(const double* p) { return __ldcg(p); }
+
+// The set of blocks that cooperate on one system: the whole grid
+// (cooperative launch, software barrier) or one thread-block cluster
+// (hardware cluster barrier).
+template <int MODE>
+struct Team {
+    int rank, nblk;
+    __device__ Team()
+    {
+        if (MODE == SYNC_CLUSTER) {
+            cg::cluster_group c = cg::this_cluster();
+            rank = (int)c.block_rank();
+            nblk = (int)c.num_blocks();
+        }
+        else {
+            rank = blockIdx.x;
+            nblk = gridDim.x;
+        }
+    }
+};
 
 __device__ __forceinline__ bool gridBarrier(const GridSync& g)
 {
@@ -63,11 +91,20 @@ __device__ __forceinline__ bool gridBarrier(const GridSync& g)
     return sOk != 0;
 }
 
-template <class T> __device__ __forceinline__ T ld(const T* p) { return *p; }
+template <int MODE>
+__device__ __forceinline__ bool teamSync(const GridSync& g)
+{
+    if (MODE == SYNC_CLUSTER) {
+        cg::this_cluster().sync();
+        return true;
+    }
+    return gridBarrier(g);
+}
 
-// block reduction of NV sums (or maxima) into partial[k*gridDim + block]
-template <int NV>
-__device__ __forceinline__ void blockPartials(double (&v)[NV], const bool (&isMax)[NV], double* partial)
+// block reduction of NV sums (or maxima) into partial[k*nblk + rank]
+template <int NV, int MODE>
+__device__ __forceinline__ void blockPartials(double (&v)[NV], const bool (&isMax)[NV], double* partial,
+                                              const Team<MODE>& tm)
 {
     __shared__ double sred[NV][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -85,19 +122,20 @@ __device__ __forceinline__ void blockPartials(double (&v)[NV], const bool (&isMa
         const int nw = blockDim.x >> 5;
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
-            double t = lane < nw ? sred[k][lane] : (isMax[k] ? 0.0 : 0.0);
+            double t = lane < nw ? sred[k][lane] : 0.0;
             for (int o = 16; o > 0; o >>= 1) {
                 const double u = __shfl_down_sync(0xffffffffu, t, o);
                 t = isMax[k] ? fmax(t, u) : t + u;
             }
-            if (lane == 0) partial[k * gridDim.x + blockIdx.x] = t;
+            if (lane == 0) __stcg(&partial[k * tm.nblk + tm.rank], t);
         }
     }
 }
 
-// after a barrier: every block combines the partials in the same order
-template <int NV>
-__device__ __forceinline__ void allCombine(const double* partial, const bool (&isMax)[NV], double (&out)[NV])
+// after a team barrier: every block combines the partials in the same order
+template <int NV, int MODE>
+__device__ __forceinline__ void allCombine(const double* partial, const bool (&isMax)[NV], double (&out)[NV],
+                                           const Team<MODE>& tm)
 {
     __shared__ double sres[NV];
     if (threadIdx.x < 32) {
@@ -105,8 +143,8 @@ __device__ __forceinline__ void allCombine(const double* partial, const bool (&i
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
             double t = 0.0;
-            for (int i = lane; i < (int)gridDim.x; i += 32) {
-                const double u = *(volatile const double*)&partial[k * gridDim.x + i];
+            for (int i = lane; i < tm.nblk; i += 32) {
+                const double u = ldcg(&partial[k * tm.nblk + i]);
                 t = isMax[k] ? fmax(t, u) : t + u;
             }
             for (int o = 16; o > 0; o >>= 1) {
@@ -163,10 +201,10 @@ __device__ __forceinline__ bool invertBlock(const T (&A)[B * B], T (&R)[B * B])
 }
 
 // --------------------------------------------------------- phases ---------
-template <class T, int B>
-__device__ bool phaseFactor(const KArgs<T>& a)
+template <class T, int B, int MODE>
+__device__ bool phaseFactor(const KArgs<T>& a, const Team<MODE>& tm)
 {
-    const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
+    const int gt = tm.rank * blockDim.x + threadIdx.x, gs = tm.nblk * blockDim.x;
     const int dim = a.dim, ld = a.ldN;
     for (int l = 0; l < a.numLev; ++l) {
         const int i0 = a.levPtr[l], i1 = a.levPtr[l + 1];
@@ -179,7 +217,7 @@ __device__ bool phaseFactor(const KArgs<T>& a)
                 T As[B * B], Dk[B * B], L[B * B], U[B * B];
                 ldBlock<T, B>(a.A, s, ld, i, As);
 #pragma unroll
-                for (int e = 0; e < B * B; ++e) Dk[e] = a.FD[e * ld + k];
+                for (int e = 0; e < B * B; ++e) Dk[e] = ldcg(&a.FD[e * ld + k]);
 #pragma unroll
                 for (int r = 0; r < B; ++r)
 #pragma unroll
@@ -211,17 +249,18 @@ __device__ bool phaseFactor(const KArgs<T>& a)
 #pragma unroll
             for (int e = 0; e < B * B; ++e) a.FD[e * ld + i] = R[e];
         }
-        if (!gridBarrier(a.gs)) return false;
+        if (!teamSync<MODE>(a.gs)) return false;
     }
     return true;
 }
 
-// forward sweep: y = L^-1 d.  With fuse != 0 the right-hand side is the
-// BiCGStab direction p = r + (-beta)(omega v - p), formed and stored here.
-template <class T, int B>
-__device__ bool sweepLower(const KArgs<T>& a, const T* d, T* y, bool fuseP, T beta, T omega)
+// forward sweep: y = L^-1 d.  With fuseP the right-hand side is the BiCGStab
+// direction p = r + (-beta)(omega v - p), formed and stored here.
+template <class T, int B, int MODE>
+__device__ bool sweepLower(const KArgs<T>& a, const T* d, T* y, bool fuseP, T beta, T omega,
+                           const Team<MODE>& tm)
 {
-    const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
+    const int gt = tm.rank * blockDim.x + threadIdx.x, gs = tm.nblk * blockDim.x;
     const int dim = a.dim, ld = a.ldN;
     for (int l = 0; l < a.numLev; ++l) {
         const int i0 = a.levPtr[l], i1 = a.levPtr[l + 1];
@@ -230,11 +269,11 @@ __device__ bool sweepLower(const KArgs<T>& a, const T* d, T* y, bool fuseP, T be
             if (fuseP) {
 #pragma unroll
                 for (int e = 0; e < B; ++e) {
-                    T tmp = a.v[i * B + e];
+                    T tmp = ldcg(&a.v[i * B + e]);
                     tmp *= omega;
-                    tmp -= a.p[i * B + e];
+                    tmp -= ldcg(&a.p[i * B + e]);
                     tmp *= -beta;
-                    T pe = a.r[i * B + e];
+                    T pe = ldcg(&a.r[i * B + e]);
                     pe += tmp;
                     a.p[i * B + e] = pe;
                     acc[e] = pe;
@@ -242,45 +281,45 @@ __device__ bool sweepLower(const KArgs<T>& a, const T* d, T* y, bool fuseP, T be
             }
             else {
 #pragma unroll
-                for (int e = 0; e < B; ++e) acc[e] = d[i * B + e];
+                for (int e = 0; e < B; ++e) acc[e] = ldcg(&d[i * B + e]);
             }
             for (int s = 0; s < dim; ++s) {
                 const int k = a.col[s * ld + i];
                 if (k < 0) continue;
                 T yk[B];
 #pragma unroll
-                for (int e = 0; e < B; ++e) yk[e] = y[k * B + e];
+                for (int e = 0; e < B; ++e) yk[e] = ldcg(&y[k * B + e]);
 #pragma unroll
                 for (int r = 0; r < B; ++r)
 #pragma unroll
-                    for (int c = 0; c < B; ++c) acc[r] -= a.FL[(s * B * B + r * B + c) * ld + i] * yk[c];
+                    for (int c = 0; c < B; ++c) acc[r] -= ldcg(&a.FL[(s * B * B + r * B + c) * ld + i]) * yk[c];
             }
 #pragma unroll
             for (int e = 0; e < B; ++e) y[i * B + e] = acc[e];
         }
-        if (!gridBarrier(a.gs)) return false;
+        if (!teamSync<MODE>(a.gs)) return false;
     }
     return true;
 }
 
 // backward sweep in place: y = D^-1 (y - U y)
-template <class T, int B>
-__device__ bool sweepUpper(const KArgs<T>& a, T* y)
+template <class T, int B, int MODE>
+__device__ bool sweepUpper(const KArgs<T>& a, T* y, const Team<MODE>& tm)
 {
-    const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
+    const int gt = tm.rank * blockDim.x + threadIdx.x, gs = tm.nblk * blockDim.x;
     const int dim = a.dim, ld = a.ldN;
     for (int l = a.numLev - 1; l >= 0; --l) {
         const int i0 = a.levPtr[l], i1 = a.levPtr[l + 1];
         for (int i = i0 + gt; i < i1; i += gs) {
             T acc[B];
 #pragma unroll
-            for (int e = 0; e < B; ++e) acc[e] = y[i * B + e];
+            for (int e = 0; e < B; ++e) acc[e] = ldcg(&y[i * B + e]);
             for (int s = 2 * dim; s > dim; --s) {
                 const int k = a.col[s * ld + i];
                 if (k < 0) continue;
                 T yk[B];
 #pragma unroll
-                for (int e = 0; e < B; ++e) yk[e] = y[k * B + e];
+                for (int e = 0; e < B; ++e) yk[e] = ldcg(&y[k * B + e]);
 #pragma unroll
                 for (int r = 0; r < B; ++r)
 #pragma unroll
@@ -291,18 +330,170 @@ __device__ bool sweepUpper(const KArgs<T>& a, T* y)
             for (int r = 0; r < B; ++r) {
                 T t = T(0);
 #pragma unroll
-                for (int c = 0; c < B; ++c) t += a.FD[(r * B + c) * ld + i] * acc[c];
+                for (int c = 0; c < B; ++c) t += ldcg(&a.FD[(r * B + c) * ld + i]) * acc[c];
                 out[r] = t;
             }
 #pragma unroll
             for (int e = 0; e < B; ++e) y[i * B + e] = out[e];
         }
-        if (!gridBarrier(a.gs)) return false;
+        if (!teamSync<MODE>(a.gs)) return false;
     }
     return true;
 }
 
-// out = A in for the rows of this thread; returns the row values
+// ---------------------------------------------- cluster / DSMEM sweeps ---
+// One row per thread: row levPtr[l] + (rank*NT + tid).  Each block keeps the
+// results of the level it just computed in shared memory; the next level reads
+// its (structured-grid: all) dependencies from the previous level through
+// distributed shared memory instead of L2.  The cluster barrier is split:
+// after a level is stored the block arrives, loads the next level's matrix
+// blocks and column indices (which do not depend on the sweep), then waits.
+__device__ __forceinline__ void clusterArrive() { asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory"); }
+__device__ __forceinline__ void clusterWait() { asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory"); }
+
+template <class T, int B, int NT>
+__device__ __forceinline__ void readDep(const T* y, int k, int prevLo, int prevHi, T (*buf)[NT * B], int pb,
+                                        T (&yk)[B])
+{
+    if (k >= prevLo && k < prevHi) {
+        const int t = k - prevLo;
+        const T* rb = cg::this_cluster().map_shared_rank(&buf[pb][0], t / NT);
+#pragma unroll
+        for (int e = 0; e < B; ++e) yk[e] = rb[(t % NT) * B + e];
+    }
+    else {
+#pragma unroll
+        for (int e = 0; e < B; ++e) yk[e] = ldcg(&y[k * B + e]);
+    }
+}
+
+template <class T, int B, int NT>
+__device__ __noinline__ void sweepLowerDs(const KArgs<T>& a, const T* d, T* y, bool fuseP, T beta, T omega,
+                             const Team<SYNC_CLUSTER>& tm, T (*buf)[NT * B])
+{
+    const int tid = threadIdx.x, gt = tm.rank * NT + tid;
+    const int dim = a.dim, ld = a.ldN;
+    int kc[3];
+    T Lb[3][B * B];
+    auto load = [&](int l) {
+        const int i = __ldg(&a.levPtr[l]) + gt;
+        const bool act = i < __ldg(&a.levPtr[l + 1]);
+#pragma unroll
+        for (int s = 0; s < 3; ++s) {
+            kc[s] = (act && s < dim) ? __ldg(&a.col[s * ld + i]) : -1;
+            if (kc[s] >= 0)
+#pragma unroll
+                for (int e = 0; e < B * B; ++e) Lb[s][e] = ldcg(&a.FL[(s * B * B + e) * ld + i]);
+        }
+    };
+    load(0);
+    for (int l = 0; l < a.numLev; ++l) {
+        const int i0 = __ldg(&a.levPtr[l]), i1 = __ldg(&a.levPtr[l + 1]);
+        const int prevLo = l > 0 ? __ldg(&a.levPtr[l - 1]) : 0;
+        const int i = i0 + gt;
+        if (i < i1) {
+            T acc[B];
+            if (fuseP) {
+#pragma unroll
+                for (int e = 0; e < B; ++e) {
+                    T tmp = ldcg(&a.v[i * B + e]);
+                    tmp *= omega;
+                    tmp -= ldcg(&a.p[i * B + e]);
+                    tmp *= -beta;
+                    T pe = ldcg(&a.r[i * B + e]);
+                    pe += tmp;
+                    a.p[i * B + e] = pe;
+                    acc[e] = pe;
+                }
+            }
+            else {
+#pragma unroll
+                for (int e = 0; e < B; ++e) acc[e] = ldcg(&d[i * B + e]);
+            }
+#pragma unroll
+            for (int s = 0; s < 3; ++s) {
+                if (kc[s] < 0) continue;
+                T yk[B];
+                readDep<T, B, NT>(y, kc[s], prevLo, i0, buf, (l - 1) & 1, yk);
+#pragma unroll
+                for (int r = 0; r < B; ++r)
+#pragma unroll
+                    for (int c = 0; c < B; ++c) acc[r] -= Lb[s][r * B + c] * yk[c];
+            }
+#pragma unroll
+            for (int e = 0; e < B; ++e) {
+                y[i * B + e] = acc[e];
+                buf[l & 1][tid * B + e] = acc[e];
+            }
+        }
+        clusterArrive();
+        if (l + 1 < a.numLev) load(l + 1);
+        clusterWait();
+    }
+}
+
+template <class T, int B, int NT>
+__device__ __noinline__ void sweepUpperDs(const KArgs<T>& a, T* y, const Team<SYNC_CLUSTER>& tm, T (*buf)[NT * B])
+{
+    const int tid = threadIdx.x, gt = tm.rank * NT + tid;
+    const int dim = a.dim, ld = a.ldN;
+    int kc[3];
+    T Ub[3][B * B];
+    T Db[B * B];
+    auto load = [&](int l) {
+        const int i = __ldg(&a.levPtr[l]) + gt;
+        const bool act = i < __ldg(&a.levPtr[l + 1]);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const int s = 2 * dim - q;  // descending column order
+            kc[q] = (act && q < dim) ? __ldg(&a.col[s * ld + i]) : -1;
+            if (kc[q] >= 0)
+#pragma unroll
+                for (int e = 0; e < B * B; ++e) Ub[q][e] = a.A[(s * B * B + e) * ld + i];
+        }
+        if (act)
+#pragma unroll
+            for (int e = 0; e < B * B; ++e) Db[e] = ldcg(&a.FD[e * ld + i]);
+    };
+    load(a.numLev - 1);
+    for (int l = a.numLev - 1; l >= 0; --l) {
+        const int i0 = __ldg(&a.levPtr[l]), i1 = __ldg(&a.levPtr[l + 1]);
+        const int nextHi = (l + 1 < a.numLev) ? __ldg(&a.levPtr[l + 2]) : i1;
+        const int i = i0 + gt;
+        if (i < i1) {
+            T acc[B];
+#pragma unroll
+            for (int e = 0; e < B; ++e) acc[e] = ldcg(&y[i * B + e]);
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                if (kc[q] < 0) continue;
+                T yk[B];
+                readDep<T, B, NT>(y, kc[q], i1, nextHi, buf, (l + 1) & 1, yk);
+#pragma unroll
+                for (int r = 0; r < B; ++r)
+#pragma unroll
+                    for (int c = 0; c < B; ++c) acc[r] -= Ub[q][r * B + c] * yk[c];
+            }
+            T out[B];
+#pragma unroll
+            for (int r = 0; r < B; ++r) {
+                T t = T(0);
+#pragma unroll
+                for (int c = 0; c < B; ++c) t += Db[r * B + c] * acc[c];
+                out[r] = t;
+            }
+#pragma unroll
+            for (int e = 0; e < B; ++e) {
+                y[i * B + e] = out[e];
+                buf[l & 1][tid * B + e] = out[e];
+            }
+        }
+        clusterArrive();
+        if (l > 0) load(l - 1);
+        clusterWait();
+    }
+}
+
 template <class T, int B>
 __device__ __forceinline__ void spmvRow(const KArgs<T>& a, const T* in, int i, T (&acc)[B])
 {
@@ -314,7 +505,7 @@ __device__ __forceinline__ void spmvRow(const KArgs<T>& a, const T* in, int i, T
         if (k < 0) continue;
         T xk[B];
 #pragma unroll
-        for (int e = 0; e < B; ++e) xk[e] = in[k * B + e];
+        for (int e = 0; e < B; ++e) xk[e] = ldcg(&in[k * B + e]);
 #pragma unroll
         for (int r = 0; r < B; ++r)
 #pragma unroll
@@ -322,18 +513,19 @@ __device__ __forceinline__ void spmvRow(const KArgs<T>& a, const T* in, int i, T
     }
 }
 
-template <class T, int B>
-__global__ void __launch_bounds__(SOLVER_THREADS) kBicgstab(KArgs<T> a)
+template <class T, int B, int MODE, int NT>
+__global__ void __launch_bounds__(NT, 1) kBicgstab(KArgs<T> a)
 {
-    const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
+    const Team<MODE> tm;
+    const int gt = tm.rank * blockDim.x + threadIdx.x, gs = tm.nblk * blockDim.x;
     const int N = a.N;
+    __shared__ T lbuf[2][MODE == SYNC_CLUSTER ? NT * B : 1];
     const double eps = 2.2250738585072014e-308 * 1e10;  // numeric_limits<double>::min()*1e10
     if (a.factor) {
-        if (!phaseFactor<T, B>(a)) goto timeout;
+        if (!phaseFactor<T, B, MODE>(a, tm)) goto timeout;
         if (*(volatile int*)&a.st->code == GBFV_ERR_SINGULAR) goto done;
     }
     {
-        // x = 0, r = b, v = p = 0; initial criterion on max|r|
         double mx[1] = {0.0};
         const bool isMax1[1] = {true};
         for (int i = gt; i < N; i += gs)
@@ -346,10 +538,10 @@ __global__ void __launch_bounds__(SOLVER_THREADS) kBicgstab(KArgs<T> a)
                 a.p[i * B + e] = T(0);
                 mx[0] = fmax(mx[0], fabs((double)bi));
             }
-        blockPartials<1>(mx, isMax1, a.partial);
-        if (!gridBarrier(a.gs)) goto timeout;
+        blockPartials<1, MODE>(mx, isMax1, a.partial, tm);
+        if (!teamSync<MODE>(a.gs)) goto timeout;
         double tot[1];
-        allCombine<1>(a.partial, isMax1, tot);
+        allCombine<1, MODE>(a.partial, isMax1, tot, tm);
         double resErr = fmax(tot[0], eps);
         const double initErr = resErr;
         auto converged = [&](double re) { return re / fmax(1e-20, initErr) <= a.redTol || re <= a.absTol; };
@@ -358,26 +550,28 @@ __global__ void __launch_bounds__(SOLVER_THREADS) kBicgstab(KArgs<T> a)
             goto done;
         }
         double rho = 1.0, alpha = 1.0, omega = 1.0;
-        // first rho_i = (b, r) = (b, b)
         {
+            // partials of the next reduction go to the second half of the buffer so the
+            // combine above cannot race with them
             double dd[1] = {0.0};
             const bool isSum1[1] = {false};
             for (int i = gt; i < N; i += gs) {
                 double t = 0.0;
 #pragma unroll
-                for (int e = 0; e < B; ++e) t += (double)(a.rhs[i * B + e] * a.r[i * B + e]);
+                for (int e = 0; e < B; ++e) t += (double)(a.rhs[i * B + e] * a.rhs[i * B + e]);
                 dd[0] += t;
             }
-            blockPartials<1>(dd, isSum1, a.partial);
-            if (!gridBarrier(a.gs)) goto timeout;
+            blockPartials<1, MODE>(dd, isSum1, a.partial + 2 * tm.nblk, tm);
+            if (!teamSync<MODE>(a.gs)) goto timeout;
         }
         int it = 0;
+        int buf = 1;  // which half of the partial buffer holds (b, r)
         for (; it < a.maxIter; ++it) {
             double rho_i;
             {
                 const bool isSum1[1] = {false};
                 double tot1[1];
-                allCombine<1>(a.partial, isSum1, tot1);
+                allCombine<1, MODE>(a.partial + 2 * tm.nblk * buf, isSum1, tot1, tm);
                 rho_i = tot1[0];
             }
             if (fabs(rho) <= eps || fabs(omega) <= eps) {
@@ -386,10 +580,20 @@ __global__ void __launch_bounds__(SOLVER_THREADS) kBicgstab(KArgs<T> a)
             }
             const double beta = (rho_i / rho) * (alpha / omega);
             rho = rho_i;
-            // y = K^-1 p with p formed inside the forward sweep
-            if (!sweepLower<T, B>(a, nullptr, a.y, true, (T)beta, (T)omega)) goto timeout;
-            if (!sweepUpper<T, B>(a, a.y)) goto timeout;
-            // v = A y ; denom = (b, v)
+            if constexpr (MODE == SYNC_CLUSTER) {
+                if (a.dsmem) {
+                    sweepLowerDs<T, B, NT>(a, nullptr, a.y, true, (T)beta, (T)omega, tm, lbuf);
+                    sweepUpperDs<T, B, NT>(a, a.y, tm, lbuf);
+                }
+                else {
+                    sweepLower<T, B, MODE>(a, nullptr, a.y, true, (T)beta, (T)omega, tm);
+                    sweepUpper<T, B, MODE>(a, a.y, tm);
+                }
+            }
+            else {
+                if (!sweepLower<T, B, MODE>(a, nullptr, a.y, true, (T)beta, (T)omega, tm)) goto timeout;
+                if (!sweepUpper<T, B, MODE>(a, a.y, tm)) goto timeout;
+            }
             {
                 double dd[1] = {0.0};
                 const bool isSum1[1] = {false};
@@ -404,10 +608,11 @@ __global__ void __launch_bounds__(SOLVER_THREADS) kBicgstab(KArgs<T> a)
                     }
                     dd[0] += t;
                 }
-                blockPartials<1>(dd, isSum1, a.partial);
-                if (!gridBarrier(a.gs)) goto timeout;
+                buf ^= 1;
+                blockPartials<1, MODE>(dd, isSum1, a.partial + 2 * tm.nblk * buf, tm);
+                if (!teamSync<MODE>(a.gs)) goto timeout;
                 double tot1[1];
-                allCombine<1>(a.partial, isSum1, tot1);
+                allCombine<1, MODE>(a.partial + 2 * tm.nblk * buf, isSum1, tot1, tm);
                 const double denom = tot1[0];
                 if (fabs(denom) <= eps) {
                     if (gt == 0) a.st->code = GBFV_ERR_BREAKDOWN;
@@ -419,7 +624,6 @@ __global__ void __launch_bounds__(SOLVER_THREADS) kBicgstab(KArgs<T> a)
                     break;
                 }
             }
-            // h = x + alpha y ; s = r - alpha v ; criterion(h, y, s)
             {
                 double red[2] = {0.0, 0.0};
                 const bool kinds[2] = {true, true};
@@ -427,32 +631,44 @@ __global__ void __launch_bounds__(SOLVER_THREADS) kBicgstab(KArgs<T> a)
                 for (int i = gt; i < N; i += gs)
 #pragma unroll
                     for (int e = 0; e < B; ++e) {
-                        T tmp = a.y[i * B + e];
+                        T tmp = ldcg(&a.y[i * B + e]);
                         if (tmp != T(0)) red[1] = 1.0;
                         tmp *= ta;
-                        tmp += a.x[i * B + e];
+                        tmp += ldcg(&a.x[i * B + e]);
                         a.x[i * B + e] = tmp;
-                        tmp = a.v[i * B + e];
+                        tmp = ldcg(&a.v[i * B + e]);
                         tmp *= ta;
-                        const T si = a.r[i * B + e] - tmp;
+                        const T si = ldcg(&a.r[i * B + e]) - tmp;
                         a.r[i * B + e] = si;
                         red[0] = fmax(red[0], fabs((double)si));
                     }
-                blockPartials<2>(red, kinds, a.partial);
-                if (!gridBarrier(a.gs)) goto timeout;
+                buf ^= 1;
+                blockPartials<2, MODE>(red, kinds, a.partial + 2 * tm.nblk * buf, tm);
+                if (!teamSync<MODE>(a.gs)) goto timeout;
                 double tot2[2];
-                allCombine<2>(a.partial, kinds, tot2);
+                allCombine<2, MODE>(a.partial + 2 * tm.nblk * buf, kinds, tot2, tm);
                 resErr = tot2[0];
                 const bool stag = tot2[1] == 0.0;
                 if (converged(resErr)) {
-                    if (gt == 0) { a.st->converged = 1; }
+                    if (gt == 0) a.st->converged = 1;
                     break;
                 }
                 if (stag || resErr > a.maxRes) break;
             }
-            // z = K^-1 s ; t = A z (t aliases y)
-            if (!sweepLower<T, B>(a, a.r, a.z, false, T(0), T(0))) goto timeout;
-            if (!sweepUpper<T, B>(a, a.z)) goto timeout;
+            if constexpr (MODE == SYNC_CLUSTER) {
+                if (a.dsmem) {
+                    sweepLowerDs<T, B, NT>(a, a.r, a.z, false, T(0), T(0), tm, lbuf);
+                    sweepUpperDs<T, B, NT>(a, a.z, tm, lbuf);
+                }
+                else {
+                    sweepLower<T, B, MODE>(a, a.r, a.z, false, T(0), T(0), tm);
+                    sweepUpper<T, B, MODE>(a, a.z, tm);
+                }
+            }
+            else {
+                if (!sweepLower<T, B, MODE>(a, a.r, a.z, false, T(0), T(0), tm)) goto timeout;
+                if (!sweepUpper<T, B, MODE>(a, a.z, tm)) goto timeout;
+            }
             {
                 double dd[2] = {0.0, 0.0};
                 const bool isSum2[2] = {false, false};
@@ -464,15 +680,16 @@ __global__ void __launch_bounds__(SOLVER_THREADS) kBicgstab(KArgs<T> a)
                     for (int e = 0; e < B; ++e) {
                         a.y[i * B + e] = acc[e];
                         t0 += (double)(acc[e] * acc[e]);
-                        t1 += (double)(acc[e] * a.r[i * B + e]);
+                        t1 += (double)(acc[e] * ldcg(&a.r[i * B + e]));
                     }
                     dd[0] += t0;
                     dd[1] += t1;
                 }
-                blockPartials<2>(dd, isSum2, a.partial);
-                if (!gridBarrier(a.gs)) goto timeout;
+                buf ^= 1;
+                blockPartials<2, MODE>(dd, isSum2, a.partial + 2 * tm.nblk * buf, tm);
+                if (!teamSync<MODE>(a.gs)) goto timeout;
                 double tot2[2];
-                allCombine<2>(a.partial, isSum2, tot2);
+                allCombine<2, MODE>(a.partial + 2 * tm.nblk * buf, isSum2, tot2, tm);
                 const double denom = tot2[0];
                 if (fabs(denom) <= eps) {
                     if (gt == 0) a.st->code = GBFV_ERR_BREAKDOWN;
@@ -484,7 +701,6 @@ __global__ void __launch_bounds__(SOLVER_THREADS) kBicgstab(KArgs<T> a)
                     break;
                 }
             }
-            // x += omega z ; criterion(x, z, s) ; r = s - omega t ; next (b, r)
             {
                 double red[2] = {0.0, 0.0};
                 const bool kinds[2] = {false, true};
@@ -493,31 +709,23 @@ __global__ void __launch_bounds__(SOLVER_THREADS) kBicgstab(KArgs<T> a)
                     double t = 0.0;
 #pragma unroll
                     for (int e = 0; e < B; ++e) {
-                        const T zi = a.z[i * B + e];
+                        const T zi = ldcg(&a.z[i * B + e]);
                         if (zi != T(0)) red[1] = 1.0;
-                        a.x[i * B + e] += to * zi;
-                        const T ri = a.r[i * B + e] + (-to) * a.y[i * B + e];
+                        a.x[i * B + e] = ldcg(&a.x[i * B + e]) + to * zi;
+                        const T ri = ldcg(&a.r[i * B + e]) + (-to) * ldcg(&a.y[i * B + e]);
                         a.r[i * B + e] = ri;
                         t += (double)(a.rhs[i * B + e] * ri);
                     }
                     red[0] += t;
                 }
-                blockPartials<2>(red, kinds, a.partial);
-                if (!gridBarrier(a.gs)) goto timeout;
-                // the stagnation flag of z decides failure; the residual of
-                // this check is still s, which was not converged
-                __shared__ double sflag;
-                if (threadIdx.x < 32) {
-                    double t = 0.0;
-                    for (int i = threadIdx.x; i < (int)gridDim.x; i += 32)
-                        t = fmax(t, *(volatile const double*)&a.partial[1 * gridDim.x + i]);
-                    for (int o = 16; o > 0; o >>= 1) t = fmax(t, __shfl_xor_sync(0xffffffffu, t, o));
-                    if (threadIdx.x == 0) sflag = t;
-                }
-                __syncthreads();
-                const bool stag = sflag == 0.0;
-                __syncthreads();
-                if (stag) break;
+                buf ^= 1;
+                blockPartials<2, MODE>(red, kinds, a.partial + 2 * tm.nblk * buf, tm);
+                if (!teamSync<MODE>(a.gs)) goto timeout;
+                // z == 0 everywhere is stagnation (the residual of this check is still s)
+                const bool kindMax[2] = {false, true};
+                double tot2[2];
+                allCombine<2, MODE>(a.partial + 2 * tm.nblk * buf, kindMax, tot2, tm);
+                if (tot2[1] == 0.0) break;
             }
         }
         if (gt == 0) {
@@ -533,17 +741,48 @@ timeout:
 }
 
 // ------------------------------------------------- launch + FP64 helpers --
-template <class T>
-int launchBicgstab(const KArgs<T>& a, int b, int nblocks, cudaStream_t s)
+template <class T, int B, int MODE, int NT>
+static int launchOne(const KArgs<T>& a, int nblocks, cudaStream_t s)
 {
     void* args[] = {(void*)&a};
     cudaError_t e;
-    if (b == 2)
-        e = cudaLaunchCooperativeKernel((void*)kBicgstab<T, 2>, nblocks, SOLVER_THREADS, args, 0, s);
-    else
-        e = cudaLaunchCooperativeKernel((void*)kBicgstab<T, 3>, nblocks, SOLVER_THREADS, args, 0, s);
+    auto fn = kBicgstab<T, B, MODE, NT>;
+    if (MODE == SYNC_GRID) {
+        e = cudaLaunchCooperativeKernel((void*)fn, nblocks, NT, args, 0, s);
+    }
+    else {
+        static bool attrSet = false;
+        if (!attrSet) {
+            cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+            attrSet = true;
+        }
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(nblocks, 1, 1);
+        cfg.blockDim = dim3(NT, 1, 1);
+        cfg.dynamicSmemBytes = 0;
+        cfg.stream = s;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = nblocks;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        e = cudaLaunchKernelEx(&cfg, fn, a);
+    }
     countLaunch();
     return e == cudaSuccess ? GBFV_OK : GBFV_ERR_CUDA;
+}
+
+template <class T>
+int launchBicgstab(const KArgs<T>& a, int b, int mode, int nblocks, cudaStream_t s)
+{
+    constexpr int NTC = clusterThreads<T>();
+    if (mode == SYNC_GRID)
+        return b == 2 ? launchOne<T, 2, SYNC_GRID, SOLVER_THREADS>(a, nblocks, s)
+                      : launchOne<T, 3, SYNC_GRID, SOLVER_THREADS>(a, nblocks, s);
+    return b == 2 ? launchOne<T, 2, SYNC_CLUSTER, NTC>(a, nblocks, s)
+                  : launchOne<T, 3, SYNC_CLUSTER, NTC>(a, nblocks, s);
 }
 
 template <class T>
@@ -553,16 +792,45 @@ int maxSolverBlocks(int b)
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     if (b == 2)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kBicgstab<T, 2>, SOLVER_THREADS, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kBicgstab<T, 2, SYNC_GRID, SOLVER_THREADS>,
+                                                      SOLVER_THREADS, 0);
     else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kBicgstab<T, 3>, SOLVER_THREADS, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kBicgstab<T, 3, SYNC_GRID, SOLVER_THREADS>,
+                                                      SOLVER_THREADS, 0);
     return nsm * (occ > 0 ? occ : 1);
 }
 
-template int launchBicgstab<double>(const KArgs<double>&, int, int, cudaStream_t);
-template int launchBicgstab<float>(const KArgs<float>&, int, int, cudaStream_t);
+template <class T>
+int maxClusterBlocks(int b)
+{
+    constexpr int NTC = clusterThreads<T>();
+    int n = 0;
+    cudaLaunchConfig_t cfg = {};
+    cfg.blockDim = dim3(NTC, 1, 1);
+    cfg.gridDim = dim3(16, 1, 1);
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = 16;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    const void* fn = b == 2 ? (const void*)kBicgstab<T, 2, SYNC_CLUSTER, NTC>
+                            : (const void*)kBicgstab<T, 3, SYNC_CLUSTER, NTC>;
+    cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (cudaOccupancyMaxPotentialClusterSize(&n, fn, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        n = 8;
+    }
+    return n > 0 ? n : 1;
+}
+
+template int launchBicgstab<double>(const KArgs<double>&, int, int, int, cudaStream_t);
+template int launchBicgstab<float>(const KArgs<float>&, int, int, int, cudaStream_t);
 template int maxSolverBlocks<double>(int);
 template int maxSolverBlocks<float>(int);
+template int maxClusterBlocks<double>(int);
+template int maxClusterBlocks<float>(int);
 
 // A32 = (float) A64 over all slots
 __global__ void kCastMatrix(const double* __restrict__ src, float* __restrict__ dst, long n)

@@ -7,7 +7,10 @@
 
 namespace gbfv {
 
-constexpr int SOLVER_THREADS = 256;
+constexpr int SOLVER_THREADS = 256;   // blocks of the cooperative-grid variant
+template <class T> constexpr int clusterThreads() { return sizeof(T) == 4 ? 512 : 256; }  // cluster variant
+constexpr int SYNC_GRID = 0;     // whole grid, cooperative launch, software barrier
+constexpr int SYNC_CLUSTER = 1;  // one thread-block cluster, hardware barrier
 
 // software grid barrier state (device memory, zero-initialised)
 struct GridSync {
@@ -27,16 +30,19 @@ struct KArgs {
     T* FD;              // inverted pivots [e*ldN + p]
     const T* rhs;       // [p*b + e]
     T *x, *r, *p, *v, *y, *z;
-    double* partial;    // [4*gridDim]
+    double* partial;    // [4*blocks]: two halves, alternately used
     GridSync gs;
     DevStatus* st;
     double redTol, absTol, maxRes;
     int maxIter;
     int factor;         // factorize before iterating
+    int dsmem;          // cluster mode: every level fits one row per thread, so the
+                        // previous level's results are exchanged in distributed shared memory
 };
 
-template <class T> int launchBicgstab(const KArgs<T>& a, int b, int nblocks, cudaStream_t s);
+template <class T> int launchBicgstab(const KArgs<T>& a, int b, int mode, int nblocks, cudaStream_t s);
 template <class T> int maxSolverBlocks(int b);
+template <class T> int maxClusterBlocks(int b);
 void launchCastMatrix(const double* src, float* dst, long n, cudaStream_t s);
 void launchAccumulate(int n, double* x, const float* d, cudaStream_t s);
 void launchResidual64(int N, int ld, int nslot, int b, const int* col, const double* A, const double* rhs,

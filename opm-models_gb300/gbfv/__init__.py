@@ -121,6 +121,30 @@ class Context:
                                             _d(sdt), _i(sn), _i(sl), C.byref(tl))
         return st, sdt, sn, sl, tl.value
 
+    def stream(self):
+        return self.lib.gbfv_stream(self.h)
+
+    def save_state(self):
+        capi.check(self.lib.gbfv_save_state(self.h), "gbfv_save_state")
+
+    def restore_state(self):
+        capi.check(self.lib.gbfv_restore_state(self.h), "gbfv_restore_state")
+
+    def kernel_stats(self):
+        k = capi.KernelStats()
+        capi.check(self.lib.gbfv_get_kernel_stats(self.h, C.byref(k)), "gbfv_get_kernel_stats")
+        return {f: getattr(k, f) for f, _ in capi.KernelStats._fields_}
+
+    def solver_config(self, precision):
+        mode, nb, nt = C.c_int(), C.c_int(), C.c_int()
+        ms = np.zeros(16)
+        self.lib.gbfv_solver_config(self.h, precision, C.byref(mode), C.byref(nb), _d(ms), C.byref(nt))
+        return {"mode": "cluster" if mode.value == 1 else "grid", "blocks": nb.value,
+                "tune_ms": ms[:nt.value].tolist()}
+
+    def reset_kernel_stats(self):
+        self.lib.gbfv_reset_kernel_stats(self.h)
+
     def phase_times(self):
         a = np.zeros(4)
         self.lib.gbfv_phase_times(self.h, _d(a))

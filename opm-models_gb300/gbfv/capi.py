@@ -94,6 +94,15 @@ class Params(C.Structure):
     ]
 
 
+class KernelStats(C.Structure):
+    _fields_ = [
+        ("solve_ms", C.c_double), ("solve_launches", C.c_int64), ("solve_iterations", C.c_int64),
+        ("solve_factorizations", C.c_int64), ("solve_bytes", C.c_double),
+        ("linearize_ms", C.c_double), ("linearize_launches", C.c_int64),
+        ("linearize_bytes", C.c_double),
+    ]
+
+
 class NewtonReport(C.Structure):
     _fields_ = [
         ("converged", C.c_int32), ("iterations", C.c_int32), ("linear_iterations", C.c_int32),
@@ -181,6 +190,13 @@ def load():
         "gbfv_kernel_launches": (C.c_int64, []),
         "gbfv_last_error": (C.c_char_p, []),
         "gbfv_phase_times": (C.c_int, [vp, dp]),
+        "gbfv_stream": (vp, [vp]),
+        "gbfv_save_state": (C.c_int, [vp]),
+        "gbfv_restore_state": (C.c_int, [vp]),
+        "gbfv_get_kernel_stats": (C.c_int, [vp, C.POINTER(KernelStats)]),
+        "gbfv_reset_kernel_stats": (C.c_int, [vp]),
+        "gbfv_solver_config": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), dp,
+                                         C.POINTER(C.c_int)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
