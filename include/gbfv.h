@@ -332,6 +332,11 @@ int gbfv_get_kernel_stats(const gbfv_ctx* ctx, gbfv_kernel_stats* out);
 int gbfv_solver_config(const gbfv_ctx* ctx, int precision, int* mode, int* blocks,
                        double* tune_ms, int* num_tuned);
 int gbfv_reset_kernel_stats(gbfv_ctx* ctx);
+/* with GBFV_PROFILE set in the environment at creation: nanoseconds spent
+ * by the persistent solve kernel per phase since the last call ([0]
+ * factorization, [1] forward sweeps, [2] backward sweeps, [3] SpMV + dots,
+ * [4] vector updates + norms, [5] remaining); zeros otherwise            */
+int gbfv_solver_phase_ns(gbfv_ctx* ctx, unsigned long long* ns8);
 
 #ifdef __cplusplus
 }

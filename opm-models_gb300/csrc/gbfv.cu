@@ -96,6 +96,13 @@ struct SolverData {
     int maxGrid[2] = {1, 1};
     int maxCluster[2] = {1, 1};
     double tuneMs[2][16] = {};
+    int adjacentLevels = 0;  // every dependency is exactly one level away
+    std::vector<int> colHost;   // [s*ldN + p] host copy of the ELL columns
+    int* pushL = nullptr;       // push targets for the current (C, G, NT)
+    int* pushU = nullptr;
+    int* levVals = nullptr;     // values each block receives per level and sweep
+    int pushKey[3] = {0, 0, 0};
+    unsigned long long* prof = nullptr;  // per-phase timers of the solve kernel (GBFV_PROFILE=1)
     // cumulative statistics of the persistent solve kernel
     cudaEvent_t evA = nullptr, evB = nullptr;
     double statMs = 0, statBytes = 0;
@@ -141,6 +148,10 @@ int allocSolver(SolverData& S, int maxBlocksOverride = 0)
     CK(cudaMemset(S.bar, 0, 4 * sizeof(unsigned)));
     CK(cudaEventCreate(&S.evA));
     CK(cudaEventCreate(&S.evB));
+    if (getenv("GBFV_PROFILE")) {
+        CK(cudaMalloc((void**)&S.prof, 8 * sizeof(unsigned long long)));
+        CK(cudaMemset(S.prof, 0, 8 * sizeof(unsigned long long)));
+    }
     return GBFV_OK;
 }
 
@@ -169,6 +180,10 @@ void freeSolver(SolverData& S)
     cudaFree(S.rref);
     cudaFree(S.partial);
     cudaFree(S.bar);
+    if (S.prof) cudaFree(S.prof);
+    cudaFree(S.pushL);
+    cudaFree(S.pushU);
+    cudaFree(S.levVals);
     if (S.evA) cudaEventDestroy(S.evA);
     if (S.evB) cudaEventDestroy(S.evB);
 }
@@ -274,6 +289,68 @@ void buildOrder(int N, const std::vector<std::vector<int>>& lower, std::vector<i
     }
 }
 
+// Push targets of the cluster sweeps for cluster size C, G level groups and
+// NT threads per block: for each row and each neighbour in the dependency
+// direction, the consumer's block and the offset of its slot (see
+// SweepMap in solver.cu).
+int buildPushTargets(SolverData& S, int C, int G, int NT)
+{
+    if (S.pushKey[0] == C && S.pushKey[1] == G && S.pushKey[2] == NT && S.pushL) return GBFV_OK;
+    const int N = S.N, ld = S.ldN, dim = S.dim, B = S.b, NG = NT / G;
+    std::vector<int> lev(N);
+    for (size_t l = 0; l + 1 < S.levPtr.size(); ++l)
+        for (int p = S.levPtr[l]; p < S.levPtr[l + 1]; ++p) lev[p] = (int)l;
+    auto target = [&](int j, int slot) {
+        const int t = j - S.levPtr[lev[j]];
+        const int w = t >> 5;
+        const int owner = w % C;
+        const int uu = ((w / C) << 5) | (t & 31);
+        const int cslot = (lev[j] % G) * NG + uu;
+        return (owner << 24) | ((cslot * 3 + slot) * B);
+    };
+    const int nl = (int)S.levPtr.size() - 1;
+    std::vector<int> hL((size_t)3 * ld, -1), hU((size_t)3 * ld, -1), hV((size_t)C * nl * 2, 0);
+    for (int p = 0; p < N; ++p) {
+        const int owner = ((p - S.levPtr[lev[p]]) >> 5) % C;
+        for (int q = 0; q < dim; ++q) {
+            const int ju = S.colHost[(size_t)(dim + 1 + q) * ld + p];  // upper neighbour +q
+            if (ju >= 0) {
+                hL[(size_t)q * ld + p] = target(ju, dim - 1 - q);
+                hV[((size_t)owner * nl + lev[p]) * 2 + 1] += B;  // p receives ju in the backward sweep
+            }
+            const int jl = S.colHost[(size_t)q * ld + p];  // lower neighbour in slot q
+            if (jl >= 0) {
+                hU[(size_t)q * ld + p] = target(jl, q);
+                hV[((size_t)owner * nl + lev[p]) * 2] += B;  // p receives jl in the forward sweep
+            }
+        }
+    }
+    cudaFree(S.pushL);
+    cudaFree(S.pushU);
+    cudaFree(S.levVals);
+    S.pushL = S.pushU = S.levVals = nullptr;
+    int st;
+    if ((st = upload(&S.pushL, hL)) || (st = upload(&S.pushU, hU)) || (st = upload(&S.levVals, hV))) return st;
+    S.pushKey[0] = C;
+    S.pushKey[1] = G;
+    S.pushKey[2] = NT;
+    return GBFV_OK;
+}
+
+// 1 if every lower dependency of a row sits exactly one level below it
+int adjacentLevels(const std::vector<std::vector<int>>& lower, const std::vector<int>& perm,
+                   const std::vector<int>& levPtr)
+{
+    const int N = (int)perm.size();
+    std::vector<int> lev(N);
+    for (size_t l = 0; l + 1 < levPtr.size(); ++l)
+        for (int p = levPtr[l]; p < levPtr[l + 1]; ++p) lev[p] = (int)l;
+    for (int i = 0; i < N; ++i)
+        for (int k : lower[i])
+            if (lev[perm[k]] != lev[perm[i]] - 1) return 0;
+    return 1;
+}
+
 // solver-precision iteration; returns status and fills iterations
 template <class T>
 int runKrylovCfg(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hst, const T* A, T* FL, T* FD,
@@ -308,10 +385,25 @@ int runKrylovCfg(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* h
     a.maxRes = maxRes;
     a.maxIter = maxIter;
     a.factor = factor;
+    a.prof = S.prof;
     {
         int maxW = 0;
         for (size_t l = 0; l + 1 < S.levPtr.size(); ++l) maxW = std::max(maxW, S.levPtr[l + 1] - S.levPtr[l]);
-        a.dsmem = (mode == SYNC_CLUSTER && maxW <= nblocks * clusterThreads<T>() && !getenv("GBFV_NO_DSMEM")) ? 1 : 0;
+        a.dsmem = (mode == SYNC_CLUSTER && S.adjacentLevels && maxW <= nblocks * clusterThreads<T>() &&
+                   (int)S.levPtr.size() - 1 <= MAX_PUSH_LEVELS && !getenv("GBFV_NO_DSMEM")) ? 1 : 0;
+        // as many level groups as fit (each group must cover the widest level)
+        a.grp = 1;
+        for (int g : {8, 4, 2})
+            if (maxW <= nblocks * (clusterThreads<T>() / g)) { a.grp = g; break; }
+        if (const char* e = getenv("GBFV_GROUPS")) a.grp = std::max(1, std::min(a.grp, atoi(e)));
+        a.pushL = a.pushU = a.levVals = nullptr;
+        if (a.dsmem) {
+            const int ps = buildPushTargets(S, nblocks, a.grp, clusterThreads<T>());
+            if (ps) return ps;
+            a.pushL = S.pushL;
+            a.pushU = S.pushU;
+            a.levVals = S.levVals;
+        }
     }
     int rs;
     if ((rs = resetStatus(stream, st))) return rs;
@@ -869,6 +961,8 @@ static int createImpl(gbfv_ctx* C, const gbfv_problem* P)
     S.nslot = nslot;
     S.ldN = ld;
     S.levPtr = levPtr;
+    S.adjacentLevels = adjacentLevels(lower, C->perm, levPtr);
+    S.colHost = hCol;
     if ((st = upload(&S.col, hCol)) || (st = upload(&S.levPtrD, levPtr))) return st;
     if ((st = allocSolver(S))) return st;
     if ((st = devAlloc(&C->st, 1))) return st;
@@ -1222,6 +1316,16 @@ int gbfv_solver_config(const gbfv_ctx* C, int precision, int* mode, int* blocks,
     return GBFV_OK;
 }
 
+int gbfv_solver_phase_ns(gbfv_ctx* C, unsigned long long* ns8)
+{
+    if (!C || !ns8) return GBFV_ERR_ARG;
+    if (!C->S.prof) { std::memset(ns8, 0, 8 * sizeof(unsigned long long)); return GBFV_OK; }
+    CK(cudaStreamSynchronize(C->stream));
+    CK(cudaMemcpy(ns8, C->S.prof, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    CK(cudaMemset(C->S.prof, 0, 8 * sizeof(unsigned long long)));
+    return GBFV_OK;
+}
+
 int gbfv_reset_kernel_stats(gbfv_ctx* C)
 {
     if (!C) return GBFV_ERR_ARG;
@@ -1450,6 +1554,8 @@ gbfv_linsolver* gbfv_linsolver_create(int n, int b, const int32_t* rowPtr, const
     S.nslot = nslot;
     S.ldN = ld;
     S.levPtr = levPtr;
+    S.adjacentLevels = adjacentLevels(lower, L->perm, levPtr);
+    S.colHost = hCol;
     int st;
     if ((st = upload(&S.col, hCol)) || (st = upload(&S.levPtrD, levPtr)) || (st = allocSolver(S)))
         return fail(L, st);

@@ -36,6 +36,31 @@ namespace gbfv {
 __device__ __forceinline__ float ldcg(const float* p) { return __ldcg(p); }
 __device__ __forceinline__ double ldcg(const double* p) { return __ldcg(p); }
 
+__device__ __forceinline__ unsigned long long gtimer()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+// phase timer (only block 0 / thread 0 writes; no contention)
+struct PhaseClock {
+    unsigned long long* prof;
+    unsigned long long t;
+    bool on;
+    __device__ PhaseClock(unsigned long long* p, int gt) : prof(p), t(0), on(p != nullptr && gt == 0)
+    {
+        if (on) t = gtimer();
+    }
+    __device__ __forceinline__ void tick(int k)
+    {
+        if (!on) return;
+        const unsigned long long n = gtimer();
+        prof[k] += n - t;
+        t = n;
+    }
+};
+
 // The set of blocks that cooperate on one system: the whole grid
 // (cooperative launch, software barrier) or one thread-block cluster
 // (hardware cluster barrier).
@@ -351,147 +376,412 @@ __device__ bool sweepUpper(const KArgs<T>& a, T* y, const Team<MODE>& tm)
 __device__ __forceinline__ void clusterArrive() { asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory"); }
 __device__ __forceinline__ void clusterWait() { asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory"); }
 
-template <class T, int B, int NT>
-__device__ __forceinline__ void readDep(const T* y, int k, int prevLo, int prevHi, T (*buf)[NT * B], int pb,
-                                        T (&yk)[B])
+// ----------------------------------------------- cluster push sweeps ----
+// Rows of a level are dealt to the blocks of the cluster a warp at a time:
+// position t belongs to block (t/32) % C, local slot ((t/32)/C)*32 + t%32,
+// so each warp reads 32 consecutive rows.  A row's dependencies (its lower
+// neighbours in the forward sweep, upper ones in the backward sweep) are all
+// in the previous level.  Each producer pushes its result into the
+// consumers' shared memory with st.async; the bytes are counted on the
+// consumer block's mbarrier (expect_tx / complete_tx), which the consumer
+// waits on -- a point-to-point handshake, no release barrier per level.  A
+// relaxed cluster barrier per level only keeps the blocks within one level of
+// each other, so two dependency buffers suffice.
+__device__ __forceinline__ void clusterArriveRelaxed()
 {
-    if (k >= prevLo && k < prevHi) {
-        const int t = k - prevLo;
-        const T* rb = cg::this_cluster().map_shared_rank(&buf[pb][0], t / NT);
+    asm volatile("barrier.cluster.arrive.relaxed.aligned;\n" ::: "memory");
+}
+__device__ __forceinline__ unsigned smemAddr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ unsigned mapaRank(unsigned a, int rank)
+{
+    unsigned r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ void mbarInit(unsigned a, int count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbarArriveTx(unsigned a, unsigned bytes)
+{
+    // relaxed: arming publishes nothing, so it must not wait for this thread's
+    // loads in flight (a release arrive would)
+    asm volatile("mbarrier.arrive.expect_tx.relaxed.cta.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes) : "memory");
+}
+// bounded wait for the phase with the given parity, relaxed: orders nothing,
+// so it does not wait for this thread's loads in flight; false on timeout
+__device__ __forceinline__ bool mbarWaitRelaxed(unsigned a, unsigned parity)
+{
+    for (int spin = 0; spin < (1 << 16); ++spin) {
+        unsigned done;
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.relaxed.cta.shared::cta.b64 p, [%1], %2; "
+            "selp.u32 %0, 1, 0, p; }"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+// bounded wait (acquire) for the phase with the given parity; false on timeout
+__device__ __forceinline__ bool mbarWait(unsigned a, unsigned parity)
+{
+    for (int spin = 0; spin < (1 << 16); ++spin) {
+        unsigned done;
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; "
+            "selp.u32 %0, 1, 0, p; }"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+__device__ __forceinline__ void stAsync(unsigned dst, float v, unsigned mbar)
+{
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b32 [%0], %1, [%2];" ::"r"(dst),
+                 "r"(__float_as_uint(v)), "r"(mbar)
+                 : "memory");
+}
+__device__ __forceinline__ void stAsync(unsigned dst, double v, unsigned mbar)
+{
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b64 [%0], %1, [%2];" ::"r"(dst),
+                 "l"(__double_as_longlong(v)), "r"(mbar)
+                 : "memory");
+}
+
+// consumer in this block: plain shared store, CTA-scope release, then
+// count the bytes on the local mbarrier
+template <class T, int B>
+__device__ __forceinline__ void pushLocal(T* dst, const T (&v)[B], unsigned mbar)
+{
 #pragma unroll
-        for (int e = 0; e < B; ++e) yk[e] = rb[(t % NT) * B + e];
+    for (int e = 0; e < B; ++e) dst[e] = v[e];
+    asm volatile("fence.acq_rel.cta;" ::: "memory");
+    asm volatile("mbarrier.complete_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"((unsigned)(B * sizeof(T)))
+                 : "memory");
+}
+
+struct PushState {
+    unsigned mb[2];   // shared addresses of the two data mbarriers
+    unsigned ph[2];   // parity of the next phase to wait for
+    unsigned dep;     // shared address of the dependency buffer [2][NT][3][B]
+    unsigned lev;     // shared address of the level-done mbarrier (C arrivals)
+    unsigned levPh;
+    int ok;
+};
+
+// All-to-all level barrier of the cluster without acquire at cluster scope:
+// thread t < C of every block arrives (relaxed) on block t's level-done
+// mbarrier, then every thread waits on its own.  Data ordering is not its job
+// (the st.async transaction counts do that); it only keeps the blocks within
+// one level of each other.
+__device__ __forceinline__ void levelBarrier(PushState& ps, int C, int rank)
+{
+    __syncthreads();
+    const int t = threadIdx.x;
+    if (t < C) {
+        if (t == rank)
+            asm volatile("mbarrier.arrive.relaxed.cta.shared::cta.b64 _, [%0];" ::"r"(ps.lev) : "memory");
+        else
+            asm volatile("mbarrier.arrive.relaxed.cluster.shared::cluster.b64 _, [%0];" ::"r"(mapaRank(ps.lev, t))
+                         : "memory");
+    }
+    if (ps.ok && !mbarWaitRelaxed(ps.lev, ps.levPh)) ps.ok = 0;
+    ps.levPh ^= 1u;
+}
+
+__device__ __forceinline__ void levelSlot(int t, int C, int& owner, int& loc)
+{
+    const int w = t >> 5;
+    owner = w % C;
+    loc = ((w / C) << 5) | (t & 31);
+}
+
+// Level-rotating thread groups: the block's threads form G groups of NT/G;
+// group (l mod G) computes level l.  Right after computing a level a group
+// loads the matrix blocks and right-hand sides of its next level (l + G), so
+// those loads have G-1 levels to complete before they are used.  Every
+// thread takes part in each level's mbarrier phase (idle groups expect zero
+// bytes) and in the relaxed cluster barrier.
+template <class T, int B, int NT>
+struct SweepMap {
+    int C, G, NG, rank, tid, grp, u;
+    __device__ SweepMap(const Team<SYNC_CLUSTER>& tm, int G_) : C(tm.nblk), G(G_), rank(tm.rank)
+    {
+        tid = threadIdx.x;
+        NG = NT / G;
+        grp = tid / NG;
+        u = tid - grp * NG;
+    }
+    // this thread's position inside a level it works on
+    __device__ __forceinline__ int pos() const { return ((((u >> 5) * C) + rank) << 5) | (u & 31); }
+    // block and thread slot of position t of level l
+    __device__ __forceinline__ void slotOf(int t, int l, int& owner, int& cslot) const
+    {
+        const int w = t >> 5;
+        owner = w % C;
+        const int uu = ((w / C) << 5) | (t & 31);
+        cslot = (l % G) * NG + uu;
+    }
+};
+
+// A push target is the consumer block (bits 24..31) and the element offset
+// of the consumer's slot inside one half of the dependency buffer
+// (precomputed on the host for the launch configuration).
+template <class T, int B>
+__device__ __forceinline__ void pushValues(int target, int half, const T (&out)[B], const Team<SYNC_CLUSTER>& tm,
+                                           const T* dep, const PushState& ps, int mbIdx)
+{
+    const int owner = target >> 24;
+    const int off = (target & 0xffffff) + half;
+    if (owner == tm.rank) {
+        pushLocal<T, B>(const_cast<T*>(dep) + off, out, ps.mb[mbIdx]);
     }
     else {
+        const unsigned dst = mapaRank(ps.dep + (unsigned)(off * sizeof(T)), owner);
+        const unsigned mb = mapaRank(ps.mb[mbIdx], owner);
 #pragma unroll
-        for (int e = 0; e < B; ++e) yk[e] = ldcg(&y[k * B + e]);
+        for (int e = 0; e < B; ++e) stAsync(dst + e * (unsigned)sizeof(T), out[e], mb);
     }
 }
 
-template <class T, int B, int NT>
-__device__ __noinline__ void sweepLowerDs(const KArgs<T>& a, const T* d, T* y, bool fuseP, T beta, T omega,
-                             const Team<SYNC_CLUSTER>& tm, T (*buf)[NT * B])
+// Asynchronous global -> shared copies (no registers held, not waited for by
+// barriers or fences); each thread waits for its own with wait_all.
+template <int S>
+__device__ __forceinline__ void cpAsync(unsigned dst, const void* src)
 {
-    const int tid = threadIdx.x, gt = tm.rank * NT + tid;
-    const int dim = a.dim, ld = a.ldN;
-    int kc[3];
-    T Lb[3][B * B];
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(dst), "l"(src), "n"(S) : "memory");
+}
+__device__ __forceinline__ void cpCommit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cpWaitAll() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Shared memory of the push sweeps beyond the dependency buffer: one staging
+// slot per thread for the operands of the next level it computes (field f of
+// thread t at [f*NT + t]), the level pointers and this block's expected bytes
+// per level (forward and backward sweep).
+template <class T, int B, int NT>
+struct PushSmem {
+    static constexpr int NF = 4 * B * B + 3 * B;  // 3 off-diagonal blocks, pivot, 3 vectors
+    static constexpr int NI = 6;                   // 3 neighbour columns, 3 push targets
+    T* st;
+    int* sn;
+    int* lev;    // [numLev + 1]
+    int* nval;   // [2*l + 0/1]: values this block receives at level l (forward/backward)
+    __device__ PushSmem(unsigned char* base, int numLev)
+    {
+        st = reinterpret_cast<T*>(base);
+        sn = reinterpret_cast<int*>(st + NF * NT);
+        lev = sn + NI * NT;
+        nval = lev + numLev + 1;
+    }
+    static constexpr size_t bytes(int numLev)
+    {
+        return sizeof(T) * (size_t)NF * NT + sizeof(int) * ((size_t)NI * NT + 3 * (size_t)numLev + 1);
+    }
+};
+
+// forward sweep y = L^-1 d (fuseP: d is the BiCGStab direction p, formed here).
+// The group that computed the previous level stages the operands of its next
+// level while the current group works, so those copies stay off the current
+// level's critical path.
+template <class T, int B, int NT>
+__device__ __forceinline__ void sweepLowerPush(const KArgs<T>& a, const T* d, T* y, bool fuseP, T beta, T omega,
+                                               const Team<SYNC_CLUSTER>& tm, const T* dep, PushState& ps,
+                                               const PushSmem<T, B, NT>& sm)
+{
+    constexpr int BB = B * B, VB = 4 * BB;
+    const SweepMap<T, B, NT> mp(tm, a.grp);
+    const int dim = a.dim, ld = a.ldN, nl = a.numLev, G = mp.G, tid = mp.tid;
+    const int half = NT * 3 * B;
+    const T* st = sm.st;
+    const int* sn = sm.sn;
+    const unsigned stA = smemAddr(sm.st) + tid * sizeof(T), snA = smemAddr(sm.sn) + tid * sizeof(int);
+    int iCur = -1;
     auto load = [&](int l) {
-        const int i = __ldg(&a.levPtr[l]) + gt;
-        const bool act = i < __ldg(&a.levPtr[l + 1]);
+        iCur = -1;
+        if (l >= nl) return;
+        const int i = sm.lev[l] + mp.pos();
+        if (i >= sm.lev[l + 1]) return;
+        iCur = i;
 #pragma unroll
         for (int s = 0; s < 3; ++s) {
-            kc[s] = (act && s < dim) ? __ldg(&a.col[s * ld + i]) : -1;
-            if (kc[s] >= 0)
+            if (s >= dim) break;
+            cpAsync<4>(snA + (s * NT) * 4, &a.col[s * ld + i]);
+            cpAsync<4>(snA + ((3 + s) * NT) * 4, &a.pushL[s * ld + i]);
 #pragma unroll
-                for (int e = 0; e < B * B; ++e) Lb[s][e] = ldcg(&a.FL[(s * B * B + e) * ld + i]);
+            for (int e = 0; e < BB; ++e)
+                cpAsync<sizeof(T)>(stA + ((s * BB + e) * NT) * sizeof(T), &a.FL[(s * BB + e) * ld + i]);
         }
+        if (fuseP) {
+#pragma unroll
+            for (int e = 0; e < B; ++e) {
+                cpAsync<sizeof(T)>(stA + ((VB + e) * NT) * sizeof(T), &a.v[i * B + e]);
+                cpAsync<sizeof(T)>(stA + ((VB + B + e) * NT) * sizeof(T), &a.p[i * B + e]);
+                cpAsync<sizeof(T)>(stA + ((VB + 2 * B + e) * NT) * sizeof(T), &a.r[i * B + e]);
+            }
+        }
+        else {
+#pragma unroll
+            for (int e = 0; e < B; ++e) cpAsync<sizeof(T)>(stA + ((VB + e) * NT) * sizeof(T), &d[i * B + e]);
+        }
+        cpCommit();
     };
-    load(0);
-    for (int l = 0; l < a.numLev; ++l) {
-        const int i0 = __ldg(&a.levPtr[l]), i1 = __ldg(&a.levPtr[l + 1]);
-        const int prevLo = l > 0 ? __ldg(&a.levPtr[l - 1]) : 0;
-        const int i = i0 + gt;
-        if (i < i1) {
-            T acc[B];
-            if (fuseP) {
+    load(mp.grp);
+    if (tid == 0) mbarArriveTx(ps.mb[0], (unsigned)(sm.nval[0] * sizeof(T)));
+    for (int l = 0; l < nl; ++l) {
+        const int k = l & 1;
+        const bool mine = mp.grp == l % G;
+        if (mine && ps.ok && !mbarWait(ps.mb[k], ps.ph[k])) ps.ok = 0;  // after a timeout: no more waits
+        ps.ph[k] ^= 1u;
+        if (mine) {
+            const int i = iCur;
+            if (i >= 0) {
+                cpWaitAll();
+                T out[B], pv[B];
+                if (fuseP) {
+#pragma unroll
+                    for (int e = 0; e < B; ++e) {
+                        T tmp = st[(VB + e) * NT + tid];
+                        tmp *= omega;
+                        tmp -= st[(VB + B + e) * NT + tid];
+                        tmp *= -beta;
+                        T pe = st[(VB + 2 * B + e) * NT + tid];
+                        pe += tmp;
+                        pv[e] = pe;
+                        out[e] = pe;
+                    }
+                }
+                else {
+#pragma unroll
+                    for (int e = 0; e < B; ++e) out[e] = st[(VB + e) * NT + tid];
+                }
+                const T* md = dep + (k * NT + tid) * 3 * B;
+#pragma unroll
+                for (int s = 0; s < 3; ++s) {
+                    if (s >= dim) break;
+                    if (sn[s * NT + tid] < 0) continue;
+#pragma unroll
+                    for (int r = 0; r < B; ++r)
+#pragma unroll
+                        for (int c = 0; c < B; ++c) out[r] -= st[(s * BB + r * B + c) * NT + tid] * md[s * B + c];
+                }
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    if (q >= dim) break;
+                    const int tg = sn[(3 + q) * NT + tid];
+                    if (tg >= 0) pushValues<T, B>(tg, (k ^ 1) * half, out, tm, dep, ps, k ^ 1);
+                }
 #pragma unroll
                 for (int e = 0; e < B; ++e) {
-                    T tmp = ldcg(&a.v[i * B + e]);
-                    tmp *= omega;
-                    tmp -= ldcg(&a.p[i * B + e]);
-                    tmp *= -beta;
-                    T pe = ldcg(&a.r[i * B + e]);
-                    pe += tmp;
-                    a.p[i * B + e] = pe;
-                    acc[e] = pe;
+                    y[i * B + e] = out[e];
+                    if (fuseP) a.p[i * B + e] = pv[e];
                 }
             }
-            else {
-#pragma unroll
-                for (int e = 0; e < B; ++e) acc[e] = ldcg(&d[i * B + e]);
-            }
-#pragma unroll
-            for (int s = 0; s < 3; ++s) {
-                if (kc[s] < 0) continue;
-                T yk[B];
-                readDep<T, B, NT>(y, kc[s], prevLo, i0, buf, (l - 1) & 1, yk);
-#pragma unroll
-                for (int r = 0; r < B; ++r)
-#pragma unroll
-                    for (int c = 0; c < B; ++c) acc[r] -= Lb[s][r * B + c] * yk[c];
-            }
-#pragma unroll
-            for (int e = 0; e < B; ++e) {
-                y[i * B + e] = acc[e];
-                buf[l & 1][tid * B + e] = acc[e];
-            }
+            if (G == 1) load(l + 1);
         }
-        clusterArrive();
-        if (l + 1 < a.numLev) load(l + 1);
-        clusterWait();
+        else if (G > 1 && l >= 1 && mp.grp == (l - 1) % G) {
+            load(l - 1 + G);
+        }
+        if (tid == 0 && l + 1 < nl) mbarArriveTx(ps.mb[k ^ 1], (unsigned)(sm.nval[2 * (l + 1)] * sizeof(T)));
+        levelBarrier(ps, mp.C, mp.rank);
     }
+    cg::this_cluster().sync();  // publish the global stores to the next phase
 }
 
+// backward sweep in place: y = D^-1 (y - U y)
 template <class T, int B, int NT>
-__device__ __noinline__ void sweepUpperDs(const KArgs<T>& a, T* y, const Team<SYNC_CLUSTER>& tm, T (*buf)[NT * B])
+__device__ __forceinline__ void sweepUpperPush(const KArgs<T>& a, T* y, const Team<SYNC_CLUSTER>& tm, const T* dep,
+                                               PushState& ps, const PushSmem<T, B, NT>& sm)
 {
-    const int tid = threadIdx.x, gt = tm.rank * NT + tid;
-    const int dim = a.dim, ld = a.ldN;
-    int kc[3];
-    T Ub[3][B * B];
-    T Db[B * B];
+    constexpr int BB = B * B, VB = 4 * BB;
+    const SweepMap<T, B, NT> mp(tm, a.grp);
+    const int dim = a.dim, ld = a.ldN, nl = a.numLev, G = mp.G, tid = mp.tid;
+    const int half = NT * 3 * B;
+    const T* st = sm.st;
+    const int* sn = sm.sn;
+    const unsigned stA = smemAddr(sm.st) + tid * sizeof(T), snA = smemAddr(sm.sn) + tid * sizeof(int);
+    int iCur = -1;
     auto load = [&](int l) {
-        const int i = __ldg(&a.levPtr[l]) + gt;
-        const bool act = i < __ldg(&a.levPtr[l + 1]);
+        iCur = -1;
+        if (l < 0) return;
+        const int i = sm.lev[l] + mp.pos();
+        if (i >= sm.lev[l + 1]) return;
+        iCur = i;
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
+            if (q >= dim) break;
             const int s = 2 * dim - q;  // descending column order
-            kc[q] = (act && q < dim) ? __ldg(&a.col[s * ld + i]) : -1;
-            if (kc[q] >= 0)
+            cpAsync<4>(snA + (q * NT) * 4, &a.col[s * ld + i]);
+            cpAsync<4>(snA + ((3 + q) * NT) * 4, &a.pushU[q * ld + i]);
 #pragma unroll
-                for (int e = 0; e < B * B; ++e) Ub[q][e] = a.A[(s * B * B + e) * ld + i];
+            for (int e = 0; e < BB; ++e)
+                cpAsync<sizeof(T)>(stA + ((q * BB + e) * NT) * sizeof(T), &a.A[(s * BB + e) * ld + i]);
         }
-        if (act)
 #pragma unroll
-            for (int e = 0; e < B * B; ++e) Db[e] = ldcg(&a.FD[e * ld + i]);
+        for (int e = 0; e < BB; ++e) cpAsync<sizeof(T)>(stA + ((3 * BB + e) * NT) * sizeof(T), &a.FD[e * ld + i]);
+#pragma unroll
+        for (int e = 0; e < B; ++e) cpAsync<sizeof(T)>(stA + ((VB + e) * NT) * sizeof(T), &y[i * B + e]);
+        cpCommit();
     };
-    load(a.numLev - 1);
-    for (int l = a.numLev - 1; l >= 0; --l) {
-        const int i0 = __ldg(&a.levPtr[l]), i1 = __ldg(&a.levPtr[l + 1]);
-        const int nextHi = (l + 1 < a.numLev) ? __ldg(&a.levPtr[l + 2]) : i1;
-        const int i = i0 + gt;
-        if (i < i1) {
-            T acc[B];
-#pragma unroll
-            for (int e = 0; e < B; ++e) acc[e] = ldcg(&y[i * B + e]);
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                if (kc[q] < 0) continue;
-                T yk[B];
-                readDep<T, B, NT>(y, kc[q], i1, nextHi, buf, (l + 1) & 1, yk);
-#pragma unroll
-                for (int r = 0; r < B; ++r)
-#pragma unroll
-                    for (int c = 0; c < B; ++c) acc[r] -= Ub[q][r * B + c] * yk[c];
-            }
-            T out[B];
-#pragma unroll
-            for (int r = 0; r < B; ++r) {
-                T t = T(0);
-#pragma unroll
-                for (int c = 0; c < B; ++c) t += Db[r * B + c] * acc[c];
-                out[r] = t;
-            }
-#pragma unroll
-            for (int e = 0; e < B; ++e) {
-                y[i * B + e] = out[e];
-                buf[l & 1][tid * B + e] = out[e];
-            }
-        }
-        clusterArrive();
-        if (l > 0) load(l - 1);
-        clusterWait();
+    // group of level l is l % G, also for the descending sweep
+    {
+        int first = -1;
+        for (int l = nl - 1; l >= 0 && l >= nl - G; --l)
+            if (l % G == mp.grp) first = l;
+        load(first);
+        if (tid == 0) mbarArriveTx(ps.mb[(nl - 1) & 1], (unsigned)(sm.nval[2 * (nl - 1) + 1] * sizeof(T)));
     }
+    for (int l = nl - 1; l >= 0; --l) {
+        const int k = l & 1;
+        const bool mine = mp.grp == l % G;
+        if (mine && ps.ok && !mbarWait(ps.mb[k], ps.ph[k])) ps.ok = 0;
+        ps.ph[k] ^= 1u;
+        if (mine) {
+            const int i = iCur;
+            if (i >= 0) {
+                cpWaitAll();
+                T acc[B];
+#pragma unroll
+                for (int e = 0; e < B; ++e) acc[e] = st[(VB + e) * NT + tid];
+                const T* md = dep + (k * NT + tid) * 3 * B;
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    if (q >= dim) break;
+                    if (sn[q * NT + tid] < 0) continue;
+#pragma unroll
+                    for (int r = 0; r < B; ++r)
+#pragma unroll
+                        for (int c = 0; c < B; ++c) acc[r] -= st[(q * BB + r * B + c) * NT + tid] * md[q * B + c];
+                }
+                T out[B];
+#pragma unroll
+                for (int r = 0; r < B; ++r) {
+                    T t = T(0);
+#pragma unroll
+                    for (int c = 0; c < B; ++c) t += st[(3 * BB + r * B + c) * NT + tid] * acc[c];
+                    out[r] = t;
+                }
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    if (q >= dim) break;
+                    const int tg = sn[(3 + q) * NT + tid];
+                    if (tg >= 0) pushValues<T, B>(tg, (k ^ 1) * half, out, tm, dep, ps, k ^ 1);
+                }
+#pragma unroll
+                for (int e = 0; e < B; ++e) y[i * B + e] = out[e];
+            }
+            if (G == 1) load(l - 1);
+        }
+        else if (G > 1 && l <= nl - 2 && mp.grp == (l + 1) % G) {
+            load(l + 1 - G);
+        }
+        if (tid == 0 && l > 0) mbarArriveTx(ps.mb[k ^ 1], (unsigned)(sm.nval[2 * (l - 1) + 1] * sizeof(T)));
+        levelBarrier(ps, mp.C, mp.rank);
+    }
+    cg::this_cluster().sync();
 }
 
 template <class T, int B>
@@ -519,10 +809,37 @@ __global__ void __launch_bounds__(NT, 1) kBicgstab(KArgs<T> a)
     const Team<MODE> tm;
     const int gt = tm.rank * blockDim.x + threadIdx.x, gs = tm.nblk * blockDim.x;
     const int N = a.N;
-    __shared__ T lbuf[2][MODE == SYNC_CLUSTER ? NT * B : 1];
+    __shared__ T dep[MODE == SYNC_CLUSTER ? 2 * NT * 3 * B : 1];
+    __shared__ __align__(8) unsigned long long mbar[3];
+    extern __shared__ __align__(16) unsigned char dynSmem[];
+    PushState ps;
+    ps.ok = 1;
+    const PushSmem<T, B, NT> psm(dynSmem, a.numLev);
+    if constexpr (MODE == SYNC_CLUSTER) {
+        ps.mb[0] = smemAddr(&mbar[0]);
+        ps.mb[1] = smemAddr(&mbar[1]);
+        ps.ph[0] = ps.ph[1] = 0;
+        ps.dep = smemAddr(dep);
+        ps.lev = smemAddr(&mbar[2]);
+        ps.levPh = 0;
+        if (a.dsmem) {
+            for (int j = threadIdx.x; j <= a.numLev; j += NT) psm.lev[j] = a.levPtr[j];
+            for (int j = threadIdx.x; j < 2 * a.numLev; j += NT) psm.nval[j] = a.levVals[tm.rank * 2 * a.numLev + j];
+        }
+        if (a.dsmem && threadIdx.x == 0) {
+            // one arrival per phase (thread 0, carrying the expected bytes)
+            mbarInit(ps.mb[0], 1);
+            mbarInit(ps.mb[1], 1);
+            mbarInit(ps.lev, tm.nblk);
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        cg::this_cluster().sync();
+    }
     const double eps = 2.2250738585072014e-308 * 1e10;  // numeric_limits<double>::min()*1e10
+    PhaseClock pc(a.prof, gt);
     if (a.factor) {
         if (!phaseFactor<T, B, MODE>(a, tm)) goto timeout;
+        pc.tick(0);
         if (*(volatile int*)&a.st->code == GBFV_ERR_SINGULAR) goto done;
     }
     {
@@ -580,10 +897,13 @@ __global__ void __launch_bounds__(NT, 1) kBicgstab(KArgs<T> a)
             }
             const double beta = (rho_i / rho) * (alpha / omega);
             rho = rho_i;
+            pc.tick(5);
             if constexpr (MODE == SYNC_CLUSTER) {
                 if (a.dsmem) {
-                    sweepLowerDs<T, B, NT>(a, nullptr, a.y, true, (T)beta, (T)omega, tm, lbuf);
-                    sweepUpperDs<T, B, NT>(a, a.y, tm, lbuf);
+                    sweepLowerPush<T, B, NT>(a, nullptr, a.y, true, (T)beta, (T)omega, tm, dep, ps, psm);
+                    pc.tick(1);
+                    sweepUpperPush<T, B, NT>(a, a.y, tm, dep, ps, psm);
+                    pc.tick(2);
                 }
                 else {
                     sweepLower<T, B, MODE>(a, nullptr, a.y, true, (T)beta, (T)omega, tm);
@@ -613,6 +933,7 @@ __global__ void __launch_bounds__(NT, 1) kBicgstab(KArgs<T> a)
                 if (!teamSync<MODE>(a.gs)) goto timeout;
                 double tot1[1];
                 allCombine<1, MODE>(a.partial + 2 * tm.nblk * buf, isSum1, tot1, tm);
+                pc.tick(3);
                 const double denom = tot1[0];
                 if (fabs(denom) <= eps) {
                     if (gt == 0) a.st->code = GBFV_ERR_BREAKDOWN;
@@ -655,10 +976,13 @@ __global__ void __launch_bounds__(NT, 1) kBicgstab(KArgs<T> a)
                 }
                 if (stag || resErr > a.maxRes) break;
             }
+            pc.tick(4);
             if constexpr (MODE == SYNC_CLUSTER) {
                 if (a.dsmem) {
-                    sweepLowerDs<T, B, NT>(a, a.r, a.z, false, T(0), T(0), tm, lbuf);
-                    sweepUpperDs<T, B, NT>(a, a.z, tm, lbuf);
+                    sweepLowerPush<T, B, NT>(a, a.r, a.z, false, T(0), T(0), tm, dep, ps, psm);
+                    pc.tick(1);
+                    sweepUpperPush<T, B, NT>(a, a.z, tm, dep, ps, psm);
+                    pc.tick(2);
                 }
                 else {
                     sweepLower<T, B, MODE>(a, a.r, a.z, false, T(0), T(0), tm);
@@ -690,6 +1014,7 @@ __global__ void __launch_bounds__(NT, 1) kBicgstab(KArgs<T> a)
                 if (!teamSync<MODE>(a.gs)) goto timeout;
                 double tot2[2];
                 allCombine<2, MODE>(a.partial + 2 * tm.nblk * buf, isSum2, tot2, tm);
+                pc.tick(3);
                 const double denom = tot2[0];
                 if (fabs(denom) <= eps) {
                     if (gt == 0) a.st->code = GBFV_ERR_BREAKDOWN;
@@ -733,6 +1058,7 @@ __global__ void __launch_bounds__(NT, 1) kBicgstab(KArgs<T> a)
             a.st->resid = resErr;
             a.st->resid0 = initErr;
         }
+        if (!ps.ok) atomicExch(&a.st->code, GBFV_ERR_TIMEOUT);
     }
 done:
     return;
@@ -754,12 +1080,14 @@ static int launchOne(const KArgs<T>& a, int nblocks, cudaStream_t s)
         static bool attrSet = false;
         if (!attrSet) {
             cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+            cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)PushSmem<T, B, NT>::bytes(MAX_PUSH_LEVELS));
             attrSet = true;
         }
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(nblocks, 1, 1);
         cfg.blockDim = dim3(NT, 1, 1);
-        cfg.dynamicSmemBytes = 0;
+        cfg.dynamicSmemBytes = a.dsmem ? PushSmem<T, B, NT>::bytes(a.numLev) : 0;
         cfg.stream = s;
         cudaLaunchAttribute at[1];
         at[0].id = cudaLaunchAttributeClusterDimension;
@@ -817,7 +1145,10 @@ int maxClusterBlocks(int b)
     cfg.numAttrs = 1;
     const void* fn = b == 2 ? (const void*)kBicgstab<T, 2, SYNC_CLUSTER, NTC>
                             : (const void*)kBicgstab<T, 3, SYNC_CLUSTER, NTC>;
+    const size_t dyn = b == 2 ? PushSmem<T, 2, NTC>::bytes(MAX_PUSH_LEVELS) : PushSmem<T, 3, NTC>::bytes(MAX_PUSH_LEVELS);
     cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    cfg.dynamicSmemBytes = dyn;
     if (cudaOccupancyMaxPotentialClusterSize(&n, fn, &cfg) != cudaSuccess) {
         cudaGetLastError();
         n = 8;

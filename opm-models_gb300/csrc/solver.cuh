@@ -9,6 +9,7 @@ namespace gbfv {
 
 constexpr int SOLVER_THREADS = 256;   // blocks of the cooperative-grid variant
 template <class T> constexpr int clusterThreads() { return sizeof(T) == 4 ? 512 : 256; }  // cluster variant
+constexpr int MAX_PUSH_LEVELS = 4096;  // push sweeps keep the level pointers in shared memory
 constexpr int SYNC_GRID = 0;     // whole grid, cooperative launch, software barrier
 constexpr int SYNC_CLUSTER = 1;  // one thread-block cluster, hardware barrier
 
@@ -36,6 +37,12 @@ struct KArgs {
     double redTol, absTol, maxRes;
     int maxIter;
     int factor;         // factorize before iterating
+    unsigned long long* prof;  // optional per-phase nanoseconds (block 0, thread 0): factor,
+                               // L sweep, U sweep, SpMV+dot, update+max, count of iterations
+    int grp;            // push sweeps: number of level-rotating thread groups
+    const int* pushL;   // push sweeps: consumer block/slot of each upper neighbour [q*ldN + p]
+    const int* pushU;   // push sweeps: consumer block/slot of each lower neighbour [q*ldN + p]
+    const int* levVals; // push sweeps: values block r receives at level l, [(r*numLev + l)*2 + fwd/bwd]
     int dsmem;          // cluster mode: every level fits one row per thread, so the
                         // previous level's results are exchanged in distributed shared memory
 };

@@ -195,6 +195,7 @@ def load():
         "gbfv_restore_state": (C.c_int, [vp]),
         "gbfv_get_kernel_stats": (C.c_int, [vp, C.POINTER(KernelStats)]),
         "gbfv_reset_kernel_stats": (C.c_int, [vp]),
+        "gbfv_solver_phase_ns": (C.c_int, [vp, C.POINTER(C.c_uint64)]),
         "gbfv_solver_config": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), dp,
                                          C.POINTER(C.c_int)]),
     }
