@@ -338,6 +338,32 @@ int gbfv_reset_kernel_stats(gbfv_ctx* ctx);
  * [4] vector updates + norms, [5] remaining); zeros otherwise            */
 int gbfv_solver_phase_ns(gbfv_ctx* ctx, unsigned long long* ns8);
 
+/* ------------------------------------------------------------------ */
+/* Allocation-free Newton error.  No counterpart in the reference: its
+ * NewtonMethod computes the same maximum norm on the host
+ * (newtonmethod.hh:572-598, preSolve_).  For callers that hold the
+ * residual in their own device memory and may not allocate device memory
+ * during a step (a host simulator that owns the whole HBM budget through
+ * its own pool allocator): max over cells p with skip[p] == 0 of
+ * |residual[p*num_eq + k]|, the value gbfv_newton_error returns.
+ *   residual  device pointer, num_cells*num_eq doubles (cell-major)
+ *   skip      device pointer to num_cells int32 flags (non-zero: constraint
+ *             or auxiliary cell, left out), or NULL for none
+ *   stream    cudaStream_t to run on (NULL: legacy default stream); the
+ *             call returns after the stream has reached its end
+ * Nothing is allocated: the scratch is a fixed static device array of
+ * GBFV_NOALLOC_MAX_CELLS/256 partial maxima (512 KiB) plus one result word,
+ * and num_cells above GBFV_NOALLOC_MAX_CELLS is rejected with GBFV_ERR_ARG.
+ * No scratch word has to start at zero (each call writes every word it
+ * reads).  The first call on each device looks up the scratch address
+ * (cudaGetSymbolAddress, with that device current) and should come before
+ * any stream capture.  Calls that overlap in time share the scratch and
+ * race: serialize them.  Returns GBFV_ERR_NONFINITE (error = NaN) when a
+ * considered entry is not finite.                                         */
+#define GBFV_NOALLOC_MAX_CELLS (1 << 24)
+int gbfv_newton_error_noalloc(const double* residual, const int32_t* skip, int32_t num_cells,
+                              int32_t num_eq, void* stream, double* error);
+
 #ifdef __cplusplus
 }
 #endif

@@ -23,6 +23,7 @@ UNITS = {
     "linearize.cu": ["-fmad=false"],
     "solver.cu": [],
     "gbfv.cu": [],
+    "noalloc.cu": [],
 }
 
 

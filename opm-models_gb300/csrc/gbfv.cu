@@ -192,6 +192,11 @@ void freeSolver(SolverData& S)
 
 }  // namespace
 
+namespace gbfv {
+// error message for gbfv_last_error from other translation units
+void setLastError(const std::string& s) { setError(s); }
+}  // namespace gbfv
+
 // ===================================================================== ctx
 struct gbfv_ctx {
     int N = 0, b = 0, dim = 0, model = 0, ldN = 0;
