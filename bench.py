@@ -45,6 +45,9 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="blackoil-100x100x20", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="one linearization + one mixed solve of the workload (for ncu captures); "
+                         "prints the solve's iterations, launches and algorithmic bytes")
     return ap.parse_args()
 
 
@@ -340,8 +343,31 @@ def run_ours(args):
     return 0
 
 
+def run_profile_case(args):
+    """Initial state of the workload: one linearization (iteration 0) and one
+    mixed-precision solve, the unit an ncu capture of the solver covers."""
+    import __graft_entry__ as ge
+    ge.build()
+    from gbfv import Context, capi
+    w = WORKLOADS[args.workload]
+    ctx = Context(build_problem(args.workload), params(capi.PREC_MIXED))
+    if ctx.linearize(w["dt"], 0):
+        raise RuntimeError("linearization failed")
+    lin = ctx.kernel_stats()
+    ctx.reset_kernel_stats()
+    st, _, it = ctx.solve(want_dx=False)
+    ks = ctx.kernel_stats()
+    print(json.dumps({"workload": args.workload, "status": st, "iterations": it,
+                      "solve_launches": ks["solve_launches"], "solve_bytes": ks["solve_bytes"],
+                      "solve_ms": ks["solve_ms"], "linearize_bytes_per_call": lin["linearize_bytes"],
+                      "linearize_ms": lin["linearize_ms"]}))
+    return 0 if st == 0 else 1
+
+
 def main():
     args = parse()
+    if args.profile_case:
+        return run_profile_case(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -331,12 +331,60 @@ int gbfv_get_kernel_stats(const gbfv_ctx* ctx, gbfv_kernel_stats* out);
  * cooperative grid (mode 0), blocks, and the candidate timings [ms]       */
 int gbfv_solver_config(const gbfv_ctx* ctx, int precision, int* mode, int* blocks,
                        double* tune_ms, int* num_tuned);
+/* fix the launch configuration of the persistent solve kernel of a
+ * precision (mode 1 = cluster of `blocks` blocks, 0 = cooperative grid) and
+ * skip the autotuner; GBFV_ERR_UNSUPPORTED beyond what the device allows  */
+int gbfv_set_solver_config(gbfv_ctx* ctx, int precision, int mode, int blocks);
 int gbfv_reset_kernel_stats(gbfv_ctx* ctx);
 /* with GBFV_PROFILE set in the environment at creation: nanoseconds spent
  * by the persistent solve kernel per phase since the last call ([0]
  * factorization, [1] forward sweeps, [2] backward sweeps, [3] SpMV + dots,
  * [4] vector updates + norms, [5] remaining); zeros otherwise            */
 int gbfv_solver_phase_ns(gbfv_ctx* ctx, unsigned long long* ns8);
+
+/* ------------------------------------------------------------------ */
+/* Batched systems (ensemble realizations, served requests).  No single
+ * counterpart in the reference, which advances one problem per simulator
+ * (Simulator::run, simulator.hh:738); each system here follows exactly the
+ * reference's time loop and Newton method (fvbaseproblem.hh:512-606,
+ * newtonmethod.hh:228-806) as gbfv_time_integration does.  The device work
+ * of all systems is issued together: one batched launch per phase (IQ +
+ * assembly + Newton error; FP64 residual; one persistent BiCGStab/ILU0
+ * launch in which clusters of cluster_size blocks take systems from a work
+ * queue, largest first; Newton update), each phase a captured CUDA graph
+ * replayed every round.  A system's results equal those of the same
+ * problem run alone with gbfv_set_solver_config(ctx, precision, 1,
+ * cluster_size).  All systems share params and the model.               */
+typedef struct gbfv_batch gbfv_batch;
+typedef struct gbfv_batch_stats {
+    int32_t num_systems;
+    int32_t cluster_size;      /* blocks per cluster of the batched solve  */
+    int32_t num_clusters;      /* clusters resident at once               */
+    int32_t pad;
+    int64_t rounds;            /* Newton rounds                           */
+    int64_t graph_launches;
+    int64_t kernel_launches;
+    int64_t solve_launches;    /* batched persistent solve launches        */
+    double solve_ms;           /* device time of those launches            */
+    double solve_bytes;        /* their algorithmic bytes                  */
+    double linearize_ms;       /* device time of the linearization graphs  */
+} gbfv_batch_stats;
+/* cluster_size 0: 8 (or the device maximum below it)                    */
+gbfv_batch* gbfv_batch_create(const gbfv_problem* problems, int num_systems,
+                              const gbfv_params* params, int cluster_size, int* status);
+int gbfv_batch_destroy(gbfv_batch* batch);
+/* the context of system i (set_solution / get_solution / save_state ...;
+ * owned by the batch)                                                    */
+gbfv_ctx* gbfv_batch_system(gbfv_batch* batch, int i);
+/* every system: num_steps time steps from dt0 (gbfv_time_integration
+ * semantics); returns the first failing system's status or GBFV_OK      */
+int gbfv_batch_time_integration(gbfv_batch* batch, int num_steps, double dt0,
+                                double end_time, int fixed_dt);
+int gbfv_batch_system_report(const gbfv_batch* batch, int i, int* status, int* steps_done,
+                             double* step_dt, int32_t* step_newton, int32_t* step_linear,
+                             int* linearizations);
+int gbfv_batch_get_stats(const gbfv_batch* batch, gbfv_batch_stats* out);
+void* gbfv_batch_stream(gbfv_batch* batch);
 
 /* ------------------------------------------------------------------ */
 /* Allocation-free Newton error.  No counterpart in the reference: its

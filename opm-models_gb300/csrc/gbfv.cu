@@ -356,13 +356,11 @@ int adjacentLevels(const std::vector<std::vector<int>>& lower, const std::vector
     return 1;
 }
 
-// solver-precision iteration; returns status and fills iterations
+// kernel arguments of one solve of S in launch configuration (mode, nblocks)
 template <class T>
-int runKrylovCfg(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hst, const T* A, T* FL, T* FD,
-                 const T* rhs, T* const* vec, int factor, double redTol, double absTol, double maxRes,
-                 int maxIter, int mode, int nblocks, int& iters, float* msOut, bool stats)
+int fillKArgs(SolverData& S, DevStatus* st, const T* A, T* FL, T* FD, const T* rhs, T* const* vec, int factor,
+              double redTol, double absTol, double maxRes, int maxIter, int mode, int nblocks, KArgs<T>& a)
 {
-    KArgs<T> a;
     a.N = S.N;
     a.ldN = S.ldN;
     a.dim = S.dim;
@@ -410,7 +408,18 @@ int runKrylovCfg(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* h
             a.levVals = S.levVals;
         }
     }
-    int rs;
+    return GBFV_OK;
+}
+
+// solver-precision iteration; returns status and fills iterations
+template <class T>
+int runKrylovCfg(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hst, const T* A, T* FL, T* FD,
+                 const T* rhs, T* const* vec, int factor, double redTol, double absTol, double maxRes,
+                 int maxIter, int mode, int nblocks, int& iters, float* msOut, bool stats)
+{
+    KArgs<T> a;
+    int rs = fillKArgs<T>(S, st, A, FL, FD, rhs, vec, factor, redTol, absTol, maxRes, maxIter, mode, nblocks, a);
+    if (rs) return rs;
     if ((rs = resetStatus(stream, st))) return rs;
     CK(cudaMemsetAsync(S.bar, 0, 4 * sizeof(unsigned), stream));
     cudaEventRecord(S.evA, stream);
@@ -1306,6 +1315,19 @@ int gbfv_get_kernel_stats(const gbfv_ctx* Cc, gbfv_kernel_stats* out)
     return GBFV_OK;
 }
 
+int gbfv_set_solver_config(gbfv_ctx* C, int precision, int mode, int blocks)
+{
+    if (!C || (mode != SYNC_CLUSTER && mode != SYNC_GRID) || blocks < 1) return GBFV_ERR_ARG;
+    const int k = precision == GBFV_PREC_MIXED ? 1 : 0;
+    SolverData& S = C->S;
+    if (mode == SYNC_CLUSTER && blocks > S.maxCluster[k]) return GBFV_ERR_UNSUPPORTED;
+    if (mode == SYNC_GRID && blocks > S.maxGrid[k]) return GBFV_ERR_UNSUPPORTED;
+    S.mode[k] = mode;
+    S.nblk[k] = blocks;
+    S.tuned[k] = 1;
+    return GBFV_OK;
+}
+
 int gbfv_solver_config(const gbfv_ctx* C, int precision, int* mode, int* blocks, double* tuneMs, int* nt)
 {
     if (!C) return GBFV_ERR_ARG;
@@ -1628,5 +1650,677 @@ int gbfv_linsolver_solve(gbfv_linsolver* L, const double* rhs, double* x, int* i
         for (int e = 0; e < b; ++e) x[(size_t)i * b + e] = L->stage[(size_t)L->perm[i] * b + e];
     return st;
 }
+
+}  // extern "C"
+
+// ================================================================ batch
+// Many independent systems (ensemble realizations, served requests) advanced
+// together.  Each system keeps its own context (device state, storage cache,
+// solver data); the batch runs rounds, and in each round every system that
+// needs it goes through one step of its own Newton / time-step state machine
+// -- the same decisions as gbfv_newton_apply and gbfv_time_integration -- with
+// the device work of all systems issued as one batched launch per phase:
+//   L  constraints + intensive quantities + assembly + Newton error
+//   S  FP64 residual, FP32 factorization + BiCGStab (one persistent launch,
+//      clusters take systems from a work queue), refinement
+//   U  update guard, Newton update with chopping / switching
+// Each phase is a captured CUDA graph, replayed every round; which systems
+// take part is data (an active flag per system), so the graphs never change.
+// Every system runs the same device code as alone, with the same solver
+// launch configuration, so its result does not depend on the batch.
+namespace {
+
+enum SysPhase { PH_LIN = 0, PH_SOLVE = 1, PH_UPDATE = 2, PH_DONE = 3, PH_FAILED = 4, PH_IDLE = 5 };
+
+struct SysState {
+    int phase = PH_IDLE;
+    int status = GBFV_OK;
+    // time integration
+    int numSteps = 0, step = 0, fixedDt = 0, fails = 0, linItStep = 0, linearizations = 0;
+    double dt = 0, dt0 = 0, t = 0, endTime = 1e100;
+    std::vector<double> stepDt;
+    std::vector<int> stepNewton, stepLinear;
+    // Newton
+    int numIterations = 0;
+    double error = 0, lastError = 0;
+    // mixed-precision refinement of the current solve
+    double resErr = 0, resErr0 = 0;
+    int solveIters = 0, refs = 0, lastKs = GBFV_OK, lastIt = 0, solveDone = 0, solveStatus = GBFV_OK;
+};
+
+struct GraphSet {
+    cudaGraphExec_t exec = nullptr;
+    int kernels = 0;
+};
+
+}  // namespace
+
+struct gbfv_batch {
+    int K = 0, b = 0, model = 0, precision = GBFV_PREC_MIXED;
+    gbfv_params prm;
+    cudaStream_t stream = nullptr;
+    std::vector<gbfv_ctx*> ctx;
+    std::vector<SysState> sys;
+    int cluster = 0, numClusters = 1, maxLev = 1, gxLin = 16, gxSol = 16;
+    // device tables and their pinned host mirrors
+    LinJob* dLin = nullptr;
+    SolveJob* dSol = nullptr;
+    JobState *dJs = nullptr, *hJs = nullptr;
+    int *dAct = nullptr, *hAct = nullptr;          // systems taking part in a solve phase
+    DevStatus *dSt = nullptr, *hSt = nullptr;
+    KArgs<float> *dK32 = nullptr, *hK32 = nullptr;
+    KArgs<double> *dK64 = nullptr, *hK64 = nullptr;
+    int *dOrder = nullptr, *hOrder = nullptr;      // [K] order, then the count at [K]
+    int* dQueue = nullptr;
+    GraphSet gLin, gCheck, gUpd, gRes0, gKry, gRef;
+    UpdateParams up{};
+    cudaEvent_t evA = nullptr, evB = nullptr;
+    // statistics
+    int64_t rounds = 0, graphLaunches = 0, kernelLaunches = 0;
+    double solveMs = 0, solveBytes = 0, linMs = 0;
+    int64_t solveLaunches = 0;
+};
+
+namespace {
+
+template <class T>
+int pinnedAlloc(T** p, size_t n)
+{
+    *p = nullptr;
+    CK(cudaMallocHost((void**)p, sizeof(T) * std::max<size_t>(n, 1)));
+    std::memset(*p, 0, sizeof(T) * std::max<size_t>(n, 1));
+    return GBFV_OK;
+}
+
+// capture the work that fn issues on the batch stream into an executable graph
+template <class F>
+int captureGraph(gbfv_batch* B, GraphSet& g, F&& fn)
+{
+    const int64_t before = g_launches;
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal));
+    const int st = fn();
+    const cudaError_t e = cudaStreamEndCapture(B->stream, &graph);
+    if (st != GBFV_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return st;
+    }
+    CK(e);
+    const cudaError_t ei = cudaGraphInstantiate(&g.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    CK(ei);
+    g.kernels = (int)(g_launches - before);
+    g_launches = before;  // counted when the graph is replayed
+    return GBFV_OK;
+}
+
+int replay(gbfv_batch* B, GraphSet& g, bool sync)
+{
+    CK(cudaGraphLaunch(g.exec, B->stream));
+    g_launches += g.kernels;
+    B->kernelLaunches += g.kernels;
+    B->graphLaunches++;
+    if (sync) CK(cudaStreamSynchronize(B->stream));
+    return GBFV_OK;
+}
+
+double bitsToDouble(unsigned long long bits)
+{
+    double v;
+    std::memcpy(&v, &bits, sizeof(v));
+    return v;
+}
+
+int buildBatchGraphs(gbfv_batch* B)
+{
+    const int K = B->K;
+    cudaStream_t s = B->stream;
+    int st;
+    // L: constraints, IQ, assembly, Newton error; statuses to the host
+    st = captureGraph(B, B->gLin, [&]() -> int {
+        CK(cudaMemcpyAsync(B->dJs, B->hJs, sizeof(JobState) * K, cudaMemcpyHostToDevice, s));
+        CK(cudaMemsetAsync(B->dSt, 0, sizeof(DevStatus) * K, s));
+        launchBatchLinearize(B->dLin, B->dJs, K, B->gxLin, s);
+        launchBatchNewtonError(B->dLin, B->dJs, K, B->gxLin, s);
+        CK(cudaMemcpyAsync(B->hSt, B->dSt, sizeof(DevStatus) * K, cudaMemcpyDeviceToHost, s));
+        return GBFV_OK;
+    });
+    if (st) return st;
+    // U1: update guard
+    st = captureGraph(B, B->gCheck, [&]() -> int {
+        CK(cudaMemcpyAsync(B->dJs, B->hJs, sizeof(JobState) * K, cudaMemcpyHostToDevice, s));
+        CK(cudaMemsetAsync(B->dSt, 0, sizeof(DevStatus) * K, s));
+        launchBatchCheckUpdate(B->dLin, B->dJs, K, B->gxLin, s);
+        CK(cudaMemcpyAsync(B->hSt, B->dSt, sizeof(DevStatus) * K, cudaMemcpyDeviceToHost, s));
+        return GBFV_OK;
+    });
+    if (st) return st;
+    // U2: Newton update
+    st = captureGraph(B, B->gUpd, [&]() -> int {
+        CK(cudaMemcpyAsync(B->dJs, B->hJs, sizeof(JobState) * K, cudaMemcpyHostToDevice, s));
+        launchBatchNewtonUpdate(B->dLin, B->dJs, K, B->gxLin, B->up, s);
+        return GBFV_OK;
+    });
+    if (st) return st;
+    if (B->precision == GBFV_PREC_MIXED) {
+        // S0: FP32 matrix, x = 0, FP64 residual of the Newton system
+        st = captureGraph(B, B->gRes0, [&]() -> int {
+            CK(cudaMemcpyAsync(B->dAct, B->hAct, sizeof(int) * K, cudaMemcpyHostToDevice, s));
+            CK(cudaMemsetAsync(B->dSt, 0, sizeof(DevStatus) * K, s));
+            launchBatchCast(B->dSol, B->dAct, K, B->gxSol, s);
+            launchBatchZeroX(B->dSol, B->dAct, K, B->gxSol, s);
+            launchBatchResidual64(B->dSol, B->dAct, K, B->gxSol, B->b, s);
+            CK(cudaMemcpyAsync(B->hSt, B->dSt, sizeof(DevStatus) * K, cudaMemcpyDeviceToHost, s));
+            return GBFV_OK;
+        });
+        if (st) return st;
+        // S2: accumulate the inner solution, FP64 residual again
+        st = captureGraph(B, B->gRef, [&]() -> int {
+            CK(cudaMemcpyAsync(B->dAct, B->hAct, sizeof(int) * K, cudaMemcpyHostToDevice, s));
+            CK(cudaMemsetAsync(B->dSt, 0, sizeof(DevStatus) * K, s));
+            launchBatchAccumulate(B->dSol, B->dAct, K, B->gxSol, s);
+            launchBatchResidual64(B->dSol, B->dAct, K, B->gxSol, B->b, s);
+            CK(cudaMemcpyAsync(B->hSt, B->dSt, sizeof(DevStatus) * K, cudaMemcpyDeviceToHost, s));
+            return GBFV_OK;
+        });
+        if (st) return st;
+    }
+    // S1: the persistent batched solve
+    st = captureGraph(B, B->gKry, [&]() -> int {
+        CK(cudaMemcpyAsync(B->dOrder, B->hOrder, sizeof(int) * (K + 1), cudaMemcpyHostToDevice, s));
+        CK(cudaMemsetAsync(B->dQueue, 0, sizeof(int), s));
+        CK(cudaMemsetAsync(B->dSt, 0, sizeof(DevStatus) * K, s));
+        int ls;
+        if (B->precision == GBFV_PREC_MIXED) {
+            CK(cudaMemcpyAsync(B->dK32, B->hK32, sizeof(KArgs<float>) * K, cudaMemcpyHostToDevice, s));
+            ls = launchBicgstabBatch<float>(B->dK32, B->dOrder, B->dOrder + K, B->dQueue, B->b, B->cluster,
+                                            B->numClusters, B->maxLev, s);
+        }
+        else {
+            CK(cudaMemcpyAsync(B->dK64, B->hK64, sizeof(KArgs<double>) * K, cudaMemcpyHostToDevice, s));
+            ls = launchBicgstabBatch<double>(B->dK64, B->dOrder, B->dOrder + K, B->dQueue, B->b, B->cluster,
+                                             B->numClusters, B->maxLev, s);
+        }
+        if (ls) return ls;
+        CK(cudaMemcpyAsync(B->hSt, B->dSt, sizeof(DevStatus) * K, cudaMemcpyDeviceToHost, s));
+        return GBFV_OK;
+    });
+    return st;
+}
+
+// the fail path of gbfv_newton_apply followed by the dt-halving of
+// gbfv_time_integration (fvbaseproblem.hh:523-542)
+void batchFail(gbfv_batch* B, int i, int status)
+{
+    SysState& y = B->sys[i];
+    gbfv_ctx* C = B->ctx[i];
+    cudaMemcpyAsync(C->x, C->xOld, sizeof(double) * C->N * C->b, cudaMemcpyDeviceToDevice, B->stream);
+    cudaMemcpyAsync(C->meaning, C->meaningOld, sizeof(int) * C->N, cudaMemcpyDeviceToDevice, B->stream);
+    y.numIterations = B->prm.newton_target_iterations * 2;
+    if (status == GBFV_ERR_CUDA || status == GBFV_ERR_TIMEOUT || status == GBFV_ERR_OOM) {
+        y.phase = PH_FAILED;
+        y.status = status;
+        return;
+    }
+    y.fails++;
+    const double nextDt0 = y.dt / 2.0;
+    if (y.dt < B->prm.min_time_step * (1 + 1e-9) || y.fails >= B->prm.max_time_step_divisions) {
+        y.phase = PH_FAILED;
+        y.status = GBFV_ERR_NOT_CONVERGED;
+        return;
+    }
+    y.dt = std::max(nextDt0, B->prm.min_time_step);
+    y.numIterations = 0;
+    y.error = y.lastError = 0;
+    y.phase = PH_LIN;
+}
+
+// end of a converged Newton solve: advance the time level, next step size
+void batchStepDone(gbfv_batch* B, int i)
+{
+    SysState& y = B->sys[i];
+    gbfv_ctx* C = B->ctx[i];
+    y.stepDt.push_back(y.dt);
+    y.stepNewton.push_back(y.numIterations);
+    y.stepLinear.push_back(y.linItStep);
+    cudaMemcpyAsync(C->xOld, C->x, sizeof(double) * C->N * C->b, cudaMemcpyDeviceToDevice, B->stream);
+    cudaMemcpyAsync(C->meaningOld, C->meaning, sizeof(int) * C->N, cudaMemcpyDeviceToDevice, B->stream);
+    y.t += y.dt;
+    y.step++;
+    C->numIterations = y.numIterations;
+    if (y.fixedDt) y.dt = y.dt0;
+    else {
+        const double maxTs = std::max(0.0, y.endTime - y.t);
+        double dtNext = std::min(B->prm.max_time_step, gbfv_suggest_time_step(C, y.dt, y.numIterations));
+        if (dtNext < maxTs && maxTs < dtNext * 2) dtNext = maxTs / 2 * 1.01;
+        y.dt = std::min(maxTs, dtNext);
+    }
+    y.fails = 0;
+    y.linItStep = 0;
+    y.numIterations = 0;
+    y.error = y.lastError = 0;
+    y.phase = (y.step >= y.numSteps || y.t >= y.endTime) ? PH_DONE : PH_LIN;
+}
+
+bool batchProceed(const gbfv_batch* B, const SysState& y)
+{
+    if (y.numIterations < 1) return true;
+    if (y.error <= B->prm.newton_tolerance) return false;
+    if (y.numIterations >= B->prm.newton_max_iterations) return y.error * 4.0 < y.lastError;
+    return true;
+}
+
+// the Newton loop has left the loop body: converged or not (newton_apply tail)
+void batchNewtonEnd(gbfv_batch* B, int i)
+{
+    SysState& y = B->sys[i];
+    if (y.error <= B->prm.newton_tolerance) batchStepDone(B, i);
+    else batchFail(B, i, GBFV_ERR_NOT_CONVERGED);
+}
+
+// one solve phase for every system in PH_SOLVE; leaves them in PH_UPDATE or failed
+int batchSolvePhase(gbfv_batch* B)
+{
+    const int K = B->K;
+    std::vector<int> S;
+    for (int i = 0; i < K; ++i)
+        if (B->sys[i].phase == PH_SOLVE) S.push_back(i);
+    if (S.empty()) return GBFV_OK;
+    const gbfv_params& prm = B->prm;
+    const double absTol = absTolOf(prm);
+    const double eps = std::numeric_limits<double>::min() * 1e10;
+    auto solveOrder = [&](const std::vector<int>& R) {
+        std::vector<int> o(R);
+        std::stable_sort(o.begin(), o.end(), [&](int a, int c) { return B->ctx[a]->N > B->ctx[c]->N; });
+        for (size_t q = 0; q < o.size(); ++q) B->hOrder[q] = o[q];
+        B->hOrder[K] = (int)o.size();
+    };
+    auto krylov = [&](const std::vector<int>& R, int ref) -> int {
+        for (int i : R) {
+            gbfv_ctx* C = B->ctx[i];
+            SolverData& Sd = C->S;
+            int rs;
+            if (B->precision == GBFV_PREC_MIXED) {
+                const SysState& y = B->sys[i];
+                const double target = std::max(prm.linear_tolerance * y.resErr0, absTol);
+                const double need = target / y.resErr;
+                const double innerTol = std::min(0.5, std::max(0.5 * need, prm.inner_tolerance));
+                float* vec[6] = {Sd.v32[1], Sd.v32[2], Sd.v32[3], Sd.v32[4], Sd.v32[5], Sd.v32[6]};
+                rs = fillKArgs<float>(Sd, &B->dSt[i], Sd.A32, Sd.FL32, Sd.FD32, Sd.v32[0], vec, ref == 0, innerTol,
+                                      0.0, prm.linear_max_error, prm.linear_max_iterations, SYNC_CLUSTER, B->cluster,
+                                      B->hK32[i]);
+            }
+            else {
+                rs = fillKArgs<double>(Sd, &B->dSt[i], C->jval, Sd.FL64, Sd.FD64, C->residual, Sd.v64, 1,
+                                       prm.linear_tolerance, absTol, prm.linear_max_error, prm.linear_max_iterations,
+                                       SYNC_CLUSTER, B->cluster, B->hK64[i]);
+            }
+            if (rs) return rs;
+        }
+        solveOrder(R);
+        cudaEventRecord(B->evA, B->stream);
+        int rs = replay(B, B->gKry, false);
+        if (rs) return rs;
+        cudaEventRecord(B->evB, B->stream);
+        CK(cudaStreamSynchronize(B->stream));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, B->evA, B->evB);
+        B->solveMs += ms;
+        B->solveLaunches++;
+        for (int i : R) {
+            const DevStatus& h = B->hSt[i];
+            B->solveBytes += solveBytes(B->ctx[i]->S, h.iterations, B->precision == GBFV_PREC_MIXED ? ref == 0 : 1,
+                                        B->precision == GBFV_PREC_MIXED ? 4 : 8);
+        }
+        return GBFV_OK;
+    };
+    if (B->precision != GBFV_PREC_MIXED) {
+        int rs = krylov(S, 0);
+        if (rs) return rs;
+        for (int i : S) {
+            const DevStatus& h = B->hSt[i];
+            SysState& y = B->sys[i];
+            y.linItStep += h.iterations;
+            const int ks = h.code ? h.code : (h.converged ? GBFV_OK : GBFV_ERR_NOT_CONVERGED);
+            if (ks != GBFV_OK) batchFail(B, i, ks);
+            else y.phase = PH_UPDATE;
+        }
+        return GBFV_OK;
+    }
+    // mixed: r = b - A*0, then refinement rounds (solveMixed)
+    for (int i = 0; i < K; ++i) B->hAct[i] = 0;
+    for (int i : S) B->hAct[i] = 1;
+    int rs = replay(B, B->gRes0, true);
+    if (rs) return rs;
+    std::vector<int> R;
+    for (int i : S) {
+        SysState& y = B->sys[i];
+        y.resErr = std::max(bitsToDouble(B->hSt[i].errorBits), eps);
+        y.resErr0 = y.resErr;
+        y.solveIters = 0;
+        y.refs = 0;
+        if (y.resErr / std::max(1e-20, y.resErr0) <= prm.linear_tolerance || y.resErr <= absTol) y.phase = PH_UPDATE;
+        else R.push_back(i);
+    }
+    for (int ref = 0; ref < std::max(1, prm.max_refinements) && !R.empty(); ++ref) {
+        if ((rs = krylov(R, ref))) return rs;
+        std::vector<int> R2;
+        for (int i : R) {
+            const DevStatus& h = B->hSt[i];
+            SysState& y = B->sys[i];
+            y.lastIt = h.iterations;
+            y.solveIters += h.iterations;
+            y.linItStep += h.iterations;
+            y.refs++;
+            y.lastKs = h.code ? h.code : (h.converged ? GBFV_OK : GBFV_ERR_NOT_CONVERGED);
+            if (y.lastKs != GBFV_OK && y.lastKs != GBFV_ERR_NOT_CONVERGED) batchFail(B, i, y.lastKs);
+            else R2.push_back(i);
+        }
+        R.swap(R2);
+        if (R.empty()) break;
+        for (int i = 0; i < K; ++i) B->hAct[i] = 0;
+        for (int i : R) B->hAct[i] = 1;
+        if ((rs = replay(B, B->gRef, true))) return rs;
+        std::vector<int> R3;
+        for (int i : R) {
+            SysState& y = B->sys[i];
+            y.resErr = bitsToDouble(B->hSt[i].errorBits);
+            if (!std::isfinite(y.resErr)) batchFail(B, i, GBFV_ERR_NONFINITE);
+            else if (y.resErr / std::max(1e-20, y.resErr0) <= prm.linear_tolerance || y.resErr <= absTol)
+                y.phase = PH_UPDATE;
+            else if (y.resErr > prm.linear_max_error * y.resErr0) batchFail(B, i, GBFV_ERR_NOT_CONVERGED);
+            else if (y.lastKs == GBFV_ERR_NOT_CONVERGED && y.lastIt >= prm.linear_max_iterations)
+                batchFail(B, i, GBFV_ERR_NOT_CONVERGED);
+            else R3.push_back(i);
+        }
+        R.swap(R3);
+    }
+    for (int i : R) batchFail(B, i, GBFV_ERR_NOT_CONVERGED);
+    return GBFV_OK;
+}
+
+// one round: L for systems in PH_LIN, S, U; returns a CUDA-level status
+int batchRound(gbfv_batch* B)
+{
+    const int K = B->K;
+    const gbfv_params& prm = B->prm;
+    bool any = false;
+    for (int i = 0; i < K; ++i) {
+        SysState& y = B->sys[i];
+        B->hJs[i].active = y.phase == PH_LIN;
+        if (y.phase == PH_LIN) {
+            any = true;
+            B->hJs[i].dt = y.dt;
+            B->hJs[i].iter0 = y.numIterations == 0;
+            y.lastError = y.error;
+        }
+    }
+    if (!any) return GBFV_OK;
+    B->rounds++;
+    cudaEventRecord(B->evA, B->stream);
+    int rs = replay(B, B->gLin, false);
+    if (rs) return rs;
+    cudaEventRecord(B->evB, B->stream);
+    CK(cudaStreamSynchronize(B->stream));
+    {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, B->evA, B->evB);
+        B->linMs += ms;
+    }
+    for (int i = 0; i < K; ++i) {
+        if (!B->hJs[i].active) continue;
+        SysState& y = B->sys[i];
+        y.linearizations++;
+        const DevStatus& h = B->hSt[i];
+        y.error = bitsToDouble(h.errorBits);
+        if (h.nonfinite) batchFail(B, i, GBFV_ERR_NONFINITE);
+        else if (y.error > prm.newton_max_error) batchFail(B, i, GBFV_ERR_NUMERICAL);
+        else if (!batchProceed(B, y)) {
+            y.numIterations++;
+            batchNewtonEnd(B, i);
+        }
+        else y.phase = PH_SOLVE;
+    }
+    if ((rs = batchSolvePhase(B))) return rs;
+    bool anyU = false;
+    for (int i = 0; i < K; ++i) {
+        B->hJs[i].active = B->sys[i].phase == PH_UPDATE;
+        anyU |= B->hJs[i].active != 0;
+    }
+    if (!anyU) return GBFV_OK;
+    if ((rs = replay(B, B->gCheck, true))) return rs;
+    for (int i = 0; i < K; ++i) {
+        if (!B->hJs[i].active) continue;
+        if (B->hSt[i].nonfinite) {
+            B->hJs[i].active = 0;
+            batchFail(B, i, GBFV_ERR_NONFINITE);
+        }
+    }
+    if ((rs = replay(B, B->gUpd, false))) return rs;
+    for (int i = 0; i < K; ++i)
+        if (B->hJs[i].active) {
+            SysState& y = B->sys[i];
+            y.numIterations++;
+            // the loop condition of gbfv_newton_apply, checked before the next linearization
+            if (batchProceed(B, y)) y.phase = PH_LIN;
+            else batchNewtonEnd(B, i);
+        }
+    return GBFV_OK;
+}
+
+void freeBatch(gbfv_batch* B)
+{
+    if (!B) return;
+    for (GraphSet* g : {&B->gLin, &B->gCheck, &B->gUpd, &B->gRes0, &B->gKry, &B->gRef})
+        if (g->exec) cudaGraphExecDestroy(g->exec);
+    cudaFree(B->dLin);
+    cudaFree(B->dSol);
+    cudaFree(B->dJs);
+    cudaFree(B->dAct);
+    cudaFree(B->dSt);
+    cudaFree(B->dK32);
+    cudaFree(B->dK64);
+    cudaFree(B->dOrder);
+    cudaFree(B->dQueue);
+    cudaFreeHost(B->hJs);
+    cudaFreeHost(B->hAct);
+    cudaFreeHost(B->hSt);
+    cudaFreeHost(B->hK32);
+    cudaFreeHost(B->hK64);
+    cudaFreeHost(B->hOrder);
+    if (B->evA) cudaEventDestroy(B->evA);
+    if (B->evB) cudaEventDestroy(B->evB);
+    if (B->stream) cudaStreamDestroy(B->stream);
+    for (gbfv_ctx* C : B->ctx) gbfv_destroy(C);
+    delete B;
+}
+
+int setupBatch(gbfv_batch* B, int cluster)
+{
+    const int K = B->K;
+    int st;
+    CK(cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&B->evA));
+    CK(cudaEventCreate(&B->evB));
+    if ((st = devAlloc(&B->dLin, K)) || (st = devAlloc(&B->dSol, K)) || (st = devAlloc(&B->dJs, K)) ||
+        (st = devAlloc(&B->dAct, K)) || (st = devAlloc(&B->dSt, K)) || (st = devAlloc(&B->dK32, K)) ||
+        (st = devAlloc(&B->dK64, K)) || (st = devAlloc(&B->dOrder, K + 1)) || (st = devAlloc(&B->dQueue, 1)))
+        return st;
+    if ((st = pinnedAlloc(&B->hJs, K)) || (st = pinnedAlloc(&B->hAct, K)) || (st = pinnedAlloc(&B->hSt, K)) ||
+        (st = pinnedAlloc(&B->hK32, K)) || (st = pinnedAlloc(&B->hK64, K)) || (st = pinnedAlloc(&B->hOrder, K + 1)))
+        return st;
+    std::vector<LinJob> lj(K);
+    std::vector<SolveJob> sj(K);
+    int maxN = 1, maxLev = 1, maxC = 16;
+    for (int i = 0; i < K; ++i) {
+        gbfv_ctx* C = B->ctx[i];
+        LinJob& j = lj[i];
+        j.m = C->mesh;
+        j.phys = C->dphys;
+        j.x = C->x;
+        j.xOld = C->xOld;
+        j.meaning = C->meaning;
+        j.meaningOld = C->meaningOld;
+        j.iq = C->iq;
+        j.storageOld = C->storageOld;
+        j.residual = C->residual;
+        j.jval = C->jval;
+        j.dx = B->precision == GBFV_PREC_MIXED ? C->S.xref : C->S.v64[0];
+        j.wasSwitched = C->wasSwitched;
+        j.st = &B->dSt[i];
+        SolveJob& s = sj[i];
+        SolverData& S = C->S;
+        s.N = S.N;
+        s.ld = S.ldN;
+        s.nslot = S.nslot;
+        s.b = S.b;
+        s.nval = (long)S.nslot * S.b * S.b * S.ldN;
+        s.col = S.col;
+        s.A64 = C->jval;
+        s.A32 = S.A32;
+        s.rhs = C->residual;
+        s.xref = S.xref;
+        s.rref = S.rref;
+        s.r32 = S.v32[0];
+        s.dx32 = S.v32[1];
+        s.st = &B->dSt[i];
+        maxN = std::max(maxN, C->N);
+        maxLev = std::max(maxLev, (int)S.levPtr.size() - 1);
+        maxC = std::min(maxC, S.maxCluster[B->precision == GBFV_PREC_MIXED ? 1 : 0]);
+    }
+    B->maxLev = std::min(maxLev, MAX_PUSH_LEVELS);
+    B->cluster = cluster > 0 ? std::min(cluster, maxC) : std::min(8, maxC);
+    B->numClusters = B->precision == GBFV_PREC_MIXED ? maxActiveClusters<float>(B->b, B->cluster)
+                                                     : maxActiveClusters<double>(B->b, B->cluster);
+    if (B->numClusters < 1) B->numClusters = 1;
+    B->numClusters = std::min(B->numClusters, K);
+    B->gxLin = std::max(1, std::min((maxN + 127) / 128, std::max(16, (152 * 16 + K - 1) / K)));
+    B->gxSol = std::max(1, std::min((maxN + 255) / 256, std::max(16, (152 * 8 + K - 1) / K)));
+    CK(cudaMemcpy(B->dLin, lj.data(), sizeof(LinJob) * K, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(B->dSol, sj.data(), sizeof(SolveJob) * K, cudaMemcpyHostToDevice));
+    UpdateParams& up = B->up;
+    up.dsMax = B->prm.ds_max;
+    up.dpMaxRel = B->prm.dp_max_rel;
+    up.oscThreshold = B->prm.pv_oscillation_threshold;
+    up.pMin = B->prm.pressure_min;
+    up.pMax = B->prm.pressure_max;
+    up.swMax = B->prm.max_water_saturation;
+    up.waterOnly = B->prm.water_only_threshold;
+    CK(cudaDeviceSynchronize());
+    return buildBatchGraphs(B);
+}
+
+}  // namespace
+
+extern "C" {
+
+gbfv_batch* gbfv_batch_create(const gbfv_problem* probs, int num_systems, const gbfv_params* params,
+                              int cluster_size, int* status)
+{
+    auto fail = [&](gbfv_batch* B, int st) -> gbfv_batch* {
+        if (status) *status = st;
+        freeBatch(B);
+        return nullptr;
+    };
+    if (!probs || num_systems <= 0) return fail(nullptr, GBFV_ERR_ARG);
+    gbfv_batch* B = new gbfv_batch();
+    if (params) B->prm = *params;
+    else gbfv_default_params(&B->prm);
+    B->precision = B->prm.precision;
+    B->K = num_systems;
+    for (int i = 0; i < num_systems; ++i) {
+        int st = GBFV_OK;
+        gbfv_ctx* C = gbfv_create(&probs[i], &B->prm, &st);
+        if (!C) return fail(B, st ? st : GBFV_ERR_ARG);
+        B->ctx.push_back(C);
+        if (i == 0) {
+            B->b = C->b;
+            B->model = C->model;
+        }
+        else if (C->b != B->b || C->model != B->model) {
+            setError("all systems of a batch must use the same model");
+            return fail(B, GBFV_ERR_ARG);
+        }
+    }
+    B->sys.resize(num_systems);
+    const int st = setupBatch(B, cluster_size);
+    if (st) return fail(B, st);
+    if (status) *status = GBFV_OK;
+    return B;
+}
+
+int gbfv_batch_destroy(gbfv_batch* B)
+{
+    freeBatch(B);
+    return GBFV_OK;
+}
+
+gbfv_ctx* gbfv_batch_system(gbfv_batch* B, int i)
+{
+    if (!B || i < 0 || i >= B->K) return nullptr;
+    return B->ctx[i];
+}
+
+int gbfv_batch_time_integration(gbfv_batch* B, int num_steps, double dt0, double end_time, int fixed_dt)
+{
+    if (!B || num_steps < 0 || !(dt0 > 0)) return GBFV_ERR_ARG;
+    for (int i = 0; i < B->K; ++i) {
+        gbfv_ctx* C = B->ctx[i];
+        CK(cudaStreamSynchronize(C->stream));  // set_solution etc. ran on the context's stream
+        SysState& y = B->sys[i];
+        y = SysState();
+        y.numSteps = num_steps;
+        y.dt = y.dt0 = dt0;
+        y.endTime = end_time;
+        y.fixedDt = fixed_dt;
+        y.phase = num_steps > 0 ? PH_LIN : PH_DONE;
+    }
+    for (;;) {
+        bool pending = false;
+        for (const SysState& y : B->sys) pending |= y.phase == PH_LIN;
+        if (!pending) break;
+        const int rs = batchRound(B);
+        if (rs) return rs;
+    }
+    CK(cudaStreamSynchronize(B->stream));
+    int worst = GBFV_OK;
+    for (const SysState& y : B->sys)
+        if (y.phase == PH_FAILED && worst == GBFV_OK) worst = y.status;
+    return worst;
+}
+
+int gbfv_batch_system_report(const gbfv_batch* B, int i, int* status, int* steps_done, double* step_dt,
+                             int32_t* step_newton, int32_t* step_linear, int* linearizations)
+{
+    if (!B || i < 0 || i >= B->K) return GBFV_ERR_ARG;
+    const SysState& y = B->sys[i];
+    if (status) *status = y.phase == PH_FAILED ? y.status : GBFV_OK;
+    if (steps_done) *steps_done = (int)y.stepDt.size();
+    for (size_t k = 0; k < y.stepDt.size(); ++k) {
+        if (step_dt) step_dt[k] = y.stepDt[k];
+        if (step_newton) step_newton[k] = y.stepNewton[k];
+        if (step_linear) step_linear[k] = y.stepLinear[k];
+    }
+    if (linearizations) *linearizations = y.linearizations;
+    return GBFV_OK;
+}
+
+int gbfv_batch_get_stats(const gbfv_batch* B, gbfv_batch_stats* out)
+{
+    if (!B || !out) return GBFV_ERR_ARG;
+    out->num_systems = B->K;
+    out->cluster_size = B->cluster;
+    out->num_clusters = B->numClusters;
+    out->rounds = B->rounds;
+    out->graph_launches = B->graphLaunches;
+    out->kernel_launches = B->kernelLaunches;
+    out->solve_ms = B->solveMs;
+    out->solve_bytes = B->solveBytes;
+    out->solve_launches = B->solveLaunches;
+    out->linearize_ms = B->linMs;
+    return GBFV_OK;
+}
+
+void* gbfv_batch_stream(gbfv_batch* B) { return B ? (void*)B->stream : nullptr; }
 
 }  // extern "C"

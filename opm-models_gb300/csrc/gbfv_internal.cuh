@@ -97,6 +97,7 @@ struct IqBuffers {
     double* sto;   // [(e*(b+1) + k)*ldN + p], k = 0 value, 1..b derivatives
 };
 
+
 // device-side status words (bounded waits report here instead of trapping)
 struct DevStatus {
     int code;        // gbfv_status of the last device-side failure
@@ -110,6 +111,28 @@ struct DevStatus {
     unsigned long long errorBits;  // Newton error as ordered bits (max |r|)
     double resid;    // final residual max-norm
     double resid0;   // initial residual max-norm
+};
+// One system of a batch for the batched linearization / Newton kernels
+// (grid (gx, K), blockIdx.y = system): the same per-cell code as the
+// single-system kernels, with this system's buffers.
+struct LinJob {
+    DevMesh m;
+    const DevPhysics* phys;
+    double *x, *xOld;
+    int *meaning, *meaningOld;
+    IqBuffers iq;
+    double* storageOld;
+    double* residual;
+    double* jval;
+    const double* dx;
+    int* wasSwitched;
+    DevStatus* st;
+};
+// per-round state of a batched system
+struct JobState {
+    double dt;
+    int iter0;   // Newton iteration 0: refresh the storage cache
+    int active;
 };
 
 extern int64_t g_launches;
@@ -127,6 +150,11 @@ void launchCheckUpdate(int n, const double* dx, DevStatus* st, cudaStream_t s);
 void launchNewtonUpdate(const DevMesh& m, const DevPhysics* phys, const double* dx, double* x,
                         int* meaning, int* wasSwitched, UpdateParams prm, DevStatus* st,
                         cudaStream_t s);
+void launchBatchLinearize(const LinJob* jobs, const JobState* js, int K, int gx, cudaStream_t s);
+void launchBatchNewtonError(const LinJob* jobs, const JobState* js, int K, int gx, cudaStream_t s);
+void launchBatchCheckUpdate(const LinJob* jobs, const JobState* js, int K, int gx, cudaStream_t s);
+void launchBatchNewtonUpdate(const LinJob* jobs, const JobState* js, int K, int gx, UpdateParams prm,
+                             cudaStream_t s);
 void launchBoundaryStates(const DevPhysics* phys, BFace* bf, const int* bfMaterial, int nbf,
                           cudaStream_t s);
 

@@ -25,10 +25,9 @@ using D3 = Dual<3>;
 
 // ------------------------------------------------------- constraints -----
 // FvBaseLinearizer::applyConstraintsToSolution_ (fvbaselinearizer.hh:630-645)
-__global__ void kApplyConstraints(DevMesh m, double* __restrict__ x, double* __restrict__ xOld,
-                                  int* __restrict__ meaning, int* __restrict__ meaningOld)
+__device__ __forceinline__ void kApplyConstraintsBody(const DevMesh& m, double* __restrict__ x, double* __restrict__ xOld,
+                                  int* __restrict__ meaning, int* __restrict__ meaningOld, const int k)
 {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= m.numConsCells) return;
     const int p = m.consCells[k];
     const int c = m.consOf[k];
@@ -38,6 +37,12 @@ __global__ void kApplyConstraints(DevMesh m, double* __restrict__ x, double* __r
     }
     meaning[p] = m.consMeaning[c];
     meaningOld[p] = m.consMeaning[c];
+}
+
+__global__ void kApplyConstraints(DevMesh m, double* __restrict__ x, double* __restrict__ xOld,
+                                  int* __restrict__ meaning, int* __restrict__ meaningOld)
+{
+    kApplyConstraintsBody(m, x, xOld, meaning, meaningOld, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 void launchApplyConstraints(const DevMesh& m, double* x, double* xOld, int* meaning, int* meaningOld,
@@ -51,10 +56,9 @@ void launchApplyConstraints(const DevMesh& m, double* x, double* xOld, int* mean
 // ------------------------------------------------------------- K1 --------
 // ImmiscibleIntensiveQuantities::update (immiscibleintensivequantities.hh:93-151)
 // and ImmiscibleLocalResidual::computeStorage (immisciblelocalresidual.hh:75-109)
-__global__ void __launch_bounds__(256) kIqImmiscible(DevMesh m, const DevPhysics* __restrict__ phys,
-                                                     const double* __restrict__ x, IqBuffers iq)
+__device__ __forceinline__ void kIqImmiscibleBody(const DevMesh& m, const DevPhysics* __restrict__ phys,
+                                                     const double* __restrict__ x, IqBuffers iq, const int p)
 {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= m.N) return;
     const int ld = m.ldN;
     const TwoPhaseLaw L = phys->law[m.material[p]];
@@ -99,14 +103,19 @@ __global__ void __launch_bounds__(256) kIqImmiscible(DevMesh m, const DevPhysics
     }
 }
 
+__global__ void __launch_bounds__(256) kIqImmiscible(DevMesh m, const DevPhysics* __restrict__ phys,
+                                                     const double* __restrict__ x, IqBuffers iq)
+{
+    kIqImmiscibleBody(m, phys, x, iq, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
 // BlackOilIntensiveQuantities::update (blackoilintensivequantities.hh:179-462)
 // for water meaning Sw, pressure meaning Po, gas meaning Sg / Rs, zero p_c,
 // Corey relperm via updateRelperms; storage per blackoillocalresidual.hh:101-188
-__global__ void __launch_bounds__(256) kIqBlackoil(DevMesh m, const DevPhysics* __restrict__ phys,
+__device__ __forceinline__ void kIqBlackoilBody(const DevMesh& m, const DevPhysics* __restrict__ phys,
                                                    const double* __restrict__ x,
-                                                   const int* __restrict__ meaning, IqBuffers iq)
+                                                   const int* __restrict__ meaning, IqBuffers iq, const int p)
 {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= m.N) return;
     const int ld = m.ldN;
     const BlackOilPvt& T = phys->pvt;
@@ -176,6 +185,13 @@ __global__ void __launch_bounds__(256) kIqBlackoil(DevMesh m, const DevPhysics* 
     }
 }
 
+__global__ void __launch_bounds__(256) kIqBlackoil(DevMesh m, const DevPhysics* __restrict__ phys,
+                                                   const double* __restrict__ x,
+                                                   const int* __restrict__ meaning, IqBuffers iq)
+{
+    kIqBlackoilBody(m, phys, x, meaning, iq, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
 void launchIq(const DevMesh& m, const DevPhysics* phys, const double* x, const int* meaning,
               IqBuffers iq, cudaStream_t s)
 {
@@ -237,13 +253,12 @@ __device__ __forceinline__ Dual<B> darcyPhase(const Dual<B>& pI, double pJ, cons
     return fv * nrm;
 }
 
-__global__ void __launch_bounds__(128) kAssembleImmiscible(DevMesh m, const DevPhysics* __restrict__ phys,
+__device__ __forceinline__ void kAssembleImmiscibleBody(const DevMesh& m, const DevPhysics* __restrict__ phys,
                                                            IqBuffers iq, double* __restrict__ storageOld,
                                                            int iter0, double dt,
                                                            double* __restrict__ residual,
-                                                           double* __restrict__ jval)
+                                                           double* __restrict__ jval, const int p)
 {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= m.N) return;
     const int ld = m.ldN;
     D2 pI[2], rhoI[2], lamI[2];
@@ -338,13 +353,21 @@ __global__ void __launch_bounds__(128) kAssembleImmiscible(DevMesh m, const DevP
     }
 }
 
-__global__ void __launch_bounds__(128) kAssembleBlackoil(DevMesh m, const DevPhysics* __restrict__ phys,
+__global__ void __launch_bounds__(128) kAssembleImmiscible(DevMesh m, const DevPhysics* __restrict__ phys,
+                                                           IqBuffers iq, double* __restrict__ storageOld,
+                                                           int iter0, double dt,
+                                                           double* __restrict__ residual,
+                                                           double* __restrict__ jval)
+{
+    kAssembleImmiscibleBody(m, phys, iq, storageOld, iter0, dt, residual, jval, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+__device__ __forceinline__ void kAssembleBlackoilBody(const DevMesh& m, const DevPhysics* __restrict__ phys,
                                                          IqBuffers iq, double* __restrict__ storageOld,
                                                          int iter0, double dt,
                                                          double* __restrict__ residual,
-                                                         double* __restrict__ jval)
+                                                         double* __restrict__ jval, const int p)
 {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= m.N) return;
     const int ld = m.ldN;
     const BlackOilPvt& T = phys->pvt;
@@ -424,6 +447,15 @@ __global__ void __launch_bounds__(128) kAssembleBlackoil(DevMesh m, const DevPhy
         for (int v = 0; v < 3; ++v)
             jval[(ds * 9 + e * 3 + v) * ld + p] = cons ? (e == v ? 1.0 : 0.0) : res[e].d[v];
     }
+}
+
+__global__ void __launch_bounds__(128) kAssembleBlackoil(DevMesh m, const DevPhysics* __restrict__ phys,
+                                                         IqBuffers iq, double* __restrict__ storageOld,
+                                                         int iter0, double dt,
+                                                         double* __restrict__ residual,
+                                                         double* __restrict__ jval)
+{
+    kAssembleBlackoilBody(m, phys, iq, storageOld, iter0, dt, residual, jval, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 void launchAssemble(const DevMesh& m, const DevPhysics* phys, IqBuffers iq, double* storageOld,
@@ -539,11 +571,11 @@ __device__ bool adaptPv(const BlackOilPvt& T, const UpdateParams& prm, double* p
 
 // NewtonMethod::update_ / BlackOilNewtonMethod::updatePrimaryVariables_
 // (newtonmethod.hh:665-731, blackoilnewtonmethod.hh:226-427)
-__global__ void kNewtonUpdate(DevMesh m, const DevPhysics* __restrict__ phys, const double* __restrict__ dx,
-                              double* __restrict__ x, int* __restrict__ meaning,
-                              int* __restrict__ wasSwitched, UpdateParams prm, DevStatus* st)
+__device__ __forceinline__ int kNewtonUpdateCell(const DevMesh& m, const DevPhysics* __restrict__ phys,
+                                                 const double* __restrict__ dx, double* __restrict__ x,
+                                                 int* __restrict__ meaning, int* __restrict__ wasSwitched,
+                                                 const UpdateParams& prm, const int p)
 {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
     int sw = 0;
     if (p < m.N) {
         const int k = m.cflag[p];
@@ -592,6 +624,14 @@ __global__ void kNewtonUpdate(DevMesh m, const DevPhysics* __restrict__ phys, co
             meaning[p] = mm;
         }
     }
+    return sw;
+}
+
+__global__ void kNewtonUpdate(DevMesh m, const DevPhysics* __restrict__ phys, const double* __restrict__ dx,
+                              double* __restrict__ x, int* __restrict__ meaning,
+                              int* __restrict__ wasSwitched, UpdateParams prm, DevStatus* st)
+{
+    int sw = kNewtonUpdateCell(m, phys, dx, x, meaning, wasSwitched, prm, blockIdx.x * blockDim.x + threadIdx.x);
     sw = __syncthreads_count(sw);
     if (threadIdx.x == 0 && sw) atomicAdd(&st->switched, sw);
 }
@@ -601,6 +641,130 @@ void launchNewtonUpdate(const DevMesh& m, const DevPhysics* phys, const double* 
                         cudaStream_t s)
 {
     kNewtonUpdate<<<(m.N + 255) / 256, 256, 0, s>>>(m, phys, dx, x, meaning, wasSwitched, prm, st);
+    countLaunch();
+}
+
+// ------------------------------------------------------------ batched ----
+// Grid (gx, K): blockIdx.y is the system, its blocks stride over its cells and
+// run the same per-cell code as the single-system kernels above.
+__global__ void __launch_bounds__(128) kBatchConstraints(const LinJob* __restrict__ jobs,
+                                                         const JobState* __restrict__ js)
+{
+    if (!js[blockIdx.y].active) return;
+    const LinJob& j = jobs[blockIdx.y];
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < j.m.numConsCells; k += gridDim.x * blockDim.x)
+        kApplyConstraintsBody(j.m, j.x, j.xOld, j.meaning, j.meaningOld, k);
+}
+
+__global__ void __launch_bounds__(128) kBatchIq(const LinJob* __restrict__ jobs, const JobState* __restrict__ js)
+{
+    if (!js[blockIdx.y].active) return;
+    const LinJob& j = jobs[blockIdx.y];
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < j.m.N; p += gridDim.x * blockDim.x) {
+        if (j.m.model == GBFV_MODEL_IMMISCIBLE_2P)
+            kIqImmiscibleBody(j.m, j.phys, j.x, j.iq, p);
+        else
+            kIqBlackoilBody(j.m, j.phys, j.x, j.meaning, j.iq, p);
+    }
+}
+
+__global__ void __launch_bounds__(128) kBatchAssemble(const LinJob* __restrict__ jobs,
+                                                      const JobState* __restrict__ js)
+{
+    const JobState st = js[blockIdx.y];
+    if (!st.active) return;
+    const LinJob& j = jobs[blockIdx.y];
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < j.m.N; p += gridDim.x * blockDim.x) {
+        if (j.m.model == GBFV_MODEL_IMMISCIBLE_2P)
+            kAssembleImmiscibleBody(j.m, j.phys, j.iq, j.storageOld, st.iter0, st.dt, j.residual, j.jval, p);
+        else
+            kAssembleBlackoilBody(j.m, j.phys, j.iq, j.storageOld, st.iter0, st.dt, j.residual, j.jval, p);
+    }
+}
+
+void launchBatchLinearize(const LinJob* jobs, const JobState* js, int K, int gx, cudaStream_t s)
+{
+    kBatchConstraints<<<dim3(gx, K), 128, 0, s>>>(jobs, js);
+    kBatchIq<<<dim3(gx, K), 128, 0, s>>>(jobs, js);
+    kBatchAssemble<<<dim3(gx, K), 128, 0, s>>>(jobs, js);
+    countLaunch(3);
+}
+
+// max |r| over unconstrained cells of each system (as kNewtonError)
+__global__ void __launch_bounds__(256) kBatchNewtonError(const LinJob* __restrict__ jobs,
+                                                         const JobState* __restrict__ js)
+{
+    if (!js[blockIdx.y].active) return;
+    const LinJob& j = jobs[blockIdx.y];
+    __shared__ unsigned long long smax[8];
+    __shared__ int snf[8];
+    double e = 0.0;
+    int nf = 0;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < j.m.N; p += gridDim.x * blockDim.x)
+        if (j.m.cflag[p] < 0 && j.m.volume[p] > 0.0)
+            for (int k = 0; k < j.m.b; ++k) {
+                const double v = j.residual[p * j.m.b + k];
+                if (!isfinite(v)) nf = 1;
+                else e = fmax(e, fabs(v));
+            }
+    unsigned long long bits = __double_as_longlong(e);
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long ob = __shfl_down_sync(0xffffffffu, bits, o);
+        bits = ob > bits ? ob : bits;
+        nf |= __shfl_down_sync(0xffffffffu, nf, o);
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) { smax[w] = bits; snf[w] = nf; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long b = 0;
+        int f = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) { b = smax[i] > b ? smax[i] : b; f |= snf[i]; }
+        atomicMax(&j.st->errorBits, b);
+        if (f) atomicOr(&j.st->nonfinite, 1);
+    }
+}
+
+void launchBatchNewtonError(const LinJob* jobs, const JobState* js, int K, int gx, cudaStream_t s)
+{
+    kBatchNewtonError<<<dim3(gx, K), 256, 0, s>>>(jobs, js);
+    countLaunch();
+}
+
+__global__ void __launch_bounds__(256) kBatchCheckUpdate(const LinJob* __restrict__ jobs,
+                                                         const JobState* __restrict__ js)
+{
+    if (!js[blockIdx.y].active) return;
+    const LinJob& j = jobs[blockIdx.y];
+    const int n = j.m.N * j.m.b;
+    int bad = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        if (!isfinite(j.dx[i])) bad = 1;
+    bad = __syncthreads_or(bad);
+    if (bad && threadIdx.x == 0) atomicOr(&j.st->nonfinite, 1);
+}
+
+void launchBatchCheckUpdate(const LinJob* jobs, const JobState* js, int K, int gx, cudaStream_t s)
+{
+    kBatchCheckUpdate<<<dim3(gx, K), 256, 0, s>>>(jobs, js);
+    countLaunch();
+}
+
+__global__ void __launch_bounds__(256) kBatchNewtonUpdate(const LinJob* __restrict__ jobs,
+                                                          const JobState* __restrict__ js, UpdateParams prm)
+{
+    if (!js[blockIdx.y].active) return;
+    const LinJob& j = jobs[blockIdx.y];
+    int sw = 0;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < j.m.N; p += gridDim.x * blockDim.x)
+        sw += kNewtonUpdateCell(j.m, j.phys, j.dx, j.x, j.meaning, j.wasSwitched, prm, p);
+    if (sw) atomicAdd(&j.st->switched, sw);
+}
+
+void launchBatchNewtonUpdate(const LinJob* jobs, const JobState* js, int K, int gx, UpdateParams prm,
+                             cudaStream_t s)
+{
+    kBatchNewtonUpdate<<<dim3(gx, K), 256, 0, s>>>(jobs, js, prm);
     countLaunch();
 }
 

@@ -803,15 +803,14 @@ __device__ __forceinline__ void spmvRow(const KArgs<T>& a, const T* in, int i, T
     }
 }
 
+// The whole solve of one system by one team (a cluster, or the cooperative
+// grid): optional ILU(0) factorization, then BiCGStab to the tolerance.
 template <class T, int B, int MODE, int NT>
-__global__ void __launch_bounds__(NT, 1) kBicgstab(KArgs<T> a)
+__device__ __forceinline__ void bicgstabBody(const KArgs<T>& a, const Team<MODE>& tm, T* dep,
+                                             unsigned long long* mbar, unsigned char* dynSmem)
 {
-    const Team<MODE> tm;
     const int gt = tm.rank * blockDim.x + threadIdx.x, gs = tm.nblk * blockDim.x;
     const int N = a.N;
-    __shared__ T dep[MODE == SYNC_CLUSTER ? 2 * NT * 3 * B : 1];
-    __shared__ __align__(8) unsigned long long mbar[3];
-    extern __shared__ __align__(16) unsigned char dynSmem[];
     PushState ps;
     ps.ok = 1;
     const PushSmem<T, B, NT> psm(dynSmem, a.numLev);
@@ -1066,6 +1065,45 @@ timeout:
     if (gt == 0) a.st->code = GBFV_ERR_TIMEOUT;
 }
 
+template <class T, int B, int MODE, int NT>
+__global__ void __launch_bounds__(NT, 1) kBicgstab(KArgs<T> a)
+{
+    __shared__ T dep[MODE == SYNC_CLUSTER ? 2 * NT * 3 * B : 1];
+    __shared__ __align__(8) unsigned long long mbar[3];
+    extern __shared__ __align__(16) unsigned char dynSmem[];
+    const Team<MODE> tm;
+    bicgstabBody<T, B, MODE, NT>(a, tm, dep, mbar, dynSmem);
+}
+
+// Batched solve: every cluster of the grid takes systems from a work queue
+// (order[0..count), largest first) and solves each with the same body as the
+// single-system kernel, so a system's result does not depend on the batch.
+template <class T, int B, int NT>
+__global__ void __launch_bounds__(NT, 1) kBicgstabBatch(const KArgs<T>* __restrict__ args,
+                                                        const int* __restrict__ order, const int* count, int* queue)
+{
+    __shared__ T dep[2 * NT * 3 * B];
+    __shared__ __align__(8) unsigned long long mbar[3];
+    __shared__ int sNext;
+    extern __shared__ __align__(16) unsigned char dynSmem[];
+    cg::cluster_group cl = cg::this_cluster();
+    const Team<SYNC_CLUSTER> tm;
+    for (;;) {
+        if (tm.rank == 0 && threadIdx.x == 0) sNext = atomicAdd(queue, 1);
+        cl.sync();
+        const int q = *cl.map_shared_rank(&sNext, 0);
+        cl.sync();  // every block has read the index before block 0 takes the next one
+        if (q >= *count) break;
+        const KArgs<T> a = args[order[q]];
+        bicgstabBody<T, B, SYNC_CLUSTER, NT>(a, tm, dep, mbar, dynSmem);
+        cl.sync();
+        if (a.dsmem && threadIdx.x == 0)
+            for (int k = 0; k < 3; ++k)
+                asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smemAddr(&mbar[k])) : "memory");
+        cl.sync();
+    }
+}
+
 // ------------------------------------------------- launch + FP64 helpers --
 template <class T, int B, int MODE, int NT>
 static int launchOne(const KArgs<T>& a, int nblocks, cudaStream_t s)
@@ -1111,6 +1149,72 @@ int launchBicgstab(const KArgs<T>& a, int b, int mode, int nblocks, cudaStream_t
                       : launchOne<T, 3, SYNC_GRID, SOLVER_THREADS>(a, nblocks, s);
     return b == 2 ? launchOne<T, 2, SYNC_CLUSTER, NTC>(a, nblocks, s)
                   : launchOne<T, 3, SYNC_CLUSTER, NTC>(a, nblocks, s);
+}
+
+template <class T, int B>
+static int launchBatchB(const KArgs<T>* args, const int* order, const int* count, int* queue, int clusterSize,
+                        int numClusters, int maxLev, cudaStream_t s)
+{
+    constexpr int NT = clusterThreads<T>();
+    auto fn = kBicgstabBatch<T, B, NT>;
+    static bool attrSet = false;
+    if (!attrSet) {
+        cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)PushSmem<T, B, NT>::bytes(MAX_PUSH_LEVELS));
+        attrSet = true;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(clusterSize * numClusters, 1, 1);
+    cfg.blockDim = dim3(NT, 1, 1);
+    cfg.dynamicSmemBytes = PushSmem<T, B, NT>::bytes(maxLev);
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = clusterSize;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, fn, args, order, count, queue);
+    countLaunch();
+    return e == cudaSuccess ? GBFV_OK : GBFV_ERR_CUDA;
+}
+
+template <class T>
+int launchBicgstabBatch(const KArgs<T>* args, const int* order, const int* count, int* queue, int b,
+                        int clusterSize, int numClusters, int maxLev, cudaStream_t s)
+{
+    return b == 2 ? launchBatchB<T, 2>(args, order, count, queue, clusterSize, numClusters, maxLev, s)
+                  : launchBatchB<T, 3>(args, order, count, queue, clusterSize, numClusters, maxLev, s);
+}
+
+// how many clusters of the given size fit on the device at once
+template <class T>
+int maxActiveClusters(int b, int clusterSize)
+{
+    constexpr int NT = clusterThreads<T>();
+    const void* fn = b == 2 ? (const void*)kBicgstabBatch<T, 2, NT> : (const void*)kBicgstabBatch<T, 3, NT>;
+    const size_t dyn = b == 2 ? PushSmem<T, 2, NT>::bytes(MAX_PUSH_LEVELS) : PushSmem<T, 3, NT>::bytes(MAX_PUSH_LEVELS);
+    cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    cudaLaunchConfig_t cfg = {};
+    cfg.blockDim = dim3(NT, 1, 1);
+    cfg.gridDim = dim3(clusterSize, 1, 1);
+    cfg.dynamicSmemBytes = dyn;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = clusterSize;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, fn, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        n = 0;
+    }
+    return n;
 }
 
 template <class T>
@@ -1162,6 +1266,12 @@ template int maxSolverBlocks<double>(int);
 template int maxSolverBlocks<float>(int);
 template int maxClusterBlocks<double>(int);
 template int maxClusterBlocks<float>(int);
+template int launchBicgstabBatch<double>(const KArgs<double>*, const int*, const int*, int*, int, int, int, int,
+                                         cudaStream_t);
+template int launchBicgstabBatch<float>(const KArgs<float>*, const int*, const int*, int*, int, int, int, int,
+                                        cudaStream_t);
+template int maxActiveClusters<double>(int, int);
+template int maxActiveClusters<float>(int, int);
 
 // A32 = (float) A64 over all slots
 __global__ void kCastMatrix(const double* __restrict__ src, float* __restrict__ dst, long n)
@@ -1196,38 +1306,52 @@ void launchAccumulate(int n, double* x, const float* d, cudaStream_t s)
 // FP64 true residual of the refinement: r = b - A x, r32 = (float) r,
 // max|r| into st->resid (as ordered bits in errorBits)
 template <int B>
-__global__ void kResidual64(int N, int ld, int nslot, const int* __restrict__ col,
-                            const double* __restrict__ A, const double* __restrict__ b,
-                            const double* __restrict__ x, double* __restrict__ r,
-                            float* __restrict__ r32, DevStatus* st)
+__device__ __forceinline__ double residual64Row(int i, int ld, int nslot, const int* __restrict__ col,
+                                                const double* __restrict__ A, const double* __restrict__ b,
+                                                const double* __restrict__ x, double* __restrict__ r,
+                                                float* __restrict__ r32, double mx)
 {
-    double mx = 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
-        double acc[B];
+    double acc[B];
 #pragma unroll
-        for (int e = 0; e < B; ++e) acc[e] = 0.0;
-        for (int s = 0; s < nslot; ++s) {
-            const int k = col[s * ld + i];
-            if (k < 0) continue;
+    for (int e = 0; e < B; ++e) acc[e] = 0.0;
+    for (int s = 0; s < nslot; ++s) {
+        const int k = col[s * ld + i];
+        if (k < 0) continue;
 #pragma unroll
-            for (int rr = 0; rr < B; ++rr)
+        for (int rr = 0; rr < B; ++rr)
 #pragma unroll
-                for (int c = 0; c < B; ++c) acc[rr] += A[(s * B * B + rr * B + c) * ld + i] * x[k * B + c];
-        }
-#pragma unroll
-        for (int e = 0; e < B; ++e) {
-            const double ri = b[i * B + e] - acc[e];
-            r[i * B + e] = ri;
-            r32[i * B + e] = (float)ri;
-            mx = fmax(mx, fabs(ri));
-        }
+            for (int c = 0; c < B; ++c) acc[rr] += A[(s * B * B + rr * B + c) * ld + i] * x[k * B + c];
     }
+#pragma unroll
+    for (int e = 0; e < B; ++e) {
+        const double ri = b[i * B + e] - acc[e];
+        r[i * B + e] = ri;
+        r32[i * B + e] = (float)ri;
+        mx = fmax(mx, fabs(ri));
+    }
+    return mx;
+}
+
+__device__ __forceinline__ void warpMaxToStatus(double mx, DevStatus* st)
+{
     unsigned long long bits = __double_as_longlong(mx);
     for (int o = 16; o > 0; o >>= 1) {
         const unsigned long long ob = __shfl_down_sync(0xffffffffu, bits, o);
         bits = ob > bits ? ob : bits;
     }
     if ((threadIdx.x & 31) == 0) atomicMax(&st->errorBits, bits);
+}
+
+template <int B>
+__global__ void kResidual64(int N, int ld, int nslot, const int* __restrict__ col,
+                            const double* __restrict__ A, const double* __restrict__ b,
+                            const double* __restrict__ x, double* __restrict__ r,
+                            float* __restrict__ r32, DevStatus* st)
+{
+    double mx = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
+        mx = residual64Row<B>(i, ld, nslot, col, A, b, x, r, r32, mx);
+    warpMaxToStatus(mx, st);
 }
 
 void launchResidual64(int N, int ld, int nslot, int b, const int* col, const double* A, const double* rhs,
@@ -1239,6 +1363,67 @@ void launchResidual64(int N, int ld, int nslot, int b, const int* col, const dou
         kResidual64<2><<<nb, 256, 0, s>>>(N, ld, nslot, col, A, rhs, x, r, r32, st);
     else
         kResidual64<3><<<nb, 256, 0, s>>>(N, ld, nslot, col, A, rhs, x, r, r32, st);
+    countLaunch();
+}
+
+// ------------------------------------------- batched refinement helpers --
+// Grid (gx, K): blockIdx.y is the system, blocks of a system stride over its
+// rows; systems with active[k] == 0 are skipped.
+__global__ void kBatchCast(const SolveJob* __restrict__ jobs, const int* __restrict__ active)
+{
+    const SolveJob& j = jobs[blockIdx.y];
+    if (!active[blockIdx.y]) return;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < j.nval; i += (long)gridDim.x * blockDim.x)
+        j.A32[i] = (float)j.A64[i];
+}
+
+__global__ void kBatchZeroX(const SolveJob* __restrict__ jobs, const int* __restrict__ active)
+{
+    const SolveJob& j = jobs[blockIdx.y];
+    if (!active[blockIdx.y]) return;
+    const int n = j.N * j.b;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) j.xref[i] = 0.0;
+}
+
+__global__ void kBatchAccumulate(const SolveJob* __restrict__ jobs, const int* __restrict__ active)
+{
+    const SolveJob& j = jobs[blockIdx.y];
+    if (!active[blockIdx.y]) return;
+    const int n = j.N * j.b;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        j.xref[i] += (double)j.dx32[i];
+}
+
+template <int B>
+__global__ void kBatchResidual64(const SolveJob* __restrict__ jobs, const int* __restrict__ active)
+{
+    const SolveJob& j = jobs[blockIdx.y];
+    if (!active[blockIdx.y] || j.b != B) return;
+    double mx = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < j.N; i += gridDim.x * blockDim.x)
+        mx = residual64Row<B>(i, j.ld, j.nslot, j.col, j.A64, j.rhs, j.xref, j.rref, j.r32, mx);
+    warpMaxToStatus(mx, j.st);
+}
+
+void launchBatchCast(const SolveJob* jobs, const int* active, int K, int gx, cudaStream_t s)
+{
+    kBatchCast<<<dim3(gx, K), 256, 0, s>>>(jobs, active);
+    countLaunch();
+}
+void launchBatchZeroX(const SolveJob* jobs, const int* active, int K, int gx, cudaStream_t s)
+{
+    kBatchZeroX<<<dim3(gx, K), 256, 0, s>>>(jobs, active);
+    countLaunch();
+}
+void launchBatchAccumulate(const SolveJob* jobs, const int* active, int K, int gx, cudaStream_t s)
+{
+    kBatchAccumulate<<<dim3(gx, K), 256, 0, s>>>(jobs, active);
+    countLaunch();
+}
+void launchBatchResidual64(const SolveJob* jobs, const int* active, int K, int gx, int b, cudaStream_t s)
+{
+    if (b == 2) kBatchResidual64<2><<<dim3(gx, K), 256, 0, s>>>(jobs, active);
+    else kBatchResidual64<3><<<dim3(gx, K), 256, 0, s>>>(jobs, active);
     countLaunch();
 }
 

@@ -48,8 +48,34 @@ struct KArgs {
 };
 
 template <class T> int launchBicgstab(const KArgs<T>& a, int b, int mode, int nblocks, cudaStream_t s);
+
+// One system of a batched mixed-precision refinement (FP64 true residual of
+// the Newton system, FP32 inner solve)
+struct SolveJob {
+    int N, ld, nslot, b;
+    long nval;              // nslot*b*b*ld matrix entries
+    const int* col;
+    const double* A64;      // FP64 Jacobian (block-ELL)
+    float* A32;             // its FP32 copy
+    const double* rhs;      // FP64 right-hand side (the Newton residual)
+    double* xref;           // FP64 accumulated solution
+    double* rref;           // FP64 true residual
+    float* r32;             // its FP32 copy: right-hand side of the inner solve
+    const float* dx32;      // inner solution added to xref
+    DevStatus* st;
+};
+void launchBatchCast(const SolveJob* jobs, const int* active, int K, int gx, cudaStream_t s);
+void launchBatchZeroX(const SolveJob* jobs, const int* active, int K, int gx, cudaStream_t s);
+void launchBatchAccumulate(const SolveJob* jobs, const int* active, int K, int gx, cudaStream_t s);
+void launchBatchResidual64(const SolveJob* jobs, const int* active, int K, int gx, int b, cudaStream_t s);
 template <class T> int maxSolverBlocks(int b);
 template <class T> int maxClusterBlocks(int b);
+// batched solve: clusters of clusterSize blocks take systems args[order[q]],
+// q = 0..*count-1 (device memory), from the queue counter (zero before the launch)
+template <class T>
+int launchBicgstabBatch(const KArgs<T>* args, const int* order, const int* count, int* queue, int b,
+                        int clusterSize, int numClusters, int maxLev, cudaStream_t s);
+template <class T> int maxActiveClusters(int b, int clusterSize);
 void launchCastMatrix(const double* src, float* dst, long n, cudaStream_t s);
 void launchAccumulate(int n, double* x, const float* d, cudaStream_t s);
 void launchResidual64(int N, int ld, int nslot, int b, const int* col, const double* A, const double* rhs,

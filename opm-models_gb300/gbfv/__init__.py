@@ -12,7 +12,7 @@ import numpy as np
 
 from . import capi, problems  # noqa: F401
 
-__all__ = ["Context", "LinearSolver", "capi", "problems", "default_params"]
+__all__ = ["Context", "LinearSolver", "Batch", "capi", "problems", "default_params"]
 
 default_params = capi.default_params
 
@@ -28,15 +28,19 @@ def _i(a):
 class Context:
     """One grid on the GPU: linearizer + BiCGStab/ILU0 backend + Newton."""
 
-    def __init__(self, problem, params=None, set_initial=True):
+    def __init__(self, problem, params=None, set_initial=True, handle=None):
         self.lib = capi.load()
         self.problem = problem
         self.params = params if params is not None else capi.default_params()
-        self._s = problem.struct()
-        st = C.c_int()
-        self.h = self.lib.gbfv_create(C.byref(self._s), C.byref(self.params), C.byref(st))
-        if not self.h:
-            capi.check(st.value, "gbfv_create")
+        self._owned = handle is None
+        if handle is None:
+            self._s = problem.struct()
+            st = C.c_int()
+            self.h = self.lib.gbfv_create(C.byref(self._s), C.byref(self.params), C.byref(st))
+            if not self.h:
+                capi.check(st.value, "gbfv_create")
+        else:
+            self.h = handle
         n, b, nnz = C.c_int(), C.c_int(), C.c_int()
         self.lib.gbfv_dims(self.h, C.byref(n), C.byref(b), C.byref(nnz))
         self.N, self.b, self.nnz = n.value, b.value, nnz.value
@@ -45,7 +49,8 @@ class Context:
 
     def close(self):
         if getattr(self, "h", None):
-            self.lib.gbfv_destroy(self.h)
+            if self._owned:
+                self.lib.gbfv_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -142,6 +147,10 @@ class Context:
         return {"mode": "cluster" if mode.value == 1 else "grid", "blocks": nb.value,
                 "tune_ms": ms[:nt.value].tolist()}
 
+    def set_solver_config(self, precision, mode, blocks):
+        """Fix the persistent solver's launch configuration (mode 1 = cluster)."""
+        capi.check(self.lib.gbfv_set_solver_config(self.h, precision, mode, blocks), "gbfv_set_solver_config")
+
     def reset_kernel_stats(self):
         self.lib.gbfv_reset_kernel_stats(self.h)
 
@@ -181,6 +190,67 @@ class LinearSolver:
     def close(self):
         if getattr(self, "h", None):
             self.lib.gbfv_linsolver_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many independent systems advanced together (gbfv_batch_*): one batched
+    launch per phase for all of them, each phase a replayed CUDA graph, one
+    persistent BiCGStab/ILU0 launch whose clusters take systems from a queue."""
+
+    def __init__(self, problems, params=None, cluster_size=0, set_initial=True):
+        self.lib = capi.load()
+        self.problems = list(problems)
+        self.params = params if params is not None else capi.default_params()
+        self._structs = [p.struct() for p in self.problems]
+        arr = (capi.Problem * len(self._structs))(*self._structs)
+        st = C.c_int()
+        self.h = self.lib.gbfv_batch_create(arr, len(self._structs), C.byref(self.params), cluster_size,
+                                            C.byref(st))
+        if not self.h:
+            capi.check(st.value, "gbfv_batch_create")
+        self.systems = [Context(p, self.params, set_initial=False, handle=self.lib.gbfv_batch_system(self.h, i))
+                        for i, p in enumerate(self.problems)]
+        if set_initial:
+            for c, p in zip(self.systems, self.problems):
+                if p.init_pv is not None:
+                    c.set_solution(p.init_pv, p.init_meaning)
+
+    def __len__(self):
+        return len(self.systems)
+
+    def time_integration(self, steps, dt0, end_time=1e100, fixed_dt=False):
+        return self.lib.gbfv_batch_time_integration(self.h, steps, dt0, end_time, int(fixed_dt))
+
+    def report(self, i, max_steps=4096):
+        st, n, nl = C.c_int(), C.c_int(), C.c_int()
+        sdt = np.zeros(max_steps)
+        sn = np.zeros(max_steps, np.int32)
+        sl = np.zeros(max_steps, np.int32)
+        capi.check(self.lib.gbfv_batch_system_report(self.h, i, C.byref(st), C.byref(n), _d(sdt), _i(sn), _i(sl),
+                                                     C.byref(nl)), "gbfv_batch_system_report")
+        k = n.value
+        return st.value, sdt[:k].copy(), sn[:k].copy(), sl[:k].copy(), nl.value
+
+    def stats(self):
+        s = capi.BatchStats()
+        capi.check(self.lib.gbfv_batch_get_stats(self.h, C.byref(s)), "gbfv_batch_get_stats")
+        return {f: getattr(s, f) for f, _ in capi.BatchStats._fields_}
+
+    def stream(self):
+        return self.lib.gbfv_batch_stream(self.h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            for c in self.systems:
+                c.h = None
+            self.lib.gbfv_batch_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -148,6 +148,13 @@ def as_ptr(a, ctype):
     return a.ctypes.data_as(C.POINTER(ctype))
 
 
+class BatchStats(C.Structure):
+    _fields_ = [("num_systems", C.c_int32), ("cluster_size", C.c_int32), ("num_clusters", C.c_int32),
+                ("pad", C.c_int32), ("rounds", C.c_int64), ("graph_launches", C.c_int64),
+                ("kernel_launches", C.c_int64), ("solve_launches", C.c_int64), ("solve_ms", C.c_double),
+                ("solve_bytes", C.c_double), ("linearize_ms", C.c_double)]
+
+
 _LIB = None
 
 
@@ -198,6 +205,16 @@ def load():
         "gbfv_solver_phase_ns": (C.c_int, [vp, C.POINTER(C.c_uint64)]),
         "gbfv_solver_config": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), dp,
                                          C.POINTER(C.c_int)]),
+        "gbfv_set_solver_config": (C.c_int, [vp, C.c_int, C.c_int, C.c_int]),
+        "gbfv_batch_create": (vp, [C.POINTER(Problem), C.c_int, C.POINTER(Params), C.c_int,
+                                   C.POINTER(C.c_int)]),
+        "gbfv_batch_destroy": (C.c_int, [vp]),
+        "gbfv_batch_system": (vp, [vp, C.c_int]),
+        "gbfv_batch_time_integration": (C.c_int, [vp, C.c_int, C.c_double, C.c_double, C.c_int]),
+        "gbfv_batch_system_report": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), dp, ip, ip,
+                                               C.POINTER(C.c_int)]),
+        "gbfv_batch_get_stats": (C.c_int, [vp, C.POINTER(BatchStats)]),
+        "gbfv_batch_stream": (vp, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
