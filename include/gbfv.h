@@ -380,11 +380,39 @@ gbfv_ctx* gbfv_batch_system(gbfv_batch* batch, int i);
  * semantics); returns the first failing system's status or GBFV_OK      */
 int gbfv_batch_time_integration(gbfv_batch* batch, int num_steps, double dt0,
                                 double end_time, int fixed_dt);
+/* autotuner of the batched solve: linearizes every system at its current
+ * state, times one batched solve for each cluster size 2, 4, 8, 16 (up to
+ * the device limit) and keeps the fastest; the systems' states are not
+ * changed.  ms[k] = the solve time of candidate k (up to 8)              */
+int gbfv_batch_autotune(gbfv_batch* batch, double dt, int* cluster_size, double* ms, int* num_candidates);
 int gbfv_batch_system_report(const gbfv_batch* batch, int i, int* status, int* steps_done,
                              double* step_dt, int32_t* step_newton, int32_t* step_linear,
                              int* linearizations);
 int gbfv_batch_get_stats(const gbfv_batch* batch, gbfv_batch_stats* out);
 void* gbfv_batch_stream(gbfv_batch* batch);
+
+/* ------------------------------------------------------------------ */
+/* Serving: a batch whose slots are filled and emptied while it runs
+ * (continuous batching).  A request (one system, its initial state and
+ * its time steps) is admitted into a free slot between rounds; every
+ * gbfv_serve_step runs one round for all running systems, so requests that
+ * arrive while others are on the GPU join at the next round and their work
+ * overlaps on the device.  A finished slot keeps its state (read it through
+ * gbfv_batch_system) until gbfv_serve_release frees its device memory.
+ * Admission by HBM footprint is the caller's policy, with
+ * gbfv_footprint_bytes as the estimate of one system.                    */
+/* estimated device bytes of one system (context + solver buffers)        */
+int64_t gbfv_footprint_bytes(int num_cells, int block_size, int dim);
+gbfv_batch* gbfv_serve_create(int capacity, int model, const gbfv_params* params,
+                              int cluster_size, int max_cells, int* status);
+int gbfv_serve_admit(gbfv_batch* server, const gbfv_problem* problem, const double* pv,
+                     const int32_t* meaning, int num_steps, double dt0, int fixed_dt, int* slot);
+/* one round; running = systems still iterating                           */
+int gbfv_serve_step(gbfv_batch* server, int* running);
+/* state: 0 empty, 1 running, 2 done, 3 failed (status = its error)       */
+int gbfv_serve_slot(const gbfv_batch* server, int slot, int* state, int* status);
+int gbfv_serve_release(gbfv_batch* server, int slot);
+int64_t gbfv_serve_footprint(const gbfv_batch* server);
 
 /* ------------------------------------------------------------------ */
 /* Allocation-free Newton error.  No counterpart in the reference: its

@@ -294,6 +294,64 @@ void buildOrder(int N, const std::vector<std::vector<int>>& lower, std::vector<i
     }
 }
 
+// Which levels of a sweep need the cluster-wide level barrier.  A block
+// pushes the results of level l into the consumer block's dependency buffer
+// (l+1) mod PUSH_BUFFERS, which the consumer last read at level
+// l+1-PUSH_BUFFERS; the push is safe once the consumer has finished that
+// level.  Blocks finish their levels in order (a block-local barrier per
+// level); a row starts after its block finished the previous level and after
+// its dependencies were computed.  know[Y] = the latest level that block Y is
+// known to have finished when a row starts, propagated along those two
+// orderings and along the cluster barriers placed so far.  Where a push is
+// not covered, a cluster barrier is placed after the previous level.
+// barrierAfter[l] (level index, in the sweep's own order) is the result.
+void placeLevelBarriers(const SolverData& S, int C, const std::vector<int>& lev, bool forward,
+                        std::vector<char>& barrierAfter)
+{
+    const int N = S.N, ld = S.ldN, dim = S.dim, nl = (int)S.levPtr.size() - 1, D = PUSH_BUFFERS;
+    barrierAfter.assign(nl, 0);
+    auto owner = [&](int p) { return ((p - S.levPtr[lev[p]]) >> 5) % C; };
+    std::vector<int> K((size_t)C * C, -1), Knew;   // K[X*C + Y]: known finished step of Y when X finished its last
+    std::vector<int> know((size_t)N * C, -1);
+    std::vector<int> acc(C);
+    for (int step = 0; step < nl; ++step) {
+        const int l = forward ? step : nl - 1 - step;
+        auto attempt = [&]() -> bool {
+            Knew = K;
+            for (int X = 0; X < C; ++X) Knew[(size_t)X * C + X] = step;
+            for (int p = S.levPtr[l]; p < S.levPtr[l + 1]; ++p) {
+                const int X = owner(p);
+                for (int Y = 0; Y < C; ++Y) acc[Y] = K[(size_t)X * C + Y];
+                for (int q = 0; q < dim; ++q) {
+                    const int sl = forward ? q : 2 * dim - q;   // dependencies of p in this sweep
+                    const int j = S.colHost[(size_t)sl * ld + p];
+                    if (j < 0) continue;
+                    const int* kj = &know[(size_t)j * C];
+                    for (int Y = 0; Y < C; ++Y) acc[Y] = std::max(acc[Y], kj[Y]);
+                }
+                for (int q = 0; q < dim; ++q) {
+                    const int sl = forward ? dim + 1 + q : q;   // consumers of p
+                    const int u = S.colHost[(size_t)sl * ld + p];
+                    if (u >= 0 && acc[owner(u)] < step + 1 - D) return false;
+                }
+                std::copy(acc.begin(), acc.end(), &know[(size_t)p * C]);
+                int* kx = &Knew[(size_t)X * C];
+                for (int Y = 0; Y < C; ++Y) kx[Y] = std::max(kx[Y], acc[Y]);
+                kx[X] = step;
+            }
+            return true;
+        };
+        if (!attempt()) {
+            // a cluster barrier after the previous step: every block knows every
+            // block finished it
+            barrierAfter[forward ? l - 1 : l + 1] = 1;
+            for (int& v : K) v = std::max(v, step - 1);
+            attempt();
+        }
+        K.swap(Knew);
+    }
+}
+
 // Push targets of the cluster sweeps for cluster size C, G level groups and
 // NT threads per block: for each row and each neighbour in the dependency
 // direction, the consumer's block and the offset of its slot (see
@@ -330,6 +388,18 @@ int buildPushTargets(SolverData& S, int C, int G, int NT)
             }
         }
     }
+    if (!getenv("GBFV_LEVEL_BARRIER")) {
+        std::vector<char> barF, barB;
+        placeLevelBarriers(S, C, lev, true, barF);
+        placeLevelBarriers(S, C, lev, false, barB);
+        for (int r = 0; r < C; ++r)
+            for (int l = 0; l < nl; ++l) {
+                if (barF[l]) hV[((size_t)r * nl + l) * 2] |= PUSH_BARRIER_FLAG;
+                if (barB[l]) hV[((size_t)r * nl + l) * 2 + 1] |= PUSH_BARRIER_FLAG;
+            }
+    }
+    else
+        for (int& v : hV) v |= PUSH_BARRIER_FLAG;
     cudaFree(S.pushL);
     cudaFree(S.pushU);
     cudaFree(S.levVals);
@@ -1697,6 +1767,9 @@ struct GraphSet {
 
 struct gbfv_batch {
     int K = 0, b = 0, model = 0, precision = GBFV_PREC_MIXED;
+    int dynamic = 0;          // slots admitted and released while running (serving)
+    int maxCells = 0;         // largest admissible system of a dynamic batch
+    int64_t footprint = 0;    // estimated device bytes of the admitted systems
     gbfv_params prm;
     cudaStream_t stream = nullptr;
     std::vector<gbfv_ctx*> ctx;
@@ -1774,6 +1847,11 @@ double bitsToDouble(unsigned long long bits)
 int buildBatchGraphs(gbfv_batch* B)
 {
     const int K = B->K;
+    for (GraphSet* g : {&B->gLin, &B->gCheck, &B->gUpd, &B->gRes0, &B->gKry, &B->gRef})
+        if (g->exec) {
+            cudaGraphExecDestroy(g->exec);
+            g->exec = nullptr;
+        }
     cudaStream_t s = B->stream;
     int st;
     // L: constraints, IQ, assembly, Newton error; statuses to the host
@@ -2096,7 +2174,9 @@ int batchRound(gbfv_batch* B)
             batchFail(B, i, GBFV_ERR_NONFINITE);
         }
     }
-    if ((rs = replay(B, B->gUpd, false))) return rs;
+    // synchronised: the graph reads the pinned per-system state, which the
+    // next round rewrites
+    if ((rs = replay(B, B->gUpd, true))) return rs;
     for (int i = 0; i < K; ++i)
         if (B->hJs[i].active) {
             SysState& y = B->sys[i];
@@ -2131,8 +2211,45 @@ void freeBatch(gbfv_batch* B)
     if (B->evA) cudaEventDestroy(B->evA);
     if (B->evB) cudaEventDestroy(B->evB);
     if (B->stream) cudaStreamDestroy(B->stream);
-    for (gbfv_ctx* C : B->ctx) gbfv_destroy(C);
+    for (gbfv_ctx* C : B->ctx)
+        if (C) gbfv_destroy(C);
     delete B;
+}
+
+// the batched kernels' view of system i
+void fillJobs(gbfv_batch* B, int i, LinJob& j, SolveJob& s)
+{
+    gbfv_ctx* C = B->ctx[i];
+    std::memset(&j, 0, sizeof(j));
+    std::memset(&s, 0, sizeof(s));
+    j.m = C->mesh;
+    j.phys = C->dphys;
+    j.x = C->x;
+    j.xOld = C->xOld;
+    j.meaning = C->meaning;
+    j.meaningOld = C->meaningOld;
+    j.iq = C->iq;
+    j.storageOld = C->storageOld;
+    j.residual = C->residual;
+    j.jval = C->jval;
+    j.dx = B->precision == GBFV_PREC_MIXED ? C->S.xref : C->S.v64[0];
+    j.wasSwitched = C->wasSwitched;
+    j.st = &B->dSt[i];
+    SolverData& S = C->S;
+    s.N = S.N;
+    s.ld = S.ldN;
+    s.nslot = S.nslot;
+    s.b = S.b;
+    s.nval = (long)S.nslot * S.b * S.b * S.ldN;
+    s.col = S.col;
+    s.A64 = C->jval;
+    s.A32 = S.A32;
+    s.rhs = C->residual;
+    s.xref = S.xref;
+    s.rref = S.rref;
+    s.r32 = S.v32[0];
+    s.dx32 = S.v32[1];
+    s.st = &B->dSt[i];
 }
 
 int setupBatch(gbfv_batch* B, int cluster)
@@ -2154,39 +2271,18 @@ int setupBatch(gbfv_batch* B, int cluster)
     int maxN = 1, maxLev = 1, maxC = 16;
     for (int i = 0; i < K; ++i) {
         gbfv_ctx* C = B->ctx[i];
-        LinJob& j = lj[i];
-        j.m = C->mesh;
-        j.phys = C->dphys;
-        j.x = C->x;
-        j.xOld = C->xOld;
-        j.meaning = C->meaning;
-        j.meaningOld = C->meaningOld;
-        j.iq = C->iq;
-        j.storageOld = C->storageOld;
-        j.residual = C->residual;
-        j.jval = C->jval;
-        j.dx = B->precision == GBFV_PREC_MIXED ? C->S.xref : C->S.v64[0];
-        j.wasSwitched = C->wasSwitched;
-        j.st = &B->dSt[i];
-        SolveJob& s = sj[i];
-        SolverData& S = C->S;
-        s.N = S.N;
-        s.ld = S.ldN;
-        s.nslot = S.nslot;
-        s.b = S.b;
-        s.nval = (long)S.nslot * S.b * S.b * S.ldN;
-        s.col = S.col;
-        s.A64 = C->jval;
-        s.A32 = S.A32;
-        s.rhs = C->residual;
-        s.xref = S.xref;
-        s.rref = S.rref;
-        s.r32 = S.v32[0];
-        s.dx32 = S.v32[1];
-        s.st = &B->dSt[i];
+        if (!C) continue;
+        fillJobs(B, i, lj[i], sj[i]);
         maxN = std::max(maxN, C->N);
-        maxLev = std::max(maxLev, (int)S.levPtr.size() - 1);
-        maxC = std::min(maxC, S.maxCluster[B->precision == GBFV_PREC_MIXED ? 1 : 0]);
+        maxLev = std::max(maxLev, (int)C->S.levPtr.size() - 1);
+        maxC = std::min(maxC, C->S.maxCluster[B->precision == GBFV_PREC_MIXED ? 1 : 0]);
+    }
+    if (B->dynamic) {
+        // slots are filled later: size the launches for any admissible system
+        maxN = std::max(maxN, B->maxCells);
+        maxLev = MAX_PUSH_LEVELS;
+        maxC = std::min(maxC, B->precision == GBFV_PREC_MIXED ? maxClusterBlocks<float>(B->b)
+                                                              : maxClusterBlocks<double>(B->b));
     }
     B->maxLev = std::min(maxLev, MAX_PUSH_LEVELS);
     B->cluster = cluster > 0 ? std::min(cluster, maxC) : std::min(8, maxC);
@@ -2289,6 +2385,55 @@ int gbfv_batch_time_integration(gbfv_batch* B, int num_steps, double dt0, double
     return worst;
 }
 
+int gbfv_batch_autotune(gbfv_batch* B, double dt, int* cluster_out, double* ms_out, int* num_out)
+{
+    if (!B || !(dt > 0)) return GBFV_ERR_ARG;
+    for (int i = 0; i < B->K; ++i) CK(cudaStreamSynchronize(B->ctx[i]->stream));
+    int maxC = 16;
+    for (gbfv_ctx* C : B->ctx) maxC = std::min(maxC, C->S.maxCluster[B->precision == GBFV_PREC_MIXED ? 1 : 0]);
+    // linearize every system at its current state (Newton iteration 0)
+    for (int i = 0; i < B->K; ++i) {
+        B->hJs[i].active = 1;
+        B->hJs[i].dt = dt;
+        B->hJs[i].iter0 = 1;
+    }
+    int rs = replay(B, B->gLin, true);
+    if (rs) return rs;
+    const double ms0 = B->solveMs;
+    double best = 1e300;
+    int pick = B->cluster, n = 0;
+    for (int c = 2; c <= maxC; c *= 2) {
+        B->cluster = c;
+        B->numClusters = std::max(1, std::min(B->K, B->precision == GBFV_PREC_MIXED ? maxActiveClusters<float>(B->b, c)
+                                                                                  : maxActiveClusters<double>(B->b, c)));
+        if (B->gKry.exec) cudaGraphExecDestroy(B->gKry.exec);
+        B->gKry.exec = nullptr;
+        if ((rs = buildBatchGraphs(B))) return rs;
+        for (SysState& y : B->sys) {
+            y = SysState();
+            y.phase = PH_SOLVE;
+        }
+        const double before = B->solveMs;
+        if ((rs = batchSolvePhase(B))) return rs;
+        const double ms = B->solveMs - before;
+        if (ms_out && n < 8) ms_out[n] = ms;
+        n++;
+        if (ms < best) { best = ms; pick = c; }
+    }
+    B->solveMs = ms0;
+    B->solveBytes = 0;
+    B->solveLaunches = 0;
+    B->cluster = pick;
+    B->numClusters = std::max(1, std::min(B->K, B->precision == GBFV_PREC_MIXED ? maxActiveClusters<float>(B->b, pick)
+                                                                             : maxActiveClusters<double>(B->b, pick)));
+    if ((rs = buildBatchGraphs(B))) return rs;
+    for (SysState& y : B->sys) y = SysState();
+    CK(cudaStreamSynchronize(B->stream));
+    if (cluster_out) *cluster_out = pick;
+    if (num_out) *num_out = n;
+    return GBFV_OK;
+}
+
 int gbfv_batch_system_report(const gbfv_batch* B, int i, int* status, int* steps_done, double* step_dt,
                              int32_t* step_newton, int32_t* step_linear, int* linearizations)
 {
@@ -2322,5 +2467,129 @@ int gbfv_batch_get_stats(const gbfv_batch* B, gbfv_batch_stats* out)
 }
 
 void* gbfv_batch_stream(gbfv_batch* B) { return B ? (void*)B->stream : nullptr; }
+
+// ---------------------------------------------------------------- serving
+int64_t gbfv_footprint_bytes(int num_cells, int block_size, int dim)
+{
+    if (num_cells <= 0 || (block_size != 2 && block_size != 3) || (dim != 2 && dim != 3)) return -1;
+    const int64_t b = block_size, bb = b * b, ns = 2 * dim + 1, nd = 2 * dim;
+    const int64_t iq = (b == 2 ? 6 + 12 : 11 + 30) + b * (b + 1);
+    // solver: FP64 + FP32 factors, FP32 matrix, Krylov vectors, columns, push tables
+    const int64_t solver = dim * bb * 12 + bb * 12 + ns * bb * 4 + 6 * b * 8 + 7 * b * 4 + 2 * b * 8 + ns * 4 + 6 * 4;
+    // context: state vectors, Jacobian, IQ buffers, mesh (faces, cells), snapshot
+    const int64_t ctx = 5 * b * 8 + ns * bb * 8 + 3 * 4 + iq * 8 + nd * (4 + 5 * 8) + 64 + b * 8 + 8 + 64;
+    return (int64_t)num_cells * (solver + ctx) + (4 << 20);
+}
+
+gbfv_batch* gbfv_serve_create(int capacity, int model, const gbfv_params* params, int cluster_size, int max_cells,
+                              int* status)
+{
+    auto fail = [&](gbfv_batch* B, int st) -> gbfv_batch* {
+        if (status) *status = st;
+        freeBatch(B);
+        return nullptr;
+    };
+    if (capacity <= 0 || max_cells <= 0 || (model != GBFV_MODEL_IMMISCIBLE_2P && model != GBFV_MODEL_BLACKOIL_3P))
+        return fail(nullptr, GBFV_ERR_ARG);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(nullptr, GBFV_ERR_NO_DEVICE);
+    gbfv_batch* B = new gbfv_batch();
+    if (params) B->prm = *params;
+    else gbfv_default_params(&B->prm);
+    B->precision = B->prm.precision;
+    B->K = capacity;
+    B->dynamic = 1;
+    B->maxCells = max_cells;
+    B->model = model;
+    B->b = model == GBFV_MODEL_IMMISCIBLE_2P ? 2 : 3;
+    B->ctx.assign(capacity, nullptr);
+    B->sys.resize(capacity);
+    const int st = setupBatch(B, cluster_size);
+    if (st) return fail(B, st);
+    if (status) *status = GBFV_OK;
+    return B;
+}
+
+int gbfv_serve_admit(gbfv_batch* B, const gbfv_problem* prob, const double* pv, const int32_t* meaning,
+                     int num_steps, double dt0, int fixed_dt, int* slot)
+{
+    if (!B || !B->dynamic || !prob || !pv || num_steps <= 0 || !(dt0 > 0) || !slot) return GBFV_ERR_ARG;
+    if (prob->num_cells > B->maxCells) {
+        setError("system larger than the server's max_cells");
+        return GBFV_ERR_ARG;
+    }
+    int i = -1;
+    for (int k = 0; k < B->K; ++k)
+        if (!B->ctx[k]) { i = k; break; }
+    if (i < 0) {
+        setError("no free slot");
+        return GBFV_ERR_UNSUPPORTED;
+    }
+    int st = GBFV_OK;
+    gbfv_ctx* C = gbfv_create(prob, &B->prm, &st);
+    if (!C) return st ? st : GBFV_ERR_ARG;
+    if (C->b != B->b || C->model != B->model) {
+        gbfv_destroy(C);
+        setError("the system's model differs from the server's");
+        return GBFV_ERR_ARG;
+    }
+    if ((st = gbfv_set_solution(C, pv, meaning))) {
+        gbfv_destroy(C);
+        return st;
+    }
+    // the same solver launch configuration as the rest of the batch
+    const int k = B->precision == GBFV_PREC_MIXED ? 1 : 0;
+    C->S.mode[k] = SYNC_CLUSTER;
+    C->S.nblk[k] = B->cluster;
+    C->S.tuned[k] = 1;
+    B->ctx[i] = C;
+    LinJob lj;
+    SolveJob sj;
+    fillJobs(B, i, lj, sj);
+    CK(cudaMemcpy(&B->dLin[i], &lj, sizeof(LinJob), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(&B->dSol[i], &sj, sizeof(SolveJob), cudaMemcpyHostToDevice));
+    SysState& y = B->sys[i];
+    y = SysState();
+    y.numSteps = num_steps;
+    y.dt = y.dt0 = dt0;
+    y.fixedDt = fixed_dt;
+    y.phase = PH_LIN;
+    B->footprint += gbfv_footprint_bytes(C->N, C->b, C->dim);
+    *slot = i;
+    return GBFV_OK;
+}
+
+int gbfv_serve_step(gbfv_batch* B, int* running)
+{
+    if (!B) return GBFV_ERR_ARG;
+    const int rs = batchRound(B);
+    int n = 0;
+    for (const SysState& y : B->sys) n += y.phase == PH_LIN;
+    if (running) *running = n;
+    return rs;
+}
+
+int gbfv_serve_slot(const gbfv_batch* B, int slot, int* state, int* status)
+{
+    if (!B || slot < 0 || slot >= B->K) return GBFV_ERR_ARG;
+    const SysState& y = B->sys[slot];
+    if (state) *state = !B->ctx[slot] ? 0 : (y.phase == PH_DONE ? 2 : (y.phase == PH_FAILED ? 3 : 1));
+    if (status) *status = y.phase == PH_FAILED ? y.status : GBFV_OK;
+    return GBFV_OK;
+}
+
+int gbfv_serve_release(gbfv_batch* B, int slot)
+{
+    if (!B || !B->dynamic || slot < 0 || slot >= B->K || !B->ctx[slot]) return GBFV_ERR_ARG;
+    CK(cudaStreamSynchronize(B->stream));
+    gbfv_ctx* C = B->ctx[slot];
+    B->footprint -= gbfv_footprint_bytes(C->N, C->b, C->dim);
+    gbfv_destroy(C);
+    B->ctx[slot] = nullptr;
+    B->sys[slot] = SysState();
+    return GBFV_OK;
+}
+
+int64_t gbfv_serve_footprint(const gbfv_batch* B) { return B ? B->footprint : -1; }
 
 }  // extern "C"

@@ -465,9 +465,9 @@ __device__ __forceinline__ void pushLocal(T* dst, const T (&v)[B], unsigned mbar
 }
 
 struct PushState {
-    unsigned mb[2];   // shared addresses of the two data mbarriers
-    unsigned ph[2];   // parity of the next phase to wait for
-    unsigned dep;     // shared address of the dependency buffer [2][NT][3][B]
+    unsigned mb[PUSH_BUFFERS];   // shared addresses of the data mbarriers, one per dependency buffer
+    unsigned ph[PUSH_BUFFERS];   // parity of the next phase to wait for
+    unsigned dep;     // shared address of the dependency buffers [PUSH_BUFFERS][NT][3][B]
     unsigned lev;     // shared address of the level-done mbarrier (C arrivals)
     unsigned levPh;
     int ok;
@@ -564,24 +564,30 @@ __device__ __forceinline__ void cpWaitAll() { asm volatile("cp.async.wait_all;" 
 // per level (forward and backward sweep).
 template <class T, int B, int NT>
 struct PushSmem {
+    static constexpr int NDEP = PUSH_BUFFERS * NT * 3 * B;  // dependency buffers
     static constexpr int NF = 4 * B * B + 3 * B;  // 3 off-diagonal blocks, pivot, 3 vectors
     static constexpr int NI = 6;                   // 3 neighbour columns, 3 push targets
+    T* dep;      // [PUSH_BUFFERS][NT][3][B]: values pushed by the producers of a level's rows
     T* st;
     int* sn;
     int* lev;    // [numLev + 1]
-    int* nval;   // [2*l + 0/1]: values this block receives at level l (forward/backward)
+    int* nval;   // [2*l + 0/1]: values this block receives at level l (forward/backward), and
+                 // PUSH_BARRIER_FLAG if a cluster barrier follows level l in that sweep
     __device__ PushSmem(unsigned char* base, int numLev)
     {
-        st = reinterpret_cast<T*>(base);
+        dep = reinterpret_cast<T*>(base);
+        st = dep + NDEP;
         sn = reinterpret_cast<int*>(st + NF * NT);
         lev = sn + NI * NT;
         nval = lev + numLev + 1;
     }
     static constexpr size_t bytes(int numLev)
     {
-        return sizeof(T) * (size_t)NF * NT + sizeof(int) * ((size_t)NI * NT + 3 * (size_t)numLev + 1);
+        return sizeof(T) * ((size_t)NDEP + (size_t)NF * NT) +
+               sizeof(int) * ((size_t)NI * NT + 3 * (size_t)numLev + 1);
     }
 };
+constexpr int PUSH_COUNT_MASK = PUSH_BARRIER_FLAG - 1;
 
 // forward sweep y = L^-1 d (fuseP: d is the BiCGStab direction p, formed here).
 // The group that computed the previous level stages the operands of its next
@@ -630,9 +636,9 @@ __device__ __forceinline__ void sweepLowerPush(const KArgs<T>& a, const T* d, T*
         cpCommit();
     };
     load(mp.grp);
-    if (tid == 0) mbarArriveTx(ps.mb[0], (unsigned)(sm.nval[0] * sizeof(T)));
+    if (tid == 0) mbarArriveTx(ps.mb[0], (unsigned)((sm.nval[0] & PUSH_COUNT_MASK) * sizeof(T)));
     for (int l = 0; l < nl; ++l) {
-        const int k = l & 1;
+        const int k = l & (PUSH_BUFFERS - 1), kn = (l + 1) & (PUSH_BUFFERS - 1);
         const bool mine = mp.grp == l % G;
         if (mine && ps.ok && !mbarWait(ps.mb[k], ps.ph[k])) ps.ok = 0;  // after a timeout: no more waits
         ps.ph[k] ^= 1u;
@@ -672,7 +678,7 @@ __device__ __forceinline__ void sweepLowerPush(const KArgs<T>& a, const T* d, T*
                 for (int q = 0; q < 3; ++q) {
                     if (q >= dim) break;
                     const int tg = sn[(3 + q) * NT + tid];
-                    if (tg >= 0) pushValues<T, B>(tg, (k ^ 1) * half, out, tm, dep, ps, k ^ 1);
+                    if (tg >= 0) pushValues<T, B>(tg, kn * half, out, tm, dep, ps, kn);
                 }
 #pragma unroll
                 for (int e = 0; e < B; ++e) {
@@ -685,8 +691,10 @@ __device__ __forceinline__ void sweepLowerPush(const KArgs<T>& a, const T* d, T*
         else if (G > 1 && l >= 1 && mp.grp == (l - 1) % G) {
             load(l - 1 + G);
         }
-        if (tid == 0 && l + 1 < nl) mbarArriveTx(ps.mb[k ^ 1], (unsigned)(sm.nval[2 * (l + 1)] * sizeof(T)));
-        levelBarrier(ps, mp.C, mp.rank);
+        if (tid == 0 && l + 1 < nl)
+            mbarArriveTx(ps.mb[kn], (unsigned)((sm.nval[2 * (l + 1)] & PUSH_COUNT_MASK) * sizeof(T)));
+        if (sm.nval[2 * l] & PUSH_BARRIER_FLAG) levelBarrier(ps, mp.C, mp.rank);
+        else __syncthreads();
     }
     cg::this_cluster().sync();  // publish the global stores to the next phase
 }
@@ -732,10 +740,12 @@ __device__ __forceinline__ void sweepUpperPush(const KArgs<T>& a, T* y, const Te
         for (int l = nl - 1; l >= 0 && l >= nl - G; --l)
             if (l % G == mp.grp) first = l;
         load(first);
-        if (tid == 0) mbarArriveTx(ps.mb[(nl - 1) & 1], (unsigned)(sm.nval[2 * (nl - 1) + 1] * sizeof(T)));
+        if (tid == 0)
+            mbarArriveTx(ps.mb[(nl - 1) & (PUSH_BUFFERS - 1)],
+                         (unsigned)((sm.nval[2 * (nl - 1) + 1] & PUSH_COUNT_MASK) * sizeof(T)));
     }
     for (int l = nl - 1; l >= 0; --l) {
-        const int k = l & 1;
+        const int k = l & (PUSH_BUFFERS - 1), kn = (l + PUSH_BUFFERS - 1) & (PUSH_BUFFERS - 1);
         const bool mine = mp.grp == l % G;
         if (mine && ps.ok && !mbarWait(ps.mb[k], ps.ph[k])) ps.ok = 0;
         ps.ph[k] ^= 1u;
@@ -768,7 +778,7 @@ __device__ __forceinline__ void sweepUpperPush(const KArgs<T>& a, T* y, const Te
                 for (int q = 0; q < 3; ++q) {
                     if (q >= dim) break;
                     const int tg = sn[(3 + q) * NT + tid];
-                    if (tg >= 0) pushValues<T, B>(tg, (k ^ 1) * half, out, tm, dep, ps, k ^ 1);
+                    if (tg >= 0) pushValues<T, B>(tg, kn * half, out, tm, dep, ps, kn);
                 }
 #pragma unroll
                 for (int e = 0; e < B; ++e) y[i * B + e] = out[e];
@@ -778,8 +788,10 @@ __device__ __forceinline__ void sweepUpperPush(const KArgs<T>& a, T* y, const Te
         else if (G > 1 && l <= nl - 2 && mp.grp == (l + 1) % G) {
             load(l + 1 - G);
         }
-        if (tid == 0 && l > 0) mbarArriveTx(ps.mb[k ^ 1], (unsigned)(sm.nval[2 * (l - 1) + 1] * sizeof(T)));
-        levelBarrier(ps, mp.C, mp.rank);
+        if (tid == 0 && l > 0)
+            mbarArriveTx(ps.mb[kn], (unsigned)((sm.nval[2 * (l - 1) + 1] & PUSH_COUNT_MASK) * sizeof(T)));
+        if (sm.nval[2 * l + 1] & PUSH_BARRIER_FLAG) levelBarrier(ps, mp.C, mp.rank);
+        else __syncthreads();
     }
     cg::this_cluster().sync();
 }
@@ -806,20 +818,22 @@ __device__ __forceinline__ void spmvRow(const KArgs<T>& a, const T* in, int i, T
 // The whole solve of one system by one team (a cluster, or the cooperative
 // grid): optional ILU(0) factorization, then BiCGStab to the tolerance.
 template <class T, int B, int MODE, int NT>
-__device__ __forceinline__ void bicgstabBody(const KArgs<T>& a, const Team<MODE>& tm, T* dep,
-                                             unsigned long long* mbar, unsigned char* dynSmem)
+__device__ __forceinline__ void bicgstabBody(const KArgs<T>& a, const Team<MODE>& tm, unsigned long long* mbar,
+                                             unsigned char* dynSmem)
 {
     const int gt = tm.rank * blockDim.x + threadIdx.x, gs = tm.nblk * blockDim.x;
     const int N = a.N;
     PushState ps;
     ps.ok = 1;
     const PushSmem<T, B, NT> psm(dynSmem, a.numLev);
+    T* const dep = psm.dep;
     if constexpr (MODE == SYNC_CLUSTER) {
-        ps.mb[0] = smemAddr(&mbar[0]);
-        ps.mb[1] = smemAddr(&mbar[1]);
-        ps.ph[0] = ps.ph[1] = 0;
+        for (int k = 0; k < PUSH_BUFFERS; ++k) {
+            ps.mb[k] = smemAddr(&mbar[k]);
+            ps.ph[k] = 0;
+        }
         ps.dep = smemAddr(dep);
-        ps.lev = smemAddr(&mbar[2]);
+        ps.lev = smemAddr(&mbar[PUSH_BUFFERS]);
         ps.levPh = 0;
         if (a.dsmem) {
             for (int j = threadIdx.x; j <= a.numLev; j += NT) psm.lev[j] = a.levPtr[j];
@@ -827,8 +841,7 @@ __device__ __forceinline__ void bicgstabBody(const KArgs<T>& a, const Team<MODE>
         }
         if (a.dsmem && threadIdx.x == 0) {
             // one arrival per phase (thread 0, carrying the expected bytes)
-            mbarInit(ps.mb[0], 1);
-            mbarInit(ps.mb[1], 1);
+            for (int k = 0; k < PUSH_BUFFERS; ++k) mbarInit(ps.mb[k], 1);
             mbarInit(ps.lev, tm.nblk);
             asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         }
@@ -1068,11 +1081,10 @@ timeout:
 template <class T, int B, int MODE, int NT>
 __global__ void __launch_bounds__(NT, 1) kBicgstab(KArgs<T> a)
 {
-    __shared__ T dep[MODE == SYNC_CLUSTER ? 2 * NT * 3 * B : 1];
-    __shared__ __align__(8) unsigned long long mbar[3];
+    __shared__ __align__(8) unsigned long long mbar[PUSH_BUFFERS + 1];
     extern __shared__ __align__(16) unsigned char dynSmem[];
     const Team<MODE> tm;
-    bicgstabBody<T, B, MODE, NT>(a, tm, dep, mbar, dynSmem);
+    bicgstabBody<T, B, MODE, NT>(a, tm, mbar, dynSmem);
 }
 
 // Batched solve: every cluster of the grid takes systems from a work queue
@@ -1082,8 +1094,7 @@ template <class T, int B, int NT>
 __global__ void __launch_bounds__(NT, 1) kBicgstabBatch(const KArgs<T>* __restrict__ args,
                                                         const int* __restrict__ order, const int* count, int* queue)
 {
-    __shared__ T dep[2 * NT * 3 * B];
-    __shared__ __align__(8) unsigned long long mbar[3];
+    __shared__ __align__(8) unsigned long long mbar[PUSH_BUFFERS + 1];
     __shared__ int sNext;
     extern __shared__ __align__(16) unsigned char dynSmem[];
     cg::cluster_group cl = cg::this_cluster();
@@ -1095,10 +1106,10 @@ __global__ void __launch_bounds__(NT, 1) kBicgstabBatch(const KArgs<T>* __restri
         cl.sync();  // every block has read the index before block 0 takes the next one
         if (q >= *count) break;
         const KArgs<T> a = args[order[q]];
-        bicgstabBody<T, B, SYNC_CLUSTER, NT>(a, tm, dep, mbar, dynSmem);
+        bicgstabBody<T, B, SYNC_CLUSTER, NT>(a, tm, mbar, dynSmem);
         cl.sync();
         if (a.dsmem && threadIdx.x == 0)
-            for (int k = 0; k < 3; ++k)
+            for (int k = 0; k < PUSH_BUFFERS + 1; ++k)
                 asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smemAddr(&mbar[k])) : "memory");
         cl.sync();
     }

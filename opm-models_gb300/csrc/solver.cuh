@@ -9,7 +9,9 @@ namespace gbfv {
 
 constexpr int SOLVER_THREADS = 256;   // blocks of the cooperative-grid variant
 template <class T> constexpr int clusterThreads() { return sizeof(T) == 4 ? 512 : 256; }  // cluster variant
-constexpr int MAX_PUSH_LEVELS = 4096;  // push sweeps keep the level pointers in shared memory
+constexpr int MAX_PUSH_LEVELS = 2048;  // push sweeps keep the level pointers in shared memory
+constexpr int PUSH_BUFFERS = 4;        // push sweeps: dependency buffers (levels in flight) per block
+constexpr int PUSH_BARRIER_FLAG = 1 << 30;  // in levVals: a cluster barrier follows this level
 constexpr int SYNC_GRID = 0;     // whole grid, cooperative launch, software barrier
 constexpr int SYNC_CLUSTER = 1;  // one thread-block cluster, hardware barrier
 

@@ -228,6 +228,13 @@ class Batch:
     def time_integration(self, steps, dt0, end_time=1e100, fixed_dt=False):
         return self.lib.gbfv_batch_time_integration(self.h, steps, dt0, end_time, int(fixed_dt))
 
+    def autotune(self, dt):
+        """Pick the cluster size of the batched solve by timing each candidate."""
+        c, n = C.c_int(), C.c_int()
+        ms = np.zeros(8)
+        capi.check(self.lib.gbfv_batch_autotune(self.h, dt, C.byref(c), _d(ms), C.byref(n)), "gbfv_batch_autotune")
+        return c.value, ms[:n.value].copy()
+
     def report(self, i, max_steps=4096):
         st, n, nl = C.c_int(), C.c_int(), C.c_int()
         sdt = np.zeros(max_steps)

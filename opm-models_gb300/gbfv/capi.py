@@ -215,6 +215,15 @@ def load():
                                                C.POINTER(C.c_int)]),
         "gbfv_batch_get_stats": (C.c_int, [vp, C.POINTER(BatchStats)]),
         "gbfv_batch_stream": (vp, [vp]),
+        "gbfv_batch_autotune": (C.c_int, [vp, C.c_double, C.POINTER(C.c_int), dp, C.POINTER(C.c_int)]),
+        "gbfv_footprint_bytes": (C.c_int64, [C.c_int, C.c_int, C.c_int]),
+        "gbfv_serve_create": (vp, [C.c_int, C.c_int, C.POINTER(Params), C.c_int, C.c_int, C.POINTER(C.c_int)]),
+        "gbfv_serve_admit": (C.c_int, [vp, C.POINTER(Problem), dp, ip, C.c_int, C.c_double, C.c_int,
+                                       C.POINTER(C.c_int)]),
+        "gbfv_serve_step": (C.c_int, [vp, C.POINTER(C.c_int)]),
+        "gbfv_serve_slot": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+        "gbfv_serve_release": (C.c_int, [vp, C.c_int]),
+        "gbfv_serve_footprint": (C.c_int64, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
