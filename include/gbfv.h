@@ -341,6 +341,11 @@ int gbfv_reset_kernel_stats(gbfv_ctx* ctx);
  * factorization, [1] forward sweeps, [2] backward sweeps, [3] SpMV + dots,
  * [4] vector updates + norms, [5] remaining); zeros otherwise            */
 int gbfv_solver_phase_ns(gbfv_ctx* ctx, unsigned long long* ns8);
+/* with GBFV_PROFILE: SM cycles one working thread of the forward sweeps
+ * spent per level since the last call: [0] waiting for its data, [1]
+ * computing, [2] pushing results and storing, [3] in the level barrier;
+ * [4] the number of levels sampled                                       */
+int gbfv_solver_level_cycles(gbfv_ctx* ctx, unsigned long long* c8);
 
 /* ------------------------------------------------------------------ */
 /* Batched systems (ensemble realizations, served requests).  No single

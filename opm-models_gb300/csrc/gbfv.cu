@@ -149,8 +149,8 @@ int allocSolver(SolverData& S, int maxBlocksOverride = 0)
     CK(cudaEventCreate(&S.evA));
     CK(cudaEventCreate(&S.evB));
     if (getenv("GBFV_PROFILE")) {
-        CK(cudaMalloc((void**)&S.prof, 8 * sizeof(unsigned long long)));
-        CK(cudaMemset(S.prof, 0, 8 * sizeof(unsigned long long)));
+        CK(cudaMalloc((void**)&S.prof, 16 * sizeof(unsigned long long)));
+        CK(cudaMemset(S.prof, 0, 16 * sizeof(unsigned long long)));
     }
     return GBFV_OK;
 }
@@ -360,6 +360,7 @@ int buildPushTargets(SolverData& S, int C, int G, int NT)
 {
     if (S.pushKey[0] == C && S.pushKey[1] == G && S.pushKey[2] == NT && S.pushL) return GBFV_OK;
     const int N = S.N, ld = S.ldN, dim = S.dim, B = S.b, NG = NT / G;
+    const int PB = padB(B);  // values per dependency slot
     std::vector<int> lev(N);
     for (size_t l = 0; l + 1 < S.levPtr.size(); ++l)
         for (int p = S.levPtr[l]; p < S.levPtr[l + 1]; ++p) lev[p] = (int)l;
@@ -369,7 +370,7 @@ int buildPushTargets(SolverData& S, int C, int G, int NT)
         const int owner = w % C;
         const int uu = ((w / C) << 5) | (t & 31);
         const int cslot = (lev[j] % G) * NG + uu;
-        return (owner << 24) | ((cslot * 3 + slot) * B);
+        return (owner << 24) | ((cslot * 3 + slot) * PB);
     };
     const int nl = (int)S.levPtr.size() - 1;
     std::vector<int> hL((size_t)3 * ld, -1), hU((size_t)3 * ld, -1), hV((size_t)C * nl * 2, 0);
@@ -379,12 +380,12 @@ int buildPushTargets(SolverData& S, int C, int G, int NT)
             const int ju = S.colHost[(size_t)(dim + 1 + q) * ld + p];  // upper neighbour +q
             if (ju >= 0) {
                 hL[(size_t)q * ld + p] = target(ju, dim - 1 - q);
-                hV[((size_t)owner * nl + lev[p]) * 2 + 1] += B;  // p receives ju in the backward sweep
+                hV[((size_t)owner * nl + lev[p]) * 2 + 1] += PB;  // p receives ju in the backward sweep
             }
             const int jl = S.colHost[(size_t)q * ld + p];  // lower neighbour in slot q
             if (jl >= 0) {
                 hU[(size_t)q * ld + p] = target(jl, q);
-                hV[((size_t)owner * nl + lev[p]) * 2] += B;  // p receives jl in the forward sweep
+                hV[((size_t)owner * nl + lev[p]) * 2] += PB;  // p receives jl in the forward sweep
             }
         }
     }
@@ -1420,6 +1421,16 @@ int gbfv_solver_phase_ns(gbfv_ctx* C, unsigned long long* ns8)
     CK(cudaStreamSynchronize(C->stream));
     CK(cudaMemcpy(ns8, C->S.prof, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
     CK(cudaMemset(C->S.prof, 0, 8 * sizeof(unsigned long long)));
+    return GBFV_OK;
+}
+
+int gbfv_solver_level_cycles(gbfv_ctx* C, unsigned long long* c8)
+{
+    if (!C || !c8) return GBFV_ERR_ARG;
+    if (!C->S.prof) { std::memset(c8, 0, 8 * sizeof(unsigned long long)); return GBFV_OK; }
+    CK(cudaStreamSynchronize(C->stream));
+    CK(cudaMemcpy(c8, C->S.prof + 8, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    CK(cudaMemset(C->S.prof + 8, 0, 8 * sizeof(unsigned long long)));
     return GBFV_OK;
 }
 

@@ -439,35 +439,40 @@ __device__ __forceinline__ bool mbarWait(unsigned a, unsigned parity)
     }
     return false;
 }
-__device__ __forceinline__ void stAsync(unsigned dst, float v, unsigned mbar)
-{
-    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b32 [%0], %1, [%2];" ::"r"(dst),
-                 "r"(__float_as_uint(v)), "r"(mbar)
-                 : "memory");
-}
-__device__ __forceinline__ void stAsync(unsigned dst, double v, unsigned mbar)
-{
-    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b64 [%0], %1, [%2];" ::"r"(dst),
-                 "l"(__double_as_longlong(v)), "r"(mbar)
-                 : "memory");
-}
-
-// consumer in this block: plain shared store, CTA-scope release, then
-// count the bytes on the local mbarrier
+// A pushed block of B values occupies a slot of padB(B) values (3 -> 4), so
+// that one vector st.async carries it (16-byte aligned for float, two 16-byte
+// stores for double).
+// remote push of one slot: vector st.async, bytes counted on the consumer's mbarrier
 template <class T, int B>
-__device__ __forceinline__ void pushLocal(T* dst, const T (&v)[B], unsigned mbar)
+__device__ __forceinline__ void stAsyncSlot(unsigned dst, const T (&v)[B], unsigned mbar)
 {
+    if constexpr (sizeof(T) == 4 && B == 3) {
+        asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.b32 [%0], {%1, %2, %3, %4}, [%5];" ::"r"(dst),
+                     "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])), "r"(0u),
+                     "r"(mbar)
+                     : "memory");
+    }
+    else if constexpr (sizeof(T) == 4 && B == 2) {
+        asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.b32 [%0], {%1, %2}, [%3];" ::"r"(dst),
+                     "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(mbar)
+                     : "memory");
+    }
+    else {
 #pragma unroll
-    for (int e = 0; e < B; ++e) dst[e] = v[e];
-    asm volatile("fence.acq_rel.cta;" ::: "memory");
-    asm volatile("mbarrier.complete_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"((unsigned)(B * sizeof(T)))
-                 : "memory");
+        for (int e = 0; e < B; e += 2) {
+            const double hi = (e + 1 < B) ? (double)v[e + 1] : 0.0;
+            asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.b64 [%0], {%1, %2}, [%3];" ::"r"(
+                             dst + e * 8u),
+                         "l"(__double_as_longlong((double)v[e])), "l"(__double_as_longlong(hi)), "r"(mbar)
+                         : "memory");
+        }
+    }
 }
 
 struct PushState {
     unsigned mb[PUSH_BUFFERS];   // shared addresses of the data mbarriers, one per dependency buffer
     unsigned ph[PUSH_BUFFERS];   // parity of the next phase to wait for
-    unsigned dep;     // shared address of the dependency buffers [PUSH_BUFFERS][NT][3][B]
+    unsigned dep;     // shared address of the dependency buffers [PUSH_BUFFERS][NT][3][padB(B)]
     unsigned lev;     // shared address of the level-done mbarrier (C arrivals)
     unsigned levPh;
     int ok;
@@ -535,17 +540,13 @@ template <class T, int B>
 __device__ __forceinline__ void pushValues(int target, int half, const T (&out)[B], const Team<SYNC_CLUSTER>& tm,
                                            const T* dep, const PushState& ps, int mbIdx)
 {
+    // also a consumer in this block gets its values by st.async (to this block's
+    // own shared memory): the transaction count orders them, no fence needed
     const int owner = target >> 24;
     const int off = (target & 0xffffff) + half;
-    if (owner == tm.rank) {
-        pushLocal<T, B>(const_cast<T*>(dep) + off, out, ps.mb[mbIdx]);
-    }
-    else {
-        const unsigned dst = mapaRank(ps.dep + (unsigned)(off * sizeof(T)), owner);
-        const unsigned mb = mapaRank(ps.mb[mbIdx], owner);
-#pragma unroll
-        for (int e = 0; e < B; ++e) stAsync(dst + e * (unsigned)sizeof(T), out[e], mb);
-    }
+    const unsigned dst = mapaRank(ps.dep + (unsigned)(off * sizeof(T)), owner);
+    const unsigned mb = mapaRank(ps.mb[mbIdx], owner);
+    stAsyncSlot<T, B>(dst, out, mb);
 }
 
 // Asynchronous global -> shared copies (no registers held, not waited for by
@@ -564,10 +565,12 @@ __device__ __forceinline__ void cpWaitAll() { asm volatile("cp.async.wait_all;" 
 // per level (forward and backward sweep).
 template <class T, int B, int NT>
 struct PushSmem {
-    static constexpr int NDEP = PUSH_BUFFERS * NT * 3 * B;  // dependency buffers
-    static constexpr int NF = 4 * B * B + 3 * B;  // 3 off-diagonal blocks, pivot, 3 vectors
+    static constexpr int NDEP = PUSH_BUFFERS * NT * 3 * padB(B);  // dependency buffers
+    // staged fields: forward sweep 3 factor blocks + 3 vectors, backward
+    // sweep 3 matrix blocks + inverted pivot + 1 vector
+    static constexpr int NF = 4 * B * B + B > 3 * B * B + 3 * B ? 4 * B * B + B : 3 * B * B + 3 * B;
     static constexpr int NI = 6;                   // 3 neighbour columns, 3 push targets
-    T* dep;      // [PUSH_BUFFERS][NT][3][B]: values pushed by the producers of a level's rows
+    T* dep;      // [PUSH_BUFFERS][NT][3][padB(B)]: values pushed by the producers of a level's rows
     T* st;
     int* sn;
     int* lev;    // [numLev + 1]
@@ -598,10 +601,10 @@ __device__ __forceinline__ void sweepLowerPush(const KArgs<T>& a, const T* d, T*
                                                const Team<SYNC_CLUSTER>& tm, const T* dep, PushState& ps,
                                                const PushSmem<T, B, NT>& sm)
 {
-    constexpr int BB = B * B, VB = 4 * BB;
+    constexpr int BB = B * B, VB = 3 * BB, PB = padB(B);
     const SweepMap<T, B, NT> mp(tm, a.grp);
     const int dim = a.dim, ld = a.ldN, nl = a.numLev, G = mp.G, tid = mp.tid;
-    const int half = NT * 3 * B;
+    const int half = NT * 3 * PB;
     const T* st = sm.st;
     const int* sn = sm.sn;
     const unsigned stA = smemAddr(sm.st) + tid * sizeof(T), snA = smemAddr(sm.sn) + tid * sizeof(int);
@@ -637,16 +640,21 @@ __device__ __forceinline__ void sweepLowerPush(const KArgs<T>& a, const T* d, T*
     };
     load(mp.grp);
     if (tid == 0) mbarArriveTx(ps.mb[0], (unsigned)((sm.nval[0] & PUSH_COUNT_MASK) * sizeof(T)));
+    // optional cycle counts of one working thread (GBFV_PROFILE): data wait,
+    // compute, pushes + stores, level barrier
+    const bool probe = a.prof != nullptr && tm.rank == 0 && tid == 0;
+    unsigned long long cyc[4] = {0, 0, 0, 0}, t0 = 0, t1 = 0, t2 = 0, t3 = 0, nprobe = 0;
     for (int l = 0; l < nl; ++l) {
         const int k = l & (PUSH_BUFFERS - 1), kn = (l + 1) & (PUSH_BUFFERS - 1);
         const bool mine = mp.grp == l % G;
-        if (mine && ps.ok && !mbarWait(ps.mb[k], ps.ph[k])) ps.ok = 0;  // after a timeout: no more waits
-        ps.ph[k] ^= 1u;
         if (mine) {
             const int i = iCur;
+            // the row's staged operands go to registers before the data wait
+            T out[B];
+            bool has[3] = {false, false, false};
+            int tg[3] = {-1, -1, -1};
             if (i >= 0) {
                 cpWaitAll();
-                T out[B], pv[B];
                 if (fuseP) {
 #pragma unroll
                     for (int e = 0; e < B; ++e) {
@@ -656,7 +664,7 @@ __device__ __forceinline__ void sweepLowerPush(const KArgs<T>& a, const T* d, T*
                         tmp *= -beta;
                         T pe = st[(VB + 2 * B + e) * NT + tid];
                         pe += tmp;
-                        pv[e] = pe;
+                        a.p[i * B + e] = pe;  // the new direction p = r - beta (p - omega v)
                         out[e] = pe;
                     }
                 }
@@ -664,37 +672,62 @@ __device__ __forceinline__ void sweepLowerPush(const KArgs<T>& a, const T* d, T*
 #pragma unroll
                     for (int e = 0; e < B; ++e) out[e] = st[(VB + e) * NT + tid];
                 }
-                const T* md = dep + (k * NT + tid) * 3 * B;
 #pragma unroll
                 for (int s = 0; s < 3; ++s) {
                     if (s >= dim) break;
-                    if (sn[s * NT + tid] < 0) continue;
+                    has[s] = sn[s * NT + tid] >= 0;
+                    tg[s] = sn[(3 + s) * NT + tid];
+                }
+            }
+            if (probe) t0 = clock64();
+            if (ps.ok && !mbarWait(ps.mb[k], ps.ph[k])) ps.ok = 0;  // after a timeout: no more waits
+            if (probe) t1 = t2 = clock64();
+            if (i >= 0) {
+                const T* md = dep + (k * NT + tid) * 3 * PB;
+#pragma unroll
+                for (int s = 0; s < 3; ++s) {
+                    if (s >= dim) break;
+                    if (!has[s]) continue;
+                    T m[B];
+#pragma unroll
+                    for (int c = 0; c < B; ++c) m[c] = md[s * PB + c];
 #pragma unroll
                     for (int r = 0; r < B; ++r)
 #pragma unroll
-                        for (int c = 0; c < B; ++c) out[r] -= st[(s * BB + r * B + c) * NT + tid] * md[s * B + c];
+                        for (int c = 0; c < B; ++c) out[r] -= st[(s * BB + r * B + c) * NT + tid] * m[c];
                 }
+                if (probe) t2 = clock64();
 #pragma unroll
                 for (int q = 0; q < 3; ++q) {
                     if (q >= dim) break;
-                    const int tg = sn[(3 + q) * NT + tid];
-                    if (tg >= 0) pushValues<T, B>(tg, kn * half, out, tm, dep, ps, kn);
+                    if (tg[q] >= 0) pushValues<T, B>(tg[q], kn * half, out, tm, dep, ps, kn);
                 }
 #pragma unroll
-                for (int e = 0; e < B; ++e) {
-                    y[i * B + e] = out[e];
-                    if (fuseP) a.p[i * B + e] = pv[e];
-                }
+                for (int e = 0; e < B; ++e) y[i * B + e] = out[e];
             }
             if (G == 1) load(l + 1);
         }
         else if (G > 1 && l >= 1 && mp.grp == (l - 1) % G) {
             load(l - 1 + G);
         }
+        ps.ph[k] ^= 1u;
+        if (probe && mine) t3 = clock64();
         if (tid == 0 && l + 1 < nl)
             mbarArriveTx(ps.mb[kn], (unsigned)((sm.nval[2 * (l + 1)] & PUSH_COUNT_MASK) * sizeof(T)));
         if (sm.nval[2 * l] & PUSH_BARRIER_FLAG) levelBarrier(ps, mp.C, mp.rank);
         else __syncthreads();
+        if (probe && mine) {
+            const unsigned long long t4 = clock64();
+            cyc[0] += t1 - t0;
+            cyc[1] += t2 - t1;
+            cyc[2] += t3 - t2;
+            cyc[3] += t4 - t3;
+            nprobe++;
+        }
+    }
+    if (probe) {
+        for (int j = 0; j < 4; ++j) a.prof[8 + j] += cyc[j];
+        a.prof[12] += nprobe;
     }
     cg::this_cluster().sync();  // publish the global stores to the next phase
 }
@@ -704,10 +737,10 @@ template <class T, int B, int NT>
 __device__ __forceinline__ void sweepUpperPush(const KArgs<T>& a, T* y, const Team<SYNC_CLUSTER>& tm, const T* dep,
                                                PushState& ps, const PushSmem<T, B, NT>& sm)
 {
-    constexpr int BB = B * B, VB = 4 * BB;
+    constexpr int BB = B * B, VB = 4 * BB, PB = padB(B);
     const SweepMap<T, B, NT> mp(tm, a.grp);
     const int dim = a.dim, ld = a.ldN, nl = a.numLev, G = mp.G, tid = mp.tid;
-    const int half = NT * 3 * B;
+    const int half = NT * 3 * PB;
     const T* st = sm.st;
     const int* sn = sm.sn;
     const unsigned stA = smemAddr(sm.st) + tid * sizeof(T), snA = smemAddr(sm.sn) + tid * sizeof(int);
@@ -747,24 +780,37 @@ __device__ __forceinline__ void sweepUpperPush(const KArgs<T>& a, T* y, const Te
     for (int l = nl - 1; l >= 0; --l) {
         const int k = l & (PUSH_BUFFERS - 1), kn = (l + PUSH_BUFFERS - 1) & (PUSH_BUFFERS - 1);
         const bool mine = mp.grp == l % G;
-        if (mine && ps.ok && !mbarWait(ps.mb[k], ps.ph[k])) ps.ok = 0;
-        ps.ph[k] ^= 1u;
         if (mine) {
             const int i = iCur;
+            // the row's staged operands go to registers before the data wait
+            T acc[B];
+            bool has[3] = {false, false, false};
+            int tg[3] = {-1, -1, -1};
             if (i >= 0) {
                 cpWaitAll();
-                T acc[B];
 #pragma unroll
                 for (int e = 0; e < B; ++e) acc[e] = st[(VB + e) * NT + tid];
-                const T* md = dep + (k * NT + tid) * 3 * B;
 #pragma unroll
                 for (int q = 0; q < 3; ++q) {
                     if (q >= dim) break;
-                    if (sn[q * NT + tid] < 0) continue;
+                    has[q] = sn[q * NT + tid] >= 0;
+                    tg[q] = sn[(3 + q) * NT + tid];
+                }
+            }
+            if (ps.ok && !mbarWait(ps.mb[k], ps.ph[k])) ps.ok = 0;
+            if (i >= 0) {
+                const T* md = dep + (k * NT + tid) * 3 * PB;
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    if (q >= dim) break;
+                    if (!has[q]) continue;
+                    T m[B];
+#pragma unroll
+                    for (int c = 0; c < B; ++c) m[c] = md[q * PB + c];
 #pragma unroll
                     for (int r = 0; r < B; ++r)
 #pragma unroll
-                        for (int c = 0; c < B; ++c) acc[r] -= st[(q * BB + r * B + c) * NT + tid] * md[q * B + c];
+                        for (int c = 0; c < B; ++c) acc[r] -= st[(q * BB + r * B + c) * NT + tid] * m[c];
                 }
                 T out[B];
 #pragma unroll
@@ -777,8 +823,7 @@ __device__ __forceinline__ void sweepUpperPush(const KArgs<T>& a, T* y, const Te
 #pragma unroll
                 for (int q = 0; q < 3; ++q) {
                     if (q >= dim) break;
-                    const int tg = sn[(3 + q) * NT + tid];
-                    if (tg >= 0) pushValues<T, B>(tg, kn * half, out, tm, dep, ps, kn);
+                    if (tg[q] >= 0) pushValues<T, B>(tg[q], kn * half, out, tm, dep, ps, kn);
                 }
 #pragma unroll
                 for (int e = 0; e < B; ++e) y[i * B + e] = out[e];
@@ -788,6 +833,7 @@ __device__ __forceinline__ void sweepUpperPush(const KArgs<T>& a, T* y, const Te
         else if (G > 1 && l <= nl - 2 && mp.grp == (l + 1) % G) {
             load(l + 1 - G);
         }
+        ps.ph[k] ^= 1u;
         if (tid == 0 && l > 0)
             mbarArriveTx(ps.mb[kn], (unsigned)((sm.nval[2 * (l - 1) + 1] & PUSH_COUNT_MASK) * sizeof(T)));
         if (sm.nval[2 * l + 1] & PUSH_BARRIER_FLAG) levelBarrier(ps, mp.C, mp.rank);

@@ -12,6 +12,8 @@ template <class T> constexpr int clusterThreads() { return sizeof(T) == 4 ? 512 
 constexpr int MAX_PUSH_LEVELS = 2048;  // push sweeps keep the level pointers in shared memory
 constexpr int PUSH_BUFFERS = 4;        // push sweeps: dependency buffers (levels in flight) per block
 constexpr int PUSH_BARRIER_FLAG = 1 << 30;  // in levVals: a cluster barrier follows this level
+// values per pushed dependency slot: a block of B values padded for one vector store
+__host__ __device__ constexpr int padB(int B) { return B == 3 ? 4 : B; }
 constexpr int SYNC_GRID = 0;     // whole grid, cooperative launch, software barrier
 constexpr int SYNC_CLUSTER = 1;  // one thread-block cluster, hardware barrier
 
