@@ -379,14 +379,17 @@ def _member(args):
     return problems.ensemble_member(n, seed, sigma)
 
 
-def ensemble_problems(count):
+def ensemble_problems(count, rank=0, world=1):
     """Seeded ensemble: cell counts uniform in [10k, 200k], lognormal
-    permeability with sigma uniform in [0.5, 1.5] (built in a spawned pool)."""
+    permeability with sigma uniform in [0.5, 1.5] (built in a spawned pool).
+    With several ranks each builds the members assigned to it by size."""
     import multiprocessing as mp
+    from gbfv import replicas
     rng = np.random.default_rng(ENSEMBLE["seed"])
     sizes = rng.integers(ENSEMBLE["lo"], ENSEMBLE["hi"] + 1, count)
     sig = rng.uniform(*ENSEMBLE["sigma"], count)
-    jobs = [(int(n), ENSEMBLE["seed"] + i, float(g)) for i, (n, g) in enumerate(zip(sizes, sig))]
+    mine = replicas.assign([int(n) for n in sizes], world)[rank]
+    jobs = [(int(sizes[i]), ENSEMBLE["seed"] + i, float(sig[i])) for i in mine]
     with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
         return pool.map(_member, jobs, chunksize=1)
 
@@ -397,14 +400,22 @@ def run_ensemble(args):
     CUDA graphs).  value = sum over systems of Newton iterations x cells /
     device time of the whole batch; one_at_a_time = the same systems solved
     one after another through single contexts (a sample of them)."""
+    rank, world, local = dist_env()
     t0 = time.time()
-    probs = ensemble_problems(args.ensemble)  # before any CUDA call (spawned pool)
+    probs = ensemble_problems(args.ensemble, rank, world)  # before any CUDA call (spawned pool)
     t_build = time.time() - t0
     import torch
-    torch.cuda.set_device(0)
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
     import __graft_entry__ as ge
+    if rank == 0:
+        ge.build()
+    if world > 1:
+        dist.barrier()
     ge.build()
-    from gbfv import Batch, Context, capi
+    from gbfv import Batch, Context, capi, replicas
     prm = params(capi.PREC_MIXED)
     t0 = time.time()
     B = Batch(probs, prm)
@@ -433,16 +444,28 @@ def run_ensemble(args):
     for _ in range(args.warmup):
         one_run()
     s0 = B.stats()
-    sampler = ClockSampler(0)
-    sampler.start()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local) if rank == 0 else None
+    if sampler:
+        sampler.start()
     ms_tot, cits_tot = 0.0, 0
     for _ in range(args.steps):
         ms, cits = one_run()
         ms_tot += ms
         cits_tot += cits
-    clocks = sampler.stop()
+    torch.cuda.synchronize()
+    clocks = sampler.stop() if sampler else None
     s1 = B.stats()
+    # whole job: the slowest rank's time, all ranks' work (no data-path collective)
+    ms_tot, cits_tot = replicas.reduce_timing(ms_tot, cits_tot, device="cuda")
     value = cits_tot / (ms_tot / 1000.0)
+    if rank != 0:
+        B.close()
+        dist.barrier()
+        dist.destroy_process_group()
+        return 0
     newton = [B.report(i)[2].tolist() for i in range(len(probs))]
     # one at a time: a sample of the same systems through single contexts
     sample = list(range(0, len(probs), max(1, len(probs) // 8)))[:8]
@@ -483,7 +506,7 @@ def run_ensemble(args):
                   "graph_launches_per_step": (s1["graph_launches"] - s0["graph_launches"]) / args.steps,
                   "build_s": t_build, "create_s": t_create},
         "one_at_a_time": {"value": one_cits / (one_ms / 1000.0), "systems_sampled": len(sample)},
-        "batched_over_one_at_a_time": value / (one_cits / (one_ms / 1000.0)),
+        "batched_over_one_at_a_time": (value / world) / (one_cits / (one_ms / 1000.0)),
         "gpu_launches": int((s1["kernel_launches"] - s0["kernel_launches"]) / args.steps),
         "newton_iterations_first_systems": newton[:4],
         "roofline": {"bound": "hbm", "kernel": "kBicgstabBatch<float,2> (batched persistent ILU0 + BiCGStab)",
@@ -565,7 +588,14 @@ def run_serve(args):
         "p50_ms": served[top]["p50_ms"], "p99_ms": served[top]["p99_ms"],
         "clocks": clocks,
     }
+    if world > 1:
+        line["n_gpus"] = world
+        line["config"]["parallelism"] = "replicas (systems assigned to ranks by size)"
+        line["config"]["systems_on_rank0"] = len(probs)
     print(json.dumps(line))
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
     return 0
 
 
