@@ -420,6 +420,14 @@ int gbfv_serve_release(gbfv_batch* server, int slot);
 int64_t gbfv_serve_footprint(const gbfv_batch* server);
 
 /* ------------------------------------------------------------------ */
+/* Self-test of the device-side wait bound (no counterpart in the
+ * reference): one block waits, with the bounded wait of the solver's
+ * sweeps, on a barrier phase that nothing completes.  Returns
+ * GBFV_ERR_TIMEOUT when the wait gave up as designed (the device stays
+ * usable), and the kernel's time in ms.                                   */
+int gbfv_selftest_wait_timeout(double* ms);
+
+/* ------------------------------------------------------------------ */
 /* Allocation-free Newton error.  No counterpart in the reference: its
  * NewtonMethod computes the same maximum norm on the host
  * (newtonmethod.hh:572-598, preSolve_).  For callers that hold the

@@ -374,8 +374,9 @@ int buildPushTargets(SolverData& S, int C, int G, int NT)
     };
     const int nl = (int)S.levPtr.size() - 1;
     std::vector<int> hL((size_t)3 * ld, -1), hU((size_t)3 * ld, -1), hV((size_t)C * nl * 2, 0);
+    auto ownerOf = [&](int p) { return ((p - S.levPtr[lev[p]]) >> 5) % C; };
     for (int p = 0; p < N; ++p) {
-        const int owner = ((p - S.levPtr[lev[p]]) >> 5) % C;
+        const int owner = ownerOf(p);
         for (int q = 0; q < dim; ++q) {
             const int ju = S.colHost[(size_t)(dim + 1 + q) * ld + p];  // upper neighbour +q
             if (ju >= 0) {
@@ -2602,5 +2603,31 @@ int gbfv_serve_release(gbfv_batch* B, int slot)
 }
 
 int64_t gbfv_serve_footprint(const gbfv_batch* B) { return B ? B->footprint : -1; }
+
+int gbfv_selftest_wait_timeout(double* ms)
+{
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GBFV_ERR_NO_DEVICE;
+    DevStatus* d = nullptr;
+    DevStatus h;
+    cudaEvent_t e0, e1;
+    CK(cudaMalloc((void**)&d, sizeof(DevStatus)));
+    CK(cudaMemset(d, 0, sizeof(DevStatus)));
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    cudaEventRecord(e0, 0);
+    launchWaitTimeoutProbe(d, 0);
+    cudaEventRecord(e1, 0);
+    const cudaError_t e = cudaMemcpy(&h, d, sizeof(DevStatus), cudaMemcpyDeviceToHost);
+    float t = 0;
+    cudaEventElapsedTime(&t, e0, e1);
+    if (ms) *ms = t;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(d);
+    CK(e);
+    if (h.iterations != 1) return GBFV_ERR_CUDA;
+    return h.code;
+}
 
 }  // extern "C"

@@ -61,11 +61,16 @@ template <int N> GB_HD Dual<N> operator-(const Dual<N>& a)
 { Dual<N> r; r.v = -a.v;
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = -a.d[i]; return r; }
+// Values follow the reference's operation order exactly (they decide upwind
+// directions and saturation branches); derivatives may round differently by
+// an ulp, so they use fused multiply-adds and one reciprocal per division
+// instead of a division per derivative -- FP64 issue is this GPU's scarce
+// resource.
 // (u w)' = u' w + w' u
 template <int N> GB_HD Dual<N> operator*(const Dual<N>& a, const Dual<N>& b)
 { Dual<N> r; r.v = a.v * b.v;
 #pragma unroll
-  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * b.v + b.d[i] * a.v; return r; }
+  for (int i = 0; i < N; ++i) r.d[i] = fma(a.d[i], b.v, b.d[i] * a.v); return r; }
 template <int N> GB_HD Dual<N> operator*(const Dual<N>& a, double s)
 { Dual<N> r; r.v = a.v * s;
 #pragma unroll
@@ -73,14 +78,14 @@ template <int N> GB_HD Dual<N> operator*(const Dual<N>& a, double s)
 template <int N> GB_HD Dual<N> operator*(double s, const Dual<N>& a) { return a * s; }
 // (u / w)' = (w u' - u w') / w^2
 template <int N> GB_HD Dual<N> operator/(const Dual<N>& a, const Dual<N>& b)
-{ Dual<N> r; const double u = a.v, w = b.v;
+{ Dual<N> r; const double u = a.v, w = b.v, iw2 = 1.0 / (w * w);
 #pragma unroll
-  for (int i = 0; i < N; ++i) r.d[i] = (w * a.d[i] - u * b.d[i]) / (w * w);
+  for (int i = 0; i < N; ++i) r.d[i] = fma(w, a.d[i], -(u * b.d[i])) * iw2;
   r.v = u / w; return r; }
 template <int N> GB_HD Dual<N> operator/(const Dual<N>& a, double s)
-{ Dual<N> r; r.v = a.v / s;
+{ Dual<N> r; r.v = a.v / s; const double is = 1.0 / s;
 #pragma unroll
-  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] / s; return r; }
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * is; return r; }
 // s / w: -s/w^2 w'
 template <int N> GB_HD Dual<N> operator/(double s, const Dual<N>& a)
 { Dual<N> r; r.v = s / a.v; const double df = -s / (a.v * a.v);

@@ -220,11 +220,12 @@ template <int B>
 __device__ __forceinline__ void writeOffBlock(double* __restrict__ jval, int ld, int slot, int q,
                                               const Dual<B>* flux, double Vq, bool zero)
 {
+    const double iv = 1.0 / Vq;  // Jacobian entries only: one reciprocal per block
 #pragma unroll
     for (int e = 0; e < B; ++e)
 #pragma unroll
         for (int v = 0; v < B; ++v) {
-            const double d = zero ? 0.0 : (0.0 - flux[e].d[v]) / Vq;
+            const double d = zero ? 0.0 : (0.0 - flux[e].d[v]) * iv;
             jval[(slot * B * B + e * B + v) * ld + q] = d;
         }
 }

@@ -29,6 +29,8 @@ namespace cg = cooperative_groups;
 
 namespace gbfv {
 
+// every device-side wait gives up after 4e9 SM cycles (about two seconds)
+// and reports GBFV_ERR_TIMEOUT instead of hanging
 #define GB_TIMEOUT_CYCLES 4000000000LL
 
 // loads of data written inside the kernel by other blocks go to L2 directly
@@ -412,7 +414,8 @@ __device__ __forceinline__ void mbarArriveTx(unsigned a, unsigned bytes)
 // so it does not wait for this thread's loads in flight; false on timeout
 __device__ __forceinline__ bool mbarWaitRelaxed(unsigned a, unsigned parity)
 {
-    for (int spin = 0; spin < (1 << 16); ++spin) {
+    const long long t0 = clock64();
+    for (;;) {
         unsigned done;
         asm volatile(
             "{ .reg .pred p; mbarrier.try_wait.parity.relaxed.cta.shared::cta.b64 p, [%1], %2; "
@@ -421,13 +424,14 @@ __device__ __forceinline__ bool mbarWaitRelaxed(unsigned a, unsigned parity)
             : "r"(a), "r"(parity)
             : "memory");
         if (done) return true;
+        if (clock64() - t0 > GB_TIMEOUT_CYCLES) return false;
     }
-    return false;
 }
 // bounded wait (acquire) for the phase with the given parity; false on timeout
 __device__ __forceinline__ bool mbarWait(unsigned a, unsigned parity)
 {
-    for (int spin = 0; spin < (1 << 16); ++spin) {
+    const long long t0 = clock64();
+    for (;;) {
         unsigned done;
         asm volatile(
             "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; "
@@ -436,8 +440,8 @@ __device__ __forceinline__ bool mbarWait(unsigned a, unsigned parity)
             : "r"(a), "r"(parity)
             : "memory");
         if (done) return true;
+        if (clock64() - t0 > GB_TIMEOUT_CYCLES) return false;
     }
-    return false;
 }
 // A pushed block of B values occupies a slot of padB(B) values (3 -> 4), so
 // that one vector st.async carries it (16-byte aligned for float, two 16-byte
@@ -1159,6 +1163,29 @@ __global__ void __launch_bounds__(NT, 1) kBicgstabBatch(const KArgs<T>* __restri
                 asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smemAddr(&mbar[k])) : "memory");
         cl.sync();
     }
+}
+
+// ------------------------------------------------ bounded-wait self-test --
+// One block waits, with the sweeps' bounded wait, on an mbarrier phase that
+// nothing completes; the wait gives up and the kernel reports
+// GBFV_ERR_TIMEOUT, as a solve whose data never arrives would.
+__global__ void kWaitTimeoutProbe(DevStatus* st)
+{
+    __shared__ __align__(8) unsigned long long mb;
+    if (threadIdx.x == 0) mbarInit(smemAddr(&mb), 1);
+    __syncthreads();
+    const bool ok = mbarWait(smemAddr(&mb), 0u);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        st->code = ok ? GBFV_OK : GBFV_ERR_TIMEOUT;
+        st->iterations = 1;
+    }
+}
+
+void launchWaitTimeoutProbe(DevStatus* st, cudaStream_t s)
+{
+    kWaitTimeoutProbe<<<1, 32, 0, s>>>(st);
+    countLaunch();
 }
 
 // ------------------------------------------------- launch + FP64 helpers --

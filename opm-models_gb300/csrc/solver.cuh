@@ -81,6 +81,7 @@ int launchBicgstabBatch(const KArgs<T>* args, const int* order, const int* count
                         int clusterSize, int numClusters, int maxLev, cudaStream_t s);
 template <class T> int maxActiveClusters(int b, int clusterSize);
 void launchCastMatrix(const double* src, float* dst, long n, cudaStream_t s);
+void launchWaitTimeoutProbe(DevStatus* st, cudaStream_t s);
 void launchAccumulate(int n, double* x, const float* d, cudaStream_t s);
 void launchResidual64(int N, int ld, int nslot, int b, const int* col, const double* A, const double* rhs,
                       const double* x, double* r, float* r32, DevStatus* st, cudaStream_t s);

@@ -224,6 +224,7 @@ def load():
         "gbfv_serve_slot": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "gbfv_serve_release": (C.c_int, [vp, C.c_int]),
         "gbfv_serve_footprint": (C.c_int64, [vp]),
+        "gbfv_selftest_wait_timeout": (C.c_int, [dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -75,3 +75,12 @@ def test_blackoil_builder_wells_and_tables():
     k = p.perm.reshape(-1, 3)
     assert np.allclose(k[:, 2], 0.1 * k[:, 0])
     assert p.porosity.min() >= 0.15 and p.porosity.max() <= 0.30
+
+
+def test_footprint_estimate_is_monotone(built):
+    lib = capi.load()
+    f = lib.gbfv_footprint_bytes
+    a, b = f(100000, 3, 3), f(200000, 3, 3)
+    assert 0 < a < b and b - a > 100000 * 1000       # at least 1 KB per cell of a 3x3 system
+    assert f(100000, 2, 3) < a                         # 2x2 blocks take less
+    assert f(0, 3, 3) == -1 and f(10, 4, 3) == -1      # rejected arguments
