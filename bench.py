@@ -304,12 +304,18 @@ def run_ours(args):
     kst = mixed["kst"]
     achieved = kst["solve_bytes"] / (kst["solve_ms"] / 1000.0) / 1e9 if kst["solve_ms"] > 0 else 0.0
     avg_launch_ms = kst["solve_ms"] / max(1, kst["solve_launches"])
+    # DRAM traffic of the solver per launch: the ratio of DRAM bytes
+    # (dram__bytes_read.sum + dram__bytes_write.sum) to algorithmic bytes of an
+    # ncu capture of this workload's solve (profiles/traffic.json), applied to
+    # this run's algorithmic bytes per launch
     traffic = None
     tfile = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tfile):
         try:
             with open(tfile) as f:
-                traffic = json.load(f).get(args.workload)
+                ent = json.load(f).get(args.workload)
+            if ent:
+                traffic = ent["dram_per_algorithmic_byte"] * kst["solve_bytes"] / max(1, kst["solve_launches"])
         except Exception:
             traffic = None
     lin_ach = kst["linearize_bytes"] / (kst["linearize_ms"] / 1000.0) / 1e9 if kst["linearize_ms"] > 0 else 0.0
@@ -353,7 +359,22 @@ def run_ours(args):
 
 def run_profile_case(args):
     """Initial state of the workload: one linearization (iteration 0) and one
-    mixed-precision solve, the unit an ncu capture of the solver covers."""
+    mixed-precision solve, the unit an ncu capture of the solver covers.
+    With --ensemble K: one batched time step of K realizations (clusters of
+    2 blocks); prints the batched solve's launches and algorithmic bytes."""
+    if args.ensemble > 0:
+        probs = ensemble_problems(args.ensemble)  # spawned pool, before any CUDA call
+        import __graft_entry__ as ge
+        ge.build()
+        from gbfv import Batch, capi
+        B = Batch(probs, params(capi.PREC_MIXED), cluster_size=2)
+        st = B.time_integration(1, ENSEMBLE["dt"])
+        s1 = B.stats()
+        print(json.dumps({"ensemble": len(probs), "status": st, "solve_launches": s1["solve_launches"],
+                          "solve_bytes": s1["solve_bytes"], "solve_ms": s1["solve_ms"],
+                          "cells": int(sum(p.num_cells for p in probs))}))
+        B.close()
+        return 0 if st == 0 else 1
     import __graft_entry__ as ge
     ge.build()
     from gbfv import Context, capi
@@ -492,6 +513,14 @@ def run_ensemble(args):
     solve_ms = s1["solve_ms"] - s0["solve_ms"]
     solve_bytes = s1["solve_bytes"] - s0["solve_bytes"]
     achieved = solve_bytes / (solve_ms / 1000.0) / 1e9 if solve_ms > 0 else 0.0
+    solve_launches = max(1, s1["solve_launches"] - s0["solve_launches"])
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tfile):
+        with open(tfile) as f:
+            ent = json.load(f).get("ensemble")
+        if ent:  # DRAM bytes per algorithmic byte of an ncu capture of the batched solve
+            traffic = ent["dram_per_algorithmic_byte"] * solve_bytes / solve_launches
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_tot / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -512,7 +541,7 @@ def run_ensemble(args):
         "gpu_launches": int((s1["kernel_launches"] - s0["kernel_launches"]) / args.steps),
         "newton_iterations_first_systems": newton[:4],
         "roofline": {"bound": "hbm", "kernel": "kBicgstabBatch<float,2> (batched persistent ILU0 + BiCGStab)",
-                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                      "peak_kind": peak_kind},
         "clocks": clocks,
     }
