@@ -632,12 +632,12 @@ def run_serve(args):
 
 def main():
     args = parse()
+    if args.profile_case:
+        return run_profile_case(args)
     if args.serve:
         return run_serve(args)
     if args.ensemble > 0:
         return run_ensemble(args)
-    if args.profile_case:
-        return run_profile_case(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)
