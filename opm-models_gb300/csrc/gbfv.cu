@@ -101,7 +101,8 @@ struct SolverData {
     int* pushL = nullptr;       // push targets for the current (C, G, NT)
     int* pushU = nullptr;
     int* levVals = nullptr;     // values each block receives per level and sweep
-    int pushKey[3] = {0, 0, 0};
+    int pushKey[4] = {0, 0, 0, 0};
+    int ownerMode = 0;          // rows of a level to blocks: warp round-robin (0) / contiguous (1)
     unsigned long long* prof = nullptr;  // per-phase timers of the solve kernel (GBFV_PROFILE=1)
     // cumulative statistics of the persistent solve kernel
     cudaEvent_t evA = nullptr, evB = nullptr;
@@ -294,6 +295,27 @@ void buildOrder(int N, const std::vector<std::vector<int>>& lower, std::vector<i
     }
 }
 
+// Block and thread slot (within the level group) that own position t of a
+// level of width W: warps dealt round-robin (mode 0) or contiguous shares
+// rounded to whole warps (mode 1); the device side is SweepMap::pos.
+inline void levelSlot(int t, int W, int C, int mode, int& owner, int& uu)
+{
+    if (mode == 0) {
+        const int w = t >> 5;
+        owner = w % C;
+        uu = ((w / C) << 5) | (t & 31);
+        return;
+    }
+    const int chunk = (((W + C - 1) / C) + 31) & ~31;
+    owner = t / chunk;
+    uu = t - owner * chunk;
+}
+// the most rows one block takes in a level of width W
+inline int levelChunk(int W, int C, int mode)
+{
+    return mode == 0 ? 32 * ((W + 32 * C - 1) / (32 * C)) : (((W + C - 1) / C) + 31) & ~31;
+}
+
 // Which levels of a sweep need the cluster-wide level barrier.  A block
 // pushes the results of level l into the consumer block's dependency buffer
 // (l+1) mod PUSH_BUFFERS, which the consumer last read at level
@@ -305,12 +327,17 @@ void buildOrder(int N, const std::vector<std::vector<int>>& lower, std::vector<i
 // orderings and along the cluster barriers placed so far.  Where a push is
 // not covered, a cluster barrier is placed after the previous level.
 // barrierAfter[l] (level index, in the sweep's own order) is the result.
-void placeLevelBarriers(const SolverData& S, int C, const std::vector<int>& lev, bool forward,
+void placeLevelBarriers(const SolverData& S, int C, int mode, const std::vector<int>& lev, bool forward,
                         std::vector<char>& barrierAfter)
 {
     const int N = S.N, ld = S.ldN, dim = S.dim, nl = (int)S.levPtr.size() - 1, D = PUSH_BUFFERS;
     barrierAfter.assign(nl, 0);
-    auto owner = [&](int p) { return ((p - S.levPtr[lev[p]]) >> 5) % C; };
+    auto owner = [&](int p) {
+        int o, uu;
+        const int l = lev[p];
+        levelSlot(p - S.levPtr[l], S.levPtr[l + 1] - S.levPtr[l], C, mode, o, uu);
+        return o;
+    };
     std::vector<int> K((size_t)C * C, -1), Knew;   // K[X*C + Y]: known finished step of Y when X finished its last
     std::vector<int> know((size_t)N * C, -1);
     std::vector<int> acc(C);
@@ -356,25 +383,30 @@ void placeLevelBarriers(const SolverData& S, int C, const std::vector<int>& lev,
 // NT threads per block: for each row and each neighbour in the dependency
 // direction, the consumer's block and the offset of its slot (see
 // SweepMap in solver.cu).
-int buildPushTargets(SolverData& S, int C, int G, int NT)
+int buildPushTargets(SolverData& S, int C, int G, int NT, int mode)
 {
-    if (S.pushKey[0] == C && S.pushKey[1] == G && S.pushKey[2] == NT && S.pushL) return GBFV_OK;
+    if (S.pushKey[0] == C && S.pushKey[1] == G && S.pushKey[2] == NT && S.pushKey[3] == mode && S.pushL)
+        return GBFV_OK;
     const int N = S.N, ld = S.ldN, dim = S.dim, B = S.b, NG = NT / G;
     const int PB = padB(B);  // values per dependency slot
     std::vector<int> lev(N);
     for (size_t l = 0; l + 1 < S.levPtr.size(); ++l)
         for (int p = S.levPtr[l]; p < S.levPtr[l + 1]; ++p) lev[p] = (int)l;
     auto target = [&](int j, int slot) {
-        const int t = j - S.levPtr[lev[j]];
-        const int w = t >> 5;
-        const int owner = w % C;
-        const int uu = ((w / C) << 5) | (t & 31);
-        const int cslot = (lev[j] % G) * NG + uu;
+        const int l = lev[j];
+        int owner, uu;
+        levelSlot(j - S.levPtr[l], S.levPtr[l + 1] - S.levPtr[l], C, mode, owner, uu);
+        const int cslot = (l % G) * NG + uu;
         return (owner << 24) | ((cslot * 3 + slot) * PB);
     };
     const int nl = (int)S.levPtr.size() - 1;
     std::vector<int> hL((size_t)3 * ld, -1), hU((size_t)3 * ld, -1), hV((size_t)C * nl * 2, 0);
-    auto ownerOf = [&](int p) { return ((p - S.levPtr[lev[p]]) >> 5) % C; };
+    auto ownerOf = [&](int p) {
+        int o, uu;
+        const int l = lev[p];
+        levelSlot(p - S.levPtr[l], S.levPtr[l + 1] - S.levPtr[l], C, mode, o, uu);
+        return o;
+    };
     for (int p = 0; p < N; ++p) {
         const int owner = ownerOf(p);
         for (int q = 0; q < dim; ++q) {
@@ -392,8 +424,8 @@ int buildPushTargets(SolverData& S, int C, int G, int NT)
     }
     if (!getenv("GBFV_LEVEL_BARRIER")) {
         std::vector<char> barF, barB;
-        placeLevelBarriers(S, C, lev, true, barF);
-        placeLevelBarriers(S, C, lev, false, barB);
+        placeLevelBarriers(S, C, mode, lev, true, barF);
+        placeLevelBarriers(S, C, mode, lev, false, barB);
         for (int r = 0; r < C; ++r)
             for (int l = 0; l < nl; ++l) {
                 if (barF[l]) hV[((size_t)r * nl + l) * 2] |= PUSH_BARRIER_FLAG;
@@ -411,6 +443,7 @@ int buildPushTargets(SolverData& S, int C, int G, int NT)
     S.pushKey[0] = C;
     S.pushKey[1] = G;
     S.pushKey[2] = NT;
+    S.pushKey[3] = mode;
     return GBFV_OK;
 }
 
@@ -462,18 +495,23 @@ int fillKArgs(SolverData& S, DevStatus* st, const T* A, T* FL, T* FD, const T* r
     a.factor = factor;
     a.prof = S.prof;
     {
-        int maxW = 0;
-        for (size_t l = 0; l + 1 < S.levPtr.size(); ++l) maxW = std::max(maxW, S.levPtr[l + 1] - S.levPtr[l]);
-        a.dsmem = (mode == SYNC_CLUSTER && S.adjacentLevels && maxW <= nblocks * clusterThreads<T>() &&
+        int omode = S.ownerMode;
+        if (const char* e = getenv("GBFV_OWNER")) omode = strcmp(e, "contig") == 0 ? 1 : 0;
+        a.ownerMode = omode;
+        int maxChunk = 0;  // the most rows one block takes in a level
+        for (size_t l = 0; l + 1 < S.levPtr.size(); ++l)
+            maxChunk = std::max(maxChunk, levelChunk(S.levPtr[l + 1] - S.levPtr[l], nblocks, omode));
+        constexpr int NTC = clusterThreads<T>();
+        a.dsmem = (mode == SYNC_CLUSTER && S.adjacentLevels && maxChunk <= NTC &&
                    (int)S.levPtr.size() - 1 <= MAX_PUSH_LEVELS && !getenv("GBFV_NO_DSMEM")) ? 1 : 0;
-        // as many level groups as fit (each group must cover the widest level)
+        // as many level groups as fit (each group must cover a block's share of the widest level)
         a.grp = 1;
         for (int g : {8, 4, 2})
-            if (maxW <= nblocks * (clusterThreads<T>() / g)) { a.grp = g; break; }
+            if (maxChunk <= NTC / g) { a.grp = g; break; }
         if (const char* e = getenv("GBFV_GROUPS")) a.grp = std::max(1, std::min(a.grp, atoi(e)));
         a.pushL = a.pushU = a.levVals = nullptr;
         if (a.dsmem) {
-            const int ps = buildPushTargets(S, nblocks, a.grp, clusterThreads<T>());
+            const int ps = buildPushTargets(S, nblocks, a.grp, NTC, omode);
             if (ps) return ps;
             a.pushL = S.pushL;
             a.pushU = S.pushU;

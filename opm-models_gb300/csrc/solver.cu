@@ -525,15 +525,14 @@ struct SweepMap {
         grp = tid / NG;
         u = tid - grp * NG;
     }
-    // this thread's position inside a level it works on
-    __device__ __forceinline__ int pos() const { return ((((u >> 5) * C) + rank) << 5) | (u & 31); }
-    // block and thread slot of position t of level l
-    __device__ __forceinline__ void slotOf(int t, int l, int& owner, int& cslot) const
+    // this thread's position inside level l of width W, or -1: warps dealt
+    // round-robin to the blocks (ownerMode 0), or each block a contiguous
+    // share rounded to whole warps (ownerMode 1)
+    __device__ __forceinline__ int pos(int W, int ownerMode) const
     {
-        const int w = t >> 5;
-        owner = w % C;
-        const int uu = ((w / C) << 5) | (t & 31);
-        cslot = (l % G) * NG + uu;
+        if (ownerMode == 0) return ((((u >> 5) * C) + rank) << 5) | (u & 31);
+        const int chunk = (((W + C - 1) / C) + 31) & ~31;
+        return u < chunk ? rank * chunk + u : -1;
     }
 };
 
@@ -616,8 +615,9 @@ __device__ __forceinline__ void sweepLowerPush(const KArgs<T>& a, const T* d, T*
     auto load = [&](int l) {
         iCur = -1;
         if (l >= nl) return;
-        const int i = sm.lev[l] + mp.pos();
-        if (i >= sm.lev[l + 1]) return;
+        const int t = mp.pos(sm.lev[l + 1] - sm.lev[l], a.ownerMode);
+        const int i = sm.lev[l] + t;
+        if (t < 0 || i >= sm.lev[l + 1]) return;
         iCur = i;
 #pragma unroll
         for (int s = 0; s < 3; ++s) {
@@ -752,8 +752,9 @@ __device__ __forceinline__ void sweepUpperPush(const KArgs<T>& a, T* y, const Te
     auto load = [&](int l) {
         iCur = -1;
         if (l < 0) return;
-        const int i = sm.lev[l] + mp.pos();
-        if (i >= sm.lev[l + 1]) return;
+        const int t = mp.pos(sm.lev[l + 1] - sm.lev[l], a.ownerMode);
+        const int i = sm.lev[l] + t;
+        if (t < 0 || i >= sm.lev[l + 1]) return;
         iCur = i;
 #pragma unroll
         for (int q = 0; q < 3; ++q) {

@@ -44,6 +44,7 @@ struct KArgs {
     unsigned long long* prof;  // optional per-phase nanoseconds (block 0, thread 0): factor,
                                // L sweep, U sweep, SpMV+dot, update+max, count of iterations
     int grp;            // push sweeps: number of level-rotating thread groups
+    int ownerMode;      // push sweeps: rows of a level dealt to blocks by warp round-robin (0) or contiguously (1)
     const int* pushL;   // push sweeps: consumer block/slot of each upper neighbour [q*ldN + p]
     const int* pushU;   // push sweeps: consumer block/slot of each lower neighbour [q*ldN + p]
     const int* levVals; // push sweeps: values block r receives at level l, [(r*numLev + l)*2 + fwd/bwd]
