@@ -545,7 +545,14 @@ def run_ensemble(args):
                      "peak_kind": peak_kind},
         "clocks": clocks,
     }
+    if world > 1:
+        line["n_gpus"] = world
+        line["config"]["parallelism"] = "replicas (systems assigned to ranks by size)"
+        line["config"]["systems_on_rank0"] = len(probs)
     print(json.dumps(line))
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
     return 0
 
 
@@ -619,14 +626,7 @@ def run_serve(args):
         "p50_ms": served[top]["p50_ms"], "p99_ms": served[top]["p99_ms"],
         "clocks": clocks,
     }
-    if world > 1:
-        line["n_gpus"] = world
-        line["config"]["parallelism"] = "replicas (systems assigned to ranks by size)"
-        line["config"]["systems_on_rank0"] = len(probs)
     print(json.dumps(line))
-    if world > 1:
-        dist.barrier()
-        dist.destroy_process_group()
     return 0
 
 
