@@ -267,6 +267,22 @@ def run_ours(args):
         cfg = ctx.solver_config(prec)
         results[name] = dict(ms=ms, cits=cits, its=its, launches=launches, kst=kst, clocks=clocks, ctx=ctx,
                              cfg=cfg)
+    # error of the mixed-precision solve against the FP64 solve of the same
+    # Newton system (first Newton iteration of the first time step; the FP64
+    # GPU path equals the CPU oracle to 1e-8 in the parity tests)
+    solve_err = None
+    try:
+        cm, cf = results["mixed"]["ctx"], results["fp64"]["ctx"]
+        dxs = []
+        for c in (cm, cf):
+            c.restore_state()
+            if c.linearize(w["dt"], 0):
+                raise RuntimeError("linearization failed")
+            _, dx, _ = c.solve(want_dx=True)
+            dxs.append(dx)
+        solve_err = float(np.max(np.abs(dxs[0] - dxs[1])) / max(np.max(np.abs(dxs[1])), 1e-300))
+    except Exception:
+        solve_err = None
     # end-to-end through the C ABI with host buffers (mixed form)
     ctx = results["mixed"]["ctx"]
     pv_host = torch.empty(N * 3, dtype=torch.float64, pin_memory=True).numpy()
@@ -335,6 +351,7 @@ def run_ours(args):
         "mixed_over_plain": value / plain_value,
         "newton_iterations": sn0.tolist(), "linear_iterations": sl0.tolist(),
         "same_newton_iterations": bool(np.array_equal(sn0, spn)),
+        "mixed_solve_error_vs_fp64": solve_err,
         "e2e": {"value": e2e_cits / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(N * 3 * 8 + N * 4),
                 "d2h_bytes_per_step": int(N * 3 * 8 + N * 4)},
         "gpu_launches": int(mixed["launches"] / args.steps),
