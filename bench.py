@@ -574,7 +574,7 @@ def run_ensemble(args):
 
 
 SERVE = dict(lo=20000, hi=1000000, pool=12, requests=24, rates=(50, 200, 1000, 2000), seed=2024, dt=86400.0,
-             capacity=16, cluster=8)
+             capacity=16, cluster=8, lanes=((150000, 12, 4),))
 
 
 def _serve_problem(job):
@@ -603,10 +603,10 @@ def run_serve(args):
     import __graft_entry__ as ge
     ge.build()
     from gbfv import capi
-    from gbfv.serving import Request, Server, latency_summary, serve, serve_one_at_a_time
+    from gbfv.serving import (LanedServer, Request, Server, latency_summary, serve, serve_laned,
+                              serve_one_at_a_time)
     prm = params(capi.PREC_MIXED)
-    srv = Server(capi.MODEL_BLACKOIL_3P, prm, capacity=SERVE["capacity"], cluster_size=SERVE["cluster"],
-                 max_cells=max(p.num_cells for p in probs))
+    big = max(p.num_cells for p in probs)
 
     def trace(rate, seed):
         r = np.random.default_rng(seed)
@@ -614,15 +614,25 @@ def run_serve(args):
         return [Request(probs[i % len(probs)], steps=1, dt=SERVE["dt"], arrival=float(a), rid=i)
                 for i, a in enumerate(t)]
 
+    # one lane: every request in one batch
+    srv = Server(capi.MODEL_BLACKOIL_3P, prm, capacity=SERVE["capacity"], cluster_size=SERVE["cluster"],
+                 max_cells=big)
     serve(srv, trace(1000, 1)[:4])  # warm-up: module load, graphs, pinned buffers
+    top_rate = SERVE["rates"][-1]
+    single = latency_summary(serve(srv, trace(top_rate, top_rate)))
+    srv.close()
+    # size lanes: requests up to 150k cells in clusters of 4, larger ones in
+    # clusters of 16, side by side on their own streams
+    laned = LanedServer(capi.MODEL_BLACKOIL_3P, prm, lanes=SERVE["lanes"] + ((big, 4, 16),))
+    serve_laned(laned, trace(1000, 1)[:6])
     sampler = ClockSampler(0)
     sampler.start()
     served = {}
     for rate in SERVE["rates"]:
-        reqs = serve(srv, trace(rate, rate))
+        reqs = serve_laned(laned, trace(rate, rate))
         served[str(rate)] = latency_summary(reqs)
     clocks = sampler.stop()
-    srv.close()
+    laned.close()
     base = {}
     for rate in (SERVE["rates"][0], SERVE["rates"][-1]):
         reqs = serve_one_at_a_time(trace(rate, rate), params(capi.PREC_FP64))
@@ -636,9 +646,11 @@ def run_serve(args):
         "config": {"workload": "served stream of single-time-step black-oil solves, Poisson arrivals at %s req/s, "
                                "%d requests per rate, continuous batching, admission by HBM footprint, "
                                "mixed precision" % (list(SERVE["rates"]), SERVE["requests"]),
-                   "pool_cells": [int(p.num_cells) for p in probs], "capacity": SERVE["capacity"],
-                   "cluster_size": SERVE["cluster"], "parallelism": "single GPU"},
+                   "pool_cells": [int(p.num_cells) for p in probs],
+                   "lanes": "cells <= 150k: 12 slots, clusters of 4; larger: 4 slots, clusters of 16",
+                   "parallelism": "single GPU"},
         "served": served,
+        "one_lane_at_top_rate": single,
         "one_at_a_time_fp64": base,
         "p50_ms": served[top]["p50_ms"], "p99_ms": served[top]["p99_ms"],
         "clocks": clocks,

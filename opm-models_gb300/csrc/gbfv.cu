@@ -25,7 +25,8 @@
 #include "solver.cuh"
 
 namespace gbfv {
-int64_t g_launches = 0;
+std::atomic<int64_t> g_launches{0};
+thread_local int t_captureLaunches = -1;
 }
 
 using namespace gbfv;
@@ -703,7 +704,7 @@ void gbfv_default_params(gbfv_params* p)
     p->max_time_step_divisions = 10;
 }
 
-int64_t gbfv_kernel_launches(void) { return g_launches; }
+int64_t gbfv_kernel_launches(void) { return g_launches.load(); }
 const char* gbfv_last_error(void) { return t_lastError.c_str(); }
 
 static int createImpl(gbfv_ctx* C, const gbfv_problem* P)
@@ -1859,7 +1860,10 @@ int pinnedAlloc(T** p, size_t n)
 template <class F>
 int captureGraph(gbfv_batch* B, GraphSet& g, F&& fn)
 {
-    const int64_t before = g_launches;
+    struct CountScope {
+        CountScope() { t_captureLaunches = 0; }
+        ~CountScope() { t_captureLaunches = -1; }
+    } scope;
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal));
     const int st = fn();
@@ -1872,8 +1876,7 @@ int captureGraph(gbfv_batch* B, GraphSet& g, F&& fn)
     const cudaError_t ei = cudaGraphInstantiate(&g.exec, graph, 0);
     cudaGraphDestroy(graph);
     CK(ei);
-    g.kernels = (int)(g_launches - before);
-    g_launches = before;  // counted when the graph is replayed
+    g.kernels = t_captureLaunches;  // counted when the graph is replayed
     return GBFV_OK;
 }
 

@@ -17,6 +17,7 @@
 // Vectors (solution, residual, Krylov vectors) are block vectors in the same
 // cell order: entry e of cell p at [p*b + e].
 #pragma once
+#include <atomic>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -135,8 +136,16 @@ struct JobState {
     int active;
 };
 
-extern int64_t g_launches;
-inline void countLaunch(int n = 1) { g_launches += n; }
+// kernel launches of this library (several host threads may launch: atomic);
+// while a thread captures a CUDA graph its launches are counted for the
+// graph instead and added to the total each time the graph is replayed
+extern std::atomic<int64_t> g_launches;
+extern thread_local int t_captureLaunches;
+inline void countLaunch(int n = 1)
+{
+    if (t_captureLaunches >= 0) t_captureLaunches += n;
+    else g_launches += n;
+}
 
 // ---------------------------------------------------- kernel launchers ----
 void launchApplyConstraints(const DevMesh& m, double* x, double* xOld, int* meaning, int* meaningOld,

@@ -134,13 +134,13 @@ class Server:
             pass
 
 
-def serve(server, requests, clock=time.perf_counter, keep_solution=True):
-    """Run a trace of requests (arrival times in seconds from the start)
-    through the server; fills admitted / finished (state on the host) /
+def serve(server, requests, clock=time.perf_counter, keep_solution=True, t0=None):
+    """Run a trace of requests (arrival times in seconds from t0, default
+    now) through the server; fills admitted / finished (state on the host) /
     status of each."""
     pending = collections.deque(sorted(requests, key=lambda r: r.arrival))
     queue = collections.deque()
-    t0 = clock()
+    t0 = clock() if t0 is None else t0
     left = len(pending)
     while left:
         now = clock() - t0
@@ -155,6 +155,64 @@ def serve(server, requests, clock=time.perf_counter, keep_solution=True):
             time.sleep(max(0.0, min(0.001, pending[0].arrival - now)))
         elif queue:
             raise RuntimeError("a queued request does not fit the server even when it is empty")
+    return requests
+
+
+class LanedServer:
+    """Several servers ("lanes") side by side, each for requests up to its
+    size limit, each with its own CUDA stream and host thread.  In one lane
+    every round waits for its slowest system, so small requests would wait
+    for the million-cell solves of large ones; in their own lane they take
+    rounds of their own size while the large ones run beside them.  Each lane
+    holds a share of the HBM budget and of the GPU's clusters (its capacity
+    times its cluster size in blocks)."""
+
+    def __init__(self, model, params, lanes=((150000, 12, 4), (1 << 21, 4, 16)), hbm_budget=None):
+        if hbm_budget is None:
+            import torch
+            free, _ = torch.cuda.mem_get_info()
+            hbm_budget = int(0.8 * free)
+        shares = [cap * cl for _, cap, cl in lanes]
+        self.lanes = []
+        for (max_cells, cap, cl), sh in zip(lanes, shares):
+            srv = Server(model, params, capacity=cap, cluster_size=cl, max_cells=max_cells,
+                         hbm_budget=int(hbm_budget * sh / sum(shares)))
+            self.lanes.append((max_cells, srv))
+
+    def lane_of(self, problem):
+        for i, (max_cells, _) in enumerate(self.lanes):
+            if problem.num_cells <= max_cells:
+                return i
+        raise ValueError("request larger than every lane")
+
+    def close(self):
+        for _, srv in self.lanes:
+            srv.close()
+
+
+def serve_laned(laned, requests, clock=time.perf_counter, keep_solution=True):
+    """Run a trace through a LanedServer: one host thread per lane, a common
+    time origin."""
+    import threading
+    parts = [[] for _ in laned.lanes]
+    for r in requests:
+        parts[laned.lane_of(r.problem)].append(r)
+    t0 = clock()
+    errors = []
+
+    def run(i):
+        try:
+            serve(laned.lanes[i][1], parts[i], clock, keep_solution, t0)
+        except Exception as e:  # reported after the other lanes finish
+            errors.append(e)
+
+    threads = [threading.Thread(target=run, args=(i,)) for i in range(len(parts)) if parts[i]]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    if errors:
+        raise errors[0]
     return requests
 
 

@@ -91,3 +91,19 @@ def test_served_trace_latencies(built):
     assert s["requests"] == 6 and s["failed"] == 0
     assert 0 < s["p50_ms"] <= s["p99_ms"]
     assert all(r.admitted >= r.arrival for r in reqs)
+
+
+def test_laned_server_results_equal_alone(built):
+    from gbfv.serving import LanedServer, serve_laned
+    prm = _prm()
+    probs = [problems.blackoil(10, 9, 3, seed=31), problems.blackoil(16, 14, 5, seed=32),
+             problems.blackoil(8, 8, 3, seed=33), problems.blackoil(15, 15, 4, seed=34)]
+    laned = LanedServer(capi.MODEL_BLACKOIL_3P, prm, lanes=((400, 2, CLUSTER), (4096, 2, CLUSTER)))
+    assert [laned.lane_of(p) for p in probs] == [0, 1, 0, 1]
+    reqs = [Request(p, steps=1, arrival=0.001 * i, rid=i) for i, p in enumerate(probs)]
+    serve_laned(laned, reqs)
+    laned.close()
+    for req in reqs:
+        assert req.status == 0
+        st, sn, sl, (x, m) = _alone(req.problem, prm, 1, 86400.0)
+        assert np.array_equal(req.solution[0], x) and np.array_equal(req.solution[1], m), req.rid
