@@ -64,6 +64,14 @@ enum gbfv_law {
 };
 
 /* boundary condition kinds (ImmiscibleBoundaryRateVector setters) */
+/* flux module (Properties::FluxModule): Darcy (darcyfluxmodule.hh:183-525,
+ * the default) or two-point transmissibilities (transfluxmodule.hh:201-480,
+ * used by lens_immiscible_ecfv_ad_trans.cc:55-58; immiscible model only)   */
+enum gbfv_flux {
+    GBFV_FLUX_DARCY = 0,
+    GBFV_FLUX_TRANS = 1
+};
+
 enum gbfv_bc {
     GBFV_BC_NOFLOW = 0,   /* setNoFlow()                                    */
     GBFV_BC_FREEFLOW = 1, /* setFreeFlow(fs): Dirichlet state (p_w, S_w)    */
@@ -151,6 +159,7 @@ typedef struct gbfv_problem {
     double rho[2], mu[2];     /* immiscible: constant liquid density/visc.   */
     const gbfv_blackoil_pvt* pvt; /* black-oil only, else NULL               */
     double temperature;
+    int32_t flux_module;      /* enum gbfv_flux: Properties::FluxModule      */
 } gbfv_problem;
 
 /* run-time parameters; names and defaults follow the reference's

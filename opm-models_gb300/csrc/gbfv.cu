@@ -851,6 +851,64 @@ static int createImpl(gbfv_ctx* C, const gbfv_problem* P)
             hArea[o] = P->conn_area[c];
         }
     }
+    // transmissibility flux module (transfluxmodule.hh:201-480): face
+    // transmissibilities, hydrostatic depth terms and upwind tie rules
+    const int fluxModule = P->flux_module;
+    if (fluxModule != GBFV_FLUX_DARCY && fluxModule != GBFV_FLUX_TRANS) return GBFV_ERR_ARG;
+    if (fluxModule == GBFV_FLUX_TRANS && P->model != GBFV_MODEL_IMMISCIBLE_2P) {
+        setError("the transmissibility flux module is supported for the immiscible model");
+        return GBFV_ERR_UNSUPPORTED;
+    }
+    int dimWorld = 1;  // the highest coordinate axis the faces use, plus one
+    for (int c = 0; c < P->num_conn; ++c)
+        for (int d = 0; d < 3; ++d)
+            if (P->conn_normal[3 * c + d] != 0.0) dimWorld = std::max(dimWorld, d + 1);
+    auto axisOfNormal = [&](const double* n) {
+        int idx = 0;
+        double val = 0.0;
+        for (int d = 0; d < dimWorld; ++d)
+            if (std::abs(n[d]) > val) { val = std::abs(n[d]); idx = d; }
+        return idx;
+    };
+    std::vector<double> hTrans, hDzg;
+    std::vector<int> hTie;
+    if (fluxModule == GBFV_FLUX_TRANS) {
+        hTrans.assign((size_t)ndir * ld, 0.0);
+        hDzg.assign((size_t)ndir * ld, 0.0);
+        hTie.assign((size_t)ndir * ld, 1);
+        const double gz = g[dimWorld - 1];
+        for (int p = 0; p < N; ++p) {
+            const int I = iperm[p];
+            const double* xI = &P->center[3 * I];
+            for (int dir = 0; dir < ndir; ++dir) {
+                const int J = nbrDir[(size_t)I * ndir + dir];
+                if (J < 0) continue;
+                const int c = connOf[(size_t)I * ndir + dir];
+                const double* xJ = &P->center[3 * J];
+                const double* xf = &P->conn_center[3 * c];
+                const double* n = &P->conn_normal[3 * c];
+                double nd0 = 0, nd1 = 0, s0 = 0, s1 = 0;
+                for (int d = 0; d < 3; ++d) {
+                    const double d0 = xf[d] - xI[d], d1 = xf[d] - xJ[d];
+                    nd0 += n[d] * d0;
+                    nd1 += n[d] * d1;
+                    s0 += d0 * d0;
+                    s1 += d1 * d1;
+                }
+                nd0 = std::abs(nd0);
+                nd1 = std::abs(nd1);
+                const int idx = axisOfNormal(n);
+                const double T0 = P->perm[3 * I + idx] * nd0 / s0;
+                const double T1 = P->perm[3 * J + idx] * nd1 / s1;
+                const size_t o = (size_t)dir * ld + p;
+                hTrans[o] = T0 * T1 / (T0 + T1);
+                const double distZ = xI[dimWorld - 1] - xJ[dimWorld - 1];
+                hDzg[o] = distZ * gz;
+                const double Vin = P->volume[I], Vex = P->volume[J];
+                hTie[o] = Vin > Vex ? 1 : (Vin < Vex ? 0 : (I < J ? 1 : 0));
+            }
+        }
+    }
     std::vector<double> hVol(ld, 1.0), hPor(ld, 0.0), hPerm((size_t)3 * ld, 0.0);
     std::vector<int> hMat(ld, 0), hCflag(ld, -1);
     for (int p = 0; p < N; ++p) {
@@ -963,6 +1021,25 @@ static int createImpl(gbfv_ctx* C, const gbfv_problem* P)
                     bf.mobb[a] = krb[a] / P->mu[a];
                     bf.rhob[a] = P->rho[a];
                 }
+                if (fluxModule == GBFV_FLUX_TRANS) {
+                    // transmissibilityBoundary_ (transfluxmodule.hh:457-480) takes the
+                    // geometry of the cell's interior face with the boundary face's index
+                    const int c = P->conn_ptr[I] + (f - P->bface_ptr[I]);
+                    if (c >= P->conn_ptr[I + 1]) {
+                        setError("transmissibility boundary face without an interior face of the same index");
+                        return GBFV_ERR_UNSUPPORTED;
+                    }
+                    const double* n = &P->conn_normal[3 * c];
+                    const double* xc = &P->conn_center[3 * c];
+                    double nd = 0, s0 = 0;
+                    for (int d = 0; d < 3; ++d) {
+                        const double t = xc[d] - xI[d];
+                        nd += n[d] * t;
+                        s0 += t * t;
+                    }
+                    bf.transB = P->perm[3 * I + axisOfNormal(n)] * nd / s0;
+                    bf.dzgB = (xI[dimWorld - 1] - xf[dimWorld - 1]) * g[dimWorld - 1];
+                }
             }
             hBf.push_back(bf);
         }
@@ -1056,6 +1133,17 @@ static int createImpl(gbfv_ctx* C, const gbfv_problem* P)
     m.consMeaning = dConsMeaning;
     m.numConsCells = (int)consCells.size();
     m.inst = nullptr;
+    m.fluxModule = fluxModule;
+    m.trans = m.dzg = nullptr;
+    m.tieUpI = nullptr;
+    if (fluxModule == GBFV_FLUX_TRANS) {
+        double *dTrans, *dDzg;
+        int* dTie;
+        if ((st = up(&dTrans, hTrans)) || (st = up(&dDzg, hDzg)) || (st = up(&dTie, hTie))) return st;
+        m.trans = dTrans;
+        m.dzg = dDzg;
+        m.tieUpI = dTie;
+    }
     if ((st = devAlloc(&C->dphys, 1))) return st;
     CK(cudaMemcpy(C->dphys, &ph, sizeof(DevPhysics), cudaMemcpyHostToDevice));
     // state

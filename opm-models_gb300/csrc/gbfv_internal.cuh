@@ -44,6 +44,8 @@ struct BFace {
     double mobb[2]; // kr/mu of the boundary state
     double rhob[2]; // boundary densities
     double rate[3]; // mass-rate boundary values per equation
+    double transB;  // transmissibility flux module: boundary transmissibility
+    double dzgB;    // and (z_cell - z_face) * g
 };
 
 // static description of one grid (or one batch of grids) on the device
@@ -74,6 +76,10 @@ struct DevMesh {
     int numConsCells;
     int slotOfDir[6];     // ELL slot of intersection direction
     const int* inst;      // [p] instance of the cell (batched systems)
+    int fluxModule;       // enum gbfv_flux
+    const double* trans;  // [dir*ldN + p] transmissibility flux module: face transmissibility
+    const double* dzg;    // [dir*ldN + p] (z_I - z_J) * g
+    const int* tieUpI;    // [dir*ldN + p] interior upstream when the pressure difference is zero
 };
 
 struct DevPhysics {

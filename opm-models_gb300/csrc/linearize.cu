@@ -254,6 +254,26 @@ __device__ __forceinline__ Dual<B> darcyPhase(const Dual<B>& pI, double pJ, cons
     return fv * nrm;
 }
 
+// Transmissibility flux of one phase, focus = interior cell
+// (transfluxmodule.hh:201-318): hydrostatic correction with the average
+// density, upwind by the sign of the pressure difference, ties decided on the
+// host (larger volume, then lower global index), q = dp * lambda_up * (-T).
+__device__ __forceinline__ D2 transPhase(const D2& pI, double pJ, const D2& rhoI, double rhoJ, const D2& lamI,
+                                         double lamJ, double T, double dzg, bool tieUpI, bool& upI)
+{
+    if (lamI.v <= 0.0 && lamJ <= 0.0) {
+        upI = true;
+        return D2(0.0);
+    }
+    D2 rhoAvg = (rhoI + rhoJ) / 2.0;
+    D2 pEx(pJ);
+    pEx = pEx + rhoAvg * dzg;
+    D2 pd = pEx - pI;
+    upI = pd.v > 0.0 ? false : (pd.v < 0.0 ? true : tieUpI);
+    if (upI) return (pd * lamI) * (-T);
+    return pd * (lamJ * (-T));
+}
+
 __device__ __forceinline__ void kAssembleImmiscibleBody(const DevMesh& m, const DevPhysics* __restrict__ phys,
                                                            IqBuffers iq, double* __restrict__ storageOld,
                                                            int iter0, double dt,
@@ -285,7 +305,10 @@ __device__ __forceinline__ void kAssembleImmiscibleBody(const DevMesh& m, const 
             const double rhoJ = iq.val[(2 + a) * ld + q];
             const double lamJ = iq.val[(4 + a) * ld + q];
             bool upI;
-            D2 vf = darcyPhase<2>(pI[a], pJ, rhoI[a], rhoJ, lamI[a], lamJ, dTot, gIn, gEx, Kh, nrm, upI);
+            D2 vf = m.fluxModule == GBFV_FLUX_TRANS
+                        ? transPhase(pI[a], pJ, rhoI[a], rhoJ, lamI[a], lamJ, m.trans[dir * ld + p],
+                                     m.dzg[dir * ld + p], m.tieUpI[dir * ld + p] != 0, upI)
+                        : darcyPhase<2>(pI[a], pJ, rhoI[a], rhoJ, lamI[a], lamJ, dTot, gIn, gEx, Kh, nrm, upI);
             flux[a] = D2(0.0) + (upI ? vf * rhoI[a] : vf * rhoJ);
         }
         double alpha = 1.0;
@@ -320,6 +343,18 @@ __device__ __forceinline__ void kAssembleImmiscibleBody(const DevMesh& m, const 
         D2 values[2] = {D2(0.0), D2(0.0)};
         if (bf.type == GBFV_BC_MASSRATE) {
             for (int e = 0; e < 2; ++e) values[e] = D2(bf.rate[e]);
+        }
+        else if (bf.type == GBFV_BC_FREEFLOW && m.fluxModule == GBFV_FLUX_TRANS) {
+            // calculateBoundaryGradients_ of the transmissibility module (transfluxmodule.hh:324-415)
+            for (int a = 0; a < 2; ++a) {
+                D2 rhoAvg = (rhoI[a] + bf.rhob[a]) / 2.0;
+                D2 pEx(bf.pb[a]);
+                pEx = pEx + rhoAvg * bf.dzgB;
+                D2 pd = pEx - pI[a];
+                D2 vf = pd.v > 0.0 ? (pd * bf.mobb[a]) * (-bf.transB) : (pd * lamI[a]) * (-bf.transB);
+                D2 dens = bf.pb[a] > pI[a].v ? D2(bf.rhob[a]) : rhoI[a];
+                values[a] = values[a] + vf * dens;
+            }
         }
         else if (bf.type == GBFV_BC_FREEFLOW) {
             const double distSq = bf.tmpA * bf.tmpA;

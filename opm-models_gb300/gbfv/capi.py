@@ -45,6 +45,8 @@ GAS_RS = 1
 GAS_RV = 2
 PREC_FP64 = 0
 PREC_MIXED = 1
+FLUX_DARCY = 0
+FLUX_TRANS = 1
 MAT_STRIDE = 8
 
 dp = C.POINTER(C.c_double)
@@ -76,6 +78,7 @@ class Problem(C.Structure):
         ("gravity", C.c_double * 3), ("num_materials", C.c_int32), ("material_params", dp),
         ("rho", C.c_double * 2), ("mu", C.c_double * 2),
         ("pvt", C.POINTER(BlackOilPvt)), ("temperature", C.c_double),
+        ("flux_module", C.c_int32),
     ]
 
 

@@ -56,6 +56,7 @@ class ProblemData:
         self.init_meaning = None
         self.temperature = 293.15
         self.info = {}
+        self.flux_module = capi.FLUX_DARCY
 
     @property
     def num_cells(self):
@@ -97,6 +98,7 @@ class ProblemData:
         s.rho = (C.c_double * 2)(*self.rho)
         s.mu = (C.c_double * 2)(*self.mu)
         s.temperature = self.temperature
+        s.flux_module = self.flux_module
         if self.pvt_arrays is not None:
             a = self.pvt_arrays
             pv = capi.BlackOilPvt()
@@ -219,8 +221,10 @@ def bc_params(swr, snr, pe, lam):
     return [capi.LAW_REG_BROOKS_COREY, swr, snr, pe, lam, 0, 0, 0]
 
 
-def lens(nx=48, ny=32, law="vg", dim=2, nz=16):
-    """LensProblem (lensproblem.hh:227-627), default 2D 48x32 over 6 m x 4 m."""
+def lens(nx=48, ny=32, law="vg", dim=2, nz=16, flux="darcy"):
+    """LensProblem (lensproblem.hh:227-627), default 2D 48x32 over 6 m x 4 m;
+    flux="trans" selects the transmissibility flux module
+    (lens_immiscible_ecfv_ad_trans.cc:55-58)."""
     lx, ly, lz = 6.0, 4.0, 1.0
     g = structured_grid(nx, ny, nz, lx, ly, lz, dim)
     p = ProblemData(capi.MODEL_IMMISCIBLE_2P)
@@ -288,7 +292,11 @@ def lens(nx=48, ny=32, law="vg", dim=2, nz=16):
     pw = 1e5 - rho_w * gy * depth
     p.init_pv = np.ascontiguousarray(np.stack([pw, np.ones(N)], 1).ravel())
     p.init_meaning = np.zeros(N, np.int32)
-    p.info = dict(name="lens", nx=nx, ny=ny, nz=(nz if dim == 3 else 1), dim=dim)
+    p.info = dict(name="lens", nx=nx, ny=ny, nz=(nz if dim == 3 else 1), dim=dim, flux=flux)
+    if flux == "trans":
+        p.flux_module = capi.FLUX_TRANS
+    elif flux != "darcy":
+        raise ValueError("flux must be 'darcy' or 'trans'")
     return p
 
 

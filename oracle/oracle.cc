@@ -76,6 +76,8 @@ struct Prob {
     std::vector<double> coreyN;
     double rho[2] = {0, 0}, mu[2] = {0, 0};
     BlackOilPvt pvt;
+    int fluxModule = GBFV_FLUX_DARCY;
+    int dimWorld = 3;   // the highest coordinate axis the faces use, plus one
 };
 
 template <class T>
@@ -101,6 +103,14 @@ static Prob copyProblem(const gbfv_problem& q)
     P.connNormal = cp(q.conn_normal, 3 * (size_t)q.num_conn);
     P.connCenter = cp(q.conn_center, 3 * (size_t)q.num_conn);
     P.connArea = cp(q.conn_area, q.num_conn);
+    P.fluxModule = q.flux_module;
+    {
+        int maxAxis = 0;
+        for (int c = 0; c < q.num_conn; ++c)
+            for (int d = 0; d < 3; ++d)
+                if (q.conn_normal[3 * c + d] != 0.0) maxAxis = std::max(maxAxis, d);
+        P.dimWorld = maxAxis + 1;
+    }
     P.bfPtr = cp(q.bface_ptr, N + 1);
     P.bfType = cp(q.bface_type, q.num_bfaces);
     P.bfNormal = cp(q.bface_normal, 3 * (size_t)q.num_bfaces);
@@ -295,6 +305,87 @@ static void darcyInterior(const Prob& P, int I, int J, int c, const D* pI, const
     }
 }
 
+// ------------------------------------------------------ transmissibility --
+// TransExtensiveQuantities::transmissibility_ (transfluxmodule.hh:425-456):
+// T0 T1 / (T0 + T1), T_k = K_kk |n . d_k| / |d_k|^2, k the axis of n
+static double transInteriorT(const Prob& P, int I, int J, int c)
+{
+    const double* n = &P.connNormal[3 * c];
+    const double* xf = &P.connCenter[3 * c];
+    double d0[3], d1[3];
+    for (int d = 0; d < 3; ++d) {
+        d0[d] = xf[d] - P.center[3 * I + d];
+        d1[d] = xf[d] - P.center[3 * J + d];
+    }
+    double nd0 = 0, nd1 = 0, s0 = 0, s1 = 0;
+    for (int d = 0; d < 3; ++d) {
+        nd0 += n[d] * d0[d];
+        nd1 += n[d] * d1[d];
+        s0 += d0[d] * d0[d];
+        s1 += d1[d] * d1[d];
+    }
+    nd0 = std::abs(nd0);
+    nd1 = std::abs(nd1);
+    int idx = 0;
+    double val = 0.0;
+    for (int d = 0; d < P.dimWorld; ++d)
+        if (std::abs(n[d]) > val) { val = std::abs(n[d]); idx = d; }
+    const double T0 = P.perm[3 * I + idx] * nd0 / s0;
+    const double T1 = P.perm[3 * J + idx] * nd1 / s1;
+    return T0 * T1 / (T0 + T1);
+}
+
+// transmissibilityBoundary_ (transfluxmodule.hh:457-480): the reference takes
+// the geometry of the element's interior face with the boundary face's
+// index (stencil.interiorFace(scvfIdx)); on square cells with a diagonal,
+// axis-independent K that equals the boundary face's own half transmissibility
+static double transBoundaryT(const Prob& P, int I, int k)
+{
+    const int c = P.connPtr[I] + k;
+    if (c >= P.connPtr[I + 1]) return std::numeric_limits<double>::quiet_NaN();
+    const double* n = &P.connNormal[3 * c];
+    const double* xf = &P.connCenter[3 * c];
+    double nd = 0, s0 = 0;
+    for (int d = 0; d < 3; ++d) {
+        const double t = xf[d] - P.center[3 * I + d];
+        nd += n[d] * t;
+        s0 += t * t;
+    }
+    int idx = 0;
+    double val = 0.0;
+    for (int d = 0; d < P.dimWorld; ++d)
+        if (std::abs(n[d]) > val) { val = std::abs(n[d]); idx = d; }
+    return P.perm[3 * I + idx] * nd / s0;
+}
+
+// calculateGradients_ of the transmissibility module for one phase, focus =
+// interior element I (transfluxmodule.hh:201-318): hydrostatic correction
+// with the average density, upwind by the sign of the pressure difference
+// (ties: larger volume, then lower global index), q = dp * lambda_up * (-T)
+template <class D>
+static D transInterior(const Prob& P, int I, int J, double T, const D& pI, double pJ, const D& rhoI, double rhoJ,
+                       const D& lamI, double lamJ, bool& upInterior)
+{
+    if (lamI.v <= 0.0 && lamJ <= 0.0) {
+        upInterior = true;
+        return D(0.0);
+    }
+    const double g = P.g[P.dimWorld - 1];
+    const double distZ = P.center[3 * I + P.dimWorld - 1] - P.center[3 * J + P.dimWorld - 1];
+    D rhoAvg = (rhoI + rhoJ) / 2.0;
+    D pEx(pJ);
+    pEx += rhoAvg * (distZ * g);
+    D pd = pEx - pI;
+    if (pd.v > 0.0) upInterior = false;
+    else if (pd.v < 0.0) upInterior = true;
+    else {
+        const double Vin = P.volume[I], Vex = P.volume[J];
+        upInterior = Vin > Vex ? true : (Vin < Vex ? false : I < J);
+    }
+    if (upInterior) return pd * lamI * (-T);
+    return pd * (lamJ * (-T));
+}
+
 // ------------------------------------------------------ linearization -----
 struct Bcrs {
     int n = 0, b = 2;
@@ -406,7 +497,13 @@ static void linearizeImmiscible(Sim& S, const std::vector<IQ2>& iq)
             for (int a = 0; a < 2; ++a) { pJ[a] = qj.p[a].v; rhoJ[a] = qj.rho[a].v; lamJ[a] = qj.lam[a].v; }
             D2 vf[2];
             bool upI[2];
-            darcyInterior<D2, 2>(P, I, Jc, c, qi.p, pJ, qi.rho, rhoJ, qi.lam, lamJ, vf, upI);
+            if (P.fluxModule == GBFV_FLUX_TRANS) {
+                const double T = transInteriorT(P, I, Jc, c);
+                for (int a = 0; a < 2; ++a)
+                    vf[a] = transInterior<D2>(P, I, Jc, T, qi.p[a], pJ[a], qi.rho[a], rhoJ[a], qi.lam[a], lamJ[a], upI[a]);
+            }
+            else
+                darcyInterior<D2, 2>(P, I, Jc, c, qi.p, pJ, qi.rho, rhoJ, qi.lam, lamJ, vf, upI);
             D2 flux[2];
             for (int a = 0; a < 2; ++a) {
                 flux[a] = D2(0.0);
@@ -458,6 +555,23 @@ static void linearizeImmiscible(Sim& S, const std::vector<IQ2>& iq)
                 const double pcn = L.pcnw(SwE);
                 const double pb[2] = {pw, pw + pcn - 0.0};
                 const double krb[2] = {L.krw(SwE), L.krn(1.0 - SnE)};
+                if (P.fluxModule == GBFV_FLUX_TRANS) {
+                    // calculateBoundaryGradients_ (transfluxmodule.hh:324-415)
+                    const double T = transBoundaryT(P, I, f - P.bfPtr[I]);
+                    const double g = P.g[P.dimWorld - 1];
+                    const double distZ = P.center[3 * I + P.dimWorld - 1] - P.bfCenter[3 * f + P.dimWorld - 1];
+                    for (int a = 0; a < 2; ++a) {
+                        D2 rhoAvg = (qi.rho[a] + P.rho[a]) / 2.0;
+                        D2 pEx(pb[a]);
+                        pEx += rhoAvg * (distZ * g);
+                        D2 pd = pEx - qi.p[a];
+                        D2 vf = pd.v > 0.0 ? pd * (krb[a] / P.mu[a]) * (-T) : pd * qi.lam[a] * (-T);
+                        D2 dens = pb[a] > qi.p[a].v ? D2(P.rho[a]) : qi.rho[a];
+                        values[a] += vf * dens;
+                    }
+                }
+                else
+                {
                 const double* xI = &P.center[3 * I];
                 const double* xf = &P.bfCenter[3 * f];
                 const double* n = &P.bfNormal[3 * f];
@@ -486,6 +600,7 @@ static void linearizeImmiscible(Sim& S, const std::vector<IQ2>& iq)
                     }
                     D2 dens = pb[a] > qi.p[a].v ? D2(P.rho[a]) : qi.rho[a];
                     values[a] += vf * dens;
+                }
                 }
             }
             const double aa = P.bfArea[f] * 1.0;

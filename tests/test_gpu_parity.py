@@ -153,3 +153,23 @@ def test_mixed_precision_same_newton(built):
     # both runs stop at the same Newton tolerance; the states agree to the
     # size the 1e-6 linear tolerance leaves in each update
     assert rel_state_diff(b, a, 3) <= 2e-5
+
+
+def test_lens_trans_linearization_and_newton(built):
+    """Transmissibility flux module (lens_immiscible_ecfv_ad_trans): residual
+    and Jacobian at the initial and a later state, then 30 time steps with the
+    same Newton counts and final state as the oracle."""
+    prob = problems.lens(flux="trans")
+    prm = capi.default_params(linear_tolerance=1e-6)
+    ctx, orc = _pair(prob, linear_tolerance=1e-6)
+    er, ej = _compare_linearization(ctx, orc, 250.0, 0)
+    assert er <= RTOL_LIN and ej <= RTOL_LIN, (er, ej)
+    stg, _, sng, _, _ = ctx.time_integration(30, 250.0)
+    sto, _, sno, _, _ = orc.time_integration(30, 250.0)
+    assert stg == sto == 0
+    assert np.array_equal(sng, sno)
+    xg, _ = ctx.solution()
+    xo, _ = orc.solution()
+    assert rel_state_diff(xg, xo, 2) <= 1e-8
+    er, ej = _compare_linearization(ctx, orc, 250.0, 1, state=(xo, None))
+    assert er <= RTOL_LIN and ej <= RTOL_LIN, (er, ej)

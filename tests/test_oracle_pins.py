@@ -17,8 +17,8 @@ import oracle as O
 from gbfv import capi, problems
 
 
-def _lens_state(steps=5):
-    prob = problems.lens()
+def _lens_state(steps=5, flux="darcy"):
+    prob = problems.lens(flux=flux)
     prm = capi.default_params(linear_tolerance=1e-6)
     orc = O.Oracle(prob, prm)
     st, *_ = orc.time_integration(steps, 250.0)
@@ -26,8 +26,9 @@ def _lens_state(steps=5):
     return prob, prm, orc
 
 
-def test_ad_jacobian_matches_central_differences():
-    prob, prm, orc = _lens_state()
+@pytest.mark.parametrize("flux", ["darcy", "trans"])
+def test_ad_jacobian_matches_central_differences(flux):
+    prob, prm, orc = _lens_state(flux=flux)
     x0, m0 = orc.solution()
     dt = 300.0
     orc.linearize(dt, 0)              # fixes the storage cache at x0
@@ -58,12 +59,13 @@ def test_ad_jacobian_matches_central_differences():
     assert checked == 20
 
 
-@pytest.mark.parametrize("which", ["lens", "blackoil"])
+@pytest.mark.parametrize("which", ["lens", "lens-trans", "blackoil"])
 def test_interior_fluxes_cancel(which):
-    if which == "lens":
-        prob = problems.lens()
+    if which.startswith("lens"):
+        flux = "trans" if which == "lens-trans" else "darcy"
+        prob = problems.lens(flux=flux)
         prob.bface_type[:] = capi.BC_NOFLOW
-        _, _, o = _lens_state(3)
+        _, _, o = _lens_state(3, flux)
         state = o.solution()
     else:
         prob = problems.blackoil(8, 7, 3)
@@ -256,3 +258,57 @@ def test_two_cell_residual_matches_symbolic_derivation():
                 d00 += float((phi * rho[a] * (1 if a == 0 else -1)) / dt)
             assert np.isclose(blk[(0, 0)][a, v], d00, rtol=1e-11, atol=0), (a, v)
             assert np.isclose(blk[(1, 0)][a, v], d10, rtol=1e-11, atol=0), (a, v)
+
+
+def test_two_cell_trans_residual_matches_symbolic_derivation():
+    """transfluxmodule.hh:201-318, 425-456 on a 1x2 vertical lens column."""
+    sp = pytest.importorskip("sympy")
+    prob = problems.lens(nx=1, ny=2, flux="trans")
+    prob.bface_type[:] = capi.BC_NOFLOW
+    prm = capi.default_params()
+    orc = O.Oracle(prob, prm)
+    x = np.array([1.3e5, 0.62, 1.1e5, 0.71])
+    orc.set_solution(x)
+    dt = 500.0
+    orc.linearize(dt, 0)
+    orc.linearize(dt, 1)
+    r0 = orc.residual()
+    R = sp.Rational
+    pw0, S0 = sp.symbols("pw0 S0")
+    mats = {0: (R(5, 100), R(37, 10000), R(47, 10)), 1: (R(18, 100), R(45, 100000), R(73, 10))}
+
+    def vg(S, m_id):
+        swr, alpha, n = mats[m_id]
+        m = 1 - 1 / n
+        Se = (S - swr) / (1 - swr)
+        pc = ((Se ** (-1 / m) - 1) ** (1 / n)) / alpha
+        krw = sp.sqrt(Se) * (1 - (1 - Se ** (1 / m)) ** m) ** 2
+        krn = (1 - Se) ** R(1, 3) * (1 - Se ** (1 / m)) ** (2 * m)
+        return pc, krw, krn
+
+    rho = (R(1000), R(1460))
+    mu = (R(1, 1000), R(57, 100000))
+    g = R(-981, 100)
+    K0, K1 = R(46, 10 ** 11), R(905, 10 ** 14)     # background below, lens above
+    half = 1                                          # half cell height (cells 2 m high)
+    T0, T1 = K0 * half / half ** 2, K1 * half / half ** 2
+    T = T0 * T1 / (T0 + T1)
+    area, V = R(6), R(12)
+    pw1, S1 = R(11, 1) * 10 ** 4, R(71, 100)
+    pc0, krw0, krn0 = vg(S0, 0)
+    pc1, krw1, krn1 = vg(S1, 1)
+    p_I = (pw0, pw0 + pc0)
+    p_J = (pw1, pw1 + pc1)
+    lam_I = (krw0 / mu[0], krn0 / mu[1])
+    lam_J = (krw1 / mu[0], krn1 / mu[1])
+    subs = {pw0: R(13, 1) * 10 ** 4, S0: R(62, 100)}
+    distZ = 1 - 3
+    ref = []
+    for a in range(2):
+        rhoAvg = (rho[a] + rho[a]) / 2
+        pd = p_J[a] + rhoAvg * (distZ * g) - p_I[a]
+        up_interior = not (float(pd.subs(subs)) > 0)
+        mob = lam_I[a] if up_interior else lam_J[a]
+        flux = pd * mob * (-T) * rho[a] * area
+        ref.append(float((flux / V).subs(subs)))
+    assert np.allclose(r0[:2], ref, rtol=1e-12, atol=0)
