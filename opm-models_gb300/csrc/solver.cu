@@ -850,19 +850,30 @@ __device__ __forceinline__ void sweepUpperPush(const KArgs<T>& a, T* y, const Te
 template <class T, int B>
 __device__ __forceinline__ void spmvRow(const KArgs<T>& a, const T* in, int i, T (&acc)[B])
 {
-    const int ld = a.ldN;
+    // all column indices first, then every gather and matrix load without a
+    // branch in between (more loads in flight); a missing neighbour (column
+    // -1) contributes zero through the selects, its block is never trusted
+    const int ld = a.ldN, ns = a.nslot;
+    int k[MAX_SLOTS];
+#pragma unroll
+    for (int s = 0; s < MAX_SLOTS; ++s) k[s] = s < ns ? __ldg(&a.col[s * ld + i]) : -1;
 #pragma unroll
     for (int e = 0; e < B; ++e) acc[e] = T(0);
-    for (int s = 0; s < a.nslot; ++s) {
-        const int k = a.col[s * ld + i];
-        if (k < 0) continue;
+#pragma unroll
+    for (int s = 0; s < MAX_SLOTS; ++s) {
+        if (s >= ns) break;
+        const bool has = k[s] >= 0;
+        const int kk = has ? k[s] : 0;
         T xk[B];
 #pragma unroll
-        for (int e = 0; e < B; ++e) xk[e] = ldcg(&in[k * B + e]);
+        for (int e = 0; e < B; ++e) xk[e] = has ? ldcg(&in[kk * B + e]) : T(0);
 #pragma unroll
         for (int r = 0; r < B; ++r)
 #pragma unroll
-            for (int c = 0; c < B; ++c) acc[r] += a.A[(s * B * B + r * B + c) * ld + i] * xk[c];
+            for (int c = 0; c < B; ++c) {
+                const T av = a.A[(s * B * B + r * B + c) * ld + i];
+                acc[r] += (has ? av : T(0)) * xk[c];
+            }
     }
 }
 
