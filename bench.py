@@ -142,14 +142,14 @@ def params(precision):
                                inner_tolerance=1e-6)
 
 
-def cpu_sample(prob, iters=2):
+def cpu_sample(prob, iters=2, threads=None):
     """The oracle (the reference algorithm restated on the CPU) on the first
     `iters` Newton iterations of the first time step: OpenMP over elements in
     the linearization, sequential BiCGStab/ILU0 (as the reference)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     O.build()
-    threads = os.cpu_count() or 1
+    threads = threads or os.cpu_count() or 1
     O.set_threads(threads)
     orc = O.Oracle(prob, params(0))
     t0 = time.perf_counter()
@@ -365,8 +365,11 @@ def run_ours(args):
     }
     if world == 1 and not args.no_cpu_baseline:
         v, dt, threads = cpu_sample(prob)
+        v1, dt1, _ = cpu_sample(prob, iters=1, threads=1)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": "first 2 Newton iterations of time step 1 (%.1f s)" % dt}
+                                "sample": "first 2 Newton iterations of time step 1 (%.1f s)" % dt,
+                                "one_thread": {"value": v1, "cores": 1,
+                                               "sample": "first Newton iteration of time step 1 (%.1f s)" % dt1}}
     print(json.dumps(line))
     if world > 1:
         dist.barrier()

@@ -174,3 +174,33 @@ def test_lens_trans_linearization_and_newton(built):
     # a later state (the oracle's), storage cache rebuilt from it (iteration 0)
     er, ej = _compare_linearization(ctx, orc, 250.0, 0, state=(xo, None))
     assert er <= RTOL_LIN and ej <= RTOL_LIN, (er, ej)
+
+
+@pytest.mark.parametrize("flux", ["darcy", "trans"])
+def test_lens_3d_linearization_and_steps(built, flux):
+    """3D lens (16x10x6), both flux modules: linearization at the initial
+    state, then 6 time steps with the oracle's Newton counts and state."""
+    prob = problems.lens(nx=16, ny=10, dim=3, nz=6, flux=flux)
+    ctx, orc = _pair(prob, linear_tolerance=1e-8)
+    er, ej = _compare_linearization(ctx, orc, 250.0, 0)
+    assert er <= RTOL_LIN and ej <= RTOL_LIN, (er, ej)
+    stg, _, sng, _, _ = ctx.time_integration(6, 250.0)
+    sto, _, sno, _, _ = orc.time_integration(6, 250.0)
+    assert stg == sto == 0 and np.array_equal(sng, sno)
+    assert rel_state_diff(ctx.solution()[0], orc.solution()[0], 2) <= 1e-8
+
+
+def test_blackoil_primary_variable_switching_happens(built):
+    """The black-oil runs exercise switching: gas appears near the producer
+    (Rs -> Sg) and the GPU switches the same cells as the oracle."""
+    prob = problems.blackoil(12, 10, 4)
+    prm = capi.default_params(linear_tolerance=1e-8, newton_tolerance=1e-7)
+    ctx, orc = _pair(prob, linear_tolerance=1e-8, newton_tolerance=1e-7)
+    m0 = ctx.solution()[1].copy()
+    assert ctx.time_integration(4, 86400.0, fixed_dt=True)[0] == 0
+    assert orc.time_integration(4, 86400.0, fixed_dt=True)[0] == 0
+    xg, mg = ctx.solution()
+    xo, mo = orc.solution()
+    assert np.array_equal(mg, mo)
+    assert int((mg != m0).sum()) > 0, "no primary-variable switch happened"
+    assert rel_state_diff(xg, xo, 3) <= 1e-8
