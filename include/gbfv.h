@@ -341,7 +341,9 @@ int gbfv_get_kernel_stats(const gbfv_ctx* ctx, gbfv_kernel_stats* out);
 int gbfv_solver_config(const gbfv_ctx* ctx, int precision, int* mode, int* blocks,
                        double* tune_ms, int* num_tuned);
 /* fix the launch configuration of the persistent solve kernel of a
- * precision (mode 1 = cluster of `blocks` blocks, 0 = cooperative grid) and
+ * precision (mode 1 = cluster of `blocks` blocks, 0 = cooperative grid,
+ * 2 = hybrid: `blocks` in clusters of 16 over the GPU, the first cluster
+ * factorizes and sweeps, all blocks share SpMV, updates and reductions) and
  * skip the autotuner; GBFV_ERR_UNSUPPORTED beyond what the device allows  */
 int gbfv_set_solver_config(gbfv_ctx* ctx, int precision, int mode, int blocks);
 int gbfv_reset_kernel_stats(gbfv_ctx* ctx);

@@ -96,6 +96,7 @@ struct SolverData {
     int tuned[2] = {0, 0};
     int maxGrid[2] = {1, 1};
     int maxCluster[2] = {1, 1};
+    int maxHybrid[2] = {0, 0};  // blocks of a hybrid launch (whole resident clusters of HYBRID_CLUSTER)
     double tuneMs[2][16] = {};
     int adjacentLevels = 0;  // every dependency is exactly one level away
     std::vector<int> colHost;   // [s*ldN + p] host copy of the ELL columns
@@ -131,6 +132,8 @@ int allocSolver(SolverData& S, int maxBlocksOverride = 0)
     S.maxGrid[1] = maxSolverBlocks<float>(S.b);
     S.maxCluster[0] = std::min(16, maxClusterBlocks<double>(S.b));
     S.maxCluster[1] = std::min(16, maxClusterBlocks<float>(S.b));
+    S.maxHybrid[0] = S.maxCluster[0] >= HYBRID_CLUSTER ? maxHybridBlocks<double>(S.b) : 0;
+    S.maxHybrid[1] = S.maxCluster[1] >= HYBRID_CLUSTER ? maxHybridBlocks<float>(S.b) : 0;
     // default before tuning: one block for small systems, else a cluster of 8
     for (int k = 0; k < 2; ++k) {
         S.mode[k] = SYNC_CLUSTER;
@@ -141,6 +144,10 @@ int allocSolver(SolverData& S, int maxBlocksOverride = 0)
         int n = 0;
         if (sscanf(f, "cluster:%d", &n) == 1 && n > 0)
             for (int k = 0; k < 2; ++k) { S.mode[k] = SYNC_CLUSTER; S.nblk[k] = std::min(n, S.maxCluster[k]); S.tuned[k] = 1; }
+        else if (strncmp(f, "hybrid", 6) == 0)
+            for (int k = 0; k < 2; ++k) {
+                if (S.maxHybrid[k] > HYBRID_CLUSTER) { S.mode[k] = SYNC_HYBRID; S.nblk[k] = S.maxHybrid[k]; S.tuned[k] = 1; }
+            }
         else if (sscanf(f, "grid:%d", &n) == 1 && n > 0)
             for (int k = 0; k < 2; ++k) { S.mode[k] = SYNC_GRID; S.nblk[k] = std::min(n, S.maxGrid[k]); S.tuned[k] = 1; }
     }
@@ -500,11 +507,15 @@ int fillKArgs(SolverData& S, DevStatus* st, const T* A, T* FL, T* FD, const T* r
         if (const char* e = getenv("GBFV_OWNER")) omode = strcmp(e, "contig") == 0 ? 1 : 0;
         a.ownerMode = omode;
         int maxChunk = 0;  // the most rows one block takes in a level
+        // the cluster that sweeps: the whole launch, or the first cluster of a hybrid one
+        const int C = mode == SYNC_HYBRID ? HYBRID_CLUSTER : nblocks;
+        a.hybrid = mode == SYNC_HYBRID ? HYBRID_CLUSTER : 0;
         for (size_t l = 0; l + 1 < S.levPtr.size(); ++l)
-            maxChunk = std::max(maxChunk, levelChunk(S.levPtr[l + 1] - S.levPtr[l], nblocks, omode));
+            maxChunk = std::max(maxChunk, levelChunk(S.levPtr[l + 1] - S.levPtr[l], C, omode));
         constexpr int NTC = clusterThreads<T>();
-        a.dsmem = (mode == SYNC_CLUSTER && S.adjacentLevels && maxChunk <= NTC &&
+        a.dsmem = ((mode == SYNC_CLUSTER || mode == SYNC_HYBRID) && S.adjacentLevels && maxChunk <= NTC &&
                    (int)S.levPtr.size() - 1 <= MAX_PUSH_LEVELS && !getenv("GBFV_NO_DSMEM")) ? 1 : 0;
+        if (mode == SYNC_HYBRID && !a.dsmem) return GBFV_ERR_UNSUPPORTED;  // the hybrid sweeps need the push tables
         // as many level groups as fit (each group must cover a block's share of the widest level)
         a.grp = 1;
         for (int g : {8, 4, 2})
@@ -512,7 +523,7 @@ int fillKArgs(SolverData& S, DevStatus* st, const T* A, T* FL, T* FD, const T* r
         if (const char* e = getenv("GBFV_GROUPS")) a.grp = std::max(1, std::min(a.grp, atoi(e)));
         a.pushL = a.pushU = a.levVals = nullptr;
         if (a.dsmem) {
-            const int ps = buildPushTargets(S, nblocks, a.grp, NTC, omode);
+            const int ps = buildPushTargets(S, C, a.grp, NTC, omode);
             if (ps) return ps;
             a.pushL = S.pushL;
             a.pushU = S.pushU;
@@ -576,6 +587,7 @@ void tuneSolver(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hs
     if (S.N > 4 * 4096) {
         cands.push_back({SYNC_GRID, std::min(nsm, S.maxGrid[k])});
         cands.push_back({SYNC_GRID, std::min(2 * nsm, S.maxGrid[k])});
+        if (S.maxHybrid[k] > HYBRID_CLUSTER && !getenv("GBFV_NO_HYBRID")) cands.push_back({SYNC_HYBRID, S.maxHybrid[k]});
     }
     double best = 1e300;
     Cand pick = {S.mode[k], S.nblk[k]};
@@ -1516,10 +1528,12 @@ int gbfv_get_kernel_stats(const gbfv_ctx* Cc, gbfv_kernel_stats* out)
 
 int gbfv_set_solver_config(gbfv_ctx* C, int precision, int mode, int blocks)
 {
-    if (!C || (mode != SYNC_CLUSTER && mode != SYNC_GRID) || blocks < 1) return GBFV_ERR_ARG;
+    if (!C || (mode != SYNC_CLUSTER && mode != SYNC_GRID && mode != SYNC_HYBRID) || blocks < 1) return GBFV_ERR_ARG;
     const int k = precision == GBFV_PREC_MIXED ? 1 : 0;
     SolverData& S = C->S;
     if (mode == SYNC_CLUSTER && blocks > S.maxCluster[k]) return GBFV_ERR_UNSUPPORTED;
+    if (mode == SYNC_HYBRID && (blocks > S.maxHybrid[k] || blocks % HYBRID_CLUSTER || blocks <= HYBRID_CLUSTER))
+        return GBFV_ERR_UNSUPPORTED;
     if (mode == SYNC_GRID && blocks > S.maxGrid[k]) return GBFV_ERR_UNSUPPORTED;
     S.mode[k] = mode;
     S.nblk[k] = blocks;

@@ -889,7 +889,12 @@ __device__ __forceinline__ void bicgstabBody(const KArgs<T>& a, const Team<MODE>
     ps.ok = 1;
     const PushSmem<T, B, NT> psm(dynSmem, a.numLev);
     T* const dep = psm.dep;
-    if constexpr (MODE == SYNC_CLUSTER) {
+    // hybrid launch (grid of clusters): cluster 0 factorizes and sweeps, every
+    // block of the grid shares SpMV, vector updates and reductions
+    const bool sweeper = MODE == SYNC_CLUSTER || (a.hybrid && blockIdx.x < a.hybrid);
+    if (MODE == SYNC_CLUSTER || a.hybrid) {
+        const cg::cluster_group cl = cg::this_cluster();
+        const int crank = (int)cl.block_rank(), csize = (int)cl.num_blocks();
         for (int k = 0; k < PUSH_BUFFERS; ++k) {
             ps.mb[k] = smemAddr(&mbar[k]);
             ps.ph[k] = 0;
@@ -897,22 +902,30 @@ __device__ __forceinline__ void bicgstabBody(const KArgs<T>& a, const Team<MODE>
         ps.dep = smemAddr(dep);
         ps.lev = smemAddr(&mbar[PUSH_BUFFERS]);
         ps.levPh = 0;
-        if (a.dsmem) {
+        if (a.dsmem && sweeper) {
             for (int j = threadIdx.x; j <= a.numLev; j += NT) psm.lev[j] = a.levPtr[j];
-            for (int j = threadIdx.x; j < 2 * a.numLev; j += NT) psm.nval[j] = a.levVals[tm.rank * 2 * a.numLev + j];
+            for (int j = threadIdx.x; j < 2 * a.numLev; j += NT) psm.nval[j] = a.levVals[crank * 2 * a.numLev + j];
         }
-        if (a.dsmem && threadIdx.x == 0) {
+        if (a.dsmem && sweeper && threadIdx.x == 0) {
             // one arrival per phase (thread 0, carrying the expected bytes)
             for (int k = 0; k < PUSH_BUFFERS; ++k) mbarInit(ps.mb[k], 1);
-            mbarInit(ps.lev, tm.nblk);
+            mbarInit(ps.lev, csize);
             asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         }
-        cg::this_cluster().sync();
+        cl.sync();
     }
     const double eps = 2.2250738585072014e-308 * 1e10;  // numeric_limits<double>::min()*1e10
     PhaseClock pc(a.prof, gt);
     if (a.factor) {
-        if (!phaseFactor<T, B, MODE>(a, tm)) goto timeout;
+        if (MODE == SYNC_GRID && a.hybrid) {
+            if (sweeper) {
+                const Team<SYNC_CLUSTER> tc;
+                phaseFactor<T, B, SYNC_CLUSTER>(a, tc);
+            }
+            if (!teamSync<MODE>(a.gs)) goto timeout;
+        }
+        else if (!phaseFactor<T, B, MODE>(a, tm))
+            goto timeout;
         pc.tick(0);
         if (*(volatile int*)&a.st->code == GBFV_ERR_SINGULAR) goto done;
     }
@@ -983,6 +996,14 @@ __device__ __forceinline__ void bicgstabBody(const KArgs<T>& a, const Team<MODE>
                     sweepLower<T, B, MODE>(a, nullptr, a.y, true, (T)beta, (T)omega, tm);
                     sweepUpper<T, B, MODE>(a, a.y, tm);
                 }
+            }
+            else if (a.hybrid) {
+                if (sweeper) {
+                    const Team<SYNC_CLUSTER> tc;
+                    sweepLowerPush<T, B, NT>(a, nullptr, a.y, true, (T)beta, (T)omega, tc, dep, ps, psm);
+                    sweepUpperPush<T, B, NT>(a, a.y, tc, dep, ps, psm);
+                }
+                if (!teamSync<MODE>(a.gs)) goto timeout;
             }
             else {
                 if (!sweepLower<T, B, MODE>(a, nullptr, a.y, true, (T)beta, (T)omega, tm)) goto timeout;
@@ -1062,6 +1083,14 @@ __device__ __forceinline__ void bicgstabBody(const KArgs<T>& a, const Team<MODE>
                     sweepLower<T, B, MODE>(a, a.r, a.z, false, T(0), T(0), tm);
                     sweepUpper<T, B, MODE>(a, a.z, tm);
                 }
+            }
+            else if (a.hybrid) {
+                if (sweeper) {
+                    const Team<SYNC_CLUSTER> tc;
+                    sweepLowerPush<T, B, NT>(a, a.r, a.z, false, T(0), T(0), tc, dep, ps, psm);
+                    sweepUpperPush<T, B, NT>(a, a.z, tc, dep, ps, psm);
+                }
+                if (!teamSync<MODE>(a.gs)) goto timeout;
             }
             else {
                 if (!sweepLower<T, B, MODE>(a, a.r, a.z, false, T(0), T(0), tm)) goto timeout;
@@ -1236,10 +1265,72 @@ static int launchOne(const KArgs<T>& a, int nblocks, cudaStream_t s)
     return e == cudaSuccess ? GBFV_OK : GBFV_ERR_CUDA;
 }
 
+// hybrid: the grid kernel over nblocks blocks in clusters of HYBRID_CLUSTER,
+// cooperative (every block resident, for the software grid barrier)
+template <class T, int B>
+static int launchHybrid(const KArgs<T>& a, int nblocks, cudaStream_t s)
+{
+    constexpr int NT = clusterThreads<T>();
+    auto fn = kBicgstab<T, B, SYNC_GRID, NT>;
+    static bool attrSet = false;
+    if (!attrSet) {
+        cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)PushSmem<T, B, NT>::bytes(MAX_PUSH_LEVELS));
+        attrSet = true;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(nblocks, 1, 1);
+    cfg.blockDim = dim3(NT, 1, 1);
+    cfg.dynamicSmemBytes = a.dsmem ? PushSmem<T, B, NT>::bytes(a.numLev) : 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[2];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = HYBRID_CLUSTER;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    at[1].id = cudaLaunchAttributeCooperative;
+    at[1].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 2;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, fn, a);
+    countLaunch();
+    return e == cudaSuccess ? GBFV_OK : GBFV_ERR_CUDA;
+}
+
+// how many blocks a hybrid launch may have (whole clusters that are resident at once)
+template <class T>
+int maxHybridBlocks(int b)
+{
+    constexpr int NT = clusterThreads<T>();
+    const void* fn = b == 2 ? (const void*)kBicgstab<T, 2, SYNC_GRID, NT> : (const void*)kBicgstab<T, 3, SYNC_GRID, NT>;
+    const size_t dyn = b == 2 ? PushSmem<T, 2, NT>::bytes(MAX_PUSH_LEVELS) : PushSmem<T, 3, NT>::bytes(MAX_PUSH_LEVELS);
+    cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    cudaLaunchConfig_t cfg = {};
+    cfg.blockDim = dim3(NT, 1, 1);
+    cfg.gridDim = dim3(HYBRID_CLUSTER, 1, 1);
+    cfg.dynamicSmemBytes = dyn;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = HYBRID_CLUSTER;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, fn, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        n = 0;
+    }
+    return n * HYBRID_CLUSTER;
+}
+
 template <class T>
 int launchBicgstab(const KArgs<T>& a, int b, int mode, int nblocks, cudaStream_t s)
 {
     constexpr int NTC = clusterThreads<T>();
+    if (mode == SYNC_HYBRID) return b == 2 ? launchHybrid<T, 2>(a, nblocks, s) : launchHybrid<T, 3>(a, nblocks, s);
     if (mode == SYNC_GRID)
         return b == 2 ? launchOne<T, 2, SYNC_GRID, SOLVER_THREADS>(a, nblocks, s)
                       : launchOne<T, 3, SYNC_GRID, SOLVER_THREADS>(a, nblocks, s);
@@ -1362,6 +1453,8 @@ template int maxSolverBlocks<double>(int);
 template int maxSolverBlocks<float>(int);
 template int maxClusterBlocks<double>(int);
 template int maxClusterBlocks<float>(int);
+template int maxHybridBlocks<double>(int);
+template int maxHybridBlocks<float>(int);
 template int launchBicgstabBatch<double>(const KArgs<double>*, const int*, const int*, int*, int, int, int, int,
                                          cudaStream_t);
 template int launchBicgstabBatch<float>(const KArgs<float>*, const int*, const int*, int*, int, int, int, int,

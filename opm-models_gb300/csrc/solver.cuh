@@ -16,6 +16,8 @@ constexpr int PUSH_BARRIER_FLAG = 1 << 30;  // in levVals: a cluster barrier fol
 __host__ __device__ constexpr int padB(int B) { return B == 3 ? 4 : B; }
 constexpr int SYNC_GRID = 0;     // whole grid, cooperative launch, software barrier
 constexpr int SYNC_CLUSTER = 1;  // one thread-block cluster, hardware barrier
+constexpr int SYNC_HYBRID = 2;   // launch mode: clusters over the whole GPU, cluster 0 sweeps, all share the rest
+constexpr int HYBRID_CLUSTER = 16;  // cluster size of the hybrid launch
 
 // software grid barrier state (device memory, zero-initialised)
 struct GridSync {
@@ -43,6 +45,7 @@ struct KArgs {
     int factor;         // factorize before iterating
     unsigned long long* prof;  // optional per-phase nanoseconds (block 0, thread 0): factor,
                                // L sweep, U sweep, SpMV+dot, update+max, count of iterations
+    int hybrid;         // hybrid launch: the sweeping cluster's blocks (0 = not hybrid)
     int grp;            // push sweeps: number of level-rotating thread groups
     int ownerMode;      // push sweeps: rows of a level dealt to blocks by warp round-robin (0) or contiguously (1)
     const int* pushL;   // push sweeps: consumer block/slot of each upper neighbour [q*ldN + p]
@@ -75,6 +78,7 @@ void launchBatchAccumulate(const SolveJob* jobs, const int* active, int K, int g
 void launchBatchResidual64(const SolveJob* jobs, const int* active, int K, int gx, int b, cudaStream_t s);
 template <class T> int maxSolverBlocks(int b);
 template <class T> int maxClusterBlocks(int b);
+template <class T> int maxHybridBlocks(int b);
 // batched solve: clusters of clusterSize blocks take systems args[order[q]],
 // q = 0..*count-1 (device memory), from the queue counter (zero before the launch)
 template <class T>

@@ -144,7 +144,7 @@ class Context:
         mode, nb, nt = C.c_int(), C.c_int(), C.c_int()
         ms = np.zeros(16)
         self.lib.gbfv_solver_config(self.h, precision, C.byref(mode), C.byref(nb), _d(ms), C.byref(nt))
-        return {"mode": "cluster" if mode.value == 1 else "grid", "blocks": nb.value,
+        return {"mode": {0: "grid", 1: "cluster", 2: "hybrid"}.get(mode.value, "?"), "blocks": nb.value,
                 "tune_ms": ms[:nt.value].tolist()}
 
     def set_solver_config(self, precision, mode, blocks):
