@@ -355,7 +355,8 @@ def run_ours(args):
         "e2e": {"value": e2e_cits / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(N * 3 * 8 + N * 4),
                 "d2h_bytes_per_step": int(N * 3 * 8 + N * 4)},
         "gpu_launches": int(mixed["launches"] / args.steps),
-        "roofline": {"bound": "hbm", "kernel": "kBicgstab<float,3> (persistent ILU0 + BiCGStab)",
+        "roofline": {"bound": "hbm", "kernel": "kBicgstab<float,3> (persistent ILU0 + BiCGStab, %s launch of %d blocks)"
+                     % (mixed["cfg"]["mode"], mixed["cfg"]["blocks"]),
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_kind": peak_kind,
                      "avg_launch_ms": avg_launch_ms, "bytes_per_launch": kst["solve_bytes"] / max(1, kst["solve_launches"])},
