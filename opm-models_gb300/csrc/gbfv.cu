@@ -132,8 +132,14 @@ int allocSolver(SolverData& S, int maxBlocksOverride = 0)
     S.maxGrid[1] = maxSolverBlocks<float>(S.b);
     S.maxCluster[0] = std::min(16, maxClusterBlocks<double>(S.b));
     S.maxCluster[1] = std::min(16, maxClusterBlocks<float>(S.b));
-    S.maxHybrid[0] = S.maxCluster[0] >= HYBRID_CLUSTER ? maxHybridBlocks<double>(S.b) : 0;
-    S.maxHybrid[1] = S.maxCluster[1] >= HYBRID_CLUSTER ? maxHybridBlocks<float>(S.b) : 0;
+    // The hybrid launch (a cooperative grid of clusters) is left out under a
+    // profiler that injects itself into the process (CUDA_INJECTION64_PATH): a
+    // kernel-replay capture of it ended in a device fault, while the same runs
+    // without the profiler pass.  GBFV_NO_HYBRID leaves it out as well.
+    const char* inj = getenv("CUDA_INJECTION64_PATH");
+    const bool hybridOk = !getenv("GBFV_NO_HYBRID") && !(inj && *inj);
+    S.maxHybrid[0] = hybridOk && S.maxCluster[0] >= HYBRID_CLUSTER ? maxHybridBlocks<double>(S.b) : 0;
+    S.maxHybrid[1] = hybridOk && S.maxCluster[1] >= HYBRID_CLUSTER ? maxHybridBlocks<float>(S.b) : 0;
     // default before tuning: one block for small systems, else a cluster of 8
     for (int k = 0; k < 2; ++k) {
         S.mode[k] = SYNC_CLUSTER;
@@ -495,6 +501,7 @@ int fillKArgs(SolverData& S, DevStatus* st, const T* A, T* FL, T* FD, const T* r
     a.gs.count = S.bar;
     a.gs.gen = S.bar + 1;
     a.gs.abort = (int*)(S.bar + 2);
+    a.gs.perCluster = mode == SYNC_HYBRID ? HYBRID_CLUSTER : 0;
     a.st = st;
     a.redTol = redTol;
     a.absTol = absTol;
@@ -522,6 +529,7 @@ int fillKArgs(SolverData& S, DevStatus* st, const T* A, T* FL, T* FD, const T* r
             if (maxChunk <= NTC / g) { a.grp = g; break; }
         if (const char* e = getenv("GBFV_GROUPS")) a.grp = std::max(1, std::min(a.grp, atoi(e)));
         a.pushL = a.pushU = a.levVals = nullptr;
+        a.cluster = a.dsmem ? C : 0;
         if (a.dsmem) {
             const int ps = buildPushTargets(S, C, a.grp, NTC, omode);
             if (ps) return ps;
@@ -587,7 +595,7 @@ void tuneSolver(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hs
     if (S.N > 4 * 4096) {
         cands.push_back({SYNC_GRID, std::min(nsm, S.maxGrid[k])});
         cands.push_back({SYNC_GRID, std::min(2 * nsm, S.maxGrid[k])});
-        if (S.maxHybrid[k] > HYBRID_CLUSTER && !getenv("GBFV_NO_HYBRID")) cands.push_back({SYNC_HYBRID, S.maxHybrid[k]});
+        if (S.maxHybrid[k] > HYBRID_CLUSTER) cands.push_back({SYNC_HYBRID, S.maxHybrid[k]});
     }
     double best = 1e300;
     Cand pick = {S.mode[k], S.nblk[k]};

@@ -83,37 +83,57 @@ struct Team {
     }
 };
 
+// one arrival at the software grid barrier out of `expected`, bounded; false
+// when this arrival or another one gave up (the abort word is then set)
+__device__ __forceinline__ int gridArrive(const GridSync& g, unsigned expected)
+{
+    int ok = 1;
+    volatile unsigned* vgen = g.gen;
+    const unsigned my = *vgen;
+    __threadfence();
+    const unsigned arrived = atomicAdd(g.count, 1u);
+    if (arrived == expected - 1) {
+        atomicExch(g.count, 0u);
+        __threadfence();
+        atomicAdd(g.gen, 1u);
+    }
+    else {
+        const long long t0 = clock64();
+        while (*vgen == my) {
+            if (*(volatile int*)g.abort) { ok = 0; break; }
+            if (clock64() - t0 > GB_TIMEOUT_CYCLES) {
+                atomicExch(g.abort, 1);
+                ok = 0;
+                break;
+            }
+            __nanosleep(64);
+        }
+    }
+    __threadfence();
+    return ok;
+}
+
+// Barrier over the whole cooperative grid.  A wait that gives up makes the
+// blocks leave at different barriers; that is harmless when blocks share only
+// global memory, but not inside a cluster whose blocks write into each
+// other's shared memory (a block must not exit while a peer may still push
+// into it).  So in a hybrid launch (g.perCluster > 0) each cluster arrives
+// once, through its rank-0 block, and all blocks of the cluster take that
+// block's decision: a cluster's blocks always leave together.
 __device__ __forceinline__ bool gridBarrier(const GridSync& g)
 {
     __shared__ int sOk;
     __syncthreads();
     if (gridDim.x == 1) return true;
-    if (threadIdx.x == 0) {
-        int ok = 1;
-        volatile unsigned* vgen = g.gen;
-        const unsigned my = *vgen;
-        __threadfence();
-        const unsigned arrived = atomicAdd(g.count, 1u);
-        if (arrived == gridDim.x - 1) {
-            atomicExch(g.count, 0u);
-            __threadfence();
-            atomicAdd(g.gen, 1u);
-        }
-        else {
-            const long long t0 = clock64();
-            while (*vgen == my) {
-                if (*(volatile int*)g.abort) { ok = 0; break; }
-                if (clock64() - t0 > GB_TIMEOUT_CYCLES) {
-                    atomicExch(g.abort, 1);
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(64);
-            }
-        }
-        __threadfence();
-        sOk = ok;
+    if (g.perCluster > 0) {
+        cg::cluster_group cl = cg::this_cluster();
+        if (threadIdx.x == 0) __threadfence();  // this block's writes are visible GPU-wide
+        cl.sync();
+        if (cl.block_rank() == 0 && threadIdx.x == 0) sOk = gridArrive(g, gridDim.x / cl.num_blocks());
+        cl.sync();
+        return *cl.map_shared_rank(&sOk, 0) != 0;
     }
+    if (threadIdx.x == 0) sOk = gridArrive(g, gridDim.x);
     __syncthreads();
     return sOk != 0;
 }
@@ -541,11 +561,15 @@ struct SweepMap {
 // (precomputed on the host for the launch configuration).
 template <class T, int B>
 __device__ __forceinline__ void pushValues(int target, int half, const T (&out)[B], const Team<SYNC_CLUSTER>& tm,
-                                           const T* dep, const PushState& ps, int mbIdx)
+                                           const T* dep, PushState& ps, int mbIdx)
 {
     // also a consumer in this block gets its values by st.async (to this block's
     // own shared memory): the transaction count orders them, no fence needed
     const int owner = target >> 24;
+    if (owner >= tm.nblk) {  // a table for another cluster size: no push outside the cluster
+        ps.ok = 0;
+        return;
+    }
     const int off = (target & 0xffffff) + half;
     const unsigned dst = mapaRank(ps.dep + (unsigned)(off * sizeof(T)), owner);
     const unsigned mb = mapaRank(ps.mb[mbIdx], owner);
@@ -684,7 +708,8 @@ __device__ __forceinline__ void sweepLowerPush(const KArgs<T>& a, const T* d, T*
                 }
             }
             if (probe) t0 = clock64();
-            if (ps.ok && !mbarWait(ps.mb[k], ps.ph[k])) ps.ok = 0;  // after a timeout: no more waits
+            // after a timeout: no more waits and no more pushes
+            if (ps.ok && !mbarWait(ps.mb[k], ps.ph[k])) ps.ok = 0;
             if (probe) t1 = t2 = clock64();
             if (i >= 0) {
                 const T* md = dep + (k * NT + tid) * 3 * PB;
@@ -704,7 +729,7 @@ __device__ __forceinline__ void sweepLowerPush(const KArgs<T>& a, const T* d, T*
 #pragma unroll
                 for (int q = 0; q < 3; ++q) {
                     if (q >= dim) break;
-                    if (tg[q] >= 0) pushValues<T, B>(tg[q], kn * half, out, tm, dep, ps, kn);
+                    if (tg[q] >= 0 && ps.ok) pushValues<T, B>(tg[q], kn * half, out, tm, dep, ps, kn);
                 }
 #pragma unroll
                 for (int e = 0; e < B; ++e) y[i * B + e] = out[e];
@@ -828,7 +853,7 @@ __device__ __forceinline__ void sweepUpperPush(const KArgs<T>& a, T* y, const Te
 #pragma unroll
                 for (int q = 0; q < 3; ++q) {
                     if (q >= dim) break;
-                    if (tg[q] >= 0) pushValues<T, B>(tg[q], kn * half, out, tm, dep, ps, kn);
+                    if (tg[q] >= 0 && ps.ok) pushValues<T, B>(tg[q], kn * half, out, tm, dep, ps, kn);
                 }
 #pragma unroll
                 for (int e = 0; e < B; ++e) y[i * B + e] = out[e];
@@ -895,6 +920,12 @@ __device__ __forceinline__ void bicgstabBody(const KArgs<T>& a, const Team<MODE>
     if (MODE == SYNC_CLUSTER || a.hybrid) {
         const cg::cluster_group cl = cg::this_cluster();
         const int crank = (int)cl.block_rank(), csize = (int)cl.num_blocks();
+        // the push tables and the hybrid split assume one cluster size; a launch
+        // with another (the same in every block) reports an error and does nothing
+        if ((a.dsmem && csize != a.cluster) || (a.hybrid && (csize != a.hybrid || csize != a.gs.perCluster))) {
+            if (crank == 0 && threadIdx.x == 0) a.st->code = GBFV_ERR_CUDA;
+            return;
+        }
         for (int k = 0; k < PUSH_BUFFERS; ++k) {
             ps.mb[k] = smemAddr(&mbar[k]);
             ps.ph[k] = 0;

@@ -24,6 +24,8 @@ struct GridSync {
     unsigned* count;
     unsigned* gen;
     int* abort;
+    int perCluster;     // hybrid launch: blocks per cluster; the cluster arrives once and
+                        // its blocks share one decision (0: every block arrives)
 };
 
 // everything one solve needs; T is the Krylov/preconditioner precision
@@ -53,6 +55,7 @@ struct KArgs {
     const int* levVals; // push sweeps: values block r receives at level l, [(r*numLev + l)*2 + fwd/bwd]
     int dsmem;          // cluster mode: every level fits one row per thread, so the
                         // previous level's results are exchanged in distributed shared memory
+    int cluster;        // push sweeps: the cluster size the push tables were built for
 };
 
 template <class T> int launchBicgstab(const KArgs<T>& a, int b, int mode, int nblocks, cudaStream_t s);
