@@ -336,15 +336,21 @@ typedef struct gbfv_kernel_stats {
 } gbfv_kernel_stats;
 int gbfv_get_kernel_stats(const gbfv_ctx* ctx, gbfv_kernel_stats* out);
 /* launch configuration the autotuner chose for the persistent solve kernel
- * of a precision (GBFV_PREC_FP64 / GBFV_PREC_MIXED): cluster (mode 1) or
- * cooperative grid (mode 0), blocks, and the candidate timings [ms]       */
+ * of a precision (GBFV_PREC_FP64 / GBFV_PREC_MIXED): cluster (mode 1),
+ * cooperative grid (mode 0) or hybrid (mode 2), possibly with
+ * GBFV_SOLVER_TILES, blocks, and the candidate timings [ms]               */
 int gbfv_solver_config(const gbfv_ctx* ctx, int precision, int* mode, int* blocks,
                        double* tune_ms, int* num_tuned);
 /* fix the launch configuration of the persistent solve kernel of a
  * precision (mode 1 = cluster of `blocks` blocks, 0 = cooperative grid,
  * 2 = hybrid: `blocks` in clusters of 16 over the GPU, the first cluster
  * factorizes and sweeps, all blocks share SpMV, updates and reductions) and
- * skip the autotuner; GBFV_ERR_UNSUPPORTED beyond what the device allows  */
+ * skip the autotuner; GBFV_ERR_UNSUPPORTED beyond what the device allows.
+ * Modes 1 and 2 or-ed with GBFV_SOLVER_TILES deal the rows of every ILU
+ * level to the sweeping cluster's blocks by the spatial tile of their cell
+ * (grid contexts only; GBFV_ERR_UNSUPPORTED where a tile's level is wider
+ * than a block or the tables exceed shared memory)                        */
+#define GBFV_SOLVER_TILES 4
 int gbfv_set_solver_config(gbfv_ctx* ctx, int precision, int mode, int blocks);
 int gbfv_reset_kernel_stats(gbfv_ctx* ctx);
 /* with GBFV_PROFILE set in the environment at creation: nanoseconds spent
@@ -355,7 +361,9 @@ int gbfv_solver_phase_ns(gbfv_ctx* ctx, unsigned long long* ns8);
 /* with GBFV_PROFILE: SM cycles one working thread of the forward sweeps
  * spent per level since the last call: [0] waiting for its data, [1]
  * computing, [2] pushing results and storing, [3] in the level barrier;
- * [4] the number of levels sampled                                       */
+ * [4] the number of levels sampled.  With GBFV_SOLVER_TILES (thread 0 of
+ * block 5): [0] staging the level's operands, [1] waiting for the halo
+ * values, [2] computing, pushing and storing, [3] the level barrier       */
 int gbfv_solver_level_cycles(gbfv_ctx* ctx, unsigned long long* c8);
 
 /* ------------------------------------------------------------------ */

@@ -105,6 +105,16 @@ struct SolverData {
     int* levVals = nullptr;     // values each block receives per level and sweep
     int pushKey[4] = {0, 0, 0, 0};
     int ownerMode = 0;          // rows of a level to blocks: warp round-robin (0) / contiguous (1)
+    // spatial-tile sweeps (see buildTileTables)
+    std::vector<int> tileKey;   // [p] tile of row p out of TILE_KEYS (empty: no tiles)
+    int4* tInfo = nullptr;      // [r*numLev + l]: first row, row count, forward / backward halo slots
+    int* tDepF = nullptr;       // [q*ldN + p] dependency code of row p, forward sweep
+    int* tDepB = nullptr;       // backward sweep
+    int* tPushF = nullptr;      // [t*ldN + p] consumers of row p in other tiles, forward sweep
+    int* tPushB = nullptr;
+    int tHalo = 0;              // halo slots per block (the most any block receives in one sweep)
+    int tWidth = 0;             // the most rows a block computes in one level
+    int tileKeyC = 0;           // cluster size the tables were built for
     unsigned long long* prof = nullptr;  // per-phase timers of the solve kernel (GBFV_PROFILE=1)
     // cumulative statistics of the persistent solve kernel
     cudaEvent_t evA = nullptr, evB = nullptr;
@@ -121,10 +131,12 @@ int allocSolver(SolverData& S, int maxBlocksOverride = 0)
     if ((st = devAlloc(&S.A32, S.nslot * bb * ld))) return st;
     if ((st = devAlloc(&S.FL32, S.dim * bb * ld))) return st;
     if ((st = devAlloc(&S.FD32, bb * ld))) return st;
+    // Krylov vectors padded by 16 values: the tile sweeps' bulk copies round a
+    // run of rows up to a 16-byte boundary
     for (auto& p : S.v64)
-        if ((st = devAlloc(&p, (size_t)S.N * S.b))) return st;
+        if ((st = devAlloc(&p, (size_t)S.N * S.b + 16))) return st;
     for (auto& p : S.v32)
-        if ((st = devAlloc(&p, (size_t)S.N * S.b))) return st;
+        if ((st = devAlloc(&p, (size_t)S.N * S.b + 16))) return st;
     if ((st = devAlloc(&S.xref, (size_t)S.N * S.b))) return st;
     if ((st = devAlloc(&S.rref, (size_t)S.N * S.b))) return st;
     (void)maxBlocksOverride;
@@ -148,11 +160,21 @@ int allocSolver(SolverData& S, int maxBlocksOverride = 0)
     // forced configuration, e.g. GBFV_SOLVER=cluster:16 or grid:152
     if (const char* f = getenv("GBFV_SOLVER")) {
         int n = 0;
+        // ":tiles" selects the spatial-tile sweeps, e.g. GBFV_SOLVER=cluster:16:tiles
+        const int tf = strstr(f, "tiles") ? SYNC_TILES : 0;
         if (sscanf(f, "cluster:%d", &n) == 1 && n > 0)
-            for (int k = 0; k < 2; ++k) { S.mode[k] = SYNC_CLUSTER; S.nblk[k] = std::min(n, S.maxCluster[k]); S.tuned[k] = 1; }
+            for (int k = 0; k < 2; ++k) {
+                S.mode[k] = SYNC_CLUSTER | tf;
+                S.nblk[k] = std::min(n, S.maxCluster[k]);
+                S.tuned[k] = 1;
+            }
         else if (strncmp(f, "hybrid", 6) == 0)
             for (int k = 0; k < 2; ++k) {
-                if (S.maxHybrid[k] > HYBRID_CLUSTER) { S.mode[k] = SYNC_HYBRID; S.nblk[k] = S.maxHybrid[k]; S.tuned[k] = 1; }
+                if (S.maxHybrid[k] > HYBRID_CLUSTER) {
+                    S.mode[k] = SYNC_HYBRID | tf;
+                    S.nblk[k] = S.maxHybrid[k];
+                    S.tuned[k] = 1;
+                }
             }
         else if (sscanf(f, "grid:%d", &n) == 1 && n > 0)
             for (int k = 0; k < 2; ++k) { S.mode[k] = SYNC_GRID; S.nblk[k] = std::min(n, S.maxGrid[k]); S.tuned[k] = 1; }
@@ -184,6 +206,11 @@ void freeSolver(SolverData& S)
 {
     cudaFree(S.col);
     cudaFree(S.levPtrD);
+    cudaFree(S.tInfo);
+    cudaFree(S.tDepF);
+    cudaFree(S.tDepB);
+    cudaFree(S.tPushF);
+    cudaFree(S.tPushB);
     cudaFree(S.FL64);
     cudaFree(S.FD64);
     cudaFree(S.A32);
@@ -283,9 +310,10 @@ int resetStatus(cudaStream_t s, DevStatus* d)
     return GBFV_OK;
 }
 
-// levels and wavefront-major order from a lower-triangular dependency walk
+// levels and wavefront-major order from a lower-triangular dependency walk;
+// inside a level, rows are ordered by key (when given), then naturally
 void buildOrder(int N, const std::vector<std::vector<int>>& lower, std::vector<int>& perm,
-                std::vector<int>& iperm, std::vector<int>& levPtr)
+                std::vector<int>& iperm, std::vector<int>& levPtr, const std::vector<int>* key = nullptr)
 {
     std::vector<int> level(N, 0);
     int maxLev = 0;
@@ -302,11 +330,55 @@ void buildOrder(int N, const std::vector<std::vector<int>>& lower, std::vector<i
     iperm.assign(N, 0);
     perm.assign(N, 0);
     std::vector<int> pos(cnt.begin(), cnt.end() - 1);
+    if (key) {
+        std::vector<int> idx(N);
+        for (int i = 0; i < N; ++i) idx[i] = i;
+        std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) {
+            return level[x] != level[y] ? level[x] < level[y] : (*key)[x] < (*key)[y];
+        });
+        for (int p = 0; p < N; ++p) {
+            iperm[p] = idx[p];
+            perm[idx[p]] = p;
+        }
+        return;
+    }
     for (int i = 0; i < N; ++i) {  // natural order inside a level
         const int p = pos[level[i]]++;
         iperm[p] = i;
         perm[i] = p;
     }
+}
+
+// Spatial tiles of the cluster sweeps: TILE_KEYS = 16 tiles, 4 x 4 over the
+// two axes with the most cells, each cell's index along an axis counted from
+// the lower boundary (natural order: the lower neighbour comes first).  For
+// a cluster of C blocks (C dividing 16) block key / (16 / C) owns the cell,
+// so rows ordered by key inside a level are contiguous per block.
+std::vector<int> tileKeys(int N, int dim, int ndir, const std::vector<int>& nbrDir)
+{
+    std::vector<int> key(N, 0);
+    if (dim < 2) return key;
+    std::vector<int> idx((size_t)N * dim, 0);
+    int ext[3] = {1, 1, 1};
+    for (int I = 0; I < N; ++I)
+        for (int a = 0; a < dim; ++a) {
+            const int K = nbrDir[(size_t)I * ndir + 2 * a];
+            idx[(size_t)I * dim + a] = K >= 0 ? idx[(size_t)K * dim + a] + 1 : 0;
+            ext[a] = std::max(ext[a], idx[(size_t)I * dim + a] + 1);
+        }
+    int ax0 = 0, ax1 = 1;  // the two longest axes, ax0 >= ax1
+    if (dim == 3) {
+        int o[3] = {0, 1, 2};
+        std::sort(o, o + 3, [&](int x, int y) { return ext[x] != ext[y] ? ext[x] > ext[y] : x < y; });
+        ax0 = o[0];
+        ax1 = o[1];
+    }
+    for (int I = 0; I < N; ++I) {
+        const int t0 = (int)((long)idx[(size_t)I * dim + ax0] * 4 / ext[ax0]);
+        const int t1 = (int)((long)idx[(size_t)I * dim + ax1] * 4 / ext[ax1]);
+        key[I] = t0 * 4 + t1;
+    }
+    return key;
 }
 
 // Block and thread slot (within the level group) that own position t of a
@@ -461,6 +533,112 @@ int buildPushTargets(SolverData& S, int C, int G, int NT, int mode)
     return GBFV_OK;
 }
 
+// Tables of the spatial-tile sweeps for a cluster of C blocks of NT threads.
+// Block r owns the rows whose tile key / (TILE_KEYS / C) is r; inside a
+// level they are contiguous (the order is by key), so block r computes rows
+// first..first+count-1 of level l, one per thread (tileFits: at most NT).  A dependency on a row of
+// the same block is read from the block's copy of the previous level (by
+// its position there); one on another block's row arrives by a push into a
+// halo slot, numbered per block and sweep, so no slot is written twice in a
+// sweep and no flow control is needed.  Unsupported (no tiles, too many
+// levels or halo slots): GBFV_ERR_UNSUPPORTED.
+int buildTileTables(SolverData& S, int C)
+{
+    if (S.tileKeyC == C && S.tInfo) return GBFV_OK;
+    const int N = S.N, ld = S.ldN, dim = S.dim, nl = (int)S.levPtr.size() - 1;
+    if (S.tileKey.empty() || C < 2 || TILE_KEYS % C || !S.adjacentLevels || nl > TILE_MAX_LEVELS || dim > 3)
+        return GBFV_ERR_UNSUPPORTED;
+    const int per = TILE_KEYS / C;
+    std::vector<int> lev(N), own(N), pos(N);
+    for (int l = 0; l < nl; ++l)
+        for (int p = S.levPtr[l]; p < S.levPtr[l + 1]; ++p) {
+            lev[p] = l;
+            own[p] = S.tileKey[p] / per;
+        }
+    std::vector<int4> info((size_t)C * nl, make_int4(0, 0, 0, 0));
+    for (int l = 0; l < nl; ++l) {
+        int prev = -1;
+        for (int p = S.levPtr[l]; p < S.levPtr[l + 1]; ++p) {
+            const int r = own[p];
+            if (r < prev) return GBFV_ERR_UNSUPPORTED;  // not contiguous per block
+            int4& f = info[(size_t)r * nl + l];
+            if (r != prev) f.x = p;
+            pos[p] = p - f.x;
+            f.y++;
+            prev = r;
+        }
+    }
+    std::vector<int> depF((size_t)3 * ld, -1), depB((size_t)3 * ld, -1), pushF((size_t)3 * ld, -1),
+        pushB((size_t)3 * ld, -1);
+    std::vector<int> hF(C, 0), hB(C, 0);
+    auto addPush = [&](std::vector<int>& push, int producer, int target) {
+        for (int t = 0; t < 3; ++t)
+            if (push[(size_t)t * ld + producer] < 0) {
+                push[(size_t)t * ld + producer] = target;
+                return true;
+            }
+        return false;
+    };
+    // forward sweep in level order, backward sweep in reverse level order, so
+    // a block's halo slots are numbered in the order it uses them
+    for (int p = 0; p < N; ++p) {
+        const int r = own[p];
+        for (int q = 0; q < dim; ++q) {
+            const int j = S.colHost[(size_t)q * ld + p];  // lower neighbour in slot q
+            if (j < 0) continue;
+            if (own[j] == r) depF[(size_t)q * ld + p] = pos[j];
+            else {
+                const int h = hF[r]++;
+                depF[(size_t)q * ld + p] = TILE_HALO | h;
+                if (!addPush(pushF, j, (r << 24) | h)) return GBFV_ERR_UNSUPPORTED;
+                info[(size_t)r * nl + lev[p]].z++;
+            }
+        }
+    }
+    for (int p = N - 1; p >= 0; --p) {
+        const int r = own[p];
+        for (int q = 0; q < dim; ++q) {
+            const int j = S.colHost[(size_t)(2 * dim - q) * ld + p];  // upper neighbours, descending columns
+            if (j < 0) continue;
+            if (own[j] == r) depB[(size_t)q * ld + p] = pos[j];
+            else {
+                const int h = hB[r]++;
+                depB[(size_t)q * ld + p] = TILE_HALO | h;
+                if (!addPush(pushB, j, (r << 24) | h)) return GBFV_ERR_UNSUPPORTED;
+                info[(size_t)r * nl + lev[p]].w++;
+            }
+        }
+    }
+    int halo = 1, wmax = 0;
+    for (int r = 0; r < C; ++r) halo = std::max(halo, std::max(hF[r], hB[r]));
+    for (const int4& f : info) wmax = std::max(wmax, f.y);
+    if (halo > TILE_MASK) return GBFV_ERR_UNSUPPORTED;
+    cudaFree(S.tInfo);
+    cudaFree(S.tDepF);
+    cudaFree(S.tDepB);
+    cudaFree(S.tPushF);
+    cudaFree(S.tPushB);
+    S.tInfo = nullptr;
+    S.tDepF = S.tDepB = S.tPushF = S.tPushB = nullptr;
+    S.tileKeyC = 0;
+    int st;
+    if ((st = upload(&S.tInfo, info)) || (st = upload(&S.tDepF, depF)) || (st = upload(&S.tDepB, depB)) ||
+        (st = upload(&S.tPushF, pushF)) || (st = upload(&S.tPushB, pushB)))
+        return st;
+    S.tHalo = halo;
+    S.tWidth = wmax;
+    S.tileKeyC = C;
+    return GBFV_OK;
+}
+
+// the tile sweeps of precision T fit: one row per thread, shared memory
+template <class T>
+bool tileFits(const SolverData& S, int NT)
+{
+    const int nl = (int)S.levPtr.size() - 1;
+    return S.tWidth <= NT && tileSmemBytes<T>(S.b, nl, S.tHalo, S.tWidth, S.dim) <= solverSmemLimit<T>(S.b);
+}
+
 // 1 if every lower dependency of a row sits exactly one level below it
 int adjacentLevels(const std::vector<std::vector<int>>& lower, const std::vector<int>& perm,
                    const std::vector<int>& levPtr)
@@ -480,6 +658,8 @@ template <class T>
 int fillKArgs(SolverData& S, DevStatus* st, const T* A, T* FL, T* FD, const T* rhs, T* const* vec, int factor,
               double redTol, double absTol, double maxRes, int maxIter, int mode, int nblocks, KArgs<T>& a)
 {
+    const bool tiles = (mode & SYNC_TILES) != 0;
+    mode &= ~SYNC_TILES;
     a.N = S.N;
     a.ldN = S.ldN;
     a.dim = S.dim;
@@ -520,6 +700,30 @@ int fillKArgs(SolverData& S, DevStatus* st, const T* A, T* FL, T* FD, const T* r
         for (size_t l = 0; l + 1 < S.levPtr.size(); ++l)
             maxChunk = std::max(maxChunk, levelChunk(S.levPtr[l + 1] - S.levPtr[l], C, omode));
         constexpr int NTC = clusterThreads<T>();
+        a.tile = 0;
+        a.tinfo = nullptr;
+        a.tdepF = a.tdepB = a.tpushF = a.tpushB = nullptr;
+        a.thalo = 0;
+        a.twidth = 0;
+        if (tiles) {
+            if (mode != SYNC_CLUSTER && mode != SYNC_HYBRID) return GBFV_ERR_UNSUPPORTED;
+            const int ts = buildTileTables(S, C);
+            if (ts) return ts;
+            if (!tileFits<T>(S, NTC)) return GBFV_ERR_UNSUPPORTED;
+            a.tile = 1;
+            a.dsmem = 0;
+            a.grp = 1;
+            a.pushL = a.pushU = a.levVals = nullptr;
+            a.cluster = C;
+            a.tinfo = S.tInfo;
+            a.tdepF = S.tDepF;
+            a.tdepB = S.tDepB;
+            a.tpushF = S.tPushF;
+            a.tpushB = S.tPushB;
+            a.thalo = S.tHalo;
+            a.twidth = S.tWidth;
+            return GBFV_OK;
+        }
         a.dsmem = ((mode == SYNC_CLUSTER || mode == SYNC_HYBRID) && S.adjacentLevels && maxChunk <= NTC &&
                    (int)S.levPtr.size() - 1 <= MAX_PUSH_LEVELS && !getenv("GBFV_NO_DSMEM")) ? 1 : 0;
         if (mode == SYNC_HYBRID && !a.dsmem) return GBFV_ERR_UNSUPPORTED;  // the hybrid sweeps need the push tables
@@ -553,7 +757,7 @@ int runKrylovCfg(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* h
     if ((rs = resetStatus(stream, st))) return rs;
     CK(cudaMemsetAsync(S.bar, 0, 4 * sizeof(unsigned), stream));
     cudaEventRecord(S.evA, stream);
-    const int ls = launchBicgstab<T>(a, S.b, mode, nblocks, stream);
+    const int ls = launchBicgstab<T>(a, S.b, mode & ~SYNC_TILES, nblocks, stream);
     if (ls != GBFV_OK) {
         setError(std::string("cooperative launch failed: ") + cudaGetErrorString(cudaGetLastError()));
         return ls;
@@ -597,6 +801,10 @@ void tuneSolver(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hs
         cands.push_back({SYNC_GRID, std::min(2 * nsm, S.maxGrid[k])});
         if (S.maxHybrid[k] > HYBRID_CLUSTER) cands.push_back({SYNC_HYBRID, S.maxHybrid[k]});
     }
+    // The spatial-tile sweeps are not a candidate: on the black-oil workloads
+    // they were slower than the push sweeps (a level's rows of one tile sit on
+    // one SM), so they only run when asked for (GBFV_SOLVER=...:tiles,
+    // gbfv_set_solver_config with GBFV_SOLVER_TILES).
     double best = 1e300;
     Cand pick = {S.mode[k], S.nblk[k]};
     int idx = 0;
@@ -839,7 +1047,8 @@ static int createImpl(gbfv_ctx* C, const gbfv_problem* P)
             if (K >= 0) lower[I].push_back(K);
         }
     std::vector<int> levPtr;
-    buildOrder(N, lower, C->perm, C->iperm, levPtr);
+    const std::vector<int> tkey = tileKeys(N, dim, ndir, nbrDir);
+    buildOrder(N, lower, C->perm, C->iperm, levPtr, &tkey);
     const int ld = ((N + 63) / 64) * 64;
     C->ldN = ld;
     const auto& perm = C->perm;
@@ -1196,6 +1405,10 @@ static int createImpl(gbfv_ctx* C, const gbfv_problem* P)
     S.levPtr = levPtr;
     S.adjacentLevels = adjacentLevels(lower, C->perm, levPtr);
     S.colHost = hCol;
+    if (dim >= 2) {
+        S.tileKey.resize(N);
+        for (int p = 0; p < N; ++p) S.tileKey[p] = tkey[iperm[p]];
+    }
     if ((st = upload(&S.col, hCol)) || (st = upload(&S.levPtrD, levPtr))) return st;
     if ((st = allocSolver(S))) return st;
     if ((st = devAlloc(&C->st, 1))) return st;
@@ -1536,13 +1749,22 @@ int gbfv_get_kernel_stats(const gbfv_ctx* Cc, gbfv_kernel_stats* out)
 
 int gbfv_set_solver_config(gbfv_ctx* C, int precision, int mode, int blocks)
 {
-    if (!C || (mode != SYNC_CLUSTER && mode != SYNC_GRID && mode != SYNC_HYBRID) || blocks < 1) return GBFV_ERR_ARG;
+    const int base = mode & ~SYNC_TILES;
+    if (!C || (base != SYNC_CLUSTER && base != SYNC_GRID && base != SYNC_HYBRID) || blocks < 1 ||
+        (base == SYNC_GRID && mode != base))
+        return GBFV_ERR_ARG;
     const int k = precision == GBFV_PREC_MIXED ? 1 : 0;
     SolverData& S = C->S;
-    if (mode == SYNC_CLUSTER && blocks > S.maxCluster[k]) return GBFV_ERR_UNSUPPORTED;
-    if (mode == SYNC_HYBRID && (blocks > S.maxHybrid[k] || blocks % HYBRID_CLUSTER || blocks <= HYBRID_CLUSTER))
+    if (base == SYNC_CLUSTER && blocks > S.maxCluster[k]) return GBFV_ERR_UNSUPPORTED;
+    if (base == SYNC_HYBRID && (blocks > S.maxHybrid[k] || blocks % HYBRID_CLUSTER || blocks <= HYBRID_CLUSTER))
         return GBFV_ERR_UNSUPPORTED;
-    if (mode == SYNC_GRID && blocks > S.maxGrid[k]) return GBFV_ERR_UNSUPPORTED;
+    if (base == SYNC_GRID && blocks > S.maxGrid[k]) return GBFV_ERR_UNSUPPORTED;
+    if (mode & SYNC_TILES) {
+        const int c = base == SYNC_HYBRID ? HYBRID_CLUSTER : blocks;
+        if (buildTileTables(S, c) != GBFV_OK) return GBFV_ERR_UNSUPPORTED;
+        const bool fits = k ? tileFits<float>(S, clusterThreads<float>()) : tileFits<double>(S, clusterThreads<double>());
+        if (!fits) return GBFV_ERR_UNSUPPORTED;
+    }
     S.mode[k] = mode;
     S.nblk[k] = blocks;
     S.tuned[k] = 1;

@@ -499,6 +499,8 @@ struct PushState {
     unsigned dep;     // shared address of the dependency buffers [PUSH_BUFFERS][NT][3][padB(B)]
     unsigned lev;     // shared address of the level-done mbarrier (C arrivals)
     unsigned levPh;
+    unsigned tph;     // tile sweeps: parity of the current sweep's phase of every level's halo mbarrier
+    int sbuf;         // tile sweeps: the staging buffer of the next level
     int ok;
 };
 
@@ -583,6 +585,11 @@ __device__ __forceinline__ void cpAsync(unsigned dst, const void* src)
 {
     asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(dst), "l"(src), "n"(S) : "memory");
 }
+// 16-byte copy, both addresses 16-byte aligned, not cached in L1
+__device__ __forceinline__ void cpAsync16(unsigned dst, const void* src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
 __device__ __forceinline__ void cpCommit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cpWaitAll() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
@@ -618,6 +625,72 @@ struct PushSmem {
     }
 };
 constexpr int PUSH_COUNT_MASK = PUSH_BARRIER_FLAG - 1;
+
+// Shared memory of the tile sweeps: per level this block's (first row, rows,
+// forward / backward halo slots) and the mbarrier that counts the bytes
+// pushed into it for that level; the halo slots; two copies of this block's
+// results of a level (the current and the previous one); two staging
+// buffers.  A level's operands of one block are contiguous runs (its rows
+// are), staged in 16-byte chunks, the next level's while the current one is
+// computed.  A run starts at the 16-byte boundary below its first row, so a
+// few elements precede the first row's.
+template <class T, int B, int NT>
+struct TileSmem {
+    static constexpr int E = 16 / sizeof(T);  // elements of T per 16 bytes
+    int4* info;
+    unsigned long long* mb;   // [nl] halo data of a level
+    T* halo;                  // [slot][padB(B)]
+    T* loc;                   // [2][NT][padB(B)]: results of levels of parity 0 and 1
+    T* stT;                   // [2][regT]: matrix blocks and vectors of a level
+    int* stI;                 // [2][regI]: dependency codes and push targets of a level
+    int* bad;                 // block rank 0's copy: a wait of some block of the cluster gave up (sticky)
+    int capS, capA, capI, regT, regI;
+    __host__ __device__ static constexpr int rup(int x, int m) { return (x + m - 1) / m * m; }
+    // capacities for levels of at most w rows: a field of one value per row
+    // (T or int), a vector of B values per row; per buffer the larger of the
+    // forward sweep's (dim*B*B fields, 3 vectors) and the backward sweep's
+    // ((dim+1)*B*B fields, 1 vector), and 2*dim int fields
+    __host__ __device__ static void caps(int w, int dim, int& cS, int& cA, int& cI, int& rT, int& rI)
+    {
+        cS = rup(w + E, E);
+        cA = rup(w * B + E, E);
+        cI = rup(w + 4, 4);
+        const int f = dim * B * B * cS + 3 * cA, g = (dim + 1) * B * B * cS + cA;
+        rT = f > g ? f : g;
+        rI = 2 * dim * cI;
+    }
+    __host__ __device__ static size_t a16(size_t x) { return (x + 15) & ~(size_t)15; }
+    struct Off {
+        size_t mb, halo, loc, stT, stI, bad, end;
+    };
+    __host__ __device__ static Off offsets(int nl, int hs, int w, int dim)
+    {
+        int cS, cA, cI, rT, rI;
+        caps(w, dim, cS, cA, cI, rT, rI);
+        Off o;
+        o.mb = a16(16 * (size_t)nl);
+        o.halo = a16(o.mb + 8 * (size_t)nl);
+        o.loc = a16(o.halo + sizeof(T) * (size_t)hs * padB(B));
+        o.stT = a16(o.loc + sizeof(T) * 2 * (size_t)NT * padB(B));
+        o.stI = a16(o.stT + sizeof(T) * 2 * (size_t)rT);
+        o.bad = a16(o.stI + sizeof(int) * 2 * (size_t)rI);
+        o.end = o.bad + 16;
+        return o;
+    }
+    __host__ __device__ static size_t bytes(int nl, int hs, int w, int dim) { return offsets(nl, hs, w, dim).end; }
+    __device__ TileSmem(unsigned char* base, int nl, int hs, int w, int dim)
+    {
+        const Off o = offsets(nl, hs, w, dim);
+        caps(w, dim, capS, capA, capI, regT, regI);
+        info = reinterpret_cast<int4*>(base);
+        mb = reinterpret_cast<unsigned long long*>(base + o.mb);
+        halo = reinterpret_cast<T*>(base + o.halo);
+        loc = reinterpret_cast<T*>(base + o.loc);
+        stT = reinterpret_cast<T*>(base + o.stT);
+        stI = reinterpret_cast<int*>(base + o.stI);
+        bad = reinterpret_cast<int*>(base + o.bad);
+    }
+};
 
 // forward sweep y = L^-1 d (fuseP: d is the BiCGStab direction p, formed here).
 // The group that computed the previous level stages the operands of its next
@@ -872,6 +945,324 @@ __device__ __forceinline__ void sweepUpperPush(const KArgs<T>& a, T* y, const Te
     cg::this_cluster().sync();
 }
 
+// ------------------------------------------------ spatial-tile sweeps ----
+// Block r of the cluster owns the rows of one spatial tile (all levels); at
+// level l its thread u computes row first(l) + u.  Dependencies inside the
+// tile come from the block's copy of the previous level (a __syncthreads
+// apart); those across a tile boundary are pushed by the producing block
+// with st.async into a halo slot of the consumer, counted on the consumer's
+// mbarrier of that level.  Each halo slot is written once per sweep, so a
+// block runs ahead of its downstream neighbours as far as its own
+// dependencies allow: the sweep is a pipeline over the tiles, and the
+// critical path crosses a block boundary only at tile edges.
+
+// push of a row's result into a halo slot of another block of the cluster
+template <class T, int B>
+__device__ __forceinline__ void tilePush(int target, const T (&out)[B], unsigned mbLevel, unsigned halo0,
+                                         const Team<SYNC_CLUSTER>& tm, int hcap, PushState& ps)
+{
+    const int owner = target >> 24, h = target & TILE_MASK;
+    if (owner >= tm.nblk || h >= hcap) {  // tables for another cluster: push nothing
+        ps.ok = 0;
+        return;
+    }
+    const unsigned dst = mapaRank(halo0 + (unsigned)(h * padB(B) * sizeof(T)), owner);
+    stAsyncSlot<T, B>(dst, out, mapaRank(mbLevel, owner));
+}
+
+// the dependency value of code c: this block's previous level or a halo slot
+template <class T, int B>
+__device__ __forceinline__ const T* tileDep(int c, const T* prev, const T* halo, int hcap, int NT, PushState& ps)
+{
+    if (c & TILE_HALO) {
+        const int h = c & TILE_MASK;
+        if (h < hcap) return halo + h * padB(B);
+    }
+    else if (c < NT)
+        return prev + c * padB(B);
+    ps.ok = 0;
+    return nullptr;
+}
+
+// End of a tile sweep: the cluster barrier publishes the global stores and
+// frees the halo slots for the next sweep.  A wait that gave up anywhere in
+// the cluster is made known to every thread of it (block rank 0 keeps the
+// flag); from then on no block arms, waits or pushes, so no mbarrier phase
+// is armed twice, and the solve ends with GBFV_ERR_TIMEOUT.
+template <class T, int B, int NT>
+__device__ __forceinline__ void tileSweepEnd(const TileSmem<T, B, NT>& ts, PushState& ps)
+{
+    cg::cluster_group cl = cg::this_cluster();
+    if (!ps.ok) *cl.map_shared_rank(ts.bad, 0) = 1;
+    ps.tph ^= 1u;
+    cl.sync();
+    if (*cl.map_shared_rank(ts.bad, 0)) ps.ok = 0;
+}
+
+// The block stages level l's operands into buffer bf with 16-byte cp.async
+// chunks spread over its threads (one commit group per level).  Forward
+// sweep: the dim*B*B factor fields, nv vectors, dependency codes and push
+// targets; backward sweep: the dim*B*B upper blocks, the B*B inverted pivot
+// fields, the vector y, codes and targets.
+template <class T, int B, int NT>
+__device__ __forceinline__ void tileStage(const KArgs<T>& a, const TileSmem<T, B, NT>& ts, int l, int bf, bool fwd,
+                                          const T* v0, const T* v1, const T* v2, int nv)
+{
+    constexpr int E = TileSmem<T, B, NT>::E, BB = B * B;
+    const int dim = a.dim, ld = a.ldN;
+    const int4 f = ts.info[l];
+    const int first = f.x, cnt = f.y;
+    const int a0S = first & ~(E - 1), a0A = (first * B) & ~(E - 1), a0I = first & ~3;
+    // 16-byte chunks per field of each kind
+    const int cS = TileSmem<T, B, NT>::rup((first - a0S + cnt) * (int)sizeof(T), 16) / 16;
+    const int cA = TileSmem<T, B, NT>::rup((first * B - a0A + cnt * B) * (int)sizeof(T), 16) / 16;
+    const int cI = TileSmem<T, B, NT>::rup((first - a0I + cnt) * 4, 16) / 16;
+    const int nS = fwd ? dim * BB : (dim + 1) * BB;
+    const int n1 = nS * cS, n2 = n1 + nv * cA, n3 = n2 + 2 * dim * cI;
+    const unsigned sT = smemAddr(ts.stT + bf * ts.regT), sI = smemAddr(ts.stI + bf * ts.regI);
+    for (int k = threadIdx.x; k < n3; k += NT) {
+        if (k < n1) {
+            const int j = k / cS, c = k - j * cS;
+            const T* src;
+            if (fwd)
+                src = a.FL + (size_t)j * ld;  // field s*B*B + e of the lower factor
+            else if (j < dim * BB) {
+                const int q = j / BB, e = j - q * BB;
+                src = a.A + (size_t)((2 * dim - q) * BB + e) * ld;  // descending column order
+            }
+            else
+                src = a.FD + (size_t)(j - dim * BB) * ld;
+            cpAsync16(sT + (unsigned)((j * ts.capS) * sizeof(T) + c * 16), src + a0S + c * E);
+        }
+        else if (k < n2) {
+            const int v = (k - n1) / cA, c = k - n1 - v * cA;
+            const T* src = v == 0 ? v0 : v == 1 ? v1 : v2;
+            cpAsync16(sT + (unsigned)((nS * ts.capS + v * ts.capA) * sizeof(T) + c * 16), src + a0A + c * E);
+        }
+        else {
+            const int m = (k - n2) / cI, c = k - n2 - m * cI;  // dependency codes, then push targets
+            const int* src = m < dim ? (fwd ? a.tdepF : a.tdepB) + (size_t)m * ld
+                                     : (fwd ? a.tpushF : a.tpushB) + (size_t)(m - dim) * ld;
+            cpAsync16(sI + (unsigned)(m * ts.capI * 4 + c * 16), src + a0I + c * 4);
+        }
+    }
+    cpCommit();
+}
+
+// Before level l is computed: stage it unless the previous level did, then
+// the next level of this block into the other buffer (read two levels ago:
+// every thread is past that level's barrier); wait for level l's copies and
+// make them visible to the whole block.  Returns the buffer of level l.
+template <class T, int B, int NT>
+__device__ __forceinline__ int tileStageStep(const KArgs<T>& a, const TileSmem<T, B, NT>& ts, int l, int next,
+                                             int& staged, bool fwd, const T* v0, const T* v1, const T* v2, int nv,
+                                             PushState& ps)
+{
+    const int bf = ps.sbuf;
+    if (staged != l) tileStage<T, B, NT>(a, ts, l, bf, fwd, v0, v1, v2, nv);
+    if (next >= 0) {
+        tileStage<T, B, NT>(a, ts, next, bf ^ 1, fwd, v0, v1, v2, nv);
+        asm volatile("cp.async.wait_group 1;" ::: "memory");
+    }
+    else
+        cpWaitAll();
+    staged = next;
+    ps.sbuf = bf ^ 1;
+    __syncthreads();
+    return bf;
+}
+
+// forward sweep y = L^-1 d (fuseP: d is the BiCGStab direction p, formed here)
+template <class T, int B, int NT>
+__device__ __forceinline__ void sweepLowerTile(const KArgs<T>& a, const T* d, T* y, bool fuseP, T beta, T omega,
+                                               const Team<SYNC_CLUSTER>& tm, const TileSmem<T, B, NT>& ts,
+                                               PushState& ps)
+{
+    constexpr int BB = B * B, PB = padB(B), E = TileSmem<T, B, NT>::E;
+    const int dim = a.dim, nl = a.numLev, u = threadIdx.x, hcap = a.thalo;
+    const int capS = ts.capS, capA = ts.capA, capI = ts.capI, nS = dim * BB;
+    const unsigned mb0 = smemAddr(ts.mb), halo0 = smemAddr(ts.halo);
+    const unsigned par = ps.tph;
+    // this sweep's phase of every level's mbarrier: one arrival carrying the
+    // bytes the other blocks push into this one at that level
+    if (ps.ok)
+        for (int l = u; l < nl; l += NT) mbarArriveTx(mb0 + 8u * l, (unsigned)(ts.info[l].z * PB * sizeof(T)));
+    const T* v0 = fuseP ? a.v : d;
+    const int nv = fuseP ? 3 : 1;
+    // optional cycle counts of thread 0 of block 5 (GBFV_PROFILE): staging,
+    // halo wait, compute + pushes + stores, level barrier
+    const bool probe = a.prof != nullptr && tm.rank == 5 % tm.nblk && u == 0;
+    unsigned long long cyc[4] = {0, 0, 0, 0}, nprobe = 0, t0 = 0, t1 = 0, t2 = 0, t3 = 0;
+    int staged = -1;
+    for (int l = 0; l < nl; ++l) {
+        const int4 f = ts.info[l];
+        if (f.y == 0) continue;  // no rows of this tile at this level (the same for the whole block)
+        const int next = l + 1 < nl && ts.info[l + 1].y > 0 ? l + 1 : -1;
+        if (probe) t0 = clock64();
+        const int bf = tileStageStep<T, B, NT>(a, ts, l, next, staged, true, v0, a.p, a.r, nv, ps);
+        if (probe) t1 = clock64();
+        const T* sT = ts.stT + bf * ts.regT;
+        const int* sI = ts.stI + bf * ts.regI;
+        const int shS = f.x & (E - 1), shA = (f.x * B) & (E - 1), shI = f.x & 3;
+        const bool act = u < f.y;
+        const int i = f.x + u;
+        T out[B];
+        int code[3] = {-1, -1, -1}, tg[3] = {-1, -1, -1};
+        if (act) {
+            const T* vs = sT + nS * capS + shA + u * B;
+            if (fuseP) {
+#pragma unroll
+                for (int e = 0; e < B; ++e) {
+                    T tmp = vs[e];
+                    tmp *= omega;
+                    tmp -= vs[capA + e];
+                    tmp *= -beta;
+                    T pe = vs[2 * capA + e];
+                    pe += tmp;
+                    a.p[i * B + e] = pe;  // the new direction p = r - beta (p - omega v)
+                    out[e] = pe;
+                }
+            }
+            else {
+#pragma unroll
+                for (int e = 0; e < B; ++e) out[e] = vs[e];
+            }
+#pragma unroll
+            for (int s = 0; s < 3; ++s) {
+                if (s >= dim) break;
+                code[s] = sI[s * capI + shI + u];
+                tg[s] = sI[(dim + s) * capI + shI + u];
+            }
+        }
+        // after a timeout: no more waits and no more pushes
+        if (f.z > 0 && ps.ok && !mbarWait(mb0 + 8u * l, par)) ps.ok = 0;
+        if (probe) t2 = clock64();
+        if (act) {
+            const T* prev = ts.loc + ((l + 1) & 1) * NT * PB;  // level l - 1
+            const T* fl = sT + shS + u;
+#pragma unroll
+            for (int s = 0; s < 3; ++s) {
+                if (s >= dim) break;
+                if (code[s] < 0) continue;
+                const T* md = tileDep<T, B>(code[s], prev, ts.halo, hcap, NT, ps);
+                if (!md) continue;
+                T m[B];
+#pragma unroll
+                for (int c = 0; c < B; ++c) m[c] = md[c];
+#pragma unroll
+                for (int r = 0; r < B; ++r)
+#pragma unroll
+                    for (int c = 0; c < B; ++c) out[r] -= fl[(s * BB + r * B + c) * capS] * m[c];
+            }
+            T* mine = ts.loc + (l & 1) * NT * PB + u * PB;
+#pragma unroll
+            for (int e = 0; e < B; ++e) mine[e] = out[e];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                if (q >= dim) break;
+                if (tg[q] >= 0 && ps.ok && l + 1 < nl)
+                    tilePush<T, B>(tg[q], out, mb0 + 8u * (l + 1), halo0, tm, hcap, ps);
+            }
+#pragma unroll
+            for (int e = 0; e < B; ++e) y[i * B + e] = out[e];
+        }
+        if (probe) t3 = clock64();
+        __syncthreads();
+        if (probe) {
+            const unsigned long long t4 = clock64();
+            cyc[0] += t1 - t0;
+            cyc[1] += t2 - t1;
+            cyc[2] += t3 - t2;
+            cyc[3] += t4 - t3;
+            nprobe++;
+        }
+    }
+    if (probe) {
+        for (int j = 0; j < 4; ++j) a.prof[8 + j] += cyc[j];
+        a.prof[12] += nprobe;
+    }
+    tileSweepEnd<T, B, NT>(ts, ps);
+}
+
+// backward sweep in place: y = D^-1 (y - U y)
+template <class T, int B, int NT>
+__device__ __forceinline__ void sweepUpperTile(const KArgs<T>& a, T* y, const Team<SYNC_CLUSTER>& tm,
+                                               const TileSmem<T, B, NT>& ts, PushState& ps)
+{
+    constexpr int BB = B * B, PB = padB(B), E = TileSmem<T, B, NT>::E;
+    const int dim = a.dim, nl = a.numLev, u = threadIdx.x, hcap = a.thalo;
+    const int capS = ts.capS, capI = ts.capI, nS = (dim + 1) * BB;
+    const unsigned mb0 = smemAddr(ts.mb), halo0 = smemAddr(ts.halo);
+    const unsigned par = ps.tph;
+    if (ps.ok)
+        for (int l = u; l < nl; l += NT) mbarArriveTx(mb0 + 8u * l, (unsigned)(ts.info[l].w * PB * sizeof(T)));
+    int staged = -1;
+    for (int l = nl - 1; l >= 0; --l) {
+        const int4 f = ts.info[l];
+        if (f.y == 0) continue;
+        const int next = l > 0 && ts.info[l - 1].y > 0 ? l - 1 : -1;
+        const int bf = tileStageStep<T, B, NT>(a, ts, l, next, staged, false, y, nullptr, nullptr, 1, ps);
+        const T* sT = ts.stT + bf * ts.regT;
+        const int* sI = ts.stI + bf * ts.regI;
+        const int shS = f.x & (E - 1), shA = (f.x * B) & (E - 1), shI = f.x & 3;
+        const bool act = u < f.y;
+        const int i = f.x + u;
+        T acc[B];
+        int code[3] = {-1, -1, -1}, tg[3] = {-1, -1, -1};
+        if (act) {
+#pragma unroll
+            for (int e = 0; e < B; ++e) acc[e] = sT[nS * capS + shA + u * B + e];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                if (q >= dim) break;
+                code[q] = sI[q * capI + shI + u];
+                tg[q] = sI[(dim + q) * capI + shI + u];
+            }
+        }
+        if (f.w > 0 && ps.ok && !mbarWait(mb0 + 8u * l, par)) ps.ok = 0;
+        if (act) {
+            const T* prev = ts.loc + ((l + 1) & 1) * NT * PB;  // level l + 1
+            const T* au = sT + shS + u;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                if (q >= dim) break;
+                if (code[q] < 0) continue;
+                const T* md = tileDep<T, B>(code[q], prev, ts.halo, hcap, NT, ps);
+                if (!md) continue;
+                T m[B];
+#pragma unroll
+                for (int c = 0; c < B; ++c) m[c] = md[c];
+#pragma unroll
+                for (int r = 0; r < B; ++r)
+#pragma unroll
+                    for (int c = 0; c < B; ++c) acc[r] -= au[(q * BB + r * B + c) * capS] * m[c];
+            }
+            const T* fd = au + dim * BB * capS;
+            T out[B];
+#pragma unroll
+            for (int r = 0; r < B; ++r) {
+                T t = T(0);
+#pragma unroll
+                for (int c = 0; c < B; ++c) t += fd[(r * B + c) * capS] * acc[c];
+                out[r] = t;
+            }
+            T* mine = ts.loc + (l & 1) * NT * PB + u * PB;
+#pragma unroll
+            for (int e = 0; e < B; ++e) mine[e] = out[e];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                if (q >= dim) break;
+                if (tg[q] >= 0 && ps.ok && l > 0)
+                    tilePush<T, B>(tg[q], out, mb0 + 8u * (l - 1), halo0, tm, hcap, ps);
+            }
+#pragma unroll
+            for (int e = 0; e < B; ++e) y[i * B + e] = out[e];
+        }
+        __syncthreads();
+    }
+    tileSweepEnd<T, B, NT>(ts, ps);
+}
+
 template <class T, int B>
 __device__ __forceinline__ void spmvRow(const KArgs<T>& a, const T* in, int i, T (&acc)[B])
 {
@@ -913,7 +1304,10 @@ __device__ __forceinline__ void bicgstabBody(const KArgs<T>& a, const Team<MODE>
     PushState ps;
     ps.ok = 1;
     const PushSmem<T, B, NT> psm(dynSmem, a.numLev);
+    const TileSmem<T, B, NT> tsm(dynSmem, a.numLev, a.thalo, a.twidth, a.dim);  // the same memory, tile layout
     T* const dep = psm.dep;
+    ps.tph = 0;
+    ps.sbuf = 0;
     // hybrid launch (grid of clusters): cluster 0 factorizes and sweeps, every
     // block of the grid shares SpMV, vector updates and reductions
     const bool sweeper = MODE == SYNC_CLUSTER || (a.hybrid && blockIdx.x < a.hybrid);
@@ -922,7 +1316,8 @@ __device__ __forceinline__ void bicgstabBody(const KArgs<T>& a, const Team<MODE>
         const int crank = (int)cl.block_rank(), csize = (int)cl.num_blocks();
         // the push tables and the hybrid split assume one cluster size; a launch
         // with another (the same in every block) reports an error and does nothing
-        if ((a.dsmem && csize != a.cluster) || (a.hybrid && (csize != a.hybrid || csize != a.gs.perCluster))) {
+        if (((a.dsmem || a.tile) && csize != a.cluster) ||
+            (a.hybrid && (csize != a.hybrid || csize != a.gs.perCluster))) {
             if (crank == 0 && threadIdx.x == 0) a.st->code = GBFV_ERR_CUDA;
             return;
         }
@@ -941,6 +1336,17 @@ __device__ __forceinline__ void bicgstabBody(const KArgs<T>& a, const Team<MODE>
             // one arrival per phase (thread 0, carrying the expected bytes)
             for (int k = 0; k < PUSH_BUFFERS; ++k) mbarInit(ps.mb[k], 1);
             mbarInit(ps.lev, csize);
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        if (a.tile && sweeper) {
+            // this block's per-level table and one halo mbarrier per level
+            for (int j = threadIdx.x; j < a.numLev; j += NT) {
+                tsm.info[j] = a.tinfo[crank * a.numLev + j];
+                mbarInit(smemAddr(&tsm.mb[j]), 1);
+            }
+            if (threadIdx.x == 0) {
+                *tsm.bad = 0;
+            }
             asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         }
         cl.sync();
@@ -1017,7 +1423,13 @@ __device__ __forceinline__ void bicgstabBody(const KArgs<T>& a, const Team<MODE>
             rho = rho_i;
             pc.tick(5);
             if constexpr (MODE == SYNC_CLUSTER) {
-                if (a.dsmem) {
+                if (a.tile) {
+                    sweepLowerTile<T, B, NT>(a, nullptr, a.y, true, (T)beta, (T)omega, tm, tsm, ps);
+                    pc.tick(1);
+                    sweepUpperTile<T, B, NT>(a, a.y, tm, tsm, ps);
+                    pc.tick(2);
+                }
+                else if (a.dsmem) {
                     sweepLowerPush<T, B, NT>(a, nullptr, a.y, true, (T)beta, (T)omega, tm, dep, ps, psm);
                     pc.tick(1);
                     sweepUpperPush<T, B, NT>(a, a.y, tm, dep, ps, psm);
@@ -1031,8 +1443,14 @@ __device__ __forceinline__ void bicgstabBody(const KArgs<T>& a, const Team<MODE>
             else if (a.hybrid) {
                 if (sweeper) {
                     const Team<SYNC_CLUSTER> tc;
-                    sweepLowerPush<T, B, NT>(a, nullptr, a.y, true, (T)beta, (T)omega, tc, dep, ps, psm);
-                    sweepUpperPush<T, B, NT>(a, a.y, tc, dep, ps, psm);
+                    if (a.tile) {
+                        sweepLowerTile<T, B, NT>(a, nullptr, a.y, true, (T)beta, (T)omega, tc, tsm, ps);
+                        sweepUpperTile<T, B, NT>(a, a.y, tc, tsm, ps);
+                    }
+                    else {
+                        sweepLowerPush<T, B, NT>(a, nullptr, a.y, true, (T)beta, (T)omega, tc, dep, ps, psm);
+                        sweepUpperPush<T, B, NT>(a, a.y, tc, dep, ps, psm);
+                    }
                 }
                 if (!teamSync<MODE>(a.gs)) goto timeout;
             }
@@ -1104,7 +1522,13 @@ __device__ __forceinline__ void bicgstabBody(const KArgs<T>& a, const Team<MODE>
             }
             pc.tick(4);
             if constexpr (MODE == SYNC_CLUSTER) {
-                if (a.dsmem) {
+                if (a.tile) {
+                    sweepLowerTile<T, B, NT>(a, a.r, a.z, false, T(0), T(0), tm, tsm, ps);
+                    pc.tick(1);
+                    sweepUpperTile<T, B, NT>(a, a.z, tm, tsm, ps);
+                    pc.tick(2);
+                }
+                else if (a.dsmem) {
                     sweepLowerPush<T, B, NT>(a, a.r, a.z, false, T(0), T(0), tm, dep, ps, psm);
                     pc.tick(1);
                     sweepUpperPush<T, B, NT>(a, a.z, tm, dep, ps, psm);
@@ -1118,8 +1542,14 @@ __device__ __forceinline__ void bicgstabBody(const KArgs<T>& a, const Team<MODE>
             else if (a.hybrid) {
                 if (sweeper) {
                     const Team<SYNC_CLUSTER> tc;
-                    sweepLowerPush<T, B, NT>(a, a.r, a.z, false, T(0), T(0), tc, dep, ps, psm);
-                    sweepUpperPush<T, B, NT>(a, a.z, tc, dep, ps, psm);
+                    if (a.tile) {
+                        sweepLowerTile<T, B, NT>(a, a.r, a.z, false, T(0), T(0), tc, tsm, ps);
+                        sweepUpperTile<T, B, NT>(a, a.z, tc, tsm, ps);
+                    }
+                    else {
+                        sweepLowerPush<T, B, NT>(a, a.r, a.z, false, T(0), T(0), tc, dep, ps, psm);
+                        sweepUpperPush<T, B, NT>(a, a.z, tc, dep, ps, psm);
+                    }
                 }
                 if (!teamSync<MODE>(a.gs)) goto timeout;
             }
@@ -1281,7 +1711,9 @@ static int launchOne(const KArgs<T>& a, int nblocks, cudaStream_t s)
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(nblocks, 1, 1);
         cfg.blockDim = dim3(NT, 1, 1);
-        cfg.dynamicSmemBytes = a.dsmem ? PushSmem<T, B, NT>::bytes(a.numLev) : 0;
+        cfg.dynamicSmemBytes = a.tile    ? TileSmem<T, B, NT>::bytes(a.numLev, a.thalo, a.twidth, a.dim)
+                               : a.dsmem ? PushSmem<T, B, NT>::bytes(a.numLev)
+                                         : 0;
         cfg.stream = s;
         cudaLaunchAttribute at[1];
         at[0].id = cudaLaunchAttributeClusterDimension;
@@ -1313,7 +1745,9 @@ static int launchHybrid(const KArgs<T>& a, int nblocks, cudaStream_t s)
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(nblocks, 1, 1);
     cfg.blockDim = dim3(NT, 1, 1);
-    cfg.dynamicSmemBytes = a.dsmem ? PushSmem<T, B, NT>::bytes(a.numLev) : 0;
+    cfg.dynamicSmemBytes = a.tile    ? TileSmem<T, B, NT>::bytes(a.numLev, a.thalo, a.twidth, a.dim)
+                           : a.dsmem ? PushSmem<T, B, NT>::bytes(a.numLev)
+                                     : 0;
     cfg.stream = s;
     cudaLaunchAttribute at[2];
     at[0].id = cudaLaunchAttributeClusterDimension;
@@ -1478,6 +1912,25 @@ int maxClusterBlocks(int b)
     return n > 0 ? n : 1;
 }
 
+template <class T>
+size_t tileSmemBytes(int b, int numLev, int haloSlots, int width, int dim)
+{
+    constexpr int NT = clusterThreads<T>();
+    return b == 2 ? TileSmem<T, 2, NT>::bytes(numLev, haloSlots, width, dim)
+                  : TileSmem<T, 3, NT>::bytes(numLev, haloSlots, width, dim);
+}
+
+template <class T>
+size_t solverSmemLimit(int b)
+{
+    constexpr int NT = clusterThreads<T>();
+    return b == 2 ? PushSmem<T, 2, NT>::bytes(MAX_PUSH_LEVELS) : PushSmem<T, 3, NT>::bytes(MAX_PUSH_LEVELS);
+}
+
+template size_t tileSmemBytes<double>(int, int, int, int, int);
+template size_t tileSmemBytes<float>(int, int, int, int, int);
+template size_t solverSmemLimit<double>(int);
+template size_t solverSmemLimit<float>(int);
 template int launchBicgstab<double>(const KArgs<double>&, int, int, int, cudaStream_t);
 template int launchBicgstab<float>(const KArgs<float>&, int, int, int, cudaStream_t);
 template int maxSolverBlocks<double>(int);

@@ -18,6 +18,14 @@ constexpr int SYNC_GRID = 0;     // whole grid, cooperative launch, software bar
 constexpr int SYNC_CLUSTER = 1;  // one thread-block cluster, hardware barrier
 constexpr int SYNC_HYBRID = 2;   // launch mode: clusters over the whole GPU, cluster 0 sweeps, all share the rest
 constexpr int HYBRID_CLUSTER = 16;  // cluster size of the hybrid launch
+// Spatial-tile sweeps (a flag or-ed into the cluster and hybrid modes): the
+// rows of every level are dealt to the sweeping cluster's blocks by the
+// spatial tile of their cell, so most dependencies stay inside a block.
+constexpr int SYNC_TILES = 4;
+constexpr int TILE_KEYS = 16;           // tiles the rows are ordered by (4 x 4)
+constexpr int TILE_MAX_LEVELS = 1024;   // tile sweeps keep per-level data in shared memory
+constexpr int TILE_HALO = 1 << 30;      // dependency code: a value pushed by another block (halo slot)
+constexpr int TILE_MASK = (1 << 24) - 1;
 
 // software grid barrier state (device memory, zero-initialised)
 struct GridSync {
@@ -56,9 +64,20 @@ struct KArgs {
     int dsmem;          // cluster mode: every level fits one row per thread, so the
                         // previous level's results are exchanged in distributed shared memory
     int cluster;        // push sweeps: the cluster size the push tables were built for
+    int tile;           // spatial-tile sweeps (instead of the push sweeps)
+    const int4* tinfo;  // tile sweeps: [r*numLev + l] first row, rows, forward / backward halo slots
+    const int* tdepF;   // tile sweeps: [q*ldN + p] row p's dependency q: -1 none, a position in the
+    const int* tdepB;   //   block's previous level, or TILE_HALO | halo slot
+    const int* tpushF;  // tile sweeps: [t*ldN + p] (consumer block << 24) | halo slot, or -1
+    const int* tpushB;
+    int thalo;          // tile sweeps: halo slots per block
+    int twidth;         // tile sweeps: the most rows a block computes in one level
 };
 
 template <class T> int launchBicgstab(const KArgs<T>& a, int b, int mode, int nblocks, cudaStream_t s);
+// dynamic shared memory of the tile sweeps, and the most a solve launch may use
+template <class T> size_t tileSmemBytes(int b, int numLev, int haloSlots, int width, int dim);
+template <class T> size_t solverSmemLimit(int b);
 
 // One system of a batched mixed-precision refinement (FP64 true residual of
 // the Newton system, FP32 inner solve)

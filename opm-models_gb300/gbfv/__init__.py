@@ -144,11 +144,16 @@ class Context:
         mode, nb, nt = C.c_int(), C.c_int(), C.c_int()
         ms = np.zeros(16)
         self.lib.gbfv_solver_config(self.h, precision, C.byref(mode), C.byref(nb), _d(ms), C.byref(nt))
-        return {"mode": {0: "grid", 1: "cluster", 2: "hybrid"}.get(mode.value, "?"), "blocks": nb.value,
+        name = {0: "grid", 1: "cluster", 2: "hybrid"}.get(mode.value & 3, "?")
+        if mode.value & capi.SOLVER_TILES:
+            name += "+tiles"
+        return {"mode": name, "blocks": nb.value,
                 "tune_ms": ms[:nt.value].tolist()}
 
     def set_solver_config(self, precision, mode, blocks):
-        """Fix the persistent solver's launch configuration (mode 1 = cluster)."""
+        """Fix the persistent solver's launch configuration (mode 0 = grid,
+        1 = cluster, 2 = hybrid; or-ed with capi.SOLVER_TILES: spatial-tile
+        sweeps)."""
         capi.check(self.lib.gbfv_set_solver_config(self.h, precision, mode, blocks), "gbfv_set_solver_config")
 
     def reset_kernel_stats(self):

@@ -45,6 +45,12 @@ GAS_RS = 1
 GAS_RV = 2
 PREC_FP64 = 0
 PREC_MIXED = 1
+
+# persistent solver launch modes (gbfv_set_solver_config)
+SOLVER_GRID = 0
+SOLVER_CLUSTER = 1
+SOLVER_HYBRID = 2
+SOLVER_TILES = 4   # or-ed into SOLVER_CLUSTER / SOLVER_HYBRID: spatial-tile sweeps
 FLUX_DARCY = 0
 FLUX_TRANS = 1
 MAT_STRIDE = 8

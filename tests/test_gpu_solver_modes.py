@@ -1,0 +1,87 @@
+"""GPU checks of the persistent solver's launch modes: the spatial-tile
+sweeps (rows of every ILU level dealt to the cluster's blocks by the tile of
+their cell, dependencies across tiles pushed into halo slots) give the same
+result as the push sweeps with the same cluster, and agree with the CPU
+oracle in FP64, alone and in the hybrid launch."""
+import numpy as np
+import pytest
+
+import oracle as O
+from gbfv import Context, capi, problems
+from parity import rel_state_diff
+
+pytestmark = pytest.mark.gpu
+
+TILES = capi.SOLVER_TILES
+
+
+def _run(prob, prm, prec, mode, blocks, steps, dt):
+    ctx = Context(prob, prm)
+    ctx.set_solver_config(prec, mode, blocks)
+    st, sdt, sn, sl, _ = ctx.time_integration(steps, dt, fixed_dt=True)
+    x, m = ctx.solution()
+    cfg = ctx.solver_config(prec)
+    ctx.close()
+    return st, sn, sl, x, m, cfg
+
+
+@pytest.mark.parametrize("shape", [(32, 28, 6), (9, 7, 3)])
+def test_tile_sweeps_equal_push_sweeps(built, shape):
+    prob = problems.blackoil(*shape, seed=5)
+    prm = capi.default_params(linear_tolerance=1e-6, newton_tolerance=1e-6, precision=capi.PREC_MIXED,
+                              inner_tolerance=1e-5)
+    a = _run(prob, prm, capi.PREC_MIXED, capi.SOLVER_CLUSTER, 16, 3, 86400.0)
+    b = _run(prob, prm, capi.PREC_MIXED, capi.SOLVER_CLUSTER | TILES, 16, 3, 86400.0)
+    assert a[0] == 0 and b[0] == 0
+    assert b[5]["mode"] == "cluster+tiles" and b[5]["blocks"] == 16
+    # the same arithmetic per row, the same reductions: the same iterates
+    assert np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2]), (a[1], b[1], a[2], b[2])
+    assert np.array_equal(a[3], b[3]) and np.array_equal(a[4], b[4])
+
+
+def test_tile_sweeps_lens_fp64_match_oracle(built):
+    prob = problems.lens()
+    prm = capi.default_params(linear_tolerance=1e-6)
+    orc = O.Oracle(prob, prm)
+    so, dto, no, lo, tlo = orc.time_integration(30, 250.0)
+    ctx = Context(prob, prm)
+    ctx.set_solver_config(capi.PREC_FP64, capi.SOLVER_CLUSTER | TILES, 16)
+    sg, dtg, ng, lg, tlg = ctx.time_integration(30, 250.0)
+    assert so == 0 and sg == 0
+    assert np.array_equal(no, ng), (no, ng)
+    assert np.allclose(dto, dtg, rtol=1e-12, atol=0)
+    assert rel_state_diff(ctx.solution()[0], orc.solution()[0], 2) <= 1e-8
+
+
+@pytest.mark.parametrize("mode,blocks", [(capi.SOLVER_CLUSTER | TILES, 16), (capi.SOLVER_HYBRID | TILES, 32)])
+def test_tile_sweeps_blackoil_fp64_match_oracle(built, mode, blocks):
+    prob = problems.blackoil(24, 20, 6)
+    prm = capi.default_params(linear_tolerance=1e-6, newton_tolerance=1e-6)
+    orc = O.Oracle(prob, prm)
+    so, _, no, _, _ = orc.time_integration(4, 86400.0, fixed_dt=True)
+    sg, ng, lg, x, m, cfg = _run(prob, prm, capi.PREC_FP64, mode, blocks, 4, 86400.0)
+    assert so == 0 and sg == 0
+    assert cfg["mode"].endswith("+tiles")
+    assert np.array_equal(no, ng), (no, ng)
+    pvo, mo = orc.solution()
+    assert np.array_equal(mo, m)
+    assert rel_state_diff(x, pvo, 3) <= 1e-8
+
+
+def test_hybrid_tiles_mixed_equal_alone_runs(built):
+    """Two contexts with the same hybrid+tiles configuration give the same
+    bits (the pipeline's timing does not enter the arithmetic)."""
+    prob = problems.blackoil(40, 36, 8, seed=9)
+    prm = capi.default_params(linear_tolerance=1e-6, newton_tolerance=1e-6, precision=capi.PREC_MIXED,
+                              inner_tolerance=1e-5)
+    a = _run(prob, prm, capi.PREC_MIXED, capi.SOLVER_HYBRID | TILES, 32, 2, 86400.0)
+    b = _run(prob, prm, capi.PREC_MIXED, capi.SOLVER_HYBRID | TILES, 32, 2, 86400.0)
+    assert a[0] == 0 and b[0] == 0
+    assert np.array_equal(a[2], b[2]) and np.array_equal(a[3], b[3])
+
+
+def test_tile_flag_needs_a_cluster_mode(built):
+    ctx = Context(problems.blackoil(8, 8, 3), capi.default_params())
+    with pytest.raises(Exception):
+        ctx.set_solver_config(capi.PREC_FP64, capi.SOLVER_GRID | TILES, 16)
+    ctx.close()
