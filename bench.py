@@ -301,6 +301,23 @@ def run_ours(args):
         out_pv[:], out_m[:] = ctx.solution()
         e2e_s += time.perf_counter() - t0
         e2e_cits += int(sn.sum()) * N
+    # restart file of the final state (the reference's Simulator::serialize
+    # layout), written and read back outside the timed regions
+    restart_line = None
+    if rank == 0:
+        import tempfile
+        from gbfv import restart
+        edges, verts = restart.cartesian_counts((w["nx"], w["ny"], w["nz"]))
+        inf = restart.info(edges, verts, time=w["steps"] * w["dt"], time_step_index=w["steps"])
+        with tempfile.TemporaryDirectory() as td:
+            path = os.path.join(td, restart.restart_file_name(".", "gbfv", inf.time))
+            t0 = time.perf_counter()
+            ctx.write_restart(path, inf)
+            t1 = time.perf_counter()
+            ctx.read_restart(path, inf)
+            t2 = time.perf_counter()
+            restart_line = {"cells": N, "bytes": os.path.getsize(path), "write_ms": (t1 - t0) * 1e3,
+                            "read_ms": (t2 - t1) * 1e3, "threads": min(16, os.cpu_count() or 1)}
     if world > 1:
         t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -363,6 +380,7 @@ def run_ours(args):
         "solver_config": {"mixed": mixed["cfg"], "fp64": plain["cfg"]},
         "linearize_roofline": {"achieved": lin_ach, "frac": lin_ach / peak, "ms": kst["linearize_ms"] / args.steps},
         "clocks": mixed["clocks"],
+        "restart": restart_line,
     }
     if world == 1 and not args.no_cpu_baseline:
         v, dt, threads = cpu_sample(prob)

@@ -439,6 +439,52 @@ int gbfv_serve_release(gbfv_batch* server, int slot);
 int64_t gbfv_serve_footprint(const gbfv_batch* server);
 
 /* ------------------------------------------------------------------ */
+/* Restart files in the reference's text format (Opm::Restart,
+ * opm/models/io/restart.hh:101-265, written by Simulator::serialize,
+ * simulator.hh:906-962): the magic cookie (restart.hh:57-75), the
+ * "Simulator" section (simulator.hh:930-943), the problem's
+ * "VTKMultiWriter" section when it writes VTK output (fvbaseproblem.hh:
+ * 755-760, vtkmultiwriter.hh:408-437; no .pvd meta file here: length and
+ * position 0) and the ECFV "Entities: Codim 0" section, one line per cell
+ * in natural order (ecfvdiscretization.hh:212-226): the primary variables
+ * (fvbasediscretization.hh:1440-1454), for black-oil followed by the gas,
+ * water and pressure meanings and the PVT region (blackoilmodel.hh:
+ * 468-493).  Floating point as "%.20g" (the stream's precision(20)).      */
+typedef struct gbfv_restart_info {
+    int32_t num_cpus;            /* gridView.comm().size() (cookie)          */
+    int32_t rank;                /* gridView.comm().rank() (cookie)          */
+    int32_t num_edges;           /* gridView.size(dim - 1) (cookie)          */
+    int32_t num_vertices;        /* gridView.size(dim) (cookie)              */
+    int32_t episode_index;       /* Simulator section                        */
+    int32_t time_step_index;
+    double episode_start_time;
+    double episode_length;
+    double start_time;
+    double time;
+    int32_t vtk_section;         /* 1: with the VTKMultiWriter section       */
+    int32_t vtk_writer_num;      /* its curWriterNum_                        */
+} gbfv_restart_info;
+/* the file's text for num_cells cells of b primary variables (natural
+ * order) and, for black-oil, their gas meanings (NULL: immiscible); *len =
+ * its size in bytes; buf NULL asks for the size only                      */
+int gbfv_format_restart(const gbfv_restart_info* info, int32_t num_cells, int32_t b, const double* pv,
+                        const int32_t* gas_meaning, char* buf, size_t cap, size_t* len);
+/* read a file's text back (Restart::deserialize*, restart.hh:166-265):
+ * `expect` gives the cookie's grid counts, out the Simulator section (and
+ * whether a VTK section was present); GBFV_ERR_ARG on any mismatch        */
+int gbfv_parse_restart(const char* text, size_t len, const gbfv_restart_info* expect, int32_t num_cells, int32_t b,
+                       double* pv, int32_t* gas_meaning, gbfv_restart_info* out);
+/* restartFileName_ (restart.hh:80-95): <dir/>sim_name_time=<t>_rank=<r>.ers */
+int gbfv_restart_file_name(const char* output_dir, const char* sim_name, double time, int32_t rank, char* buf,
+                           size_t cap);
+/* write the context's current solution to a restart file; read one back
+ * into the context (solution and its previous time level, as
+ * BlackOilModel::deserialize sets solution(1) = solution(0)); info: cookie
+ * counts in, Simulator section out                                        */
+int gbfv_write_restart(gbfv_ctx* ctx, const char* path, const gbfv_restart_info* info);
+int gbfv_read_restart(gbfv_ctx* ctx, const char* path, gbfv_restart_info* info);
+
+/* ------------------------------------------------------------------ */
 /* Self-test of the device-side wait bound (no counterpart in the
  * reference): one block waits, with the bounded wait of the solver's
  * sweeps, on a barrier phase that nothing completes.  Returns

@@ -145,11 +145,18 @@ int allocSolver(SolverData& S, int maxBlocksOverride = 0)
     S.maxCluster[0] = std::min(16, maxClusterBlocks<double>(S.b));
     S.maxCluster[1] = std::min(16, maxClusterBlocks<float>(S.b));
     // The hybrid launch (a cooperative grid of clusters) is left out under a
-    // profiler that injects itself into the process (CUDA_INJECTION64_PATH): a
+    // profiler that injects itself into the process (Nsight Compute sets
+    // NV_COMPUTE_PROFILER_PERFWORKS_DIR and NV_NSIGHT_INJECTION_TRANSPORT_TYPE
+    // in the profiled process; other tools CUDA_INJECTION64_PATH): a
     // kernel-replay capture of it ended in a device fault, while the same runs
     // without the profiler pass.  GBFV_NO_HYBRID leaves it out as well.
-    const char* inj = getenv("CUDA_INJECTION64_PATH");
-    const bool hybridOk = !getenv("GBFV_NO_HYBRID") && !(inj && *inj);
+    bool profiled = false;
+    for (const char* v : {"CUDA_INJECTION64_PATH", "NV_COMPUTE_PROFILER_PERFWORKS_DIR",
+                          "NV_NSIGHT_INJECTION_TRANSPORT_TYPE"}) {
+        const char* e = getenv(v);
+        if (e && *e) profiled = true;
+    }
+    const bool hybridOk = !getenv("GBFV_NO_HYBRID") && !profiled;
     S.maxHybrid[0] = hybridOk && S.maxCluster[0] >= HYBRID_CLUSTER ? maxHybridBlocks<double>(S.b) : 0;
     S.maxHybrid[1] = hybridOk && S.maxCluster[1] >= HYBRID_CLUSTER ? maxHybridBlocks<float>(S.b) : 0;
     // default before tuning: one block for small systems, else a cluster of 8

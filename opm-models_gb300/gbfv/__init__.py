@@ -76,6 +76,16 @@ class Context:
         capi.check(self.lib.gbfv_get_solution(self.h, _d(pv), _i(m)), "gbfv_get_solution")
         return pv, m
 
+    # Simulator::serialize / deserialize (restart files, gbfv.restart)
+    def write_restart(self, path, info):
+        capi.check(self.lib.gbfv_write_restart(self.h, path.encode(), C.byref(info)), "gbfv_write_restart")
+
+    def read_restart(self, path, info):
+        """Read the solution from a restart file; returns its Simulator section."""
+        out = capi.RestartInfo.from_buffer_copy(info)
+        capi.check(self.lib.gbfv_read_restart(self.h, path.encode(), C.byref(out)), "gbfv_read_restart")
+        return out
+
     # FvBaseLinearizer
     def linearize(self, dt, newton_iter=0):
         self.lib.gbfv_set_timestep(self.h, dt)

@@ -164,6 +164,15 @@ class BatchStats(C.Structure):
                 ("solve_bytes", C.c_double), ("linearize_ms", C.c_double)]
 
 
+class RestartInfo(C.Structure):
+    """gbfv_restart_info: the restart file's cookie counts and Simulator section."""
+    _fields_ = [("num_cpus", C.c_int32), ("rank", C.c_int32), ("num_edges", C.c_int32),
+                ("num_vertices", C.c_int32), ("episode_index", C.c_int32), ("time_step_index", C.c_int32),
+                ("episode_start_time", C.c_double), ("episode_length", C.c_double),
+                ("start_time", C.c_double), ("time", C.c_double), ("vtk_section", C.c_int32),
+                ("vtk_writer_num", C.c_int32)]
+
+
 _LIB = None
 
 
@@ -234,6 +243,14 @@ def load():
         "gbfv_serve_release": (C.c_int, [vp, C.c_int]),
         "gbfv_serve_footprint": (C.c_int64, [vp]),
         "gbfv_selftest_wait_timeout": (C.c_int, [dp]),
+        "gbfv_format_restart": (C.c_int, [C.POINTER(RestartInfo), C.c_int32, C.c_int32, dp, ip, C.c_char_p,
+                                          C.c_size_t, C.POINTER(C.c_size_t)]),
+        "gbfv_parse_restart": (C.c_int, [C.c_char_p, C.c_size_t, C.POINTER(RestartInfo), C.c_int32, C.c_int32,
+                                         dp, ip, C.POINTER(RestartInfo)]),
+        "gbfv_restart_file_name": (C.c_int, [C.c_char_p, C.c_char_p, C.c_double, C.c_int32, C.c_char_p,
+                                             C.c_size_t]),
+        "gbfv_write_restart": (C.c_int, [vp, C.c_char_p, C.POINTER(RestartInfo)]),
+        "gbfv_read_restart": (C.c_int, [vp, C.c_char_p, C.POINTER(RestartInfo)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
