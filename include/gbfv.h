@@ -186,7 +186,20 @@ typedef struct gbfv_params {
     double min_time_step;             /* MinTimeStepSize            0       */
     double max_time_step;             /* MaxTimeStepSize            inf     */
     int32_t max_time_step_divisions;  /* MaxTimeStepDivisions       10      */
+    int32_t local_linearizer;         /* LocalLinearizerSplice: enum gbfv_local_linearizer */
+    int32_t numeric_difference_method;/* NumericDifferenceMethod (FD)  +1     */
 } gbfv_params;
+
+/* local linearizer (Properties::LocalLinearizerSplice): automatic
+ * differentiation (FvBaseAdLocalLinearizer, the default) or finite
+ * differences (FvBaseFdLocalLinearizer, fvbasefdlocallinearizer.hh:
+ * 135-523: one cell's primary variable perturbed by BaseEpsilon /
+ * primaryVarWeight at a time; numeric_difference_method +1 forward,
+ * 0 central, -1 backward differences)                                     */
+enum gbfv_local_linearizer {
+    GBFV_LIN_AD = 0,
+    GBFV_LIN_FD = 1
+};
 
 /* fill *p with the reference's defaults */
 void gbfv_default_params(gbfv_params* p);

@@ -259,6 +259,11 @@ struct gbfv_ctx {
     double *x = nullptr, *xOld = nullptr, *storageOld = nullptr, *residual = nullptr, *jval = nullptr;
     int *meaning = nullptr, *meaningOld = nullptr, *wasSwitched = nullptr;
     IqBuffers iq{};
+    // finite-difference linearizer (allocated on first use): deflected
+    // states and their intensive quantities; the reference pressure
+    FdIq fd{};
+    double* fdX[6] = {};
+    double* refP = nullptr;
     double* dx = nullptr;
     SolverData S;
     DevStatus* st = nullptr;
@@ -937,6 +942,8 @@ void gbfv_default_params(gbfv_params* p)
     p->min_time_step = 0.0;
     p->max_time_step = std::numeric_limits<double>::infinity();
     p->max_time_step_divisions = 10;
+    p->local_linearizer = GBFV_LIN_AD;
+    p->numeric_difference_method = 1;
 }
 
 int64_t gbfv_kernel_launches(void) { return g_launches.load(); }
@@ -1391,6 +1398,11 @@ static int createImpl(gbfv_ctx* C, const gbfv_problem* P)
         return st;
     CK(cudaMemset(C->meaning, 0, sizeof(int) * N));
     CK(cudaMemset(C->meaningOld, 0, sizeof(int) * N));
+    if ((st = devAlloc(&C->refP, 1))) return st;
+    {
+        const double one = 1.0;
+        CK(cudaMemcpy(C->refP, &one, sizeof(double), cudaMemcpyHostToDevice));
+    }
     CK(cudaMemset(C->wasSwitched, 0, sizeof(int) * N));
     CK(cudaMemset(C->x, 0, sizeof(double) * nb));
     CK(cudaMemset(C->xOld, 0, sizeof(double) * nb));
@@ -1438,11 +1450,23 @@ static int createImpl(gbfv_ctx* C, const gbfv_problem* P)
     return GBFV_OK;
 }
 
+// the local linearizer settings are one of the supported ones
+static bool linearizerOk(const gbfv_params& p)
+{
+    return (p.local_linearizer == GBFV_LIN_AD || p.local_linearizer == GBFV_LIN_FD) &&
+           p.numeric_difference_method >= -1 && p.numeric_difference_method <= 1;
+}
+
 gbfv_ctx* gbfv_create(const gbfv_problem* prob, const gbfv_params* params, int* status)
 {
     gbfv_ctx* C = new gbfv_ctx();
     if (params) C->prm = *params;
     else gbfv_default_params(&C->prm);
+    if (!linearizerOk(C->prm)) {
+        if (status) *status = GBFV_ERR_ARG;
+        delete C;
+        return nullptr;
+    }
     int st = GBFV_ERR_ARG;
     try {
         st = prob ? createImpl(C, prob) : GBFV_ERR_ARG;
@@ -1474,6 +1498,14 @@ int gbfv_destroy(gbfv_ctx* C)
     cudaFree(C->iq.val);
     cudaFree(C->iq.der);
     cudaFree(C->iq.sto);
+    for (int k = 0; k < 3; ++k)
+        for (IqBuffers* q : {&C->fd.plus[k], &C->fd.minus[k]}) {
+            cudaFree(q->val);
+            cudaFree(q->der);
+            cudaFree(q->sto);
+        }
+    for (double* p : C->fdX) cudaFree(p);
+    cudaFree(C->refP);
     cudaFree(C->jval);
     freeSolver(C->S);
     cudaFree(C->st);
@@ -1493,7 +1525,7 @@ int gbfv_destroy(gbfv_ctx* C)
 
 int gbfv_set_params(gbfv_ctx* C, const gbfv_params* p)
 {
-    if (!C || !p) return GBFV_ERR_ARG;
+    if (!C || !p || !linearizerOk(*p)) return GBFV_ERR_ARG;
     C->prm = *p;
     return GBFV_OK;
 }
@@ -1521,6 +1553,8 @@ int gbfv_set_solution(gbfv_ctx* C, const double* pv, const int32_t* meaning)
         for (int I = 0; I < N; ++I) hm[C->perm[I]] = meaning[I];
     CK(cudaMemcpy(C->meaning, hm.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(C->meaningOld, hm.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
+    launchSetRefPressure(C->x, C->perm[0] * b, C->refP, C->stream);
+    CK(cudaStreamSynchronize(C->stream));
     return GBFV_OK;
 }
 
@@ -1567,10 +1601,53 @@ static void collectLinStats(gbfv_ctx* C)
     C->linPending = 0;
 }
 
+// buffers of the finite-difference linearizer (once per context)
+static int ensureFd(gbfv_ctx* C)
+{
+    if (C->fdX[0]) return GBFV_OK;
+    const int b = C->b;
+    const size_t ld = C->ldN, nv = b == 2 ? 6 : 11, nd = b == 2 ? 12 : 30, ns = (size_t)b * (b + 1);
+    int st;
+    for (int k = 0; k < b; ++k)
+        for (IqBuffers* q : {&C->fd.plus[k], &C->fd.minus[k]})
+            if ((st = devAlloc(&q->val, nv * ld)) || (st = devAlloc(&q->der, nd * ld)) ||
+                (st = devAlloc(&q->sto, ns * ld)))
+                return st;
+    for (int k = 0; k < 2 * b; ++k)
+        if ((st = devAlloc(&C->fdX[k], (size_t)C->N * b))) return st;
+    return GBFV_OK;
+}
+
 static int linearizeImpl(gbfv_ctx* C)
 {
     collectLinStats(C);
     launchApplyConstraints(C->mesh, C->x, C->xOld, C->meaning, C->meaningOld, C->stream);
+    if (C->prm.local_linearizer == GBFV_LIN_FD) {
+        // FvBaseFdLocalLinearizer: the unperturbed intensive quantities, those
+        // of the deflected states, then every element's columns
+        int st = ensureFd(C);
+        if (st) return st;
+        const int method = C->prm.numeric_difference_method, b = C->b;
+        cudaEventRecord(C->evL0, C->stream);
+        launchIq(C->mesh, C->dphys, C->x, C->meaning, C->iq, C->stream);
+        for (int pv = 0; pv < b; ++pv) {
+            if (method >= 0) {
+                launchFdDeflect(C->mesh, b, C->x, C->meaning, C->refP, pv, 1, C->fdX[pv], C->stream);
+                launchIq(C->mesh, C->dphys, C->fdX[pv], C->meaning, C->fd.plus[pv], C->stream);
+            }
+            if (method <= 0) {
+                launchFdDeflect(C->mesh, b, C->x, C->meaning, C->refP, pv, method == 0 ? 0 : -1, C->fdX[b + pv],
+                                C->stream);
+                launchIq(C->mesh, C->dphys, C->fdX[b + pv], C->meaning, C->fd.minus[pv], C->stream);
+            }
+        }
+        launchAssembleFd(C->mesh, C->dphys, C->iq, C->fd, C->meaning, C->refP, method, C->storageOld,
+                         C->newtonIter == 0, C->dt, C->residual, C->jval, C->stream);
+        cudaEventRecord(C->evL1, C->stream);
+        C->linPending = 1;
+        CK(cudaGetLastError());
+        return GBFV_OK;
+    }
     cudaEventRecord(C->evL0, C->stream);
     launchIq(C->mesh, C->dphys, C->x, C->meaning, C->iq, C->stream);
     launchAssemble(C->mesh, C->dphys, C->iq, C->storageOld, C->newtonIter == 0, C->dt, C->residual, C->jval,
@@ -1841,6 +1918,9 @@ int gbfv_newton_apply(gbfv_ctx* C, double dt, gbfv_newton_report* rep)
     C->numIterations = 0;
     C->error = 0;
     C->lastError = 0;
+    // FvBaseDiscretization::update -> updateBegin (the reference pressure of
+    // the finite-difference linearizer) before NewtonMethod::apply
+    if (C->prm.local_linearizer == GBFV_LIN_FD) launchSetRefPressure(C->x, C->perm[0] * C->b, C->refP, C->stream);
     const gbfv_params& prm = C->prm;
     auto converged = [&]() { return C->error <= prm.newton_tolerance; };
     auto proceed = [&]() {
@@ -2711,6 +2791,10 @@ gbfv_batch* gbfv_batch_create(const gbfv_problem* probs, int num_systems, const 
         return nullptr;
     };
     if (!probs || num_systems <= 0) return fail(nullptr, GBFV_ERR_ARG);
+    if (params && params->local_linearizer != GBFV_LIN_AD) {
+        setError("batched systems are linearized by automatic differentiation only");
+        return fail(nullptr, GBFV_ERR_UNSUPPORTED);
+    }
     gbfv_batch* B = new gbfv_batch();
     if (params) B->prm = *params;
     else gbfv_default_params(&B->prm);
@@ -2881,6 +2965,10 @@ gbfv_batch* gbfv_serve_create(int capacity, int model, const gbfv_params* params
         freeBatch(B);
         return nullptr;
     };
+    if (params && params->local_linearizer != GBFV_LIN_AD) {
+        setError("served systems are linearized by automatic differentiation only");
+        return fail(nullptr, GBFV_ERR_UNSUPPORTED);
+    }
     if (capacity <= 0 || max_cells <= 0 || (model != GBFV_MODEL_IMMISCIBLE_2P && model != GBFV_MODEL_BLACKOIL_3P))
         return fail(nullptr, GBFV_ERR_ARG);
     int ndev = 0;

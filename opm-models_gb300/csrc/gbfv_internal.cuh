@@ -104,6 +104,13 @@ struct IqBuffers {
     double* sto;   // [(e*(b+1) + k)*ldN + p], k = 0 value, 1..b derivatives
 };
 
+// finite-difference linearizer: intensive quantities of the deflected
+// states, per primary variable (+eps and the second, minus state)
+struct FdIq {
+    IqBuffers plus[3];
+    IqBuffers minus[3];
+};
+
 
 // device-side status words (bounded waits report here instead of trapping)
 struct DevStatus {
@@ -160,6 +167,12 @@ void launchIq(const DevMesh& m, const DevPhysics* phys, const double* x, const i
               IqBuffers iq, cudaStream_t s);
 void launchAssemble(const DevMesh& m, const DevPhysics* phys, IqBuffers iq, double* storageOld,
                     int iter0, double dt, double* residual, double* jval, cudaStream_t s);
+void launchSetRefPressure(const double* x, int idx, double* refP, cudaStream_t s);
+void launchFdDeflect(const DevMesh& m, int b, const double* x, const int* meaning, const double* refP, int pv,
+                     int dir, double* xd, cudaStream_t s);
+void launchAssembleFd(const DevMesh& m, const DevPhysics* phys, IqBuffers iq0, const FdIq& fd, const int* meaning,
+                      const double* refP, int method, double* storageOld, int iter0, double dt, double* residual,
+                      double* jval, cudaStream_t s);
 void launchNewtonError(const DevMesh& m, const double* residual, DevStatus* st, cudaStream_t s);
 void launchCheckUpdate(int n, const double* dx, DevStatus* st, cudaStream_t s);
 void launchNewtonUpdate(const DevMesh& m, const DevPhysics* phys, const double* dx, double* x,

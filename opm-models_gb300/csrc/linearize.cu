@@ -274,13 +274,16 @@ __device__ __forceinline__ D2 transPhase(const D2& pI, double pJ, const D2& rhoI
     return pd * (lamJ * (-T));
 }
 
-__device__ __forceinline__ void kAssembleImmiscibleBody(const DevMesh& m, const DevPhysics* __restrict__ phys,
-                                                           IqBuffers iq, double* __restrict__ storageOld,
-                                                           int iter0, double dt,
-                                                           double* __restrict__ residual,
-                                                           double* __restrict__ jval, const int p)
+// The local residual of element p (FvBaseLocalResidual::eval,
+// fvbaselocalresidual.hh:158-191) divided by its volume, with the element's
+// own intensive quantities from `iq` and its neighbours' from `nbr` (the same
+// buffers for AD; the deflected state of p for finite differences).  Each
+// interior face's flux (times the face area) goes to sink(dir, q, flux).
+template <class Sink>
+__device__ __forceinline__ void localImmiscible(const DevMesh& m, const IqBuffers& iq, const IqBuffers& nbr,
+                                                double* __restrict__ storageOld, int iter0, double dt, const int p,
+                                                D2 (&res)[2], Sink& sink)
 {
-    if (p >= m.N) return;
     const int ld = m.ldN;
     D2 pI[2], rhoI[2], lamI[2];
     for (int a = 0; a < 2; ++a) {
@@ -288,7 +291,8 @@ __device__ __forceinline__ void kAssembleImmiscibleBody(const DevMesh& m, const 
         rhoI[a] = ldDual<2>(iq, ld, 2 + a, 2 + a, p);
         lamI[a] = ldDual<2>(iq, ld, 4 + a, 4 + a, p);
     }
-    D2 res[2] = {D2(0.0), D2(0.0)};
+    res[0] = D2(0.0);
+    res[1] = D2(0.0);
     const int ndir = 2 * m.dim;
     for (int dir = 0; dir < ndir; ++dir) {
         const int q = m.nbr[dir * ld + p];
@@ -301,9 +305,9 @@ __device__ __forceinline__ void kAssembleImmiscibleBody(const DevMesh& m, const 
         const double nrm = (dir & 1) ? 1.0 : -1.0;
         D2 flux[2];
         for (int a = 0; a < 2; ++a) {
-            const double pJ = iq.val[a * ld + q];
-            const double rhoJ = iq.val[(2 + a) * ld + q];
-            const double lamJ = iq.val[(4 + a) * ld + q];
+            const double pJ = nbr.val[a * ld + q];
+            const double rhoJ = nbr.val[(2 + a) * ld + q];
+            const double lamJ = nbr.val[(4 + a) * ld + q];
             bool upI;
             D2 vf = m.fluxModule == GBFV_FLUX_TRANS
                         ? transPhase(pI[a], pJ, rhoI[a], rhoJ, lamI[a], lamJ, m.trans[dir * ld + p],
@@ -315,7 +319,7 @@ __device__ __forceinline__ void kAssembleImmiscibleBody(const DevMesh& m, const 
         alpha *= area;
         for (int e = 0; e < 2; ++e) flux[e] = flux[e] * alpha;
         for (int e = 0; e < 2; ++e) res[e] = res[e] + flux[e];
-        writeOffBlock<2>(jval, ld, m.slotOfDir[dir ^ 1], q, flux, m.volume[q], m.cflag[q] >= 0);
+        sink(dir, q, flux);
     }
     const double V = m.volume[p];
     {
@@ -380,13 +384,45 @@ __device__ __forceinline__ void kAssembleImmiscibleBody(const DevMesh& m, const 
         for (int e = 0; e < 2; ++e) res[e] = res[e] + values[e];
     }
     for (int e = 0; e < 2; ++e) res[e] = res[e] / V;
+}
+
+// AD: a face's flux derivatives are the off-diagonal block (q, p)
+template <int B>
+struct OffBlockSink {
+    const DevMesh& m;
+    double* jval;
+    __device__ void operator()(int dir, int q, const Dual<B>* flux) const
+    {
+        writeOffBlock<B>(jval, m.ldN, m.slotOfDir[dir ^ 1], q, flux, m.volume[q], m.cflag[q] >= 0);
+    }
+};
+
+// the residual row and diagonal block of element p (identity in constraint rows)
+template <int B>
+__device__ __forceinline__ void writeDiag(const DevMesh& m, const Dual<B> (&res)[B], double* __restrict__ residual,
+                                          double* __restrict__ jval, const int p)
+{
+    const int ld = m.ldN;
     const bool cons = m.cflag[p] >= 0;
     const int ds = m.dim;  // diagonal slot
-    for (int e = 0; e < 2; ++e) {
-        residual[2 * p + e] = cons ? 0.0 : res[e].v;
-        for (int v = 0; v < 2; ++v)
-            jval[(ds * 4 + e * 2 + v) * ld + p] = cons ? (e == v ? 1.0 : 0.0) : res[e].d[v];
+    for (int e = 0; e < B; ++e) {
+        residual[B * p + e] = cons ? 0.0 : res[e].v;
+        for (int v = 0; v < B; ++v)
+            jval[(ds * B * B + e * B + v) * ld + p] = cons ? (e == v ? 1.0 : 0.0) : res[e].d[v];
     }
+}
+
+__device__ __forceinline__ void kAssembleImmiscibleBody(const DevMesh& m, const DevPhysics* __restrict__ phys,
+                                                           IqBuffers iq, double* __restrict__ storageOld,
+                                                           int iter0, double dt,
+                                                           double* __restrict__ residual,
+                                                           double* __restrict__ jval, const int p)
+{
+    if (p >= m.N) return;
+    OffBlockSink<2> sink{m, jval};
+    D2 res[2];
+    localImmiscible(m, iq, iq, storageOld, iter0, dt, p, res, sink);
+    writeDiag<2>(m, res, residual, jval, p);
 }
 
 __global__ void __launch_bounds__(128) kAssembleImmiscible(DevMesh m, const DevPhysics* __restrict__ phys,
@@ -398,13 +434,12 @@ __global__ void __launch_bounds__(128) kAssembleImmiscible(DevMesh m, const DevP
     kAssembleImmiscibleBody(m, phys, iq, storageOld, iter0, dt, residual, jval, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
-__device__ __forceinline__ void kAssembleBlackoilBody(const DevMesh& m, const DevPhysics* __restrict__ phys,
-                                                         IqBuffers iq, double* __restrict__ storageOld,
-                                                         int iter0, double dt,
-                                                         double* __restrict__ residual,
-                                                         double* __restrict__ jval, const int p)
+template <class Sink>
+__device__ __forceinline__ void localBlackoil(const DevMesh& m, const DevPhysics* __restrict__ phys,
+                                              const IqBuffers& iq, const IqBuffers& nbr,
+                                              double* __restrict__ storageOld, int iter0, double dt, const int p,
+                                              D3 (&res)[3], Sink& sink)
 {
-    if (p >= m.N) return;
     const int ld = m.ldN;
     const BlackOilPvt& T = phys->pvt;
     // own quantities: p as a seeded variable, the rest from K1
@@ -418,7 +453,7 @@ __device__ __forceinline__ void kAssembleBlackoilBody(const DevMesh& m, const De
     RsI = ldDual<3>(iq, ld, 10, 9, p);
     const double rhoRef[3] = {T.rhoRefW, T.rhoRefO, T.rhoRefG};
     const int comp[3] = {1, 0, 2};
-    D3 res[3] = {D3(0.0), D3(0.0), D3(0.0)};
+    for (int e = 0; e < 3; ++e) res[e] = D3(0.0);
     for (int dir = 0; dir < 6; ++dir) {
         const int q = m.nbr[dir * ld + p];
         if (q < 0) continue;
@@ -428,18 +463,18 @@ __device__ __forceinline__ void kAssembleBlackoilBody(const DevMesh& m, const De
         const double Kh = m.Kh[dir * ld + p];
         const double area = m.area[dir * ld + p];
         const double nrm = (dir & 1) ? 1.0 : -1.0;
-        const double pJ = iq.val[0 * ld + q];
+        const double pJ = nbr.val[0 * ld + q];
         D3 flux[3] = {D3(0.0), D3(0.0), D3(0.0)};
         for (int a = 0; a < 3; ++a) {
-            const double rhoJ = iq.val[(1 + a) * ld + q];
-            const double lamJ = iq.val[(4 + a) * ld + q];
+            const double rhoJ = nbr.val[(1 + a) * ld + q];
+            const double lamJ = nbr.val[(4 + a) * ld + q];
             bool upI;
             D3 vf = darcyPhase<3>(pI, pJ, rhoI[a], rhoJ, lamI[a], lamJ, dTot, gIn, gEx, Kh, nrm, upI);
-            D3 invB = upI ? invBI[a] : D3(iq.val[(7 + a) * ld + q]);
+            D3 invB = upI ? invBI[a] : D3(nbr.val[(7 + a) * ld + q]);
             D3 svf = invB * vf;
             flux[comp[a]] = flux[comp[a]] + svf * rhoRef[a];
             if (a == 1) {
-                D3 Rs = upI ? RsI : D3(iq.val[10 * ld + q]);
+                D3 Rs = upI ? RsI : D3(nbr.val[10 * ld + q]);
                 flux[2] = flux[2] + Rs * svf * T.rhoRefG;
             }
         }
@@ -447,7 +482,7 @@ __device__ __forceinline__ void kAssembleBlackoilBody(const DevMesh& m, const De
         alpha *= area;
         for (int e = 0; e < 3; ++e) flux[e] = flux[e] * alpha;
         for (int e = 0; e < 3; ++e) res[e] = res[e] + flux[e];
-        writeOffBlock<3>(jval, ld, m.slotOfDir[dir ^ 1], q, flux, m.volume[q], m.cflag[q] >= 0);
+        sink(dir, q, flux);
     }
     const double V = m.volume[p];
     {
@@ -476,13 +511,19 @@ __device__ __forceinline__ void kAssembleBlackoilBody(const DevMesh& m, const De
         for (int e = 0; e < 3; ++e) res[e] = res[e] + D3(bf.rate[e]) * aa;
     }
     for (int e = 0; e < 3; ++e) res[e] = res[e] / V;
-    const bool cons = m.cflag[p] >= 0;
-    const int ds = m.dim;
-    for (int e = 0; e < 3; ++e) {
-        residual[3 * p + e] = cons ? 0.0 : res[e].v;
-        for (int v = 0; v < 3; ++v)
-            jval[(ds * 9 + e * 3 + v) * ld + p] = cons ? (e == v ? 1.0 : 0.0) : res[e].d[v];
-    }
+}
+
+__device__ __forceinline__ void kAssembleBlackoilBody(const DevMesh& m, const DevPhysics* __restrict__ phys,
+                                                         IqBuffers iq, double* __restrict__ storageOld,
+                                                         int iter0, double dt,
+                                                         double* __restrict__ residual,
+                                                         double* __restrict__ jval, const int p)
+{
+    if (p >= m.N) return;
+    OffBlockSink<3> sink{m, jval};
+    D3 res[3];
+    localBlackoil(m, phys, iq, iq, storageOld, iter0, dt, p, res, sink);
+    writeDiag<3>(m, res, residual, jval, p);
 }
 
 __global__ void __launch_bounds__(128) kAssembleBlackoil(DevMesh m, const DevPhysics* __restrict__ phys,
@@ -502,6 +543,207 @@ void launchAssemble(const DevMesh& m, const DevPhysics* phys, IqBuffers iq, doub
         kAssembleImmiscible<<<nb, bs, 0, s>>>(m, phys, iq, storageOld, iter0, dt, residual, jval);
     else
         kAssembleBlackoil<<<nb, bs, 0, s>>>(m, phys, iq, storageOld, iter0, dt, residual, jval);
+    countLaunch();
+}
+
+// ------------------------------------------ finite-difference linearizer --
+// FvBaseFdLocalLinearizer (fvbasefdlocallinearizer.hh:222-510).  Element p's
+// Jacobian column for primary variable pv is its local residual at a
+// deflected state of p minus the one at another state, divided by the total
+// deflection: forward (method +1) x + eps against x, central (0) x + eps
+// against (x + eps) - (eps + eps), backward (-1) x against x - eps.  eps =
+// BaseEpsilon / primaryVarWeight, BaseEpsilon = max(0.9123e-10, machine
+// epsilon * 1.23e3) (fvbasefdlocallinearizer.hh:75-79, 272-283).  The
+// neighbours keep their intensive quantities; the old time level's storage
+// comes from the cache the unperturbed evaluation filled.
+//
+// The deflected intensive quantities of every cell are computed at once
+// (one deflected copy of the state per primary variable and direction: a
+// cell's quantities depend on its own variables only), then one thread per
+// element evaluates its local residual at each deflected state.
+
+// primaryVarWeight: immisciblemodel.hh:321-333 (pressure 10 / reference
+// pressure), blackoilmodel.hh:395-440 (Sw 1, po 1/300e5, gas variable by its
+// meaning: Sg 1, Rs 1/250, Rv 1/0.025)
+__device__ __forceinline__ double fdEps(const DevMesh& m, int b, const int* __restrict__ meaning, double refP, int p,
+                                        int pv)
+{
+    const double baseEps = fmax(0.9123e-10, 2.220446049250313e-16 * 1.23e3);
+    double w;
+    if (m.model == GBFV_MODEL_IMMISCIBLE_2P)
+        w = pv == 0 ? 10 / refP : 1.0;
+    else if (pv == 0)
+        w = 1.0;
+    else if (pv == 1)
+        w = 1.0 / 300e5;
+    else {
+        const int g = meaning[p];
+        w = g == GBFV_GAS_SG ? 1.0 : g == GBFV_GAS_RS ? 1.0 / 250. : 1.0 / 0.025;
+    }
+    return baseEps / w;
+}
+
+// the reference pressure: the pressure of the first cell (natural order) at
+// the start of a time step (ImmiscibleModel::updateBegin, immisciblemodel.hh:301-316)
+__global__ void kSetRefPressure(const double* __restrict__ x, int idx, double* refP) { *refP = x[idx]; }
+
+void launchSetRefPressure(const double* x, int idx, double* refP, cudaStream_t s)
+{
+    kSetRefPressure<<<1, 1, 0, s>>>(x, idx, refP);
+    countLaunch();
+}
+
+// deflected copy of the state: primary variable pv of every cell moved by
+// +eps (dir > 0), from +eps back by eps + eps (dir == 0, central), or by
+// -(0 + eps) (dir < 0, backward)
+__global__ void __launch_bounds__(256) kFdDeflect(DevMesh m, int b, const double* __restrict__ x,
+                                                  const int* __restrict__ meaning, const double* __restrict__ refP,
+                                                  int pv, int dir, double* __restrict__ xd)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= m.N) return;
+    for (int e = 0; e < b; ++e) xd[b * p + e] = x[b * p + e];
+    const double eps = fdEps(m, b, meaning, *refP, p, pv);
+    double v = x[b * p + pv];
+    if (dir > 0)
+        v += eps;
+    else if (dir == 0) {
+        v += eps;
+        v -= eps + eps;
+    }
+    else
+        v -= 0.0 + eps;
+    xd[b * p + pv] = v;
+}
+
+void launchFdDeflect(const DevMesh& m, int b, const double* x, const int* meaning, const double* refP, int pv,
+                     int dir, double* xd, cudaStream_t s)
+{
+    const int bs = 256, nb = (m.N + bs - 1) / bs;
+    kFdDeflect<<<nb, bs, 0, s>>>(m, b, x, meaning, refP, pv, dir, xd);
+    countLaunch();
+}
+
+// FD: a face's flux values (times the area)
+template <int B>
+struct FluxValueSink {
+    double (*f)[B];
+    __device__ void operator()(int dir, int q, const Dual<B>* flux) const
+    {
+        for (int e = 0; e < B; ++e) f[dir][e] = flux[e].v;
+    }
+};
+
+template <int B, class Local>
+__device__ __forceinline__ void fdElement(const DevMesh& m, const FdIq& fd, IqBuffers iq0,
+                                          const int* __restrict__ meaning, const double* __restrict__ refP,
+                                          int method, double* __restrict__ storageOld, int iter0,
+                                          double* __restrict__ residual, double* __restrict__ jval, const int p,
+                                          Local local)
+{
+    using D = Dual<B>;
+    const int ld = m.ldN;
+    const int ndir = 2 * m.dim;
+    double f0[6][B], fd1[6][B];
+    FluxValueSink<B> s0{f0}, s1{fd1};
+    D res0[B], res1[B];
+    local(iq0, iter0, res0, s0);  // localResidual_.eval(residual_, elemCtx)
+    const bool cons = m.cflag[p] >= 0;
+    const int ds = m.dim;
+    for (int e = 0; e < B; ++e) residual[B * p + e] = cons ? 0.0 : res0[e].v;
+    const double refPv = *refP;
+    for (int pv = 0; pv < B; ++pv) {
+        const double eps = fdEps(m, B, meaning, refPv, p, pv);
+        double delta = 0.0;
+        double dI[B], dJ[6][B];
+        // the neighbours' residual in this element's context: (0 - flux) / V_q
+        if (method >= 0) {
+            delta += eps;
+            local(fd.plus[pv], 0, res1, s1);
+            for (int e = 0; e < B; ++e) dI[e] = res1[e].v;
+            for (int dir = 0; dir < ndir; ++dir) {
+                const int q = m.nbr[dir * ld + p];
+                if (q < 0) continue;
+                for (int e = 0; e < B; ++e) dJ[dir][e] = (0.0 - fd1[dir][e]) / m.volume[q];
+            }
+        }
+        else {
+            for (int e = 0; e < B; ++e) dI[e] = res0[e].v;
+            for (int dir = 0; dir < ndir; ++dir) {
+                const int q = m.nbr[dir * ld + p];
+                if (q < 0) continue;
+                for (int e = 0; e < B; ++e) dJ[dir][e] = (0.0 - f0[dir][e]) / m.volume[q];
+            }
+        }
+        if (method <= 0) {
+            delta += eps;
+            local(fd.minus[pv], 0, res1, s1);
+            for (int e = 0; e < B; ++e) dI[e] -= res1[e].v;
+            for (int dir = 0; dir < ndir; ++dir) {
+                const int q = m.nbr[dir * ld + p];
+                if (q < 0) continue;
+                for (int e = 0; e < B; ++e) dJ[dir][e] -= (0.0 - fd1[dir][e]) / m.volume[q];
+            }
+        }
+        else {
+            for (int e = 0; e < B; ++e) dI[e] -= res0[e].v;
+            for (int dir = 0; dir < ndir; ++dir) {
+                const int q = m.nbr[dir * ld + p];
+                if (q < 0) continue;
+                for (int e = 0; e < B; ++e) dJ[dir][e] -= (0.0 - f0[dir][e]) / m.volume[q];
+            }
+        }
+        for (int e = 0; e < B; ++e)
+            jval[(ds * B * B + e * B + pv) * ld + p] = cons ? (e == pv ? 1.0 : 0.0) : dI[e] / delta;
+        for (int dir = 0; dir < ndir; ++dir) {
+            const int q = m.nbr[dir * ld + p];
+            if (q < 0) continue;
+            const bool zq = m.cflag[q] >= 0;
+            for (int e = 0; e < B; ++e)
+                jval[(m.slotOfDir[dir ^ 1] * B * B + e * B + pv) * ld + q] = zq ? 0.0 : dJ[dir][e] / delta;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128) kAssembleFdImmiscible(DevMesh m, IqBuffers iq0, FdIq fd,
+                                                             const int* __restrict__ meaning,
+                                                             const double* __restrict__ refP, int method,
+                                                             double* __restrict__ storageOld, int iter0, double dt,
+                                                             double* __restrict__ residual, double* __restrict__ jval)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= m.N) return;
+    fdElement<2>(m, fd, iq0, meaning, refP, method, storageOld, iter0, residual, jval, p,
+                 [&](const IqBuffers& own, int it0, D2 (&res)[2], FluxValueSink<2>& sink) {
+                     localImmiscible(m, own, iq0, storageOld, it0, dt, p, res, sink);
+                 });
+}
+
+__global__ void __launch_bounds__(128) kAssembleFdBlackoil(DevMesh m, const DevPhysics* __restrict__ phys,
+                                                           IqBuffers iq0, FdIq fd, const int* __restrict__ meaning,
+                                                           const double* __restrict__ refP, int method,
+                                                           double* __restrict__ storageOld, int iter0, double dt,
+                                                           double* __restrict__ residual, double* __restrict__ jval)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= m.N) return;
+    fdElement<3>(m, fd, iq0, meaning, refP, method, storageOld, iter0, residual, jval, p,
+                 [&](const IqBuffers& own, int it0, D3 (&res)[3], FluxValueSink<3>& sink) {
+                     localBlackoil(m, phys, own, iq0, storageOld, it0, dt, p, res, sink);
+                 });
+}
+
+void launchAssembleFd(const DevMesh& m, const DevPhysics* phys, IqBuffers iq0, const FdIq& fd, const int* meaning,
+                      const double* refP, int method, double* storageOld, int iter0, double dt, double* residual,
+                      double* jval, cudaStream_t s)
+{
+    const int bs = 128, nb = (m.N + bs - 1) / bs;
+    if (m.model == GBFV_MODEL_IMMISCIBLE_2P)
+        kAssembleFdImmiscible<<<nb, bs, 0, s>>>(m, iq0, fd, meaning, refP, method, storageOld, iter0, dt, residual,
+                                                jval);
+    else
+        kAssembleFdBlackoil<<<nb, bs, 0, s>>>(m, phys, iq0, fd, meaning, refP, method, storageOld, iter0, dt,
+                                              residual, jval);
     countLaunch();
 }
 

@@ -51,6 +51,8 @@ SOLVER_GRID = 0
 SOLVER_CLUSTER = 1
 SOLVER_HYBRID = 2
 SOLVER_TILES = 4   # or-ed into SOLVER_CLUSTER / SOLVER_HYBRID: spatial-tile sweeps
+LIN_AD = 0         # local linearizer: automatic differentiation
+LIN_FD = 1         # finite differences (FvBaseFdLocalLinearizer)
 FLUX_DARCY = 0
 FLUX_TRANS = 1
 MAT_STRIDE = 8
@@ -100,6 +102,7 @@ class Params(C.Structure):
         ("pressure_max", C.c_double), ("max_water_saturation", C.c_double),
         ("water_only_threshold", C.c_double), ("min_time_step", C.c_double),
         ("max_time_step", C.c_double), ("max_time_step_divisions", C.c_int32),
+        ("local_linearizer", C.c_int32), ("numeric_difference_method", C.c_int32),
     ]
 
 
@@ -145,6 +148,8 @@ def default_params(**overrides):
     p.min_time_step = 0.0
     p.max_time_step = float("inf")
     p.max_time_step_divisions = 10
+    p.local_linearizer = LIN_AD
+    p.numeric_difference_method = 1
     for k, v in overrides.items():
         setattr(p, k, v)
     return p

@@ -417,6 +417,7 @@ struct Sim {
     int lastLinIters = 0;
     double error = 0, lastError = 0;
     int numIterations = 0;
+    double refPressure = 1.0;  // ImmiscibleModel::referencePressure_ (immisciblemodel.hh:301-316)
 };
 
 static void buildPattern(Sim& S)
@@ -475,233 +476,339 @@ static void scatterElement(Sim& S, int I, const Dual<B>* resI, const std::vector
     }
 }
 
-// one element of FvBaseAdLocalLinearizer::linearize + scatter, immiscible
-static void linearizeImmiscible(Sim& S, const std::vector<IQ2>& iq)
+// FvBaseLocalResidual::eval of element I (fvbaselocalresidual.hh:158-191):
+// res = the element's own residual, resJ = its neighbours' (-flux / V_J, in
+// connection order), sc = the parity scale (sum of |terms| / V).  qi is I's
+// intensive quantities (perturbed ones for the finite-difference
+// linearizer), iq every cell's unperturbed ones.  iter0: Newton iteration 0
+// with no stashed intensive quantities -- the storage becomes the cached old
+// time level (fvbaselocalresidual.hh:535-571); otherwise the cache is read.
+static void elementImmiscible(Sim& S, int I, const IQ2& qi, const std::vector<IQ2>& iq, bool iter0, D2* res,
+                              std::vector<D2>& resJ, double* sc)
 {
     const Prob& P = S.P;
-    const int N = S.N;
-    const bool iter0 = S.newtonIter == 0;
-#pragma omp parallel for schedule(static)
-    for (int I = 0; I < N; ++I) {
-        const IQ2& qi = iq[I];
-        D2 res[2];
-        double sc[2] = {0, 0};
-        const int nc = P.connPtr[I + 1] - P.connPtr[I];
-        std::vector<D2> resJ(2 * nc, D2(0.0));
-        // evalFluxes
-        int k = 0;
-        for (int c = P.connPtr[I]; c < P.connPtr[I + 1]; ++c, ++k) {
-            const int Jc = P.connNbr[c];
-            const IQ2& qj = iq[Jc];
-            double pJ[2], rhoJ[2], lamJ[2];
-            for (int a = 0; a < 2; ++a) { pJ[a] = qj.p[a].v; rhoJ[a] = qj.rho[a].v; lamJ[a] = qj.lam[a].v; }
-            D2 vf[2];
-            bool upI[2];
+    for (int e = 0; e < 2; ++e) {
+        res[e] = D2(0.0);
+        sc[e] = 0.0;
+    }
+    const int nc = P.connPtr[I + 1] - P.connPtr[I];
+    resJ.assign(2 * nc, D2(0.0));
+    // evalFluxes
+    int k = 0;
+    for (int c = P.connPtr[I]; c < P.connPtr[I + 1]; ++c, ++k) {
+        const int Jc = P.connNbr[c];
+        const IQ2& qj = iq[Jc];
+        double pJ[2], rhoJ[2], lamJ[2];
+        for (int a = 0; a < 2; ++a) { pJ[a] = qj.p[a].v; rhoJ[a] = qj.rho[a].v; lamJ[a] = qj.lam[a].v; }
+        D2 vf[2];
+        bool upI[2];
+        if (P.fluxModule == GBFV_FLUX_TRANS) {
+            const double T = transInteriorT(P, I, Jc, c);
+            for (int a = 0; a < 2; ++a)
+                vf[a] = transInterior<D2>(P, I, Jc, T, qi.p[a], pJ[a], qi.rho[a], rhoJ[a], qi.lam[a], lamJ[a], upI[a]);
+        }
+        else
+            darcyInterior<D2, 2>(P, I, Jc, c, qi.p, pJ, qi.rho, rhoJ, qi.lam, lamJ, vf, upI);
+        D2 flux[2];
+        for (int a = 0; a < 2; ++a) {
+            flux[a] = D2(0.0);
+            if (upI[a]) flux[a] += vf[a] * qi.rho[a];
+            else flux[a] += vf[a] * rhoJ[a];
+        }
+        double alpha = 1.0;
+        alpha *= P.connArea[c];
+        for (int e = 0; e < 2; ++e) flux[e] *= alpha;
+        for (int e = 0; e < 2; ++e) {
+            res[e] += flux[e];
+            resJ[k * 2 + e] -= flux[e];
+            sc[e] += std::abs(flux[e].v);
+        }
+    }
+    // evalVolumeTerms_
+    {
+        const double scvVolume = P.volume[I] * 1.0;
+        D2 tmp[2];
+        for (int a = 0; a < 2; ++a) tmp[a] = (D2(qi.phi) * qi.S[a]) * qi.rho[a];
+        double tmp2[2];
+        if (iter0) {
+            for (int e = 0; e < 2; ++e) tmp2[e] = tmp[e].v;
+            for (int e = 0; e < 2; ++e) S.storageOld[I * 2 + e] = tmp2[e];
+        }
+        else
+            for (int e = 0; e < 2; ++e) tmp2[e] = S.storageOld[I * 2 + e];
+        for (int e = 0; e < 2; ++e) {
+            sc[e] += std::abs(tmp[e].v) * (scvVolume / S.dt) + std::abs(tmp2[e]) * (scvVolume / S.dt);
+            tmp[e] -= tmp2[e];
+            tmp[e] *= scvVolume / S.dt;
+            res[e] += tmp[e];
+        }
+        for (int e = 0; e < 2; ++e) res[e] -= 0.0 * scvVolume;
+    }
+    // evalBoundary_
+    for (int f = P.bfPtr[I]; f < P.bfPtr[I + 1]; ++f) {
+        D2 values[2] = {D2(0.0), D2(0.0)};
+        const int type = P.bfType[f];
+        if (type == GBFV_BC_MASSRATE) {
+            for (int e = 0; e < 2; ++e) values[e] = D2(P.bfValue[4 * f + e]);
+        }
+        else if (type == GBFV_BC_FREEFLOW) {
+            const TwoPhaseLaw& L = P.laws[P.material[I]];
+            const double pw = P.bfValue[4 * f + 0], Swb = P.bfValue[4 * f + 1];
+            const double sumRes = L.Swr + L.Snr;
+            const double SwE = (Swb - L.Swr) / (1.0 - sumRes);
+            const double SnE = ((1 - Swb) - L.Snr) / (1.0 - sumRes);
+            const double pcn = L.pcnw(SwE);
+            const double pb[2] = {pw, pw + pcn - 0.0};
+            const double krb[2] = {L.krw(SwE), L.krn(1.0 - SnE)};
             if (P.fluxModule == GBFV_FLUX_TRANS) {
-                const double T = transInteriorT(P, I, Jc, c);
-                for (int a = 0; a < 2; ++a)
-                    vf[a] = transInterior<D2>(P, I, Jc, T, qi.p[a], pJ[a], qi.rho[a], rhoJ[a], qi.lam[a], lamJ[a], upI[a]);
-            }
-            else
-                darcyInterior<D2, 2>(P, I, Jc, c, qi.p, pJ, qi.rho, rhoJ, qi.lam, lamJ, vf, upI);
-            D2 flux[2];
-            for (int a = 0; a < 2; ++a) {
-                flux[a] = D2(0.0);
-                if (upI[a]) flux[a] += vf[a] * qi.rho[a];
-                else flux[a] += vf[a] * rhoJ[a];
-            }
-            double alpha = 1.0;
-            alpha *= P.connArea[c];
-            for (int e = 0; e < 2; ++e) flux[e] *= alpha;
-            for (int e = 0; e < 2; ++e) {
-                res[e] += flux[e];
-                resJ[k * 2 + e] -= flux[e];
-                sc[e] += std::abs(flux[e].v);
-            }
-        }
-        // evalVolumeTerms_
-        {
-            const double scvVolume = P.volume[I] * 1.0;
-            D2 tmp[2];
-            for (int a = 0; a < 2; ++a) tmp[a] = (D2(qi.phi) * qi.S[a]) * qi.rho[a];
-            double tmp2[2];
-            if (iter0) {
-                for (int e = 0; e < 2; ++e) tmp2[e] = tmp[e].v;
-                for (int e = 0; e < 2; ++e) S.storageOld[I * 2 + e] = tmp2[e];
-            }
-            else
-                for (int e = 0; e < 2; ++e) tmp2[e] = S.storageOld[I * 2 + e];
-            for (int e = 0; e < 2; ++e) {
-                sc[e] += std::abs(tmp[e].v) * (scvVolume / S.dt) + std::abs(tmp2[e]) * (scvVolume / S.dt);
-                tmp[e] -= tmp2[e];
-                tmp[e] *= scvVolume / S.dt;
-                res[e] += tmp[e];
-            }
-            for (int e = 0; e < 2; ++e) res[e] -= 0.0 * scvVolume;
-        }
-        // evalBoundary_
-        for (int f = P.bfPtr[I]; f < P.bfPtr[I + 1]; ++f) {
-            D2 values[2] = {D2(0.0), D2(0.0)};
-            const int type = P.bfType[f];
-            if (type == GBFV_BC_MASSRATE) {
-                for (int e = 0; e < 2; ++e) values[e] = D2(P.bfValue[4 * f + e]);
-            }
-            else if (type == GBFV_BC_FREEFLOW) {
-                const TwoPhaseLaw& L = P.laws[P.material[I]];
-                const double pw = P.bfValue[4 * f + 0], Swb = P.bfValue[4 * f + 1];
-                const double sumRes = L.Swr + L.Snr;
-                const double SwE = (Swb - L.Swr) / (1.0 - sumRes);
-                const double SnE = ((1 - Swb) - L.Snr) / (1.0 - sumRes);
-                const double pcn = L.pcnw(SwE);
-                const double pb[2] = {pw, pw + pcn - 0.0};
-                const double krb[2] = {L.krw(SwE), L.krn(1.0 - SnE)};
-                if (P.fluxModule == GBFV_FLUX_TRANS) {
-                    // calculateBoundaryGradients_ (transfluxmodule.hh:324-415)
-                    const double T = transBoundaryT(P, I, f - P.bfPtr[I]);
-                    const double g = P.g[P.dimWorld - 1];
-                    const double distZ = P.center[3 * I + P.dimWorld - 1] - P.bfCenter[3 * f + P.dimWorld - 1];
-                    for (int a = 0; a < 2; ++a) {
-                        D2 rhoAvg = (qi.rho[a] + P.rho[a]) / 2.0;
-                        D2 pEx(pb[a]);
-                        pEx += rhoAvg * (distZ * g);
-                        D2 pd = pEx - qi.p[a];
-                        D2 vf = pd.v > 0.0 ? pd * (krb[a] / P.mu[a]) * (-T) : pd * qi.lam[a] * (-T);
-                        D2 dens = pb[a] > qi.p[a].v ? D2(P.rho[a]) : qi.rho[a];
-                        values[a] += vf * dens;
-                    }
-                }
-                else
-                {
-                const double* xI = &P.center[3 * I];
-                const double* xf = &P.bfCenter[3 * f];
-                const double* n = &P.bfNormal[3 * f];
-                double distSq = 0;
-                for (int d = 0; d < 3; ++d) { const double t = xf[d] - xI[d]; distSq += t * t; }
-                double dIn[3];
-                for (int d = 0; d < 3; ++d) dIn[d] = xI[d] - xf[d];
-                double absDist2 = 0, gTimesDist = 0;
-                for (int d = 0; d < 3; ++d) absDist2 += dIn[d] * dIn[d];
-                for (int d = 0; d < 3; ++d) gTimesDist += P.g[d] * dIn[d];
+                // calculateBoundaryGradients_ (transfluxmodule.hh:324-415)
+                const double T = transBoundaryT(P, I, f - P.bfPtr[I]);
+                const double g = P.g[P.dimWorld - 1];
+                const double distZ = P.center[3 * I + P.dimWorld - 1] - P.bfCenter[3 * f + P.dimWorld - 1];
                 for (int a = 0; a < 2; ++a) {
-                    D2 deltay = pb[a] - qi.p[a];
-                    D2 pg[3];
-                    for (int d = 0; d < 3; ++d) pg[d] = deltay * ((xf[d] - xI[d]) / distSq);
-                    D2 pStatIn = (-gTimesDist) * qi.rho[a];
-                    D2 fsc = pStatIn / absDist2;
-                    for (int d = 0; d < 3; ++d) pg[d] += dIn[d] * fsc;
-                    D2 tmp(0.0);
-                    for (int d = 0; d < 3; ++d) tmp += pg[d] * n[d];
-                    D2 mob = tmp > 0.0 ? D2(krb[a] / P.mu[a]) : qi.lam[a];
-                    D2 vf(0.0);
-                    for (int d = 0; d < 3; ++d) {
-                        D2 fv = P.perm[3 * I + d] * pg[d];
-                        fv *= -mob;
-                        vf += fv * n[d];
-                    }
+                    D2 rhoAvg = (qi.rho[a] + P.rho[a]) / 2.0;
+                    D2 pEx(pb[a]);
+                    pEx += rhoAvg * (distZ * g);
+                    D2 pd = pEx - qi.p[a];
+                    D2 vf = pd.v > 0.0 ? pd * (krb[a] / P.mu[a]) * (-T) : pd * qi.lam[a] * (-T);
                     D2 dens = pb[a] > qi.p[a].v ? D2(P.rho[a]) : qi.rho[a];
                     values[a] += vf * dens;
                 }
-                }
             }
-            const double aa = P.bfArea[f] * 1.0;
-            for (int e = 0; e < 2; ++e) values[e] *= aa;
-            for (int e = 0; e < 2; ++e) res[e] += values[e];
-            for (int e = 0; e < 2; ++e) sc[e] += std::abs(values[e].v);
+            else
+            {
+            const double* xI = &P.center[3 * I];
+            const double* xf = &P.bfCenter[3 * f];
+            const double* n = &P.bfNormal[3 * f];
+            double distSq = 0;
+            for (int d = 0; d < 3; ++d) { const double t = xf[d] - xI[d]; distSq += t * t; }
+            double dIn[3];
+            for (int d = 0; d < 3; ++d) dIn[d] = xI[d] - xf[d];
+            double absDist2 = 0, gTimesDist = 0;
+            for (int d = 0; d < 3; ++d) absDist2 += dIn[d] * dIn[d];
+            for (int d = 0; d < 3; ++d) gTimesDist += P.g[d] * dIn[d];
+            for (int a = 0; a < 2; ++a) {
+                D2 deltay = pb[a] - qi.p[a];
+                D2 pg[3];
+                for (int d = 0; d < 3; ++d) pg[d] = deltay * ((xf[d] - xI[d]) / distSq);
+                D2 pStatIn = (-gTimesDist) * qi.rho[a];
+                D2 fsc = pStatIn / absDist2;
+                for (int d = 0; d < 3; ++d) pg[d] += dIn[d] * fsc;
+                D2 tmp(0.0);
+                for (int d = 0; d < 3; ++d) tmp += pg[d] * n[d];
+                D2 mob = tmp > 0.0 ? D2(krb[a] / P.mu[a]) : qi.lam[a];
+                D2 vf(0.0);
+                for (int d = 0; d < 3; ++d) {
+                    D2 fv = P.perm[3 * I + d] * pg[d];
+                    fv *= -mob;
+                    vf += fv * n[d];
+                }
+                D2 dens = pb[a] > qi.p[a].v ? D2(P.rho[a]) : qi.rho[a];
+                values[a] += vf * dens;
+            }
+            }
         }
-        // volumetric residual (fvbaselocalresidual.hh:174-190)
-        for (int e = 0; e < 2; ++e) res[e] /= P.volume[I];
-        for (int e = 0; e < 2; ++e) S.rscale[I * 2 + e] = sc[e] / P.volume[I];
-        k = 0;
-        for (int c = P.connPtr[I]; c < P.connPtr[I + 1]; ++c, ++k)
-            for (int e = 0; e < 2; ++e) resJ[k * 2 + e] /= P.volume[P.connNbr[c]];
+        const double aa = P.bfArea[f] * 1.0;
+        for (int e = 0; e < 2; ++e) values[e] *= aa;
+        for (int e = 0; e < 2; ++e) res[e] += values[e];
+        for (int e = 0; e < 2; ++e) sc[e] += std::abs(values[e].v);
+    }
+    // volumetric residual (fvbaselocalresidual.hh:174-190)
+    for (int e = 0; e < 2; ++e) res[e] /= P.volume[I];
+    k = 0;
+    for (int c = P.connPtr[I]; c < P.connPtr[I + 1]; ++c, ++k)
+        for (int e = 0; e < 2; ++e) resJ[k * 2 + e] /= P.volume[P.connNbr[c]];
+}
+
+static void elementBlackoil(Sim& S, int I, const IQ3& qi, const std::vector<IQ3>& iq, bool iter0, D3* res,
+                            std::vector<D3>& resJ, double* sc)
+{
+    const Prob& P = S.P;
+    const BlackOilPvt& T = P.pvt;
+    const double rhoRef[3] = {T.rhoRefW, T.rhoRefO, T.rhoRefG};
+    const int compOfPhase[3] = {1, 0, 2};
+    for (int e = 0; e < 3; ++e) {
+        res[e] = D3(0.0);
+        sc[e] = 0.0;
+    }
+    const int nc = P.connPtr[I + 1] - P.connPtr[I];
+    resJ.assign(3 * nc, D3(0.0));
+    int k = 0;
+    for (int c = P.connPtr[I]; c < P.connPtr[I + 1]; ++c, ++k) {
+        const int Jc = P.connNbr[c];
+        const IQ3& qj = iq[Jc];
+        double pJ[3], rhoJ[3], lamJ[3];
+        for (int a = 0; a < 3; ++a) { pJ[a] = qj.p[a].v; rhoJ[a] = qj.rho[a].v; lamJ[a] = qj.lam[a].v; }
+        D3 vf[3];
+        bool upI[3];
+        darcyInterior<D3, 3>(P, I, Jc, c, qi.p, pJ, qi.rho, rhoJ, qi.lam, lamJ, vf, upI);
+        D3 flux[3] = {D3(0.0), D3(0.0), D3(0.0)};
+        // BlackOilLocalResidual::computeFlux / evalPhaseFluxes_
+        for (int a = 0; a < 3; ++a) {
+            D3 invB = upI[a] ? qi.invB[a] : D3(qj.invB[a].v);
+            D3 svf = invB * vf[a];
+            flux[compOfPhase[a]] += svf * rhoRef[a];
+            if (a == 1) {
+                D3 Rs = upI[a] ? qi.Rs : D3(qj.Rs.v);
+                flux[2] += Rs * svf * T.rhoRefG;
+            }
+        }
+        double alpha = 1.0;
+        alpha *= P.connArea[c];
+        for (int e = 0; e < 3; ++e) flux[e] *= alpha;
+        for (int e = 0; e < 3; ++e) {
+            res[e] += flux[e];
+            resJ[k * 3 + e] -= flux[e];
+            sc[e] += std::abs(flux[e].v);
+        }
+    }
+    {
+        const double scvVolume = P.volume[I] * 1.0;
+        D3 tmp[3] = {D3(0.0), D3(0.0), D3(0.0)};
+        // BlackOilLocalResidual::computeStorage
+        D3 phi(qi.phi);
+        for (int a = 0; a < 3; ++a) {
+            D3 sv = qi.S[a] * qi.invB[a] * phi;
+            tmp[compOfPhase[a]] += sv;
+            if (a == 1) tmp[2] += qi.Rs * sv;
+        }
+        tmp[1] *= T.rhoRefW;
+        tmp[2] *= T.rhoRefG;
+        tmp[0] *= T.rhoRefO;
+        double tmp2[3];
+        if (iter0) {
+            for (int e = 0; e < 3; ++e) tmp2[e] = tmp[e].v;
+            for (int e = 0; e < 3; ++e) S.storageOld[I * 3 + e] = tmp2[e];
+        }
+        else
+            for (int e = 0; e < 3; ++e) tmp2[e] = S.storageOld[I * 3 + e];
+        for (int e = 0; e < 3; ++e) {
+            sc[e] += std::abs(tmp[e].v) * (scvVolume / S.dt) + std::abs(tmp2[e]) * (scvVolume / S.dt);
+            tmp[e] -= tmp2[e];
+            tmp[e] *= scvVolume / S.dt;
+            res[e] += tmp[e];
+        }
+        for (int e = 0; e < 3; ++e) res[e] -= 0.0 * scvVolume;
+    }
+    // black-oil problems here only have no-flow or mass-rate boundaries
+    for (int f = P.bfPtr[I]; f < P.bfPtr[I + 1]; ++f) {
+        if (P.bfType[f] != GBFV_BC_MASSRATE) continue;
+        const double aa = P.bfArea[f] * 1.0;
+        for (int e = 0; e < 3; ++e) res[e] += D3(P.bfValue[4 * f + e]) * aa;
+    }
+    for (int e = 0; e < 3; ++e) res[e] /= P.volume[I];
+    k = 0;
+    for (int c = P.connPtr[I]; c < P.connPtr[I + 1]; ++c, ++k)
+        for (int e = 0; e < 3; ++e) resJ[k * 3 + e] /= P.volume[P.connNbr[c]];
+}
+
+// one element of FvBaseAdLocalLinearizer::linearize + scatter, per model
+static void linearizeImmiscible(Sim& S, const std::vector<IQ2>& iq)
+{
+    const bool iter0 = S.newtonIter == 0;
+#pragma omp parallel for schedule(static)
+    for (int I = 0; I < S.N; ++I) {
+        D2 res[2];
+        double sc[2];
+        std::vector<D2> resJ;
+        elementImmiscible(S, I, iq[I], iq, iter0, res, resJ, sc);
+        for (int e = 0; e < 2; ++e) S.rscale[I * 2 + e] = sc[e] / S.P.volume[I];
         scatterElement<2>(S, I, res, resJ);
     }
 }
 
 static void linearizeBlackoil(Sim& S, const std::vector<IQ3>& iq)
 {
-    const Prob& P = S.P;
-    const BlackOilPvt& T = P.pvt;
-    const int N = S.N;
     const bool iter0 = S.newtonIter == 0;
-    const double rhoRef[3] = {T.rhoRefW, T.rhoRefO, T.rhoRefG};
-    const int compOfPhase[3] = {1, 0, 2};
 #pragma omp parallel for schedule(static)
-    for (int I = 0; I < N; ++I) {
-        const IQ3& qi = iq[I];
+    for (int I = 0; I < S.N; ++I) {
         D3 res[3];
-        double sc[3] = {0, 0, 0};
-        const int nc = P.connPtr[I + 1] - P.connPtr[I];
-        std::vector<D3> resJ(3 * nc, D3(0.0));
-        int k = 0;
-        for (int c = P.connPtr[I]; c < P.connPtr[I + 1]; ++c, ++k) {
-            const int Jc = P.connNbr[c];
-            const IQ3& qj = iq[Jc];
-            double pJ[3], rhoJ[3], lamJ[3];
-            for (int a = 0; a < 3; ++a) { pJ[a] = qj.p[a].v; rhoJ[a] = qj.rho[a].v; lamJ[a] = qj.lam[a].v; }
-            D3 vf[3];
-            bool upI[3];
-            darcyInterior<D3, 3>(P, I, Jc, c, qi.p, pJ, qi.rho, rhoJ, qi.lam, lamJ, vf, upI);
-            D3 flux[3] = {D3(0.0), D3(0.0), D3(0.0)};
-            // BlackOilLocalResidual::computeFlux / evalPhaseFluxes_
-            for (int a = 0; a < 3; ++a) {
-                D3 invB = upI[a] ? qi.invB[a] : D3(qj.invB[a].v);
-                D3 svf = invB * vf[a];
-                flux[compOfPhase[a]] += svf * rhoRef[a];
-                if (a == 1) {
-                    D3 Rs = upI[a] ? qi.Rs : D3(qj.Rs.v);
-                    flux[2] += Rs * svf * T.rhoRefG;
-                }
-            }
-            double alpha = 1.0;
-            alpha *= P.connArea[c];
-            for (int e = 0; e < 3; ++e) flux[e] *= alpha;
-            for (int e = 0; e < 3; ++e) {
-                res[e] += flux[e];
-                resJ[k * 3 + e] -= flux[e];
-                sc[e] += std::abs(flux[e].v);
-            }
-        }
-        {
-            const double scvVolume = P.volume[I] * 1.0;
-            D3 tmp[3] = {D3(0.0), D3(0.0), D3(0.0)};
-            // BlackOilLocalResidual::computeStorage
-            D3 phi(qi.phi);
-            for (int a = 0; a < 3; ++a) {
-                D3 sv = qi.S[a] * qi.invB[a] * phi;
-                tmp[compOfPhase[a]] += sv;
-                if (a == 1) tmp[2] += qi.Rs * sv;
-            }
-            tmp[1] *= T.rhoRefW;
-            tmp[2] *= T.rhoRefG;
-            tmp[0] *= T.rhoRefO;
-            double tmp2[3];
-            if (iter0) {
-                for (int e = 0; e < 3; ++e) tmp2[e] = tmp[e].v;
-                for (int e = 0; e < 3; ++e) S.storageOld[I * 3 + e] = tmp2[e];
-            }
-            else
-                for (int e = 0; e < 3; ++e) tmp2[e] = S.storageOld[I * 3 + e];
-            for (int e = 0; e < 3; ++e) {
-                sc[e] += std::abs(tmp[e].v) * (scvVolume / S.dt) + std::abs(tmp2[e]) * (scvVolume / S.dt);
-                tmp[e] -= tmp2[e];
-                tmp[e] *= scvVolume / S.dt;
-                res[e] += tmp[e];
-            }
-            for (int e = 0; e < 3; ++e) res[e] -= 0.0 * scvVolume;
-        }
-        // black-oil problems here only have no-flow or mass-rate boundaries
-        for (int f = P.bfPtr[I]; f < P.bfPtr[I + 1]; ++f) {
-            if (P.bfType[f] != GBFV_BC_MASSRATE) continue;
-            const double aa = P.bfArea[f] * 1.0;
-            for (int e = 0; e < 3; ++e) res[e] += D3(P.bfValue[4 * f + e]) * aa;
-        }
-        for (int e = 0; e < 3; ++e) res[e] /= P.volume[I];
-        for (int e = 0; e < 3; ++e) S.rscale[I * 3 + e] = sc[e] / P.volume[I];
-        k = 0;
-        for (int c = P.connPtr[I]; c < P.connPtr[I + 1]; ++c, ++k)
-            for (int e = 0; e < 3; ++e) resJ[k * 3 + e] /= P.volume[P.connNbr[c]];
+        double sc[3];
+        std::vector<D3> resJ;
+        elementBlackoil(S, I, iq[I], iq, iter0, res, resJ, sc);
+        for (int e = 0; e < 3; ++e) S.rscale[I * 3 + e] = sc[e] / S.P.volume[I];
         scatterElement<3>(S, I, res, resJ);
+    }
+}
+
+// ------------------------------------------ finite-difference linearizer --
+// primaryVarWeight: immisciblemodel.hh:321-333 (pressure 10 / reference
+// pressure, else 1), blackoilmodel.hh:395-440 (Sw 1, po 1/300e5, the gas
+// variable by its meaning: Sg 1, Rs 1/250, Rv 1/0.025)
+static double pvWeight(const Sim& S, int I, int pv)
+{
+    if (S.P.model == GBFV_MODEL_IMMISCIBLE_2P) return pv == 0 ? 10 / S.refPressure : 1.0;
+    if (pv == 0) return 1.0;
+    if (pv == 1) return 1.0 / 300e5;
+    const int m = S.meaning[I];
+    return m == GBFV_GAS_SG ? 1.0 : m == GBFV_GAS_RS ? 1.0 / 250. : 1.0 / 0.025;
+}
+
+// FvBaseFdLocalLinearizer::linearize / evalPartialDerivative_ /
+// updateLocalJacobian_ (fvbasefdlocallinearizer.hh:222-240, 414-510): the
+// element's local residual, then per primary variable of the element the
+// residual at the deflected state(s) -- +eps (method >= 0), then
+// -(delta + eps) from there (method <= 0) -- their difference divided by
+// the total deflection delta.  eps = BaseEpsilon / primaryVarWeight with
+// BaseEpsilon = max(0.9123e-10, machine epsilon * 1.23e3)
+// (fvbasefdlocallinearizer.hh:75-79, 272-283).  The neighbours keep their
+// unperturbed intensive quantities; the storage of the old time level comes
+// from the cache the unperturbed evaluation filled (stashed quantities,
+// fvbaselocalresidual.hh:537-564).
+template <int B, class IQ, class IqFn, class ElemFn>
+static void linearizeFd(Sim& S, const std::vector<IQ>& iq, IqFn iqOf, ElemFn elem)
+{
+    using D = Dual<B>;
+    const Prob& P = S.P;
+    const bool iter0 = S.newtonIter == 0;
+    const int method = S.prm.numeric_difference_method;
+    const double baseEps = std::max(0.9123e-10, std::numeric_limits<double>::epsilon() * 1.23e3);
+#pragma omp parallel for schedule(static)
+    for (int I = 0; I < S.N; ++I) {
+        D res0[B], resD[B];
+        double sc[B], scD[B];
+        std::vector<D> resJ0, resJD;
+        elem(S, I, iq[I], iq, iter0, res0, resJ0, sc);
+        for (int e = 0; e < B; ++e) S.rscale[I * B + e] = sc[e] / P.volume[I];
+        for (int e = 0; e < B; ++e) S.residual[I * B + e] = res0[e].v;
+        const int nc = P.connPtr[I + 1] - P.connPtr[I];
+        std::vector<double> dJ((size_t)B * nc);
+        double* diag = &S.J.val[(size_t)S.diagSlot[I] * B * B];
+        for (int pv = 0; pv < B; ++pv) {
+            double xs[B];
+            for (int e = 0; e < B; ++e) xs[e] = S.x[(size_t)I * B + e];
+            const double eps = baseEps / pvWeight(S, I, pv);
+            double delta = 0.0;
+            double dI[B];
+            if (method >= 0) {
+                xs[pv] += eps;
+                delta += eps;
+                elem(S, I, iqOf(S, I, xs), iq, false, resD, resJD, scD);
+                for (int e = 0; e < B; ++e) dI[e] = resD[e].v;
+                for (int k = 0; k < B * nc; ++k) dJ[k] = resJD[k].v;
+            }
+            else {
+                for (int e = 0; e < B; ++e) dI[e] = res0[e].v;
+                for (int k = 0; k < B * nc; ++k) dJ[k] = resJ0[k].v;
+            }
+            if (method <= 0) {
+                xs[pv] -= delta + eps;
+                delta += eps;
+                elem(S, I, iqOf(S, I, xs), iq, false, resD, resJD, scD);
+                for (int e = 0; e < B; ++e) dI[e] -= resD[e].v;
+                for (int k = 0; k < B * nc; ++k) dJ[k] -= resJD[k].v;
+            }
+            else {
+                for (int e = 0; e < B; ++e) dI[e] -= res0[e].v;
+                for (int k = 0; k < B * nc; ++k) dJ[k] -= resJ0[k].v;
+            }
+            for (int e = 0; e < B; ++e) diag[e * B + pv] = dI[e] / delta;
+            int k = 0;
+            for (int c = P.connPtr[I]; c < P.connPtr[I + 1]; ++c, ++k) {
+                double* ob = &S.J.val[(size_t)S.connSlot[c] * B * B];
+                for (int e = 0; e < B; ++e) ob[e * B + pv] = dJ[(size_t)k * B + e] / delta;
+            }
+        }
     }
 }
 
@@ -725,17 +832,27 @@ static void linearize(Sim& S)
     applyConstraintsToSolution(S);
     std::fill(S.J.val.begin(), S.J.val.end(), 0.0);
     std::fill(S.residual.begin(), S.residual.end(), 0.0);
+    const bool fd = S.prm.local_linearizer == GBFV_LIN_FD;
     if (S.P.model == GBFV_MODEL_IMMISCIBLE_2P) {
         std::vector<IQ2> iq(S.N);
 #pragma omp parallel for schedule(static)
         for (int I = 0; I < S.N; ++I) iq[I] = immiscibleIQ(S.P, I, &S.x[I * 2]);
-        linearizeImmiscible(S, iq);
+        if (fd)
+            linearizeFd<2>(S, iq, [](const Sim& s, int I, const double* x) { return immiscibleIQ(s.P, I, x); },
+                           elementImmiscible);
+        else
+            linearizeImmiscible(S, iq);
     }
     else {
         std::vector<IQ3> iq(S.N);
 #pragma omp parallel for schedule(static)
         for (int I = 0; I < S.N; ++I) iq[I] = blackoilIQ(S.P, I, &S.x[I * 3], S.meaning[I]);
-        linearizeBlackoil(S, iq);
+        if (fd)
+            linearizeFd<3>(S, iq,
+                           [](const Sim& s, int I, const double* x) { return blackoilIQ(s.P, I, x, s.meaning[I]); },
+                           elementBlackoil);
+        else
+            linearizeBlackoil(S, iq);
     }
     for (double v : S.residual)
         if (!std::isfinite(v)) throw NumericalProblem("non-finite residual", GBFV_ERR_NONFINITE);
@@ -1112,6 +1229,7 @@ static int solveLinear(Sim& S, int& iters)
 static bool newtonApply(Sim& S, double dt, gbfv_newton_report& rep)
 {
     S.dt = dt;
+    S.refPressure = S.x[0];  // updateBegin (immisciblemodel.hh:301-316), before NewtonMethod::apply
     std::memset(&rep, 0, sizeof(rep));
     S.numIterations = 0;
     S.error = 0;
@@ -1214,6 +1332,8 @@ void oracle_default_params(gbfv_params* p)
     p->min_time_step = 0.0;
     p->max_time_step = std::numeric_limits<double>::infinity();
     p->max_time_step_divisions = 10;
+    p->local_linearizer = GBFV_LIN_AD;
+    p->numeric_difference_method = 1;
 }
 
 void* oracle_create(const gbfv_problem* prob, const gbfv_params* prm)
@@ -1256,6 +1376,7 @@ int oracle_set_solution(void* h, const double* pv, const int32_t* meaning)
     Sim& S = *static_cast<Sim*>(h);
     std::memcpy(S.x.data(), pv, sizeof(double) * S.N * S.b);
     S.xOld = S.x;
+    S.refPressure = S.x[0];
     if (meaning)
         for (int I = 0; I < S.N; ++I) S.meaning[I] = meaning[I];
     S.meaningOld = S.meaning;
