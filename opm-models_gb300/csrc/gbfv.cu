@@ -20,6 +20,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/gbfv.h"
 #include "gbfv_internal.cuh"
 #include "solver.cuh"
@@ -36,6 +38,17 @@ namespace {
 thread_local std::string t_lastError;
 
 void setError(const std::string& s) { t_lastError = s; }
+
+// NVTX range over a scope: one per Newton phase (linearize, Newton error,
+// solve, update) and per time step, so an attached profiler shows the
+// phases of NewtonMethod::apply (newtonmethod.hh:239-262 times the same ones);
+// without a tool attached the calls return at once
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 #define CK(call)                                                                        \
     do {                                                                                \
@@ -259,6 +272,7 @@ struct gbfv_ctx {
     double *x = nullptr, *xOld = nullptr, *storageOld = nullptr, *residual = nullptr, *jval = nullptr;
     int *meaning = nullptr, *meaningOld = nullptr, *wasSwitched = nullptr;
     IqBuffers iq{};
+    std::string solveLog;  // GBFV_SOLVE_LOG at creation: per-solve JSON lines appended here
     // finite-difference linearizer (allocated on first use): deflected
     // states and their intensive quantities; the reference pressure
     FdIq fd{};
@@ -1467,6 +1481,7 @@ gbfv_ctx* gbfv_create(const gbfv_problem* prob, const gbfv_params* params, int* 
         delete C;
         return nullptr;
     }
+    if (const char* lg = getenv("GBFV_SOLVE_LOG")) C->solveLog = lg;
     int st = GBFV_ERR_ARG;
     try {
         st = prob ? createImpl(C, prob) : GBFV_ERR_ARG;
@@ -1620,6 +1635,7 @@ static int ensureFd(gbfv_ctx* C)
 
 static int linearizeImpl(gbfv_ctx* C)
 {
+    NvtxRange nr("gbfv linearize");
     collectLinStats(C);
     launchApplyConstraints(C->mesh, C->x, C->xOld, C->meaning, C->meaningOld, C->stream);
     if (C->prm.local_linearizer == GBFV_LIN_FD) {
@@ -1719,6 +1735,8 @@ int gbfv_newton_error(gbfv_ctx* C, double* err)
 
 static int solveImpl(gbfv_ctx* C, int* iterations)
 {
+    NvtxRange nr("gbfv solve");
+    const double ms0 = C->S.statMs, bytes0 = C->S.statBytes;
     int it = 0, ref = 0, st;
     if (C->prm.precision == GBFV_PREC_MIXED) {
         st = solveMixed(C->S, C->stream, C->st, C->hst, C->jval, C->residual, C->prm, it, ref);
@@ -1736,6 +1754,20 @@ static int solveImpl(gbfv_ctx* C, int* iterations)
     C->lastRefinements = ref;
     if (iterations) *iterations = it;
     C->haveDx = 1;
+    if (!C->solveLog.empty()) {
+        // one JSON line per solve (GBFV_SOLVE_LOG): iterations, refinements,
+        // device time and algorithmic bytes of the solver launches
+        const double ms = C->S.statMs - ms0, bytes = C->S.statBytes - bytes0;
+        if (FILE* f = fopen(C->solveLog.c_str(), "a")) {
+            fprintf(f,
+                    "{\"cells\": %d, \"newton_iteration\": %d, \"precision\": \"%s\", \"status\": %d, "
+                    "\"iterations\": %d, \"refinements\": %d, \"solve_ms\": %.6g, \"bytes\": %.6g, "
+                    "\"achieved_gbs\": %.6g}\n",
+                    C->N, C->newtonIter, C->prm.precision == GBFV_PREC_MIXED ? "mixed" : "fp64", st, it, ref, ms,
+                    bytes, ms > 0 ? bytes / (ms * 1e6) : 0.0);
+            fclose(f);
+        }
+    }
     return st;
 }
 
@@ -1756,6 +1788,7 @@ int gbfv_solve(gbfv_ctx* C, double* dx, int* iterations)
 
 static int updateImpl(gbfv_ctx* C, int* switched)
 {
+    NvtxRange nr("gbfv update");
     int st;
     if ((st = resetStatus(C->stream, C->st))) return st;
     launchCheckUpdate(C->N * C->b, C->dx, C->st, C->stream);
@@ -1912,6 +1945,7 @@ int gbfv_phase_times(const gbfv_ctx* C, double* ms4)
 int gbfv_newton_apply(gbfv_ctx* C, double dt, gbfv_newton_report* rep)
 {
     if (!C || !(dt > 0)) return GBFV_ERR_ARG;
+    NvtxRange nr("gbfv newton_apply");
     gbfv_newton_report r;
     std::memset(&r, 0, sizeof(r));
     C->dt = dt;

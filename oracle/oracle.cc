@@ -30,7 +30,9 @@
 //                                       blackoilprimaryvariables.hh:549-910
 //   time integration                    fvbaseproblem.hh:512-606,
 //                                       simulator.hh:505-512, 780-802
+#ifdef _OPENMP
 #include <omp.h>
+#endif
 
 #include <cmath>
 #include <cstdint>
@@ -1362,8 +1364,13 @@ void* oracle_create(const gbfv_problem* prob, const gbfv_params* prm)
 
 void oracle_destroy(void* h) { delete static_cast<Sim*>(h); }
 
+#ifdef _OPENMP
 void oracle_set_threads(int n) { omp_set_num_threads(n > 0 ? n : 1); }
 int oracle_get_threads(void) { return omp_get_max_threads(); }
+#else  // serial build (the sanitizer target)
+void oracle_set_threads(int) {}
+int oracle_get_threads(void) { return 1; }
+#endif
 
 int oracle_set_params(void* h, const gbfv_params* prm)
 {

@@ -13,7 +13,9 @@ import subprocess
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB = os.path.join(HERE, "_build", "liboracle.so")
+# GBFV_ORACLE_LIB selects another build of the same source (the sanitizer
+# build of the Makefile's `sanitize` target)
+LIB = os.environ.get("GBFV_ORACLE_LIB") or os.path.join(HERE, "_build", "liboracle.so")
 
 
 def build(quiet=True):
