@@ -1,0 +1,44 @@
+"""Generate the full-size fixture c2_newton_log.npz with the oracle.
+
+Workload C2 (blackoil-100x100x20: 200k cells, 10 time steps of one day,
+BiCGStab + ILU(0) to 1e-6, Newton tolerance 1e-6, FP64): the oracle's
+Newton and linear iteration counts per step, and the final primary
+variables of every 997th cell (natural order) with their meanings.  The GPU
+test (tests/test_gpu_full_size.py) reruns the workload and compares.
+Run from the repository root (a few minutes on the host cores):
+    python tests/golden/make_c2_golden.py
+"""
+import os
+import sys
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "opm-models_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import numpy as np  # noqa: E402
+
+import oracle as O  # noqa: E402
+from gbfv import capi, problems  # noqa: E402
+
+STRIDE = 997
+
+
+def main():
+    prob = problems.blackoil(100, 100, 20)
+    prm = capi.default_params(linear_tolerance=1e-6, newton_tolerance=1e-6)
+    O.set_threads(os.cpu_count() or 1)
+    orc = O.Oracle(prob, prm)
+    t0 = time.time()
+    st, dts, nits, lits, _ = orc.time_integration(10, 86400.0, fixed_dt=True)
+    assert st == 0
+    x, m = orc.solution()
+    idx = np.arange(0, prob.num_cells, STRIDE)
+    np.savez_compressed(os.path.join(HERE, "c2_newton_log.npz"), newton=nits, linear=lits, dt=dts,
+                        cells=idx, pv=x.reshape(-1, 3)[idx], meaning=m[idx])
+    print("C2 oracle: newton", nits.tolist(), "linear", lits.tolist(), "%.0f s" % (time.time() - t0))
+
+
+if __name__ == "__main__":
+    main()
