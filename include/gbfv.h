@@ -364,6 +364,10 @@ int gbfv_solver_config(const gbfv_ctx* ctx, int precision, int* mode, int* block
  * (grid contexts only; GBFV_ERR_UNSUPPORTED where a tile's level is wider
  * than a block or the tables exceed shared memory)                        */
 #define GBFV_SOLVER_TILES 4
+/* or-ed into mode 2 for GBFV_PREC_MIXED: the hybrid launch with blocks of
+ * 256 threads instead of 512 (a cheaper level step where a level's share per
+ * block fits 256 rows; one of the autotuner's candidates)                  */
+#define GBFV_SOLVER_NARROW 8
 int gbfv_set_solver_config(gbfv_ctx* ctx, int precision, int mode, int blocks);
 int gbfv_reset_kernel_stats(gbfv_ctx* ctx);
 /* with GBFV_PROFILE set in the environment at creation: nanoseconds spent

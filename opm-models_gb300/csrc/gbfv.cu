@@ -110,6 +110,7 @@ struct SolverData {
     int maxGrid[2] = {1, 1};
     int maxCluster[2] = {1, 1};
     int maxHybrid[2] = {0, 0};  // blocks of a hybrid launch (whole resident clusters of HYBRID_CLUSTER)
+    int maxHybridNarrow = 0;    // the same for the FP32 hybrid launch with SOLVER_THREADS-thread blocks
     double tuneMs[2][16] = {};
     int adjacentLevels = 0;  // every dependency is exactly one level away
     std::vector<int> colHost;   // [s*ldN + p] host copy of the ELL columns
@@ -172,6 +173,7 @@ int allocSolver(SolverData& S, int maxBlocksOverride = 0)
     const bool hybridOk = !getenv("GBFV_NO_HYBRID") && !profiled;
     S.maxHybrid[0] = hybridOk && S.maxCluster[0] >= HYBRID_CLUSTER ? maxHybridBlocks<double>(S.b) : 0;
     S.maxHybrid[1] = hybridOk && S.maxCluster[1] >= HYBRID_CLUSTER ? maxHybridBlocks<float>(S.b) : 0;
+    S.maxHybridNarrow = S.maxHybrid[1] > 0 ? maxHybridBlocks<float>(S.b, true) : 0;
     // default before tuning: one block for small systems, else a cluster of 8
     for (int k = 0; k < 2; ++k) {
         S.mode[k] = SYNC_CLUSTER;
@@ -188,14 +190,18 @@ int allocSolver(SolverData& S, int maxBlocksOverride = 0)
                 S.nblk[k] = std::min(n, S.maxCluster[k]);
                 S.tuned[k] = 1;
             }
-        else if (strncmp(f, "hybrid", 6) == 0)
+        else if (strncmp(f, "hybrid", 6) == 0) {
+            // "hybrid:256": FP32 blocks of SOLVER_THREADS threads
+            const bool nw = strstr(f, ":256") != nullptr;
             for (int k = 0; k < 2; ++k) {
-                if (S.maxHybrid[k] > HYBRID_CLUSTER) {
-                    S.mode[k] = SYNC_HYBRID | tf;
-                    S.nblk[k] = S.maxHybrid[k];
+                const int mx = k == 1 && nw ? S.maxHybridNarrow : S.maxHybrid[k];
+                if (mx > HYBRID_CLUSTER) {
+                    S.mode[k] = SYNC_HYBRID | tf | (k == 1 && nw ? SYNC_NARROW : 0);
+                    S.nblk[k] = mx;
                     S.tuned[k] = 1;
                 }
             }
+        }
         else if (sscanf(f, "grid:%d", &n) == 1 && n > 0)
             for (int k = 0; k < 2; ++k) { S.mode[k] = SYNC_GRID; S.nblk[k] = std::min(n, S.maxGrid[k]); S.tuned[k] = 1; }
     }
@@ -685,7 +691,9 @@ int fillKArgs(SolverData& S, DevStatus* st, const T* A, T* FL, T* FD, const T* r
               double redTol, double absTol, double maxRes, int maxIter, int mode, int nblocks, KArgs<T>& a)
 {
     const bool tiles = (mode & SYNC_TILES) != 0;
-    mode &= ~SYNC_TILES;
+    const bool narrow = (mode & SYNC_NARROW) != 0;
+    mode &= ~(SYNC_TILES | SYNC_NARROW);
+    if (narrow && (mode != SYNC_HYBRID || tiles)) return GBFV_ERR_UNSUPPORTED;
     a.N = S.N;
     a.ldN = S.ldN;
     a.dim = S.dim;
@@ -725,7 +733,8 @@ int fillKArgs(SolverData& S, DevStatus* st, const T* A, T* FL, T* FD, const T* r
         a.hybrid = mode == SYNC_HYBRID ? HYBRID_CLUSTER : 0;
         for (size_t l = 0; l + 1 < S.levPtr.size(); ++l)
             maxChunk = std::max(maxChunk, levelChunk(S.levPtr[l + 1] - S.levPtr[l], C, omode));
-        constexpr int NTC = clusterThreads<T>();
+        // threads per block of the sweeping cluster
+        const int NTC = narrow ? SOLVER_THREADS : clusterThreads<T>();
         a.tile = 0;
         a.tinfo = nullptr;
         a.tdepF = a.tdepB = a.tpushF = a.tpushB = nullptr;
@@ -827,6 +836,7 @@ void tuneSolver(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hs
         cands.push_back({SYNC_GRID, std::min(nsm, S.maxGrid[k])});
         cands.push_back({SYNC_GRID, std::min(2 * nsm, S.maxGrid[k])});
         if (S.maxHybrid[k] > HYBRID_CLUSTER) cands.push_back({SYNC_HYBRID, S.maxHybrid[k]});
+        if (k == 1 && S.maxHybridNarrow > HYBRID_CLUSTER) cands.push_back({SYNC_HYBRID | SYNC_NARROW, S.maxHybridNarrow});
     }
     // The spatial-tile sweeps are not a candidate: on the black-oil workloads
     // they were slower than the push sweeps (a level's rows of one tile sit on
@@ -1867,14 +1877,16 @@ int gbfv_get_kernel_stats(const gbfv_ctx* Cc, gbfv_kernel_stats* out)
 
 int gbfv_set_solver_config(gbfv_ctx* C, int precision, int mode, int blocks)
 {
-    const int base = mode & ~SYNC_TILES;
-    if (!C || (base != SYNC_CLUSTER && base != SYNC_GRID && base != SYNC_HYBRID) || blocks < 1 ||
-        (base == SYNC_GRID && mode != base))
-        return GBFV_ERR_ARG;
+    const int base = mode & ~(SYNC_TILES | SYNC_NARROW);
     const int k = precision == GBFV_PREC_MIXED ? 1 : 0;
+    if (!C || (base != SYNC_CLUSTER && base != SYNC_GRID && base != SYNC_HYBRID) || blocks < 1 ||
+        (base == SYNC_GRID && mode != base) ||
+        ((mode & SYNC_NARROW) && (base != SYNC_HYBRID || k != 1 || (mode & SYNC_TILES))))
+        return GBFV_ERR_ARG;
     SolverData& S = C->S;
+    const int maxH = (mode & SYNC_NARROW) ? S.maxHybridNarrow : S.maxHybrid[k];
     if (base == SYNC_CLUSTER && blocks > S.maxCluster[k]) return GBFV_ERR_UNSUPPORTED;
-    if (base == SYNC_HYBRID && (blocks > S.maxHybrid[k] || blocks % HYBRID_CLUSTER || blocks <= HYBRID_CLUSTER))
+    if (base == SYNC_HYBRID && (blocks > maxH || blocks % HYBRID_CLUSTER || blocks <= HYBRID_CLUSTER))
         return GBFV_ERR_UNSUPPORTED;
     if (base == SYNC_GRID && blocks > S.maxGrid[k]) return GBFV_ERR_UNSUPPORTED;
     if (mode & SYNC_TILES) {

@@ -1730,10 +1730,9 @@ static int launchOne(const KArgs<T>& a, int nblocks, cudaStream_t s)
 
 // hybrid: the grid kernel over nblocks blocks in clusters of HYBRID_CLUSTER,
 // cooperative (every block resident, for the software grid barrier)
-template <class T, int B>
+template <class T, int B, int NT>
 static int launchHybrid(const KArgs<T>& a, int nblocks, cudaStream_t s)
 {
-    constexpr int NT = clusterThreads<T>();
     auto fn = kBicgstab<T, B, SYNC_GRID, NT>;
     static bool attrSet = false;
     if (!attrSet) {
@@ -1764,10 +1763,9 @@ static int launchHybrid(const KArgs<T>& a, int nblocks, cudaStream_t s)
 }
 
 // how many blocks a hybrid launch may have (whole clusters that are resident at once)
-template <class T>
-int maxHybridBlocks(int b)
+template <class T, int NT>
+static int maxHybridBlocksNT(int b)
 {
-    constexpr int NT = clusterThreads<T>();
     const void* fn = b == 2 ? (const void*)kBicgstab<T, 2, SYNC_GRID, NT> : (const void*)kBicgstab<T, 3, SYNC_GRID, NT>;
     const size_t dyn = b == 2 ? PushSmem<T, 2, NT>::bytes(MAX_PUSH_LEVELS) : PushSmem<T, 3, NT>::bytes(MAX_PUSH_LEVELS);
     cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
@@ -1792,10 +1790,22 @@ int maxHybridBlocks(int b)
 }
 
 template <class T>
+int maxHybridBlocks(int b, bool narrow)
+{
+    return narrow ? maxHybridBlocksNT<T, SOLVER_THREADS>(b) : maxHybridBlocksNT<T, clusterThreads<T>()>(b);
+}
+
+template <class T>
 int launchBicgstab(const KArgs<T>& a, int b, int mode, int nblocks, cudaStream_t s)
 {
     constexpr int NTC = clusterThreads<T>();
-    if (mode == SYNC_HYBRID) return b == 2 ? launchHybrid<T, 2>(a, nblocks, s) : launchHybrid<T, 3>(a, nblocks, s);
+    const bool narrow = (mode & SYNC_NARROW) != 0;
+    mode &= ~SYNC_NARROW;
+    if (mode == SYNC_HYBRID && narrow)
+        return b == 2 ? launchHybrid<T, 2, SOLVER_THREADS>(a, nblocks, s)
+                      : launchHybrid<T, 3, SOLVER_THREADS>(a, nblocks, s);
+    if (mode == SYNC_HYBRID)
+        return b == 2 ? launchHybrid<T, 2, NTC>(a, nblocks, s) : launchHybrid<T, 3, NTC>(a, nblocks, s);
     if (mode == SYNC_GRID)
         return b == 2 ? launchOne<T, 2, SYNC_GRID, SOLVER_THREADS>(a, nblocks, s)
                       : launchOne<T, 3, SYNC_GRID, SOLVER_THREADS>(a, nblocks, s);
@@ -1937,8 +1947,8 @@ template int maxSolverBlocks<double>(int);
 template int maxSolverBlocks<float>(int);
 template int maxClusterBlocks<double>(int);
 template int maxClusterBlocks<float>(int);
-template int maxHybridBlocks<double>(int);
-template int maxHybridBlocks<float>(int);
+template int maxHybridBlocks<double>(int, bool);
+template int maxHybridBlocks<float>(int, bool);
 template int launchBicgstabBatch<double>(const KArgs<double>*, const int*, const int*, int*, int, int, int, int,
                                          cudaStream_t);
 template int launchBicgstabBatch<float>(const KArgs<float>*, const int*, const int*, int*, int, int, int, int,

@@ -18,6 +18,10 @@ constexpr int SYNC_GRID = 0;     // whole grid, cooperative launch, software bar
 constexpr int SYNC_CLUSTER = 1;  // one thread-block cluster, hardware barrier
 constexpr int SYNC_HYBRID = 2;   // launch mode: clusters over the whole GPU, cluster 0 sweeps, all share the rest
 constexpr int HYBRID_CLUSTER = 16;  // cluster size of the hybrid launch
+// or-ed into SYNC_HYBRID: blocks of SOLVER_THREADS threads (the FP32 solver
+// otherwise runs clusterThreads<float>() per block); fewer threads make a
+// level step cheaper where a level's share per block still fits
+constexpr int SYNC_NARROW = 8;
 // Spatial-tile sweeps (a flag or-ed into the cluster and hybrid modes): the
 // rows of every level are dealt to the sweeping cluster's blocks by the
 // spatial tile of their cell, so most dependencies stay inside a block.
@@ -100,7 +104,7 @@ void launchBatchAccumulate(const SolveJob* jobs, const int* active, int K, int g
 void launchBatchResidual64(const SolveJob* jobs, const int* active, int K, int gx, int b, cudaStream_t s);
 template <class T> int maxSolverBlocks(int b);
 template <class T> int maxClusterBlocks(int b);
-template <class T> int maxHybridBlocks(int b);
+template <class T> int maxHybridBlocks(int b, bool narrow = false);
 // batched solve: clusters of clusterSize blocks take systems args[order[q]],
 // q = 0..*count-1 (device memory), from the queue counter (zero before the launch)
 template <class T>

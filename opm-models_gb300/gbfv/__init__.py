@@ -155,6 +155,8 @@ class Context:
         ms = np.zeros(16)
         self.lib.gbfv_solver_config(self.h, precision, C.byref(mode), C.byref(nb), _d(ms), C.byref(nt))
         name = {0: "grid", 1: "cluster", 2: "hybrid"}.get(mode.value & 3, "?")
+        if mode.value & capi.SOLVER_NARROW:
+            name += "-256"
         if mode.value & capi.SOLVER_TILES:
             name += "+tiles"
         return {"mode": name, "blocks": nb.value,

@@ -51,6 +51,7 @@ SOLVER_GRID = 0
 SOLVER_CLUSTER = 1
 SOLVER_HYBRID = 2
 SOLVER_TILES = 4   # or-ed into SOLVER_CLUSTER / SOLVER_HYBRID: spatial-tile sweeps
+SOLVER_NARROW = 8  # or-ed into SOLVER_HYBRID (mixed precision): 256-thread blocks
 LIN_AD = 0         # local linearizer: automatic differentiation
 LIN_FD = 1         # finite differences (FvBaseFdLocalLinearizer)
 FLUX_DARCY = 0

@@ -85,3 +85,21 @@ def test_tile_flag_needs_a_cluster_mode(built):
     with pytest.raises(Exception):
         ctx.set_solver_config(capi.PREC_FP64, capi.SOLVER_GRID | TILES, 16)
     ctx.close()
+
+
+def test_narrow_hybrid_mixed_keeps_the_fp64_newton_counts(built):
+    """The mixed-precision hybrid launch with 256-thread blocks: the same
+    Newton counts as the FP64 run and its state to what the linear
+    tolerance leaves, as the 512-thread launch."""
+    prob = problems.blackoil(40, 36, 8, seed=9)
+    pmx = capi.default_params(linear_tolerance=1e-6, newton_tolerance=1e-6, precision=capi.PREC_MIXED,
+                              inner_tolerance=1e-5)
+    p64 = capi.default_params(linear_tolerance=1e-6, newton_tolerance=1e-6)
+    st, n, _, x, m, cfg = _run(prob, pmx, capi.PREC_MIXED, capi.SOLVER_HYBRID | capi.SOLVER_NARROW, 32, 3,
+                               86400.0)
+    assert st == 0 and cfg["mode"] == "hybrid-256"
+    st, n64, _, x64, m64, _ = _run(prob, p64, capi.PREC_FP64, capi.SOLVER_CLUSTER, 16, 3, 86400.0)
+    assert st == 0
+    assert np.array_equal(n, n64), (n, n64)
+    assert np.array_equal(m, m64)
+    assert rel_state_diff(x, x64, 3) <= 2e-5
