@@ -364,10 +364,9 @@ int gbfv_solver_config(const gbfv_ctx* ctx, int precision, int* mode, int* block
  * (grid contexts only; GBFV_ERR_UNSUPPORTED where a tile's level is wider
  * than a block or the tables exceed shared memory)                        */
 #define GBFV_SOLVER_TILES 4
-/* or-ed into mode 1 or 2 for GBFV_PREC_MIXED: blocks of 256 threads
- * instead of 512 (a cheaper level step where a level's share per block fits
- * 256 rows; the hybrid one is an autotuner candidate, the cluster one is
- * what a batch with gbfv_batch_stats.block_threads == 256 runs)           */
+/* or-ed into mode 2 for GBFV_PREC_MIXED: the hybrid launch with blocks of
+ * 256 threads instead of 512 (a cheaper level step where a level's share per
+ * block fits 256 rows; one of the autotuner's candidates)                  */
 #define GBFV_SOLVER_NARROW 8
 int gbfv_set_solver_config(gbfv_ctx* ctx, int precision, int mode, int blocks);
 int gbfv_reset_kernel_stats(gbfv_ctx* ctx);
@@ -396,15 +395,13 @@ int gbfv_solver_level_cycles(gbfv_ctx* ctx, unsigned long long* c8);
  * queue, largest first; Newton update), each phase a captured CUDA graph
  * replayed every round.  A system's results equal those of the same
  * problem run alone with gbfv_set_solver_config(ctx, precision, 1,
- * cluster_size), or-ed with GBFV_SOLVER_NARROW when the batch's
- * block_threads is 256 for GBFV_PREC_MIXED (gbfv_batch_autotune may pick
- * that).  All systems share params and the model.                       */
+ * cluster_size).  All systems share params and the model.               */
 typedef struct gbfv_batch gbfv_batch;
 typedef struct gbfv_batch_stats {
     int32_t num_systems;
     int32_t cluster_size;      /* blocks per cluster of the batched solve  */
     int32_t num_clusters;      /* clusters resident at once               */
-    int32_t block_threads;     /* threads per block of the batched solve  */
+    int32_t pad;
     int64_t rounds;            /* Newton rounds                           */
     int64_t graph_launches;
     int64_t kernel_launches;

@@ -693,7 +693,7 @@ int fillKArgs(SolverData& S, DevStatus* st, const T* A, T* FL, T* FD, const T* r
     const bool tiles = (mode & SYNC_TILES) != 0;
     const bool narrow = (mode & SYNC_NARROW) != 0;
     mode &= ~(SYNC_TILES | SYNC_NARROW);
-    if (narrow && (mode == SYNC_GRID || tiles)) return GBFV_ERR_UNSUPPORTED;
+    if (narrow && (mode != SYNC_HYBRID || tiles)) return GBFV_ERR_UNSUPPORTED;
     a.N = S.N;
     a.ldN = S.ldN;
     a.dim = S.dim;
@@ -1881,7 +1881,7 @@ int gbfv_set_solver_config(gbfv_ctx* C, int precision, int mode, int blocks)
     const int k = precision == GBFV_PREC_MIXED ? 1 : 0;
     if (!C || (base != SYNC_CLUSTER && base != SYNC_GRID && base != SYNC_HYBRID) || blocks < 1 ||
         (base == SYNC_GRID && mode != base) ||
-        ((mode & SYNC_NARROW) && (base == SYNC_GRID || k != 1 || (mode & SYNC_TILES))))
+        ((mode & SYNC_NARROW) && (base != SYNC_HYBRID || k != 1 || (mode & SYNC_TILES))))
         return GBFV_ERR_ARG;
     SolverData& S = C->S;
     const int maxH = (mode & SYNC_NARROW) ? S.maxHybridNarrow : S.maxHybrid[k];
@@ -2292,7 +2292,6 @@ struct gbfv_batch {
     std::vector<gbfv_ctx*> ctx;
     std::vector<SysState> sys;
     int cluster = 0, numClusters = 1, maxLev = 1, gxLin = 16, gxSol = 16;
-    int narrow = 0;  // FP32 batched solve with SOLVER_THREADS-thread blocks (more clusters per SM)
     // device tables and their pinned host mirrors
     LinJob* dLin = nullptr;
     SolveJob* dSol = nullptr;
@@ -2432,12 +2431,12 @@ int buildBatchGraphs(gbfv_batch* B)
         if (B->precision == GBFV_PREC_MIXED) {
             CK(cudaMemcpyAsync(B->dK32, B->hK32, sizeof(KArgs<float>) * K, cudaMemcpyHostToDevice, s));
             ls = launchBicgstabBatch<float>(B->dK32, B->dOrder, B->dOrder + K, B->dQueue, B->b, B->cluster,
-                                            B->numClusters, B->maxLev, B->narrow != 0, s);
+                                            B->numClusters, B->maxLev, s);
         }
         else {
             CK(cudaMemcpyAsync(B->dK64, B->hK64, sizeof(KArgs<double>) * K, cudaMemcpyHostToDevice, s));
             ls = launchBicgstabBatch<double>(B->dK64, B->dOrder, B->dOrder + K, B->dQueue, B->b, B->cluster,
-                                             B->numClusters, B->maxLev, false, s);
+                                             B->numClusters, B->maxLev, s);
         }
         if (ls) return ls;
         CK(cudaMemcpyAsync(B->hSt, B->dSt, sizeof(DevStatus) * K, cudaMemcpyDeviceToHost, s));
@@ -2545,8 +2544,8 @@ int batchSolvePhase(gbfv_batch* B)
                 const double innerTol = std::min(0.5, std::max(0.5 * need, prm.inner_tolerance));
                 float* vec[6] = {Sd.v32[1], Sd.v32[2], Sd.v32[3], Sd.v32[4], Sd.v32[5], Sd.v32[6]};
                 rs = fillKArgs<float>(Sd, &B->dSt[i], Sd.A32, Sd.FL32, Sd.FD32, Sd.v32[0], vec, ref == 0, innerTol,
-                                      0.0, prm.linear_max_error, prm.linear_max_iterations,
-                                      SYNC_CLUSTER | (B->narrow ? SYNC_NARROW : 0), B->cluster, B->hK32[i]);
+                                      0.0, prm.linear_max_error, prm.linear_max_iterations, SYNC_CLUSTER, B->cluster,
+                                      B->hK32[i]);
             }
             else {
                 rs = fillKArgs<double>(Sd, &B->dSt[i], C->jval, Sd.FL64, Sd.FD64, C->residual, Sd.v64, 1,
@@ -2925,17 +2924,11 @@ int gbfv_batch_autotune(gbfv_batch* B, double dt, int* cluster_out, double* ms_o
     if (rs) return rs;
     const double ms0 = B->solveMs;
     double best = 1e300;
-    int pick = B->cluster, pickNarrow = B->narrow, n = 0;
-    // cluster sizes, and for FP32 also blocks of SOLVER_THREADS threads (two
-    // clusters' blocks fit an SM where one of 512 threads does)
-    const bool mixed = B->precision == GBFV_PREC_MIXED;
-    for (int cand = 0; cand < 2 * 4; ++cand) {
-        const int c = 2 << (cand >> 1), nw = cand & 1;
-        if (c > maxC || (nw && !mixed)) continue;
+    int pick = B->cluster, n = 0;
+    for (int c = 2; c <= maxC; c *= 2) {
         B->cluster = c;
-        B->narrow = nw;
-        B->numClusters = std::max(1, std::min(B->K, mixed ? maxActiveClusters<float>(B->b, c, nw != 0)
-                                                          : maxActiveClusters<double>(B->b, c)));
+        B->numClusters = std::max(1, std::min(B->K, B->precision == GBFV_PREC_MIXED ? maxActiveClusters<float>(B->b, c)
+                                                                                  : maxActiveClusters<double>(B->b, c)));
         if (B->gKry.exec) cudaGraphExecDestroy(B->gKry.exec);
         B->gKry.exec = nullptr;
         if ((rs = buildBatchGraphs(B))) return rs;
@@ -2948,19 +2941,14 @@ int gbfv_batch_autotune(gbfv_batch* B, double dt, int* cluster_out, double* ms_o
         const double ms = B->solveMs - before;
         if (ms_out && n < 8) ms_out[n] = ms;
         n++;
-        if (ms < best) {
-            best = ms;
-            pick = c;
-            pickNarrow = nw;
-        }
+        if (ms < best) { best = ms; pick = c; }
     }
     B->solveMs = ms0;
     B->solveBytes = 0;
     B->solveLaunches = 0;
     B->cluster = pick;
-    B->narrow = pickNarrow;
-    B->numClusters = std::max(1, std::min(B->K, mixed ? maxActiveClusters<float>(B->b, pick, pickNarrow != 0)
-                                                      : maxActiveClusters<double>(B->b, pick)));
+    B->numClusters = std::max(1, std::min(B->K, B->precision == GBFV_PREC_MIXED ? maxActiveClusters<float>(B->b, pick)
+                                                                             : maxActiveClusters<double>(B->b, pick)));
     if ((rs = buildBatchGraphs(B))) return rs;
     for (SysState& y : B->sys) y = SysState();
     CK(cudaStreamSynchronize(B->stream));
@@ -2991,7 +2979,6 @@ int gbfv_batch_get_stats(const gbfv_batch* B, gbfv_batch_stats* out)
     out->num_systems = B->K;
     out->cluster_size = B->cluster;
     out->num_clusters = B->numClusters;
-    out->block_threads = B->precision == GBFV_PREC_MIXED && !B->narrow ? clusterThreads<float>() : SOLVER_THREADS;
     out->rounds = B->rounds;
     out->graph_launches = B->graphLaunches;
     out->kernel_launches = B->kernelLaunches;

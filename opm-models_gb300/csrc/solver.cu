@@ -1801,10 +1801,6 @@ int launchBicgstab(const KArgs<T>& a, int b, int mode, int nblocks, cudaStream_t
     constexpr int NTC = clusterThreads<T>();
     const bool narrow = (mode & SYNC_NARROW) != 0;
     mode &= ~SYNC_NARROW;
-    if (narrow && mode == SYNC_GRID) return GBFV_ERR_UNSUPPORTED;
-    if (narrow && mode == SYNC_CLUSTER && NTC != SOLVER_THREADS)
-        return b == 2 ? launchOne<T, 2, SYNC_CLUSTER, SOLVER_THREADS>(a, nblocks, s)
-                      : launchOne<T, 3, SYNC_CLUSTER, SOLVER_THREADS>(a, nblocks, s);
     if (mode == SYNC_HYBRID && narrow)
         return b == 2 ? launchHybrid<T, 2, SOLVER_THREADS>(a, nblocks, s)
                       : launchHybrid<T, 3, SOLVER_THREADS>(a, nblocks, s);
@@ -1817,10 +1813,11 @@ int launchBicgstab(const KArgs<T>& a, int b, int mode, int nblocks, cudaStream_t
                   : launchOne<T, 3, SYNC_CLUSTER, NTC>(a, nblocks, s);
 }
 
-template <class T, int B, int NT>
+template <class T, int B>
 static int launchBatchB(const KArgs<T>* args, const int* order, const int* count, int* queue, int clusterSize,
                         int numClusters, int maxLev, cudaStream_t s)
 {
+    constexpr int NT = clusterThreads<T>();
     auto fn = kBicgstabBatch<T, B, NT>;
     static bool attrSet = false;
     if (!attrSet) {
@@ -1848,20 +1845,17 @@ static int launchBatchB(const KArgs<T>* args, const int* order, const int* count
 
 template <class T>
 int launchBicgstabBatch(const KArgs<T>* args, const int* order, const int* count, int* queue, int b,
-                        int clusterSize, int numClusters, int maxLev, bool narrow, cudaStream_t s)
+                        int clusterSize, int numClusters, int maxLev, cudaStream_t s)
 {
-    constexpr int NT = clusterThreads<T>();
-    if (narrow && NT != SOLVER_THREADS)
-        return b == 2 ? launchBatchB<T, 2, SOLVER_THREADS>(args, order, count, queue, clusterSize, numClusters, maxLev, s)
-                      : launchBatchB<T, 3, SOLVER_THREADS>(args, order, count, queue, clusterSize, numClusters, maxLev, s);
-    return b == 2 ? launchBatchB<T, 2, NT>(args, order, count, queue, clusterSize, numClusters, maxLev, s)
-                  : launchBatchB<T, 3, NT>(args, order, count, queue, clusterSize, numClusters, maxLev, s);
+    return b == 2 ? launchBatchB<T, 2>(args, order, count, queue, clusterSize, numClusters, maxLev, s)
+                  : launchBatchB<T, 3>(args, order, count, queue, clusterSize, numClusters, maxLev, s);
 }
 
 // how many clusters of the given size fit on the device at once
-template <class T, int NT>
-static int maxActiveClustersNT(int b, int clusterSize)
+template <class T>
+int maxActiveClusters(int b, int clusterSize)
 {
+    constexpr int NT = clusterThreads<T>();
     const void* fn = b == 2 ? (const void*)kBicgstabBatch<T, 2, NT> : (const void*)kBicgstabBatch<T, 3, NT>;
     const size_t dyn = b == 2 ? PushSmem<T, 2, NT>::bytes(MAX_PUSH_LEVELS) : PushSmem<T, 3, NT>::bytes(MAX_PUSH_LEVELS);
     cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
@@ -1883,14 +1877,6 @@ static int maxActiveClustersNT(int b, int clusterSize)
         n = 0;
     }
     return n;
-}
-
-template <class T>
-int maxActiveClusters(int b, int clusterSize, bool narrow)
-{
-    constexpr int NT = clusterThreads<T>();
-    return narrow && NT != SOLVER_THREADS ? maxActiveClustersNT<T, SOLVER_THREADS>(b, clusterSize)
-                                          : maxActiveClustersNT<T, NT>(b, clusterSize);
 }
 
 template <class T>
@@ -1963,12 +1949,12 @@ template int maxClusterBlocks<double>(int);
 template int maxClusterBlocks<float>(int);
 template int maxHybridBlocks<double>(int, bool);
 template int maxHybridBlocks<float>(int, bool);
-template int launchBicgstabBatch<double>(const KArgs<double>*, const int*, const int*, int*, int, int, int, int, bool,
+template int launchBicgstabBatch<double>(const KArgs<double>*, const int*, const int*, int*, int, int, int, int,
                                          cudaStream_t);
-template int launchBicgstabBatch<float>(const KArgs<float>*, const int*, const int*, int*, int, int, int, int, bool,
+template int launchBicgstabBatch<float>(const KArgs<float>*, const int*, const int*, int*, int, int, int, int,
                                         cudaStream_t);
-template int maxActiveClusters<double>(int, int, bool);
-template int maxActiveClusters<float>(int, int, bool);
+template int maxActiveClusters<double>(int, int);
+template int maxActiveClusters<float>(int, int);
 
 // A32 = (float) A64 over all slots
 __global__ void kCastMatrix(const double* __restrict__ src, float* __restrict__ dst, long n)

@@ -109,9 +109,8 @@ template <class T> int maxHybridBlocks(int b, bool narrow = false);
 // q = 0..*count-1 (device memory), from the queue counter (zero before the launch)
 template <class T>
 int launchBicgstabBatch(const KArgs<T>* args, const int* order, const int* count, int* queue, int b,
-                        int clusterSize, int numClusters, int maxLev, bool narrow, cudaStream_t s);
-// narrow: blocks of SOLVER_THREADS threads (where the precision's cluster blocks are larger)
-template <class T> int maxActiveClusters(int b, int clusterSize, bool narrow = false);
+                        int clusterSize, int numClusters, int maxLev, cudaStream_t s);
+template <class T> int maxActiveClusters(int b, int clusterSize);
 void launchCastMatrix(const double* src, float* dst, long n, cudaStream_t s);
 void launchWaitTimeoutProbe(DevStatus* st, cudaStream_t s);
 void launchAccumulate(int n, double* x, const float* d, cudaStream_t s);

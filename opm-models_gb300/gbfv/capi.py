@@ -165,7 +165,7 @@ def as_ptr(a, ctype):
 
 class BatchStats(C.Structure):
     _fields_ = [("num_systems", C.c_int32), ("cluster_size", C.c_int32), ("num_clusters", C.c_int32),
-                ("block_threads", C.c_int32), ("rounds", C.c_int64), ("graph_launches", C.c_int64),
+                ("pad", C.c_int32), ("rounds", C.c_int64), ("graph_launches", C.c_int64),
                 ("kernel_launches", C.c_int64), ("solve_launches", C.c_int64), ("solve_ms", C.c_double),
                 ("solve_bytes", C.c_double), ("linearize_ms", C.c_double)]
 

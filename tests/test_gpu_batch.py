@@ -84,29 +84,3 @@ def test_batch_blackoil_with_wells(built):
         assert st == 0 and np.array_equal(bsn, sn) and np.array_equal(bsl, sl)
         assert np.array_equal(B.systems[i].solution()[0], ctx.solution()[0])
     B.close()
-
-
-def test_autotuned_batch_equals_alone_with_its_configuration(built):
-    """After gbfv_batch_autotune (cluster sizes, and for mixed precision
-    also 256-thread blocks), every system still equals its solo run with
-    the configuration the tuner picked."""
-    probs = _members([9000, 30000, 4000], seed0=555)
-    prm = capi.default_params(linear_tolerance=1e-6, newton_tolerance=1e-6, precision=capi.PREC_MIXED,
-                              inner_tolerance=1e-5)
-    B = Batch(probs, prm, cluster_size=2)
-    c, ms = B.autotune(200.0)
-    st = B.stats()
-    assert st["cluster_size"] == c and st["block_threads"] in (256, 512) and len(ms) >= 2
-    assert B.time_integration(2, 200.0) == 0
-    mode = capi.SOLVER_CLUSTER | (capi.SOLVER_NARROW if st["block_threads"] == 256 else 0)
-    for i, p in enumerate(probs):
-        _, _, bsn, bsl, _ = B.report(i)
-        xb, mb = B.systems[i].solution()
-        ctx = Context(p, prm)
-        ctx.set_solver_config(capi.PREC_MIXED, mode, c)
-        s, _, sn, sl, _ = ctx.time_integration(2, 200.0)
-        x, m = ctx.solution()
-        ctx.close()
-        assert s == 0 and np.array_equal(bsn, sn) and np.array_equal(bsl, sl), (i, bsn, sn, bsl, sl)
-        assert np.array_equal(xb, x) and np.array_equal(mb, m), i
-    B.close()
