@@ -6,7 +6,7 @@
 // the sparsity pattern, orders cells wavefront-major (see
 // gbfv_internal.cuh), precomputes per-face geometry and transmissibility
 // factors, boundary fluid states and the ILU(0) level sets, and uploads
-// everything.  The Newton driver (gbfv_newton_apply) follows
+// everything.  The Newton loop (gbfv_newton_apply) follows
 // NewtonMethod::apply (newtonmethod.hh:228-438); each iteration reads back
 // two scalars (Newton error, solver status).
 #include <cuda_runtime.h>
