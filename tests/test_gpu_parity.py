@@ -204,3 +204,38 @@ def test_blackoil_primary_variable_switching_happens(built):
     assert np.array_equal(mg, mo)
     assert int((mg != m0).sum()) > 0, "no primary-variable switch happened"
     assert rel_state_diff(xg, xo, 3) <= 1e-8
+
+
+@pytest.mark.parametrize("shape", [(1, 1, 1), (1, 1, 5), (5, 1, 1), (2, 1, 3), (1, 4, 1)])
+def test_degenerate_blackoil_grids(built, shape):
+    """Single cells, single rows and columns (both wells in one cell for
+    1x1x1): the linearization at the 1e-12 bar, two steps with the oracle's
+    Newton counts and state."""
+    prob = problems.blackoil(*shape)
+    prm = capi.default_params(linear_tolerance=1e-6, newton_tolerance=1e-6)
+    ctx, orc = Context(prob, prm), O.Oracle(prob, prm)
+    er, ej = _compare_linearization(ctx, orc, 86400.0, 0)
+    assert er <= RTOL_LIN and ej <= RTOL_LIN, (shape, er, ej)
+    ctx.close()
+    ctx, orc = Context(prob, prm), O.Oracle(prob, prm)
+    so, _, no, _, _ = orc.time_integration(2, 86400.0, fixed_dt=True)
+    sg, _, ng, _, _ = ctx.time_integration(2, 86400.0, fixed_dt=True)
+    assert so == 0 and sg == 0 and np.array_equal(no, ng), (shape, no, ng)
+    assert rel_state_diff(ctx.solution()[0], orc.solution()[0], 3) <= 1e-8
+    ctx.close()
+
+
+@pytest.mark.parametrize("shape", [(1, 5), (5, 1), (1, 1), (2, 2)])
+def test_degenerate_lens_grids(built, shape):
+    prob = problems.lens(nx=shape[0], ny=shape[1])
+    prm = capi.default_params(linear_tolerance=1e-6)
+    ctx, orc = Context(prob, prm), O.Oracle(prob, prm)
+    er, ej = _compare_linearization(ctx, orc, 250.0, 0)
+    assert er <= RTOL_LIN and ej <= RTOL_LIN, (shape, er, ej)
+    ctx.close()
+    ctx, orc = Context(prob, prm), O.Oracle(prob, prm)
+    so, dto, no, _, _ = orc.time_integration(2, 250.0)
+    sg, dtg, ng, _, _ = ctx.time_integration(2, 250.0)
+    assert so == 0 and sg == 0 and np.array_equal(no, ng), (shape, no, ng)
+    assert rel_state_diff(ctx.solution()[0], orc.solution()[0], 2) <= 1e-8
+    ctx.close()
