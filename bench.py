@@ -51,6 +51,9 @@ def parse():
                          "the single-grid workload")
     ap.add_argument("--serve", action="store_true",
                     help="served stream: Poisson arrivals of single-time-step black-oil solves (20k-1M cells)")
+    ap.add_argument("--linearizers", action="store_true",
+                    help="linearization only: the AD and the finite-difference local linearizers (forward, "
+                         "central) on the workload's initial state, device time per call, and the CPU oracle's")
     ap.add_argument("--profile-case", action="store_true",
                     help="one linearization + one mixed solve of the workload (for ncu captures); "
                          "prints the solve's iterations, launches and algorithmic bytes")
@@ -432,6 +435,50 @@ def run_profile_case(args):
     return 0 if st == 0 else 1
 
 
+def run_linearizers(args):
+    """FvBaseLinearizer::linearize alone on the workload's initial state
+    (Newton iteration 1, old storage cached by an iteration-0 call): the AD
+    local linearizer and the finite-difference one (forward and central
+    differences), device time per call over --steps x 10 calls after
+    --warmup, and the CPU oracle on all host threads (one call each)."""
+    import __graft_entry__ as ge
+    ge.build()
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from gbfv import Context, capi
+    w = WORKLOADS[args.workload]
+    prob = build_problem(args.workload)
+    out = {"metric": "cells linearized/s", "unit": "cells/s", "workload": args.workload, "cells": prob.num_cells,
+           "gpu": {}, "cpu_oracle": {}}
+    for name, lin, meth in (("ad", capi.LIN_AD, 1), ("fd_forward", capi.LIN_FD, 1), ("fd_central", capi.LIN_FD, 0)):
+        prm = capi.default_params(linear_tolerance=1e-6, newton_tolerance=1e-6, local_linearizer=lin,
+                                  numeric_difference_method=meth)
+        ctx = Context(prob, prm)
+        if ctx.linearize(w["dt"], 0):
+            raise RuntimeError("linearization failed")
+        for _ in range(max(1, args.warmup)):
+            ctx.linearize(w["dt"], 1)
+        ctx.reset_kernel_stats()
+        n = 10 * max(1, args.steps)
+        for _ in range(n):
+            if ctx.linearize(w["dt"], 1):
+                raise RuntimeError("linearization failed")
+        ms = ctx.kernel_stats()["linearize_ms"] / n
+        out["gpu"][name] = {"ms": ms, "value": prob.num_cells / (ms / 1e3)}
+        ctx.close()
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    for name, lin in (("ad", capi.LIN_AD), ("fd_forward", capi.LIN_FD)):
+        orc = O.Oracle(prob, capi.default_params(linear_tolerance=1e-6, newton_tolerance=1e-6, local_linearizer=lin))
+        orc.linearize(w["dt"], 0)
+        t0 = time.perf_counter()
+        orc.linearize(w["dt"], 1)
+        dt = time.perf_counter() - t0
+        out["cpu_oracle"][name] = {"ms": dt * 1e3, "value": prob.num_cells / dt, "cores": threads}
+    print(json.dumps(out))
+    return 0
+
+
 ENSEMBLE = dict(lo=10000, hi=200000, sigma=(0.5, 1.5), seed=1000, steps=2, dt=250.0)
 
 
@@ -685,6 +732,8 @@ def main():
     args = parse()
     if args.profile_case:
         return run_profile_case(args)
+    if args.linearizers:
+        return run_linearizers(args)
     if args.serve:
         return run_serve(args)
     if args.ensemble > 0:
