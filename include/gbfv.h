@@ -509,6 +509,18 @@ int gbfv_read_restart(gbfv_ctx* ctx, const char* path, gbfv_restart_info* info);
  * usable), and the kernel's time in ms.                                   */
 int gbfv_selftest_wait_timeout(double* ms);
 
+/* Host-only check of the push sweeps' level-barrier placement (no
+ * counterpart in the reference): for a pattern of num_rows rows in level
+ * order (lev_ptr[num_levels+1]; col[s*num_rows + p], slots 0..dim-1 the
+ * lower neighbours, dim the row itself, dim+1..2dim the upper ones, -1 for
+ * none), cluster blocks dealing each level's rows a warp at a time
+ * (owner_mode 0) or in contiguous shares (1) and `buffers` dependency
+ * buffers per block, barrier_after[l] = 1 where the forward (or backward)
+ * sweep needs a cluster barrier after level l.                            */
+int gbfv_selftest_level_barriers(int32_t num_rows, int32_t dim, const int32_t* lev_ptr, int32_t num_levels,
+                                 const int32_t* col, int32_t cluster, int32_t owner_mode, int32_t buffers,
+                                 int32_t forward, int8_t* barrier_after);
+
 /* ------------------------------------------------------------------ */
 /* Allocation-free Newton error.  No counterpart in the reference: its
  * NewtonMethod computes the same maximum norm on the host

@@ -445,15 +445,19 @@ inline int levelChunk(int W, int C, int mode)
 // orderings and along the cluster barriers placed so far.  Where a push is
 // not covered, a cluster barrier is placed after the previous level.
 // barrierAfter[l] (level index, in the sweep's own order) is the result.
-void placeLevelBarriers(const SolverData& S, int C, int mode, const std::vector<int>& lev, bool forward,
-                        std::vector<char>& barrierAfter)
+// The pattern: N rows in level order, levPtr, columns colHost[s*ld + p]
+// (lower slots 0..dim-1, diagonal dim, upper dim+1..2dim, -1 for none);
+// D dependency buffers per block.
+void placeLevelBarriersCore(int N, int ld, int dim, const std::vector<int>& levPtr, const std::vector<int>& colHost,
+                            int C, int mode, int D, const std::vector<int>& lev, bool forward,
+                            std::vector<char>& barrierAfter)
 {
-    const int N = S.N, ld = S.ldN, dim = S.dim, nl = (int)S.levPtr.size() - 1, D = PUSH_BUFFERS;
+    const int nl = (int)levPtr.size() - 1;
     barrierAfter.assign(nl, 0);
     auto owner = [&](int p) {
         int o, uu;
         const int l = lev[p];
-        levelSlot(p - S.levPtr[l], S.levPtr[l + 1] - S.levPtr[l], C, mode, o, uu);
+        levelSlot(p - levPtr[l], levPtr[l + 1] - levPtr[l], C, mode, o, uu);
         return o;
     };
     std::vector<int> K((size_t)C * C, -1), Knew;   // K[X*C + Y]: known finished step of Y when X finished its last
@@ -464,19 +468,19 @@ void placeLevelBarriers(const SolverData& S, int C, int mode, const std::vector<
         auto attempt = [&]() -> bool {
             Knew = K;
             for (int X = 0; X < C; ++X) Knew[(size_t)X * C + X] = step;
-            for (int p = S.levPtr[l]; p < S.levPtr[l + 1]; ++p) {
+            for (int p = levPtr[l]; p < levPtr[l + 1]; ++p) {
                 const int X = owner(p);
                 for (int Y = 0; Y < C; ++Y) acc[Y] = K[(size_t)X * C + Y];
                 for (int q = 0; q < dim; ++q) {
                     const int sl = forward ? q : 2 * dim - q;   // dependencies of p in this sweep
-                    const int j = S.colHost[(size_t)sl * ld + p];
+                    const int j = colHost[(size_t)sl * ld + p];
                     if (j < 0) continue;
                     const int* kj = &know[(size_t)j * C];
                     for (int Y = 0; Y < C; ++Y) acc[Y] = std::max(acc[Y], kj[Y]);
                 }
                 for (int q = 0; q < dim; ++q) {
                     const int sl = forward ? dim + 1 + q : q;   // consumers of p
-                    const int u = S.colHost[(size_t)sl * ld + p];
+                    const int u = colHost[(size_t)sl * ld + p];
                     if (u >= 0 && acc[owner(u)] < step + 1 - D) return false;
                 }
                 std::copy(acc.begin(), acc.end(), &know[(size_t)p * C]);
@@ -488,13 +492,20 @@ void placeLevelBarriers(const SolverData& S, int C, int mode, const std::vector<
         };
         if (!attempt()) {
             // a cluster barrier after the previous step: every block knows every
-            // block finished it
+            // block finished it (then every push is covered, D >= 2)
             barrierAfter[forward ? l - 1 : l + 1] = 1;
             for (int& v : K) v = std::max(v, step - 1);
             attempt();
         }
         K.swap(Knew);
     }
+}
+
+void placeLevelBarriers(const SolverData& S, int C, int mode, const std::vector<int>& lev, bool forward,
+                        std::vector<char>& barrierAfter)
+{
+    placeLevelBarriersCore(S.N, S.ldN, S.dim, S.levPtr, S.colHost, C, mode, PUSH_BUFFERS, lev, forward,
+                           barrierAfter);
 }
 
 // Push targets of the cluster sweeps for cluster size C, G level groups and
@@ -3118,6 +3129,25 @@ int gbfv_serve_release(gbfv_batch* B, int slot)
 }
 
 int64_t gbfv_serve_footprint(const gbfv_batch* B) { return B ? B->footprint : -1; }
+
+int gbfv_selftest_level_barriers(int32_t num_rows, int32_t dim, const int32_t* lev_ptr, int32_t num_levels,
+                                 const int32_t* col, int32_t cluster, int32_t owner_mode, int32_t buffers,
+                                 int32_t forward, int8_t* barrier_after)
+{
+    if (num_rows < 1 || dim < 1 || dim > 3 || num_levels < 1 || !lev_ptr || !col || cluster < 1 ||
+        cluster > 16 || (owner_mode != 0 && owner_mode != 1) || buffers < 2 || !barrier_after)
+        return GBFV_ERR_ARG;
+    std::vector<int> levPtr(lev_ptr, lev_ptr + num_levels + 1);
+    if (levPtr[0] != 0 || levPtr[num_levels] != num_rows) return GBFV_ERR_ARG;
+    std::vector<int> colHost(col, col + (size_t)(2 * dim + 1) * num_rows), lev(num_rows);
+    for (int l = 0; l < num_levels; ++l)
+        for (int p = levPtr[l]; p < levPtr[l + 1]; ++p) lev[p] = l;
+    std::vector<char> out;
+    placeLevelBarriersCore(num_rows, num_rows, dim, levPtr, colHost, cluster, owner_mode, buffers, lev,
+                           forward != 0, out);
+    for (int l = 0; l < num_levels; ++l) barrier_after[l] = (int8_t)out[l];
+    return GBFV_OK;
+}
 
 int gbfv_selftest_wait_timeout(double* ms)
 {
