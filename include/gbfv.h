@@ -209,6 +209,13 @@ void gbfv_default_params(gbfv_params* p);
 /* ------------------------------------------------------------------ */
 typedef struct gbfv_ctx gbfv_ctx;
 
+/* Largest grid (cells) or matrix (block rows) one context or linear solver
+ * takes: device arrays are planes of a row count padded to 64 and indexed
+ * with 32-bit integers, and the largest holds 63 planes (7 block slots of
+ * 3 x 3), so 64 x the padded row count must stay below 2^31.  Larger inputs
+ * return GBFV_ERR_UNSUPPORTED before any device work.                      */
+#define GBFV_MAX_CELLS 33554368
+
 /* Create a context on the current CUDA device and upload the problem.
  * Mirrors FvBaseLinearizer::init + createMatrix_ (fvbaselinearizer.hh:
  * 418-452): the sparsity pattern, level sets and block-slot maps are built
@@ -442,7 +449,9 @@ void* gbfv_batch_stream(gbfv_batch* batch);
  * gbfv_batch_system) until gbfv_serve_release frees its device memory.
  * Admission by HBM footprint is the caller's policy, with
  * gbfv_footprint_bytes as the estimate of one system.                    */
-/* estimated device bytes of one system (context + solver buffers)        */
+/* estimated device bytes of one system (context + solver buffers); -1 for
+ * a size no context takes (num_cells outside 1..GBFV_MAX_CELLS, block size
+ * other than 2 or 3, dim other than 2 or 3)                               */
 int64_t gbfv_footprint_bytes(int num_cells, int block_size, int dim);
 gbfv_batch* gbfv_serve_create(int capacity, int model, const gbfv_params* params,
                               int cluster_size, int max_cells, int* status);

@@ -59,6 +59,13 @@ struct NvtxRange {
         }                                                                               \
     } while (0)
 
+// Device arrays are planes of ldN rows (the row count rounded up to 64),
+// indexed with 32-bit ints in the kernels; the most planes one array holds
+// is the block-ELL values / Jacobian's MAX_SLOTS x 3 x 3 = 63
+static_assert(MAX_SLOTS * 3 * 3 < 64, "plane count of the largest device array");
+static_assert(GBFV_MAX_CELLS % 64 == 0 && 64LL * GBFV_MAX_CELLS <= std::numeric_limits<int>::max(),
+              "GBFV_MAX_CELLS keeps every device index within 32 bits");
+
 template <class T>
 int devAlloc(T** p, size_t n)
 {
@@ -995,6 +1002,10 @@ static int createImpl(gbfv_ctx* C, const gbfv_problem* P)
     }
     if (P->model != GBFV_MODEL_IMMISCIBLE_2P && P->model != GBFV_MODEL_BLACKOIL_3P) return GBFV_ERR_ARG;
     if (P->model == GBFV_MODEL_BLACKOIL_3P && !P->pvt) return GBFV_ERR_ARG;
+    if (N > GBFV_MAX_CELLS) {
+        setError("grid larger than GBFV_MAX_CELLS (32-bit device indexing)");
+        return GBFV_ERR_UNSUPPORTED;
+    }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
         setError("no CUDA device");
@@ -2111,6 +2122,10 @@ gbfv_linsolver* gbfv_linsolver_create(int n, int b, const int32_t* rowPtr, const
         return nullptr;
     };
     if (n <= 0 || (b != 2 && b != 3) || !rowPtr || !col) return fail(nullptr, GBFV_ERR_ARG);
+    if (n > GBFV_MAX_CELLS) {
+        setError("more block rows than GBFV_MAX_CELLS (32-bit device indexing)");
+        return fail(nullptr, GBFV_ERR_UNSUPPORTED);
+    }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(nullptr, GBFV_ERR_NO_DEVICE);
     gbfv_linsolver* L = new gbfv_linsolver();
@@ -3005,7 +3020,8 @@ void* gbfv_batch_stream(gbfv_batch* B) { return B ? (void*)B->stream : nullptr; 
 // ---------------------------------------------------------------- serving
 int64_t gbfv_footprint_bytes(int num_cells, int block_size, int dim)
 {
-    if (num_cells <= 0 || (block_size != 2 && block_size != 3) || (dim != 2 && dim != 3)) return -1;
+    if (num_cells <= 0 || num_cells > GBFV_MAX_CELLS || (block_size != 2 && block_size != 3) || (dim != 2 && dim != 3))
+        return -1;
     const int64_t b = block_size, bb = b * b, ns = 2 * dim + 1, nd = 2 * dim;
     const int64_t iq = (b == 2 ? 6 + 12 : 11 + 30) + b * (b + 1);
     // solver: FP64 + FP32 factors, FP32 matrix, Krylov vectors, columns, push tables
@@ -3029,6 +3045,10 @@ gbfv_batch* gbfv_serve_create(int capacity, int model, const gbfv_params* params
     }
     if (capacity <= 0 || max_cells <= 0 || (model != GBFV_MODEL_IMMISCIBLE_2P && model != GBFV_MODEL_BLACKOIL_3P))
         return fail(nullptr, GBFV_ERR_ARG);
+    if (max_cells > GBFV_MAX_CELLS) {
+        setError("max_cells above GBFV_MAX_CELLS (32-bit device indexing)");
+        return fail(nullptr, GBFV_ERR_UNSUPPORTED);
+    }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(nullptr, GBFV_ERR_NO_DEVICE);
     gbfv_batch* B = new gbfv_batch();

@@ -54,6 +54,7 @@ SOLVER_TILES = 4   # or-ed into SOLVER_CLUSTER / SOLVER_HYBRID: spatial-tile swe
 SOLVER_NARROW = 8  # or-ed into SOLVER_HYBRID (mixed precision): 256-thread blocks
 LIN_AD = 0         # local linearizer: automatic differentiation
 LIN_FD = 1         # finite differences (FvBaseFdLocalLinearizer)
+MAX_CELLS = 33554368  # GBFV_MAX_CELLS: largest grid / block-row count (32-bit device indexing)
 FLUX_DARCY = 0
 FLUX_TRANS = 1
 MAT_STRIDE = 8

@@ -84,3 +84,34 @@ def test_footprint_estimate_is_monotone(built):
     assert 0 < a < b and b - a > 100000 * 1000       # at least 1 KB per cell of a 3x3 system
     assert f(100000, 2, 3) < a                         # 2x2 blocks take less
     assert f(0, 3, 3) == -1 and f(10, 4, 3) == -1      # rejected arguments
+
+
+def test_sizes_beyond_32bit_device_indexing_are_rejected_before_device_work(built):
+    """GBFV_MAX_CELLS: every create entry point turns a size whose device
+    indices would not fit 32 bits into GBFV_ERR_UNSUPPORTED before it reads
+    the arrays or looks for a device, so this runs without a GPU."""
+    import re
+    with open(os.path.join(ROOT, "include", "gbfv.h")) as f:
+        m = re.search(r"#define GBFV_MAX_CELLS (\d+)", f.read())
+    assert m and int(m.group(1)) == capi.MAX_CELLS
+    ld = (capi.MAX_CELLS + 63) // 64 * 64
+    assert ld == capi.MAX_CELLS and 64 * ld <= 2**31 - 1 < 64 * (ld + 64)
+    lib = capi.load()
+    st = C.c_int(-1)
+    prob = problems.blackoil(4, 4, 2)
+    s = prob.struct()
+    s.num_cells = capi.MAX_CELLS + 1
+    prm = capi.default_params()
+    assert not lib.gbfv_create(C.byref(s), C.byref(prm), C.byref(st))
+    assert st.value == capi.ERR_UNSUPPORTED
+    rp = np.zeros(2, np.int32)
+    col = np.zeros(1, np.int32)
+    st.value = -1
+    assert not lib.gbfv_linsolver_create(capi.MAX_CELLS + 1, 3, rp.ctypes.data_as(C.POINTER(C.c_int32)),
+                                         col.ctypes.data_as(C.POINTER(C.c_int32)), C.byref(prm), C.byref(st))
+    assert st.value == capi.ERR_UNSUPPORTED
+    st.value = -1
+    assert not lib.gbfv_serve_create(4, capi.MODEL_BLACKOIL_3P, C.byref(prm), 0, capi.MAX_CELLS + 1, C.byref(st))
+    assert st.value == capi.ERR_UNSUPPORTED
+    f = lib.gbfv_footprint_bytes
+    assert f(capi.MAX_CELLS, 3, 3) > 0 and f(capi.MAX_CELLS + 1, 3, 3) == -1
