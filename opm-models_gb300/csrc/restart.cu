@@ -24,11 +24,10 @@
 // Text formatting is host work (the state is copied out once); large
 // states are formatted by several threads, one contiguous range of cells
 // each, and concatenated in order.
-#include <cuda_runtime.h>
-
 #include <algorithm>
 #include <cerrno>
-#include <cinttypes>
+#include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -174,6 +173,17 @@ bool numbers(const std::string& l, int count, double* d)
     return *s == '\0';
 }
 
+// a parsed number as an integer in [lo, hi]: false for NaN, fractions and
+// values outside the range, whose bare conversion to int would be undefined
+bool asInt(double v, double lo, double hi, int32_t& out)
+{
+    if (!(v >= lo && v <= hi) || v != std::floor(v)) return false;
+    out = (int32_t)v;
+    return true;
+}
+
+constexpr double kIntMin = -2147483648.0, kIntMax = 2147483647.0;
+
 int parseRestart(const char* text, size_t len, const gbfv_restart_info& expect, int numCells, int b, double* pv,
                  int32_t* gas, gbfv_restart_info& out)
 {
@@ -184,17 +194,19 @@ int parseRestart(const char* text, size_t len, const gbfv_restart_info& expect, 
         return GBFV_ERR_ARG;
     // the section's values and its end share a line (simulator.hh:951-962)
     double sim[6];
-    if (!r.line(l) || !numbers(l, 6, sim)) {
+    int32_t episode = 0, step = 0;
+    if (!r.line(l) || !numbers(l, 6, sim) || !asInt(sim[0], kIntMin, kIntMax, episode) ||
+        !asInt(sim[5], kIntMin, kIntMax, step)) {
         gbfv::setLastError("restart file: bad Simulator section");
         return GBFV_ERR_ARG;
     }
     out = expect;
-    out.episode_index = (int32_t)sim[0];
+    out.episode_index = episode;
     out.episode_start_time = sim[1];
     out.episode_length = sim[2];
     out.start_time = sim[3];
     out.time = sim[4];
-    out.time_step_index = (int32_t)sim[5];
+    out.time_step_index = step;
     out.vtk_section = 0;
     if (!r.line(l)) {
         gbfv::setLastError("restart file: truncated");
@@ -202,15 +214,17 @@ int parseRestart(const char* text, size_t len, const gbfv_restart_info& expect, 
     }
     if (l == "VTKMultiWriter") {
         double w[1], fl[2];
+        int32_t writer = 0, metaLen = 0;
         std::string l2;
-        if (!r.line(l2) || !numbers(l2, 1, w) || !r.line(l2) || !numbers(l2, 2, fl) || fl[0] < 0 ||
-            fl[0] > (double)(r.end - r.p)) {
+        // the meta file's length: an integer no larger than what is left
+        if (!r.line(l2) || !numbers(l2, 1, w) || !asInt(w[0], kIntMin, kIntMax, writer) || !r.line(l2) ||
+            !numbers(l2, 2, fl) || !asInt(fl[0], 0.0, std::min((double)(r.end - r.p), kIntMax), metaLen)) {
             gbfv::setLastError("restart file: bad VTKMultiWriter section");
             return GBFV_ERR_ARG;
         }
         out.vtk_section = 1;
-        out.vtk_writer_num = (int32_t)w[0];
-        r.p += (size_t)fl[0];  // the meta file's bytes
+        out.vtk_writer_num = writer;
+        r.p += (size_t)metaLen;  // the meta file's bytes
         if (!sectionEnd(r, "the VTKMultiWriter section") || !r.line(l)) return GBFV_ERR_ARG;
     }
     if (l != "Entities: Codim 0") {
@@ -249,12 +263,22 @@ int parseRestart(const char* text, size_t len, const gbfv_restart_info& expect, 
             }
             for (int k = 0; k < b; ++k) pv[(size_t)c * b + k] = v[(size_t)k];
             if (gas) {
-                if (v[(size_t)b + 1] != 0 || v[(size_t)b + 2] != 0 || v[(size_t)b + 3] != 0) {
+                // the reference's enums (blackoilprimaryvariables.hh:125-143):
+                // gas Sg Rs Rv Disabled, water Sw Rvw Rsw Disabled, pressure
+                // Po Pg Pw; a PVT region index >= 0
+                int32_t gm = 0, wm = 0, pm = 0, reg = 0;
+                if (!asInt(v[(size_t)b], 0, 3, gm) || !asInt(v[(size_t)b + 1], 0, 3, wm) ||
+                    !asInt(v[(size_t)b + 2], 0, 2, pm) || !asInt(v[(size_t)b + 3], 0, kIntMax, reg)) {
+                    bad[t] = c;
+                    badKind[t] = GBFV_ERR_ARG;
+                    return;
+                }
+                if (gm == 3 || wm != 0 || pm != 0 || reg != 0) {
                     bad[t] = c;
                     badKind[t] = GBFV_ERR_UNSUPPORTED;
                     return;
                 }
-                gas[c] = (int32_t)v[(size_t)b];
+                gas[c] = gm;
             }
         }
     };
@@ -268,7 +292,8 @@ int parseRestart(const char* text, size_t len, const gbfv_restart_info& expect, 
     for (int t = 0; t < nt; ++t)
         if (bad[t] >= 0) {
             gbfv::setLastError(badKind[t] == GBFV_ERR_UNSUPPORTED
-                                   ? "restart file: water/pressure meaning or PVT region other than 0 (not supported)"
+                                   ? "restart file: disabled gas, water/pressure meaning or PVT region other than 0 "
+                                     "(not supported)"
                                    : "restart file: bad entity line " + std::to_string(bad[t]));
             return badKind[t];
         }

@@ -93,6 +93,46 @@ def test_malformed_files_are_rejected():
     assert restart.parse_restart(b"\n".join(lines), inf, n, 3, True)[0] == capi.ERR_UNSUPPORTED
 
 
+@pytest.mark.parametrize("field,value,want", [
+    (3, b"3", capi.ERR_UNSUPPORTED),   # gas meaning Disabled: valid in the reference, not in this model
+    (3, b"7", capi.ERR_ARG),           # no such gas meaning
+    (3, b"1.5", capi.ERR_ARG),
+    (3, b"nan", capi.ERR_ARG),
+    (5, b"3", capi.ERR_ARG),           # no such pressure meaning
+    (6, b"-1", capi.ERR_ARG),          # negative PVT region
+    (6, b"1", capi.ERR_UNSUPPORTED),   # a second PVT region
+])
+def test_entity_meanings_are_checked_integers(field, value, want):
+    pv, gm, shape = _oracle_state("blackoil")
+    edges, verts = restart.cartesian_counts(shape)
+    inf = restart.info(edges, verts)
+    lines = restart.format_restart(inf, pv, gm).split(b"\n")
+    i = lines.index(b"Entities: Codim 0") + 1
+    f = lines[i].split(b" ")
+    f[field] = value
+    lines[i] = b" ".join(f)
+    assert restart.parse_restart(b"\n".join(lines), inf, len(pv), 3, True)[0] == want
+
+
+@pytest.mark.parametrize("line,field,value", [(0, 0, b"1e300"), (0, 5, b"2.5"), (0, 0, b"nan"),
+                                              (2, 0, b"nan"), (3, 0, b"nan"), (3, 0, b"1e300"), (3, 0, b"-1")])
+def test_simulator_and_vtk_integers_are_checked(line, field, value):
+    """Episode and time-step indices, the writer count and the meta file's
+    length must be integers in range; a bare conversion of NaN or 1e300 to
+    an integer (or a byte offset) is undefined."""
+    pv, gm, shape = _oracle_state("blackoil")
+    edges, verts = restart.cartesian_counts(shape)
+    inf = restart.info(edges, verts)
+    inf.vtk_section, inf.vtk_writer_num = 1, 2
+    lines = restart.format_restart(inf, pv, gm).split(b"\n")
+    base = lines.index(b"Simulator") + 1   # the Simulator values; +2: writer count, +3: meta length
+    k = base + line
+    f = lines[k].split(b" ")
+    f[field] = value
+    lines[k] = b" ".join(f)
+    assert restart.parse_restart(b"\n".join(lines), inf, len(pv), 3, True)[0] == capi.ERR_ARG
+
+
 @pytest.mark.parametrize("d,name,t,r", [(".", "lens", 0.0, 0), ("", "lens", 1000.0, 0), ("out", "res", 86400.0, 1),
                                         ("out/", "res", 12.5, 0), ("a/b", "x", 3.1536e7, 3),
                                         (None, "y", 1e-3, 0)])
