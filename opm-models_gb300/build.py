@@ -25,6 +25,7 @@ UNITS = {
     "gbfv.cu": [],
     "noalloc.cu": [],
     "restart.cu": [],
+    "problem.cu": [],
 }
 
 

@@ -270,6 +270,8 @@ void freeSolver(SolverData& S)
 namespace gbfv {
 // error message for gbfv_last_error from other translation units
 void setLastError(const std::string& s) { setError(s); }
+// problem.cu: consistency of a problem description (host only)
+int checkProblem(const gbfv_problem* P, int maxMaterials, int maxTable);
 }  // namespace gbfv
 
 // ===================================================================== ctx
@@ -994,18 +996,9 @@ const char* gbfv_last_error(void) { return t_lastError.c_str(); }
 
 static int createImpl(gbfv_ctx* C, const gbfv_problem* P)
 {
+    // counts, offsets, enums and tables first: everything below follows them
+    if (const int chk = gbfv::checkProblem(P, MAX_MATERIALS, GBFV_MAX_TABLE)) return chk;
     const int N = P->num_cells;
-    if (N <= 0 || !P->center || !P->volume || !P->porosity || !P->perm || !P->material || !P->conn_ptr ||
-        !P->conn_nbr || !P->conn_normal || !P->conn_center || !P->conn_area || !P->bface_ptr) {
-        setError("incomplete problem description");
-        return GBFV_ERR_ARG;
-    }
-    if (P->model != GBFV_MODEL_IMMISCIBLE_2P && P->model != GBFV_MODEL_BLACKOIL_3P) return GBFV_ERR_ARG;
-    if (P->model == GBFV_MODEL_BLACKOIL_3P && !P->pvt) return GBFV_ERR_ARG;
-    if (N > GBFV_MAX_CELLS) {
-        setError("grid larger than GBFV_MAX_CELLS (32-bit device indexing)");
-        return GBFV_ERR_UNSUPPORTED;
-    }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
         setError("no CUDA device");
@@ -1517,7 +1510,7 @@ gbfv_ctx* gbfv_create(const gbfv_problem* prob, const gbfv_params* params, int* 
     if (const char* lg = getenv("GBFV_SOLVE_LOG")) C->solveLog = lg;
     int st = GBFV_ERR_ARG;
     try {
-        st = prob ? createImpl(C, prob) : GBFV_ERR_ARG;
+        st = createImpl(C, prob);
     }
     catch (const std::bad_alloc&) {
         st = GBFV_ERR_OOM;
