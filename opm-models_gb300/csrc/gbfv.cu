@@ -2119,6 +2119,21 @@ gbfv_linsolver* gbfv_linsolver_create(int n, int b, const int32_t* rowPtr, const
         setError("more block rows than GBFV_MAX_CELLS (32-bit device indexing)");
         return fail(nullptr, GBFV_ERR_UNSUPPORTED);
     }
+    // row pointers and column indices first: everything below follows them
+    if (rowPtr[0] != 0) {
+        setError("row_ptr[0] must be 0");
+        return fail(nullptr, GBFV_ERR_ARG);
+    }
+    for (int i = 0; i < n; ++i)
+        if (rowPtr[i + 1] < rowPtr[i]) {
+            setError("row_ptr decreases at row " + std::to_string(i));
+            return fail(nullptr, GBFV_ERR_ARG);
+        }
+    for (int k = 0; k < rowPtr[n]; ++k)
+        if (col[k] < 0 || col[k] >= n) {
+            setError("column index out of range at entry " + std::to_string(k));
+            return fail(nullptr, GBFV_ERR_ARG);
+        }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(nullptr, GBFV_ERR_NO_DEVICE);
     gbfv_linsolver* L = new gbfv_linsolver();

@@ -2,7 +2,9 @@
 before it looks for a GPU: every inconsistent count, offset, enum field or
 PVT table is GBFV_ERR_ARG, with a message, and the descriptions the problem
 builders make (every variant the GPU tests, smoke() and bench.py create)
-pass it -- without a GPU they then stop at GBFV_ERR_NO_DEVICE."""
+pass it -- without a GPU they then stop at GBFV_ERR_NO_DEVICE.  The
+stand-alone linear solver checks its row pointers and column indices the
+same way."""
 import copy
 import ctypes as C
 
@@ -153,4 +155,38 @@ def test_no_flow_only_boundaries_need_no_boundary_values(built):
     p = problems.lens(nx=6, ny=4)
     p.bface_type = np.zeros_like(p.bface_type)
     st, msg = _status(p, _null("bface_value"))
+    assert st in (capi.OK, capi.ERR_NO_DEVICE), (st, msg)
+
+
+def _linsolver_status(rp, col, n=None):
+    lib = capi.load()
+    rp = np.ascontiguousarray(rp, np.int32)
+    col = np.ascontiguousarray(col, np.int32)
+    st = C.c_int(-1)
+    prm = capi.default_params()
+    h = lib.gbfv_linsolver_create(len(rp) - 1 if n is None else n, 3, capi.as_ptr(rp, C.c_int32),
+                                  capi.as_ptr(col, C.c_int32), C.byref(prm), C.byref(st))
+    if h:
+        lib.gbfv_linsolver_destroy(h)
+    return st.value, lib.gbfv_last_error().decode()
+
+
+# a 1D three-point pattern of 4 block rows
+RP = [0, 2, 5, 8, 10]
+COL = [0, 1, 0, 1, 2, 1, 2, 3, 2, 3]
+
+
+@pytest.mark.parametrize("name,rp,col", [
+    ("row_ptr starts above 0", [1, 2, 5, 8, 10], COL),
+    ("row_ptr decreases", [0, 2, 1, 8, 10], COL),
+    ("negative column", RP, [0, 1, 0, 1, 2, 1, 2, 3, 2, -3]),
+    ("column past the last row", RP, [0, 1, 0, 1, 2, 1, 2, 4, 2, 3]),
+])
+def test_linear_solver_pattern_is_checked_before_device_work(built, name, rp, col):
+    st, msg = _linsolver_status(rp, col)
+    assert st == capi.ERR_ARG, (name, st, msg)
+
+
+def test_linear_solver_valid_pattern_passes_the_checks(built):
+    st, msg = _linsolver_status(RP, COL)
     assert st in (capi.OK, capi.ERR_NO_DEVICE), (st, msg)
