@@ -1491,10 +1491,19 @@ static int createImpl(gbfv_ctx* C, const gbfv_problem* P)
 }
 
 // the local linearizer settings are one of the supported ones
-static bool linearizerOk(const gbfv_params& p)
+// the enum-valued parameters hold values of their enums
+static bool paramsOk(const gbfv_params& p)
 {
-    return (p.local_linearizer == GBFV_LIN_AD || p.local_linearizer == GBFV_LIN_FD) &&
-           p.numeric_difference_method >= -1 && p.numeric_difference_method <= 1;
+    if (p.precision != GBFV_PREC_FP64 && p.precision != GBFV_PREC_MIXED) {
+        setError("precision is neither GBFV_PREC_FP64 nor GBFV_PREC_MIXED");
+        return false;
+    }
+    if ((p.local_linearizer != GBFV_LIN_AD && p.local_linearizer != GBFV_LIN_FD) ||
+        p.numeric_difference_method < -1 || p.numeric_difference_method > 1) {
+        setError("unknown local linearizer or numeric difference method");
+        return false;
+    }
+    return true;
 }
 
 gbfv_ctx* gbfv_create(const gbfv_problem* prob, const gbfv_params* params, int* status)
@@ -1502,7 +1511,7 @@ gbfv_ctx* gbfv_create(const gbfv_problem* prob, const gbfv_params* params, int* 
     gbfv_ctx* C = new gbfv_ctx();
     if (params) C->prm = *params;
     else gbfv_default_params(&C->prm);
-    if (!linearizerOk(C->prm)) {
+    if (!paramsOk(C->prm)) {
         if (status) *status = GBFV_ERR_ARG;
         delete C;
         return nullptr;
@@ -1566,7 +1575,7 @@ int gbfv_destroy(gbfv_ctx* C)
 
 int gbfv_set_params(gbfv_ctx* C, const gbfv_params* p)
 {
-    if (!C || !p || !linearizerOk(*p)) return GBFV_ERR_ARG;
+    if (!C || !p || !paramsOk(*p)) return GBFV_ERR_ARG;
     C->prm = *p;
     return GBFV_OK;
 }
@@ -1584,6 +1593,14 @@ int gbfv_set_solution(gbfv_ctx* C, const double* pv, const int32_t* meaning)
 {
     if (!C || !pv) return GBFV_ERR_ARG;
     const int N = C->N, b = C->b;
+    // black-oil: the gas meanings the model has (BlackOilPrimaryVariables::
+    // GasMeaning without Disabled, blackoilprimaryvariables.hh:138-143)
+    if (meaning && C->model == GBFV_MODEL_BLACKOIL_3P)
+        for (int I = 0; I < N; ++I)
+            if (meaning[I] != GBFV_GAS_SG && meaning[I] != GBFV_GAS_RS && meaning[I] != GBFV_GAS_RV) {
+                setError("gas meaning of cell " + std::to_string(I) + " is not Sg, Rs or Rv");
+                return GBFV_ERR_ARG;
+            }
     std::vector<double> h((size_t)N * b);
     for (int I = 0; I < N; ++I)
         for (int e = 0; e < b; ++e) h[(size_t)C->perm[I] * b + e] = pv[(size_t)I * b + e];
@@ -2114,7 +2131,8 @@ gbfv_linsolver* gbfv_linsolver_create(int n, int b, const int32_t* rowPtr, const
         if (L) gbfv_linsolver_destroy(L);
         return nullptr;
     };
-    if (n <= 0 || (b != 2 && b != 3) || !rowPtr || !col) return fail(nullptr, GBFV_ERR_ARG);
+    if (n <= 0 || (b != 2 && b != 3) || !rowPtr || !col || (params && !paramsOk(*params)))
+        return fail(nullptr, GBFV_ERR_ARG);
     if (n > GBFV_MAX_CELLS) {
         setError("more block rows than GBFV_MAX_CELLS (32-bit device indexing)");
         return fail(nullptr, GBFV_ERR_UNSUPPORTED);
@@ -2871,7 +2889,7 @@ gbfv_batch* gbfv_batch_create(const gbfv_problem* probs, int num_systems, const 
         freeBatch(B);
         return nullptr;
     };
-    if (!probs || num_systems <= 0) return fail(nullptr, GBFV_ERR_ARG);
+    if (!probs || num_systems <= 0 || (params && !paramsOk(*params))) return fail(nullptr, GBFV_ERR_ARG);
     if (params && params->local_linearizer != GBFV_LIN_AD) {
         setError("batched systems are linearized by automatic differentiation only");
         return fail(nullptr, GBFV_ERR_UNSUPPORTED);
@@ -3047,12 +3065,13 @@ gbfv_batch* gbfv_serve_create(int capacity, int model, const gbfv_params* params
         freeBatch(B);
         return nullptr;
     };
+    if (capacity <= 0 || max_cells <= 0 || (model != GBFV_MODEL_IMMISCIBLE_2P && model != GBFV_MODEL_BLACKOIL_3P) ||
+        (params && !paramsOk(*params)))
+        return fail(nullptr, GBFV_ERR_ARG);
     if (params && params->local_linearizer != GBFV_LIN_AD) {
         setError("served systems are linearized by automatic differentiation only");
         return fail(nullptr, GBFV_ERR_UNSUPPORTED);
     }
-    if (capacity <= 0 || max_cells <= 0 || (model != GBFV_MODEL_IMMISCIBLE_2P && model != GBFV_MODEL_BLACKOIL_3P))
-        return fail(nullptr, GBFV_ERR_ARG);
     if (max_cells > GBFV_MAX_CELLS) {
         setError("max_cells above GBFV_MAX_CELLS (32-bit device indexing)");
         return fail(nullptr, GBFV_ERR_UNSUPPORTED);

@@ -190,3 +190,27 @@ def test_linear_solver_pattern_is_checked_before_device_work(built, name, rp, co
 def test_linear_solver_valid_pattern_passes_the_checks(built):
     st, msg = _linsolver_status(RP, COL)
     assert st in (capi.OK, capi.ERR_NO_DEVICE), (st, msg)
+
+
+@pytest.mark.parametrize("field,value", [("precision", 2), ("precision", -1), ("local_linearizer", 5),
+                                         ("numeric_difference_method", 2)])
+def test_enum_parameters_are_checked_by_every_create_call(built, field, value):
+    lib = capi.load()
+    prm = capi.default_params()
+    setattr(prm, field, value)
+    st = C.c_int(-1)
+    s = LENS.struct()
+    assert not lib.gbfv_create(C.byref(s), C.byref(prm), C.byref(st)) and st.value == capi.ERR_ARG
+    rp = np.ascontiguousarray(RP, np.int32)
+    col = np.ascontiguousarray(COL, np.int32)
+    st.value = -1
+    assert not lib.gbfv_linsolver_create(4, 3, capi.as_ptr(rp, C.c_int32), capi.as_ptr(col, C.c_int32),
+                                         C.byref(prm), C.byref(st))
+    assert st.value == capi.ERR_ARG
+    st.value = -1
+    assert not lib.gbfv_serve_create(2, capi.MODEL_IMMISCIBLE_2P, C.byref(prm), 0, 1000, C.byref(st))
+    assert st.value == capi.ERR_ARG
+    st.value = -1
+    arr = (capi.Problem * 1)(s)
+    assert not lib.gbfv_batch_create(arr, 1, C.byref(prm), 0, C.byref(st))
+    assert st.value == capi.ERR_ARG

@@ -93,3 +93,18 @@ def test_served_request_that_fails_leaves_the_others_unchanged(built):
         x, m = ctx.solution()
         ctx.close()
         assert np.array_equal(r.solution[0], x) and np.array_equal(r.solution[1], m)
+
+
+def test_unknown_gas_meaning_is_rejected_and_the_context_stays_usable(built):
+    import numpy as np
+
+    from gbfv import Context, capi, problems
+    prob = problems.blackoil(6, 5, 3)
+    ctx = Context(prob, capi.default_params(linear_tolerance=1e-6, newton_tolerance=1e-6))
+    bad = np.array(prob.init_meaning, np.int32, copy=True)
+    bad[7] = 3  # GasMeaning::Disabled: not a state of this model
+    with pytest.raises(Exception):
+        ctx.set_solution(prob.init_pv, bad)
+    ctx.set_solution(prob.init_pv, prob.init_meaning)
+    assert ctx.time_integration(1, 86400.0, fixed_dt=True)[0] == 0
+    ctx.close()
