@@ -219,7 +219,14 @@ typedef struct gbfv_ctx gbfv_ctx;
 /* Create a context on the current CUDA device and upload the problem.
  * Mirrors FvBaseLinearizer::init + createMatrix_ (fvbaselinearizer.hh:
  * 418-452): the sparsity pattern, level sets and block-slot maps are built
- * once here.  *status receives the result; NULL is returned on error.    */
+ * once here.  *status receives the result; NULL is returned on error.
+ * Before any device call the description is checked for consistency
+ * (offsets start at 0, do not decrease and end at their counts; enum
+ * fields, material laws, constraint rows and gas meanings are known values;
+ * arrays a used feature needs are not NULL; PVT tables of 2..32 rows with
+ * strictly increasing pressures and R_s, positive B_o and B_g) and so are
+ * the enum-valued parameters: GBFV_ERR_ARG, with gbfv_last_error() naming
+ * the field, when one fails.                                              */
 gbfv_ctx* gbfv_create(const gbfv_problem* prob, const gbfv_params* params,
                       int* status);
 int gbfv_destroy(gbfv_ctx* ctx);
@@ -230,7 +237,9 @@ int gbfv_dims(const gbfv_ctx* ctx, int* num_cells, int* block_size,
 
 /* model().solution(timeIdx) (fvbasediscretization.hh): primary variables in
  * natural order, [num_cells*b]; meanings [num_cells] (black-oil gas
- * meaning, enum gbfv_pv_meaning; ignored for the immiscible model).       */
+ * meaning, enum gbfv_pv_meaning; ignored for the immiscible model).
+ * GBFV_ERR_ARG, with nothing changed, for a black-oil gas meaning other
+ * than Sg, Rs or Rv.                                                      */
 int gbfv_set_solution(gbfv_ctx* ctx, const double* pv,
                       const int32_t* meaning);
 int gbfv_get_solution(gbfv_ctx* ctx, double* pv, int32_t* meaning);
