@@ -8,8 +8,6 @@ is missing, :func:`load` raises -- there is no CPU fallback.
 import ctypes as C
 import os
 
-import numpy as np
-
 PKG_ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(PKG_ROOT, "_build", "libgbfv.so")
 
