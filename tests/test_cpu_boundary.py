@@ -115,3 +115,16 @@ def test_sizes_beyond_32bit_device_indexing_are_rejected_before_device_work(buil
     assert st.value == capi.ERR_UNSUPPORTED
     f = lib.gbfv_footprint_bytes
     assert f(capi.MAX_CELLS, 3, 3) > 0 and f(capi.MAX_CELLS + 1, 3, 3) == -1
+
+
+def test_integration_guide_python_blocks_run(built):
+    """The Python snippets of INTEGRATION.md bind the library as written
+    (run from the repository root, as the guide assumes)."""
+    import re
+    import sys
+    with open(os.path.join(ROOT, "INTEGRATION.md")) as f:
+        blocks = re.findall(r"```python\n(.*?)```", f.read(), re.S)
+    assert blocks
+    for code in blocks:
+        r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=120)
+        assert r.returncode == 0, code + r.stderr
