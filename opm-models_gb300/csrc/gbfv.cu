@@ -1446,9 +1446,9 @@ static int createImpl(gbfv_ctx* C, const gbfv_problem* P)
     CK(cudaMemset(C->wasSwitched, 0, sizeof(int) * N));
     CK(cudaMemset(C->x, 0, sizeof(double) * nb));
     CK(cudaMemset(C->xOld, 0, sizeof(double) * nb));
-    const int nv = b == 2 ? 6 : 11;
-    const int nd = b == 2 ? 12 : 30;
-    const int ns = b * (b + 1);
+    const int nv = iqValuePlanes(b);
+    const int nd = iqDerivPlanes(b);
+    const int ns = iqStoragePlanes(b);
     if ((st = devAlloc(&C->iq.val, (size_t)nv * ld)) || (st = devAlloc(&C->iq.der, (size_t)nd * ld)) ||
         (st = devAlloc(&C->iq.sto, (size_t)ns * ld)))
         return st;
@@ -1481,7 +1481,7 @@ static int createImpl(gbfv_ctx* C, const gbfv_problem* P)
     // algorithmic bytes per cell of the IQ + assembly passes
     {
         const double s8 = 8.0;
-        const double iqv = (b == 2 ? 6 : 11), iqd = (b == 2 ? 12 : 30), iqs = b * (b + 1);
+        const double iqv = iqValuePlanes(b), iqd = iqDerivPlanes(b), iqs = iqStoragePlanes(b);
         const double k1 = b * s8 + 8 + 4 + (b == 3 ? 4 : 0) + (iqv + iqd + iqs) * s8;
         const double k2 = (iqv + iqd + iqs) * s8 + ndir * (4 + 5 * s8) + 8 + 4 + b * s8 + b * s8 +
                           nslot * b * b * s8;
@@ -1664,7 +1664,7 @@ static int ensureFd(gbfv_ctx* C)
 {
     if (C->fdX[0]) return GBFV_OK;
     const int b = C->b;
-    const size_t ld = C->ldN, nv = b == 2 ? 6 : 11, nd = b == 2 ? 12 : 30, ns = (size_t)b * (b + 1);
+    const size_t ld = C->ldN, nv = iqValuePlanes(b), nd = iqDerivPlanes(b), ns = iqStoragePlanes(b);
     int st;
     for (int k = 0; k < b; ++k)
         for (IqBuffers* q : {&C->fd.plus[k], &C->fd.minus[k]})
@@ -3049,7 +3049,7 @@ int64_t gbfv_footprint_bytes(int num_cells, int block_size, int dim)
     if (num_cells <= 0 || num_cells > GBFV_MAX_CELLS || (block_size != 2 && block_size != 3) || (dim != 2 && dim != 3))
         return -1;
     const int64_t b = block_size, bb = b * b, ns = 2 * dim + 1, nd = 2 * dim;
-    const int64_t iq = (b == 2 ? 6 + 12 : 11 + 30) + b * (b + 1);
+    const int64_t iq = iqValuePlanes((int)b) + iqDerivPlanes((int)b) + iqStoragePlanes((int)b);
     // solver: FP64 + FP32 factors, FP32 matrix, Krylov vectors, columns, push tables
     const int64_t solver = dim * bb * 12 + bb * 12 + ns * bb * 4 + 6 * b * 8 + 7 * b * 4 + 2 * b * 8 + ns * 4 + 6 * 4;
     // context: state vectors, Jacobian, IQ buffers, mesh (faces, cells), snapshot

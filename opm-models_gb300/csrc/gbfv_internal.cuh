@@ -104,6 +104,14 @@ struct IqBuffers {
     double* sto;   // [(e*(b+1) + k)*ldN + p], k = 0 value, 1..b derivatives
 };
 
+// planes of each IqBuffers array for b equations: the immiscible IQ kernel
+// writes 6 values and 6 quantities with 2 derivatives, the black-oil one
+// 11 values and 10 quantities with 3 derivatives; storage is one value and
+// b derivatives per equation
+constexpr int iqValuePlanes(int b) { return b == 2 ? 6 : 11; }
+constexpr int iqDerivPlanes(int b) { return b == 2 ? 12 : 30; }
+constexpr int iqStoragePlanes(int b) { return b * (b + 1); }
+
 // finite-difference linearizer: intensive quantities of the deflected
 // states, per primary variable (+eps and the second, minus state)
 struct FdIq {
