@@ -442,6 +442,12 @@ int gbfv_batch_time_integration(gbfv_batch* batch, int num_steps, double dt0,
  * the device limit) and keeps the fastest; the systems' states are not
  * changed.  ms[k] = the solve time of candidate k (up to 8)              */
 int gbfv_batch_autotune(gbfv_batch* batch, double dt, int* cluster_size, double* ms, int* num_candidates);
+/* system i's last time integration: its status, the steps it completed
+ * (*steps_done, at most the num_steps of that gbfv_batch_time_integration
+ * call, or the steps of a served request) and per completed step its dt,
+ * Newton and linear iterations, written to arrays of at least *steps_done
+ * entries; any output may be NULL (a first call with NULL arrays gives the
+ * count)                                                                  */
 int gbfv_batch_system_report(const gbfv_batch* batch, int i, int* status, int* steps_done,
                              double* step_dt, int32_t* step_newton, int32_t* step_linear,
                              int* linearizations);

@@ -252,14 +252,19 @@ class Batch:
         capi.check(self.lib.gbfv_batch_autotune(self.h, dt, C.byref(c), _d(ms), C.byref(n)), "gbfv_batch_autotune")
         return c.value, ms[:n.value].copy()
 
-    def report(self, i, max_steps=4096):
+    def report(self, i):
+        """Status, per-step dt / Newton / linear iterations and the number of
+        linearizations of system i's last time integration."""
         st, n, nl = C.c_int(), C.c_int(), C.c_int()
-        sdt = np.zeros(max_steps)
-        sn = np.zeros(max_steps, np.int32)
-        sl = np.zeros(max_steps, np.int32)
+        # the step count first, then arrays of exactly that many entries
+        capi.check(self.lib.gbfv_batch_system_report(self.h, i, None, C.byref(n), None, None, None, None),
+                   "gbfv_batch_system_report")
+        k = n.value
+        sdt = np.zeros(max(k, 1))
+        sn = np.zeros(max(k, 1), np.int32)
+        sl = np.zeros(max(k, 1), np.int32)
         capi.check(self.lib.gbfv_batch_system_report(self.h, i, C.byref(st), C.byref(n), _d(sdt), _i(sn), _i(sl),
                                                      C.byref(nl)), "gbfv_batch_system_report")
-        k = n.value
         return st.value, sdt[:k].copy(), sn[:k].copy(), sl[:k].copy(), nl.value
 
     def stats(self):
