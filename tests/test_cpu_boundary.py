@@ -128,3 +128,31 @@ def test_integration_guide_python_blocks_run(built):
     for code in blocks:
         r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=120)
         assert r.returncode == 0, code + r.stderr
+
+
+def test_batch_report_sizes_its_arrays_from_the_step_count():
+    """Batch.report asks for the step count first (NULL arrays) and then
+    reads exactly that many steps, however many there are."""
+    import gbfv
+
+    class FakeLib:
+        def __init__(self, steps):
+            self.steps, self.calls = steps, []
+
+        def gbfv_batch_system_report(self, h, i, st, n, sdt, sn, sl, nl):
+            self.calls.append(sdt is None)
+            n._obj.value = self.steps
+            if sdt is not None:
+                for k in range(self.steps):
+                    sdt[k], sn[k], sl[k] = 0.5 * k, k % 7, 3 * k
+                st._obj.value, nl._obj.value = 0, self.steps + 2
+            return 0
+
+    for steps in (0, 3, 5000):
+        b = object.__new__(gbfv.Batch)
+        b.lib, b.h = FakeLib(steps), 1
+        st, sdt, sn, sl, nl = b.report(0)
+        assert b.lib.calls == [True, False]
+        assert st == 0 and nl == steps + 2 and len(sdt) == len(sn) == len(sl) == steps
+        assert np.array_equal(sdt, 0.5 * np.arange(steps)) and np.array_equal(sl, 3 * np.arange(steps))
+        b.h = None
