@@ -367,7 +367,8 @@ int gbfv_get_kernel_stats(const gbfv_ctx* ctx, gbfv_kernel_stats* out);
 /* launch configuration the autotuner chose for the persistent solve kernel
  * of a precision (GBFV_PREC_FP64 / GBFV_PREC_MIXED): cluster (mode 1),
  * cooperative grid (mode 0) or hybrid (mode 2), possibly with
- * GBFV_SOLVER_TILES, blocks, and the candidate timings [ms]               */
+ * GBFV_SOLVER_TILES, blocks, and the candidate timings [ms] in tune_ms
+ * (room for 16; *num_tuned of them are written; any output may be NULL)  */
 int gbfv_solver_config(const gbfv_ctx* ctx, int precision, int* mode, int* blocks,
                        double* tune_ms, int* num_tuned);
 /* fix the launch configuration of the persistent solve kernel of a
