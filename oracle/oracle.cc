@@ -55,6 +55,8 @@ struct NumericalProblem : std::runtime_error {
     NumericalProblem(const char* m, int c = GBFV_ERR_NUMERICAL) : std::runtime_error(m), code(c) {}
 };
 
+// entry-wise harmonic mean of the two cells' K
+// (MultiPhaseBaseProblem::intersectionIntrinsicPermeability, multiphasebaseproblem.hh:109-125)
 static double harmonicMean(double x, double y)
 {
     if (x * y <= 0) return 0.0;
@@ -207,6 +209,8 @@ struct IQ3 {
     double phi;
 };
 
+// Corey k_r = S^n, supplied through the problem's updateRelperms hook
+// (blackoilintensivequantities.hh:262, multiphasebaseproblem.hh:256-261)
 template <class E>
 static E corey(const E& S, double n)
 {
@@ -448,6 +452,8 @@ static void buildPattern(Sim& S)
     }
 }
 
+// constrained cells take their prescribed primary variables
+// (FvBaseLinearizer::applyConstraintsToSolution_, fvbaselinearizer.hh:630-645)
 static void applyConstraintsToSolution(Sim& S)
 {
     for (int I = 0; I < S.N; ++I) {
@@ -462,6 +468,9 @@ static void applyConstraintsToSolution(Sim& S)
     }
 }
 
+// an element's residual and derivative columns into the global system:
+// residual_[globI] += ..., jacobian_->addToBlock(globJ, globI, ...)
+// (FvBaseLinearizer::linearizeElement_, fvbaselinearizer.hh:595-626)
 template <int B>
 static void scatterElement(Sim& S, int I, const Dual<B>* resI, const std::vector<Dual<B>>& resJ)
 {
@@ -705,6 +714,7 @@ static void elementBlackoil(Sim& S, int I, const IQ3& qi, const std::vector<IQ3>
 }
 
 // one element of FvBaseAdLocalLinearizer::linearize + scatter, per model
+// (fvbaseadlocallinearizer.hh:173-292, fvbaselinearizer.hh:510-593)
 static void linearizeImmiscible(Sim& S, const std::vector<IQ2>& iq)
 {
     const bool iter0 = S.newtonIter == 0;
@@ -719,6 +729,8 @@ static void linearizeImmiscible(Sim& S, const std::vector<IQ2>& iq)
     }
 }
 
+// the black-oil element loop (fvbaseadlocallinearizer.hh:173-292,
+// fvbaselinearizer.hh:510-593)
 static void linearizeBlackoil(Sim& S, const std::vector<IQ3>& iq)
 {
     const bool iter0 = S.newtonIter == 0;
@@ -814,6 +826,8 @@ static void linearizeFd(Sim& S, const std::vector<IQ>& iq, IqFn iqOf, ElemFn ele
     }
 }
 
+// constrained rows: zero residual, identity diagonal, no off-diagonal blocks
+// (FvBaseLinearizer::applyConstraintsToLinearization_, fvbaselinearizer.hh:649-666)
 static void applyConstraintsToLinearization(Sim& S)
 {
     const int b = S.b;
@@ -829,6 +843,8 @@ static void applyConstraintsToLinearization(Sim& S)
     }
 }
 
+// FvBaseLinearizer::linearizeDomain / linearize_ (fvbaselinearizer.hh:201-241,
+// 510-593): constraints, intensive quantities, element loop, constraints
 static void linearize(Sim& S)
 {
     applyConstraintsToSolution(S);
@@ -863,6 +879,9 @@ static void linearize(Sim& S)
 
 // ------------------------------------------------------ linear solver -----
 // block helpers (row-major b x b)
+// pivot inverse: MatrixBlock's invertMatrix (matrixblock.hh:40-66), which
+// calls dune-common's FMatrixHelp::invertMatrix for 2x2 and 3x3 blocks
+// (not vendored; the cofactor formula restated)
 static void blockInvert(int b, double* A)
 {
     // adjugate / determinant
@@ -893,7 +912,8 @@ static void blockInvert(int b, double* A)
     A[7] = (a01 * a20 - a00 * a21) * id;
     A[8] = (a00 * a11 - a01 * a10) * id;
 }
-// A = A * M
+// A = A * M (dune-common FieldMatrix::rightmultiply, used by dune-istl's
+// block ILU(0) on the blocks istlpreconditionerwrappers.hh:161 hands it)
 static void rightMultiply(int b, double* A, const double* M)
 {
     double C[9];
@@ -905,7 +925,8 @@ static void rightMultiply(int b, double* A, const double* M)
             A[i * b + j] = s;
         }
 }
-// y -= A x
+// y -= A x (dune-common FieldMatrix::mmv, as dune-istl's ILU back-solve
+// uses it on the same blocks)
 static void mmv(int b, const double* A, const double* x, double* y)
 {
     for (int i = 0; i < b; ++i)
@@ -948,7 +969,8 @@ static void ilu0Factor(const Bcrs& A, std::vector<double>& F)
     }
 }
 
-// dune-istl blockILUBacksolve: v = (LU)^-1 d
+// dune-istl blockILUBacksolve: v = (LU)^-1 d, the apply of Dune::SeqILU that
+// PreconditionerWrapperILU wraps (istlpreconditionerwrappers.hh:149-180)
 static void ilu0Apply(const Bcrs& A, const std::vector<double>& F, std::vector<double>& v, const std::vector<double>& d)
 {
     const int b = A.b, bb = b * b;
@@ -973,7 +995,8 @@ static void ilu0Apply(const Bcrs& A, const std::vector<double>& F, std::vector<d
     }
 }
 
-// y = A x (BCRSMatrix::mv)
+// y = A x (BCRSMatrix::mv through OverlappingOperator::apply,
+// overlappingoperator.hh:58-63)
 static void spmv(const Bcrs& A, const std::vector<double>& x, std::vector<double>& y)
 {
     const int b = A.b, bb = b * b;
@@ -989,6 +1012,8 @@ static void spmv(const Bcrs& A, const std::vector<double>& x, std::vector<double
     }
 }
 
+// OverlappingScalarProduct::dot (overlappingscalarproduct.hh:58-70) on one
+// rank: the plain sum over all entries
 static double dot(const std::vector<double>& a, const std::vector<double>& b, int bs)
 {
     double s = 0;
@@ -1001,6 +1026,9 @@ static double dot(const std::vector<double>& a, const std::vector<double>& b, in
     return s;
 }
 
+// CombinedCriterion (combinedcriterion.hh:55-209): max-norm residual
+// reduction or absolute residual, divergence above maxRes; setInitial
+// :116-129, update :131-135, converged :137-144
 struct Criterion {
     double redTol, absTol, maxRes;
     double resErr = 0, initErr = 0, lastErr = 0;
@@ -1095,6 +1123,9 @@ static bool bicgstab(const Bcrs& A, const std::vector<double>& F, const std::vec
     return false;
 }
 
+// the criterion's parameters as ParallelBiCGStabSolverBackend::prepareSolver_
+// sets them (parallelbicgstabbackend.hh:136-146): an absolute tolerance
+// below 0 becomes the Newton tolerance / 100
 static Criterion makeCriterion(const gbfv_params& prm)
 {
     Criterion c;
@@ -1105,6 +1136,8 @@ static Criterion makeCriterion(const gbfv_params& prm)
 }
 
 // ------------------------------------------------------------ Newton ------
+// NewtonMethod::preSolve_ (newtonmethod.hh:572-607): max |r| over the
+// unconstrained cells of positive volume
 static double newtonError(const Sim& S)
 {
     double err = 0;
@@ -1119,6 +1152,7 @@ static double newtonError(const Sim& S)
 static double signum(double v) { return (v > 0) - (v < 0); }
 
 // BlackOilPrimaryVariables::adaptPrimaryVariables for Sw / Po / {Sg, Rs}
+// (blackoilprimaryvariables.hh:549-909)
 static bool adaptPrimaryVariables(const Sim& S, double* pv, int& meaning, double eps)
 {
     const gbfv_params& prm = S.prm;
@@ -1216,6 +1250,9 @@ static int newtonUpdate(Sim& S, const std::vector<double>& cur, const std::vecto
     return switched;
 }
 
+// ParallelBaseBackend::prepare / setResidual / setMatrix / solve
+// (parallelbasebackend.hh:182-284): the system copied into the solver's
+// own storage, then the BiCGStab loop below on it
 static int solveLinear(Sim& S, int& iters)
 {
     std::vector<double> F;
@@ -1292,6 +1329,8 @@ static bool newtonApply(Sim& S, double dt, gbfv_newton_report& rep)
     return true;
 }
 
+// NewtonMethod::suggestTimeStepSize (newtonmethod.hh:448-465): grow or
+// shrink towards the target iteration count, damped
 static double suggestTimeStep(const Sim& S, double oldDt)
 {
     const int target = S.prm.newton_target_iterations;
@@ -1308,6 +1347,8 @@ static double suggestTimeStep(const Sim& S, double oldDt)
 
 using namespace oracle;
 
+// C ABI of the oracle: the entry points of include/gbfv.h with an oracle_
+// prefix; the header's comments name the reference function each mirrors
 extern "C" {
 
 void oracle_default_params(gbfv_params* p)
