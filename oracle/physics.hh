@@ -75,6 +75,9 @@ struct TwoPhaseLaw {
     }
 
     // p_c,nw as a function of the effective wetting saturation
+    // (opm-common RegularizedVanGenuchten / RegularizedBrooksCorey ::
+    // twoPhaseSatPcnw; the law and its parameters: lensproblem.hh:111-121,
+    // 245-258)
     template <class E>
     E pcnw(const E& Sw) const
     {
@@ -92,6 +95,8 @@ struct TwoPhaseLaw {
         if (Sw >= 1.0) return pe + bcSlopeHigh * (Sw - 1.0);
         return pe * pow(Sw, -1.0 / lambda);
     }
+    // wetting relative permeability: Mualem (van Genuchten) or Burdine
+    // (Brooks-Corey), opm-common's twoPhaseSatKrw, clamped outside (0, 1)
     template <class E>
     E krw(const E& Sw) const
     {
@@ -103,6 +108,7 @@ struct TwoPhaseLaw {
         }
         return pow(Sw, 2.0 / lambda + 3.0);
     }
+    // non-wetting relative permeability (opm-common twoPhaseSatKrn);
     // argument: 1 - S_n,eff (the reference evaluates krn through Sw = 1 - Sn)
     template <class E>
     E krn(const E& Sw) const
@@ -117,6 +123,8 @@ struct TwoPhaseLaw {
 
 // ----------------------------------------------------------- tables ------
 // piecewise-linear table with linear extrapolation on the end segments
+// (opm-common Tabulated1DFunction::eval with extrapolation, as the live-oil
+// and dry-gas PVT of reservoirproblem.hh:223-305 use it)
 struct Table1D {
     std::vector<double> x, y;
     int segment(double xv) const
@@ -151,6 +159,8 @@ struct BlackOilPvt {
     Table1D mug;        // p -> mu_g
     double pwRef = 1.01325e5, bwRef = 1.0, cw = 0, muw = 1e-3;
 
+    // ConstantCompressibilityWaterPvt::inverseFormationVolumeFactor, the
+    // second-order expansion of exp(X) (reservoirproblem.hh:306-312)
     template <class E>
     E waterInvB(const E& p) const
     {
@@ -159,7 +169,9 @@ struct BlackOilPvt {
     }
     // saturated branch when gas is present and Rs is at saturation
     // (BlackOilFluidSystem::inverseFormationVolumeFactor), else the
-    // undersaturated extension through the bubble-point pressure
+    // undersaturated extension through the bubble-point pressure (LiveOilPvt
+    // set up from saturated tables only, reservoirproblem.hh:297-304; the
+    // extension's form is a row of oracle/UNPINNED.md)
     template <class E>
     void oil(const E& p, const E& Rs, bool saturated, E& invB, E& mu) const
     {
