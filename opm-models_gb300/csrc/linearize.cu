@@ -39,6 +39,7 @@ __device__ __forceinline__ void kApplyConstraintsBody(const DevMesh& m, double* 
     meaningOld[p] = m.consMeaning[c];
 }
 
+// FvBaseLinearizer::applyConstraintsToSolution_ (fvbaselinearizer.hh:630-645)
 __global__ void kApplyConstraints(DevMesh m, double* __restrict__ x, double* __restrict__ xOld,
                                   int* __restrict__ meaning, int* __restrict__ meaningOld)
 {
@@ -103,6 +104,8 @@ __device__ __forceinline__ void kIqImmiscibleBody(const DevMesh& m, const DevPhy
     }
 }
 
+// ImmiscibleIntensiveQuantities::update (immiscibleintensivequantities.hh:93-151)
+// and the storage term (immisciblelocalresidual.hh:99-109), once per cell
 __global__ void __launch_bounds__(256) kIqImmiscible(DevMesh m, const DevPhysics* __restrict__ phys,
                                                      const double* __restrict__ x, IqBuffers iq)
 {
@@ -185,6 +188,8 @@ __device__ __forceinline__ void kIqBlackoilBody(const DevMesh& m, const DevPhysi
     }
 }
 
+// BlackOilIntensiveQuantities::update (blackoilintensivequantities.hh:179-470)
+// and the storage term (blackoillocalresidual.hh:102-188), once per cell
 __global__ void __launch_bounds__(256) kIqBlackoil(DevMesh m, const DevPhysics* __restrict__ phys,
                                                    const double* __restrict__ x,
                                                    const int* __restrict__ meaning, IqBuffers iq)
@@ -425,6 +430,9 @@ __device__ __forceinline__ void kAssembleImmiscibleBody(const DevMesh& m, const 
     writeDiag<2>(m, res, residual, jval, p);
 }
 
+// one element per thread: FvBaseAdLocalLinearizer::linearize
+// (fvbaseadlocallinearizer.hh:173-292) and its scatter
+// (FvBaseLinearizer::linearizeElement_, fvbaselinearizer.hh:595-626)
 __global__ void __launch_bounds__(128) kAssembleImmiscible(DevMesh m, const DevPhysics* __restrict__ phys,
                                                            IqBuffers iq, double* __restrict__ storageOld,
                                                            int iter0, double dt,
@@ -526,6 +534,8 @@ __device__ __forceinline__ void kAssembleBlackoilBody(const DevMesh& m, const De
     writeDiag<3>(m, res, residual, jval, p);
 }
 
+// the black-oil element (fvbaseadlocallinearizer.hh:173-292,
+// fvbaselinearizer.hh:595-626)
 __global__ void __launch_bounds__(128) kAssembleBlackoil(DevMesh m, const DevPhysics* __restrict__ phys,
                                                          IqBuffers iq, double* __restrict__ storageOld,
                                                          int iter0, double dt,
@@ -595,7 +605,8 @@ void launchSetRefPressure(const double* x, int idx, double* refP, cudaStream_t s
 
 // deflected copy of the state: primary variable pv of every cell moved by
 // +eps (dir > 0), from +eps back by eps + eps (dir == 0, central), or by
-// -(0 + eps) (dir < 0, backward)
+// -(0 + eps) (dir < 0, backward) -- FvBaseFdLocalLinearizer's deflections
+// (fvbasefdlocallinearizer.hh:425-455) for all elements at once
 __global__ void __launch_bounds__(256) kFdDeflect(DevMesh m, int b, const double* __restrict__ x,
                                                   const int* __restrict__ meaning, const double* __restrict__ refP,
                                                   int pv, int dir, double* __restrict__ xd)
@@ -705,6 +716,8 @@ __device__ __forceinline__ void fdElement(const DevMesh& m, const FdIq& fd, IqBu
     }
 }
 
+// one element per thread: FvBaseFdLocalLinearizer::linearize
+// (fvbasefdlocallinearizer.hh:236-510) and the scatter (fvbaselinearizer.hh:595-626)
 __global__ void __launch_bounds__(128) kAssembleFdImmiscible(DevMesh m, IqBuffers iq0, FdIq fd,
                                                              const int* __restrict__ meaning,
                                                              const double* __restrict__ refP, int method,
@@ -790,6 +803,7 @@ void launchNewtonError(const DevMesh& m, const double* residual, DevStatus* st, 
 }
 
 // NewtonMethod::update_ guard: a non-finite update aborts the step
+// (newtonmethod.hh:677-678)
 __global__ void kCheckUpdate(int n, const double* __restrict__ dx, DevStatus* st)
 {
     int bad = 0;
@@ -905,6 +919,9 @@ __device__ __forceinline__ int kNewtonUpdateCell(const DevMesh& m, const DevPhys
     return sw;
 }
 
+// NewtonMethod::updatePrimaryVariables_ (newtonmethod.hh:723-731) for the
+// immiscible model; BlackOilNewtonMethod::updatePrimaryVariables_
+// (blackoilnewtonmethod.hh:226-427) with chopping and switching for black-oil
 __global__ void kNewtonUpdate(DevMesh m, const DevPhysics* __restrict__ phys, const double* __restrict__ dx,
                               double* __restrict__ x, int* __restrict__ meaning,
                               int* __restrict__ wasSwitched, UpdateParams prm, DevStatus* st)

@@ -63,6 +63,8 @@ __device__ unsigned long long blockMaxBits(unsigned long long bits)
     return b;
 }
 
+// NewtonMethod::preSolve_'s error (newtonmethod.hh:572-607): per block the
+// max |r| over the cells the caller does not skip, as a bit pattern
 __global__ void __launch_bounds__(NOALLOC_THREADS) kNewtonErrorPartials(const double* __restrict__ r,
                                                                           const int32_t* __restrict__ skip, int n,
                                                                           int b, NoAllocScratch* scr)
@@ -83,6 +85,7 @@ __global__ void __launch_bounds__(NOALLOC_THREADS) kNewtonErrorPartials(const do
     if (threadIdx.x == 0) scr->partial[blockIdx.x] = bits;
 }
 
+// the blocks' maxima combined into the error (newtonmethod.hh:572-607)
 __global__ void __launch_bounds__(NOALLOC_THREADS) kNewtonErrorCombine(int nblocks, NoAllocScratch* scr)
 {
     unsigned long long bits = 0;

@@ -1630,6 +1630,9 @@ timeout:
     if (gt == 0) a.st->code = GBFV_ERR_TIMEOUT;
 }
 
+// one linear solve in one launch: Dune::SeqILU<...,0> set-up
+// (istlpreconditionerwrappers.hh:151-190) and BiCGStabSolver::apply
+// (bicgstabsolver.hh:120-330) with CombinedCriterion (combinedcriterion.hh:116-144)
 template <class T, int B, int MODE, int NT>
 __global__ void __launch_bounds__(NT, 1) kBicgstab(KArgs<T> a)
 {
@@ -1956,7 +1959,9 @@ template int launchBicgstabBatch<float>(const KArgs<float>*, const int*, const i
 template int maxActiveClusters<double>(int, int);
 template int maxActiveClusters<float>(int, int);
 
-// A32 = (float) A64 over all slots
+// A32 = (float) A64 over all slots: ParallelBaseBackend::setMatrix's copy of
+// the Jacobian into the solver's own matrix (parallelbasebackend.hh:241-250),
+// in the mixed form's FP32 solver scalar
 __global__ void kCastMatrix(const double* __restrict__ src, float* __restrict__ dst, long n)
 {
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
@@ -1971,7 +1976,8 @@ void launchCastMatrix(const double* src, float* dst, long n, cudaStream_t s)
     countLaunch();
 }
 
-// x64 += d32
+// x64 += d32: a step of the mixed form's outer iterative refinement (this
+// project's; the reference solves in one precision)
 __global__ void kAccumulate(int n, double* __restrict__ x, const float* __restrict__ d)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -2025,6 +2031,9 @@ __device__ __forceinline__ void warpMaxToStatus(double mx, DevStatus* st)
     if ((threadIdx.x & 31) == 0) atomicMax(&st->errorBits, bits);
 }
 
+// FP64 true residual b - A x of the outer refinement, with the max-norm the
+// refinement's stop test uses (the same norm as CombinedCriterion's,
+// combinedcriterion.hh:116-144)
 template <int B>
 __global__ void kResidual64(int N, int ld, int nslot, const int* __restrict__ col,
                             const double* __restrict__ A, const double* __restrict__ b,
