@@ -576,25 +576,32 @@ def run_ensemble(args):
         dist.destroy_process_group()
         return 0
     newton = [B.report(i)[2].tolist() for i in range(len(probs))]
-    # one at a time: a sample of the same systems through single contexts
+    # one at a time: a sample of the same systems through single contexts,
+    # in the mixed form and in the plain FP64 form
     sample = list(range(0, len(probs), max(1, len(probs) // 8)))[:8]
     B.close()
-    one_ms, one_cits = 0.0, 0
-    for i in sample:
-        ctx = Context(probs[i], prm)
-        ctx.time_integration(ENSEMBLE["steps"], ENSEMBLE["dt"])  # warm-up incl. autotuning
-        ctx.set_solution(probs[i].init_pv, probs[i].init_meaning)
-        ext1 = torch.cuda.ExternalStream(ctx.stream())
-        torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(ext1)
-        st, sdt, sn, sl, tl = ctx.time_integration(ENSEMBLE["steps"], ENSEMBLE["dt"])
-        e1.record(ext1)
-        e1.synchronize()
-        one_ms += e0.elapsed_time(e1)
-        one_cits += int(sn.sum()) * probs[i].num_cells
-        ctx.close()
+
+    def one_at_a_time(prm1):
+        ms, cits = 0.0, 0
+        for i in sample:
+            ctx = Context(probs[i], prm1)
+            ctx.time_integration(ENSEMBLE["steps"], ENSEMBLE["dt"])  # warm-up incl. autotuning
+            ctx.set_solution(probs[i].init_pv, probs[i].init_meaning)
+            ext1 = torch.cuda.ExternalStream(ctx.stream())
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(ext1)
+            st, sdt, sn, sl, tl = ctx.time_integration(ENSEMBLE["steps"], ENSEMBLE["dt"])
+            e1.record(ext1)
+            e1.synchronize()
+            ms += e0.elapsed_time(e1)
+            cits += int(sn.sum()) * probs[i].num_cells
+            ctx.close()
+        return cits / (ms / 1000.0)
+
+    one_value = one_at_a_time(prm)
+    one_fp64 = one_at_a_time(params(capi.PREC_FP64))
     peak, peak_kind = load_peaks()
     solve_ms = s1["solve_ms"] - s0["solve_ms"]
     solve_bytes = s1["solve_bytes"] - s0["solve_bytes"]
@@ -622,8 +629,10 @@ def run_ensemble(args):
                   "rounds_per_step": (s1["rounds"] - s0["rounds"]) / args.steps,
                   "graph_launches_per_step": (s1["graph_launches"] - s0["graph_launches"]) / args.steps,
                   "build_s": t_build, "create_s": t_create},
-        "one_at_a_time": {"value": one_cits / (one_ms / 1000.0), "systems_sampled": len(sample)},
-        "batched_over_one_at_a_time": (value / world) / (one_cits / (one_ms / 1000.0)),
+        "one_at_a_time": {"value": one_value, "systems_sampled": len(sample)},
+        "one_at_a_time_plain_fp64": {"value": one_fp64, "systems_sampled": len(sample)},
+        "batched_over_one_at_a_time": (value / world) / one_value,
+        "batched_mixed_over_plain_fp64": (value / world) / one_fp64,
         "gpu_launches": int((s1["kernel_launches"] - s0["kernel_launches"]) / args.steps),
         "newton_iterations_first_systems": newton[:4],
         "roofline": {"bound": "hbm", "kernel": "kBicgstabBatch<float,2> (batched persistent ILU0 + BiCGStab)",
