@@ -508,7 +508,9 @@ def run_ensemble(args):
     (one launch per phase, one persistent solve launch per round, captured
     CUDA graphs).  value = sum over systems of Newton iterations x cells /
     device time of the whole batch; one_at_a_time = the same systems solved
-    one after another through single contexts (a sample of them)."""
+    one after another through single contexts (a sample of them), in the
+    mixed form and (one_at_a_time_plain_fp64) in plain FP64, whose ratio to
+    the batched value is batched_mixed_over_plain_fp64."""
     rank, world, local = dist_env()
     t0 = time.time()
     probs = ensemble_problems(args.ensemble, rank, world)  # before any CUDA call (spawned pool)
