@@ -1,6 +1,6 @@
 // ORACLE -- test infrastructure only.  Only tests/, __graft_entry__.smoke()
 // and bench.py's cpu_baseline / reference legs may load or run anything
-// under oracle/.  It is the checker, never the product path.
+// under oracle/.  It checks the product; it is never the product path.
 //
 // Forward-mode dual numbers restating the semantics of opm-common's
 // DenseAd::Evaluation (used by the reference through

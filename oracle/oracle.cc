@@ -1,6 +1,6 @@
 // ORACLE -- test infrastructure only.  Only tests/, __graft_entry__.smoke()
 // and bench.py's cpu_baseline / reference legs may load or run this
-// library.  It is the checker, never the product path.
+// library.  It checks the product; it is never the product path.
 //
 // CPU restatement (C++17, no dependencies) of the reference's hot path.
 // Parity status: UNPINNED against the reference's own output -- the

@@ -1,7 +1,7 @@
 """ORACLE -- test infrastructure only.
 
-Pure-Python restatement of the reference's restart file text (the checker
-of gbfv_format_restart / gbfv_parse_restart).  Only tests/ may import it.
+Pure-Python restatement of the reference's restart file text (the oracle
+for gbfv_format_restart / gbfv_parse_restart).  Only tests/ may import it.
 Parity status: unpinned against files written by the reference (it cannot
 be built here); the layout follows the reference's source text:
 
