@@ -784,8 +784,8 @@ int fillKArgs(SolverData& S, DevStatus* st, const T* A, T* FL, T* FD, const T* r
         if (mode == SYNC_HYBRID && !a.dsmem) return GBFV_ERR_UNSUPPORTED;  // the hybrid sweeps need the push tables
         // two level groups where they fit (each group must cover a block's share
         // of the widest level): staging one level ahead hides the operand loads;
-        // more groups were measured slower (C2 hybrid solve: 2 groups 135.4 ms,
-        // 4 groups 137.7 ms, 1 group 175.7 ms)
+        // more groups were measured slower (hybrid solve of the 100x100x20
+        // black-oil grid: 2 groups 135.4 ms, 4 groups 137.7 ms, 1 group 175.7 ms)
         a.grp = maxChunk <= NTC / 2 ? 2 : 1;
         if (const char* e = getenv("GBFV_GROUPS")) a.grp = std::max(1, std::min(a.grp, atoi(e)));
         a.pushL = a.pushU = a.levVals = nullptr;

@@ -1,17 +1,19 @@
-"""Generate the full-size fixture c2_newton_log.npz with the oracle.
+"""Generate the full-size fixture blackoil_100x100x20_newton_log.npz with
+the oracle.
 
-Workload C2 (blackoil-100x100x20: 200k cells, 10 time steps of one day,
+Workload blackoil-100x100x20 (200k cells, 10 time steps of one day,
 BiCGStab + ILU(0) to 1e-6, Newton tolerance 1e-6, FP64): the oracle's
 Newton and linear iteration counts per step, and the final primary
 variables of every 997th cell (natural order) with their meanings.  The GPU
 test (tests/test_gpu_full_size.py) reruns the workload and compares.
-A second log, c2_tight_log.npz, is the first two steps with tight solves
-(linear tolerance 1e-10, Newton tolerance 1e-8): with the benchmark's 1e-6
+A second log, blackoil_100x100x20_tight_log.npz, is the first two steps
+with tight solves (linear tolerance 1e-10, Newton tolerance 1e-8): with the
+benchmark's 1e-6
 the linear solutions of two correct solvers (different summation orders)
 differ by what that tolerance leaves, and the states by ~1e-5; with tight
 solves they agree to 1e-8.
 Run from the repository root (a few minutes on the host cores each):
-    python tests/golden/make_c2_golden.py [tight]
+    python tests/golden/make_blackoil_100x100x20_golden.py [tight]
 """
 import os
 import sys
@@ -34,10 +36,10 @@ def main(tight=False):
     prob = problems.blackoil(100, 100, 20)
     if tight:
         prm = capi.default_params(linear_tolerance=1e-10, newton_tolerance=1e-8)
-        steps, name = 2, "c2_tight_log.npz"
+        steps, name = 2, "blackoil_100x100x20_tight_log.npz"
     else:
         prm = capi.default_params(linear_tolerance=1e-6, newton_tolerance=1e-6)
-        steps, name = 10, "c2_newton_log.npz"
+        steps, name = 10, "blackoil_100x100x20_newton_log.npz"
     O.set_threads(os.cpu_count() or 1)
     orc = O.Oracle(prob, prm)
     t0 = time.time()

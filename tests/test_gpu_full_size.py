@@ -1,7 +1,8 @@
-"""Parity at the benchmark's full size (workload C2: 100x100x20 black-oil,
+"""Parity at the benchmark's full size (the 100x100x20 black-oil workload,
 200k cells, 10 one-day steps, BiCGStab + ILU(0) to 1e-6, Newton tolerance
 1e-6) against the oracle's log of the same run (tests/golden/
-c2_newton_log.npz, made by tests/golden/make_c2_golden.py).  Both the FP64
+blackoil_100x100x20_newton_log.npz, made by
+tests/golden/make_blackoil_100x100x20_golden.py).  Both the FP64
 and the mixed-precision run have the oracle's Newton counts per step and its
 meanings at sampled cells; the FP64 run's total of linear iterations is
 within 10 % (the dot products sum in another order, and single BiCGStab
@@ -13,7 +14,8 @@ residual leaves pressures free by kPa at this compressibility), and the
 GPU's final state is converged by the oracle's own residual: the oracle,
 given the GPU's states before and after the last step, finds a Newton error
 within the Newton tolerance.  With tight solves (linear 1e-10, Newton 1e-8,
-two steps, c2_tight_log.npz) the FP64 state agrees to STATE_RTOL_TIGHT."""
+two steps, blackoil_100x100x20_tight_log.npz) the FP64 state agrees to
+STATE_RTOL_TIGHT."""
 import os
 
 import numpy as np
@@ -26,14 +28,14 @@ from parity import rel_state_diff
 
 pytestmark = pytest.mark.gpu
 
-GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "c2_newton_log.npz")
-TIGHT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "c2_tight_log.npz")
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "blackoil_100x100x20_newton_log.npz")
+TIGHT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "blackoil_100x100x20_tight_log.npz")
 STATE_RTOL_BENCH = 1e-4
 STATE_RTOL_TIGHT = 1e-6
 
 
 @pytest.mark.parametrize("precision", [capi.PREC_FP64, capi.PREC_MIXED])
-def test_c2_against_the_oracle_log(built, precision):
+def test_blackoil_100x100x20_against_the_oracle_log(built, precision):
     g = np.load(GOLDEN)
     prob = problems.blackoil(100, 100, 20)
     prm = capi.default_params(linear_tolerance=1e-6, newton_tolerance=1e-6, precision=precision,
@@ -66,7 +68,7 @@ def test_c2_against_the_oracle_log(built, precision):
         assert abs(int(lits.sum()) - int(g["linear"].sum())) <= 0.1 * g["linear"].sum(), (lits, g["linear"])
 
 
-def test_c2_tight_solves_match_the_oracle_state(built):
+def test_blackoil_100x100x20_tight_solves_match_the_oracle_state(built):
     g = np.load(TIGHT)
     prob = problems.blackoil(100, 100, 20)
     prm = capi.default_params(linear_tolerance=1e-10, newton_tolerance=1e-8)
