@@ -557,6 +557,8 @@ int gbfv_selftest_level_barriers(int32_t num_rows, int32_t dim, const int32_t* l
  *   residual  device pointer, num_cells*num_eq doubles (cell-major)
  *   skip      device pointer to num_cells int32 flags (non-zero: constraint
  *             or auxiliary cell, left out), or NULL for none
+ *   num_cells 0 .. GBFV_NOALLOC_MAX_CELLS
+ *   num_eq    equations per cell, 1 .. 8 (GBFV_ERR_ARG outside)
  *   stream    cudaStream_t to run on (NULL: legacy default stream); the
  *             call returns after the stream has reached its end
  * Nothing is allocated: the scratch is a fixed static device array of
@@ -565,9 +567,12 @@ int gbfv_selftest_level_barriers(int32_t num_rows, int32_t dim, const int32_t* l
  * No scratch word has to start at zero (each call writes every word it
  * reads).  The first call on each device looks up the scratch address
  * (cudaGetSymbolAddress, with that device current) and should come before
- * any stream capture.  Calls that overlap in time share the scratch and
- * race: serialize them.  Returns GBFV_ERR_NONFINITE (error = NaN) when a
- * considered entry is not finite.                                         */
+ * any stream capture.  That address is kept for the life of the process:
+ * after cudaDeviceReset (or anything else that replaces the device's
+ * primary context) it is stale, so this entry point must not be called on
+ * a device that was reset after its first call there.  Calls that overlap
+ * in time share the scratch and race: serialize them.  Returns
+ * GBFV_ERR_NONFINITE (error = NaN) when a considered entry is not finite. */
 #define GBFV_NOALLOC_MAX_CELLS (1 << 24)
 int gbfv_newton_error_noalloc(const double* residual, const int32_t* skip, int32_t num_cells,
                               int32_t num_eq, void* stream, double* error);

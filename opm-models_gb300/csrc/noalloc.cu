@@ -95,7 +95,9 @@ __global__ void __launch_bounds__(NOALLOC_THREADS) kNewtonErrorCombine(int nbloc
 }
 
 // Set-up, once per device, with that device current: the address of the
-// scratch array on this device.
+// scratch array on this device.  It is cached for the life of the process;
+// a device reset after the first call would leave it stale (documented as
+// unsupported in the header).
 int scratchOfCurrentDevice(NoAllocScratch** out)
 {
     int dev = 0;
