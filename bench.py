@@ -1,14 +1,19 @@
 #!/usr/bin/env python
 """Benchmark: cell-Newton-iterations/s of the ECFV/TPFA linearization +
-BiCGStab/ILU0 Newton solve on the three-phase black-oil grid
-100x100x20 (200k cells, 3x3 blocks), 10 time steps of 1 day.
+BiCGStab/ILU0 Newton solve.
 
-One bench step = the whole 10-time-step run from the initial state (restored
-on the device before each step).  value = sum over time steps of Newton
-iterations x cells / device time, for the mixed-precision form (FP64
-residual/Jacobian/update/outer residual, FP32 ILU0 + FP32 BiCGStab inside
-FP64 iterative refinement, linear tolerance 1e-6 relative).  The plain FP64
-form is measured on the same workload and reported beside it.
+Default workload: three-phase black-oil on 100x100x100 (1M cells, 3x3
+blocks), 10 time steps of 1 day, BiCGStab + ILU(0) to 1e-6 relative residual,
+Newton tolerance 1e-6.  One bench step = one time step of that run; the steps
+cycle through the run's 10 time steps, the initial state being restored on
+the device before the first of them.  value = sum over the timed steps of
+Newton iterations x cells / device time, for the mixed-precision form (FP64
+residual/Jacobian/update/outer residual, FP32 ILU0 + FP32 BiCGStab inside FP64
+iterative refinement).  Beside it: the plain FP64 form on the same steps, the
+same two forms on 100x100x20 (200k cells), the 48x32 lens (30 steps, FP64)
+with the CPU oracle, the mixed solve's error against the FP64 solve of the
+same system for every solve of time step 1, and a matched sample: the GPU's
+rate over exactly the Newton iterations the reference arm times.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 For N > 1 (torchrun, one rank per GPU) every rank runs its own replica: the
@@ -34,8 +39,11 @@ WORKLOADS = {
     "blackoil-100x100x100": dict(nx=100, ny=100, nz=100, steps=10, dt=86400.0),
     "blackoil-50x50x20": dict(nx=50, ny=50, nz=20, steps=10, dt=86400.0),
 }
+DEFAULT_WORKLOAD = "blackoil-100x100x100"
+SECONDARY_WORKLOAD = "blackoil-100x100x20"
 METRIC = "cell-Newton-iters/s (mixed vs plain FP64, same tol); served solve p50/p99 ms"
 UNIT = "cell-Newton-iters/s"
+LENS = dict(nx=48, ny=32, steps=30, dt=250.0)
 
 
 def parse():
@@ -44,8 +52,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="blackoil-100x100x20", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="only the headline workload (no 100x100x20 and lens lines)")
     ap.add_argument("--ensemble", type=int, default=0,
                     help="batched ensemble of this many two-phase realizations (10k-200k cells) instead of "
                          "the single-grid workload")
@@ -145,7 +155,66 @@ def params(precision):
                                inner_tolerance=1e-6)
 
 
-def cpu_sample(prob, iters=2, threads=None):
+def workload_config(wl, precision="mixed"):
+    """The `config` both arms print (the reference arm times a bounded
+    sample of this same workload and says which in cpu_baseline.sample)."""
+    w = WORKLOADS[wl]
+    N = w["nx"] * w["ny"] * w["nz"]
+    return {"workload": "%s three-phase black-oil, %d cells, %d time steps x 1 day, BiCGStab+ILU0 to 1e-6, "
+                        "Newton tol 1e-6, %s precision; one bench step = one time step (cycled)"
+                        % (wl, N, w["steps"], precision),
+            "cells": N, "time_steps": w["steps"], "precision": precision,
+            "l2": "flushed (256 MiB write) between timed steps", "parallelism": "single GPU"}
+
+
+class NewtonStepper:
+    """The workload's Newton iterations one at a time, in the order
+    NewtonMethod::apply (newtonmethod.hh:228-438) runs them inside the
+    fixed-dt time loop: iteration j of a time step linearizes at the current
+    state (j = 0 also caches the old storage, the time-level advance of the
+    storage term), takes the Newton error and, unless the step has converged
+    (j >= 1 and error <= tolerance), solves and updates.  Drives a
+    gbfv.Context or an oracle.Oracle (the same method names)."""
+
+    def __init__(self, system, dt, tol, max_iter=20):
+        self.s, self.dt, self.tol, self.max_iter = system, dt, tol, max_iter
+        self.step, self.j, self.newton = 0, 0, []
+
+    def _error(self):
+        e = self.s.newton_error()
+        if isinstance(e, tuple):
+            st, e = e
+            if st:
+                raise RuntimeError("newton_error failed %d" % st)
+        return e
+
+    def next(self, want_dx=False):
+        """One Newton iteration; returns (time step, iteration, solved, dx, linear iterations)."""
+        st = self.s.linearize(self.dt, self.j)
+        if st:
+            raise RuntimeError("linearize failed %d" % st)
+        err = self._error()
+        here = (self.step, self.j)
+        if self.j >= 1 and err <= self.tol:
+            self.newton.append(self.j + 1)
+            self.step, self.j = self.step + 1, 0
+            return here + (False, None, 0)
+        if self.j + 1 >= self.max_iter:
+            raise RuntimeError("Newton did not converge in %d iterations" % self.max_iter)
+        if want_dx or not hasattr(self.s, "stream"):
+            st, dx, it = self.s.solve()
+        else:
+            st, dx, it = self.s.solve(want_dx=False)
+        if st:
+            raise RuntimeError("solve failed %d" % st)
+        st, _ = self.s.newton_update()
+        if st:
+            raise RuntimeError("newton_update failed %d" % st)
+        self.j += 1
+        return here + (True, dx, it)
+
+
+def cpu_sample(prob, iters=1, threads=None):
     """The oracle (the reference algorithm restated on the CPU) on the first
     `iters` Newton iterations of the first time step: OpenMP over elements in
     the linearization, sequential BiCGStab/ILU0 (as the reference)."""
@@ -155,75 +224,223 @@ def cpu_sample(prob, iters=2, threads=None):
     threads = threads or os.cpu_count() or 1
     O.set_threads(threads)
     orc = O.Oracle(prob, params(0))
+    ns = NewtonStepper(orc, 86400.0, params(0).newton_tolerance)
     t0 = time.perf_counter()
-    for it in range(iters):
-        st = orc.linearize(86400.0, it)
-        if st:
-            raise RuntimeError("oracle linearize failed %d" % st)
-        st, _, _ = orc.solve()
-        orc.newton_update()
+    for _ in range(iters):
+        ns.next()
     dt = time.perf_counter() - t0
     orc.close()
     return iters * prob.num_cells / dt, dt, threads
 
 
 def run_reference(args):
+    """The reference arm: the oracle (the reference's algorithm restated on
+    the CPU; the reference itself cannot be built here) on all host threads,
+    on the same workload and config as our arm.  Each bench step is one Newton
+    iteration of the workload's run, in the run's order (time step 1's
+    iterations, then time step 2's, ...): W untimed, then K timed.  Our arm's
+    matched_sample times exactly these iterations on the GPU."""
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    w = WORKLOADS[args.workload]
     prob = build_problem(args.workload)
+    orc = O.Oracle(prob, params(0))
+    ns = NewtonStepper(orc, w["dt"], params(0).newton_tolerance)
     for _ in range(args.warmup):
-        cpu_sample(prob)
-    vals, tot = [], 0.0
+        ns.next()
+    tot, done = 0.0, []
     for _ in range(args.steps):
-        v, dt, threads = cpu_sample(prob)
-        vals.append(v)
-        tot += dt
-    value = args.steps * 2 * prob.num_cells / tot
+        t0 = time.perf_counter()
+        done.append(ns.next()[:2])
+        tot += time.perf_counter() - t0
+    orc.close()
+    value = args.steps * prob.num_cells / tot
+    sample = ("Newton iterations %d..%d of the workload's run (time step, iteration): %s; one per step, the "
+              "first %d untimed" % (args.warmup + 1, args.warmup + args.steps, done, args.warmup))
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * tot / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded lognormal permeability, uniform porosity)",
-        "config": {"workload": args.workload + " black-oil, first 2 Newton iterations of time step 1",
-                   "cells": prob.num_cells, "precision": "fp64"},
+        "data": "synthetic (seeded lognormal permeability sigma 1, uniform porosity [0.15,0.30])",
+        "config": workload_config(args.workload),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": "2 Newton iterations (linearize + BiCGStab/ILU0 to 1e-6 + update) of "
-                                   "time step 1 of the %s workload, per step" % args.workload},
+                         "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
     return 0
 
 
-def timed_runs(ctx, w, steps, warmup, flush, torch, ext):
-    """Device-time K full runs (restore state on device, 10 time steps)."""
-    its = []
-    for _ in range(warmup):
-        ctx.restore_state()
-        st, sdt, sn, sl, tl = ctx.time_integration(w["steps"], w["dt"], fixed_dt=True)
+def timed_time_steps(ctx, w, steps, warmup, flush, torch, ext):
+    """Device time of `steps` time steps of the workload, after `warmup`
+    untimed ones; the steps cycle through the run's time steps, the initial
+    state restored (on the device, outside the timed region) before each
+    cycle's first step, and L2 flushed before every timed step."""
+    n = w["steps"]
+    for k in range(warmup):
+        if k % n == 0:
+            ctx.restore_state()
+        st, _, _, _, _ = ctx.time_integration(1, w["dt"], fixed_dt=True)
         if st:
-            raise RuntimeError("warm-up run failed %d" % st)
-    ms_tot, cells_its = 0.0, 0
+            raise RuntimeError("warm-up step failed %d" % st)
+    ms_tot, cells_its, newton, linear = 0.0, 0, [], []
     launches0 = ctx.lib.gbfv_kernel_launches()
     ctx.reset_kernel_stats()
-    for _ in range(steps):
+    for k in range(steps):
+        if k % n == 0:
+            ctx.restore_state()
         with torch.cuda.stream(ext):
             flush.zero_()  # write a buffer larger than L2 between timed steps
-        ctx.restore_state()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(ext)
-        st, sdt, sn, sl, tl = ctx.time_integration(w["steps"], w["dt"], fixed_dt=True)
+        st, sdt, sn, sl, tl = ctx.time_integration(1, w["dt"], fixed_dt=True)
         e1.record(ext)
         e1.synchronize()
         if st:
-            raise RuntimeError("timed run failed %d" % st)
+            raise RuntimeError("timed step failed %d" % st)
         ms_tot += e0.elapsed_time(e1)
-        cells_its += int(sn.sum()) * ctx.N
-        its.append((sn.copy(), sl.copy()))
+        cells_its += int(sn[0]) * ctx.N
+        newton.append(int(sn[0]))
+        linear.append(int(sl[0]))
     launches = ctx.lib.gbfv_kernel_launches() - launches0
-    return ms_tot, cells_its, its, launches, ctx.kernel_stats()
+    return dict(ms=ms_tot, cits=cells_its, newton=newton, linear=linear, launches=launches,
+                kst=ctx.kernel_stats())
+
+
+def newton_iteration_ms(ctx, w, count, torch, ext):
+    """Device time of each of the first `count` Newton iterations of the
+    workload's run (from the initial state), driven one at a time through the
+    C ABI as NewtonMethod::apply runs them; returns [(time step, iteration,
+    ms)]."""
+    ctx.restore_state()
+    ns = NewtonStepper(ctx, w["dt"], params(0).newton_tolerance)
+    out = []
+    for _ in range(count):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        s, j, _, _, _ = ns.next()
+        e1.record(ext)
+        e1.synchronize()
+        out.append((s, j, e0.elapsed_time(e1)))
+    return out
+
+
+def mixed_solve_errors(ctx, w, torch):
+    """Every solve of time step 1 (mixed-precision run from the initial
+    state): the same Newton system solved in plain FP64 and in the mixed
+    form; error = max |dx_mixed - dx_fp64| / max |dx_fp64|.  The mixed dx is
+    the one applied (it is the context's last solve)."""
+    from gbfv import capi
+    ctx.restore_state()
+    pm, pf = params(capi.PREC_MIXED), params(capi.PREC_FP64)
+    ns = NewtonStepper(ctx, w["dt"], pm.newton_tolerance)
+    errs = []
+    while ns.step == 0:
+        st = ctx.linearize(w["dt"], ns.j)
+        st2, err = ctx.newton_error()
+        if st or st2:
+            raise RuntimeError("linearize failed")
+        if ns.j >= 1 and err <= ns.tol:
+            break
+        ctx.set_params(pf)
+        st, dxf, _ = ctx.solve(want_dx=True)
+        ctx.set_params(pm)
+        st2, dxm, _ = ctx.solve(want_dx=True)
+        if st or st2:
+            raise RuntimeError("solve failed")
+        errs.append(float(np.max(np.abs(dxm - dxf)) / max(np.max(np.abs(dxf)), 1e-300)))
+        ctx.newton_update()
+        ns.j += 1
+    return errs
+
+
+def lens_line(torch):
+    """The 48x32 lens (lensproblem.hh:227-627), 30 time steps from dt0 = 250 s
+    with the reference's dt control, FP64, BiCGStab + ILU(0) to 1e-6: the GPU
+    (device time of the whole run, after one untimed run) beside the oracle
+    (all host threads, and one)."""
+    from gbfv import Context, capi, problems
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    prob = problems.lens(LENS["nx"], LENS["ny"])
+    prm = capi.default_params(linear_tolerance=1e-6)
+    ctx = Context(prob, prm)
+    ctx.save_state()
+    ext = torch.cuda.ExternalStream(ctx.stream())
+    ctx.time_integration(LENS["steps"], LENS["dt"])
+    ctx.restore_state()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    st, sdt, sn, sl, _ = ctx.time_integration(LENS["steps"], LENS["dt"])
+    e1.record(ext)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    ctx.close()
+    cits = int(sn.sum()) * prob.num_cells
+    out = {"workload": "lens-48x32 two-phase immiscible (VG), 1536 cells, 30 time steps from 250 s, FP64, "
+                       "BiCGStab+ILU0 to 1e-6", "status": st, "value": cits / (ms / 1e3), "ms": ms,
+           "newton_iterations": int(sn.sum()), "linear_iterations": int(sl.sum()), "final_dt": float(sdt[-1])}
+    O.build()
+    for name, threads in (("cpu_oracle", os.cpu_count() or 1), ("cpu_oracle_one_thread", 1)):
+        O.set_threads(threads)
+        orc = O.Oracle(prob, prm)
+        t0 = time.perf_counter()
+        sto, _, sno, _, _ = orc.time_integration(LENS["steps"], LENS["dt"])
+        dt = time.perf_counter() - t0
+        orc.close()
+        out[name] = {"value": int(sno.sum()) * prob.num_cells / dt, "s": dt, "cores": threads,
+                     "same_newton_iterations": bool(np.array_equal(sno, sn))}
+    return out
+
+
+def solver_traffic(wl, kst):
+    """DRAM traffic of the solver per launch: the ratio of DRAM bytes
+    (dram__bytes_read.sum + dram__bytes_write.sum) to algorithmic bytes of an
+    ncu capture of this workload's solve (profiles/traffic.json), applied to
+    this run's algorithmic bytes per launch."""
+    tfile = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(tfile) as f:
+            ent = json.load(f).get(wl)
+        if ent:
+            kind = ent.get("traffic_kind", "scaled from a capture of the cluster launch of the same kernel body")
+            return ent["dram_per_algorithmic_byte"] * kst["solve_bytes"] / max(1, kst["solve_launches"]), kind
+    except Exception:
+        pass
+    return None, None
+
+
+def run_workload(wl, args, flush, torch, world, sampler_local=None):
+    """Both forms of one workload: timed time steps, solver configuration."""
+    from gbfv import Context, capi
+    w = WORKLOADS[wl]
+    prob = build_problem(wl)
+    out = {"prob": prob}
+    for name, prec in (("mixed", capi.PREC_MIXED), ("fp64", capi.PREC_FP64)):
+        ctx = Context(prob, params(prec))
+        ctx.save_state()
+        ext = torch.cuda.ExternalStream(ctx.stream())
+        torch.cuda.synchronize()
+        sampler = ClockSampler(sampler_local) if (name == "mixed" and sampler_local is not None) else None
+        if sampler:
+            sampler.start()
+        r = timed_time_steps(ctx, w, args.steps, args.warmup, flush, torch, ext)
+        torch.cuda.synchronize()
+        r["clocks"] = sampler.stop() if sampler else None
+        r["cfg"] = ctx.solver_config(prec)
+        r["ctx"], r["ext"] = ctx, ext
+        out[name] = r
+    return out
 
 
 def run_ours(args):
@@ -241,157 +458,137 @@ def run_ours(args):
     if world > 1:
         dist.barrier()
         ge.build()
-    from gbfv import Context, capi
-    w = WORKLOADS[args.workload]
-    prob = build_problem(args.workload)
-    N = prob.num_cells
+    from gbfv import replicas
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    results = {}
-    for name, prec in (("mixed", capi.PREC_MIXED), ("fp64", capi.PREC_FP64)):
-        ctx = Context(prob, params(prec))
-        ctx.save_state()
-        ext = torch.cuda.ExternalStream(ctx.stream())
-        if world > 1:
-            dist.barrier()
-        torch.cuda.synchronize()
-        sampler = ClockSampler(local) if name == "mixed" and rank == 0 else None
-        if sampler:
-            sampler.start()
-        ms, cits, its, launches, kst = timed_runs(ctx, w, args.steps, args.warmup, flush, torch, ext)
-        torch.cuda.synchronize()
-        clocks = sampler.stop() if sampler else None
-        if world > 1:
-            t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-            c = torch.tensor([cits], dtype=torch.float64, device="cuda")
-            dist.all_reduce(c, op=dist.ReduceOp.SUM)
-            cits = float(c.item())
-        cfg = ctx.solver_config(prec)
-        results[name] = dict(ms=ms, cits=cits, its=its, launches=launches, kst=kst, clocks=clocks, ctx=ctx,
-                             cfg=cfg)
-    # error of the mixed-precision solve against the FP64 solve of the same
-    # Newton system (first Newton iteration of the first time step; the FP64
-    # GPU path equals the CPU oracle to 1e-8 in the parity tests)
-    solve_err = None
-    try:
-        cm, cf = results["mixed"]["ctx"], results["fp64"]["ctx"]
-        dxs = []
-        for c in (cm, cf):
-            c.restore_state()
-            if c.linearize(w["dt"], 0):
-                raise RuntimeError("linearization failed")
-            _, dx, _ = c.solve(want_dx=True)
-            dxs.append(dx)
-        solve_err = float(np.max(np.abs(dxs[0] - dxs[1])) / max(np.max(np.abs(dxs[1])), 1e-300))
-    except Exception:
-        solve_err = None
-    # end-to-end through the C ABI with host buffers (mixed form)
-    ctx = results["mixed"]["ctx"]
+    if world > 1:
+        dist.barrier()
+    head = run_workload(args.workload, args, flush, torch, world, sampler_local=local if rank == 0 else None)
+    w = WORKLOADS[args.workload]
+    prob = head["prob"]
+    N = prob.num_cells
+    mixed, plain = head["mixed"], head["fp64"]
+    ms_m, cits_m = replicas.reduce_timing(mixed["ms"], mixed["cits"], device="cuda") if world > 1 \
+        else (mixed["ms"], mixed["cits"])
+    ms_f, cits_f = replicas.reduce_timing(plain["ms"], plain["cits"], device="cuda") if world > 1 \
+        else (plain["ms"], plain["cits"])
+    # end-to-end through the C ABI with host buffers (mixed form): every step
+    # copies the state in from pinned host memory and the result back out
+    ctx = mixed["ctx"]
     pv_host = torch.empty(N * 3, dtype=torch.float64, pin_memory=True).numpy()
     m_host = torch.empty(N, dtype=torch.int32, pin_memory=True).numpy()
-    out_pv = torch.empty(N * 3, dtype=torch.float64, pin_memory=True).numpy()
-    out_m = torch.empty(N, dtype=torch.int32, pin_memory=True).numpy()
     pv_host[:] = prob.init_pv
     m_host[:] = prob.init_meaning
     e2e_s, e2e_cits = 0.0, 0
-    for _ in range(args.steps):
+    for k in range(args.steps):
+        if k % w["steps"] == 0:
+            pv_host[:] = prob.init_pv
+            m_host[:] = prob.init_meaning
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         ctx.set_solution(pv_host, m_host)
-        ctx.lib.gbfv_reset_kernel_stats(ctx.h)
-        st, sdt, sn, sl, tl = ctx.time_integration(w["steps"], w["dt"], fixed_dt=True)
-        out_pv[:], out_m[:] = ctx.solution()
+        st, sdt, sn, sl, tl = ctx.time_integration(1, w["dt"], fixed_dt=True)
+        pv_host[:], m_host[:] = ctx.solution()
         e2e_s += time.perf_counter() - t0
-        e2e_cits += int(sn.sum()) * N
+        if st:
+            raise RuntimeError("e2e step failed %d" % st)
+        e2e_cits += int(sn[0]) * N
+    if world > 1:
+        e2e_ms, e2e_cits = replicas.reduce_timing(e2e_s * 1e3, e2e_cits, device="cuda")
+        e2e_s = e2e_ms / 1e3
+    if rank != 0:
+        dist.barrier()
+        dist.destroy_process_group()
+        return 0
+    # per-solve error of the mixed form against FP64 on the same systems
+    solve_errs = mixed_solve_errors(ctx, w, torch)
+    # matched sample: the Newton iterations the reference arm times
+    matched = {}
+    count = args.warmup + args.steps
+    for name in ("mixed", "fp64"):
+        it_ms = newton_iteration_ms(head[name]["ctx"], w, count, torch, head[name]["ext"])
+        timed = it_ms[args.warmup:]
+        matched[name] = {"value": len(timed) * N / (sum(t[2] for t in timed) / 1e3),
+                         "iterations": [[t[0], t[1]] for t in timed]}
     # restart file of the final state (the reference's Simulator::serialize
     # layout), written and read back outside the timed regions
     restart_line = None
-    if rank == 0:
-        import tempfile
-        from gbfv import restart
-        edges, verts = restart.cartesian_counts((w["nx"], w["ny"], w["nz"]))
-        inf = restart.info(edges, verts, time=w["steps"] * w["dt"], time_step_index=w["steps"])
-        with tempfile.TemporaryDirectory() as td:
-            path = os.path.join(td, restart.restart_file_name(".", "gbfv", inf.time))
-            t0 = time.perf_counter()
-            ctx.write_restart(path, inf)
-            t1 = time.perf_counter()
-            ctx.read_restart(path, inf)
-            t2 = time.perf_counter()
-            restart_line = {"cells": N, "bytes": os.path.getsize(path), "write_ms": (t1 - t0) * 1e3,
-                            "read_ms": (t2 - t1) * 1e3, "threads": min(16, os.cpu_count() or 1)}
-    if world > 1:
-        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-        c = torch.tensor([e2e_cits], dtype=torch.float64, device="cuda")
-        dist.all_reduce(c, op=dist.ReduceOp.SUM)
-        e2e_cits = float(c.item())
-    if rank != 0:
-        if world > 1:
-            dist.barrier()
-            dist.destroy_process_group()
-        return 0
-    mixed, plain = results["mixed"], results["fp64"]
-    value = mixed["cits"] / (mixed["ms"] / 1000.0)
-    plain_value = plain["cits"] / (plain["ms"] / 1000.0)
+    import tempfile
+    from gbfv import restart
+    edges, verts = restart.cartesian_counts((w["nx"], w["ny"], w["nz"]))
+    inf = restart.info(edges, verts, time=w["steps"] * w["dt"], time_step_index=w["steps"])
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, restart.restart_file_name(".", "gbfv", inf.time))
+        t0 = time.perf_counter()
+        ctx.write_restart(path, inf)
+        t1 = time.perf_counter()
+        ctx.read_restart(path, inf)
+        t2 = time.perf_counter()
+        restart_line = {"cells": N, "bytes": os.path.getsize(path), "write_ms": (t1 - t0) * 1e3,
+                        "read_ms": (t2 - t1) * 1e3, "threads": min(16, os.cpu_count() or 1)}
+    value = cits_m / (ms_m / 1000.0)
+    plain_value = cits_f / (ms_f / 1000.0)
     peak, peak_kind = load_peaks()
     kst = mixed["kst"]
     achieved = kst["solve_bytes"] / (kst["solve_ms"] / 1000.0) / 1e9 if kst["solve_ms"] > 0 else 0.0
     avg_launch_ms = kst["solve_ms"] / max(1, kst["solve_launches"])
-    # DRAM traffic of the solver per launch: the ratio of DRAM bytes
-    # (dram__bytes_read.sum + dram__bytes_write.sum) to algorithmic bytes of an
-    # ncu capture of this workload's solve (profiles/traffic.json), applied to
-    # this run's algorithmic bytes per launch
-    traffic = None
-    tfile = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tfile):
-        try:
-            with open(tfile) as f:
-                ent = json.load(f).get(args.workload)
-            if ent:
-                traffic = ent["dram_per_algorithmic_byte"] * kst["solve_bytes"] / max(1, kst["solve_launches"])
-        except Exception:
-            traffic = None
+    traffic, traffic_kind = solver_traffic(args.workload, kst)
     lin_ach = kst["linearize_bytes"] / (kst["linearize_ms"] / 1000.0) / 1e9 if kst["linearize_ms"] > 0 else 0.0
-    sn0, sl0 = mixed["its"][0]
-    spn, spl = plain["its"][0]
+    for name in ("mixed", "fp64"):
+        head[name]["ctx"].close()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": mixed["ms"] / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64 residual/Jacobian/update + f32 ILU0/BiCGStab",
         "data": "synthetic (seeded lognormal permeability sigma 1, uniform porosity [0.15,0.30])",
-        "config": {"workload": "%s three-phase black-oil, %d cells, 10 time steps x 1 day, "
-                               "BiCGStab+ILU0 to 1e-6, Newton tol 1e-6, mixed precision" % (args.workload, N),
-                   "cells": N, "time_steps": w["steps"], "precision": "mixed", "l2": "flushed (256 MiB write) "
-                   "between timed steps", "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": workload_config(args.workload),
         "plain_fp64": {"value": plain_value, "ms_per_step": plain["ms"] / args.steps,
-                       "newton_iterations": spn.tolist(), "linear_iterations": spl.tolist()},
+                       "newton_iterations": plain["newton"], "linear_iterations": plain["linear"],
+                       "dtype": "f64"},
         "mixed_over_plain": value / plain_value,
-        "newton_iterations": sn0.tolist(), "linear_iterations": sl0.tolist(),
-        "same_newton_iterations": bool(np.array_equal(sn0, spn)),
-        "mixed_solve_error_vs_fp64": solve_err,
+        "newton_iterations": mixed["newton"], "linear_iterations": mixed["linear"],
+        "same_newton_iterations": mixed["newton"] == plain["newton"],
+        "mixed_solve_error_vs_fp64": {"time_step": 1, "per_solve": solve_errs,
+                                      "what": "max|dx_mixed - dx_fp64| / max|dx_fp64| of the same Newton "
+                                              "system; the FP64 path equals the oracle's solve to rounding"},
+        "matched_sample": {"value": matched["mixed"]["value"], "plain_fp64": matched["fp64"]["value"],
+                           "unit": UNIT, "iterations": matched["mixed"]["iterations"],
+                           "what": "GPU rate over exactly the Newton iterations (time step, iteration) the "
+                                   "reference arm times, driven one at a time through the C ABI"},
         "e2e": {"value": e2e_cits / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(N * 3 * 8 + N * 4),
                 "d2h_bytes_per_step": int(N * 3 * 8 + N * 4)},
         "gpu_launches": int(mixed["launches"] / args.steps),
         "roofline": {"bound": "hbm", "kernel": "kBicgstab<float,3> (persistent ILU0 + BiCGStab, %s launch of %d blocks)"
                      % (mixed["cfg"]["mode"], mixed["cfg"]["blocks"]),
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "peak_kind": peak_kind,
-                     "avg_launch_ms": avg_launch_ms, "bytes_per_launch": kst["solve_bytes"] / max(1, kst["solve_launches"])},
+                     "traffic": traffic, "traffic_kind": traffic_kind, "peak_kind": peak_kind,
+                     "avg_launch_ms": avg_launch_ms,
+                     "bytes_per_launch": kst["solve_bytes"] / max(1, kst["solve_launches"])},
         "solver_config": {"mixed": mixed["cfg"], "fp64": plain["cfg"]},
         "linearize_roofline": {"achieved": lin_ach, "frac": lin_ach / peak, "ms": kst["linearize_ms"] / args.steps},
         "clocks": mixed["clocks"],
         "restart": restart_line,
     }
+    # the same two forms on the 200k-cell grid
+    if args.workload != SECONDARY_WORKLOAD and not args.headline_only:
+        sec = run_workload(SECONDARY_WORKLOAD, args, flush, torch, 1)
+        sm, sf = sec["mixed"], sec["fp64"]
+        v2m, v2f = sm["cits"] / (sm["ms"] / 1e3), sf["cits"] / (sf["ms"] / 1e3)
+        k2 = sm["kst"]
+        a2 = k2["solve_bytes"] / (k2["solve_ms"] / 1e3) / 1e9 if k2["solve_ms"] > 0 else 0.0
+        line[SECONDARY_WORKLOAD] = {
+            "value": v2m, "plain_fp64": v2f, "mixed_over_plain": v2m / v2f, "ms_per_step": sm["ms"] / args.steps,
+            "newton_iterations": sm["newton"], "same_newton_iterations": sm["newton"] == sf["newton"],
+            "linear_iterations": sm["linear"], "solver_config": {"mixed": sm["cfg"], "fp64": sf["cfg"]},
+            "roofline": {"achieved": a2, "frac": a2 / peak, "unit": "GB/s", "peak_kind": peak_kind}}
+        for name in ("mixed", "fp64"):
+            sec[name]["ctx"].close()
+    if not args.headline_only:
+        line["lens-48x32"] = lens_line(torch)
     if world == 1 and not args.no_cpu_baseline:
-        v, dt, threads = cpu_sample(prob)
-        v1, dt1, _ = cpu_sample(prob, iters=1, threads=1)
+        v, dt, threads = cpu_sample(prob, iters=1)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": "first 2 Newton iterations of time step 1 (%.1f s)" % dt,
-                                "one_thread": {"value": v1, "cores": 1,
-                                               "sample": "first Newton iteration of time step 1 (%.1f s)" % dt1}}
+                                "sample": "Newton iteration 1 of time step 1 of the workload (linearize + "
+                                          "BiCGStab/ILU0 to 1e-6 + update; %.1f s)" % dt}
     print(json.dumps(line))
     if world > 1:
         dist.barrier()

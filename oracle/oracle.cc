@@ -1012,18 +1012,37 @@ static void spmv(const Bcrs& A, const std::vector<double>& x, std::vector<double
     }
 }
 
+// Summation order of the scalar products (a test switch, process-wide):
+// 0 = the reference's sequential loop; L > 0 = another correct order, the
+// one a parallel machine uses: L strided partial sums (lane t takes blocks
+// t, t + L, ...), combined by a pairwise tree.  Only the rounding of the
+// dot products changes; every other operation stays as it is.
+static int g_dotLanes = 0;
+
 // OverlappingScalarProduct::dot (overlappingscalarproduct.hh:58-70) on one
 // rank: the plain sum over all entries
 static double dot(const std::vector<double>& a, const std::vector<double>& b, int bs)
 {
-    double s = 0;
     const size_t n = a.size() / bs;
+    if (g_dotLanes <= 0) {
+        double s = 0;
+        for (size_t i = 0; i < n; ++i) {
+            double t = 0;
+            for (int e = 0; e < bs; ++e) t += a[i * bs + e] * b[i * bs + e];
+            s += t;
+        }
+        return s;
+    }
+    const size_t L = (size_t)g_dotLanes;
+    std::vector<double> part(L, 0.0);
     for (size_t i = 0; i < n; ++i) {
         double t = 0;
         for (int e = 0; e < bs; ++e) t += a[i * bs + e] * b[i * bs + e];
-        s += t;
+        part[i % L] += t;
     }
-    return s;
+    for (size_t w = 1; w < L; w *= 2)
+        for (size_t j = 0; j + w < L; j += 2 * w) part[j] += part[j + w];
+    return part[0];
 }
 
 // CombinedCriterion (combinedcriterion.hh:55-209): max-norm residual
@@ -1404,6 +1423,10 @@ void* oracle_create(const gbfv_problem* prob, const gbfv_params* prm)
 }
 
 void oracle_destroy(void* h) { delete static_cast<Sim*>(h); }
+
+// summation order of the BiCGStab scalar products: 0 the reference's
+// sequential sum, L > 0 L strided partial sums combined pairwise (test switch)
+void oracle_set_dot_lanes(int lanes) { g_dotLanes = lanes > 0 ? lanes : 0; }
 
 #ifdef _OPENMP
 void oracle_set_threads(int n) { omp_set_num_threads(n > 0 ? n : 1); }

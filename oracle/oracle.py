@@ -48,6 +48,7 @@ def load():
         "oracle_destroy": (None, [vp]),
         "oracle_set_threads": (None, [C.c_int]),
         "oracle_get_threads": (C.c_int, []),
+        "oracle_set_dot_lanes": (None, [C.c_int]),
         "oracle_set_params": (C.c_int, [vp, C.POINTER(capi.Params)]),
         "oracle_set_solution": (C.c_int, [vp, dp, ip]),
         "oracle_get_solution": (C.c_int, [vp, dp, ip]),
@@ -177,6 +178,13 @@ class Oracle:
 
 def set_threads(n):
     load().oracle_set_threads(int(n))
+
+
+def set_dot_lanes(lanes):
+    """Summation order of the BiCGStab scalar products: 0 the reference's
+    sequential sum, L > 0 L strided partial sums combined pairwise (another
+    correct order, as a parallel machine sums)."""
+    load().oracle_set_dot_lanes(int(lanes))
 
 
 def bcrs_solve(rp, col, blocks, rhs, params):
