@@ -24,6 +24,7 @@ UNITS = {
     "solver.cu": [],
     "gbfv.cu": [],
     "noalloc.cu": [],
+    "batchround.cu": ["-fmad=false"],
     "restart.cu": [],
     "problem.cu": [],
 }

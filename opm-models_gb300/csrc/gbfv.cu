@@ -125,7 +125,10 @@ struct SolverData {
     int* pushU = nullptr;
     int* levVals = nullptr;     // values each block receives per level and sweep
     int pushKey[4] = {0, 0, 0, 0};
-    int ownerMode = 0;          // rows of a level to blocks: warp round-robin (0) / contiguous (1)
+    // rows of a level to blocks: contiguous shares (1, the default: with the
+    // spatial-tile order inside a level most dependencies stay in one block,
+    // where they are plain shared stores) or warps round-robin (0)
+    int ownerMode = 1;
     // spatial-tile sweeps (see buildTileTables)
     std::vector<int> tileKey;   // [p] tile of row p out of TILE_KEYS (empty: no tiles)
     int4* tInfo = nullptr;      // [r*numLev + l]: first row, row count, forward / backward halo slots
@@ -548,15 +551,20 @@ int buildPushTargets(SolverData& S, int C, int G, int NT, int mode)
     for (int p = 0; p < N; ++p) {
         const int owner = ownerOf(p);
         for (int q = 0; q < dim; ++q) {
+            // only values pushed from another block arrive through the
+            // cluster and are counted on the consumer's mbarrier; a producer
+            // in the same block stores into the slot directly
             const int ju = S.colHost[(size_t)(dim + 1 + q) * ld + p];  // upper neighbour +q
             if (ju >= 0) {
                 hL[(size_t)q * ld + p] = target(ju, dim - 1 - q);
-                hV[((size_t)owner * nl + lev[p]) * 2 + 1] += PB;  // p receives ju in the backward sweep
+                if (ownerOf(ju) != owner)
+                    hV[((size_t)owner * nl + lev[p]) * 2 + 1] += PB;  // p receives ju in the backward sweep
             }
             const int jl = S.colHost[(size_t)q * ld + p];  // lower neighbour in slot q
             if (jl >= 0) {
                 hU[(size_t)q * ld + p] = target(jl, q);
-                hV[((size_t)owner * nl + lev[p]) * 2] += PB;  // p receives jl in the forward sweep
+                if (ownerOf(jl) != owner)
+                    hV[((size_t)owner * nl + lev[p]) * 2] += PB;  // p receives jl in the forward sweep
             }
         }
     }
@@ -745,7 +753,7 @@ int fillKArgs(SolverData& S, DevStatus* st, const T* A, T* FL, T* FD, const T* r
     a.prof = S.prof;
     {
         int omode = S.ownerMode;
-        if (const char* e = getenv("GBFV_OWNER")) omode = strcmp(e, "contig") == 0 ? 1 : 0;
+        if (const char* e = getenv("GBFV_OWNER")) omode = strcmp(e, "rr") == 0 ? 0 : 1;
         a.ownerMode = omode;
         int maxChunk = 0;  // the most rows one block takes in a level
         // the cluster that sweeps: the whole launch, or the first cluster of a hybrid one
@@ -2355,6 +2363,13 @@ struct gbfv_batch {
     int *dOrder = nullptr, *hOrder = nullptr;      // [K] order, then the count at [K]
     int* dQueue = nullptr;
     GraphSet gLin, gCheck, gUpd, gRes0, gKry, gRef;
+    // the whole Newton round as one graph: every phase and the per-system
+    // decisions between them on the device (batchround.cu)
+    RoundSys *dRound = nullptr, *hRound = nullptr;
+    GraphSet gRound;
+    int roundRefinements = 1;            // refinement launches captured in the round graph
+    std::vector<cudaEvent_t> roundEv;    // [0,1] linearization, [2+2r, 3+2r] Krylov launch r
+    int deviceRound = 1;                 // 0: the host-driven round (phase graphs, host decisions)
     UpdateParams up{};
     cudaEvent_t evA = nullptr, evB = nullptr;
     // statistics
@@ -2413,6 +2428,93 @@ double bitsToDouble(unsigned long long bits)
     double v;
     std::memcpy(&v, &bits, sizeof(v));
     return v;
+}
+
+RoundParams roundParams(const gbfv_batch* B)
+{
+    const gbfv_params& prm = B->prm;
+    RoundParams p{};
+    p.newtonTol = prm.newton_tolerance;
+    p.newtonMaxError = prm.newton_max_error;
+    p.linTol = prm.linear_tolerance;
+    p.absTol = absTolOf(prm);
+    p.innerTol = prm.inner_tolerance;
+    p.linMaxError = prm.linear_max_error;
+    p.newtonMaxIt = prm.newton_max_iterations;
+    p.linMaxIt = prm.linear_max_iterations;
+    p.mixed = B->precision == GBFV_PREC_MIXED ? 1 : 0;
+    return p;
+}
+
+// One Newton round of every system as one graph (the decisions of
+// batchRound, made on the device by batchround.cu): per-system state in,
+// linearize + Newton error, decide; mixed: FP32 matrix and FP64 residual,
+// decide; the Krylov launch and, mixed, up to max_refinements refinement
+// launches, each followed by its decision (a launch with an empty queue
+// returns at once); update guard, decide; Newton update, decide; time level;
+// per-system state out.
+int buildRoundGraph(gbfv_batch* B)
+{
+    const int K = B->K;
+    cudaStream_t s = B->stream;
+    if (B->gRound.exec) {
+        cudaGraphExecDestroy(B->gRound.exec);
+        B->gRound.exec = nullptr;
+    }
+    const RoundParams p = roundParams(B);
+    const bool mixed = p.mixed != 0;
+    B->roundRefinements = mixed ? std::max(1, B->prm.max_refinements) : 1;
+    const int nev = 2 + 2 * B->roundRefinements;
+    while ((int)B->roundEv.size() < nev) {
+        cudaEvent_t e;
+        CK(cudaEventCreate(&e));
+        B->roundEv.push_back(e);
+    }
+    return captureGraph(B, B->gRound, [&]() -> int {
+        CK(cudaMemcpyAsync(B->dRound, B->hRound, sizeof(RoundSys) * K, cudaMemcpyHostToDevice, s));
+        if (mixed) CK(cudaMemcpyAsync(B->dK32, B->hK32, sizeof(KArgs<float>) * K, cudaMemcpyHostToDevice, s));
+        else CK(cudaMemcpyAsync(B->dK64, B->hK64, sizeof(KArgs<double>) * K, cudaMemcpyHostToDevice, s));
+        launchRoundBegin(B->dRound, B->dJs, B->dSt, K, s);
+        CK(cudaEventRecordWithFlags(B->roundEv[0], s, cudaEventRecordExternal));
+        launchBatchLinearize(B->dLin, B->dJs, K, B->gxLin, s);
+        launchBatchNewtonError(B->dLin, B->dJs, K, B->gxLin, s);
+        CK(cudaEventRecordWithFlags(B->roundEv[1], s, cudaEventRecordExternal));
+        launchRoundAfterLin(B->dRound, B->dJs, B->dSt, B->dAct, B->dK32, B->dK64, B->dSol, B->dOrder, B->dQueue, p,
+                            K, s);
+        if (mixed) {
+            launchBatchCast(B->dSol, B->dAct, K, B->gxSol, s);
+            launchBatchZeroX(B->dSol, B->dAct, K, B->gxSol, s);
+            launchBatchResidual64(B->dSol, B->dAct, K, B->gxSol, B->b, s);
+            launchRoundAfterRes0(B->dRound, B->dSt, B->dAct, B->dK32, B->dSol, B->dOrder, B->dQueue, p, K, s);
+        }
+        for (int r = 0; r < B->roundRefinements; ++r) {
+            CK(cudaEventRecordWithFlags(B->roundEv[2 + 2 * r], s, cudaEventRecordExternal));
+            int ls;
+            if (mixed)
+                ls = launchBicgstabBatch<float>(B->dK32, B->dOrder, B->dOrder + K, B->dQueue, B->b, B->cluster,
+                                                B->numClusters, B->maxLev, s);
+            else
+                ls = launchBicgstabBatch<double>(B->dK64, B->dOrder, B->dOrder + K, B->dQueue, B->b, B->cluster,
+                                                 B->numClusters, B->maxLev, s);
+            if (ls) return ls;
+            CK(cudaEventRecordWithFlags(B->roundEv[3 + 2 * r], s, cudaEventRecordExternal));
+            launchRoundAfterKrylov(B->dRound, B->dSt, B->dAct, p, K, s);
+            if (mixed) {
+                launchBatchAccumulate(B->dSol, B->dAct, K, B->gxSol, s);
+                launchBatchResidual64(B->dSol, B->dAct, K, B->gxSol, B->b, s);
+                launchRoundAfterRefine(B->dRound, B->dSt, B->dAct, B->dK32, B->dSol, B->dOrder, B->dQueue, p, K,
+                                       r + 1 == B->roundRefinements, s);
+            }
+        }
+        launchRoundBeforeCheck(B->dRound, B->dJs, B->dSt, K, s);
+        launchBatchCheckUpdate(B->dLin, B->dJs, K, B->gxLin, s);
+        launchRoundAfterCheck(B->dRound, B->dJs, B->dSt, K, s);
+        launchBatchNewtonUpdate(B->dLin, B->dJs, K, B->gxLin, B->up, s);
+        launchRoundAfterUpdate(B->dRound, B->dJs, p, K, s);
+        launchRoundTimeLevel(B->dRound, B->dLin, K, B->gxLin, s);
+        CK(cudaMemcpyAsync(B->hRound, B->dRound, sizeof(RoundSys) * K, cudaMemcpyDeviceToHost, s));
+        return GBFV_OK;
+    });
 }
 
 int buildBatchGraphs(gbfv_batch* B)
@@ -2494,17 +2596,20 @@ int buildBatchGraphs(gbfv_batch* B)
         CK(cudaMemcpyAsync(B->hSt, B->dSt, sizeof(DevStatus) * K, cudaMemcpyDeviceToHost, s));
         return GBFV_OK;
     });
-    return st;
+    if (st) return st;
+    return buildRoundGraph(B);
 }
 
 // the fail path of gbfv_newton_apply followed by the dt-halving of
 // gbfv_time_integration (fvbaseproblem.hh:523-542)
-void batchFail(gbfv_batch* B, int i, int status)
+void batchFail(gbfv_batch* B, int i, int status, bool deviceCopies = true)
 {
     SysState& y = B->sys[i];
     gbfv_ctx* C = B->ctx[i];
-    cudaMemcpyAsync(C->x, C->xOld, sizeof(double) * C->N * C->b, cudaMemcpyDeviceToDevice, B->stream);
-    cudaMemcpyAsync(C->meaning, C->meaningOld, sizeof(int) * C->N, cudaMemcpyDeviceToDevice, B->stream);
+    if (deviceCopies) {  // (the device round's time-level kernel has done them)
+        cudaMemcpyAsync(C->x, C->xOld, sizeof(double) * C->N * C->b, cudaMemcpyDeviceToDevice, B->stream);
+        cudaMemcpyAsync(C->meaning, C->meaningOld, sizeof(int) * C->N, cudaMemcpyDeviceToDevice, B->stream);
+    }
     y.numIterations = B->prm.newton_target_iterations * 2;
     if (status == GBFV_ERR_CUDA || status == GBFV_ERR_TIMEOUT || status == GBFV_ERR_OOM) {
         y.phase = PH_FAILED;
@@ -2525,15 +2630,17 @@ void batchFail(gbfv_batch* B, int i, int status)
 }
 
 // end of a converged Newton solve: advance the time level, next step size
-void batchStepDone(gbfv_batch* B, int i)
+void batchStepDone(gbfv_batch* B, int i, bool deviceCopies = true)
 {
     SysState& y = B->sys[i];
     gbfv_ctx* C = B->ctx[i];
     y.stepDt.push_back(y.dt);
     y.stepNewton.push_back(y.numIterations);
     y.stepLinear.push_back(y.linItStep);
-    cudaMemcpyAsync(C->xOld, C->x, sizeof(double) * C->N * C->b, cudaMemcpyDeviceToDevice, B->stream);
-    cudaMemcpyAsync(C->meaningOld, C->meaning, sizeof(int) * C->N, cudaMemcpyDeviceToDevice, B->stream);
+    if (deviceCopies) {
+        cudaMemcpyAsync(C->xOld, C->x, sizeof(double) * C->N * C->b, cudaMemcpyDeviceToDevice, B->stream);
+        cudaMemcpyAsync(C->meaningOld, C->meaning, sizeof(int) * C->N, cudaMemcpyDeviceToDevice, B->stream);
+    }
     y.t += y.dt;
     y.step++;
     C->numIterations = y.numIterations;
@@ -2759,11 +2866,98 @@ int batchRound(gbfv_batch* B)
     return GBFV_OK;
 }
 
+// one round as one graph launch (buildRoundGraph): the host sets which
+// systems start a Newton iteration, replays the graph, and does the
+// time-step bookkeeping of the systems whose Newton loop ended
+int batchRoundDevice(gbfv_batch* B)
+{
+    const int K = B->K;
+    const gbfv_params& prm = B->prm;
+    const bool mixed = B->precision == GBFV_PREC_MIXED;
+    bool any = false;
+    for (int i = 0; i < K; ++i) {
+        SysState& y = B->sys[i];
+        RoundSys& r = B->hRound[i];
+        std::memset(&r, 0, sizeof(r));
+        r.phase = y.phase == PH_LIN ? RS_LIN : RS_IDLE;
+        r.dt = y.dt;
+        r.numIterations = y.numIterations;
+        r.error = y.error;
+        r.lastError = y.lastError;
+        r.linItStep = y.linItStep;
+        r.linearizations = y.linearizations;
+        if (y.phase != PH_LIN) continue;
+        any = true;
+        // the solve's launch arguments; the round's decisions set each
+        // launch's reduction target and factorization flag on the device
+        gbfv_ctx* C = B->ctx[i];
+        SolverData& Sd = C->S;
+        int rs;
+        if (mixed) {
+            float* vec[6] = {Sd.v32[1], Sd.v32[2], Sd.v32[3], Sd.v32[4], Sd.v32[5], Sd.v32[6]};
+            rs = fillKArgs<float>(Sd, &B->dSt[i], Sd.A32, Sd.FL32, Sd.FD32, Sd.v32[0], vec, 1, prm.inner_tolerance, 0.0,
+                                  prm.linear_max_error, prm.linear_max_iterations, SYNC_CLUSTER, B->cluster,
+                                  B->hK32[i]);
+        }
+        else
+            rs = fillKArgs<double>(Sd, &B->dSt[i], C->jval, Sd.FL64, Sd.FD64, C->residual, Sd.v64, 1,
+                                   prm.linear_tolerance, absTolOf(prm), prm.linear_max_error,
+                                   prm.linear_max_iterations, SYNC_CLUSTER, B->cluster, B->hK64[i]);
+        if (rs) return rs;
+    }
+    if (!any) return GBFV_OK;
+    B->rounds++;
+    int rs = replay(B, B->gRound, true);
+    if (rs) return rs;
+    {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, B->roundEv[0], B->roundEv[1]);
+        B->linMs += ms;
+        int launches = 0;
+        for (int i = 0; i < K; ++i) launches = std::max(launches, B->hRound[i].kryLaunches);
+        for (int r = 0; r < launches; ++r) {
+            cudaEventElapsedTime(&ms, B->roundEv[2 + 2 * r], B->roundEv[3 + 2 * r]);
+            B->solveMs += ms;
+        }
+        B->solveLaunches += launches;
+        const int sz = mixed ? 4 : 8;
+        for (int i = 0; i < K; ++i) {
+            const RoundSys& r = B->hRound[i];
+            if (!r.kryLaunches) continue;
+            const SolverData& Sd = B->ctx[i]->S;
+            const double b0 = solveBytes(Sd, 0, 0, sz);
+            B->solveBytes += r.kryLaunches * b0 + r.kryFactors * (solveBytes(Sd, 0, 1, sz) - b0) +
+                             (double)r.kryIters * (solveBytes(Sd, 1, 0, sz) - b0);
+        }
+    }
+    for (int i = 0; i < K; ++i) {
+        SysState& y = B->sys[i];
+        const RoundSys& r = B->hRound[i];
+        if (y.phase != PH_LIN) continue;
+        y.numIterations = r.numIterations;
+        y.error = r.error;
+        y.lastError = r.lastError;
+        y.linItStep = r.linItStep;
+        y.linearizations = r.linearizations;
+        if (r.phase == RS_LIN) continue;
+        if (r.phase == RS_END_OK) batchStepDone(B, i, false);
+        else if (r.phase == RS_FAIL) batchFail(B, i, r.status, false);
+        else {
+            setError("batched round ended with a system in phase " + std::to_string(r.phase));
+            return GBFV_ERR_CUDA;
+        }
+    }
+    return GBFV_OK;
+}
+
 void freeBatch(gbfv_batch* B)
 {
     if (!B) return;
-    for (GraphSet* g : {&B->gLin, &B->gCheck, &B->gUpd, &B->gRes0, &B->gKry, &B->gRef})
+    for (GraphSet* g : {&B->gLin, &B->gCheck, &B->gUpd, &B->gRes0, &B->gKry, &B->gRef, &B->gRound})
         if (g->exec) cudaGraphExecDestroy(g->exec);
+    for (cudaEvent_t e : B->roundEv) cudaEventDestroy(e);
+    cudaFree(B->dRound);
+    cudaFreeHost(B->hRound);
     cudaFree(B->dLin);
     cudaFree(B->dSol);
     cudaFree(B->dJs);
@@ -2837,6 +3031,8 @@ int setupBatch(gbfv_batch* B, int cluster)
     if ((st = pinnedAlloc(&B->hJs, K)) || (st = pinnedAlloc(&B->hAct, K)) || (st = pinnedAlloc(&B->hSt, K)) ||
         (st = pinnedAlloc(&B->hK32, K)) || (st = pinnedAlloc(&B->hK64, K)) || (st = pinnedAlloc(&B->hOrder, K + 1)))
         return st;
+    if ((st = devAlloc(&B->dRound, K)) || (st = pinnedAlloc(&B->hRound, K))) return st;
+    if (const char* e = getenv("GBFV_BATCH_HOST_ROUND")) B->deviceRound = atoi(e) ? 0 : 1;
     std::vector<LinJob> lj(K);
     std::vector<SolveJob> sj(K);
     int maxN = 1, maxLev = 1, maxC = 16;
@@ -2950,7 +3146,7 @@ int gbfv_batch_time_integration(gbfv_batch* B, int num_steps, double dt0, double
         bool pending = false;
         for (const SysState& y : B->sys) pending |= y.phase == PH_LIN;
         if (!pending) break;
-        const int rs = batchRound(B);
+        const int rs = B->deviceRound ? batchRoundDevice(B) : batchRound(B);
         if (rs) return rs;
     }
     CK(cudaStreamSynchronize(B->stream));
@@ -3147,7 +3343,7 @@ int gbfv_serve_admit(gbfv_batch* B, const gbfv_problem* prob, const double* pv, 
 int gbfv_serve_step(gbfv_batch* B, int* running)
 {
     if (!B) return GBFV_ERR_ARG;
-    const int rs = batchRound(B);
+    const int rs = B->deviceRound ? batchRoundDevice(B) : batchRound(B);
     int n = 0;
     for (const SysState& y : B->sys) n += y.phase == PH_LIN;
     if (running) *running = n;

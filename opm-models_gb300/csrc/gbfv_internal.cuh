@@ -157,6 +157,28 @@ struct JobState {
     int active;
 };
 
+// Device-side state of a batched Newton round (batchround.cu): one entry
+// per system, copied in before and out after every round.
+enum RoundPhase {
+    RS_LIN = 0,     // linearizes in this round
+    RS_SOLVE = 1,   // (inside a round) solving
+    RS_UPDATE = 2,  // (inside a round) solved, to be updated
+    RS_END_OK = 3,  // the Newton loop converged in this round: the step is complete
+    RS_FAIL = 4,    // failed in this round (status): back to the old time level
+    RS_IDLE = 5     // not taking part
+};
+struct RoundParams {
+    double newtonTol, newtonMaxError, linTol, absTol, innerTol, linMaxError;
+    int newtonMaxIt, linMaxIt, mixed, pad;
+};
+struct RoundSys {
+    int phase, status, numIterations, linearizations;
+    int linItStep, kry, refs, lastKs;
+    int lastIt, factorNext, kryLaunches, kryFactors;
+    int kryIters, pad;
+    double dt, error, lastError, resErr, resErr0;
+};
+
 // kernel launches of this library (several host threads may launch: atomic);
 // while a thread captures a CUDA graph its launches are counted for the
 // graph instead and added to the total each time the graph is replayed

@@ -117,4 +117,19 @@ void launchAccumulate(int n, double* x, const float* d, cudaStream_t s);
 void launchResidual64(int N, int ld, int nslot, int b, const int* col, const double* A, const double* rhs,
                       const double* x, double* r, float* r32, DevStatus* st, cudaStream_t s);
 
+// device-side decisions of a batched Newton round (batchround.cu)
+void launchRoundBegin(RoundSys* ys, JobState* js, DevStatus* st, int K, cudaStream_t s);
+void launchRoundAfterLin(RoundSys* ys, const JobState* js, DevStatus* st, int* act, KArgs<float>* ka32,
+                         KArgs<double>* ka64, const SolveJob* sj, int* order, int* queue, const RoundParams& p, int K,
+                         cudaStream_t s);
+void launchRoundAfterRes0(RoundSys* ys, DevStatus* st, int* act, KArgs<float>* ka, const SolveJob* sj, int* order,
+                          int* queue, const RoundParams& p, int K, cudaStream_t s);
+void launchRoundAfterKrylov(RoundSys* ys, DevStatus* st, int* act, const RoundParams& p, int K, cudaStream_t s);
+void launchRoundAfterRefine(RoundSys* ys, DevStatus* st, int* act, KArgs<float>* ka, const SolveJob* sj, int* order,
+                            int* queue, const RoundParams& p, int K, int lastRefinement, cudaStream_t s);
+void launchRoundBeforeCheck(RoundSys* ys, JobState* js, DevStatus* st, int K, cudaStream_t s);
+void launchRoundAfterCheck(RoundSys* ys, JobState* js, DevStatus* st, int K, cudaStream_t s);
+void launchRoundAfterUpdate(RoundSys* ys, const JobState* js, const RoundParams& p, int K, cudaStream_t s);
+void launchRoundTimeLevel(const RoundSys* ys, const LinJob* jobs, int K, int gx, cudaStream_t s);
+
 }  // namespace gbfv

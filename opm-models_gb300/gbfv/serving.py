@@ -239,6 +239,9 @@ def latency_summary(requests):
     lat = np.array([r.latency for r in requests if r.latency is not None])
     span = max(r.finished for r in requests) - min(r.arrival for r in requests)
     cits = sum(int(np.sum(r.newton)) * r.problem.num_cells for r in requests if r.newton is not None)
+    arr = sorted(r.arrival for r in requests)
+    offered = (len(arr) - 1) / (arr[-1] - arr[0]) if len(arr) > 1 and arr[-1] > arr[0] else None
     return {"p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
-            "mean_ms": float(lat.mean() * 1e3), "requests": len(lat), "throughput_rps": len(lat) / span,
+            "max_ms": float(lat.max() * 1e3), "mean_ms": float(lat.mean() * 1e3), "requests": len(lat),
+            "offered_rps": offered, "throughput_rps": len(lat) / span,
             "cell_newton_its_per_s": cits / span, "failed": int(sum(1 for r in requests if r.status))}

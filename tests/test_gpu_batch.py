@@ -84,3 +84,32 @@ def test_batch_blackoil_with_wells(built):
         assert st == 0 and np.array_equal(bsn, sn) and np.array_equal(bsl, sl)
         assert np.array_equal(B.systems[i].solution()[0], ctx.solution()[0])
     B.close()
+
+
+@pytest.mark.parametrize("precision", [capi.PREC_MIXED, capi.PREC_FP64])
+def test_round_is_one_graph_launch_and_equals_the_host_driven_round(built, monkeypatch, precision):
+    """The device-driven round (every phase and the per-system decisions
+    between them in one captured graph) launches exactly one graph per
+    round and gives the host-driven round's results bit for bit: the same
+    rounds, steps, Newton and linear iterations and states."""
+    probs = _members([3000, 12000, 800, 6000], seed0=31)
+    prm = capi.default_params(linear_tolerance=1e-6, newton_tolerance=1e-6, precision=precision,
+                              inner_tolerance=1e-5)
+    runs = {}
+    for mode in ("1", "0"):
+        monkeypatch.setenv("GBFV_BATCH_HOST_ROUND", mode)
+        B = Batch(probs, prm, cluster_size=CLUSTER)
+        st = B.time_integration(3, 200.0)
+        stats = B.stats()
+        res = [(B.report(i), B.systems[i].solution()) for i in range(len(probs))]
+        B.close()
+        runs[mode] = (st, stats, res)
+    (sh, hs, hres), (sd, ds, dres) = runs["1"], runs["0"]
+    assert sh == sd == 0
+    assert ds["rounds"] == hs["rounds"] > 0
+    assert ds["graph_launches"] == ds["rounds"]
+    assert hs["graph_launches"] > hs["rounds"]
+    for (hr, (hx, hm)), (dr, (dx, dm)) in zip(hres, dres):
+        for a, b in zip(hr, dr):
+            assert np.array_equal(np.asarray(a), np.asarray(b)), (a, b)
+        assert np.array_equal(hx, dx) and np.array_equal(hm, dm)

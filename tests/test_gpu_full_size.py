@@ -137,7 +137,7 @@ def test_largest_ensemble_member_in_a_batch_against_the_oracle_log(built):
     small = [problems.ensemble_member(n, 7 + i, 1.0) for i, n in enumerate((4000, 9000))]
     prm = _bench_params(capi.PREC_MIXED)
     B = Batch([small[0], big, small[1]], prm, cluster_size=4)
-    assert B.time_integration(len(g["newton"]), 250.0) == 0
+    assert B.time_integration(len(g["newton"]), 250.0, fixed_dt=True) == 0
     st, sdt, sn, sl, _ = B.report(1)
     x, m = B.systems[1].solution()
     B.close()
