@@ -779,6 +779,34 @@ def run_ensemble(args):
     # in the mixed form and in the plain FP64 form
     sample = list(range(0, len(probs), max(1, len(probs) // 8)))[:8]
     B.close()
+    # the plain FP64 form of the same batch (all systems, one untimed run
+    # after its autotuner, then one timed run)
+    B64 = Batch(probs, params(capi.PREC_FP64))
+    B64.autotune(ENSEMBLE["dt"])
+    for c in B64.systems:
+        c.save_state()
+    ext64 = torch.cuda.ExternalStream(B64.stream())
+
+    def one_run64():
+        for c in B64.systems:
+            c.restore_state()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext64)
+        st = B64.time_integration(ENSEMBLE["steps"], ENSEMBLE["dt"])
+        e1.record(ext64)
+        e1.synchronize()
+        if st:
+            raise RuntimeError("batched FP64 run failed %d" % st)
+        cits = sum(int(B64.report(i)[2].sum()) * int(Ns[i]) for i in range(len(probs)))
+        return e0.elapsed_time(e1), cits
+
+    one_run64()
+    ms64, cits64 = one_run64()
+    batched_fp64 = cits64 / (ms64 / 1000.0)
+    same_newton_fp64 = all(B64.report(i)[2].tolist() == newton[i] for i in range(len(probs)))
+    B64.close()
 
     def one_at_a_time(prm1):
         ms, cits = 0.0, 0
@@ -830,8 +858,10 @@ def run_ensemble(args):
                   "build_s": t_build, "create_s": t_create},
         "one_at_a_time": {"value": one_value, "systems_sampled": len(sample)},
         "one_at_a_time_plain_fp64": {"value": one_fp64, "systems_sampled": len(sample)},
+        "batched_plain_fp64": {"value": batched_fp64, "same_newton_iterations": same_newton_fp64},
         "batched_over_one_at_a_time": (value / world) / one_value,
         "batched_mixed_over_plain_fp64": (value / world) / one_fp64,
+        "batched_mixed_over_batched_plain_fp64": (value / world) / batched_fp64,
         "gpu_launches": int((s1["kernel_launches"] - s0["kernel_launches"]) / args.steps),
         "newton_iterations_first_systems": newton[:4],
         "roofline": {"bound": "hbm", "kernel": "kBicgstabBatch<float,2> (batched persistent ILU0 + BiCGStab)",
