@@ -125,10 +125,7 @@ struct SolverData {
     int* pushU = nullptr;
     int* levVals = nullptr;     // values each block receives per level and sweep
     int pushKey[4] = {0, 0, 0, 0};
-    // rows of a level to blocks: contiguous shares (1, the default: with the
-    // spatial-tile order inside a level most dependencies stay in one block,
-    // where they are plain shared stores) or warps round-robin (0)
-    int ownerMode = 1;
+    int ownerMode = 0;          // rows of a level to blocks: warp round-robin (0) / contiguous (1)
     // spatial-tile sweeps (see buildTileTables)
     std::vector<int> tileKey;   // [p] tile of row p out of TILE_KEYS (empty: no tiles)
     int4* tInfo = nullptr;      // [r*numLev + l]: first row, row count, forward / backward halo slots
@@ -551,20 +548,15 @@ int buildPushTargets(SolverData& S, int C, int G, int NT, int mode)
     for (int p = 0; p < N; ++p) {
         const int owner = ownerOf(p);
         for (int q = 0; q < dim; ++q) {
-            // only values pushed from another block arrive through the
-            // cluster and are counted on the consumer's mbarrier; a producer
-            // in the same block stores into the slot directly
             const int ju = S.colHost[(size_t)(dim + 1 + q) * ld + p];  // upper neighbour +q
             if (ju >= 0) {
                 hL[(size_t)q * ld + p] = target(ju, dim - 1 - q);
-                if (ownerOf(ju) != owner)
-                    hV[((size_t)owner * nl + lev[p]) * 2 + 1] += PB;  // p receives ju in the backward sweep
+                hV[((size_t)owner * nl + lev[p]) * 2 + 1] += PB;  // p receives ju in the backward sweep
             }
             const int jl = S.colHost[(size_t)q * ld + p];  // lower neighbour in slot q
             if (jl >= 0) {
                 hU[(size_t)q * ld + p] = target(jl, q);
-                if (ownerOf(jl) != owner)
-                    hV[((size_t)owner * nl + lev[p]) * 2] += PB;  // p receives jl in the forward sweep
+                hV[((size_t)owner * nl + lev[p]) * 2] += PB;  // p receives jl in the forward sweep
             }
         }
     }
@@ -753,7 +745,7 @@ int fillKArgs(SolverData& S, DevStatus* st, const T* A, T* FL, T* FD, const T* r
     a.prof = S.prof;
     {
         int omode = S.ownerMode;
-        if (const char* e = getenv("GBFV_OWNER")) omode = strcmp(e, "rr") == 0 ? 0 : 1;
+        if (const char* e = getenv("GBFV_OWNER")) omode = strcmp(e, "contig") == 0 ? 1 : 0;
         a.ownerMode = omode;
         int maxChunk = 0;  // the most rows one block takes in a level
         // the cluster that sweeps: the whole launch, or the first cluster of a hybrid one

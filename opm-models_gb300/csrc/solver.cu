@@ -560,88 +560,22 @@ struct SweepMap {
 
 // A push target is the consumer block (bits 24..31) and the element offset
 // of the consumer's slot inside one half of the dependency buffer
-// (precomputed on the host for the launch configuration).  The cluster
-// addresses of the slot and of the consumer's mbarrier are formed before the
-// level's data wait, off its critical path; false (and no push) for a target
-// outside the cluster (a table built for another cluster size).
-// Kinds of push: none, into another block of the cluster (st.async, counted
-// on that block's mbarrier), into this block (a plain shared store: the
-// block barrier between two levels orders it before the consumer's read, and
-// the consumer's mbarrier does not count it).
-constexpr int PUSH_NONE = 0, PUSH_REMOTE = 1, PUSH_LOCAL = 2;
-template <class T>
-__device__ __forceinline__ int pushAddress(int target, int half, const Team<SYNC_CLUSTER>& tm, PushState& ps,
-                                           int mbIdx, unsigned& dst, unsigned& mb)
+// (precomputed on the host for the launch configuration).
+template <class T, int B>
+__device__ __forceinline__ void pushValues(int target, int half, const T (&out)[B], const Team<SYNC_CLUSTER>& tm,
+                                           const T* dep, PushState& ps, int mbIdx)
 {
+    // also a consumer in this block gets its values by st.async (to this block's
+    // own shared memory): the transaction count orders them, no fence needed
     const int owner = target >> 24;
-    if (owner >= tm.nblk) {
+    if (owner >= tm.nblk) {  // a table for another cluster size: no push outside the cluster
         ps.ok = 0;
-        return PUSH_NONE;
+        return;
     }
     const int off = (target & 0xffffff) + half;
-    if (owner == tm.rank) {
-        dst = (unsigned)(off * sizeof(T));  // element offset in bytes inside this block's buffer
-        return PUSH_LOCAL;
-    }
-    dst = mapaRank(ps.dep + (unsigned)(off * sizeof(T)), owner);
-    mb = mapaRank(ps.mb[mbIdx], owner);
-    return PUSH_REMOTE;
-}
-
-// a local push: the slot's padB(B) values with one (or two) vector stores
-template <class T, int B>
-__device__ __forceinline__ void stLocalSlot(T* slot, const T (&v)[B])
-{
-    if constexpr (sizeof(T) == 4 && B == 3)
-        *reinterpret_cast<float4*>(slot) = make_float4(v[0], v[1], v[2], 0.0f);
-    else if constexpr (sizeof(T) == 4 && B == 2)
-        *reinterpret_cast<float2*>(slot) = make_float2(v[0], v[1]);
-    else if constexpr (sizeof(T) == 8 && B == 2)
-        *reinterpret_cast<double2*>(slot) = make_double2(v[0], v[1]);
-    else if constexpr (sizeof(T) == 8 && B == 3) {
-        *reinterpret_cast<double2*>(slot) = make_double2(v[0], v[1]);
-        *reinterpret_cast<double2*>(slot + 2) = make_double2(v[2], 0.0);
-    }
-    else {
-#pragma unroll
-        for (int c = 0; c < B; ++c) slot[c] = v[c];
-    }
-}
-
-template <class T, int B>
-__device__ __forceinline__ void doPush(int kind, unsigned dst, unsigned mb, const T* dep, const T (&out)[B])
-{
-    if (kind == PUSH_REMOTE)
-        stAsyncSlot<T, B>(dst, out, mb);
-    else if (kind == PUSH_LOCAL)
-        stLocalSlot<T, B>(const_cast<T*>(dep) + dst / sizeof(T), out);
-}
-
-// one pushed dependency slot (padB(B) values, 8- or 16-byte aligned) into registers
-template <class T, int B>
-__device__ __forceinline__ void ldSlot(const T* md, T (&m)[B])
-{
-    if constexpr (sizeof(T) == 4 && B == 3) {
-        const float4 v = *reinterpret_cast<const float4*>(md);
-        m[0] = v.x; m[1] = v.y; m[2] = v.z;
-    }
-    else if constexpr (sizeof(T) == 4 && B == 2) {
-        const float2 v = *reinterpret_cast<const float2*>(md);
-        m[0] = v.x; m[1] = v.y;
-    }
-    else if constexpr (sizeof(T) == 8 && B == 2) {
-        const double2 v = *reinterpret_cast<const double2*>(md);
-        m[0] = v.x; m[1] = v.y;
-    }
-    else if constexpr (sizeof(T) == 8 && B == 3) {
-        const double2 v0 = *reinterpret_cast<const double2*>(md);
-        const double2 v1 = *reinterpret_cast<const double2*>(md + 2);
-        m[0] = v0.x; m[1] = v0.y; m[2] = v1.x;
-    }
-    else {
-#pragma unroll
-        for (int c = 0; c < B; ++c) m[c] = md[c];
-    }
+    const unsigned dst = mapaRank(ps.dep + (unsigned)(off * sizeof(T)), owner);
+    const unsigned mb = mapaRank(ps.mb[mbIdx], owner);
+    stAsyncSlot<T, B>(dst, out, mb);
 }
 
 // Asynchronous global -> shared copies (no registers held, not waited for by
@@ -816,17 +750,10 @@ __device__ __forceinline__ void sweepLowerPush(const KArgs<T>& a, const T* d, T*
         const bool mine = mp.grp == l % G;
         if (mine) {
             const int i = iCur;
-            // the row's staged operands (right-hand side, factor blocks) and
-            // the cluster addresses of its pushes go to registers before the
-            // data wait: after it only the dependency values are read
+            // the row's staged operands go to registers before the data wait
             T out[B];
-            // factor blocks in registers where they fit without spilling
-            // (FP32 with at most 256 threads), else read from shared memory
-            constexpr bool HOIST = sizeof(T) == 4 && NT <= 256;
-            T fl[HOIST ? 3 : 1][HOIST ? BB : 1];
             bool has[3] = {false, false, false};
-            int push[3] = {PUSH_NONE, PUSH_NONE, PUSH_NONE};
-            unsigned pdst[3] = {0u, 0u, 0u}, pmb[3] = {0u, 0u, 0u};
+            int tg[3] = {-1, -1, -1};
             if (i >= 0) {
                 cpWaitAll();
                 if (fuseP) {
@@ -850,12 +777,7 @@ __device__ __forceinline__ void sweepLowerPush(const KArgs<T>& a, const T* d, T*
                 for (int s = 0; s < 3; ++s) {
                     if (s >= dim) break;
                     has[s] = sn[s * NT + tid] >= 0;
-                    const int tg = sn[(3 + s) * NT + tid];
-                    if (tg >= 0) push[s] = pushAddress<T>(tg, kn * half, tm, ps, kn, pdst[s], pmb[s]);
-                    if constexpr (HOIST) {
-#pragma unroll
-                        for (int e = 0; e < BB; ++e) fl[s][e] = st[(s * BB + e) * NT + tid];
-                    }
+                    tg[s] = sn[(3 + s) * NT + tid];
                 }
             }
             if (probe) t0 = clock64();
@@ -869,22 +791,18 @@ __device__ __forceinline__ void sweepLowerPush(const KArgs<T>& a, const T* d, T*
                     if (s >= dim) break;
                     if (!has[s]) continue;
                     T m[B];
-                    ldSlot<T, B>(md + s * PB, m);
+#pragma unroll
+                    for (int c = 0; c < B; ++c) m[c] = md[s * PB + c];
 #pragma unroll
                     for (int r = 0; r < B; ++r)
 #pragma unroll
-                        for (int c = 0; c < B; ++c) {
-                            if constexpr (HOIST)
-                                out[r] -= fl[s][r * B + c] * m[c];
-                            else
-                                out[r] -= st[(s * BB + r * B + c) * NT + tid] * m[c];
-                        }
+                        for (int c = 0; c < B; ++c) out[r] -= st[(s * BB + r * B + c) * NT + tid] * m[c];
                 }
                 if (probe) t2 = clock64();
 #pragma unroll
                 for (int q = 0; q < 3; ++q) {
                     if (q >= dim) break;
-                    if (ps.ok) doPush<T, B>(push[q], pdst[q], pmb[q], dep, out);
+                    if (tg[q] >= 0 && ps.ok) pushValues<T, B>(tg[q], kn * half, out, tm, dep, ps, kn);
                 }
 #pragma unroll
                 for (int e = 0; e < B; ++e) y[i * B + e] = out[e];
@@ -967,14 +885,10 @@ __device__ __forceinline__ void sweepUpperPush(const KArgs<T>& a, T* y, const Te
         const bool mine = mp.grp == l % G;
         if (mine) {
             const int i = iCur;
-            // the row's staged operands (vector, upper blocks, inverted pivot)
-            // and its push addresses go to registers before the data wait
+            // the row's staged operands go to registers before the data wait
             T acc[B];
-            constexpr bool HOIST = sizeof(T) == 4 && NT <= 256;
-            T au[HOIST ? 3 : 1][HOIST ? BB : 1], fd[HOIST ? BB : 1];
             bool has[3] = {false, false, false};
-            int push[3] = {PUSH_NONE, PUSH_NONE, PUSH_NONE};
-            unsigned pdst[3] = {0u, 0u, 0u}, pmb[3] = {0u, 0u, 0u};
+            int tg[3] = {-1, -1, -1};
             if (i >= 0) {
                 cpWaitAll();
 #pragma unroll
@@ -983,16 +897,7 @@ __device__ __forceinline__ void sweepUpperPush(const KArgs<T>& a, T* y, const Te
                 for (int q = 0; q < 3; ++q) {
                     if (q >= dim) break;
                     has[q] = sn[q * NT + tid] >= 0;
-                    const int tg = sn[(3 + q) * NT + tid];
-                    if (tg >= 0) push[q] = pushAddress<T>(tg, kn * half, tm, ps, kn, pdst[q], pmb[q]);
-                    if constexpr (HOIST) {
-#pragma unroll
-                        for (int e = 0; e < BB; ++e) au[q][e] = st[(q * BB + e) * NT + tid];
-                    }
-                }
-                if constexpr (HOIST) {
-#pragma unroll
-                    for (int e = 0; e < BB; ++e) fd[e] = st[(3 * BB + e) * NT + tid];
+                    tg[q] = sn[(3 + q) * NT + tid];
                 }
             }
             if (ps.ok && !mbarWait(ps.mb[k], ps.ph[k])) ps.ok = 0;
@@ -1003,34 +908,25 @@ __device__ __forceinline__ void sweepUpperPush(const KArgs<T>& a, T* y, const Te
                     if (q >= dim) break;
                     if (!has[q]) continue;
                     T m[B];
-                    ldSlot<T, B>(md + q * PB, m);
+#pragma unroll
+                    for (int c = 0; c < B; ++c) m[c] = md[q * PB + c];
 #pragma unroll
                     for (int r = 0; r < B; ++r)
 #pragma unroll
-                        for (int c = 0; c < B; ++c) {
-                            if constexpr (HOIST)
-                                acc[r] -= au[q][r * B + c] * m[c];
-                            else
-                                acc[r] -= st[(q * BB + r * B + c) * NT + tid] * m[c];
-                        }
+                        for (int c = 0; c < B; ++c) acc[r] -= st[(q * BB + r * B + c) * NT + tid] * m[c];
                 }
                 T out[B];
 #pragma unroll
                 for (int r = 0; r < B; ++r) {
                     T t = T(0);
 #pragma unroll
-                    for (int c = 0; c < B; ++c) {
-                        if constexpr (HOIST)
-                            t += fd[r * B + c] * acc[c];
-                        else
-                            t += st[(3 * BB + r * B + c) * NT + tid] * acc[c];
-                    }
+                    for (int c = 0; c < B; ++c) t += st[(3 * BB + r * B + c) * NT + tid] * acc[c];
                     out[r] = t;
                 }
 #pragma unroll
                 for (int q = 0; q < 3; ++q) {
                     if (q >= dim) break;
-                    if (ps.ok) doPush<T, B>(push[q], pdst[q], pmb[q], dep, out);
+                    if (tg[q] >= 0 && ps.ok) pushValues<T, B>(tg[q], kn * half, out, tm, dep, ps, kn);
                 }
 #pragma unroll
                 for (int e = 0; e < B; ++e) y[i * B + e] = out[e];
