@@ -527,6 +527,60 @@ int gbfv_write_restart(gbfv_ctx* ctx, const char* path, const gbfv_restart_info*
 int gbfv_read_restart(gbfv_ctx* ctx, const char* path, gbfv_restart_info* info);
 
 /* ------------------------------------------------------------------ */
+/* VTK output (the reference's VtkMultiWriter with its primary-variable and
+ * multi-phase modules: opm/models/io/vtkmultiwriter.hh:64-540,
+ * vtkprimaryvarsmodule.hh:54-170, vtkmultiphasemodule.hh:84-460).       */
+/* The output quantities of the context's current solution, evaluated on
+ * the device as the intensive quantities are: out[q*num_cells + cell],
+ * natural cell order, for plane q = 3*k + phase with k = 0 pressure,
+ * 1 density, 2 saturation, 3 mobility, 4 relative permeability,
+ * 5 viscosity (phases: wetting / non-wetting for the immiscible model, the
+ * third plane zero; water / oil / gas for black-oil), and q = 18 the
+ * porosity.                                                              */
+#define GBFV_OUTPUT_PLANES 19
+int gbfv_output_fields(gbfv_ctx* ctx, double* out);
+
+/* fields of a VTK file, the reference's VtkWrite* parameters; the default
+ * set is theirs: pressures, densities, saturations, relative
+ * permeabilities and porosity                                            */
+enum gbfv_vtk_field {
+    GBFV_VTK_PRESSURE = 1,        /* VtkWritePressures              true  */
+    GBFV_VTK_DENSITY = 2,         /* VtkWriteDensities              true  */
+    GBFV_VTK_SATURATION = 4,      /* VtkWriteSaturations            true  */
+    GBFV_VTK_MOBILITY = 8,        /* VtkWriteMobilities             false */
+    GBFV_VTK_RELPERM = 16,        /* VtkWriteRelativePermeabilities true  */
+    GBFV_VTK_VISCOSITY = 32,      /* VtkWriteViscosities            false */
+    GBFV_VTK_POROSITY = 64,       /* VtkWritePorosity               true  */
+    GBFV_VTK_PRIMARY_VARS = 128,  /* VtkWritePrimaryVars            false */
+    GBFV_VTK_DOF_INDEX = 256      /* VtkWriteDofIndex               false */
+};
+#define GBFV_VTK_DEFAULT_FIELDS (GBFV_VTK_PRESSURE | GBFV_VTK_DENSITY | GBFV_VTK_SATURATION | \
+                                 GBFV_VTK_RELPERM | GBFV_VTK_POROSITY)
+/* the grid's vertices and cells as the VTK file lists them: num_points
+ * points (x, y, z), each cell's vertices_per_cell vertex indices in VTK
+ * order (4: VTK_QUAD in 2D, 8: VTK_HEXAHEDRON in 3D), cells in natural order */
+typedef struct gbfv_vtk_grid {
+    int32_t num_points;
+    const double* points;          /* [num_points*3]                      */
+    int32_t vertices_per_cell;     /* 4 or 8                               */
+    const int32_t* cell_vertices;  /* [num_cells*vertices_per_cell]        */
+} gbfv_vtk_grid;
+/* One time step's XML UnstructuredGrid file (.vtu, ASCII as the
+ * reference's default VtkOutputFormat, fvbasediscretization.hh:237-238):
+ * the selected fields as Float32 cell data, each value rounded to float as
+ * VtkScalarFunction::evaluate does (vtkscalarfunction.hh:76-110), in the
+ * modules' order and with their names ("pressure_<phase>", ...,
+ * "porosity", "PV_<primary variable>", "DOF index").                     */
+int gbfv_write_vtk(gbfv_ctx* ctx, const gbfv_vtk_grid* grid, int32_t fields, const char* path);
+/* VtkMultiWriter::fileName_ + suffix (vtkmultiwriter.hh:478-488):
+ * <sim_name>-<writer_num as 5 digits>.vtu                                */
+int gbfv_vtk_file_name(const char* sim_name, int32_t writer_num, char* buf, size_t cap);
+/* the collection file (.pvd) listing the time steps written so far, as
+ * startMultiFile_ / the write tasklet / finishMultiFile_ write it
+ * (vtkmultiwriter.hh:74-96, 490-518): one DataSet per (time, file name)   */
+int gbfv_write_pvd(const char* path, int32_t n, const double* times, const char* const* files);
+
+/* ------------------------------------------------------------------ */
 /* Self-test of the device-side wait bound (no counterpart in the
  * reference): one block waits, with the bounded wait of the solver's
  * sweeps, on a barrier phase that nothing completes.  Returns

@@ -26,6 +26,7 @@ UNITS = {
     "noalloc.cu": [],
     "batchround.cu": ["-fmad=false"],
     "restart.cu": [],
+    "vtk.cu": [],
     "problem.cu": [],
 }
 

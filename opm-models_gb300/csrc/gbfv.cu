@@ -1633,6 +1633,27 @@ int gbfv_get_solution(gbfv_ctx* C, double* pv, int32_t* meaning)
     return GBFV_OK;
 }
 
+int gbfv_output_fields(gbfv_ctx* C, double* out)
+{
+    if (!C || !out) return GBFV_ERR_ARG;
+    const int N = C->N;
+    const size_t ld = C->ldN, n = (size_t)GBFV_OUTPUT_PLANES * ld;
+    double* d = nullptr;
+    int st;
+    if ((st = devAlloc(&d, n))) return st;
+    CK(cudaMemsetAsync(d, 0, sizeof(double) * n, C->stream));
+    launchOutputFields(C->mesh, C->dphys, C->x, C->meaning, C->iq, d, C->stream);
+    std::vector<double> h(n);
+    const cudaError_t e = cudaMemcpyAsync(h.data(), d, sizeof(double) * n, cudaMemcpyDeviceToHost, C->stream);
+    const cudaError_t e2 = cudaStreamSynchronize(C->stream);
+    cudaFree(d);
+    CK(e);
+    CK(e2);
+    for (int q = 0; q < GBFV_OUTPUT_PLANES; ++q)
+        for (int I = 0; I < N; ++I) out[(size_t)q * N + I] = h[(size_t)q * ld + C->perm[I]];
+    return GBFV_OK;
+}
+
 int gbfv_set_timestep(gbfv_ctx* C, double dt)
 {
     if (!C || !(dt > 0)) return GBFV_ERR_ARG;

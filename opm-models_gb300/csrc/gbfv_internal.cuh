@@ -195,6 +195,9 @@ void launchApplyConstraints(const DevMesh& m, double* x, double* xOld, int* mean
                             cudaStream_t s);
 void launchIq(const DevMesh& m, const DevPhysics* phys, const double* x, const int* meaning,
               IqBuffers iq, cudaStream_t s);
+// output quantities of the current state: out[plane*ldN + p], GBFV_OUTPUT_PLANES planes
+void launchOutputFields(const DevMesh& m, const DevPhysics* phys, const double* x, const int* meaning,
+                        IqBuffers iq, double* out, cudaStream_t s);
 void launchAssemble(const DevMesh& m, const DevPhysics* phys, IqBuffers iq, double* storageOld,
                     int iter0, double dt, double* residual, double* jval, cudaStream_t s);
 void launchSetRefPressure(const double* x, int idx, double* refP, cudaStream_t s);

@@ -57,8 +57,10 @@ void launchApplyConstraints(const DevMesh& m, double* x, double* xOld, int* mean
 // ------------------------------------------------------------- K1 --------
 // ImmiscibleIntensiveQuantities::update (immiscibleintensivequantities.hh:93-151)
 // and ImmiscibleLocalResidual::computeStorage (immisciblelocalresidual.hh:75-109)
+// out (output fields, see launchOutputFields): nullptr in the linearization
 __device__ __forceinline__ void kIqImmiscibleBody(const DevMesh& m, const DevPhysics* __restrict__ phys,
-                                                     const double* __restrict__ x, IqBuffers iq, const int p)
+                                                     const double* __restrict__ x, IqBuffers iq, const int p,
+                                                     double* __restrict__ out = nullptr)
 {
     if (p >= m.N) return;
     const int ld = m.ldN;
@@ -102,6 +104,18 @@ __device__ __forceinline__ void kIqImmiscibleBody(const DevMesh& m, const DevPhy
         iq.sto[(a * 3 + 1) * ld + p] = st.d[0];
         iq.sto[(a * 3 + 2) * ld + p] = st.d[1];
     }
+    if (out) {
+        for (int a = 0; a < 2; ++a) {
+            out[(0 * 3 + a) * ld + p] = pr[a].v;
+            out[(1 * 3 + a) * ld + p] = rho[a].v;
+            out[(2 * 3 + a) * ld + p] = S[a].v;
+            out[(3 * 3 + a) * ld + p] = lam[a].v;
+            out[(4 * 3 + a) * ld + p] = kr[a].v;
+            out[(5 * 3 + a) * ld + p] = phys->mu[a];
+        }
+        for (int q = 0; q < 6; ++q) out[(q * 3 + 2) * ld + p] = 0.0;
+        out[18 * ld + p] = phi;
+    }
 }
 
 // ImmiscibleIntensiveQuantities::update (immiscibleintensivequantities.hh:93-151)
@@ -117,7 +131,8 @@ __global__ void __launch_bounds__(256) kIqImmiscible(DevMesh m, const DevPhysics
 // Corey relperm via updateRelperms; storage per blackoillocalresidual.hh:101-188
 __device__ __forceinline__ void kIqBlackoilBody(const DevMesh& m, const DevPhysics* __restrict__ phys,
                                                    const double* __restrict__ x,
-                                                   const int* __restrict__ meaning, IqBuffers iq, const int p)
+                                                   const int* __restrict__ meaning, IqBuffers iq, const int p,
+                                                   double* __restrict__ out = nullptr)
 {
     if (p >= m.N) return;
     const int ld = m.ldN;
@@ -186,6 +201,17 @@ __device__ __forceinline__ void kIqBlackoilBody(const DevMesh& m, const DevPhysi
 #pragma unroll
         for (int j = 0; j < 3; ++j) iq.sto[(e * 4 + 1 + j) * ld + p] = tmp[e].d[j];
     }
+    if (out) {
+        for (int a = 0; a < 3; ++a) {
+            out[(0 * 3 + a) * ld + p] = pr.v;
+            out[(1 * 3 + a) * ld + p] = rho[a].v;
+            out[(2 * 3 + a) * ld + p] = S[a].v;
+            out[(3 * 3 + a) * ld + p] = lam[a].v;
+            out[(4 * 3 + a) * ld + p] = kr[a].v;
+            out[(5 * 3 + a) * ld + p] = mu[a].v;
+        }
+        out[18 * ld + p] = phi;
+    }
 }
 
 // BlackOilIntensiveQuantities::update (blackoilintensivequantities.hh:179-470)
@@ -195,6 +221,29 @@ __global__ void __launch_bounds__(256) kIqBlackoil(DevMesh m, const DevPhysics* 
                                                    const int* __restrict__ meaning, IqBuffers iq)
 {
     kIqBlackoilBody(m, phys, x, meaning, iq, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// The output quantities of the current state (the values the reference's
+// VtkMultiPhaseModule reads from the intensive quantities,
+// vtkmultiphasemodule.hh:195-260): the intensive-quantity pass with its
+// values also written to out[plane*ldN + p], planes [q*3 + phase] for q =
+// pressure, density, saturation, mobility, relative permeability, viscosity,
+// and plane 18 the porosity
+__global__ void __launch_bounds__(256) kOutputFields(DevMesh m, const DevPhysics* __restrict__ phys,
+                                                     const double* __restrict__ x, const int* __restrict__ meaning,
+                                                     IqBuffers iq, double* __restrict__ out)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m.model == GBFV_MODEL_IMMISCIBLE_2P) kIqImmiscibleBody(m, phys, x, iq, p, out);
+    else kIqBlackoilBody(m, phys, x, meaning, iq, p, out);
+}
+
+void launchOutputFields(const DevMesh& m, const DevPhysics* phys, const double* x, const int* meaning,
+                        IqBuffers iq, double* out, cudaStream_t s)
+{
+    const int bs = 256, nb = (m.N + bs - 1) / bs;
+    kOutputFields<<<nb, bs, 0, s>>>(m, phys, x, meaning, iq, out);
+    countLaunch();
 }
 
 void launchIq(const DevMesh& m, const DevPhysics* phys, const double* x, const int* meaning,

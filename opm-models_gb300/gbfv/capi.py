@@ -248,6 +248,10 @@ def load():
         "gbfv_serve_release": (C.c_int, [vp, C.c_int]),
         "gbfv_serve_footprint": (C.c_int64, [vp]),
         "gbfv_selftest_wait_timeout": (C.c_int, [dp]),
+        "gbfv_output_fields": (C.c_int, [vp, dp]),
+        "gbfv_write_vtk": (C.c_int, [vp, vp, C.c_int32, C.c_char_p]),
+        "gbfv_vtk_file_name": (C.c_int, [C.c_char_p, C.c_int32, C.c_char_p, C.c_size_t]),
+        "gbfv_write_pvd": (C.c_int, [C.c_char_p, C.c_int32, dp, C.POINTER(C.c_char_p)]),
         "gbfv_format_restart": (C.c_int, [C.POINTER(RestartInfo), C.c_int32, C.c_int32, dp, ip, C.c_char_p,
                                           C.c_size_t, C.POINTER(C.c_size_t)]),
         "gbfv_parse_restart": (C.c_int, [C.c_char_p, C.c_size_t, C.POINTER(RestartInfo), C.c_int32, C.c_int32,

@@ -204,7 +204,7 @@ static IQ2 immiscibleIQ(const Prob& P, int c, const double* pv)
 
 // phases: 0 water, 1 oil, 2 gas; PV: 0 Sw, 1 po, 2 Sg|Rs
 struct IQ3 {
-    D3 S[3], p[3], invB[3], rho[3], mu[3], lam[3];
+    D3 S[3], p[3], invB[3], rho[3], mu[3], lam[3], kr[3];
     D3 Rs;
     double phi;
 };
@@ -250,6 +250,7 @@ static IQ3 blackoilIQ(const Prob& P, int c, const double* pv, int gasMeaning)
     q.invB[2] = T.invBg.eval(q.p[2]);
     q.mu[2] = T.mug.eval(q.p[2]);
     for (int a = 0; a < 3; ++a) q.lam[a] = kr[a] / q.mu[a];
+    for (int a = 0; a < 3; ++a) q.kr[a] = kr[a];
     q.rho[0] = q.invB[0] * T.rhoRefW;
     q.rho[2] = q.invB[2] * T.rhoRefG;
     q.rho[1] = q.invB[1] * T.rhoRefO;
@@ -1423,6 +1424,47 @@ void* oracle_create(const gbfv_problem* prob, const gbfv_params* prm)
 }
 
 void oracle_destroy(void* h) { delete static_cast<Sim*>(h); }
+
+// The quantities the reference's VtkMultiPhaseModule writes
+// (vtkmultiphasemodule.hh:195-260), from the intensive quantities of the
+// current solution: out[(3*k + phase)*N + cell], k = 0 pressure, 1 density,
+// 2 saturation, 3 mobility, 4 relative permeability, 5 viscosity, and
+// out[18*N + cell] the porosity (the layout of gbfv_output_fields)
+int oracle_output_fields(void* h, double* out)
+{
+    auto* S = static_cast<Sim*>(h);
+    const int N = S->N, b = S->b;
+    std::fill(out, out + (size_t)19 * N, 0.0);
+    for (int c = 0; c < N; ++c) {
+        const double* pv = &S->x[(size_t)c * b];
+        auto put = [&](int k, int a, double v) { out[(size_t)(3 * k + a) * N + c] = v; };
+        if (b == 2) {
+            const IQ2 q = immiscibleIQ(S->P, c, pv);
+            for (int a = 0; a < 2; ++a) {
+                put(0, a, q.p[a].v);
+                put(1, a, q.rho[a].v);
+                put(2, a, q.S[a].v);
+                put(3, a, q.lam[a].v);
+                put(4, a, q.kr[a].v);
+                put(5, a, q.mu[a].v);
+            }
+            out[(size_t)18 * N + c] = q.phi;
+        }
+        else {
+            const IQ3 q = blackoilIQ(S->P, c, pv, S->meaning[c]);
+            for (int a = 0; a < 3; ++a) {
+                put(0, a, q.p[a].v);
+                put(1, a, q.rho[a].v);
+                put(2, a, q.S[a].v);
+                put(3, a, q.lam[a].v);
+                put(4, a, q.kr[a].v);
+                put(5, a, q.mu[a].v);
+            }
+            out[(size_t)18 * N + c] = q.phi;
+        }
+    }
+    return GBFV_OK;
+}
 
 // summation order of the BiCGStab scalar products: 0 the reference's
 // sequential sum, L > 0 L strided partial sums combined pairwise (test switch)

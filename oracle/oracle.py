@@ -49,6 +49,7 @@ def load():
         "oracle_set_threads": (None, [C.c_int]),
         "oracle_get_threads": (C.c_int, []),
         "oracle_set_dot_lanes": (None, [C.c_int]),
+        "oracle_output_fields": (C.c_int, [vp, dp]),
         "oracle_set_params": (C.c_int, [vp, C.POINTER(capi.Params)]),
         "oracle_set_solution": (C.c_int, [vp, dp, ip]),
         "oracle_get_solution": (C.c_int, [vp, dp, ip]),
@@ -128,6 +129,13 @@ class Oracle:
         r = np.zeros(self.N * self.b)
         self.lib.oracle_get_residual(self.h, _d(r))
         return r
+
+    def output_fields(self):
+        """[19, N]: the quantities the VTK output writes (layout of
+        gbfv_output_fields)."""
+        out = np.zeros(19 * self.N)
+        self.lib.oracle_output_fields(self.h, _d(out))
+        return out.reshape(19, self.N)
 
     def residual_scale(self):
         """Per-row sum of |terms| / V of the last linearization: the size of
