@@ -443,6 +443,45 @@ def run_workload(wl, args, flush, torch, world, sampler_local=None):
     return out
 
 
+def amg_line(wl, args, flush, torch, ilu_value=None):
+    """The workload through the AMG backend (linear_solver = LINSOLVER_AMG,
+    the reference's ParallelAmgBackend) in mixed precision: the same timed
+    time steps as the headline, the hierarchy built during the warm-up."""
+    from gbfv import Context, capi
+    w = WORKLOADS[wl]
+    prob = build_problem(wl)
+    prm = params(capi.PREC_MIXED)
+    prm.linear_solver = capi.LINSOLVER_AMG
+    ctx = Context(prob, prm)
+    ctx.save_state()
+    ext = torch.cuda.ExternalStream(ctx.stream())
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    st, _, _, _, _ = ctx.time_integration(1, w["dt"], fixed_dt=True)  # builds the hierarchy
+    setup_s = time.perf_counter() - t0
+    if st:
+        raise RuntimeError("AMG first step failed %d" % st)
+    r = timed_time_steps(ctx, w, args.steps, max(0, args.warmup - 1), flush, torch, ext)
+    value = r["cits"] / (r["ms"] / 1e3)
+    kst = r["kst"]
+    peak, peak_kind = load_peaks()
+    achieved = kst["solve_bytes"] / (kst["solve_ms"] / 1e3) / 1e9 if kst["solve_ms"] > 0 else 0.0
+    sizes, colors = ctx.amg_levels()
+    ctx.close()
+    out = {"value": value, "unit": UNIT, "ms_per_step": r["ms"] / args.steps,
+           "newton_iterations": r["newton"], "linear_iterations": r["linear"],
+           "first_step_with_setup_s": setup_s,
+           "levels": [int(v) for v in sizes], "colors": [int(v) for v in colors],
+           "roofline": {"kernel": "kAmgBicgstab<float,3> (persistent BiCGStab + AMG V-cycle, cooperative grid)",
+                        "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                        "peak_kind": peak_kind, "solve_ms_per_step": kst["solve_ms"] / args.steps},
+           "what": "mixed precision through the AMG backend (BiCGStab + aggregation AMG V-cycle, "
+                   "ParallelAmgBackend), same tolerances and time steps as the ILU(0) headline"}
+    if ilu_value:
+        out["amg_over_ilu0"] = value / ilu_value
+    return out
+
+
 def run_ours(args):
     import torch
     rank, world, local = dist_env()
@@ -568,6 +607,9 @@ def run_ours(args):
         "clocks": mixed["clocks"],
         "restart": restart_line,
     }
+    # the AMG backend on the same workload
+    if not args.headline_only:
+        line["amg"] = amg_line(args.workload, args, flush, torch, value)
     # the same two forms on the 200k-cell grid
     if args.workload != SECONDARY_WORKLOAD and not args.headline_only:
         sec = run_workload(SECONDARY_WORKLOAD, args, flush, torch, 1)

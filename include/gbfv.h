@@ -188,6 +188,8 @@ typedef struct gbfv_params {
     int32_t max_time_step_divisions;  /* MaxTimeStepDivisions       10      */
     int32_t local_linearizer;         /* LocalLinearizerSplice: enum gbfv_local_linearizer */
     int32_t numeric_difference_method;/* NumericDifferenceMethod (FD)  +1     */
+    int32_t linear_solver;            /* LinearSolverSplice: enum gbfv_linear_solver */
+    int32_t amg_coarsen_target;       /* AmgCoarsenTarget           5000    */
 } gbfv_params;
 
 /* local linearizer (Properties::LocalLinearizerSplice): automatic
@@ -199,6 +201,19 @@ typedef struct gbfv_params {
 enum gbfv_local_linearizer {
     GBFV_LIN_AD = 0,
     GBFV_LIN_FD = 1
+};
+
+/* linear-solver backend (Properties::LinearSolverSplice):
+ * ParallelBiCGStabSolverBackend (BiCGStab + block ILU(0), the default) or
+ * ParallelAmgBackend (parallelamgbackend.hh:85-330: BiCGStab preconditioned
+ * by one V-cycle of an aggregation AMG; SOR smoothing, Galerkin coarse
+ * matrices, coarsening down to amg_coarsen_target rows).  The AMG's
+ * aggregates, colours and coarse patterns are built from the first matrix a
+ * context or linear solver solves and kept for its later matrices; coarse
+ * values are recomputed at every solve.                                    */
+enum gbfv_linear_solver {
+    GBFV_LINSOLVER_ILU0 = 0,
+    GBFV_LINSOLVER_AMG = 1
 };
 
 /* fill *p with the reference's defaults */
@@ -322,6 +337,16 @@ int gbfv_linsolver_set_matrix(gbfv_linsolver* s, const double* blocks);
 /* setResidual(b) + solve(x): x = A^-1 rhs, iterations as gbfv_solve       */
 int gbfv_linsolver_solve(gbfv_linsolver* s, const double* rhs, double* x,
                          int* iterations);
+/* AMG backend (linear_solver GBFV_LINSOLVER_AMG), diagnostics: the
+ * hierarchy (built from the matrix last set if there is none yet) --
+ * rows (sizes) and colours (colors, may be NULL) of every level, at most
+ * 15; returns the level count or -status -- and one FP64 V-cycle
+ * v = M^-1 d of the preconditioner (natural order, n*b values).           */
+int gbfv_linsolver_amg_levels(gbfv_linsolver* s, int32_t* sizes,
+                              int32_t* colors);
+/* the same for a context: 0 levels before its first AMG solve            */
+int gbfv_amg_levels(gbfv_ctx* ctx, int32_t* sizes, int32_t* colors);
+int gbfv_linsolver_amg_apply(gbfv_linsolver* s, const double* d, double* v);
 
 /* ------------------------------------------------------------------ */
 /* diagnostics                                                          */

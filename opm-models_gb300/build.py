@@ -22,6 +22,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=o
 UNITS = {
     "linearize.cu": ["-fmad=false"],
     "solver.cu": [],
+    "amg.cu": ["-fmad=false"],
     "gbfv.cu": [],
     "noalloc.cu": [],
     "batchround.cu": ["-fmad=false"],

@@ -24,6 +24,7 @@
 
 #include "../../include/gbfv.h"
 #include "gbfv_internal.cuh"
+#include "amg.cuh"
 #include "solver.cuh"
 
 namespace gbfv {
@@ -137,6 +138,10 @@ struct SolverData {
     int tWidth = 0;             // the most rows a block computes in one level
     int tileKeyC = 0;           // cluster size the tables were built for
     unsigned long long* prof = nullptr;  // per-phase timers of the solve kernel (GBFV_PROFILE=1)
+    // AMG preconditioner (GBFV_LINSOLVER_AMG): the hierarchy, built at the
+    // first AMG solve; natural row of every internal row
+    AmgData* amg = nullptr;
+    std::vector<int> natural;
     // cumulative statistics of the persistent solve kernel
     cudaEvent_t evA = nullptr, evB = nullptr;
     double statMs = 0, statBytes = 0;
@@ -237,6 +242,8 @@ double solveBytes(const SolverData& S, int iters, int factor, int s)
 
 void freeSolver(SolverData& S)
 {
+    amgDestroy(S.amg);
+    S.amg = nullptr;
     cudaFree(S.col);
     cudaFree(S.levPtrD);
     cudaFree(S.tInfo);
@@ -897,10 +904,51 @@ double absTolOf(const gbfv_params& p)
     return p.linear_abs_tolerance < 0 ? p.newton_tolerance / 100.0 : p.linear_abs_tolerance;
 }
 
-// FP64 BiCGStab + ILU0 (plain form): solves A x = rhs into S.v64[0]
+// the AMG hierarchy of S, built from the FP64 matrix A at its first AMG solve
+int ensureAmg(SolverData& S, cudaStream_t stream, const double* A, const gbfv_params& prm)
+{
+    if (S.amg) return GBFV_OK;
+    if ((int)S.natural.size() != S.N) {
+        setError("AMG: the solver has no natural row order");
+        return GBFV_ERR_UNSUPPORTED;
+    }
+    AmgSystem sys;
+    sys.N = S.N;
+    sys.b = S.b;
+    sys.nslot = S.nslot;
+    sys.ld = S.ldN;
+    sys.colHost = S.colHost.data();
+    sys.natural = S.natural.data();
+    int st = GBFV_OK;
+    S.amg = amgCreate(sys, A, prm.amg_coarsen_target, stream, &st);
+    return S.amg ? GBFV_OK : (st ? st : GBFV_ERR_CUDA);
+}
+
+// BiCGStab + AMG V-cycle in precision T: statistics as the ILU(0) solves
+template <class T>
+int runAmg(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hst, const T* A, const T* rhs, T* x,
+           double redTol, double absTol, double maxRes, int maxIter, int& iters)
+{
+    float ms = 0;
+    double bytes = 0;
+    const int rs = amgSolve<T>(S.amg, A, rhs, x, redTol, absTol, maxRes, maxIter, stream, st, hst, iters, &ms, &bytes);
+    S.statMs += ms;
+    S.statLaunches++;
+    S.statIters += iters;
+    S.statBytes += bytes;
+    return rs;
+}
+
+// FP64 BiCGStab + ILU0 or AMG (plain form): solves A x = rhs into S.v64[0]
 int solvePlain(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hst, const double* A,
                const double* rhs, const gbfv_params& prm, int& iters)
 {
+    if (prm.linear_solver == GBFV_LINSOLVER_AMG) {
+        const int rs = ensureAmg(S, stream, A, prm);
+        if (rs) return rs;
+        return runAmg<double>(S, stream, st, hst, A, rhs, S.v64[0], prm.linear_tolerance, absTolOf(prm),
+                              prm.linear_max_error, prm.linear_max_iterations, iters);
+    }
     return runKrylov<double>(S, stream, st, hst, A, S.FL64, S.FD64, rhs, S.v64, 1, prm.linear_tolerance,
                              absTolOf(prm), prm.linear_max_error, prm.linear_max_iterations, iters);
 }
@@ -934,14 +982,18 @@ int solveMixed(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hst
     iters = 0;
     refinements = 0;
     if (converged(resErr)) return GBFV_OK;
+    const bool amg = prm.linear_solver == GBFV_LINSOLVER_AMG;
+    if (amg && (rs = ensureAmg(S, stream, A, prm))) return rs;
     for (int ref = 0; ref < std::max(1, prm.max_refinements); ++ref) {
         const double target = std::max(prm.linear_tolerance * resErr0, absTol);
         const double need = target / resErr;
         const double innerTol = std::min(0.5, std::max(0.5 * need, prm.inner_tolerance));
         int it = 0;
         float* vec[6] = {S.v32[1], S.v32[2], S.v32[3], S.v32[4], S.v32[5], S.v32[6]};
-        const int ks = runKrylov<float>(S, stream, st, hst, S.A32, S.FL32, S.FD32, S.v32[0], vec, ref == 0,
-                                        innerTol, 0.0, prm.linear_max_error, prm.linear_max_iterations, it);
+        const int ks = amg ? runAmg<float>(S, stream, st, hst, S.A32, S.v32[0], S.v32[1], innerTol, 0.0,
+                                           prm.linear_max_error, prm.linear_max_iterations, it)
+                           : runKrylov<float>(S, stream, st, hst, S.A32, S.FL32, S.FD32, S.v32[0], vec, ref == 0,
+                                              innerTol, 0.0, prm.linear_max_error, prm.linear_max_iterations, it);
         iters += it;
         refinements++;
         if (ks != GBFV_OK && ks != GBFV_ERR_NOT_CONVERGED) return ks;
@@ -989,6 +1041,8 @@ void gbfv_default_params(gbfv_params* p)
     p->max_time_step_divisions = 10;
     p->local_linearizer = GBFV_LIN_AD;
     p->numeric_difference_method = 1;
+    p->linear_solver = GBFV_LINSOLVER_ILU0;
+    p->amg_coarsen_target = 5000;
 }
 
 int64_t gbfv_kernel_launches(void) { return g_launches.load(); }
@@ -1464,6 +1518,7 @@ static int createImpl(gbfv_ctx* C, const gbfv_problem* P)
     S.levPtr = levPtr;
     S.adjacentLevels = adjacentLevels(lower, C->perm, levPtr);
     S.colHost = hCol;
+    S.natural = C->iperm;
     if (dim >= 2) {
         S.tileKey.resize(N);
         for (int p = 0; p < N; ++p) S.tileKey[p] = tkey[iperm[p]];
@@ -1501,6 +1556,11 @@ static bool paramsOk(const gbfv_params& p)
     if ((p.local_linearizer != GBFV_LIN_AD && p.local_linearizer != GBFV_LIN_FD) ||
         p.numeric_difference_method < -1 || p.numeric_difference_method > 1) {
         setError("unknown local linearizer or numeric difference method");
+        return false;
+    }
+    if ((p.linear_solver != GBFV_LINSOLVER_ILU0 && p.linear_solver != GBFV_LINSOLVER_AMG) ||
+        (p.linear_solver == GBFV_LINSOLVER_AMG && p.amg_coarsen_target < 1)) {
+        setError("unknown linear solver, or an AMG coarsening target below 1");
         return false;
     }
     return true;
@@ -2243,6 +2303,7 @@ gbfv_linsolver* gbfv_linsolver_create(int n, int b, const int32_t* rowPtr, const
     S.levPtr = levPtr;
     S.adjacentLevels = adjacentLevels(lower, L->perm, levPtr);
     S.colHost = hCol;
+    S.natural = L->iperm;
     int st;
     if ((st = upload(&S.col, hCol)) || (st = upload(&S.levPtrD, levPtr)) || (st = allocSolver(S)))
         return fail(L, st);
@@ -2309,6 +2370,57 @@ int gbfv_linsolver_solve(gbfv_linsolver* L, const double* rhs, double* x, int* i
     for (int i = 0; i < n; ++i)
         for (int e = 0; e < b; ++e) x[(size_t)i * b + e] = L->stage[(size_t)L->perm[i] * b + e];
     return st;
+}
+
+// The AMG hierarchy of a context (0 levels before its first AMG solve)
+int gbfv_amg_levels(gbfv_ctx* C, int32_t* sizes, int32_t* colors)
+{
+    if (!C || !sizes) return -GBFV_ERR_ARG;
+    if (!C->S.amg) return 0;
+    int sz[AMG_MAX_LEVELS], co[AMG_MAX_LEVELS];
+    const int n = amgLevelSizes(C->S.amg, sz);
+    amgLevelColors(C->S.amg, co);
+    for (int l = 0; l < n; ++l) {
+        sizes[l] = sz[l];
+        if (colors) colors[l] = co[l];
+    }
+    return n;
+}
+
+// The AMG hierarchy of the linear solver (built from the matrix last set
+// when there is none yet): rows and colours of every level
+int gbfv_linsolver_amg_levels(gbfv_linsolver* L, int32_t* sizes, int32_t* colors)
+{
+    if (!L || !sizes) return -GBFV_ERR_ARG;
+    int st = ensureAmg(L->S, L->stream, L->A64, L->prm);
+    if (st) return -st;
+    int sz[AMG_MAX_LEVELS], co[AMG_MAX_LEVELS];
+    const int n = amgLevelSizes(L->S.amg, sz);
+    amgLevelColors(L->S.amg, co);
+    for (int l = 0; l < n; ++l) {
+        sizes[l] = sz[l];
+        if (colors) colors[l] = co[l];
+    }
+    return n;
+}
+
+// one FP64 V-cycle of the AMG preconditioner, v = M^-1 d (natural order)
+int gbfv_linsolver_amg_apply(gbfv_linsolver* L, const double* d, double* v)
+{
+    if (!L || !d || !v) return GBFV_ERR_ARG;
+    int st = ensureAmg(L->S, L->stream, L->A64, L->prm);
+    if (st) return st;
+    const int n = L->N, b = L->b;
+    for (int i = 0; i < n; ++i)
+        for (int e = 0; e < b; ++e) L->stage[(size_t)L->perm[i] * b + e] = d[(size_t)i * b + e];
+    CK(cudaMemcpyAsync(L->rhs, L->stage, sizeof(double) * n * b, cudaMemcpyHostToDevice, L->stream));
+    st = amgApply64(L->S.amg, L->A64, L->rhs, L->S.v64[0], L->stream, L->st, L->hst);
+    if (st) return st;
+    CK(cudaMemcpyAsync(L->stage, L->S.v64[0], sizeof(double) * n * b, cudaMemcpyDeviceToHost, L->stream));
+    CK(cudaStreamSynchronize(L->stream));
+    for (int i = 0; i < n; ++i)
+        for (int e = 0; e < b; ++e) v[(size_t)i * b + e] = L->stage[(size_t)L->perm[i] * b + e];
+    return GBFV_OK;
 }
 
 }  // extern "C"
@@ -3101,6 +3213,10 @@ gbfv_batch* gbfv_batch_create(const gbfv_problem* probs, int num_systems, const 
     if (!probs || num_systems <= 0 || (params && !paramsOk(*params))) return fail(nullptr, GBFV_ERR_ARG);
     if (params && params->local_linearizer != GBFV_LIN_AD) {
         setError("batched systems are linearized by automatic differentiation only");
+        return fail(nullptr, GBFV_ERR_UNSUPPORTED);
+    }
+    if (params && params->linear_solver != GBFV_LINSOLVER_ILU0) {
+        setError("batched systems are solved with the ILU(0) backend only");
         return fail(nullptr, GBFV_ERR_UNSUPPORTED);
     }
     gbfv_batch* B = new gbfv_batch();

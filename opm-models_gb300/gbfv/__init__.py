@@ -139,6 +139,16 @@ class Context:
     def stream(self):
         return self.lib.gbfv_stream(self.h)
 
+    def amg_levels(self):
+        """Rows and colours of every level of the context's AMG hierarchy
+        (empty before its first AMG solve)."""
+        sizes = np.zeros(15, np.int32)
+        colors = np.zeros(15, np.int32)
+        n = self.lib.gbfv_amg_levels(self.h, _i(sizes), _i(colors))
+        if n < 0:
+            capi.check(-n, "gbfv_amg_levels")
+        return sizes[:n], colors[:n]
+
     def save_state(self):
         capi.check(self.lib.gbfv_save_state(self.h), "gbfv_save_state")
 
@@ -178,7 +188,9 @@ class Context:
 
 
 class LinearSolver:
-    """Stand-alone BiCGStab + ILU0 backend over a host BCRS matrix."""
+    """Stand-alone BiCGStab backend over a host BCRS matrix: block ILU(0)
+    (ParallelBiCGStabSolverBackend) or, with params.linear_solver =
+    LINSOLVER_AMG, the aggregation AMG V-cycle (ParallelAmgBackend)."""
 
     def __init__(self, row_ptr, col, b, params=None):
         self.lib = capi.load()
@@ -203,6 +215,23 @@ class LinearSolver:
         it = C.c_int()
         st = self.lib.gbfv_linsolver_solve(self.h, _d(rhs), _d(x), C.byref(it))
         return st, x, it.value
+
+    def amg_levels(self):
+        """Rows and colours of every level of the AMG hierarchy (built from
+        the matrix last set)."""
+        sizes = np.zeros(15, np.int32)
+        colors = np.zeros(15, np.int32)
+        n = self.lib.gbfv_linsolver_amg_levels(self.h, _i(sizes), _i(colors))
+        if n < 0:
+            capi.check(-n, "gbfv_linsolver_amg_levels")
+        return sizes[:n], colors[:n]
+
+    def amg_apply(self, d):
+        """One FP64 V-cycle v = M^-1 d of the AMG preconditioner."""
+        d = np.ascontiguousarray(d, float)
+        v = np.zeros(self.n * self.b)
+        capi.check(self.lib.gbfv_linsolver_amg_apply(self.h, _d(d), _d(v)), "gbfv_linsolver_amg_apply")
+        return v
 
     def close(self):
         if getattr(self, "h", None):

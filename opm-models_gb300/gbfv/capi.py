@@ -52,6 +52,8 @@ SOLVER_TILES = 4   # or-ed into SOLVER_CLUSTER / SOLVER_HYBRID: spatial-tile swe
 SOLVER_NARROW = 8  # or-ed into SOLVER_HYBRID (mixed precision): 256-thread blocks
 LIN_AD = 0         # local linearizer: automatic differentiation
 LIN_FD = 1         # finite differences (FvBaseFdLocalLinearizer)
+LINSOLVER_ILU0 = 0  # linear solver: BiCGStab + block ILU(0)
+LINSOLVER_AMG = 1   # BiCGStab + aggregation AMG V-cycle (ParallelAmgBackend)
 MAX_CELLS = 33554368  # GBFV_MAX_CELLS: largest grid / block-row count (32-bit device indexing)
 FLUX_DARCY = 0
 FLUX_TRANS = 1
@@ -103,6 +105,7 @@ class Params(C.Structure):
         ("water_only_threshold", C.c_double), ("min_time_step", C.c_double),
         ("max_time_step", C.c_double), ("max_time_step_divisions", C.c_int32),
         ("local_linearizer", C.c_int32), ("numeric_difference_method", C.c_int32),
+        ("linear_solver", C.c_int32), ("amg_coarsen_target", C.c_int32),
     ]
 
 
@@ -150,6 +153,8 @@ def default_params(**overrides):
     p.max_time_step_divisions = 10
     p.local_linearizer = LIN_AD
     p.numeric_difference_method = 1
+    p.linear_solver = LINSOLVER_ILU0
+    p.amg_coarsen_target = 5000     # AmgCoarsenTarget (parallelamgbackend.hh:72)
     for k, v in overrides.items():
         setattr(p, k, v)
     return p
@@ -217,6 +222,9 @@ def load():
         "gbfv_linsolver_destroy": (C.c_int, [vp]),
         "gbfv_linsolver_set_matrix": (C.c_int, [vp, dp]),
         "gbfv_linsolver_solve": (C.c_int, [vp, dp, dp, C.POINTER(C.c_int)]),
+        "gbfv_linsolver_amg_levels": (C.c_int, [vp, ip, ip]),
+        "gbfv_amg_levels": (C.c_int, [vp, ip, ip]),
+        "gbfv_linsolver_amg_apply": (C.c_int, [vp, dp, dp]),
         "gbfv_kernel_launches": (C.c_int64, []),
         "gbfv_last_error": (C.c_char_p, []),
         "gbfv_phase_times": (C.c_int, [vp, dp]),

@@ -34,9 +34,11 @@
 #include <omp.h>
 #endif
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <functional>
 #include <limits>
 #include <memory>
 #include <stdexcept>
@@ -406,6 +408,8 @@ struct Bcrs {
     }
 };
 
+struct AmgHierarchy;  // amg.hh
+
 struct Sim {
     Prob P;
     gbfv_params prm;
@@ -425,6 +429,7 @@ struct Sim {
     double error = 0, lastError = 0;
     int numIterations = 0;
     double refPressure = 1.0;  // ImmiscibleModel::referencePressure_ (immisciblemodel.hh:301-316)
+    std::shared_ptr<AmgHierarchy> amg;  // ParallelAmgBackend's hierarchy (structure kept across solves)
 };
 
 static void buildPattern(Sim& S)
@@ -1013,6 +1018,8 @@ static void spmv(const Bcrs& A, const std::vector<double>& x, std::vector<double
     }
 }
 
+#include "amg.hh"
+
 // Summation order of the scalar products (a test switch, process-wide):
 // 0 = the reference's sequential loop; L > 0 = another correct order, the
 // one a parallel machine uses: L strided partial sums (lane t takes blocks
@@ -1078,9 +1085,14 @@ struct Criterion {
     bool failed() const { return !converged() && (stagnates || resErr > maxRes); }
 };
 
-// BiCGStabSolver::apply (bicgstabsolver.hh:120-330) with SeqILU(0)
-static bool bicgstab(const Bcrs& A, const std::vector<double>& F, const std::vector<double>& b,
-                     std::vector<double>& x, Criterion& crit, int maxIter, int& iters)
+// the preconditioner application v = M^-1 d (v is written in full)
+using Precond = std::function<void(std::vector<double>&, const std::vector<double>&)>;
+
+// BiCGStabSolver::apply (bicgstabsolver.hh:120-330) with the preconditioner
+// of the backend: SeqILU(0) (ParallelBiCGStabSolverBackend) or the AMG
+// V-cycle (ParallelAmgBackend)
+static bool bicgstab(const Bcrs& A, const Precond& prec, const std::vector<double>& b, std::vector<double>& x,
+                     Criterion& crit, int maxIter, int& iters)
 {
     const double eps = std::numeric_limits<double>::min() * 1e10;
     const int bs = A.b;
@@ -1109,7 +1121,7 @@ static bool bicgstab(const Bcrs& A, const std::vector<double>& F, const std::vec
             p[i] = r[i];
             p[i] += tmp;
         }
-        ilu0Apply(A, F, y, p);
+        prec(y, p);
         spmv(A, y, v);
         double denom = dot(r0hat, v, bs);
         if (std::abs(denom) <= eps) throw NumericalProblem("BiCGStab breakdown", GBFV_ERR_BREAKDOWN);
@@ -1128,7 +1140,7 @@ static bool bicgstab(const Bcrs& A, const std::vector<double>& F, const std::vec
         if (crit.converged()) return true;
         if (crit.failed()) return false;
         z = s;
-        ilu0Apply(A, F, z, s);
+        prec(z, s);
         spmv(A, z, t);
         denom = dot(t, t, bs);
         if (std::abs(denom) <= eps) throw NumericalProblem("BiCGStab breakdown", GBFV_ERR_BREAKDOWN);
@@ -1276,10 +1288,22 @@ static int newtonUpdate(Sim& S, const std::vector<double>& cur, const std::vecto
 static int solveLinear(Sim& S, int& iters)
 {
     std::vector<double> F;
-    ilu0Factor(S.J, F);
+    Precond prec;
+    if (S.prm.linear_solver == GBFV_LINSOLVER_AMG) {
+        if (!S.amg) S.amg = std::make_shared<AmgHierarchy>();
+        amgSetup(*S.amg, S.J, S.prm.amg_coarsen_target);
+        const AmgHierarchy* H = S.amg.get();
+        prec = [H](std::vector<double>& v, const std::vector<double>& d) { amgApply(*H, v, d); };
+    }
+    else {
+        ilu0Factor(S.J, F);
+        const Bcrs* A = &S.J;
+        const std::vector<double>* Fp = &F;
+        prec = [A, Fp](std::vector<double>& v, const std::vector<double>& d) { ilu0Apply(*A, *Fp, v, d); };
+    }
     Criterion crit = makeCriterion(S.prm);
     std::vector<double> xsol;
-    const bool ok = bicgstab(S.J, F, S.residual, xsol, crit, S.prm.linear_max_iterations, iters);
+    const bool ok = bicgstab(S.J, prec, S.residual, xsol, crit, S.prm.linear_max_iterations, iters);
     S.dx = xsol;
     return ok ? GBFV_OK : GBFV_ERR_NOT_CONVERGED;
 }
@@ -1397,6 +1421,8 @@ void oracle_default_params(gbfv_params* p)
     p->max_time_step_divisions = 10;
     p->local_linearizer = GBFV_LIN_AD;
     p->numeric_difference_method = 1;
+    p->linear_solver = GBFV_LINSOLVER_ILU0;
+    p->amg_coarsen_target = 5000;
 }
 
 void* oracle_create(const gbfv_problem* prob, const gbfv_params* prm)
@@ -1655,9 +1681,18 @@ int oracle_bcrs_solve(int n, int b, const int32_t* rowPtr, const int32_t* col, c
     std::vector<double> F, xs, r(rhs, rhs + (size_t)n * b);
     int it = 0;
     try {
-        ilu0Factor(A, F);
+        AmgHierarchy H;
+        Precond prec;
+        if (prm->linear_solver == GBFV_LINSOLVER_AMG) {
+            amgSetup(H, A, prm->amg_coarsen_target);
+            prec = [&H](std::vector<double>& v, const std::vector<double>& d) { amgApply(H, v, d); };
+        }
+        else {
+            ilu0Factor(A, F);
+            prec = [&A, &F](std::vector<double>& v, const std::vector<double>& d) { ilu0Apply(A, F, v, d); };
+        }
         Criterion crit = makeCriterion(*prm);
-        const bool ok = bicgstab(A, F, r, xs, crit, prm->linear_max_iterations, it);
+        const bool ok = bicgstab(A, prec, r, xs, crit, prm->linear_max_iterations, it);
         std::memcpy(x, xs.data(), sizeof(double) * xs.size());
         if (iters) *iters = it;
         return ok ? GBFV_OK : GBFV_ERR_NOT_CONVERGED;
@@ -1666,6 +1701,41 @@ int oracle_bcrs_solve(int n, int b, const int32_t* rowPtr, const int32_t* col, c
         if (iters) *iters = it;
         return e.code;
     }
+}
+
+// The AMG hierarchy of a BCRS matrix and one V-cycle, for unit tests of the
+// GPU form: sizes[l] = rows of level l (AMG_MAX_LEVELS entries); agg0 (n
+// entries), colors0 (n entries), d / v (n*b) may each be NULL: the
+// aggregate and the colour of every row of level 0, v = V-cycle(d).
+// Returns the number of levels, or a negative status.
+int oracle_amg(int n, int b, const int32_t* rowPtr, const int32_t* col, const double* blocks, int coarsenTarget,
+               int32_t* sizes, int32_t* agg0, int32_t* colors0, const double* d, double* v)
+{
+    Bcrs A;
+    A.n = n;
+    A.b = b;
+    A.rowPtr.assign(rowPtr, rowPtr + n + 1);
+    A.col.assign(col, col + rowPtr[n]);
+    A.val.assign(blocks, blocks + (size_t)rowPtr[n] * b * b);
+    AmgHierarchy H;
+    try {
+        amgSetup(H, A, coarsenTarget);
+    }
+    catch (const NumericalProblem& e) {
+        return -e.code;
+    }
+    const int L = (int)H.lv.size();
+    for (int l = 0; l < AMG_MAX_LEVELS; ++l) sizes[l] = l < L ? H.lv[l].A.n : 0;
+    if (agg0)
+        for (int i = 0; i < n; ++i) agg0[i] = L > 1 ? H.lv[0].agg[i] : -1;
+    if (colors0)
+        for (int i = 0; i < n; ++i) colors0[i] = H.lv[0].color[i];
+    if (d && v) {
+        std::vector<double> dv(d, d + (size_t)n * b), vv;
+        amgApply(H, vv, dv);
+        std::memcpy(v, vv.data(), sizeof(double) * vv.size());
+    }
+    return L;
 }
 
 // ILU(0) factors and one application, for unit tests of the GPU kernels

@@ -68,6 +68,7 @@ def load():
         "oracle_bcrs_solve": (C.c_int, [C.c_int, C.c_int, ip, ip, dp, dp, dp,
                                         C.POINTER(capi.Params), C.POINTER(C.c_int)]),
         "oracle_ilu0": (C.c_int, [C.c_int, C.c_int, ip, ip, dp, dp, dp, dp]),
+        "oracle_amg": (C.c_int, [C.c_int, C.c_int, ip, ip, dp, C.c_int, ip, ip, ip, dp, dp]),
     }
     for n, (r, a) in sig.items():
         f = getattr(lib, n)
@@ -223,3 +224,23 @@ def ilu0(rp, col, blocks, d=None):
     st = lib.oracle_ilu0(n, b, _i(rp), _i(col), _d(blocks), _d(F),
                          _d(dd) if dd is not None else None, _d(v) if dd is not None else None)
     return st, F, v
+
+
+def amg(rp, col, blocks, coarsen_target=5000, d=None):
+    """The AMG hierarchy of a BCRS matrix (level sizes, level-0 aggregates and
+    colours) and, with d, one V-cycle v = M^-1 d.  Returns (levels or a
+    negative status, sizes, agg0, colors0, v)."""
+    lib = load()
+    n = len(rp) - 1
+    b = blocks.shape[-1]
+    rp = np.ascontiguousarray(rp, np.int32)
+    col = np.ascontiguousarray(col, np.int32)
+    blocks = np.ascontiguousarray(blocks, float)
+    sizes = np.zeros(15, np.int32)
+    agg0 = np.zeros(n, np.int32)
+    colors0 = np.zeros(n, np.int32)
+    v = np.zeros(n * b)
+    dd = None if d is None else np.ascontiguousarray(d, float)
+    L = lib.oracle_amg(n, b, _i(rp), _i(col), _d(blocks), int(coarsen_target), _i(sizes), _i(agg0), _i(colors0),
+                       _d(dd) if dd is not None else None, _d(v) if dd is not None else None)
+    return L, sizes[:max(L, 0)], agg0, colors0, v
