@@ -29,6 +29,7 @@
 // FMA contraction, so one FP64 V-cycle equals the oracle's bit for bit.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -50,6 +51,7 @@ constexpr double AMG_MIN_COARSEN_RATE = 1.05;
 constexpr double AMG_PROLONG_DAMP = 1.6;
 constexpr int AMG_PRE = 2, AMG_POST = 2, AMG_COARSEST_PAIRS = 2;
 constexpr int AMG_THREADS = 256;
+constexpr int AMG_TAIL_ROWS = 0;  // levels this small run in one block (0: none)
 
 // ------------------------------------------------------------ host setup --
 // one level's matrix in natural order (the level's own numbering)
@@ -243,6 +245,7 @@ struct AmgKArgs {
     double redTol, absTol, maxRes;
     int maxIter;
     T damp;
+    int tail;  // levels [tail, L) run in block 0 alone (tail >= L: none)
 };
 
 }  // namespace
@@ -372,6 +375,46 @@ struct FormP {
     T beta, omega;
 };
 
+// Row q's sum over its stored entries of A_qj x_j, in entry order, into
+// acc (SUB: acc -= A_qj x_j, the SOR update, skipping the diagonal and, with
+// fromZero, the columns >= c0 not visited yet; otherwise acc += A_qj x_j,
+// every column).  Entries go in chunks of U: the chunk's column indices,
+// then its matrix blocks and gathers, all issued before the first use, so a
+// row costs a few memory latencies instead of two per entry.
+template <class T, int B, bool SUB>
+__device__ __forceinline__ void rowProduct(const int* __restrict__ col, const T* __restrict__ val, int W, int ld,
+                                          int q, const T* x, int c0, bool fromZero, T (&acc)[B])
+{
+    constexpr int BB = B * B, U = sizeof(T) == 4 ? 8 : 4;
+    for (int k0 = 0; k0 < W; k0 += U) {
+        int j[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) j[u] = k0 + u < W ? __ldg(&col[(k0 + u) * ld + q]) : -1;
+        bool use[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) use[u] = j[u] >= 0 && (!SUB || (j[u] != q && !(fromZero && j[u] >= c0)));
+        T a[U][BB], xv[U][B];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+#pragma unroll
+            for (int e = 0; e < BB; ++e) a[u][e] = use[u] ? __ldg(&val[((size_t)(k0 + u) * BB + e) * ld + q]) : T(0);
+#pragma unroll
+            for (int c = 0; c < B; ++c) xv[u][c] = use[u] ? ldcg(&x[j[u] * B + c]) : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (!use[u]) continue;
+#pragma unroll
+            for (int r = 0; r < B; ++r)
+#pragma unroll
+                for (int c = 0; c < B; ++c) {
+                    if (SUB) acc[r] -= a[u][r * B + c] * xv[u][c];
+                    else acc[r] += a[u][r * B + c] * xv[u][c];
+                }
+        }
+    }
+}
+
 // One colour of an SOR sweep (relaxation 1) on rows [c0, c1) of a level:
 // x_q = D_q^-1 (rhs_q - sum_{j != q} A_qj x_j).  With fromZero the rows not
 // yet visited in this sweep (device index >= c0) count as zero.
@@ -379,8 +422,10 @@ template <class T, int B>
 __device__ __forceinline__ void sorColour(const AmgLevelDev<T>& L, const T* rhs, T* x, int c0, int c1, bool fromZero,
                                           const FormP<T>* fp, int gt, int gs)
 {
-    constexpr int BB = B * B;
     const int W = L.W, ld = L.ld;
+    const int* __restrict__ col = L.col;
+    const T* __restrict__ val = L.val;
+    const T* __restrict__ dinv = L.dinv;
     for (int q = c0 + gt; q < c1; q += gs) {
         T v[B];
         if (fp) {
@@ -400,22 +445,15 @@ __device__ __forceinline__ void sorColour(const AmgLevelDev<T>& L, const T* rhs,
 #pragma unroll
             for (int e = 0; e < B; ++e) v[e] = ldcg(&rhs[q * B + e]);
         }
-        for (int k = 0; k < W; ++k) {
-            const int j = __ldg(&L.col[k * ld + q]);
-            if (j < 0 || j == q || (fromZero && j >= c0)) continue;
-            T xj[B];
+        T d[B * B];
 #pragma unroll
-            for (int c = 0; c < B; ++c) xj[c] = ldcg(&x[j * B + c]);
-#pragma unroll
-            for (int r = 0; r < B; ++r)
-#pragma unroll
-                for (int c = 0; c < B; ++c) v[r] -= __ldg(&L.val[((size_t)k * BB + r * B + c) * ld + q]) * xj[c];
-        }
+        for (int e = 0; e < B * B; ++e) d[e] = __ldg(&dinv[(size_t)e * ld + q]);
+        rowProduct<T, B, true>(col, val, W, ld, q, x, c0, fromZero, v);
 #pragma unroll
         for (int r = 0; r < B; ++r) {
             T s = T(0);
 #pragma unroll
-            for (int c = 0; c < B; ++c) s += __ldg(&L.dinv[(size_t)(r * B + c) * ld + q]) * v[c];
+            for (int c = 0; c < B; ++c) s += d[r * B + c] * v[c];
             x[q * B + r] = s;
         }
     }
@@ -427,29 +465,22 @@ template <class T, int B>
 __device__ __forceinline__ void restrictDefect(const AmgLevelDev<T>& L, const T* rhs, const T* x, T* rc, int nc,
                                                int gt, int gs)
 {
-    constexpr int BB = B * B;
     const int W = L.W, ld = L.ld;
+    const int* __restrict__ col = L.col;
+    const T* __restrict__ val = L.val;
+    const int* __restrict__ mPtr = L.mPtr;
+    const int* __restrict__ mIdx = L.mIdx;
     for (int Q = gt; Q < nc; Q += gs) {
         T s[B];
 #pragma unroll
         for (int e = 0; e < B; ++e) s[e] = T(0);
-        const int m1 = __ldg(&L.mPtr[Q + 1]);
-        for (int m = __ldg(&L.mPtr[Q]); m < m1; ++m) {
-            const int q = __ldg(&L.mIdx[m]);
+        const int m1 = __ldg(&mPtr[Q + 1]);
+        for (int m = __ldg(&mPtr[Q]); m < m1; ++m) {
+            const int q = __ldg(&mIdx[m]);
             T y[B];
 #pragma unroll
             for (int e = 0; e < B; ++e) y[e] = T(0);
-            for (int k = 0; k < W; ++k) {
-                const int j = __ldg(&L.col[k * ld + q]);
-                if (j < 0) continue;
-                T xj[B];
-#pragma unroll
-                for (int c = 0; c < B; ++c) xj[c] = ldcg(&x[j * B + c]);
-#pragma unroll
-                for (int r = 0; r < B; ++r)
-#pragma unroll
-                    for (int c = 0; c < B; ++c) y[r] += __ldg(&L.val[((size_t)k * BB + r * B + c) * ld + q]) * xj[c];
-            }
+            rowProduct<T, B, false>(col, val, W, ld, q, x, 0, false, y);
 #pragma unroll
             for (int e = 0; e < B; ++e) s[e] += ldcg(&rhs[q * B + e]) - y[e];
         }
@@ -471,53 +502,106 @@ __device__ __forceinline__ void prolongate(const AmgLevelDev<T>& L, T* x, const 
     }
 }
 
-// one sweep of every colour, forward or backward, a grid barrier after each
-template <class T, int B>
-__device__ __forceinline__ bool sweep(const AmgKArgs<T>& a, const AmgLevelDev<T>& L, const T* rhs, T* x,
-                                      bool forward, bool fromZero, const FormP<T>* fp, int gt, int gs)
+// barrier between dependent passes: the whole grid, or (the tail levels
+// that block 0 runs alone) the block
+struct GridBar {
+    const GridSync* g;
+    __device__ bool operator()() const { return gridBarrier(*g); }
+};
+struct BlockBar {
+    __device__ bool operator()() const
+    {
+        __syncthreads();
+        return true;
+    }
+};
+
+// one sweep of every colour, forward or backward, a barrier after each
+template <class T, int B, class Bar>
+__device__ __forceinline__ bool sweep(const AmgLevelDev<T>& L, const T* rhs, T* x, bool forward, bool fromZero,
+                                      const FormP<T>* fp, int gt, int gs, const Bar& bar)
 {
     const int nc = L.nColors;
     for (int s = 0; s < nc; ++s) {
         const int c = forward ? s : nc - 1 - s;
         sorColour<T, B>(L, rhs, x, L.colorPtr[c], L.colorPtr[c + 1], fromZero, fp, gt, gs);
-        if (!gridBarrier(a.gs)) return false;
+        if (!bar()) return false;
     }
     return true;
 }
 
-// AMG::mgc (gamma 1) on x0 = M^-1 rhs0, zero initial guess on every level
+// level l on the way down: pre-smoothing, then the restricted defect into l + 1
+template <class T, int B, class Bar>
+__device__ __forceinline__ bool downLevel(const AmgKArgs<T>& a, int l, const T* rhs0, T* x0, const FormP<T>* fp,
+                                          int gt, int gs, const Bar& bar)
+{
+    const AmgLevelDev<T>& lv = a.lv[l];
+    const T* rhs = l == 0 ? rhs0 : lv.rhs;
+    T* x = l == 0 ? x0 : lv.x;
+    for (int s = 0; s < AMG_PRE; ++s)
+        if (!sweep<T, B>(lv, rhs, x, true, s == 0, (l == 0 && s == 0) ? fp : nullptr, gt, gs, bar)) return false;
+    const AmgLevelDev<T>& nx = a.lv[l + 1];
+    restrictDefect<T, B>(lv, rhs, x, nx.rhs, nx.n, gt, gs);
+    return bar();
+}
+
+// the coarsest level: forward + backward sweep pairs from a zero guess
+template <class T, int B, class Bar>
+__device__ __forceinline__ bool coarsest(const AmgKArgs<T>& a, const T* rhs0, T* x0, const FormP<T>* fp, int gt,
+                                         int gs, const Bar& bar)
+{
+    const int L = a.L;
+    const AmgLevelDev<T>& lv = a.lv[L - 1];
+    const T* rhs = L == 1 ? rhs0 : lv.rhs;
+    T* x = L == 1 ? x0 : lv.x;
+    for (int s = 0; s < AMG_COARSEST_PAIRS; ++s) {
+        if (!sweep<T, B>(lv, rhs, x, true, s == 0, (L == 1 && s == 0) ? fp : nullptr, gt, gs, bar)) return false;
+        if (!sweep<T, B>(lv, rhs, x, false, false, nullptr, gt, gs, bar)) return false;
+    }
+    return true;
+}
+
+// level l on the way up: the prolongated correction, then post-smoothing
+template <class T, int B, class Bar>
+__device__ __forceinline__ bool upLevel(const AmgKArgs<T>& a, int l, const T* rhs0, T* x0, int gt, int gs,
+                                        const Bar& bar)
+{
+    const AmgLevelDev<T>& lv = a.lv[l];
+    const T* rhs = l == 0 ? rhs0 : lv.rhs;
+    T* x = l == 0 ? x0 : lv.x;
+    prolongate<T, B>(lv, x, a.lv[l + 1].x, a.damp, gt, gs);
+    if (!bar()) return false;
+    for (int s = 0; s < AMG_POST; ++s)
+        if (!sweep<T, B>(lv, rhs, x, false, false, nullptr, gt, gs, bar)) return false;
+    return true;
+}
+
+// AMG::mgc (gamma 1) on x0 = M^-1 rhs0, zero initial guess on every level.
+// Levels [a.tail, L) -- the small coarse end of the hierarchy -- run in
+// block 0 alone with block barriers (a pass over a few thousand rows costs
+// less there than a grid barrier); the other blocks wait at the grid
+// barrier that follows.  The passes and their order are the same either way.
 template <class T, int B>
 __device__ bool vcycle(const AmgKArgs<T>& a, const T* rhs0, T* x0, const FormP<T>* fp, int gt, int gs)
 {
-    const int L = a.L;
-    for (int l = 0; l + 1 < L; ++l) {
-        const AmgLevelDev<T>& lv = a.lv[l];
-        const T* rhs = l == 0 ? rhs0 : lv.rhs;
-        T* x = l == 0 ? x0 : lv.x;
-        for (int s = 0; s < AMG_PRE; ++s)
-            if (!sweep<T, B>(a, lv, rhs, x, true, s == 0, (l == 0 && s == 0) ? fp : nullptr, gt, gs)) return false;
-        const AmgLevelDev<T>& nx = a.lv[l + 1];
-        restrictDefect<T, B>(lv, rhs, x, nx.rhs, nx.n, gt, gs);
-        if (!gridBarrier(a.gs)) return false;
-    }
-    {
-        const AmgLevelDev<T>& lv = a.lv[L - 1];
-        const T* rhs = L == 1 ? rhs0 : lv.rhs;
-        T* x = L == 1 ? x0 : lv.x;
-        for (int s = 0; s < AMG_COARSEST_PAIRS; ++s) {
-            if (!sweep<T, B>(a, lv, rhs, x, true, s == 0, (L == 1 && s == 0) ? fp : nullptr, gt, gs)) return false;
-            if (!sweep<T, B>(a, lv, rhs, x, false, false, nullptr, gt, gs)) return false;
+    const int L = a.L, split = a.tail < L - 1 ? a.tail : L - 1;
+    const GridBar gbar{&a.gs};
+    for (int l = 0; l < split; ++l)
+        if (!downLevel<T, B>(a, l, rhs0, x0, fp, gt, gs, gbar)) return false;
+    if (a.tail < L) {
+        if (blockIdx.x == 0) {
+            const BlockBar bbar;
+            const int bt = threadIdx.x, bs = blockDim.x;
+            for (int l = a.tail; l + 1 < L; ++l) downLevel<T, B>(a, l, rhs0, x0, fp, bt, bs, bbar);
+            coarsest<T, B>(a, rhs0, x0, fp, bt, bs, bbar);
+            for (int l = L - 2; l >= a.tail; --l) upLevel<T, B>(a, l, rhs0, x0, bt, bs, bbar);
         }
+        if (!gbar()) return false;
     }
-    for (int l = L - 2; l >= 0; --l) {
-        const AmgLevelDev<T>& lv = a.lv[l];
-        const T* rhs = l == 0 ? rhs0 : lv.rhs;
-        T* x = l == 0 ? x0 : lv.x;
-        prolongate<T, B>(lv, x, a.lv[l + 1].x, a.damp, gt, gs);
-        if (!gridBarrier(a.gs)) return false;
-        for (int s = 0; s < AMG_POST; ++s)
-            if (!sweep<T, B>(a, lv, rhs, x, false, false, nullptr, gt, gs)) return false;
-    }
+    else if (!coarsest<T, B>(a, rhs0, x0, fp, gt, gs, gbar))
+        return false;
+    for (int l = split - 1; l >= 0; --l)
+        if (!upLevel<T, B>(a, l, rhs0, x0, gt, gs, gbar)) return false;
     return true;
 }
 
@@ -525,20 +609,9 @@ __device__ bool vcycle(const AmgKArgs<T>& a, const T* rhs0, T* x0, const FormP<T
 template <class T, int B>
 __device__ __forceinline__ void spmvRow0(const AmgLevelDev<T>& L, const T* in, int q, T (&acc)[B])
 {
-    constexpr int BB = B * B;
 #pragma unroll
     for (int e = 0; e < B; ++e) acc[e] = T(0);
-    for (int k = 0; k < L.W; ++k) {
-        const int j = __ldg(&L.col[k * L.ld + q]);
-        if (j < 0) continue;
-        T xj[B];
-#pragma unroll
-        for (int c = 0; c < B; ++c) xj[c] = ldcg(&in[j * B + c]);
-#pragma unroll
-        for (int r = 0; r < B; ++r)
-#pragma unroll
-            for (int c = 0; c < B; ++c) acc[r] += __ldg(&L.val[((size_t)k * BB + r * B + c) * L.ld + q]) * xj[c];
-    }
+    rowProduct<T, B, false>(L.col, L.val, L.W, L.ld, q, in, 0, false, acc);
 }
 
 // BiCGStabSolver::apply (bicgstabsolver.hh:120-330) with the AMG V-cycle as
@@ -821,6 +894,9 @@ int ensurePrecision(AmgData& d)
         else
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occA, kAmgApply<T, 3>, AMG_THREADS, 0);
         occ = std::min(std::min(occ, occA), 8);
+        // blocks per SM of the cooperative launch (GBFV_AMG_BLOCKS_PER_SM
+        // caps it below what fits)
+        if (const char* e = getenv("GBFV_AMG_BLOCKS_PER_SM")) occ = std::max(1, std::min(occ, atoi(e)));
         if (occ < 1) {
             setLastError("AMG solve kernel does not fit an SM");
             return GBFV_ERR_UNSUPPORTED;
@@ -883,6 +959,18 @@ AmgKArgs<T> kargs(AmgData& d, DevStatus* st)
     a.gs.perCluster = 0;
     a.st = st;
     a.damp = (T)AMG_PROLONG_DAMP;
+    // the coarse end of the hierarchy that block 0 runs alone: levels of at
+    // most GBFV_AMG_TAIL rows (default AMG_TAIL_ROWS), never the finest
+    a.tail = a.L;
+    {
+        int rows = AMG_TAIL_ROWS;
+        if (const char* e = getenv("GBFV_AMG_TAIL")) rows = atoi(e);
+        for (int l = 1; l < a.L; ++l)
+            if (d.lv[l].n <= rows) {
+                a.tail = l;
+                break;
+            }
+    }
     return a;
 }
 
