@@ -30,6 +30,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <cstdio>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -230,6 +231,8 @@ struct AmgLevelDev {
     const int* agg;     // [q] coarse device row (levels but the coarsest)
     const int* mPtr;    // members of next-level row Q: mIdx[mPtr[Q] .. mPtr[Q+1]), ascending natural row
     const int* mIdx;
+    T* def;             // [q*B + e] the defects rhs - A x before restriction (levels but the coarsest)
+    int tpr;            // lanes that share one row of this level (1: a thread per row)
     int colorPtr[AMG_MAX_COLORS + 1];
 };
 
@@ -246,6 +249,7 @@ struct AmgKArgs {
     int maxIter;
     T damp;
     int tail;  // levels [tail, L) run in block 0 alone (tail >= L: none)
+    unsigned long long* prof;  // optional V-cycle timers (GBFV_AMG_PROFILE), 32 words
 };
 
 }  // namespace
@@ -261,8 +265,9 @@ struct AmgLevelHost {
     int* diagSlot = nullptr;  // [q] entry index of the diagonal
     int* gPtr = nullptr;      // Galerkin lists of this level's entries (levels > 0): [k*ld + q] ...
     int* gIdx = nullptr;      // ... fine entries k_f*ld_f + q_f of the level above
-    double *valD = nullptr, *dinvD = nullptr, *xD = nullptr, *rhsD = nullptr;
-    float *valF = nullptr, *dinvF = nullptr, *xF = nullptr, *rhsF = nullptr;
+    double *valD = nullptr, *dinvD = nullptr, *xD = nullptr, *rhsD = nullptr, *defD = nullptr;
+    float *valF = nullptr, *dinvF = nullptr, *xF = nullptr, *rhsF = nullptr, *defF = nullptr;
+    int tpr = 1;              // lanes per row of the last precision set up
     size_t nnzDev = 0;        // stored entries (W * n, including padding)
     size_t galerkinTerms = 0;
 };
@@ -279,6 +284,7 @@ struct AmgData {
     unsigned* bar = nullptr;
     int blocks[2] = {0, 0};
     cudaEvent_t evA = nullptr, evB = nullptr;
+    unsigned long long* prof = nullptr;  // V-cycle timers when GBFV_AMG_PROFILE names a file
 };
 
 namespace {
@@ -415,20 +421,87 @@ __device__ __forceinline__ void rowProduct(const int* __restrict__ col, const T*
     }
 }
 
+// The same sum with the row shared by a group of TPR lanes (TPR > 1, for the
+// small levels, where a thread per row leaves most of the GPU idle and a
+// row's W entries are a long chain of dependent loads): lane g of the group
+// loads entries k0 + u*TPR + g, and every lane of the group then applies all
+// entries in entry order from the group's shuffled values -- the same
+// operations in the same order as one thread, on every lane of the group.
+template <class T, int B, bool SUB, int TPR>
+__device__ __forceinline__ void rowProductGroup(const int* __restrict__ col, const T* __restrict__ val, int W, int ld,
+                                               int q, bool valid, const T* x, int c0, bool fromZero, int g, int lane0,
+                                               T (&acc)[B])
+{
+    constexpr int BB = B * B, U = 2;
+    for (int k0 = 0; k0 < W; k0 += TPR * U) {
+        bool use[U];
+        T a[U][BB], xv[U][B];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int k = k0 + u * TPR + g;
+            const int j = (valid && k < W) ? __ldg(&col[k * ld + q]) : -1;
+            use[u] = j >= 0 && (!SUB || (j != q && !(fromZero && j >= c0)));
+#pragma unroll
+            for (int e = 0; e < BB; ++e) a[u][e] = use[u] ? __ldg(&val[((size_t)k * BB + e) * ld + q]) : T(0);
+#pragma unroll
+            for (int c = 0; c < B; ++c) xv[u][c] = use[u] ? ldcg(&x[j * B + c]) : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll 1
+            for (int t = 0; t < TPR; ++t) {
+                const int src = lane0 + t;
+                const bool ut = __shfl_sync(0xffffffffu, use[u], src);
+                T av[BB], xt[B];
+#pragma unroll
+                for (int e = 0; e < BB; ++e) av[e] = __shfl_sync(0xffffffffu, a[u][e], src);
+#pragma unroll
+                for (int c = 0; c < B; ++c) xt[c] = __shfl_sync(0xffffffffu, xv[u][c], src);
+                if (!ut) continue;
+#pragma unroll
+                for (int r = 0; r < B; ++r)
+#pragma unroll
+                    for (int c = 0; c < B; ++c) {
+                        if (SUB) acc[r] -= av[r * B + c] * xt[c];
+                        else acc[r] += av[r * B + c] * xt[c];
+                    }
+            }
+    }
+}
+
+// A pass over rows [r0, r1) of a level with TPR lanes per row: body(q, valid,
+// g, lane0) once per row slot, on every lane (warp-uniform trip counts, so
+// the group shuffles see every lane).
+template <int TPR, class F>
+__device__ __forceinline__ void forRows(int r0, int r1, int gt, int gs, F&& body)
+{
+    if (TPR == 1) {
+        for (int q = r0 + gt; q < r1; q += gs) body(q, true, 0, 0);
+        return;
+    }
+    const int lane = threadIdx.x & 31, g = lane % TPR, lane0 = lane - g;
+    const int warp = gt >> 5, nWarps = gs >> 5;
+    constexpr int GPW = 32 / TPR;  // row groups per warp
+    for (int base = r0 + warp * GPW; base < r1; base += nWarps * GPW) {
+        const int q = base + lane / TPR;
+        body(q < r1 ? q : r0, q < r1, g, lane0);
+    }
+}
+
 // One colour of an SOR sweep (relaxation 1) on rows [c0, c1) of a level:
 // x_q = D_q^-1 (rhs_q - sum_{j != q} A_qj x_j).  With fromZero the rows not
 // yet visited in this sweep (device index >= c0) count as zero.
-template <class T, int B>
-__device__ __forceinline__ void sorColour(const AmgLevelDev<T>& L, const T* rhs, T* x, int c0, int c1, bool fromZero,
-                                          const FormP<T>* fp, int gt, int gs)
+template <class T, int B, int TPR>
+__device__ __forceinline__ void sorColourT(const AmgLevelDev<T>& L, const T* rhs, T* x, int c0, int c1, bool fromZero,
+                                           const FormP<T>* fp, int gt, int gs)
 {
     const int W = L.W, ld = L.ld;
     const int* __restrict__ col = L.col;
     const T* __restrict__ val = L.val;
     const T* __restrict__ dinv = L.dinv;
-    for (int q = c0 + gt; q < c1; q += gs) {
+    forRows<TPR>(c0, c1, gt, gs, [&](int q, bool valid, int g, int lane0) {
         T v[B];
-        if (fp) {
+        if (fp) {  // level 0 only, a thread per row
 #pragma unroll
             for (int e = 0; e < B; ++e) {
                 T tmp = ldcg(&fp->v[q * B + e]);
@@ -448,41 +521,75 @@ __device__ __forceinline__ void sorColour(const AmgLevelDev<T>& L, const T* rhs,
         T d[B * B];
 #pragma unroll
         for (int e = 0; e < B * B; ++e) d[e] = __ldg(&dinv[(size_t)e * ld + q]);
-        rowProduct<T, B, true>(col, val, W, ld, q, x, c0, fromZero, v);
+        if (TPR == 1) rowProduct<T, B, true>(col, val, W, ld, q, x, c0, fromZero, v);
+        else rowProductGroup<T, B, true, TPR>(col, val, W, ld, q, valid, x, c0, fromZero, g, lane0, v);
+        if (valid && g == 0) {
 #pragma unroll
-        for (int r = 0; r < B; ++r) {
-            T s = T(0);
+            for (int r = 0; r < B; ++r) {
+                T s = T(0);
 #pragma unroll
-            for (int c = 0; c < B; ++c) s += d[r * B + c] * v[c];
-            x[q * B + r] = s;
+                for (int c = 0; c < B; ++c) s += d[r * B + c] * v[c];
+                x[q * B + r] = s;
+            }
         }
+    });
+}
+
+template <class T, int B>
+__device__ __noinline__ void sorColour(const AmgLevelDev<T>& L, const T* rhs, T* x, int c0, int c1, bool fromZero,
+                                       const FormP<T>* fp, int gt, int gs)
+{
+    switch (fp ? 1 : L.tpr) {
+    case 8: sorColourT<T, B, 8>(L, rhs, x, c0, c1, fromZero, nullptr, gt, gs); break;
+    case 4: sorColourT<T, B, 4>(L, rhs, x, c0, c1, fromZero, nullptr, gt, gs); break;
+    default: sorColourT<T, B, 1>(L, rhs, x, c0, c1, fromZero, fp, gt, gs); break;
     }
 }
 
-// coarse right-hand side: the defects rhs - A x of each coarse row's members,
-// summed in ascending member order from 0
-template <class T, int B>
-__device__ __forceinline__ void restrictDefect(const AmgLevelDev<T>& L, const T* rhs, const T* x, T* rc, int nc,
-                                               int gt, int gs)
+// the defects d_q = rhs_q - A_q x of every row of a level (spmv order), a
+// coalesced pass over the level's rows
+template <class T, int B, int TPR>
+__device__ __forceinline__ void defectsT(const AmgLevelDev<T>& L, const T* rhs, const T* x, int gt, int gs)
 {
     const int W = L.W, ld = L.ld;
-    const int* __restrict__ col = L.col;
-    const T* __restrict__ val = L.val;
+    forRows<TPR>(0, L.n, gt, gs, [&](int q, bool valid, int g, int lane0) {
+        T y[B];
+#pragma unroll
+        for (int e = 0; e < B; ++e) y[e] = T(0);
+        if (TPR == 1) rowProduct<T, B, false>(L.col, L.val, W, ld, q, x, 0, false, y);
+        else rowProductGroup<T, B, false, TPR>(L.col, L.val, W, ld, q, valid, x, 0, false, g, lane0, y);
+        if (valid && g == 0)
+#pragma unroll
+            for (int e = 0; e < B; ++e) L.def[q * B + e] = ldcg(&rhs[q * B + e]) - y[e];
+    });
+}
+
+template <class T, int B>
+__device__ __noinline__ void defects(const AmgLevelDev<T>& L, const T* rhs, const T* x, int gt, int gs)
+{
+    switch (L.tpr) {
+    case 8: defectsT<T, B, 8>(L, rhs, x, gt, gs); break;
+    case 4: defectsT<T, B, 4>(L, rhs, x, gt, gs); break;
+    default: defectsT<T, B, 1>(L, rhs, x, gt, gs); break;
+    }
+}
+
+// coarse right-hand side: each coarse row's members' defects, in ascending
+// member order from 0
+template <class T, int B>
+__device__ __forceinline__ void restrictDefects(const AmgLevelDev<T>& L, T* rc, int nc, int gt, int gs)
+{
     const int* __restrict__ mPtr = L.mPtr;
     const int* __restrict__ mIdx = L.mIdx;
     for (int Q = gt; Q < nc; Q += gs) {
+        const int m0 = __ldg(&mPtr[Q]), m1 = __ldg(&mPtr[Q + 1]);
         T s[B];
 #pragma unroll
         for (int e = 0; e < B; ++e) s[e] = T(0);
-        const int m1 = __ldg(&mPtr[Q + 1]);
-        for (int m = __ldg(&mPtr[Q]); m < m1; ++m) {
+        for (int m = m0; m < m1; ++m) {
             const int q = __ldg(&mIdx[m]);
-            T y[B];
 #pragma unroll
-            for (int e = 0; e < B; ++e) y[e] = T(0);
-            rowProduct<T, B, false>(col, val, W, ld, q, x, 0, false, y);
-#pragma unroll
-            for (int e = 0; e < B; ++e) s[e] += ldcg(&rhs[q * B + e]) - y[e];
+            for (int e = 0; e < B; ++e) s[e] += ldcg(&L.def[q * B + e]);
         }
 #pragma unroll
         for (int e = 0; e < B; ++e) rc[Q * B + e] = s[e];
@@ -540,8 +647,10 @@ __device__ __forceinline__ bool downLevel(const AmgKArgs<T>& a, int l, const T* 
     T* x = l == 0 ? x0 : lv.x;
     for (int s = 0; s < AMG_PRE; ++s)
         if (!sweep<T, B>(lv, rhs, x, true, s == 0, (l == 0 && s == 0) ? fp : nullptr, gt, gs, bar)) return false;
+    defects<T, B>(lv, rhs, x, gt, gs);
+    if (!bar()) return false;
     const AmgLevelDev<T>& nx = a.lv[l + 1];
-    restrictDefect<T, B>(lv, rhs, x, nx.rhs, nx.n, gt, gs);
+    restrictDefects<T, B>(lv, nx.rhs, nx.n, gt, gs);
     return bar();
 }
 
@@ -586,8 +695,20 @@ __device__ bool vcycle(const AmgKArgs<T>& a, const T* rhs0, T* x0, const FormP<T
 {
     const int L = a.L, split = a.tail < L - 1 ? a.tail : L - 1;
     const GridBar gbar{&a.gs};
-    for (int l = 0; l < split; ++l)
+    // optional timers (block 0, thread 0; every block passes the same
+    // barriers): [l] down level l, [15] coarsest / tail, [16 + l] up level l
+    unsigned long long* pr = (a.prof && gt == 0) ? a.prof : nullptr;
+    unsigned long long t = pr ? gtimer() : 0;
+    auto tick = [&](int k) {
+        if (!pr) return;
+        const unsigned long long n = gtimer();
+        pr[k] += n - t;
+        t = n;
+    };
+    for (int l = 0; l < split; ++l) {
         if (!downLevel<T, B>(a, l, rhs0, x0, fp, gt, gs, gbar)) return false;
+        tick(l);
+    }
     if (a.tail < L) {
         if (blockIdx.x == 0) {
             const BlockBar bbar;
@@ -600,8 +721,12 @@ __device__ bool vcycle(const AmgKArgs<T>& a, const T* rhs0, T* x0, const FormP<T
     }
     else if (!coarsest<T, B>(a, rhs0, x0, fp, gt, gs, gbar))
         return false;
-    for (int l = split - 1; l >= 0; --l)
+    tick(15);
+    for (int l = split - 1; l >= 0; --l) {
         if (!upLevel<T, B>(a, l, rhs0, x0, gt, gs, gbar)) return false;
+        tick(16 + l);
+    }
+    if (pr) pr[31] += 1;
     return true;
 }
 
@@ -842,19 +967,48 @@ int ensurePrecision(AmgData& d)
     const int k = sizeof(T) == 4 ? 1 : 0;
     if (d.lvDev[k]) return GBFV_OK;
     const int bb = d.b * d.b;
-    std::vector<AmgLevelDev<T>> hl(d.lv.size());
     int st;
+    // blocks of the cooperative launch: as many as fit, at most 8 per SM
+    // (GBFV_AMG_BLOCKS_PER_SM caps it lower)
+    {
+        int dev = 0, nsm = 1, occ = 0, occA = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (d.b == 2) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kAmgBicgstab<T, 2>, AMG_THREADS, 0);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occA, kAmgApply<T, 2>, AMG_THREADS, 0);
+        }
+        else {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kAmgBicgstab<T, 3>, AMG_THREADS, 0);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occA, kAmgApply<T, 3>, AMG_THREADS, 0);
+        }
+        occ = std::min(std::min(occ, occA), 8);
+        if (const char* e = getenv("GBFV_AMG_BLOCKS_PER_SM")) occ = std::max(1, std::min(occ, atoi(e)));
+        if (occ < 1) {
+            setLastError("AMG solve kernel does not fit an SM");
+            return GBFV_ERR_UNSUPPORTED;
+        }
+        d.blocks[k] = nsm * occ;
+        // reduction partials: two halves of two values per block, for the
+        // largest grid either precision launches
+        if (!d.partial && ((st = dalloc(&d.partial, (size_t)4 * 8 * nsm)) || (st = dalloc(&d.bar, 4)))) return st;
+    }
+    const long threads = (long)d.blocks[k] * AMG_THREADS;
+    std::vector<AmgLevelDev<T>> hl(d.lv.size());
     for (size_t l = 0; l < d.lv.size(); ++l) {
         AmgLevelHost& h = d.lv[l];
-        T *val, *dinv, *x = nullptr, *rhs = nullptr;
+        T *val, *dinv, *x = nullptr, *rhs = nullptr, *def = nullptr;
         if ((st = dalloc(&val, (size_t)h.W * bb * h.ld)) || (st = dalloc(&dinv, (size_t)bb * h.ld))) return st;
         if (l > 0 && ((st = dalloc(&x, (size_t)h.ld * d.b)) || (st = dalloc(&rhs, (size_t)h.ld * d.b)))) return st;
+        if (l + 1 < d.lv.size() && (st = dalloc(&def, (size_t)h.ld * d.b))) return st;
         if (cudaMemset(val, 0, sizeof(T) * (size_t)h.W * bb * h.ld) != cudaSuccess) return GBFV_ERR_CUDA;
         if (sizeof(T) == 8) {
             h.valD = (double*)val; h.dinvD = (double*)dinv; h.xD = (double*)x; h.rhsD = (double*)rhs;
+            h.defD = (double*)def;
         }
         else {
             h.valF = (float*)val; h.dinvF = (float*)dinv; h.xF = (float*)x; h.rhsF = (float*)rhs;
+            h.defF = (float*)def;
         }
         AmgLevelDev<T>& g = hl[l];
         g.n = h.n;
@@ -866,10 +1020,22 @@ int ensurePrecision(AmgData& d)
         g.dinv = dinv;
         g.x = x;
         g.rhs = rhs;
+        g.def = def;
         g.agg = h.agg;
         g.mPtr = h.mPtr;
         g.mIdx = h.mIdx;
         for (int c = 0; c <= AMG_MAX_COLORS; ++c) g.colorPtr[c] = c <= h.nColors ? h.colorPtr[c] : h.n;
+        // lanes per row: a thread per row while a colour has rows for every
+        // thread, else as many lanes as spread a colour over the grid
+        // (4 or 8: wider groups measured slower, the in-order combine grows with
+        // them); the finest level always a thread per row
+        const long perColour = std::max(1L, ((long)h.n + h.nColors - 1) / h.nColors);
+        int tpr = 1;
+        if (8 * perColour <= threads) tpr = 8;
+        else if (4 * perColour <= threads) tpr = 4;
+        if (l == 0 || getenv("GBFV_AMG_ROW_PER_THREAD")) tpr = 1;
+        g.tpr = tpr;
+        h.tpr = tpr;
     }
     void* p = nullptr;
     if (cudaMalloc(&p, sizeof(AmgLevelDev<T>) * hl.size()) != cudaSuccess) return GBFV_ERR_OOM;
@@ -880,32 +1046,6 @@ int ensurePrecision(AmgData& d)
     if ((st = dalloc(&vec, (size_t)7 * d.lv[0].ld * d.b))) return st;
     if (sizeof(T) == 8) d.vecD = (double*)vec;
     else d.vecF = (float*)vec;
-    {
-        int dev = 0, nsm = 1, occ = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        if (d.b == 2)
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kAmgBicgstab<T, 2>, AMG_THREADS, 0);
-        else
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kAmgBicgstab<T, 3>, AMG_THREADS, 0);
-        int occA = 0;
-        if (d.b == 2)
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occA, kAmgApply<T, 2>, AMG_THREADS, 0);
-        else
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occA, kAmgApply<T, 3>, AMG_THREADS, 0);
-        occ = std::min(std::min(occ, occA), 8);
-        // blocks per SM of the cooperative launch (GBFV_AMG_BLOCKS_PER_SM
-        // caps it below what fits)
-        if (const char* e = getenv("GBFV_AMG_BLOCKS_PER_SM")) occ = std::max(1, std::min(occ, atoi(e)));
-        if (occ < 1) {
-            setLastError("AMG solve kernel does not fit an SM");
-            return GBFV_ERR_UNSUPPORTED;
-        }
-        d.blocks[k] = nsm * occ;
-        // reduction partials: two halves of two values per block, for the
-        // largest grid either precision launches
-        if (!d.partial && ((st = dalloc(&d.partial, (size_t)4 * 8 * nsm)) || (st = dalloc(&d.bar, 4)))) return st;
-    }
     return GBFV_OK;
 }
 
@@ -959,6 +1099,7 @@ AmgKArgs<T> kargs(AmgData& d, DevStatus* st)
     a.gs.perCluster = 0;
     a.st = st;
     a.damp = (T)AMG_PROLONG_DAMP;
+    a.prof = d.prof;
     // the coarse end of the hierarchy that block 0 runs alone: levels of at
     // most GBFV_AMG_TAIL rows (default AMG_TAIL_ROWS), never the finest
     a.tail = a.L;
@@ -1177,8 +1318,8 @@ void amgDestroy(AmgData* d)
     if (!d) return;
     for (AmgLevelHost& h : d->lv) {
         for (int* p : {h.col, h.agg, h.mPtr, h.mIdx, h.diagSlot, h.gPtr, h.gIdx}) cudaFree(p);
-        for (double* p : {h.valD, h.dinvD, h.xD, h.rhsD}) cudaFree(p);
-        for (float* p : {h.valF, h.dinvF, h.xF, h.rhsF}) cudaFree(p);
+        for (double* p : {h.valD, h.dinvD, h.xD, h.rhsD, h.defD}) cudaFree(p);
+        for (float* p : {h.valF, h.dinvF, h.xF, h.rhsF, h.defF}) cudaFree(p);
     }
     cudaFree(d->map0);
     cudaFree(d->lvDev[0]);
@@ -1187,6 +1328,7 @@ void amgDestroy(AmgData* d)
     cudaFree(d->vecF);
     cudaFree(d->partial);
     cudaFree(d->bar);
+    cudaFree(d->prof);
     if (d->evA) cudaEventDestroy(d->evA);
     if (d->evB) cudaEventDestroy(d->evB);
     delete d;
@@ -1216,6 +1358,11 @@ int amgSolve(AmgData* d, const T* A, const T* rhs, T* x, double redTol, double a
     cudaEventRecord(d->evA, s);
     rs = d->b == 2 ? amgValues<T, 2>(*d, A, s, st) : amgValues<T, 3>(*d, A, s, st);
     if (rs) return rs;
+    const char* profFile = getenv("GBFV_AMG_PROFILE");
+    if (profFile && !d->prof && cudaMalloc((void**)&d->prof, 32 * sizeof(unsigned long long)) != cudaSuccess)
+        return GBFV_ERR_OOM;
+    if (d->prof && cudaMemsetAsync(d->prof, 0, 32 * sizeof(unsigned long long), s) != cudaSuccess)
+        return GBFV_ERR_CUDA;
     AmgKArgs<T> a = kargs<T>(*d, st);
     a.redTol = redTol;
     a.absTol = absTol;
@@ -1238,6 +1385,32 @@ int amgSolve(AmgData* d, const T* A, const T* rhs, T* x, double redTol, double a
     }
     iters = hst->iterations;
     if (ms) cudaEventElapsedTime(ms, d->evA, d->evB);
+    if (profFile && d->prof) {
+        // one JSON line per solve: V-cycles, nanoseconds per level down / up,
+        // coarsest (or tail), and the whole solve
+        unsigned long long h[32];
+        float solveMs = 0;
+        cudaEventElapsedTime(&solveMs, d->evA, d->evB);
+        if (cudaMemcpy(h, d->prof, sizeof(h), cudaMemcpyDeviceToHost) == cudaSuccess)
+            if (FILE* f = std::fopen(profFile, "a")) {
+                const int L = (int)d->lv.size();
+                std::fprintf(f, "{\"precision\": %d, \"iterations\": %d, \"solve_ms\": %.4f, \"vcycles\": %llu, \"rows\": [",
+                             (int)sizeof(T) * 8, iters, solveMs, h[31]);
+                for (int l = 0; l < L; ++l) std::fprintf(f, "%s%d", l ? ", " : "", d->lv[l].n);
+                std::fprintf(f, "], \"colors\": [");
+                for (int l = 0; l < L; ++l) std::fprintf(f, "%s%d", l ? ", " : "", d->lv[l].nColors);
+                std::fprintf(f, "], \"width\": [");
+                for (int l = 0; l < L; ++l) std::fprintf(f, "%s%d", l ? ", " : "", d->lv[l].W);
+                std::fprintf(f, "], \"tpr\": [");
+                for (int l = 0; l < L; ++l) std::fprintf(f, "%s%d", l ? ", " : "", d->lv[l].tpr);
+                std::fprintf(f, "], \"down_ns\": [");
+                for (int l = 0; l + 1 < L; ++l) std::fprintf(f, "%s%llu", l ? ", " : "", h[l]);
+                std::fprintf(f, "], \"coarsest_ns\": %llu, \"up_ns\": [", h[15]);
+                for (int l = 0; l + 1 < L; ++l) std::fprintf(f, "%s%llu", l ? ", " : "", h[16 + l]);
+                std::fprintf(f, "], \"tail\": %d}\n", a.tail);
+                std::fclose(f);
+            }
+    }
     if (bytes) *bytes = iterationBytes(*d, (int)sizeof(T)) * iters;
     if (hst->code) return hst->code;
     return hst->converged ? GBFV_OK : GBFV_ERR_NOT_CONVERGED;
