@@ -190,6 +190,7 @@ typedef struct gbfv_params {
     int32_t numeric_difference_method;/* NumericDifferenceMethod (FD)  +1     */
     int32_t linear_solver;            /* LinearSolverSplice: enum gbfv_linear_solver */
     int32_t amg_coarsen_target;       /* AmgCoarsenTarget           5000    */
+    int32_t linearizer;               /* Properties::Linearizer: enum gbfv_linearizer */
 } gbfv_params;
 
 /* local linearizer (Properties::LocalLinearizerSplice): automatic
@@ -214,6 +215,20 @@ enum gbfv_local_linearizer {
 enum gbfv_linear_solver {
     GBFV_LINSOLVER_ILU0 = 0,
     GBFV_LINSOLVER_AMG = 1
+};
+
+/* linearizer (Properties::Linearizer): the element-wise FvBaseLinearizer
+ * (the default: every residual row and Jacobian row divided by its cell's
+ * volume) or TpfaLinearizer with BlackOilLocalResidualTPFA
+ * (tpfalinearizer.hh:711-866, blackoillocalresidualtpfa.hh:234-505): cell
+ * by cell over precomputed neighbour records, transmissibility fluxes times
+ * the face area, storage times volume / dt, rows not divided by the volume.
+ * TPFA takes the black-oil model with automatic differentiation, a problem
+ * without constraint cells (TpfaLinearizer applies none) and boundary faces
+ * that are no-flow or mass-rate; contexts only (not batches).            */
+enum gbfv_linearizer {
+    GBFV_LINEARIZER_ELEMENT = 0,
+    GBFV_LINEARIZER_TPFA = 1
 };
 
 /* fill *p with the reference's defaults */

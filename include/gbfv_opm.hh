@@ -69,6 +69,13 @@
 #include <type_traits>
 #include <vector>
 
+// the reference's linearization-type record, used by the TPFA linearizer's
+// interface (tpfalinearizer.hh:300-306)
+#if __has_include(<opm/models/discretization/common/linearizationtype.hh>)
+#include <opm/models/discretization/common/linearizationtype.hh>
+#define GBFV_OPM_HAVE_LINEARIZATION_TYPE 1
+#endif
+
 namespace Opm {
 
 // ------------------------------------------------------------ errors ------
@@ -547,6 +554,56 @@ private:
     GbfvResidualView residual_;
     GbfvJacobianView jacobian_;
     size_t linearizations_ = 0;
+};
+
+// ---------------------------------------------------- TPFA linearizer ----
+// The Linearizer property of a TPFA type tag: TpfaLinearizer
+// (tpfalinearizer.hh:116-370) with BlackOilLocalResidualTPFA, on the device
+// path with params.linearizer = GBFV_LINEARIZER_TPFA (black-oil, automatic
+// differentiation, no constraint cells).  Beyond the element linearizer's
+// surface it carries TpfaLinearizer's: the linearization type (the device
+// linearizes the fully implicit system; a pressure or sequential-transport
+// request is refused), the flows / flores / velocity records (empty: they
+// are filled only for the FLOWS, FLORES and DISPERC output of the
+// reference's simulator, which this path does not write) and an empty
+// constraints map (TpfaLinearizer applies none).
+template <class TypeTag>
+class GbfvTpfaLinearizer : public GbfvLinearizer<TypeTag> {
+    using Base = GbfvLinearizer<TypeTag>;
+
+public:
+    void setContextOptions(int model, gbfv_params prm)
+    {
+        if (model != GBFV_MODEL_BLACKOIL_3P)
+            throw std::runtime_error("GbfvTpfaLinearizer: the TPFA linearizer is the black-oil model's");
+        prm.linearizer = GBFV_LINEARIZER_TPFA;
+        Base::setContextOptions(model, prm);
+    }
+
+#ifdef GBFV_OPM_HAVE_LINEARIZATION_TYPE
+    void setLinearizationType(LinearizationType t)
+    {
+        if (t.type != LinearizationType::implicit)
+            throw std::runtime_error("GbfvTpfaLinearizer: only the fully implicit system is linearized on the device");
+        linearizationType_ = t;
+    }
+    const LinearizationType& getLinearizationType() const { return linearizationType_; }
+#endif
+
+    const std::vector<double>& getFlowsInfo() const { return noRecords_; }
+    const std::vector<double>& getFloresInfo() const { return noRecords_; }
+    const std::vector<double>& getVelocityInfo() const { return noRecords_; }
+    template <class Constraints = int>
+    std::vector<std::pair<unsigned, Constraints>> constraintsMap() const
+    {
+        return {};
+    }
+
+private:
+#ifdef GBFV_OPM_HAVE_LINEARIZATION_TYPE
+    LinearizationType linearizationType_{};
+#endif
+    std::vector<double> noRecords_;
 };
 
 // ----------------------------------------------------- solver backend ----

@@ -1025,17 +1025,14 @@ int ensurePrecision(AmgData& d)
         g.mPtr = h.mPtr;
         g.mIdx = h.mIdx;
         for (int c = 0; c <= AMG_MAX_COLORS; ++c) g.colorPtr[c] = c <= h.nColors ? h.colorPtr[c] : h.n;
-        // lanes per row: a thread per row while a colour has rows for every
-        // thread, else as many lanes as spread a colour over the grid
-        // (4 or 8: wider groups measured slower, the in-order combine grows with
-        // them); the finest level always a thread per row
+        // lanes per row: 8 where a colour has rows for at most one in eight
+        // threads, else a thread per row (measured: 4 lanes slowed the
+        // mid-size levels, 32 the small ones -- the in-order combine grows
+        // with the group); the finest level always a thread per row
         const long perColour = std::max(1L, ((long)h.n + h.nColors - 1) / h.nColors);
-        int tpr = 1;
-        if (8 * perColour <= threads) tpr = 8;
-        else if (4 * perColour <= threads) tpr = 4;
-        if (l == 0 || getenv("GBFV_AMG_ROW_PER_THREAD")) tpr = 1;
-        g.tpr = tpr;
-        h.tpr = tpr;
+        const int tpr = 8 * perColour <= threads ? 8 : 1;
+        g.tpr = (l == 0 || getenv("GBFV_AMG_ROW_PER_THREAD")) ? 1 : tpr;
+        h.tpr = g.tpr;
     }
     void* p = nullptr;
     if (cudaMalloc(&p, sizeof(AmgLevelDev<T>) * hl.size()) != cudaSuccess) return GBFV_ERR_OOM;

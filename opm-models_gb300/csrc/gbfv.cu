@@ -1043,6 +1043,7 @@ void gbfv_default_params(gbfv_params* p)
     p->numeric_difference_method = 1;
     p->linear_solver = GBFV_LINSOLVER_ILU0;
     p->amg_coarsen_target = 5000;
+    p->linearizer = GBFV_LINEARIZER_ELEMENT;
 }
 
 int64_t gbfv_kernel_launches(void) { return g_launches.load(); }
@@ -1196,6 +1197,27 @@ static int createImpl(gbfv_ctx* C, const gbfv_problem* P)
         setError("the transmissibility flux module is supported for the immiscible model");
         return GBFV_ERR_UNSUPPORTED;
     }
+    // TpfaLinearizer + BlackOilLocalResidualTPFA: black-oil, no constraint
+    // cells, boundary faces no-flow or mass-rate; its neighbour records carry
+    // the same face transmissibilities, depth terms and upwind ties
+    const bool tpfa = C->prm.linearizer == GBFV_LINEARIZER_TPFA;
+    if (tpfa) {
+        if (P->model != GBFV_MODEL_BLACKOIL_3P) {
+            setError("the TPFA linearizer is the black-oil model's (BlackOilLocalResidualTPFA)");
+            return GBFV_ERR_UNSUPPORTED;
+        }
+        for (int i = 0; P->constraint && i < N; ++i)
+            if (P->constraint[i] >= 0) {
+                setError("the TPFA linearizer applies no constraints; cell " + std::to_string(i) + " has one");
+                return GBFV_ERR_UNSUPPORTED;
+            }
+        for (int f = 0; f < P->num_bfaces; ++f)
+            if (P->bface_type[f] != GBFV_BC_NOFLOW && P->bface_type[f] != GBFV_BC_MASSRATE) {
+                setError("the TPFA linearizer takes no-flow and mass-rate boundary faces only");
+                return GBFV_ERR_UNSUPPORTED;
+            }
+    }
+    const bool needTrans = fluxModule == GBFV_FLUX_TRANS || tpfa;
     int dimWorld = 1;  // the highest coordinate axis the faces use, plus one
     for (int c = 0; c < P->num_conn; ++c)
         for (int d = 0; d < 3; ++d)
@@ -1209,7 +1231,7 @@ static int createImpl(gbfv_ctx* C, const gbfv_problem* P)
     };
     std::vector<double> hTrans, hDzg;
     std::vector<int> hTie;
-    if (fluxModule == GBFV_FLUX_TRANS) {
+    if (needTrans) {
         hTrans.assign((size_t)ndir * ld, 0.0);
         hDzg.assign((size_t)ndir * ld, 0.0);
         hTie.assign((size_t)ndir * ld, 1);
@@ -1471,9 +1493,10 @@ static int createImpl(gbfv_ctx* C, const gbfv_problem* P)
     m.numConsCells = (int)consCells.size();
     m.inst = nullptr;
     m.fluxModule = fluxModule;
+    m.tpfa = tpfa ? 1 : 0;
     m.trans = m.dzg = nullptr;
     m.tieUpI = nullptr;
-    if (fluxModule == GBFV_FLUX_TRANS) {
+    if (needTrans) {
         double *dTrans, *dDzg;
         int* dTie;
         if ((st = up(&dTrans, hTrans)) || (st = up(&dDzg, hDzg)) || (st = up(&dTie, hTie))) return st;
@@ -1563,6 +1586,14 @@ static bool paramsOk(const gbfv_params& p)
         setError("unknown linear solver, or an AMG coarsening target below 1");
         return false;
     }
+    if (p.linearizer != GBFV_LINEARIZER_ELEMENT && p.linearizer != GBFV_LINEARIZER_TPFA) {
+        setError("unknown linearizer");
+        return false;
+    }
+    if (p.linearizer == GBFV_LINEARIZER_TPFA && p.local_linearizer != GBFV_LIN_AD) {
+        setError("the TPFA linearizer differentiates automatically (local_linearizer GBFV_LIN_AD)");
+        return false;
+    }
     return true;
 }
 
@@ -1636,6 +1667,10 @@ int gbfv_destroy(gbfv_ctx* C)
 int gbfv_set_params(gbfv_ctx* C, const gbfv_params* p)
 {
     if (!C || !p || !paramsOk(*p)) return GBFV_ERR_ARG;
+    if (p->linearizer != C->prm.linearizer) {
+        setError("the linearizer is fixed when the context is created");
+        return GBFV_ERR_UNSUPPORTED;
+    }
     C->prm = *p;
     return GBFV_OK;
 }
@@ -3217,6 +3252,10 @@ gbfv_batch* gbfv_batch_create(const gbfv_problem* probs, int num_systems, const 
     }
     if (params && params->linear_solver != GBFV_LINSOLVER_ILU0) {
         setError("batched systems are solved with the ILU(0) backend only");
+        return fail(nullptr, GBFV_ERR_UNSUPPORTED);
+    }
+    if (params && params->linearizer != GBFV_LINEARIZER_ELEMENT) {
+        setError("batched systems are linearized element by element only");
         return fail(nullptr, GBFV_ERR_UNSUPPORTED);
     }
     gbfv_batch* B = new gbfv_batch();

@@ -80,6 +80,7 @@ struct DevMesh {
     const double* trans;  // [dir*ldN + p] transmissibility flux module: face transmissibility
     const double* dzg;    // [dir*ldN + p] (z_I - z_J) * g
     const int* tieUpI;    // [dir*ldN + p] interior upstream when the pressure difference is zero
+    int tpfa;             // TpfaLinearizer + BlackOilLocalResidualTPFA (rows not divided by the volume)
 };
 
 struct DevPhysics {

@@ -328,6 +328,30 @@ __device__ __forceinline__ D2 transPhase(const D2& pI, double pJ, const D2& rhoI
     return pd * (lamJ * (-T));
 }
 
+// One phase's flux of BlackOilLocalResidualTPFA::calculateFluxes_
+// (blackoillocalresidualtpfa.hh:334-385), focus = interior cell: darcy =
+// dp * mob_up * transMult * (-T / A).  The pressure difference and the
+// upstream choice are the transmissibility module's (transfluxmodule.hh:
+// 201-318: the average density times the depth term, the sign of the
+// difference, ties by volume then global index), which the reference's
+// TPFA path takes from its flux module.  transMult, the rock-compaction
+// multiplier average, is 1 here (no rock compaction) and multiplying by it
+// changes no bit, so it is left out.
+template <int B>
+__device__ __forceinline__ Dual<B> tpfaPhase(const Dual<B>& pI, double pJ, const Dual<B>& rhoI, double rhoJ,
+                                             const Dual<B>& lamI, double lamJ, double T, double area, double dzg,
+                                             bool tieUpI, bool& upI)
+{
+    Dual<B> rhoAvg = (rhoI + rhoJ) / 2.0;
+    Dual<B> pEx(pJ);
+    pEx = pEx + rhoAvg * dzg;
+    Dual<B> pd = pEx - pI;
+    upI = pd.v > 0.0 ? false : (pd.v < 0.0 ? true : tieUpI);
+    const double f = -T / area;
+    if (upI) return (pd * lamI) * f;
+    return pd * (lamJ * f);
+}
+
 // The local residual of element p (FvBaseLocalResidual::eval,
 // fvbaselocalresidual.hh:158-191) divided by its volume, with the element's
 // own intensive quantities from `iq` and its neighbours' from `nbr` (the same
@@ -447,7 +471,8 @@ struct OffBlockSink {
     double* jval;
     __device__ void operator()(int dir, int q, const Dual<B>* flux) const
     {
-        writeOffBlock<B>(jval, m.ldN, m.slotOfDir[dir ^ 1], q, flux, m.volume[q], m.cflag[q] >= 0);
+        // the TPFA linearizer's rows are not divided by the volume: V = 1 is exact
+        writeOffBlock<B>(jval, m.ldN, m.slotOfDir[dir ^ 1], q, flux, m.tpfa ? 1.0 : m.volume[q], m.cflag[q] >= 0);
     }
 };
 
@@ -526,7 +551,10 @@ __device__ __forceinline__ void localBlackoil(const DevMesh& m, const DevPhysics
             const double rhoJ = nbr.val[(1 + a) * ld + q];
             const double lamJ = nbr.val[(4 + a) * ld + q];
             bool upI;
-            D3 vf = darcyPhase<3>(pI, pJ, rhoI[a], rhoJ, lamI[a], lamJ, dTot, gIn, gEx, Kh, nrm, upI);
+            const size_t o = (size_t)dir * ld + p;
+            D3 vf = m.tpfa ? tpfaPhase<3>(pI, pJ, rhoI[a], rhoJ, lamI[a], lamJ, m.trans[o], area, m.dzg[o],
+                                          m.tieUpI[o] != 0, upI)
+                           : darcyPhase<3>(pI, pJ, rhoI[a], rhoJ, lamI[a], lamJ, dTot, gIn, gEx, Kh, nrm, upI);
             D3 invB = upI ? invBI[a] : D3(nbr.val[(7 + a) * ld + q]);
             D3 svf = invB * vf;
             flux[comp[a]] = flux[comp[a]] + svf * rhoRef[a];
@@ -567,7 +595,11 @@ __device__ __forceinline__ void localBlackoil(const DevMesh& m, const DevPhysics
         const double aa = bf.area * 1.0;
         for (int e = 0; e < 3; ++e) res[e] = res[e] + D3(bf.rate[e]) * aa;
     }
-    for (int e = 0; e < 3; ++e) res[e] = res[e] / V;
+    // FvBaseLinearizer divides each row by its volume; TpfaLinearizer
+    // (tpfalinearizer.hh:711-866) keeps the fluxes times the face area and
+    // the storage times volume / dt as they are
+    if (!m.tpfa)
+        for (int e = 0; e < 3; ++e) res[e] = res[e] / V;
 }
 
 __device__ __forceinline__ void kAssembleBlackoilBody(const DevMesh& m, const DevPhysics* __restrict__ phys,

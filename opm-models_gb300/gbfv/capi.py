@@ -54,6 +54,8 @@ LIN_AD = 0         # local linearizer: automatic differentiation
 LIN_FD = 1         # finite differences (FvBaseFdLocalLinearizer)
 LINSOLVER_ILU0 = 0  # linear solver: BiCGStab + block ILU(0)
 LINSOLVER_AMG = 1   # BiCGStab + aggregation AMG V-cycle (ParallelAmgBackend)
+LINEARIZER_ELEMENT = 0  # FvBaseLinearizer (rows divided by the cell volume)
+LINEARIZER_TPFA = 1     # TpfaLinearizer + BlackOilLocalResidualTPFA
 MAX_CELLS = 33554368  # GBFV_MAX_CELLS: largest grid / block-row count (32-bit device indexing)
 FLUX_DARCY = 0
 FLUX_TRANS = 1
@@ -106,6 +108,7 @@ class Params(C.Structure):
         ("max_time_step", C.c_double), ("max_time_step_divisions", C.c_int32),
         ("local_linearizer", C.c_int32), ("numeric_difference_method", C.c_int32),
         ("linear_solver", C.c_int32), ("amg_coarsen_target", C.c_int32),
+        ("linearizer", C.c_int32),
     ]
 
 
@@ -155,6 +158,7 @@ def default_params(**overrides):
     p.numeric_difference_method = 1
     p.linear_solver = LINSOLVER_ILU0
     p.amg_coarsen_target = 5000     # AmgCoarsenTarget (parallelamgbackend.hh:72)
+    p.linearizer = LINEARIZER_ELEMENT
     for k, v in overrides.items():
         setattr(p, k, v)
     return p

@@ -719,6 +719,119 @@ static void elementBlackoil(Sim& S, int I, const IQ3& qi, const std::vector<IQ3>
         for (int e = 0; e < 3; ++e) resJ[k * 3 + e] /= P.volume[P.connNbr[c]];
 }
 
+// TpfaLinearizer::linearize_ for cell I (tpfalinearizer.hh:711-866) with
+// BlackOilLocalResidualTPFA (blackoillocalresidualtpfa.hh:234-505): for
+// each neighbour record (the cell's interior faces in intersection order)
+// the flux of calculateFluxes_ times the face area into row I and, negated,
+// into column I of the neighbour's row; then the storage term times
+// volume / dt; rows are not divided by the volume.  The pressure difference
+// and the upstream choice of calculateFluxes_ come from the reference's
+// flux module (absent here) and are restated from the transmissibility
+// module (transfluxmodule.hh:201-318): average density times the depth
+// term, sign of the difference, ties by volume then global index.  The
+// face transmissibility is the transmissibility module's too (harmonic of
+// the half transmissibilities); transMult (rock compaction) is 1.
+static void elementBlackoilTpfa(Sim& S, int I, const IQ3& qi, const std::vector<IQ3>& iq, bool iter0, D3* res,
+                                std::vector<D3>& resJ, double* sc)
+{
+    const Prob& P = S.P;
+    const BlackOilPvt& T = P.pvt;
+    const double rhoRef[3] = {T.rhoRefW, T.rhoRefO, T.rhoRefG};
+    const int compOfPhase[3] = {1, 0, 2};
+    for (int e = 0; e < 3; ++e) {
+        res[e] = D3(0.0);
+        sc[e] = 0.0;
+    }
+    const int nc = P.connPtr[I + 1] - P.connPtr[I];
+    resJ.assign(3 * nc, D3(0.0));
+    const double g = P.g[P.dimWorld - 1];
+    int k = 0;
+    for (int c = P.connPtr[I]; c < P.connPtr[I + 1]; ++c, ++k) {
+        const int Jc = P.connNbr[c];
+        const IQ3& qj = iq[Jc];
+        const double trans = transInteriorT(P, I, Jc, c);
+        const double faceArea = P.connArea[c];
+        const double distZ = P.center[3 * I + P.dimWorld - 1] - P.center[3 * Jc + P.dimWorld - 1];
+        D3 flux[3] = {D3(0.0), D3(0.0), D3(0.0)};
+        for (int a = 0; a < 3; ++a) {
+            // calculatePhasePressureDiff_
+            D3 rhoAvg = (qi.rho[a] + qj.rho[a].v) / 2.0;
+            D3 pEx(qj.p[a].v);
+            pEx += rhoAvg * (distZ * g);
+            D3 pd = pEx - qi.p[a];
+            bool upI;
+            if (pd.v > 0.0) upI = false;
+            else if (pd.v < 0.0) upI = true;
+            else {
+                const double Vin = P.volume[I], Vex = P.volume[Jc];
+                upI = Vin > Vex ? true : (Vin < Vex ? false : I < Jc);
+            }
+            D3 darcyFlux = upI ? (pd * qi.lam[a]) * (-trans / faceArea) : pd * (qj.lam[a].v * (-trans / faceArea));
+            // evalPhaseFluxes_
+            D3 invB = upI ? qi.invB[a] : D3(qj.invB[a].v);
+            D3 svf = invB * darcyFlux;
+            flux[compOfPhase[a]] += svf * rhoRef[a];
+            if (a == 1) {
+                D3 Rs = upI ? qi.Rs : D3(qj.Rs.v);
+                flux[2] += Rs * svf * T.rhoRefG;
+            }
+        }
+        for (int e = 0; e < 3; ++e) flux[e] *= faceArea;
+        for (int e = 0; e < 3; ++e) {
+            res[e] += flux[e];
+            resJ[k * 3 + e] -= flux[e];
+            sc[e] += std::abs(flux[e].v);
+        }
+    }
+    {
+        const double storefac = P.volume[I] / S.dt;
+        D3 tmp[3] = {D3(0.0), D3(0.0), D3(0.0)};
+        D3 phi(qi.phi);
+        for (int a = 0; a < 3; ++a) {
+            D3 sv = qi.S[a] * qi.invB[a] * phi;
+            tmp[compOfPhase[a]] += sv;
+            if (a == 1) tmp[2] += qi.Rs * sv;
+        }
+        tmp[1] *= T.rhoRefW;
+        tmp[2] *= T.rhoRefG;
+        tmp[0] *= T.rhoRefO;
+        double tmp2[3];
+        if (iter0) {
+            for (int e = 0; e < 3; ++e) tmp2[e] = tmp[e].v;
+            for (int e = 0; e < 3; ++e) S.storageOld[I * 3 + e] = tmp2[e];
+        }
+        else
+            for (int e = 0; e < 3; ++e) tmp2[e] = S.storageOld[I * 3 + e];
+        for (int e = 0; e < 3; ++e) {
+            sc[e] += std::abs(tmp[e].v) * storefac + std::abs(tmp2[e]) * storefac;
+            tmp[e] -= tmp2[e];
+            tmp[e] *= storefac;
+            res[e] += tmp[e];
+        }
+    }
+    // boundary terms (mass rate; no-flow adds nothing), after the cell terms
+    for (int f = P.bfPtr[I]; f < P.bfPtr[I + 1]; ++f) {
+        if (P.bfType[f] != GBFV_BC_MASSRATE) continue;
+        const double aa = P.bfArea[f] * 1.0;
+        for (int e = 0; e < 3; ++e) res[e] += D3(P.bfValue[4 * f + e]) * aa;
+    }
+}
+
+// the TPFA linearizer's cell loop (tpfalinearizer.hh:711-866)
+static void linearizeBlackoilTpfa(Sim& S, const std::vector<IQ3>& iq)
+{
+    const bool iter0 = S.newtonIter == 0;
+#pragma omp parallel for schedule(static)
+    for (int I = 0; I < S.N; ++I) {
+        D3 res[3];
+        double sc[3];
+        std::vector<D3> resJ;
+        elementBlackoilTpfa(S, I, iq[I], iq, iter0, res, resJ, sc);
+        for (int e = 0; e < 3; ++e) S.rscale[I * 3 + e] = sc[e];
+        scatterElement<3>(S, I, res, resJ);
+    }
+}
+
 // one element of FvBaseAdLocalLinearizer::linearize + scatter, per model
 // (fvbaseadlocallinearizer.hh:173-292, fvbaselinearizer.hh:510-593)
 static void linearizeImmiscible(Sim& S, const std::vector<IQ2>& iq)
@@ -871,7 +984,9 @@ static void linearize(Sim& S)
         std::vector<IQ3> iq(S.N);
 #pragma omp parallel for schedule(static)
         for (int I = 0; I < S.N; ++I) iq[I] = blackoilIQ(S.P, I, &S.x[I * 3], S.meaning[I]);
-        if (fd)
+        if (S.prm.linearizer == GBFV_LINEARIZER_TPFA)
+            linearizeBlackoilTpfa(S, iq);
+        else if (fd)
             linearizeFd<3>(S, iq,
                            [](const Sim& s, int I, const double* x) { return blackoilIQ(s.P, I, x, s.meaning[I]); },
                            elementBlackoil);
@@ -1423,6 +1538,7 @@ void oracle_default_params(gbfv_params* p)
     p->numeric_difference_method = 1;
     p->linear_solver = GBFV_LINSOLVER_ILU0;
     p->amg_coarsen_target = 5000;
+    p->linearizer = GBFV_LINEARIZER_ELEMENT;
 }
 
 void* oracle_create(const gbfv_problem* prob, const gbfv_params* prm)

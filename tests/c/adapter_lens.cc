@@ -209,8 +209,43 @@ Opm::StructuredGridView<2> lensGrid()
 
 }  // namespace
 
+// The TPFA linearizer's adapter, every member compiled against the same
+// shim (its numerics are tested through the C ABI, tests/test_gpu_tpfa.py)
+template class Opm::GbfvTpfaLinearizer<LensGbfv>;
+
+// what the TPFA adapter refuses, on the host (no context is created)
+static int tpfaRefusals()
+{
+    Opm::GbfvTpfaLinearizer<LensGbfv> lin;
+    int refused = 0;
+    try {
+        lin.setContextOptions(GBFV_MODEL_IMMISCIBLE_2P, Opm::gbfvDefaultParams());
+    }
+    catch (const std::runtime_error&) {
+        ++refused;
+    }
+    Opm::LinearizationType t;
+    t.type = Opm::LinearizationType::pressure;
+    try {
+        lin.setLinearizationType(t);
+    }
+    catch (const std::runtime_error&) {
+        ++refused;
+    }
+    t.type = Opm::LinearizationType::implicit;
+    t.time = 3;
+    lin.setLinearizationType(t);
+    const bool kept = lin.getLinearizationType().time == 3;
+    lin.setContextOptions(GBFV_MODEL_BLACKOIL_3P, Opm::gbfvDefaultParams());
+    const bool empty = lin.getFlowsInfo().empty() && lin.getFloresInfo().empty() && lin.getVelocityInfo().empty() &&
+                       lin.constraintsMap().empty();
+    std::printf("tpfa refused %d kept %d empty %d\n", refused, kept ? 1 : 0, empty ? 1 : 0);
+    return refused == 2 && kept && empty ? 0 : 1;
+}
+
 int main(int argc, char** argv)
 {
+    if (argc >= 2 && std::string(argv[1]) == "tpfa") return tpfaRefusals();
     if (argc < 3) {
         std::fprintf(stderr, "usage: adapter_lens describe <file> | run <steps> <nan_step> <file>\n");
         return 2;

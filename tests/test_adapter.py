@@ -33,7 +33,8 @@ LIBDIR = os.path.join(ROOT, "opm-models_gb300", "_build")
 def _build(tmp_path):
     exe = str(tmp_path / "adapter_lens")
     cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror", "-ffp-contract=off",
-           "-I" + os.path.join(ROOT, "include"), "-o", exe, SRC, "-L" + LIBDIR, "-lgbfv",
+           "-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(ROOT, "tests", "c", "shim_include"),
+           "-o", exe, SRC, "-L" + LIBDIR, "-lgbfv",
            "-Wl,-rpath," + LIBDIR]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
@@ -135,3 +136,15 @@ def test_lens_through_the_adapter_equals_the_device_path(built, tmp_path, nan_st
     assert jac_syncs == 0 and res_syncs == 0
     assert host_syncs == steps
     assert linearizations >= int(its.sum()) and lin_total > 0
+
+
+def test_tpfa_adapter_compiles_and_refuses_on_the_host(built, tmp_path):
+    """GbfvTpfaLinearizer (the TPFA type tag's Linearizer) is instantiated
+    in full against the shim; on the host it refuses a non-black-oil model
+    and a pressure or sequential-transport linearization type, keeps the
+    implicit one, and has empty flows / flores / velocity records and
+    constraints, as TpfaLinearizer without FLOWS, FLORES or DISPERC."""
+    exe = _build(tmp_path)
+    r = subprocess.run([exe, "tpfa"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "tpfa refused 2 kept 1 empty 1" in r.stdout
