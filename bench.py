@@ -443,6 +443,28 @@ def run_workload(wl, args, flush, torch, world, sampler_local=None):
     return out
 
 
+# one-way hop of a level's result to a consumer CTA of the cluster
+# (st.async of 16 B counted on the receiver's mbarrier), measured by a
+# micro-benchmark on a GB300: the least a dependent level step can take
+LEVEL_HOP_CYCLES = 370
+
+
+def latency_floor(w, kst, clocks):
+    """Latency roofline of the ILU(0) solver: exact ILU(0) fixes the
+    wavefront level count (nx + ny + nz - 2 on these grids), every BiCGStab
+    iteration runs two preconditioner applications of a forward and a
+    backward sweep over all levels, and no level step can be shorter than
+    one hop of its result to the next level's CTA.  floor_ms = iterations x
+    4 x levels x hop; frac = floor_ms / the solver's measured time."""
+    levels = w["nx"] + w["ny"] + w["nz"] - 2
+    mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    hop_us = LEVEL_HOP_CYCLES / mhz
+    floor_ms = kst["solve_iterations"] * 4 * levels * hop_us / 1e3
+    return {"levels_per_sweep": levels, "sweeps_per_iteration": 4, "hop_cycles": LEVEL_HOP_CYCLES,
+            "hop_us": hop_us, "iterations": int(kst["solve_iterations"]), "floor_ms": floor_ms,
+            "solver_ms": kst["solve_ms"], "frac": floor_ms / kst["solve_ms"] if kst["solve_ms"] > 0 else None}
+
+
 def amg_line(wl, args, flush, torch, ilu_value=None):
     """The workload through the AMG backend (linear_solver = LINSOLVER_AMG,
     the reference's ParallelAmgBackend) in mixed precision: the same timed
@@ -601,7 +623,8 @@ def run_ours(args):
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "traffic_kind": traffic_kind, "peak_kind": peak_kind,
                      "avg_launch_ms": avg_launch_ms,
-                     "bytes_per_launch": kst["solve_bytes"] / max(1, kst["solve_launches"])},
+                     "bytes_per_launch": kst["solve_bytes"] / max(1, kst["solve_launches"]),
+                     "latency_floor": latency_floor(w, kst, mixed["clocks"])},
         "solver_config": {"mixed": mixed["cfg"], "fp64": plain["cfg"]},
         "linearize_roofline": {"achieved": lin_ach, "frac": lin_ach / peak, "ms": kst["linearize_ms"] / args.steps},
         "clocks": mixed["clocks"],

@@ -12,7 +12,8 @@
 // (Vanek-Mandel-Brezina: a root with its strong neighbours, left-over rows
 // join their strongest aggregated neighbour, the rest root aggregates of
 // their own), the Galerkin patterns with, for every coarse block, the list of
-// fine blocks it sums, and a greedy colouring of every level.  Each level is
+// fine blocks it sums, and a greedy colouring of every level (row order on
+// the finest, smallest-last order on the coarse ones).  Each level is
 // then renumbered colour by colour, so one colour of an SOR sweep is one
 // contiguous, coalesced range of rows: a dependent chain of rows (dune's
 // natural-order sweep) becomes a handful of parallel passes.  Every solve
@@ -32,6 +33,7 @@
 #include <cstdlib>
 #include <cstdio>
 #include <cstring>
+#include <set>
 #include <string>
 #include <vector>
 
@@ -199,13 +201,46 @@ void galerkin(const Csr& A, int bb, const std::vector<int>& agg, int nc, Csr& Ac
         }
 }
 
-// greedy colouring in row order; returns the colour count
-int colourRows(const Csr& A, std::vector<int>& color)
+// the rows by smallest-last order (Matula, Beck): the row of least degree
+// among those left is removed next (ties: lowest row), and the rows are
+// coloured in the reverse order of removal
+std::vector<int> smallestLast(const Csr& A)
+{
+    const int n = A.n;
+    std::vector<int> deg(n, 0);
+    for (int i = 0; i < n; ++i)
+        for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) deg[i] += A.col[k] != i;
+    std::set<std::pair<int, int>> left;
+    for (int i = 0; i < n; ++i) left.emplace(deg[i], i);
+    std::vector<char> gone(n, 0);
+    std::vector<int> order(n);
+    for (int t = n - 1; t >= 0; --t) {
+        const int v = left.begin()->second;
+        left.erase(left.begin());
+        gone[v] = 1;
+        order[t] = v;
+        for (int k = A.ptr[v]; k < A.ptr[v + 1]; ++k) {
+            const int j = A.col[k];
+            if (j == v || gone[j]) continue;
+            left.erase({deg[j], j});
+            left.emplace(--deg[j], j);
+        }
+    }
+    return order;
+}
+
+// greedy colouring (the smallest colour no coloured neighbour has) in row
+// order on the finest level, in smallest-last order on the coarse ones;
+// returns the colour count
+int colourRows(const Csr& A, bool finest, std::vector<int>& color)
 {
     color.assign(A.n, -1);
     int nc = 0;
     std::vector<char> seen;
-    for (int i = 0; i < A.n; ++i) {
+    std::vector<int> order;
+    if (!finest) order = smallestLast(A);
+    for (int t = 0; t < A.n; ++t) {
+        const int i = finest ? t : order[t];
         seen.assign(nc + 1, 0);
         for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) {
             const int j = A.col[k];
@@ -1207,7 +1242,7 @@ AmgData* amgCreate(const AmgSystem& sys, const double* A64, int coarsenTarget, c
     std::vector<std::vector<int>> pos(L), rowOf(L);
     for (int l = 0; l < L; ++l) {
         std::vector<int> color;
-        const int nc = colourRows(A[l], color);
+        const int nc = colourRows(A[l], l == 0, color);
         if (nc > AMG_MAX_COLORS)
             return fail(d, GBFV_ERR_UNSUPPORTED, "AMG: a level needs more than " + std::to_string(AMG_MAX_COLORS) +
                                                      " colours");

@@ -24,7 +24,8 @@
 //     aggregate; the rest form aggregates of their own) instead of dune's
 //     diameter-bounded aggregate growing;
 //   * the SOR sweeps visit the rows colour by colour (greedy colouring of the
-//     level's graph in row order), rows of one colour in any order -- the
+//     level's graph, in row order on the finest level and in smallest-last
+//     order on the coarse ones), rows of one colour in any order -- the
 //     natural-order sweep of dune-istl is one chain of dependent rows;
 //   * the coarsest level is smoothed (2 forward + backward sweep pairs)
 //     instead of being solved directly;
@@ -195,14 +196,52 @@ static void galerkinValues(const Bcrs& A, const std::vector<int>& gPtr, const st
         }
 }
 
-// greedy colouring in row order: the smallest colour no coloured neighbour has
-static void colour(AmgLevel& L)
+// smallest-last vertex order (Matula and Beck 1983): repeatedly remove the
+// row of least degree among those left (ties: the lowest row); the colouring
+// visits them in the reverse order of removal
+static std::vector<int> smallestLastOrder(const Bcrs& A)
+{
+    const int n = A.n;
+    std::vector<int> deg(n, 0);
+    for (int i = 0; i < n; ++i)
+        for (int k = A.rowPtr[i]; k < A.rowPtr[i + 1]; ++k)
+            if (A.col[k] != i) ++deg[i];
+    std::set<std::pair<int, int>> left;
+    for (int i = 0; i < n; ++i) left.insert({deg[i], i});
+    std::vector<char> gone(n, 0);
+    std::vector<int> order;
+    order.reserve(n);
+    while (!left.empty()) {
+        const int v = left.begin()->second;
+        left.erase(left.begin());
+        gone[v] = 1;
+        order.push_back(v);
+        for (int k = A.rowPtr[v]; k < A.rowPtr[v + 1]; ++k) {
+            const int j = A.col[k];
+            if (j == v || gone[j]) continue;
+            left.erase({deg[j], j});
+            --deg[j];
+            left.insert({deg[j], j});
+        }
+    }
+    std::reverse(order.begin(), order.end());
+    return order;
+}
+
+// greedy colouring: the smallest colour no coloured neighbour has, the rows
+// visited in row order on the finest level (a red-black colouring of the
+// 5/7-point pattern) and in smallest-last order on the coarse levels
+// (fewer colours on the aggregates' graphs)
+static void colour(AmgLevel& L, bool finest)
 {
     const Bcrs& A = L.A;
     L.color.assign(A.n, -1);
     int nc = 0;
     std::vector<int> seen;
-    for (int i = 0; i < A.n; ++i) {
+    std::vector<int> order;
+    if (!finest) order = smallestLastOrder(A);
+    for (int t = 0; t < A.n; ++t) {
+        const int i = finest ? t : order[t];
         seen.assign(nc + 1, 0);
         for (int k = A.rowPtr[i]; k < A.rowPtr[i + 1]; ++k) {
             const int j = A.col[k];
@@ -254,7 +293,7 @@ static void amgSetup(AmgHierarchy& H, const Bcrs& A, int coarsenTarget)
             L.nextN = nc;
             H.lv.push_back(std::move(next));
         }
-        for (AmgLevel& L : H.lv) colour(L);
+        for (size_t l = 0; l < H.lv.size(); ++l) colour(H.lv[l], l == 0);
         H.built = true;
     }
     else {
