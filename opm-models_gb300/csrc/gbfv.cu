@@ -142,6 +142,9 @@ struct SolverData {
     // first AMG solve; natural row of every internal row
     AmgData* amg = nullptr;
     std::vector<int> natural;
+    // max-norm residual reduction the last solve reached: the FP64 true
+    // residual for the mixed form, BiCGStab's residual for the plain one
+    double lastReduction = 0.0, lastResidual = 0.0;
     // cumulative statistics of the persistent solve kernel
     cudaEvent_t evA = nullptr, evB = nullptr;
     double statMs = 0, statBytes = 0;
@@ -943,14 +946,18 @@ int runAmg(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hst, co
 int solvePlain(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hst, const double* A,
                const double* rhs, const gbfv_params& prm, int& iters)
 {
+    int rs;
     if (prm.linear_solver == GBFV_LINSOLVER_AMG) {
-        const int rs = ensureAmg(S, stream, A, prm);
-        if (rs) return rs;
-        return runAmg<double>(S, stream, st, hst, A, rhs, S.v64[0], prm.linear_tolerance, absTolOf(prm),
-                              prm.linear_max_error, prm.linear_max_iterations, iters);
+        if ((rs = ensureAmg(S, stream, A, prm))) return rs;
+        rs = runAmg<double>(S, stream, st, hst, A, rhs, S.v64[0], prm.linear_tolerance, absTolOf(prm),
+                            prm.linear_max_error, prm.linear_max_iterations, iters);
     }
-    return runKrylov<double>(S, stream, st, hst, A, S.FL64, S.FD64, rhs, S.v64, 1, prm.linear_tolerance,
-                             absTolOf(prm), prm.linear_max_error, prm.linear_max_iterations, iters);
+    else
+        rs = runKrylov<double>(S, stream, st, hst, A, S.FL64, S.FD64, rhs, S.v64, 1, prm.linear_tolerance,
+                               absTolOf(prm), prm.linear_max_error, prm.linear_max_iterations, iters);
+    S.lastReduction = hst->resid0 > 0 ? hst->resid / hst->resid0 : 0.0;
+    S.lastResidual = hst->resid;
+    return rs;
 }
 
 // FP32 BiCGStab + FP32 ILU0 under FP64 iterative refinement (mixed form):
@@ -981,6 +988,8 @@ int solveMixed(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hst
     };
     iters = 0;
     refinements = 0;
+    S.lastReduction = 1.0;
+    S.lastResidual = resErr;
     if (converged(resErr)) return GBFV_OK;
     const bool amg = prm.linear_solver == GBFV_LINSOLVER_AMG;
     if (amg && (rs = ensureAmg(S, stream, A, prm))) return rs;
@@ -1004,6 +1013,8 @@ int solveMixed(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hst
         unsigned long long bits = hst->errorBits;
         std::memcpy(&resErr, &bits, sizeof(double));
         if (!std::isfinite(resErr)) return GBFV_ERR_NONFINITE;
+        S.lastReduction = resErr / std::max(1e-20, resErr0);
+        S.lastResidual = resErr;
         if (converged(resErr)) return GBFV_OK;
         if (resErr > prm.linear_max_error * resErr0) return GBFV_ERR_NOT_CONVERGED;
         if (ks == GBFV_ERR_NOT_CONVERGED && it >= prm.linear_max_iterations) return GBFV_ERR_NOT_CONVERGED;
@@ -1915,15 +1926,17 @@ static int solveImpl(gbfv_ctx* C, int* iterations)
     C->haveDx = 1;
     if (!C->solveLog.empty()) {
         // one JSON line per solve (GBFV_SOLVE_LOG): iterations, refinements,
-        // device time and algorithmic bytes of the solver launches
+        // the max-norm residual reduction reached and the residual (the FP64
+        // true residual for the mixed form), device time and algorithmic
+        // bytes of the solver launches
         const double ms = C->S.statMs - ms0, bytes = C->S.statBytes - bytes0;
         if (FILE* f = fopen(C->solveLog.c_str(), "a")) {
             fprintf(f,
                     "{\"cells\": %d, \"newton_iteration\": %d, \"precision\": \"%s\", \"status\": %d, "
-                    "\"iterations\": %d, \"refinements\": %d, \"solve_ms\": %.6g, \"bytes\": %.6g, "
-                    "\"achieved_gbs\": %.6g}\n",
-                    C->N, C->newtonIter, C->prm.precision == GBFV_PREC_MIXED ? "mixed" : "fp64", st, it, ref, ms,
-                    bytes, ms > 0 ? bytes / (ms * 1e6) : 0.0);
+                    "\"iterations\": %d, \"refinements\": %d, \"residual_reduction\": %.6g, \"residual\": %.6g, "
+                    "\"solve_ms\": %.6g, \"bytes\": %.6g, \"achieved_gbs\": %.6g}\n",
+                    C->N, C->newtonIter, C->prm.precision == GBFV_PREC_MIXED ? "mixed" : "fp64", st, it, ref,
+                    C->S.lastReduction, C->S.lastResidual, ms, bytes, ms > 0 ? bytes / (ms * 1e6) : 0.0);
             fclose(f);
         }
     }

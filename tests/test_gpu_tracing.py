@@ -1,7 +1,8 @@
 """Per-solve records (GBFV_SOLVE_LOG): with the variable set when a context
 is created, every linear solve appends one JSON line -- iterations,
-refinements, device time and algorithmic bytes of its solver launches --
-and the lines add up to the context's kernel statistics."""
+refinements, the residual reduction it reached (for the mixed form the FP64
+true residual's), device time and algorithmic bytes of its solver launches
+-- and the lines add up to the context's kernel statistics."""
 import json
 
 import pytest
@@ -29,3 +30,7 @@ def test_solve_log_lines(built, tmp_path, monkeypatch):
     assert sum(r["iterations"] for r in recs) == int(lits.sum())
     assert abs(sum(r["solve_ms"] for r in recs) - ks["solve_ms"]) <= 1e-6 * max(1.0, ks["solve_ms"])
     assert abs(sum(r["bytes"] for r in recs) - ks["solve_bytes"]) <= 1e-6 * ks["solve_bytes"]
+    # every mixed solve met the tolerance on its FP64 true residual: the
+    # relative reduction 1e-6 or the absolute bar (Newton tolerance / 100)
+    assert all(r["residual_reduction"] <= 1e-6 * (1 + 1e-9) or r["residual"] <= 1e-8 * (1 + 1e-9) for r in recs), \
+        [(r["residual_reduction"], r["residual"]) for r in recs]
