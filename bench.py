@@ -504,6 +504,69 @@ def amg_line(wl, args, flush, torch, ilu_value=None):
     return out
 
 
+def ensemble_leg(count, torch):
+    """A compact C4 line inside the default benchmark: `count` seeded
+    two-phase realizations (10k-200k cells) advanced together by the batched
+    path in mixed precision, the same batch in plain FP64, and a sample of 4
+    of them one at a time in plain FP64 -- the form the batched mixed rate is
+    compared with (batched_mixed_over_plain_fp64).  One untimed run of each,
+    then one timed run of ENSEMBLE["steps"] time steps."""
+    from gbfv import Batch, Context, capi
+    probs = ensemble_problems(count)
+    Ns = np.array([p.num_cells for p in probs])
+
+    def batched(prec):
+        B = Batch(probs, params(prec))
+        B.autotune(ENSEMBLE["dt"])
+        for c in B.systems:
+            c.save_state()
+        ext = torch.cuda.ExternalStream(B.stream())
+        out = None
+        for _ in range(2):
+            for c in B.systems:
+                c.restore_state()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            st = B.time_integration(ENSEMBLE["steps"], ENSEMBLE["dt"])
+            e1.record(ext)
+            e1.synchronize()
+            if st:
+                raise RuntimeError("batched run failed %d" % st)
+            cits = sum(int(B.report(i)[2].sum()) * int(Ns[i]) for i in range(len(probs)))
+            out = (cits / (e0.elapsed_time(e1) / 1000.0), [B.report(i)[2].tolist() for i in range(len(probs))])
+        B.close()
+        return out
+
+    mixed, newton = batched(capi.PREC_MIXED)
+    fp64, newton64 = batched(capi.PREC_FP64)
+    ms, cits = 0.0, 0
+    for i in range(0, len(probs), max(1, len(probs) // 4))[:4]:
+        ctx = Context(probs[i], params(capi.PREC_FP64))
+        ctx.time_integration(ENSEMBLE["steps"], ENSEMBLE["dt"])  # warm-up incl. autotuning
+        ctx.set_solution(probs[i].init_pv, probs[i].init_meaning)
+        ext1 = torch.cuda.ExternalStream(ctx.stream())
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext1)
+        st, sdt, sn, sl, tl = ctx.time_integration(ENSEMBLE["steps"], ENSEMBLE["dt"])
+        e1.record(ext1)
+        e1.synchronize()
+        ms += e0.elapsed_time(e1)
+        cits += int(sn.sum()) * probs[i].num_cells
+        ctx.close()
+    one_fp64 = cits / (ms / 1000.0)
+    return {"systems": count, "cells_total": int(Ns.sum()), "value": mixed, "unit": UNIT,
+            "batched_plain_fp64": fp64, "one_at_a_time_plain_fp64": one_fp64,
+            "batched_mixed_over_plain_fp64": mixed / one_fp64, "batched_mixed_over_batched_plain_fp64": mixed / fp64,
+            "same_newton_iterations": newton == newton64,
+            "what": "two-phase realizations with 10k-200k cells, %d time steps x %g s, batched (device-driven "
+                    "Newton rounds, one graph launch each); the full 256-member line is bench.py --ensemble 256"
+                    % (ENSEMBLE["steps"], ENSEMBLE["dt"])}
+
+
 def run_ours(args):
     import torch
     rank, world, local = dist_env()
@@ -649,6 +712,7 @@ def run_ours(args):
             sec[name]["ctx"].close()
     if not args.headline_only:
         line["lens-48x32"] = lens_line(torch)
+        line["ensemble-64"] = ensemble_leg(64, torch)
     if world == 1 and not args.no_cpu_baseline:
         v, dt, threads = cpu_sample(prob, iters=1)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",

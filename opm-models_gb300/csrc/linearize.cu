@@ -6,15 +6,21 @@
 // be compared with the CPU restatement at the 1e-12 level.
 //
 // K2 mirrors the reference's element loop (fvbaselinearizer.hh:510-626 with
-// FvBaseAdLocalLinearizer, fvbaseadlocallinearizer.hh:173-292): one thread
-// per cell I evaluates its faces with derivatives with respect to x_I only,
-// writes the residual row I, the diagonal block (I,I) and the column blocks
-// (J,I) of its neighbours.  Each block has exactly one writer, so there are
-// no atomics and the summation order inside a row is the reference's:
+// FvBaseAdLocalLinearizer, fvbaseadlocallinearizer.hh:173-292): cell I's
+// faces are evaluated with derivatives with respect to x_I only, giving the
+// residual row I, the diagonal block (I,I) and the column blocks (J,I) of
+// its neighbours.  The single-system AD path runs it face-parallel: a group
+// of 2*dim lanes per cell, one lane per intersection, the cell's own dual
+// quantities staged in shared memory, the faces summed in intersection
+// order from warp shuffles.  The batched and finite-difference paths run
+// one thread per cell.  Each block has exactly one writer, so there are no
+// atomics and the summation order inside a row is the reference's:
 // interior faces in intersection order, storage, boundary faces.  The
 // expensive intensive quantities (pow-heavy material laws, PVT tables) are
 // computed once per cell by K1 and read back -- FP64 arithmetic is the scarce
 // resource on this GPU, bytes are cheap.
+#include <cstdlib>
+
 #include "../../include/gbfv.h"
 #include "gbfv_internal.cuh"
 
@@ -353,115 +359,154 @@ __device__ __forceinline__ Dual<B> tpfaPhase(const Dual<B>& pI, double pJ, const
 }
 
 // The local residual of element p (FvBaseLocalResidual::eval,
-// fvbaselocalresidual.hh:158-191) divided by its volume, with the element's
-// own intensive quantities from `iq` and its neighbours' from `nbr` (the same
-// buffers for AD; the deflected state of p for finite differences).  Each
-// interior face's flux (times the face area) goes to sink(dir, q, flux).
-template <class Sink>
-__device__ __forceinline__ void localImmiscible(const DevMesh& m, const IqBuffers& iq, const IqBuffers& nbr,
-                                                double* __restrict__ storageOld, int iter0, double dt, const int p,
-                                                D2 (&res)[2], Sink& sink)
+// fvbaselocalresidual.hh:158-191) divided by its volume, in three parts so
+// that a cell-parallel and a face-parallel kernel run the same operations:
+// the element's own intensive quantities as duals, one interior face's flux
+// (times the face area), and the terms after the faces (storage, boundary
+// faces, the division by the volume).
+struct OwnImmiscible {
+    D2 pI[2], rhoI[2], lamI[2];
+};
+
+__device__ __forceinline__ void ownImmiscible(const DevMesh& m, const IqBuffers& iq, const int p, OwnImmiscible& o)
 {
     const int ld = m.ldN;
-    D2 pI[2], rhoI[2], lamI[2];
     for (int a = 0; a < 2; ++a) {
-        pI[a] = ldDual<2>(iq, ld, a, a, p);
-        rhoI[a] = ldDual<2>(iq, ld, 2 + a, 2 + a, p);
-        lamI[a] = ldDual<2>(iq, ld, 4 + a, 4 + a, p);
+        o.pI[a] = ldDual<2>(iq, ld, a, a, p);
+        o.rhoI[a] = ldDual<2>(iq, ld, 2 + a, 2 + a, p);
+        o.lamI[a] = ldDual<2>(iq, ld, 4 + a, 4 + a, p);
     }
-    res[0] = D2(0.0);
-    res[1] = D2(0.0);
-    const int ndir = 2 * m.dim;
-    for (int dir = 0; dir < ndir; ++dir) {
-        const int q = m.nbr[dir * ld + p];
-        if (q < 0) continue;
-        const double dTot = m.dTot[dir * ld + p];
-        const double gIn = m.gIn[dir * ld + p];
-        const double gEx = m.gEx[dir * ld + p];
-        const double Kh = m.Kh[dir * ld + p];
-        const double area = m.area[dir * ld + p];
-        const double nrm = (dir & 1) ? 1.0 : -1.0;
-        D2 flux[2];
-        for (int a = 0; a < 2; ++a) {
-            const double pJ = nbr.val[a * ld + q];
-            const double rhoJ = nbr.val[(2 + a) * ld + q];
-            const double lamJ = nbr.val[(4 + a) * ld + q];
-            bool upI;
-            D2 vf = m.fluxModule == GBFV_FLUX_TRANS
-                        ? transPhase(pI[a], pJ, rhoI[a], rhoJ, lamI[a], lamJ, m.trans[dir * ld + p],
-                                     m.dzg[dir * ld + p], m.tieUpI[dir * ld + p] != 0, upI)
-                        : darcyPhase<2>(pI[a], pJ, rhoI[a], rhoJ, lamI[a], lamJ, dTot, gIn, gEx, Kh, nrm, upI);
-            flux[a] = D2(0.0) + (upI ? vf * rhoI[a] : vf * rhoJ);
-        }
-        double alpha = 1.0;
-        alpha *= area;
-        for (int e = 0; e < 2; ++e) flux[e] = flux[e] * alpha;
-        for (int e = 0; e < 2; ++e) res[e] = res[e] + flux[e];
-        sink(dir, q, flux);
+}
+
+// interior face `dir` of element p with the neighbour's values from `nbr`:
+// false when the cell has no neighbour there
+__device__ __forceinline__ bool faceImmiscible(const DevMesh& m, const OwnImmiscible& o, const IqBuffers& nbr,
+                                               const int p, const int dir, int& q, D2 (&flux)[2])
+{
+    const int ld = m.ldN;
+    q = m.nbr[dir * ld + p];
+    if (q < 0) return false;
+    const double dTot = m.dTot[dir * ld + p];
+    const double gIn = m.gIn[dir * ld + p];
+    const double gEx = m.gEx[dir * ld + p];
+    const double Kh = m.Kh[dir * ld + p];
+    const double area = m.area[dir * ld + p];
+    const double nrm = (dir & 1) ? 1.0 : -1.0;
+    for (int a = 0; a < 2; ++a) {
+        const double pJ = nbr.val[a * ld + q];
+        const double rhoJ = nbr.val[(2 + a) * ld + q];
+        const double lamJ = nbr.val[(4 + a) * ld + q];
+        bool upI;
+        D2 vf = m.fluxModule == GBFV_FLUX_TRANS
+                    ? transPhase(o.pI[a], pJ, o.rhoI[a], rhoJ, o.lamI[a], lamJ, m.trans[dir * ld + p],
+                                 m.dzg[dir * ld + p], m.tieUpI[dir * ld + p] != 0, upI)
+                    : darcyPhase<2>(o.pI[a], pJ, o.rhoI[a], rhoJ, o.lamI[a], lamJ, dTot, gIn, gEx, Kh, nrm, upI);
+        flux[a] = D2(0.0) + (upI ? vf * o.rhoI[a] : vf * rhoJ);
     }
+    double alpha = 1.0;
+    alpha *= area;
+    for (int e = 0; e < 2; ++e) flux[e] = flux[e] * alpha;
+    return true;
+}
+
+// the terms after the interior faces for equation e (storage, boundary
+// faces, / V); the equations do not mix, so a lane per equation gives the
+// same results as one thread for all
+__device__ __forceinline__ void tailImmiscibleEq(const DevMesh& m, const OwnImmiscible& o, const IqBuffers& iq,
+                                                 double* __restrict__ storageOld, int iter0, double dt, const int p,
+                                                 const int e, D2& r)
+{
+    const int ld = m.ldN;
     const double V = m.volume[p];
+    const double scvVolume = V * 1.0;
     {
-        const double scvVolume = V * 1.0;
-        for (int e = 0; e < 2; ++e) {
-            D2 tmp;
-            tmp.v = iq.sto[(e * 3 + 0) * ld + p];
-            tmp.d[0] = iq.sto[(e * 3 + 1) * ld + p];
-            tmp.d[1] = iq.sto[(e * 3 + 2) * ld + p];
-            double tmp2;
-            if (iter0) {
-                tmp2 = tmp.v;
-                storageOld[e * ld + p] = tmp2;
-            }
-            else
-                tmp2 = storageOld[e * ld + p];
-            tmp = tmp - tmp2;
-            tmp = tmp * (scvVolume / dt);
-            res[e] = res[e] + tmp;
+        D2 tmp;
+        tmp.v = iq.sto[(e * 3 + 0) * ld + p];
+        tmp.d[0] = iq.sto[(e * 3 + 1) * ld + p];
+        tmp.d[1] = iq.sto[(e * 3 + 2) * ld + p];
+        double tmp2;
+        if (iter0) {
+            tmp2 = tmp.v;
+            storageOld[e * ld + p] = tmp2;
         }
-        for (int e = 0; e < 2; ++e) res[e] = res[e] - 0.0 * scvVolume;
+        else
+            tmp2 = storageOld[e * ld + p];
+        tmp = tmp - tmp2;
+        tmp = tmp * (scvVolume / dt);
+        r = r + tmp;
     }
+    r = r - 0.0 * scvVolume;
+    const int a = e;  // equation e is phase e's conservation
     for (int f = m.bfPtr[p]; f < m.bfPtr[p + 1]; ++f) {
         const BFace bf = m.bfaces[f];
-        D2 values[2] = {D2(0.0), D2(0.0)};
+        D2 value(0.0);
         if (bf.type == GBFV_BC_MASSRATE) {
-            for (int e = 0; e < 2; ++e) values[e] = D2(bf.rate[e]);
+            value = D2(bf.rate[e]);
         }
         else if (bf.type == GBFV_BC_FREEFLOW && m.fluxModule == GBFV_FLUX_TRANS) {
             // calculateBoundaryGradients_ of the transmissibility module (transfluxmodule.hh:324-415)
-            for (int a = 0; a < 2; ++a) {
-                D2 rhoAvg = (rhoI[a] + bf.rhob[a]) / 2.0;
-                D2 pEx(bf.pb[a]);
-                pEx = pEx + rhoAvg * bf.dzgB;
-                D2 pd = pEx - pI[a];
-                D2 vf = pd.v > 0.0 ? (pd * bf.mobb[a]) * (-bf.transB) : (pd * lamI[a]) * (-bf.transB);
-                D2 dens = bf.pb[a] > pI[a].v ? D2(bf.rhob[a]) : rhoI[a];
-                values[a] = values[a] + vf * dens;
-            }
+            D2 rhoAvg = (o.rhoI[a] + bf.rhob[a]) / 2.0;
+            D2 pEx(bf.pb[a]);
+            pEx = pEx + rhoAvg * bf.dzgB;
+            D2 pd = pEx - o.pI[a];
+            D2 vf = pd.v > 0.0 ? (pd * bf.mobb[a]) * (-bf.transB) : (pd * o.lamI[a]) * (-bf.transB);
+            D2 dens = bf.pb[a] > o.pI[a].v ? D2(bf.rhob[a]) : o.rhoI[a];
+            value = value + vf * dens;
         }
         else if (bf.type == GBFV_BC_FREEFLOW) {
             const double distSq = bf.tmpA * bf.tmpA;
             const double absDist2 = bf.dInA * bf.dInA;
             const double K = m.perm[bf.axis * ld + p];
-            for (int a = 0; a < 2; ++a) {
-                D2 deltay = bf.pb[a] - pI[a];
-                D2 pg = deltay * (bf.tmpA / distSq);
-                D2 pStatIn = (-bf.gTimesDist) * rhoI[a];
-                D2 fsc = pStatIn / absDist2;
-                pg = pg + bf.dInA * fsc;
-                const double t = pg.v * bf.nrm;
-                D2 mob = t > 0.0 ? D2(bf.mobb[a]) : lamI[a];
-                D2 fv = K * pg;
-                fv = fv * (-mob);
-                D2 vf = fv * bf.nrm;
-                D2 dens = bf.pb[a] > pI[a].v ? D2(bf.rhob[a]) : rhoI[a];
-                values[a] = values[a] + vf * dens;
-            }
+            D2 deltay = bf.pb[a] - o.pI[a];
+            D2 pg = deltay * (bf.tmpA / distSq);
+            D2 pStatIn = (-bf.gTimesDist) * o.rhoI[a];
+            D2 fsc = pStatIn / absDist2;
+            pg = pg + bf.dInA * fsc;
+            const double t = pg.v * bf.nrm;
+            D2 mob = t > 0.0 ? D2(bf.mobb[a]) : o.lamI[a];
+            D2 fv = K * pg;
+            fv = fv * (-mob);
+            D2 vf = fv * bf.nrm;
+            D2 dens = bf.pb[a] > o.pI[a].v ? D2(bf.rhob[a]) : o.rhoI[a];
+            value = value + vf * dens;
         }
         const double aa = bf.area * 1.0;
-        for (int e = 0; e < 2; ++e) values[e] = values[e] * aa;
-        for (int e = 0; e < 2; ++e) res[e] = res[e] + values[e];
+        value = value * aa;
+        r = r + value;
     }
-    for (int e = 0; e < 2; ++e) res[e] = res[e] / V;
+    r = r / V;
+}
+
+__device__ __forceinline__ void tailImmiscible(const DevMesh& m, const OwnImmiscible& o, const IqBuffers& iq,
+                                               double* __restrict__ storageOld, int iter0, double dt, const int p,
+                                               D2 (&res)[2])
+{
+    for (int e = 0; e < 2; ++e) tailImmiscibleEq(m, o, iq, storageOld, iter0, dt, p, e, res[e]);
+}
+
+// the whole local residual of element p, its faces in intersection order;
+// each interior face's flux (times the face area) also goes to
+// sink(dir, q, flux).  `iq`: the element's own intensive quantities, `nbr`:
+// its neighbours' (the same buffers for AD; the deflected state of p for
+// finite differences)
+template <class Sink>
+__device__ __forceinline__ void localImmiscible(const DevMesh& m, const IqBuffers& iq, const IqBuffers& nbr,
+                                                double* __restrict__ storageOld, int iter0, double dt, const int p,
+                                                D2 (&res)[2], Sink& sink)
+{
+    OwnImmiscible o;
+    ownImmiscible(m, iq, p, o);
+    res[0] = D2(0.0);
+    res[1] = D2(0.0);
+    const int ndir = 2 * m.dim;
+    for (int dir = 0; dir < ndir; ++dir) {
+        int q;
+        D2 flux[2];
+        if (!faceImmiscible(m, o, nbr, p, dir, q, flux)) continue;
+        for (int e = 0; e < 2; ++e) res[e] = res[e] + flux[e];
+        sink(dir, q, flux);
+    }
+    tailImmiscible(m, o, iq, storageOld, iter0, dt, p, res);
 }
 
 // AD: a face's flux derivatives are the off-diagonal block (q, p)
@@ -491,6 +536,18 @@ __device__ __forceinline__ void writeDiag(const DevMesh& m, const Dual<B> (&res)
     }
 }
 
+// row e of it
+template <int B>
+__device__ __forceinline__ void writeDiagRow(const DevMesh& m, const Dual<B>& r, const int e,
+                                             double* __restrict__ residual, double* __restrict__ jval, const int p)
+{
+    const int ld = m.ldN;
+    const bool cons = m.cflag[p] >= 0;
+    const int ds = m.dim;
+    residual[B * p + e] = cons ? 0.0 : r.v;
+    for (int v = 0; v < B; ++v) jval[(ds * B * B + e * B + v) * ld + p] = cons ? (e == v ? 1.0 : 0.0) : r.d[v];
+}
+
 __device__ __forceinline__ void kAssembleImmiscibleBody(const DevMesh& m, const DevPhysics* __restrict__ phys,
                                                            IqBuffers iq, double* __restrict__ storageOld,
                                                            int iter0, double dt,
@@ -516,90 +573,122 @@ __global__ void __launch_bounds__(128) kAssembleImmiscible(DevMesh m, const DevP
     kAssembleImmiscibleBody(m, phys, iq, storageOld, iter0, dt, residual, jval, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
+// The black-oil local residual in the same three parts: the element's own
+// quantities (p as a seeded variable, the rest from K1), one interior
+// face's flux, the terms after the faces.
+struct OwnBlackoil {
+    D3 pI, rhoI[3], lamI[3], invBI[3], RsI;
+};
+
+__device__ __forceinline__ void ownBlackoil(const DevMesh& m, const IqBuffers& iq, const int p, OwnBlackoil& o)
+{
+    const int ld = m.ldN;
+    o.pI = D3::var(iq.val[0 * ld + p], 1);
+    for (int a = 0; a < 3; ++a) {
+        o.rhoI[a] = ldDual<3>(iq, ld, 1 + a, a, p);
+        o.lamI[a] = ldDual<3>(iq, ld, 4 + a, 3 + a, p);
+        o.invBI[a] = ldDual<3>(iq, ld, 7 + a, 6 + a, p);
+    }
+    o.RsI = ldDual<3>(iq, ld, 10, 9, p);
+}
+
+__device__ __forceinline__ bool faceBlackoil(const DevMesh& m, const DevPhysics* __restrict__ phys,
+                                             const OwnBlackoil& o, const IqBuffers& nbr, const int p, const int dir,
+                                             int& q, D3 (&flux)[3])
+{
+    const int ld = m.ldN;
+    q = m.nbr[dir * ld + p];
+    if (q < 0) return false;
+    const BlackOilPvt& T = phys->pvt;
+    const double rhoRef[3] = {T.rhoRefW, T.rhoRefO, T.rhoRefG};
+    const int comp[3] = {1, 0, 2};
+    const double dTot = m.dTot[dir * ld + p];
+    const double gIn = m.gIn[dir * ld + p];
+    const double gEx = m.gEx[dir * ld + p];
+    const double Kh = m.Kh[dir * ld + p];
+    const double area = m.area[dir * ld + p];
+    const double nrm = (dir & 1) ? 1.0 : -1.0;
+    const double pJ = nbr.val[0 * ld + q];
+    for (int e = 0; e < 3; ++e) flux[e] = D3(0.0);
+    for (int a = 0; a < 3; ++a) {
+        const double rhoJ = nbr.val[(1 + a) * ld + q];
+        const double lamJ = nbr.val[(4 + a) * ld + q];
+        bool upI;
+        const size_t oo = (size_t)dir * ld + p;
+        D3 vf = m.tpfa ? tpfaPhase<3>(o.pI, pJ, o.rhoI[a], rhoJ, o.lamI[a], lamJ, m.trans[oo], area, m.dzg[oo],
+                                      m.tieUpI[oo] != 0, upI)
+                       : darcyPhase<3>(o.pI, pJ, o.rhoI[a], rhoJ, o.lamI[a], lamJ, dTot, gIn, gEx, Kh, nrm, upI);
+        D3 invB = upI ? o.invBI[a] : D3(nbr.val[(7 + a) * ld + q]);
+        D3 svf = invB * vf;
+        flux[comp[a]] = flux[comp[a]] + svf * rhoRef[a];
+        if (a == 1) {
+            D3 Rs = upI ? o.RsI : D3(nbr.val[10 * ld + q]);
+            flux[2] = flux[2] + Rs * svf * T.rhoRefG;
+        }
+    }
+    double alpha = 1.0;
+    alpha *= area;
+    for (int e = 0; e < 3; ++e) flux[e] = flux[e] * alpha;
+    return true;
+}
+
+__device__ __forceinline__ void tailBlackoilEq(const DevMesh& m, const IqBuffers& iq, double* __restrict__ storageOld,
+                                               int iter0, double dt, const int p, const int e, D3& r)
+{
+    const int ld = m.ldN;
+    const double V = m.volume[p];
+    const double scvVolume = V * 1.0;
+    {
+        D3 tmp;
+        tmp.v = iq.sto[(e * 4 + 0) * ld + p];
+        for (int j = 0; j < 3; ++j) tmp.d[j] = iq.sto[(e * 4 + 1 + j) * ld + p];
+        double tmp2;
+        if (iter0) {
+            tmp2 = tmp.v;
+            storageOld[e * ld + p] = tmp2;
+        }
+        else
+            tmp2 = storageOld[e * ld + p];
+        tmp = tmp - tmp2;
+        tmp = tmp * (scvVolume / dt);
+        r = r + tmp;
+    }
+    r = r - 0.0 * scvVolume;
+    for (int f = m.bfPtr[p]; f < m.bfPtr[p + 1]; ++f) {
+        const BFace& bf = m.bfaces[f];
+        if (bf.type != GBFV_BC_MASSRATE) continue;
+        const double aa = bf.area * 1.0;
+        r = r + D3(bf.rate[e]) * aa;
+    }
+    // FvBaseLinearizer divides each row by its volume; TpfaLinearizer
+    // (tpfalinearizer.hh:711-866) keeps the fluxes times the face area and
+    // the storage times volume / dt as they are
+    if (!m.tpfa) r = r / V;
+}
+
+__device__ __forceinline__ void tailBlackoil(const DevMesh& m, const IqBuffers& iq, double* __restrict__ storageOld,
+                                             int iter0, double dt, const int p, D3 (&res)[3])
+{
+    for (int e = 0; e < 3; ++e) tailBlackoilEq(m, iq, storageOld, iter0, dt, p, e, res[e]);
+}
+
 template <class Sink>
 __device__ __forceinline__ void localBlackoil(const DevMesh& m, const DevPhysics* __restrict__ phys,
                                               const IqBuffers& iq, const IqBuffers& nbr,
                                               double* __restrict__ storageOld, int iter0, double dt, const int p,
                                               D3 (&res)[3], Sink& sink)
 {
-    const int ld = m.ldN;
-    const BlackOilPvt& T = phys->pvt;
-    // own quantities: p as a seeded variable, the rest from K1
-    D3 pI = D3::var(iq.val[0 * ld + p], 1);
-    D3 rhoI[3], lamI[3], invBI[3], RsI;
-    for (int a = 0; a < 3; ++a) {
-        rhoI[a] = ldDual<3>(iq, ld, 1 + a, a, p);
-        lamI[a] = ldDual<3>(iq, ld, 4 + a, 3 + a, p);
-        invBI[a] = ldDual<3>(iq, ld, 7 + a, 6 + a, p);
-    }
-    RsI = ldDual<3>(iq, ld, 10, 9, p);
-    const double rhoRef[3] = {T.rhoRefW, T.rhoRefO, T.rhoRefG};
-    const int comp[3] = {1, 0, 2};
+    OwnBlackoil o;
+    ownBlackoil(m, iq, p, o);
     for (int e = 0; e < 3; ++e) res[e] = D3(0.0);
     for (int dir = 0; dir < 6; ++dir) {
-        const int q = m.nbr[dir * ld + p];
-        if (q < 0) continue;
-        const double dTot = m.dTot[dir * ld + p];
-        const double gIn = m.gIn[dir * ld + p];
-        const double gEx = m.gEx[dir * ld + p];
-        const double Kh = m.Kh[dir * ld + p];
-        const double area = m.area[dir * ld + p];
-        const double nrm = (dir & 1) ? 1.0 : -1.0;
-        const double pJ = nbr.val[0 * ld + q];
-        D3 flux[3] = {D3(0.0), D3(0.0), D3(0.0)};
-        for (int a = 0; a < 3; ++a) {
-            const double rhoJ = nbr.val[(1 + a) * ld + q];
-            const double lamJ = nbr.val[(4 + a) * ld + q];
-            bool upI;
-            const size_t o = (size_t)dir * ld + p;
-            D3 vf = m.tpfa ? tpfaPhase<3>(pI, pJ, rhoI[a], rhoJ, lamI[a], lamJ, m.trans[o], area, m.dzg[o],
-                                          m.tieUpI[o] != 0, upI)
-                           : darcyPhase<3>(pI, pJ, rhoI[a], rhoJ, lamI[a], lamJ, dTot, gIn, gEx, Kh, nrm, upI);
-            D3 invB = upI ? invBI[a] : D3(nbr.val[(7 + a) * ld + q]);
-            D3 svf = invB * vf;
-            flux[comp[a]] = flux[comp[a]] + svf * rhoRef[a];
-            if (a == 1) {
-                D3 Rs = upI ? RsI : D3(nbr.val[10 * ld + q]);
-                flux[2] = flux[2] + Rs * svf * T.rhoRefG;
-            }
-        }
-        double alpha = 1.0;
-        alpha *= area;
-        for (int e = 0; e < 3; ++e) flux[e] = flux[e] * alpha;
+        int q;
+        D3 flux[3];
+        if (!faceBlackoil(m, phys, o, nbr, p, dir, q, flux)) continue;
         for (int e = 0; e < 3; ++e) res[e] = res[e] + flux[e];
         sink(dir, q, flux);
     }
-    const double V = m.volume[p];
-    {
-        const double scvVolume = V * 1.0;
-        for (int e = 0; e < 3; ++e) {
-            D3 tmp;
-            tmp.v = iq.sto[(e * 4 + 0) * ld + p];
-            for (int j = 0; j < 3; ++j) tmp.d[j] = iq.sto[(e * 4 + 1 + j) * ld + p];
-            double tmp2;
-            if (iter0) {
-                tmp2 = tmp.v;
-                storageOld[e * ld + p] = tmp2;
-            }
-            else
-                tmp2 = storageOld[e * ld + p];
-            tmp = tmp - tmp2;
-            tmp = tmp * (scvVolume / dt);
-            res[e] = res[e] + tmp;
-        }
-        for (int e = 0; e < 3; ++e) res[e] = res[e] - 0.0 * scvVolume;
-    }
-    for (int f = m.bfPtr[p]; f < m.bfPtr[p + 1]; ++f) {
-        const BFace& bf = m.bfaces[f];
-        if (bf.type != GBFV_BC_MASSRATE) continue;
-        const double aa = bf.area * 1.0;
-        for (int e = 0; e < 3; ++e) res[e] = res[e] + D3(bf.rate[e]) * aa;
-    }
-    // FvBaseLinearizer divides each row by its volume; TpfaLinearizer
-    // (tpfalinearizer.hh:711-866) keeps the fluxes times the face area and
-    // the storage times volume / dt as they are
-    if (!m.tpfa)
-        for (int e = 0; e < 3; ++e) res[e] = res[e] / V;
+    tailBlackoil(m, iq, storageOld, iter0, dt, p, res);
 }
 
 __device__ __forceinline__ void kAssembleBlackoilBody(const DevMesh& m, const DevPhysics* __restrict__ phys,
@@ -626,14 +715,209 @@ __global__ void __launch_bounds__(128) kAssembleBlackoil(DevMesh m, const DevPhy
     kAssembleBlackoilBody(m, phys, iq, storageOld, iter0, dt, residual, jval, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
+// ------------------------------------------- K2, face-parallel form -----
+// The same element linearization with the faces in parallel: a group of G
+// lanes of one warp per cell (G = 2*dim: one lane per intersection), the
+// cell's own dual quantities staged once in shared memory for its group,
+// each lane evaluating its face's flux and writing its off-diagonal block
+// (row q, column p: one writer per block), then every lane of the group
+// summing the G fluxes in intersection order from the group's shuffles and
+// lane e adding equation e's storage and boundary terms -- the operations
+// and their order of the cell-parallel kernel, so the results are the same
+// to the bit.
+template <int B>
+__device__ __forceinline__ Dual<B> shflDualFrom(const Dual<B>& x, int src)
+{
+    Dual<B> r;
+    r.v = __shfl_sync(0xffffffffu, x.v, src);
+#pragma unroll
+    for (int j = 0; j < B; ++j) r.d[j] = __shfl_sync(0xffffffffu, x.d[j], src);
+    return r;
+}
+
+constexpr int FACE_THREADS = 256;
+// the staged states are plain arrays of doubles in dual order
+static_assert(sizeof(OwnImmiscible) == 6 * 3 * sizeof(double), "OwnImmiscible layout");
+static_assert(sizeof(OwnBlackoil) == 11 * 4 * sizeof(double), "OwnBlackoil layout");
+
+template <int G>
+__global__ void __launch_bounds__(FACE_THREADS) kAssembleImmiscibleFaces(DevMesh m, IqBuffers iq,
+                                                                         double* __restrict__ storageOld, int iter0,
+                                                                         double dt, double* __restrict__ residual,
+                                                                         double* __restrict__ jval)
+{
+    constexpr int GPW = 32 / G, CELLS = (FACE_THREADS / 32) * GPW;
+    __shared__ __align__(16) unsigned char ownRaw[CELLS * sizeof(OwnImmiscible)];
+    OwnImmiscible* own = reinterpret_cast<OwnImmiscible*>(ownRaw);
+    const int lane = threadIdx.x & 31, grp = lane / G, g = lane - grp * G;
+    const int c = (threadIdx.x >> 5) * GPW + grp;
+    const int p = blockIdx.x * CELLS + c;
+    const bool active = grp < GPW && p < m.N;
+    if (active) {
+        // the group stages the cell's 6 duals (ownImmiscible's loads, spread
+        // over the lanes): dual k is value plane k with derivative plane k
+        double* ow = reinterpret_cast<double*>(&own[c]);
+        const int ld = m.ldN;
+        for (int i = g; i < 6 * 3; i += G) {
+            const int k = i / 3, comp = i - k * 3;
+            ow[i] = comp == 0 ? iq.val[k * ld + p] : iq.der[(k * 2 + comp - 1) * ld + p];
+        }
+    }
+    __syncthreads();
+    D2 flux[2] = {D2(0.0), D2(0.0)};
+    bool has = false;
+    if (active && g < 2 * m.dim) {
+        int q;
+        has = faceImmiscible(m, own[c], iq, p, g, q, flux);
+        if (has) {
+            OffBlockSink<2> sink{m, jval};
+            sink(g, q, flux);
+        }
+    }
+    D2 res[2] = {D2(0.0), D2(0.0)};
+    const int base = grp < GPW ? lane - g : lane;
+    for (int d = 0; d < G; ++d) {
+        const int src = grp < GPW ? base + d : lane;
+        const bool hd = __shfl_sync(0xffffffffu, has, src);
+        D2 fd[2];
+        for (int e = 0; e < 2; ++e) fd[e] = shflDualFrom<2>(flux[e], src);
+        if (hd)
+            for (int e = 0; e < 2; ++e) res[e] = res[e] + fd[e];
+    }
+    // lane e of the group finishes equation e
+    if (active && g < 2) {
+        D2 r = g == 0 ? res[0] : res[1];
+        tailImmiscibleEq(m, own[c], iq, storageOld, iter0, dt, p, g, r);
+        writeDiagRow<2>(m, r, g, residual, jval, p);
+    }
+}
+
+// Black-oil: the group's fluxes go through shared memory, and the 12
+// components of the cell's three residual duals (value and 3 derivatives
+// each) are summed and finished two per lane -- dual sums, dual minus or
+// plus a scalar and dual divided by a scalar act component by component,
+// so each component sees the cell-parallel kernel's operations in its order
+__device__ __forceinline__ void tailBlackoilComponent(const DevMesh& m, const IqBuffers& iq,
+                                                      double* __restrict__ storageOld, int iter0, double dt,
+                                                      const int p, const int e, const int comp, double r,
+                                                      double* __restrict__ residual, double* __restrict__ jval)
+{
+    const int ld = m.ldN;
+    const double V = m.volume[p];
+    const double scvVolume = V * 1.0;
+    // storage: (S - S_old) * (V / dt); S_old only moves the value
+    double t = iq.sto[(e * 4 + comp) * ld + p];
+    if (comp == 0) {
+        double tmp2;
+        if (iter0) {
+            tmp2 = t;
+            storageOld[e * ld + p] = tmp2;
+        }
+        else
+            tmp2 = storageOld[e * ld + p];
+        t = t - tmp2;
+    }
+    t = t * (scvVolume / dt);
+    r = r + t;
+    if (comp == 0) r = r - 0.0 * scvVolume;
+    for (int f = m.bfPtr[p]; f < m.bfPtr[p + 1]; ++f) {
+        const BFace& bf = m.bfaces[f];
+        if (bf.type != GBFV_BC_MASSRATE) continue;
+        const double aa = bf.area * 1.0;
+        r = r + (comp == 0 ? bf.rate[e] : 0.0) * aa;
+    }
+    if (!m.tpfa) r = comp == 0 ? r / V : r * (1.0 / V);
+    const bool cons = m.cflag[p] >= 0;
+    if (comp == 0) residual[3 * p + e] = cons ? 0.0 : r;
+    else {
+        const int v = comp - 1;
+        jval[(m.dim * 9 + e * 3 + v) * ld + p] = cons ? (e == v ? 1.0 : 0.0) : r;
+    }
+}
+
+__global__ void __launch_bounds__(FACE_THREADS) kAssembleBlackoilFaces(DevMesh m, const DevPhysics* __restrict__ phys,
+                                                                       IqBuffers iq, double* __restrict__ storageOld,
+                                                                       int iter0, double dt,
+                                                                       double* __restrict__ residual,
+                                                                       double* __restrict__ jval)
+{
+    constexpr int G = 6, GPW = 32 / G, CELLS = (FACE_THREADS / 32) * GPW;
+    __shared__ __align__(16) unsigned char ownRaw[CELLS * sizeof(OwnBlackoil)];
+    __shared__ double fsm[CELLS][G][12];
+    __shared__ int hsm[CELLS][G];
+    OwnBlackoil* own = reinterpret_cast<OwnBlackoil*>(ownRaw);
+    const int lane = threadIdx.x & 31, grp = lane / G, g = lane - grp * G;
+    const int c = (threadIdx.x >> 5) * GPW + grp;
+    const int p = blockIdx.x * CELLS + c;
+    const bool active = grp < GPW && p < m.N;
+    if (active) {
+        // the group stages the cell's 11 duals (ownBlackoil's loads, spread
+        // over the lanes): dual 0 the pressure seeded as variable 1, dual
+        // k >= 1 value plane k with derivative plane k - 1
+        double* ow = reinterpret_cast<double*>(&own[c]);
+        const int ld = m.ldN;
+        for (int i = g; i < 11 * 4; i += G) {
+            const int k = i / 4, comp = i - k * 4;
+            double v;
+            if (k == 0) v = comp == 0 ? iq.val[p] : (comp == 2 ? 1.0 : 0.0);
+            else v = comp == 0 ? iq.val[k * ld + p] : iq.der[((k - 1) * 3 + comp - 1) * ld + p];
+            ow[i] = v;
+        }
+    }
+    __syncthreads();
+    if (active) {
+        int q;
+        D3 flux[3];
+        const bool has = faceBlackoil(m, phys, own[c], iq, p, g, q, flux);
+        hsm[c][g] = has ? 1 : 0;
+        if (has) {
+            OffBlockSink<3> sink{m, jval};
+            sink(g, q, flux);
+            for (int e = 0; e < 3; ++e) {
+                fsm[c][g][e * 4] = flux[e].v;
+                for (int j = 0; j < 3; ++j) fsm[c][g][e * 4 + 1 + j] = flux[e].d[j];
+            }
+        }
+    }
+    __syncwarp();
+    if (!active) return;
+    // lane g: components g and g + 6 (equation k / 4, component k % 4)
+    for (int k = g; k < 12; k += G) {
+        double r = 0.0;
+        for (int d = 0; d < G; ++d)
+            if (hsm[c][d]) r = r + fsm[c][d][k];
+        tailBlackoilComponent(m, iq, storageOld, iter0, dt, p, k / 4, k % 4, r, residual, jval);
+    }
+}
+
+// The AD element linearization of one system: the face-parallel kernels
+// (GBFV_CELL_ASSEMBLY=1 selects the cell-parallel ones, the same results)
 void launchAssemble(const DevMesh& m, const DevPhysics* phys, IqBuffers iq, double* storageOld,
                     int iter0, double dt, double* residual, double* jval, cudaStream_t s)
 {
-    const int bs = 128, nb = (m.N + bs - 1) / bs;
-    if (m.model == GBFV_MODEL_IMMISCIBLE_2P)
-        kAssembleImmiscible<<<nb, bs, 0, s>>>(m, phys, iq, storageOld, iter0, dt, residual, jval);
-    else
-        kAssembleBlackoil<<<nb, bs, 0, s>>>(m, phys, iq, storageOld, iter0, dt, residual, jval);
+    static const bool cellPath = getenv("GBFV_CELL_ASSEMBLY") != nullptr;
+    if (cellPath) {
+        const int bs = 128, nb = (m.N + bs - 1) / bs;
+        if (m.model == GBFV_MODEL_IMMISCIBLE_2P)
+            kAssembleImmiscible<<<nb, bs, 0, s>>>(m, phys, iq, storageOld, iter0, dt, residual, jval);
+        else
+            kAssembleBlackoil<<<nb, bs, 0, s>>>(m, phys, iq, storageOld, iter0, dt, residual, jval);
+    }
+    else if (m.model == GBFV_MODEL_IMMISCIBLE_2P && m.dim == 2) {
+        constexpr int cells = (FACE_THREADS / 32) * (32 / 4);
+        kAssembleImmiscibleFaces<4><<<(m.N + cells - 1) / cells, FACE_THREADS, 0, s>>>(m, iq, storageOld, iter0, dt,
+                                                                                   residual, jval);
+    }
+    else if (m.model == GBFV_MODEL_IMMISCIBLE_2P) {
+        constexpr int cells = (FACE_THREADS / 32) * (32 / 6);
+        kAssembleImmiscibleFaces<6><<<(m.N + cells - 1) / cells, FACE_THREADS, 0, s>>>(m, iq, storageOld, iter0, dt,
+                                                                                   residual, jval);
+    }
+    else {
+        constexpr int cells = (FACE_THREADS / 32) * (32 / 6);
+        kAssembleBlackoilFaces<<<(m.N + cells - 1) / cells, FACE_THREADS, 0, s>>>(m, phys, iq, storageOld, iter0,
+                                                                                 dt, residual, jval);
+    }
     countLaunch();
 }
 

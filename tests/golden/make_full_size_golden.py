@@ -17,6 +17,9 @@ Cases (the file each writes):
               tolerance 1e-12, Newton tolerance 1e-10
   c3          blackoil_100x100x100_newton_log.npz  -- 100x100x100 black-oil
               (1M cells), first two one-day steps, bench tolerances
+  c2_amg      blackoil_100x100x20_amg_log.npz      -- 100x100x20, first two
+              steps through the AMG backend (linear_solver AMG, coarsening
+              target 5000), bench tolerances
   c4member    ensemble_member_largest_log.npz      -- the largest member of
               the 256-realization two-phase ensemble (seeded as the
               benchmark builds it), two steps of 250 s, bench tolerances
@@ -72,6 +75,9 @@ def case(name):
                 997, "blackoil_100x100x20_tight12_log.npz", 0)
     if name == "c3":
         return problems.blackoil(100, 100, 100), bench, 2, 86400.0, 4999, "blackoil_100x100x100_newton_log.npz", 0
+    if name == "c2_amg":
+        return (problems.blackoil(100, 100, 20), dict(bench, linear_solver=capi.LINSOLVER_AMG), 2, 86400.0, 997,
+                "blackoil_100x100x20_amg_log.npz", 0)
     if name == "c4member":
         prob, _ = largest_ensemble_member()
         return prob, bench, 2, 250.0, 997, "ensemble_member_largest_log.npz", 0

@@ -16,9 +16,10 @@ state is also converged by the oracle's own residual.
 Tighter solves shrink the gap: linear 1e-10 / Newton 1e-8 (two steps) to
 STATE_RTOL_TIGHT, linear 1e-12 / Newton 1e-10 to STATE_RTOL_TIGHT12 -- the
 1e-8 state bar.
-100x100x100 (1M cells, two steps) and the largest member of the 256-member
-ensemble (two steps of 250 s, solved inside a batch) are held to the same
-rules."""
+100x100x100 (1M cells, two steps), the largest member of the 256-member
+ensemble (two steps of 250 s, solved inside a batch) and the 100x100x20
+workload through the AMG backend (two steps, against the oracle's AMG
+restatement) are held to the same rules."""
 import os
 
 import numpy as np
@@ -123,6 +124,26 @@ def test_blackoil_100x100x100_against_the_oracle_log(built, precision):
     if precision == capi.PREC_FP64:
         assert abs(int(lits.sum()) - int(g["linear"].sum())) <= LINEAR_TOTAL_RTOL * g["linear"].sum() + 10, \
             (lits, g["linear"])
+
+
+@pytest.mark.parametrize("precision", [capi.PREC_FP64, capi.PREC_MIXED])
+def test_blackoil_100x100x20_amg_against_the_oracle_log(built, precision):
+    """The benchmark workload's first two steps through the AMG backend
+    (the oracle's restatement, blackoil_100x100x20_amg_log.npz): the same
+    Newton counts and meanings, the state within the summation-order
+    envelope, the FP64 linear iterations within a few of the oracle's."""
+    g = _gold("blackoil_100x100x20_amg_log.npz")
+    prob = problems.blackoil(100, 100, 20)
+    prm = _bench_params(precision)
+    prm.linear_solver = capi.LINSOLVER_AMG
+    ctx = Context(prob, prm)
+    st, dts, nits, lits, _ = ctx.time_integration(len(g["newton"]), 86400.0, fixed_dt=True)
+    x, m = ctx.solution()
+    ctx.close()
+    assert st == 0
+    _check_against(g, nits, dts, x, m, 2 * _envelope())
+    if precision == capi.PREC_FP64:
+        assert abs(int(lits.sum()) - int(g["linear"].sum())) <= 0.05 * g["linear"].sum() + 2, (lits, g["linear"])
 
 
 def test_largest_ensemble_member_in_a_batch_against_the_oracle_log(built):
