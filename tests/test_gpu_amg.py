@@ -132,3 +132,37 @@ def test_blackoil_amg_needs_fewer_krylov_iterations(built):
         xs.append(dx)
     assert its[1] * 2 < its[0], its
     assert np.max(np.abs(xs[1] - xs[0])) <= 1e-3 * np.max(np.abs(xs[0]))
+
+
+def test_single_level_hierarchy_matches_the_oracle(built):
+    """A coarsening target at or above the row count leaves one level: the
+    V-cycle is the coarsest level's sweeps alone, still equal to the
+    oracle's to the last bit, and the solve still converges."""
+    rp, col, blk, r = _system(problems.blackoil(8, 6, 3), 86400.0)
+    n = len(rp) - 1
+    L, sizes, *_ , vo = O.amg(rp, col, blk, n, r)
+    assert L == 1
+    ls = _solver(rp, col, blk, n)
+    gs, gc = ls.amg_levels()
+    assert list(gs) == [n]
+    vg = ls.amg_apply(r)
+    assert np.max(np.abs(vg - vo)) <= 1e-15 * np.max(np.abs(vo))
+    sg, xg, itg = ls.solve(r)
+    assert sg == 0 and itg > 0
+
+
+def test_singular_diagonal_block_is_reported(built):
+    """A zero diagonal block on some level makes the AMG set-up report
+    GBFV_ERR_SINGULAR (the oracle's restatement refuses the same matrix),
+    not a silent NaN."""
+    rp, col, blk, r = _system(problems.blackoil(6, 5, 3), 86400.0)
+    blk = blk.copy()
+    n = len(rp) - 1
+    for k in range(rp[0], rp[1]):
+        if col[k] == 0:
+            blk[k][:] = 0.0
+    L, *_ = O.amg(rp, col, blk, 200)
+    assert L < 0 and -L == capi.ERR_SINGULAR
+    ls = _solver(rp, col, blk, 200)
+    sg, _, _ = ls.solve(r)
+    assert sg == capi.ERR_SINGULAR
