@@ -160,6 +160,29 @@ typedef struct gbfv_problem {
     const gbfv_blackoil_pvt* pvt; /* black-oil only, else NULL               */
     double temperature;
     int32_t flux_module;      /* enum gbfv_flux: Properties::FluxModule      */
+    /* Vertex-centred finite volumes (VcfvDiscretization with the stencil of
+     * vcfvstencil.hh:466-1390): num_elements > 0 selects it; 2D
+     * axis-aligned quadrilaterals, the immiscible model.  The cells above
+     * are then the grid's vertices, its degrees of freedom: centre = the
+     * vertex position, porosity / perm / material at the vertex, volume not
+     * read (the library sums each vertex's sub-control volumes), num_conn 0,
+     * no constraints.  Each element lists its corner vertices in the
+     * reference element's order: corner c at lower + (c&1, (c>>1)&1) .*
+     * (upper - lower).  The boundary arrays then hold the boundary
+     * sub-control-volume faces grouped per element (bface_ptr has
+     * num_elements + 1 entries): per boundary intersection of the element
+     * in intersection order, one face per corner of the intersection, with
+     * that corner (bface_corner), the face's integration point
+     * (bface_center: half way from the corner to the intersection's
+     * centre), the intersection's unit outer normal, half its area, and the
+     * condition the problem's boundary() gives at the integration point.   */
+    int32_t num_elements;
+    const int32_t* elem_corner;  /* [num_elements*4] vertex of each corner  */
+    const int32_t* bface_corner; /* [num_bfaces] corner of each boundary face */
+    int32_t p1_gradients;        /* UseP1FiniteElementGradients: 1 = gradients
+                                    of the P1 (Q1) finite-element interpolant
+                                    at the sub-control-volume faces (the lens
+                                    VCFV tests), 0 = two-point gradients     */
 } gbfv_problem;
 
 /* run-time parameters; names and defaults follow the reference's
@@ -362,6 +385,14 @@ int gbfv_linsolver_amg_levels(gbfv_linsolver* s, int32_t* sizes,
 /* the same for a context: 0 levels before its first AMG solve            */
 int gbfv_amg_levels(gbfv_ctx* ctx, int32_t* sizes, int32_t* colors);
 int gbfv_linsolver_amg_apply(gbfv_linsolver* s, const double* d, double* v);
+/* Patterns beyond the 5/7-point stencil's -- more than 7 distinct column
+ * offsets (at most 27, symmetric), or an ILU(0) whose lower entries update
+ * more than the diagonal, like the vertex-centred 9-point Jacobian -- are
+ * solved with the general block ILU(0) (natural-order blockILU0Decomposition,
+ * level-scheduled).  Diagnostic: one FP64 application v = (LU)^-1 d of it
+ * after factoring the matrix last set (natural order, n*b values);
+ * GBFV_ERR_UNSUPPORTED for a structured pattern.                          */
+int gbfv_linsolver_ilu0_apply(gbfv_linsolver* s, const double* d, double* v);
 
 /* ------------------------------------------------------------------ */
 /* diagnostics                                                          */

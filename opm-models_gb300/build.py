@@ -29,6 +29,8 @@ UNITS = {
     "restart.cu": [],
     "vtk.cu": [],
     "problem.cu": [],
+    "vcfv.cu": ["-fmad=false"],
+    "gilu.cu": ["-fmad=false"],
 }
 
 

@@ -25,6 +25,8 @@
 #include "../../include/gbfv.h"
 #include "gbfv_internal.cuh"
 #include "amg.cuh"
+#include "gilu.cuh"
+#include "vcfv.cuh"
 #include "solver.cuh"
 
 namespace gbfv {
@@ -142,6 +144,8 @@ struct SolverData {
     // first AMG solve; natural row of every internal row
     AmgData* amg = nullptr;
     std::vector<int> natural;
+    // block ILU(0) of a general pattern (vertex-centred grids), else NULL
+    GiluData* gilu = nullptr;
     // max-norm residual reduction the last solve reached: the FP64 true
     // residual for the mixed form, BiCGStab's residual for the plain one
     double lastReduction = 0.0, lastResidual = 0.0;
@@ -247,6 +251,8 @@ void freeSolver(SolverData& S)
 {
     amgDestroy(S.amg);
     S.amg = nullptr;
+    giluDestroy(S.gilu);
+    S.gilu = nullptr;
     cudaFree(S.col);
     cudaFree(S.levPtrD);
     cudaFree(S.tInfo);
@@ -309,6 +315,8 @@ struct gbfv_ctx {
     DevStatus* hst = nullptr;  // pinned
     // owned device arrays of the mesh
     std::vector<void*> owned;
+    // vertex-centred grid: element geometry, incidence and scratch (else NULL)
+    VcfvDev* vcfv = nullptr;
     // natural BCRS view
     std::vector<int> bcrsRowPtr, bcrsCol, bcrsSlot, bcrsRow;
     double dt = 1.0;
@@ -942,6 +950,23 @@ int runAmg(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hst, co
     return rs;
 }
 
+// BiCGStab + general block ILU(0) in precision T: statistics as above
+template <class T>
+int runGilu(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hst, const T* A, const T* rhs, T* x,
+            int factor, double redTol, double absTol, double maxRes, int maxIter, int& iters)
+{
+    float ms = 0;
+    double bytes = 0;
+    const int rs = giluSolve<T>(S.gilu, A, rhs, x, factor, redTol, absTol, maxRes, maxIter, stream, st, hst, iters,
+                                &ms, &bytes);
+    S.statMs += ms;
+    S.statLaunches++;
+    S.statIters += iters;
+    S.statBytes += bytes;
+    if (factor) S.statFactor++;
+    return rs;
+}
+
 // FP64 BiCGStab + ILU0 or AMG (plain form): solves A x = rhs into S.v64[0]
 int solvePlain(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hst, const double* A,
                const double* rhs, const gbfv_params& prm, int& iters)
@@ -952,6 +977,9 @@ int solvePlain(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hst
         rs = runAmg<double>(S, stream, st, hst, A, rhs, S.v64[0], prm.linear_tolerance, absTolOf(prm),
                             prm.linear_max_error, prm.linear_max_iterations, iters);
     }
+    else if (S.gilu)
+        rs = runGilu<double>(S, stream, st, hst, A, rhs, S.v64[0], 1, prm.linear_tolerance, absTolOf(prm),
+                             prm.linear_max_error, prm.linear_max_iterations, iters);
     else
         rs = runKrylov<double>(S, stream, st, hst, A, S.FL64, S.FD64, rhs, S.v64, 1, prm.linear_tolerance,
                                absTolOf(prm), prm.linear_max_error, prm.linear_max_iterations, iters);
@@ -1001,6 +1029,8 @@ int solveMixed(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hst
         float* vec[6] = {S.v32[1], S.v32[2], S.v32[3], S.v32[4], S.v32[5], S.v32[6]};
         const int ks = amg ? runAmg<float>(S, stream, st, hst, S.A32, S.v32[0], S.v32[1], innerTol, 0.0,
                                            prm.linear_max_error, prm.linear_max_iterations, it)
+                       : S.gilu ? runGilu<float>(S, stream, st, hst, S.A32, S.v32[0], S.v32[1], ref == 0, innerTol, 0.0,
+                                                 prm.linear_max_error, prm.linear_max_iterations, it)
                            : runKrylov<float>(S, stream, st, hst, S.A32, S.FL32, S.FD32, S.v32[0], vec, ref == 0,
                                               innerTol, 0.0, prm.linear_max_error, prm.linear_max_iterations, it);
         iters += it;
@@ -1060,10 +1090,219 @@ void gbfv_default_params(gbfv_params* p)
 int64_t gbfv_kernel_launches(void) { return g_launches.load(); }
 const char* gbfv_last_error(void) { return t_lastError.c_str(); }
 
+// material laws, liquid properties and PVT tables of the problem
+// (materialLawParams, the fluid system) in the device record
+static int buildPhysics(const gbfv_problem* P, DevPhysics& ph)
+{
+    std::memset(&ph, 0, sizeof(ph));
+    ph.numMaterials = P->num_materials;
+    for (int m = 0; m < P->num_materials; ++m) {
+        const double* mp = P->material_params + m * GBFV_MAT_STRIDE;
+        const int law = (int)mp[0];
+        TwoPhaseLaw& L = ph.law[m];
+        std::memset(&L, 0, sizeof(L));
+        if (law == GBFV_LAW_REG_VAN_GENUCHTEN || law == GBFV_LAW_REG_BROOKS_COREY) {
+            L.law = law == GBFV_LAW_REG_VAN_GENUCHTEN ? 0 : 1;
+            L.Swr = mp[1];
+            L.Snr = mp[2];
+            if (L.law == 0) { L.alpha = mp[3]; L.n = mp[4]; }
+            else { L.pe = mp[3]; L.lambda = mp[4]; }
+            finalizeLaw(L);
+        }
+        ph.coreyN[m] = law == GBFV_LAW_COREY3P ? mp[4] : 2.0;
+    }
+    ph.rho[0] = P->rho[0];
+    ph.rho[1] = P->rho[1];
+    ph.mu[0] = P->mu[0];
+    ph.mu[1] = P->mu[1];
+    if (P->pvt) {
+        const gbfv_blackoil_pvt& t = *P->pvt;
+        if (t.n_oil < 2 || t.n_oil > GBFV_MAX_TABLE || t.n_gas < 2 || t.n_gas > GBFV_MAX_TABLE) {
+            setError("PVT table size outside [2, 32]");
+            return GBFV_ERR_ARG;
+        }
+        BlackOilPvt& v = ph.pvt;
+        v.rhoRefO = t.rho_ref_oil;
+        v.rhoRefW = t.rho_ref_water;
+        v.rhoRefG = t.rho_ref_gas;
+        v.rsSat.n = v.pBubble.n = v.invBoSat.n = v.muoSat.n = t.n_oil;
+        for (int i = 0; i < t.n_oil; ++i) {
+            v.rsSat.x[i] = t.oil_p[i]; v.rsSat.y[i] = t.oil_rs[i];
+            v.pBubble.x[i] = t.oil_rs[i]; v.pBubble.y[i] = t.oil_p[i];
+            v.invBoSat.x[i] = t.oil_p[i]; v.invBoSat.y[i] = 1.0 / t.oil_bo[i];
+            v.muoSat.x[i] = t.oil_p[i]; v.muoSat.y[i] = t.oil_mu[i];
+        }
+        v.oilComp = t.oil_compressibility;
+        v.invBg.n = v.mug.n = t.n_gas;
+        for (int i = 0; i < t.n_gas; ++i) {
+            v.invBg.x[i] = t.gas_p[i]; v.invBg.y[i] = 1.0 / t.gas_bg[i];
+            v.mug.x[i] = t.gas_p[i]; v.mug.y[i] = t.gas_mu[i];
+        }
+        v.pwRef = t.water_p_ref;
+        v.bwRef = t.water_bw_ref;
+        v.cw = t.water_compressibility;
+        v.muw = t.water_mu;
+    }
+    return GBFV_OK;
+}
+
+// A context on a vertex-centred grid (VcfvDiscretization): the degrees of
+// freedom are the vertices; the Jacobian has the 3 x 3 vertex neighbourhood
+// in VCFV_SLOTS slots (ascending natural column, the diagonal in the middle)
+// and is solved by the general block ILU(0) (or the AMG backend).  The
+// per-vertex kernels (intensive quantities, Newton error and update,
+// constraints, output fields) are the cell-centred ones.
+static int createVcfvImpl(gbfv_ctx* C, const gbfv_problem* P)
+{
+    if (C->prm.local_linearizer != GBFV_LIN_AD || C->prm.linearizer != GBFV_LINEARIZER_ELEMENT) {
+        setError("vertex-centred grids take the element linearizer with automatic differentiation");
+        return GBFV_ERR_UNSUPPORTED;
+    }
+    VcfvSetup vs;
+    if (const int st = vcfvSetup(P, vs)) return st;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        setError("no CUDA device");
+        return GBFV_ERR_NO_DEVICE;
+    }
+    const int N = P->num_cells, b = 2, nslot = VCFV_SLOTS;
+    C->N = N;
+    C->model = P->model;
+    C->b = b;
+    C->dim = 2;
+    const int ld = ((N + 63) / 64) * 64;
+    C->ldN = ld;
+    if ((int64_t)nslot * b * b * ld > std::numeric_limits<int>::max()) {
+        setError("grid too large for the 9-slot Jacobian's 32-bit indexing");
+        return GBFV_ERR_UNSUPPORTED;
+    }
+    // level-major order from the lower neighbours (natural index below)
+    std::vector<std::vector<int>> lower(N);
+    for (int i = 0; i < N; ++i)
+        for (int sl = 0; sl < VCFV_DIAG; ++sl) {
+            const int q = vs.nbr[(size_t)i * nslot + sl];
+            if (q >= 0) lower[i].push_back(q);
+        }
+    std::vector<int> levPtr;
+    buildOrder(N, lower, C->perm, C->iperm, levPtr);
+    const std::vector<int>& perm = C->perm;
+    const std::vector<int>& iperm = C->iperm;
+    std::vector<int> hCol((size_t)nslot * ld, -1);
+    for (int i = 0; i < N; ++i)
+        for (int sl = 0; sl < nslot; ++sl) {
+            const int q = vs.nbr[(size_t)i * nslot + sl];
+            if (q >= 0) hCol[(size_t)sl * ld + perm[i]] = perm[q];
+        }
+    C->bcrsRowPtr.assign(N + 1, 0);
+    for (int i = 0; i < N; ++i) {
+        for (int sl = 0; sl < nslot; ++sl) {
+            const int q = vs.nbr[(size_t)i * nslot + sl];
+            if (q < 0) continue;
+            C->bcrsCol.push_back(q);
+            C->bcrsSlot.push_back(sl);
+            C->bcrsRow.push_back(perm[i]);
+        }
+        C->bcrsRowPtr[i + 1] = (int)C->bcrsCol.size();
+    }
+    DevPhysics& ph = C->hphys;
+    if (const int pst = buildPhysics(P, ph)) return pst;
+    std::vector<double> hVol(ld, 1.0), hPor(ld, 0.0), hPerm((size_t)3 * ld, 0.0);
+    std::vector<int> hMat(ld, 0), hCflag(ld, -1);
+    for (int p = 0; p < N; ++p) {
+        const int I = iperm[p];
+        hVol[p] = vs.totalVolume[I];
+        hPor[p] = P->porosity[I];
+        for (int d = 0; d < 3; ++d) hPerm[(size_t)d * ld + p] = P->perm[3 * I + d];
+        hMat[p] = P->material[I];
+    }
+    CK(cudaStreamCreateWithFlags(&C->stream, cudaStreamNonBlocking));
+    for (auto& e : C->ev) CK(cudaEventCreate(&e));
+    DevMesh& m = C->mesh;
+    std::memset(&m, 0, sizeof(m));
+    m.N = N;
+    m.ldN = ld;
+    m.dim = 2;
+    m.b = b;
+    m.model = C->model;
+    m.nslot = nslot;
+    m.fluxModule = GBFV_FLUX_DARCY;
+    int st;
+    auto up = [&](auto** dst, const auto& vec) {
+        int s2 = upload(dst, vec);
+        if (!s2) C->owned.push_back((void*)*dst);
+        return s2;
+    };
+    int *dMat, *dCflag;
+    double *dVol, *dPor, *dPerm;
+    if ((st = up(&dVol, hVol)) || (st = up(&dPor, hPor)) || (st = up(&dPerm, hPerm)) || (st = up(&dMat, hMat)) ||
+        (st = up(&dCflag, hCflag)))
+        return st;
+    m.volume = dVol;
+    m.porosity = dPor;
+    m.perm = dPerm;
+    m.material = dMat;
+    m.cflag = dCflag;
+    m.numConsCells = 0;
+    if ((st = devAlloc(&C->dphys, 1))) return st;
+    CK(cudaMemcpy(C->dphys, &ph, sizeof(DevPhysics), cudaMemcpyHostToDevice));
+    C->vcfv = vcfvUpload(P, vs, ph, perm, ld, &st);
+    if (!C->vcfv) return st;
+    // state
+    const size_t nb = (size_t)N * b;
+    if ((st = devAlloc(&C->x, nb)) || (st = devAlloc(&C->xOld, nb)) || (st = devAlloc(&C->residual, nb)) ||
+        (st = devAlloc(&C->dx, nb)) || (st = devAlloc(&C->storageOld, (size_t)b * ld)) ||
+        (st = devAlloc(&C->meaning, (size_t)N)) || (st = devAlloc(&C->meaningOld, (size_t)N)) ||
+        (st = devAlloc(&C->wasSwitched, (size_t)N)) || (st = devAlloc(&C->refP, 1)))
+        return st;
+    CK(cudaMemset(C->meaning, 0, sizeof(int) * N));
+    CK(cudaMemset(C->meaningOld, 0, sizeof(int) * N));
+    CK(cudaMemset(C->wasSwitched, 0, sizeof(int) * N));
+    CK(cudaMemset(C->x, 0, sizeof(double) * nb));
+    CK(cudaMemset(C->xOld, 0, sizeof(double) * nb));
+    {
+        const double one = 1.0;
+        CK(cudaMemcpy(C->refP, &one, sizeof(double), cudaMemcpyHostToDevice));
+    }
+    if ((st = devAlloc(&C->iq.val, (size_t)iqValuePlanes(b) * ld)) ||
+        (st = devAlloc(&C->iq.der, (size_t)iqDerivPlanes(b) * ld)) ||
+        (st = devAlloc(&C->iq.sto, (size_t)iqStoragePlanes(b) * ld)))
+        return st;
+    if ((st = devAlloc(&C->jval, (size_t)nslot * b * b * ld))) return st;
+    CK(cudaMemset(C->jval, 0, sizeof(double) * (size_t)nslot * b * b * ld));
+    // solver: the general block ILU(0) (the AMG backend on the same layout)
+    SolverData& S = C->S;
+    S.N = N;
+    S.b = b;
+    S.dim = 2;
+    S.nslot = nslot;
+    S.ldN = ld;
+    S.levPtr = levPtr;
+    S.colHost = hCol;
+    S.natural = iperm;
+    if ((st = upload(&S.col, hCol)) || (st = upload(&S.levPtrD, levPtr))) return st;
+    if ((st = allocSolver(S))) return st;
+    S.gilu = giluCreate(N, b, nslot, ld, hCol, S.col, levPtr, &st);
+    if (!S.gilu) return st;
+    if ((st = devAlloc(&C->st, 1))) return st;
+    CK(cudaMallocHost((void**)&C->hst, sizeof(DevStatus)));
+    CK(cudaMemset(C->st, 0, sizeof(DevStatus)));
+    if ((st = devAlloc(&C->xSave, nb)) || (st = devAlloc(&C->meaningSave, (size_t)N)) ||
+        (st = devAlloc(&C->switchedSave, (size_t)N)))
+        return st;
+    CK(cudaEventCreate(&C->evL0));
+    CK(cudaEventCreate(&C->evL1));
+    {
+        const double k1 = b * 8.0 + 8 + 4 + (iqValuePlanes(b) + iqDerivPlanes(b) + iqStoragePlanes(b)) * 8.0;
+        C->linBytesPer = N * k1 + vcfvLinearizeBytes(C->vcfv);
+    }
+    return GBFV_OK;
+}
+
 static int createImpl(gbfv_ctx* C, const gbfv_problem* P)
 {
     // counts, offsets, enums and tables first: everything below follows them
     if (const int chk = gbfv::checkProblem(P, MAX_MATERIALS, GBFV_MAX_TABLE)) return chk;
+    if (P->num_elements > 0) return createVcfvImpl(C, P);
     const int N = P->num_cells;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
@@ -1295,55 +1534,7 @@ static int createImpl(gbfv_ctx* C, const gbfv_problem* P)
     }
     // physics parameters
     DevPhysics& ph = C->hphys;
-    std::memset(&ph, 0, sizeof(ph));
-    ph.numMaterials = P->num_materials;
-    for (int m = 0; m < P->num_materials; ++m) {
-        const double* mp = P->material_params + m * GBFV_MAT_STRIDE;
-        const int law = (int)mp[0];
-        TwoPhaseLaw& L = ph.law[m];
-        std::memset(&L, 0, sizeof(L));
-        if (law == GBFV_LAW_REG_VAN_GENUCHTEN || law == GBFV_LAW_REG_BROOKS_COREY) {
-            L.law = law == GBFV_LAW_REG_VAN_GENUCHTEN ? 0 : 1;
-            L.Swr = mp[1];
-            L.Snr = mp[2];
-            if (L.law == 0) { L.alpha = mp[3]; L.n = mp[4]; }
-            else { L.pe = mp[3]; L.lambda = mp[4]; }
-            finalizeLaw(L);
-        }
-        ph.coreyN[m] = law == GBFV_LAW_COREY3P ? mp[4] : 2.0;
-    }
-    ph.rho[0] = P->rho[0];
-    ph.rho[1] = P->rho[1];
-    ph.mu[0] = P->mu[0];
-    ph.mu[1] = P->mu[1];
-    if (P->pvt) {
-        const gbfv_blackoil_pvt& t = *P->pvt;
-        if (t.n_oil < 2 || t.n_oil > GBFV_MAX_TABLE || t.n_gas < 2 || t.n_gas > GBFV_MAX_TABLE) {
-            setError("PVT table size outside [2, 32]");
-            return GBFV_ERR_ARG;
-        }
-        BlackOilPvt& v = ph.pvt;
-        v.rhoRefO = t.rho_ref_oil;
-        v.rhoRefW = t.rho_ref_water;
-        v.rhoRefG = t.rho_ref_gas;
-        v.rsSat.n = v.pBubble.n = v.invBoSat.n = v.muoSat.n = t.n_oil;
-        for (int i = 0; i < t.n_oil; ++i) {
-            v.rsSat.x[i] = t.oil_p[i]; v.rsSat.y[i] = t.oil_rs[i];
-            v.pBubble.x[i] = t.oil_rs[i]; v.pBubble.y[i] = t.oil_p[i];
-            v.invBoSat.x[i] = t.oil_p[i]; v.invBoSat.y[i] = 1.0 / t.oil_bo[i];
-            v.muoSat.x[i] = t.oil_p[i]; v.muoSat.y[i] = t.oil_mu[i];
-        }
-        v.oilComp = t.oil_compressibility;
-        v.invBg.n = v.mug.n = t.n_gas;
-        for (int i = 0; i < t.n_gas; ++i) {
-            v.invBg.x[i] = t.gas_p[i]; v.invBg.y[i] = 1.0 / t.gas_bg[i];
-            v.mug.x[i] = t.gas_p[i]; v.mug.y[i] = t.gas_mu[i];
-        }
-        v.pwRef = t.water_p_ref;
-        v.bwRef = t.water_bw_ref;
-        v.cw = t.water_compressibility;
-        v.muw = t.water_mu;
-    }
+    if (const int pst = buildPhysics(P, ph)) return pst;
     // boundary faces in internal order, free-flow states on the host
     std::vector<int> hBfPtr(N + 1, 0);
     std::vector<BFace> hBf;
@@ -1660,6 +1851,7 @@ int gbfv_destroy(gbfv_ctx* C)
     cudaFree(C->refP);
     cudaFree(C->jval);
     freeSolver(C->S);
+    vcfvDestroy(C->vcfv);
     cudaFree(C->st);
     cudaFree(C->xSave);
     cudaFree(C->meaningSave);
@@ -1680,6 +1872,10 @@ int gbfv_set_params(gbfv_ctx* C, const gbfv_params* p)
     if (!C || !p || !paramsOk(*p)) return GBFV_ERR_ARG;
     if (p->linearizer != C->prm.linearizer) {
         setError("the linearizer is fixed when the context is created");
+        return GBFV_ERR_UNSUPPORTED;
+    }
+    if (C->vcfv && p->local_linearizer != GBFV_LIN_AD) {
+        setError("vertex-centred grids take the AD local linearizer");
         return GBFV_ERR_UNSUPPORTED;
     }
     C->prm = *p;
@@ -1836,8 +2032,12 @@ static int linearizeImpl(gbfv_ctx* C)
     }
     cudaEventRecord(C->evL0, C->stream);
     launchIq(C->mesh, C->dphys, C->x, C->meaning, C->iq, C->stream);
-    launchAssemble(C->mesh, C->dphys, C->iq, C->storageOld, C->newtonIter == 0, C->dt, C->residual, C->jval,
-                   C->stream);
+    if (C->vcfv)
+        launchVcfvAssemble(C->vcfv, C->mesh, C->iq, C->storageOld, C->newtonIter == 0, C->dt, C->residual, C->jval,
+                           C->stream);
+    else
+        launchAssemble(C->mesh, C->dphys, C->iq, C->storageOld, C->newtonIter == 0, C->dt, C->residual, C->jval,
+                       C->stream);
     cudaEventRecord(C->evL1, C->stream);
     C->linPending = 1;
     CK(cudaGetLastError());
@@ -2297,8 +2497,14 @@ gbfv_linsolver* gbfv_linsolver_create(int n, int b, const int32_t* rowPtr, const
     std::sort(offs.begin(), offs.end());
     offs.erase(std::unique(offs.begin(), offs.end()), offs.end());
     const int nslot = (int)offs.size();
-    if (nslot > MAX_SLOTS || nslot % 2 == 0) { setError("pattern needs at most 7 symmetric offsets"); return fail(L, GBFV_ERR_UNSUPPORTED); }
-    const int dim = nslot / 2;
+    if (nslot > GILU_MAX_SLOTS || nslot % 2 == 0) {
+        setError("pattern needs at most 27 symmetric offsets");
+        return fail(L, GBFV_ERR_UNSUPPORTED);
+    }
+    // patterns beyond the 5/7-point stencil's (more offsets, or ILU(0) fill
+    // interactions) go to the general block ILU(0)
+    bool general = nslot > MAX_SLOTS;
+    const int dim = general ? 1 : nslot / 2;
     for (int s = 0; s < nslot; ++s)
         if (offs[s] != -offs[nslot - 1 - s]) { setError("asymmetric pattern offsets"); return fail(L, GBFV_ERR_UNSUPPORTED); }
     auto slotOf = [&](int off) { return (int)(std::lower_bound(offs.begin(), offs.end(), off) - offs.begin()); };
@@ -2312,14 +2518,14 @@ gbfv_linsolver* gbfv_linsolver_create(int n, int b, const int32_t* rowPtr, const
         }
         if (!diag) { setError("diagonal entry missing"); return fail(L, GBFV_ERR_ARG); }
     }
-    // ILU(0) update structure check
-    for (int i = 0; i < n; ++i)
+    // ILU(0) update structure: does a lower entry update more than the diagonal?
+    for (int i = 0; i < n && !general; ++i)
         for (int k : lower[i])
             for (int kk = rowPtr[k]; kk < rowPtr[k + 1]; ++kk) {
                 const int j = col[kk];
                 if (j <= k || j == i) continue;
                 for (int q = rowPtr[i]; q < rowPtr[i + 1]; ++q)
-                    if (col[q] == j) { setError("pattern has ILU(0) fill interactions beyond the diagonal"); return fail(L, GBFV_ERR_UNSUPPORTED); }
+                    if (col[q] == j) general = true;
             }
     std::vector<int> levPtr;
     buildOrder(n, lower, L->perm, L->iperm, levPtr);
@@ -2355,6 +2561,10 @@ gbfv_linsolver* gbfv_linsolver_create(int n, int b, const int32_t* rowPtr, const
     int st;
     if ((st = upload(&S.col, hCol)) || (st = upload(&S.levPtrD, levPtr)) || (st = allocSolver(S)))
         return fail(L, st);
+    if (general) {
+        S.gilu = giluCreate(n, b, nslot, ld, hCol, S.col, levPtr, &st);
+        if (!S.gilu) return fail(L, st);
+    }
     const size_t nval = (size_t)nslot * b * b * ld;
     if ((st = devAlloc(&L->A64, nval)) || (st = devAlloc(&L->rhs, (size_t)n * b)) || (st = devAlloc(&L->st, 1)))
         return fail(L, st);
@@ -2453,6 +2663,26 @@ int gbfv_linsolver_amg_levels(gbfv_linsolver* L, int32_t* sizes, int32_t* colors
 }
 
 // one FP64 V-cycle of the AMG preconditioner, v = M^-1 d (natural order)
+int gbfv_linsolver_ilu0_apply(gbfv_linsolver* L, const double* d, double* v)
+{
+    if (!L || !d || !v) return GBFV_ERR_ARG;
+    if (!L->S.gilu) {
+        setError("the matrix's pattern uses the structured ILU(0) solver, which has no separate apply");
+        return GBFV_ERR_UNSUPPORTED;
+    }
+    const int n = L->N, b = L->b;
+    for (int i = 0; i < n; ++i)
+        for (int e = 0; e < b; ++e) L->stage[(size_t)L->perm[i] * b + e] = d[(size_t)i * b + e];
+    CK(cudaMemcpyAsync(L->rhs, L->stage, sizeof(double) * n * b, cudaMemcpyHostToDevice, L->stream));
+    int st = giluApply64(L->S.gilu, L->A64, L->rhs, L->S.v64[0], L->stream, L->st, L->hst);
+    if (st) return st;
+    CK(cudaMemcpyAsync(L->stage, L->S.v64[0], sizeof(double) * n * b, cudaMemcpyDeviceToHost, L->stream));
+    CK(cudaStreamSynchronize(L->stream));
+    for (int i = 0; i < n; ++i)
+        for (int e = 0; e < b; ++e) v[(size_t)i * b + e] = L->stage[(size_t)L->perm[i] * b + e];
+    return GBFV_OK;
+}
+
 int gbfv_linsolver_amg_apply(gbfv_linsolver* L, const double* d, double* v)
 {
     if (!L || !d || !v) return GBFV_ERR_ARG;
@@ -3271,6 +3501,11 @@ gbfv_batch* gbfv_batch_create(const gbfv_problem* probs, int num_systems, const 
         setError("batched systems are linearized element by element only");
         return fail(nullptr, GBFV_ERR_UNSUPPORTED);
     }
+    for (int i = 0; i < num_systems; ++i)
+        if (probs[i].num_elements > 0) {
+            setError("batched systems are cell-centred grids only");
+            return fail(nullptr, GBFV_ERR_UNSUPPORTED);
+        }
     gbfv_batch* B = new gbfv_batch();
     if (params) B->prm = *params;
     else gbfv_default_params(&B->prm);
@@ -3479,6 +3714,10 @@ int gbfv_serve_admit(gbfv_batch* B, const gbfv_problem* prob, const double* pv, 
     if (prob->num_cells > B->maxCells) {
         setError("system larger than the server's max_cells");
         return GBFV_ERR_ARG;
+    }
+    if (prob->num_elements > 0) {
+        setError("served systems are cell-centred grids only");
+        return GBFV_ERR_UNSUPPORTED;
     }
     int i = -1;
     for (int k = 0; k < B->K; ++k)

@@ -1,0 +1,700 @@
+// Block ILU(0) + BiCGStab for a general block-ELL pattern.
+//
+// The structured solver (solver.cu) relies on the 5/7-point pattern, whose
+// ILU(0) only modifies the diagonal.  The vertex-centred Jacobian couples
+// every vertex with its 3 x 3 neighbourhood: there a lower entry (i, k)
+// also updates the row's other entries that row k's upper part shares, so
+// this kernel runs the full natural-order block ILU(0) (dune-istl's
+// blockILU0Decomposition as Dune::SeqILU<..., 0> calls it from
+// istlpreconditionerwrappers.hh:151-190; not vendored, restated):
+//     for each lower entry k of row i, ascending:
+//         A_ik <- A_ik * inv(U_kk)
+//         A_ij <- A_ij - A_ik * A_kj   for every j > k in both rows
+//     U_ii <- inv(A_ii)
+// Rows of one level (rows whose lower neighbours are all in earlier levels)
+// are independent; levels are separated by barriers.  The triangular
+// sweeps and BiCGStab (bicgstabsolver.hh:120-330, the structured solver's
+// iteration and criterion) run in the same persistent launch: one block
+// (block barriers) for systems whose levels fit a block, else a cooperative
+// grid with the bounded software barrier.  Block operations follow the
+// reference's order (FieldMatrix::rightmultiply, mmv, the cofactor
+// inverse), so with FMA contraction off the FP64 preconditioner is the
+// oracle's to the last bit.
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/gbfv.h"
+#include "gbfv_internal.cuh"
+#include "gilu.cuh"
+#include "krylov.cuh"
+
+namespace gbfv {
+
+void setLastError(const std::string& s);
+
+namespace {
+
+constexpr int GILU_THREADS = 256;
+
+template <class T>
+struct GiluArgs {
+    int N, ld, nslot, diag, numLev, factor;
+    const int* col;      // [s*ld + p] internal column or -1
+    const int* levPtr;   // [numLev + 1]
+    const int* updPtr;   // [N + 1] factorization updates of row p
+    const int* upd;      // (s | t << 8 | u << 16): A_pt -= A_ps * A_ku, k = col[s][p]
+    const T* A;
+    T* F;                // factors, A's layout; the diagonal slot holds inv(U_pp)
+    const T* rhs;
+    T *x, *r, *p, *v, *y, *z;
+    double* partial;
+    GridSync gs;
+    DevStatus* st;
+    double redTol, absTol, maxRes;
+    int maxIter;
+};
+
+template <class T, int B>
+__device__ __forceinline__ void ldBlk(const T* M, int s, int ld, int p, T (&o)[B * B])
+{
+#pragma unroll
+    for (int e = 0; e < B * B; ++e) o[e] = ldcg(&M[((size_t)s * B * B + e) * ld + p]);
+}
+template <class T, int B>
+__device__ __forceinline__ void stBlk(T* M, int s, int ld, int p, const T (&o)[B * B])
+{
+#pragma unroll
+    for (int e = 0; e < B * B; ++e) M[((size_t)s * B * B + e) * ld + p] = o[e];
+}
+
+// row p of the factorization (its lower neighbours are final)
+template <class T, int B>
+__device__ bool factorRow(const GiluArgs<T>& a, int p)
+{
+    const int ld = a.ld;
+    for (int s = 0; s < a.nslot; ++s) {
+        T blk[B * B];
+        ldBlk<T, B>(a.A, s, ld, p, blk);
+        stBlk<T, B>(a.F, s, ld, p, blk);
+    }
+    int q = a.updPtr[p];
+    const int q1 = a.updPtr[p + 1];
+    for (int s = 0; s < a.diag; ++s) {
+        const int k = a.col[(size_t)s * ld + p];
+        if (k < 0) continue;
+        // A_ps <- A_ps * inv(U_kk)
+        T L[B * B], Dk[B * B], C[B * B];
+        ldBlk<T, B>(a.F, s, ld, p, C);
+        ldBlk<T, B>(a.F, a.diag, ld, k, Dk);
+#pragma unroll
+        for (int i = 0; i < B; ++i)
+#pragma unroll
+            for (int j = 0; j < B; ++j) {
+                T t = T(0);
+#pragma unroll
+                for (int m = 0; m < B; ++m) t += C[i * B + m] * Dk[m * B + j];
+                L[i * B + j] = t;
+            }
+        stBlk<T, B>(a.F, s, ld, p, L);
+        // A_pt -= L * A_ku for the entries the two rows share
+        for (; q < q1 && (a.upd[q] & 0xff) == s; ++q) {
+            const int t = (a.upd[q] >> 8) & 0xff, u = (a.upd[q] >> 16) & 0xff;
+            T U[B * B], Tt[B * B];
+            ldBlk<T, B>(a.F, u, ld, k, U);
+            ldBlk<T, B>(a.F, t, ld, p, Tt);
+#pragma unroll
+            for (int i = 0; i < B; ++i)
+#pragma unroll
+                for (int j = 0; j < B; ++j) {
+                    T acc = T(0);
+#pragma unroll
+                    for (int m = 0; m < B; ++m) acc += L[i * B + m] * U[m * B + j];
+                    Tt[i * B + j] -= acc;
+                }
+            stBlk<T, B>(a.F, t, ld, p, Tt);
+        }
+    }
+    T D[B * B], R[B * B];
+    ldBlk<T, B>(a.F, a.diag, ld, p, D);
+    if (!invertBlock<T, B>(D, R)) return false;
+    stBlk<T, B>(a.F, a.diag, ld, p, R);
+    return true;
+}
+
+// v = (LU)^-1 d: the forward sweep over the levels, then the backward one
+// (dune-istl's blockILUBacksolve)
+template <class T, int B, class Bar>
+__device__ bool iluApply(const GiluArgs<T>& a, const T* d, T* v, int gt, int gs, const Bar& bar)
+{
+    const int ld = a.ld;
+    for (int l = 0; l < a.numLev; ++l) {
+        for (int p = a.levPtr[l] + gt; p < a.levPtr[l + 1]; p += gs) {
+            T rhs[B];
+#pragma unroll
+            for (int e = 0; e < B; ++e) rhs[e] = ldcg(&d[p * B + e]);
+            for (int s = 0; s < a.diag; ++s) {
+                const int k = a.col[(size_t)s * ld + p];
+                if (k < 0) continue;
+                T L[B * B];
+                ldBlk<T, B>(a.F, s, ld, p, L);
+#pragma unroll
+                for (int i = 0; i < B; ++i)
+#pragma unroll
+                    for (int j = 0; j < B; ++j) rhs[i] -= L[i * B + j] * ldcg(&v[k * B + j]);
+            }
+#pragma unroll
+            for (int e = 0; e < B; ++e) v[p * B + e] = rhs[e];
+        }
+        if (!bar()) return false;
+    }
+    for (int l = a.numLev - 1; l >= 0; --l) {
+        for (int p = a.levPtr[l] + gt; p < a.levPtr[l + 1]; p += gs) {
+            T rhs[B];
+#pragma unroll
+            for (int e = 0; e < B; ++e) rhs[e] = ldcg(&v[p * B + e]);
+            for (int s = a.nslot - 1; s > a.diag; --s) {
+                const int k = a.col[(size_t)s * ld + p];
+                if (k < 0) continue;
+                T U[B * B];
+                ldBlk<T, B>(a.F, s, ld, p, U);
+#pragma unroll
+                for (int i = 0; i < B; ++i)
+#pragma unroll
+                    for (int j = 0; j < B; ++j) rhs[i] -= U[i * B + j] * ldcg(&v[k * B + j]);
+            }
+            T Di[B * B];
+            ldBlk<T, B>(a.F, a.diag, ld, p, Di);
+#pragma unroll
+            for (int i = 0; i < B; ++i) {
+                T t = T(0);
+#pragma unroll
+                for (int j = 0; j < B; ++j) t += Di[i * B + j] * rhs[j];
+                v[p * B + i] = t;
+            }
+        }
+        if (!bar()) return false;
+    }
+    return true;
+}
+
+template <class T, int B, class Bar>
+__device__ bool factorAll(const GiluArgs<T>& a, int gt, int gs, const Bar& bar)
+{
+    for (int l = 0; l < a.numLev; ++l) {
+        for (int p = a.levPtr[l] + gt; p < a.levPtr[l + 1]; p += gs)
+            if (!factorRow<T, B>(a, p)) {
+                atomicCAS(&a.st->code, 0, (int)GBFV_ERR_SINGULAR);
+                a.st->where = p;
+            }
+        if (!bar()) return false;
+    }
+    return true;
+}
+
+// y = A x, row p, slots in ascending column order (BCRSMatrix::mv)
+template <class T, int B>
+__device__ __forceinline__ void spmvRow(const GiluArgs<T>& a, const T* xin, int p, T (&acc)[B])
+{
+#pragma unroll
+    for (int e = 0; e < B; ++e) acc[e] = T(0);
+    for (int s = 0; s < a.nslot; ++s) {
+        const int k = a.col[(size_t)s * a.ld + p];
+        if (k < 0) continue;
+        T M[B * B];
+#pragma unroll
+        for (int e = 0; e < B * B; ++e) M[e] = a.A[((size_t)s * B * B + e) * a.ld + p];
+#pragma unroll
+        for (int i = 0; i < B; ++i)
+#pragma unroll
+            for (int j = 0; j < B; ++j) acc[i] += M[i * B + j] * ldcg(&xin[k * B + j]);
+    }
+}
+
+struct GBar {
+    const GridSync* g;
+    __device__ bool operator()() const { return gridBarrier(*g); }
+};
+
+// BiCGStabSolver::apply (bicgstabsolver.hh:120-330) with the block ILU(0)
+// preconditioner, factorization included, in one cooperative launch
+template <class T, int B>
+__global__ void __launch_bounds__(GILU_THREADS) kGiluBicgstab(const GiluArgs<T> a)
+{
+    const Team<SYNC_GRID> tm;
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
+    const int N = a.N;
+    const GBar bar{&a.gs};
+    const double eps = 2.2250738585072014e-308 * 1e10;  // numeric_limits<double>::min()*1e10
+    if (a.factor) {
+        if (!factorAll<T, B>(a, gt, gs, bar)) goto timeout;
+        if (*(volatile int*)&a.st->code != 0) return;
+    }
+    {
+        double mx[1] = {0.0};
+        const bool isMax1[1] = {true};
+        for (int i = gt; i < N; i += gs)
+#pragma unroll
+            for (int e = 0; e < B; ++e) {
+                const T bi = a.rhs[i * B + e];
+                a.x[i * B + e] = T(0);
+                a.r[i * B + e] = bi;
+                a.v[i * B + e] = T(0);
+                a.p[i * B + e] = T(0);
+                mx[0] = fmax(mx[0], fabs((double)bi));
+            }
+        blockPartials<1, SYNC_GRID>(mx, isMax1, a.partial, tm);
+        if (!gridBarrier(a.gs)) goto timeout;
+    }
+    {
+        double tot[1];
+        const bool isMax1[1] = {true};
+        allCombine<1, SYNC_GRID>(a.partial, isMax1, tot, tm);
+        double resErr = fmax(tot[0], eps);
+        const double initErr = resErr;
+        auto converged = [&](double re) { return re / fmax(1e-20, initErr) <= a.redTol || re <= a.absTol; };
+        if (converged(resErr)) {
+            if (gt == 0) {
+                a.st->converged = 1;
+                a.st->iterations = 0;
+                a.st->resid = resErr;
+                a.st->resid0 = initErr;
+            }
+            return;
+        }
+        double rho = 1.0, alpha = 1.0, omega = 1.0;
+        {
+            double dd[1] = {0.0};
+            const bool isSum1[1] = {false};
+            for (int i = gt; i < N; i += gs) {
+                double t = 0.0;
+#pragma unroll
+                for (int e = 0; e < B; ++e) t += (double)(a.rhs[i * B + e] * a.rhs[i * B + e]);
+                dd[0] += t;
+            }
+            blockPartials<1, SYNC_GRID>(dd, isSum1, a.partial + 2 * tm.nblk, tm);
+            if (!gridBarrier(a.gs)) goto timeout;
+        }
+        int it = 0;
+        int buf = 1;
+        for (; it < a.maxIter; ++it) {
+            double rho_i;
+            {
+                const bool isSum1[1] = {false};
+                double tot1[1];
+                allCombine<1, SYNC_GRID>(a.partial + 2 * tm.nblk * buf, isSum1, tot1, tm);
+                rho_i = tot1[0];
+            }
+            if (fabs(rho) <= eps || fabs(omega) <= eps) {
+                if (gt == 0) a.st->code = GBFV_ERR_BREAKDOWN;
+                break;
+            }
+            const double beta = (rho_i / rho) * (alpha / omega);
+            rho = rho_i;
+            {
+                // p = r - beta (p - omega v), in the reference's steps
+                const T tb = (T)beta, to = (T)omega;
+                for (int i = gt; i < N; i += gs)
+#pragma unroll
+                    for (int e = 0; e < B; ++e) {
+                        T tmp = ldcg(&a.v[i * B + e]);
+                        tmp *= to;
+                        tmp -= ldcg(&a.p[i * B + e]);
+                        tmp *= -tb;
+                        a.p[i * B + e] = ldcg(&a.r[i * B + e]) + tmp;
+                    }
+                if (!gridBarrier(a.gs)) goto timeout;
+            }
+            if (!iluApply<T, B>(a, a.p, a.y, gt, gs, bar)) goto timeout;
+            {
+                double dd[1] = {0.0};
+                const bool isSum1[1] = {false};
+                for (int i = gt; i < N; i += gs) {
+                    T acc[B];
+                    spmvRow<T, B>(a, a.y, i, acc);
+                    double t = 0.0;
+#pragma unroll
+                    for (int e = 0; e < B; ++e) {
+                        a.v[i * B + e] = acc[e];
+                        t += (double)(a.rhs[i * B + e] * acc[e]);
+                    }
+                    dd[0] += t;
+                }
+                buf ^= 1;
+                blockPartials<1, SYNC_GRID>(dd, isSum1, a.partial + 2 * tm.nblk * buf, tm);
+                if (!gridBarrier(a.gs)) goto timeout;
+                double tot1[1];
+                allCombine<1, SYNC_GRID>(a.partial + 2 * tm.nblk * buf, isSum1, tot1, tm);
+                const double denom = tot1[0];
+                if (fabs(denom) <= eps) {
+                    if (gt == 0) a.st->code = GBFV_ERR_BREAKDOWN;
+                    break;
+                }
+                alpha = rho_i / denom;
+                if (fabs(alpha) <= eps) {
+                    if (gt == 0) a.st->code = GBFV_ERR_BREAKDOWN;
+                    break;
+                }
+            }
+            {
+                double red[2] = {0.0, 0.0};
+                const bool kinds[2] = {true, true};
+                const T ta = (T)alpha;
+                for (int i = gt; i < N; i += gs)
+#pragma unroll
+                    for (int e = 0; e < B; ++e) {
+                        T tmp = ldcg(&a.y[i * B + e]);
+                        if (tmp != T(0)) red[1] = 1.0;
+                        tmp *= ta;
+                        tmp += ldcg(&a.x[i * B + e]);
+                        a.x[i * B + e] = tmp;
+                        tmp = ldcg(&a.v[i * B + e]);
+                        tmp *= ta;
+                        const T si = ldcg(&a.r[i * B + e]) - tmp;
+                        a.r[i * B + e] = si;
+                        red[0] = fmax(red[0], fabs((double)si));
+                    }
+                buf ^= 1;
+                blockPartials<2, SYNC_GRID>(red, kinds, a.partial + 2 * tm.nblk * buf, tm);
+                if (!gridBarrier(a.gs)) goto timeout;
+                double tot2[2];
+                allCombine<2, SYNC_GRID>(a.partial + 2 * tm.nblk * buf, kinds, tot2, tm);
+                resErr = tot2[0];
+                const bool stag = tot2[1] == 0.0;
+                if (converged(resErr)) {
+                    if (gt == 0) a.st->converged = 1;
+                    break;
+                }
+                if (stag || resErr > a.maxRes) break;
+            }
+            if (!iluApply<T, B>(a, a.r, a.z, gt, gs, bar)) goto timeout;
+            {
+                double dd[2] = {0.0, 0.0};
+                const bool isSum2[2] = {false, false};
+                for (int i = gt; i < N; i += gs) {
+                    T acc[B];
+                    spmvRow<T, B>(a, a.z, i, acc);
+                    double t0 = 0.0, t1 = 0.0;
+#pragma unroll
+                    for (int e = 0; e < B; ++e) {
+                        a.y[i * B + e] = acc[e];
+                        t0 += (double)(acc[e] * acc[e]);
+                        t1 += (double)(acc[e] * ldcg(&a.r[i * B + e]));
+                    }
+                    dd[0] += t0;
+                    dd[1] += t1;
+                }
+                buf ^= 1;
+                blockPartials<2, SYNC_GRID>(dd, isSum2, a.partial + 2 * tm.nblk * buf, tm);
+                if (!gridBarrier(a.gs)) goto timeout;
+                double tot2[2];
+                allCombine<2, SYNC_GRID>(a.partial + 2 * tm.nblk * buf, isSum2, tot2, tm);
+                const double denom = tot2[0];
+                if (fabs(denom) <= eps) {
+                    if (gt == 0) a.st->code = GBFV_ERR_BREAKDOWN;
+                    break;
+                }
+                omega = tot2[1] / denom;
+                if (fabs(omega) <= eps) {
+                    if (gt == 0) a.st->code = GBFV_ERR_BREAKDOWN;
+                    break;
+                }
+            }
+            {
+                double red[2] = {0.0, 0.0};
+                const bool kinds[2] = {false, true};
+                const T to = (T)omega;
+                for (int i = gt; i < N; i += gs) {
+                    double t = 0.0;
+#pragma unroll
+                    for (int e = 0; e < B; ++e) {
+                        const T zi = ldcg(&a.z[i * B + e]);
+                        if (zi != T(0)) red[1] = 1.0;
+                        a.x[i * B + e] = ldcg(&a.x[i * B + e]) + to * zi;
+                        const T ri = ldcg(&a.r[i * B + e]) + (-to) * ldcg(&a.y[i * B + e]);
+                        a.r[i * B + e] = ri;
+                        t += (double)(a.rhs[i * B + e] * ri);
+                    }
+                    red[0] += t;
+                }
+                buf ^= 1;
+                blockPartials<2, SYNC_GRID>(red, kinds, a.partial + 2 * tm.nblk * buf, tm);
+                if (!gridBarrier(a.gs)) goto timeout;
+                double tot2[2];
+                allCombine<2, SYNC_GRID>(a.partial + 2 * tm.nblk * buf, kinds, tot2, tm);
+                if (tot2[1] == 0.0) break;
+            }
+        }
+        if (gt == 0) {
+            a.st->iterations = it;
+            a.st->resid = resErr;
+            a.st->resid0 = initErr;
+        }
+    }
+    return;
+timeout:
+    if (gt == 0) a.st->code = GBFV_ERR_TIMEOUT;
+}
+
+// factorization and one preconditioner application alone (tests)
+template <class T, int B>
+__global__ void __launch_bounds__(GILU_THREADS) kGiluApply(const GiluArgs<T> a)
+{
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
+    const GBar bar{&a.gs};
+    if (!factorAll<T, B>(a, gt, gs, bar)) {
+        if (gt == 0) a.st->code = GBFV_ERR_TIMEOUT;
+        return;
+    }
+    if (*(volatile int*)&a.st->code != 0) return;
+    if (!iluApply<T, B>(a, a.rhs, a.x, gt, gs, bar) && gt == 0) a.st->code = GBFV_ERR_TIMEOUT;
+}
+
+}  // namespace
+
+struct GiluData {
+    int N = 0, b = 0, nslot = 0, ld = 0, numLev = 0, blocks = 1, maxWidth = 0;
+    const int* col = nullptr;  // not owned
+    int* levPtr = nullptr;
+    int* updPtr = nullptr;
+    int* upd = nullptr;
+    double* F64 = nullptr;
+    float* F32 = nullptr;
+    double* vec64 = nullptr;  // x r p v y z
+    float* vec32 = nullptr;
+    double* partial = nullptr;
+    unsigned* bar = nullptr;
+    cudaEvent_t evA = nullptr, evB = nullptr;
+    size_t nnz = 0;
+};
+
+GiluData* giluCreate(int N, int b, int nslot, int ld, const std::vector<int>& colHost, const int* colDev,
+                     const std::vector<int>& levPtr, int* status)
+{
+    GiluData* d = new GiluData();
+    auto fail = [&](int st, const std::string& msg) -> GiluData* {
+        if (!msg.empty()) setLastError("ILU(0): " + msg);
+        if (status) *status = st;
+        giluDestroy(d);
+        return nullptr;
+    };
+    if ((b != 2 && b != 3) || nslot < 1 || nslot > 255 || nslot % 2 == 0) return fail(GBFV_ERR_UNSUPPORTED, "layout");
+    d->N = N;
+    d->b = b;
+    d->nslot = nslot;
+    d->ld = ld;
+    d->col = colDev;
+    d->numLev = (int)levPtr.size() - 1;
+    const int diag = nslot / 2;
+    // layout checks, the level of every row, and the update lists
+    std::vector<int> levOf(N, -1);
+    for (int l = 0; l < d->numLev; ++l) {
+        d->maxWidth = std::max(d->maxWidth, levPtr[l + 1] - levPtr[l]);
+        for (int p = levPtr[l]; p < levPtr[l + 1]; ++p) levOf[p] = l;
+    }
+    auto C = [&](int s, int p) { return colHost[(size_t)s * ld + p]; };
+    std::vector<int> updPtr(N + 1, 0), upd;
+    for (int p = 0; p < N; ++p) {
+        if (levOf[p] < 0 || C(diag, p) != p) return fail(GBFV_ERR_UNSUPPORTED, "diagonal or level missing");
+        for (int s = 0; s < nslot; ++s) {
+            const int k = C(s, p);
+            if (k < 0 || s == diag) continue;
+            if (k >= N || (s < diag) != (levOf[k] < levOf[p]) || levOf[k] == levOf[p])
+                return fail(GBFV_ERR_UNSUPPORTED, "a lower entry outside the earlier levels");
+        }
+        for (int s = 0; s < diag; ++s) {
+            const int k = C(s, p);
+            if (k < 0) continue;
+            for (int u = diag + 1; u < nslot; ++u) {
+                const int j = C(u, k);
+                if (j < 0) continue;
+                for (int t = 0; t < nslot; ++t)
+                    if (C(t, p) == j) {
+                        upd.push_back(s | (t << 8) | (u << 16));
+                        break;
+                    }
+            }
+        }
+        updPtr[p + 1] = (int)upd.size();
+    }
+    for (int s = 0; s < nslot; ++s)
+        for (int p = 0; p < N; ++p) d->nnz += C(s, p) >= 0;
+    auto up = [&](int** dst, const std::vector<int>& v) {
+        if (cudaMalloc((void**)dst, sizeof(int) * std::max<size_t>(1, v.size())) != cudaSuccess) return false;
+        return v.empty() || cudaMemcpy(*dst, v.data(), sizeof(int) * v.size(), cudaMemcpyHostToDevice) == cudaSuccess;
+    };
+    if (!up(&d->levPtr, levPtr) || !up(&d->updPtr, updPtr) || !up(&d->upd, upd)) return fail(GBFV_ERR_OOM, "");
+    // one block when every level fits it (block barriers only), else a
+    // cooperative grid (GBFV_GILU_BLOCKS overrides)
+    int dev = 0, nsm = 1, occ = 1 << 20;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    for (const void* fn : {b == 2 ? (const void*)kGiluBicgstab<double, 2> : (const void*)kGiluBicgstab<double, 3>,
+                           b == 2 ? (const void*)kGiluBicgstab<float, 2> : (const void*)kGiluBicgstab<float, 3>,
+                           b == 2 ? (const void*)kGiluApply<double, 2> : (const void*)kGiluApply<double, 3>}) {
+        int o = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, fn, GILU_THREADS, 0);
+        occ = std::min(occ, o);
+    }
+    const int maxCoop = std::max(1, occ) * nsm;
+    int blocks = N <= 65536 ? 1 : std::min(maxCoop, std::max(1, (N + 4095) / 4096));
+    if (const char* e = getenv("GBFV_GILU_BLOCKS")) blocks = std::max(1, std::min(maxCoop, atoi(e)));
+    d->blocks = blocks;
+    const size_t nv = (size_t)N * b + 16;
+    if (cudaMalloc((void**)&d->partial, sizeof(double) * 4 * (size_t)std::max(blocks, 16)) != cudaSuccess ||
+        cudaMalloc((void**)&d->bar, 4 * sizeof(unsigned)) != cudaSuccess ||
+        cudaMalloc((void**)&d->vec64, sizeof(double) * 6 * nv) != cudaSuccess ||
+        cudaMalloc((void**)&d->F64, sizeof(double) * (size_t)nslot * b * b * ld) != cudaSuccess)
+        return fail(GBFV_ERR_OOM, "");
+    cudaMemset(d->bar, 0, 4 * sizeof(unsigned));
+    cudaEventCreate(&d->evA);
+    cudaEventCreate(&d->evB);
+    if (status) *status = GBFV_OK;
+    return d;
+}
+
+void giluDestroy(GiluData* d)
+{
+    if (!d) return;
+    cudaFree(d->levPtr);
+    cudaFree(d->updPtr);
+    cudaFree(d->upd);
+    cudaFree(d->F64);
+    cudaFree(d->F32);
+    cudaFree(d->vec64);
+    cudaFree(d->vec32);
+    cudaFree(d->partial);
+    cudaFree(d->bar);
+    if (d->evA) cudaEventDestroy(d->evA);
+    if (d->evB) cudaEventDestroy(d->evB);
+    delete d;
+}
+
+namespace {
+
+template <class T>
+int args(GiluData& d, GiluArgs<T>& a, const T* A, const T* rhs, DevStatus* st)
+{
+    const size_t nv = (size_t)d.N * d.b + 16;
+    T* vec;
+    T* F;
+    if (sizeof(T) == 8) {
+        vec = (T*)d.vec64;
+        F = (T*)d.F64;
+    }
+    else {
+        if (!d.vec32 && (cudaMalloc((void**)&d.vec32, sizeof(float) * 6 * nv) != cudaSuccess ||
+                         cudaMalloc((void**)&d.F32, sizeof(float) * (size_t)d.nslot * d.b * d.b * d.ld) != cudaSuccess))
+            return GBFV_ERR_OOM;
+        vec = (T*)d.vec32;
+        F = (T*)d.F32;
+    }
+    a.N = d.N;
+    a.ld = d.ld;
+    a.nslot = d.nslot;
+    a.diag = d.nslot / 2;
+    a.numLev = d.numLev;
+    a.col = d.col;
+    a.levPtr = d.levPtr;
+    a.updPtr = d.updPtr;
+    a.upd = d.upd;
+    a.A = A;
+    a.F = F;
+    a.rhs = rhs;
+    a.x = vec;
+    a.r = vec + nv;
+    a.p = vec + 2 * nv;
+    a.v = vec + 3 * nv;
+    a.y = vec + 4 * nv;
+    a.z = vec + 5 * nv;
+    a.partial = d.partial;
+    a.gs.count = d.bar;
+    a.gs.gen = d.bar + 1;
+    a.gs.abort = (int*)(d.bar + 2);
+    a.gs.perCluster = 0;
+    a.st = st;
+    return GBFV_OK;
+}
+
+template <class T>
+int launch(const void* fn, GiluArgs<T>& a, int blocks, cudaStream_t s)
+{
+    void* argv[] = {(void*)&a};
+    const cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(GILU_THREADS), argv, 0, s);
+    countLaunch();
+    if (e != cudaSuccess) {
+        setLastError(std::string("ILU(0) cooperative launch failed: ") + cudaGetErrorString(e));
+        return GBFV_ERR_CUDA;
+    }
+    return GBFV_OK;
+}
+
+}  // namespace
+
+template <class T>
+int giluSolve(GiluData* d, const T* A, const T* rhs, T* x, int factor, double redTol, double absTol, double maxRes,
+              int maxIter, cudaStream_t s, DevStatus* st, DevStatus* hst, int& iters, float* ms, double* bytes)
+{
+    GiluArgs<T> a;
+    int rs;
+    if ((rs = args<T>(*d, a, A, rhs, st))) return rs;
+    a.factor = factor;
+    a.redTol = redTol;
+    a.absTol = absTol;
+    a.maxRes = maxRes;
+    a.maxIter = maxIter;
+    if (cudaMemsetAsync(st, 0, sizeof(DevStatus), s) != cudaSuccess ||
+        cudaMemsetAsync(d->bar, 0, 4 * sizeof(unsigned), s) != cudaSuccess)
+        return GBFV_ERR_CUDA;
+    cudaEventRecord(d->evA, s);
+    const void* fn = d->b == 2 ? (const void*)kGiluBicgstab<T, 2> : (const void*)kGiluBicgstab<T, 3>;
+    if ((rs = launch<T>(fn, a, d->blocks, s))) return rs;
+    if (cudaMemcpyAsync(x, a.x, sizeof(T) * (size_t)d->N * d->b, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+        return GBFV_ERR_CUDA;
+    cudaEventRecord(d->evB, s);
+    if (cudaMemcpyAsync(hst, st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
+        setLastError(std::string("ILU(0) solve: ") + cudaGetErrorString(cudaGetLastError()));
+        return GBFV_ERR_CUDA;
+    }
+    iters = hst->iterations;
+    if (ms) cudaEventElapsedTime(ms, d->evA, d->evB);
+    if (bytes) {
+        // per iteration: 2 sweeps over the factors (every stored block once
+        // per application) and 2 SpMVs over A, plus the vector updates
+        const double sz = sizeof(T), bb = (double)d->b * d->b, nb = (double)d->N * d->b;
+        const double mat = (double)d->nnz * (bb * sz + 4);
+        *bytes = iters * (4.0 * mat + 30.0 * nb * sz) + (factor ? 3.0 * mat : 0.0);
+    }
+    if (hst->code) return hst->code;
+    return hst->converged ? GBFV_OK : GBFV_ERR_NOT_CONVERGED;
+}
+
+int giluApply64(GiluData* d, const double* A, const double* dv, double* v, cudaStream_t s, DevStatus* st,
+                DevStatus* hst)
+{
+    GiluArgs<double> a;
+    int rs;
+    if ((rs = args<double>(*d, a, A, dv, st))) return rs;
+    a.factor = 1;
+    if (cudaMemsetAsync(st, 0, sizeof(DevStatus), s) != cudaSuccess ||
+        cudaMemsetAsync(d->bar, 0, 4 * sizeof(unsigned), s) != cudaSuccess)
+        return GBFV_ERR_CUDA;
+    const void* fn = d->b == 2 ? (const void*)kGiluApply<double, 2> : (const void*)kGiluApply<double, 3>;
+    if ((rs = launch<double>(fn, a, d->blocks, s))) return rs;
+    if (cudaMemcpyAsync(v, a.x, sizeof(double) * (size_t)d->N * d->b, cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(hst, st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return GBFV_ERR_CUDA;
+    return hst->code;
+}
+
+template int giluSolve<double>(GiluData*, const double*, const double*, double*, int, double, double, double, int,
+                               cudaStream_t, DevStatus*, DevStatus*, int&, float*, double*);
+template int giluSolve<float>(GiluData*, const float*, const float*, float*, int, double, double, double, int,
+                              cudaStream_t, DevStatus*, DevStatus*, int&, float*, double*);
+
+}  // namespace gbfv

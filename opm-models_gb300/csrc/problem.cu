@@ -63,15 +63,37 @@ int checkProblem(const gbfv_problem* P, int maxMaterials, int maxTable)
         setLastError("grid larger than GBFV_MAX_CELLS (32-bit device indexing)");
         return GBFV_ERR_UNSUPPORTED;
     }
-    if (!P->center || !P->volume || !P->porosity || !P->perm || !P->material || !P->conn_ptr || !P->conn_nbr ||
-        !P->conn_normal || !P->conn_center || !P->conn_area || !P->bface_ptr)
+    if (P->num_elements < 0) return fail("negative num_elements");
+    const bool vcfv = P->num_elements > 0;  // vertex-centred: the cells are the grid's vertices
+    if (!P->center || !P->porosity || !P->perm || !P->material || !P->bface_ptr)
+        return fail("incomplete (a required array is NULL)");
+    if (!vcfv && (!P->volume || !P->conn_ptr || !P->conn_nbr || !P->conn_normal || !P->conn_center || !P->conn_area))
         return fail("incomplete (a required array is NULL)");
     if (P->flux_module != GBFV_FLUX_DARCY && P->flux_module != GBFV_FLUX_TRANS) return fail("unknown flux module");
-    // intersections: grouped per cell, the groups covering [0, count)
-    if (P->num_conn < 0 || !offsetsOk(P->conn_ptr, N, P->num_conn))
-        return fail("conn_ptr must start at 0, not decrease and end at num_conn");
-    if (P->num_bfaces < 0 || !offsetsOk(P->bface_ptr, N, P->num_bfaces))
-        return fail("bface_ptr must start at 0, not decrease and end at num_bfaces");
+    if (vcfv) {
+        // elements: four corner vertices each; boundary faces grouped per
+        // element, each on one of its element's corners
+        if (P->num_conn != 0) return fail("a vertex-centred grid has no cell intersections (num_conn 0)");
+        if (!P->elem_corner) return fail("elem_corner is NULL");
+        for (int64_t k = 0; k < 4 * (int64_t)P->num_elements; ++k)
+            if (P->elem_corner[k] < 0 || P->elem_corner[k] >= N)
+                return fail("corner vertex out of range at element " + std::to_string(k / 4));
+        if (P->num_bfaces < 0 || !offsetsOk(P->bface_ptr, P->num_elements, P->num_bfaces))
+            return fail("bface_ptr must start at 0, not decrease and end at num_bfaces");
+        if (P->num_bfaces > 0 && (!P->bface_corner || !P->bface_center || !P->bface_area))
+            return fail("boundary faces need bface_corner, bface_center and bface_area");
+        for (int f = 0; f < P->num_bfaces; ++f)
+            if (P->bface_corner[f] < 0 || P->bface_corner[f] > 3)
+                return fail("boundary face corner outside [0, 3] at face " + std::to_string(f));
+        if (P->p1_gradients != 0 && P->p1_gradients != 1) return fail("p1_gradients must be 0 or 1");
+    }
+    else {
+        // intersections: grouped per cell, the groups covering [0, count)
+        if (P->num_conn < 0 || !offsetsOk(P->conn_ptr, N, P->num_conn))
+            return fail("conn_ptr must start at 0, not decrease and end at num_conn");
+        if (P->num_bfaces < 0 || !offsetsOk(P->bface_ptr, N, P->num_bfaces))
+            return fail("bface_ptr must start at 0, not decrease and end at num_bfaces");
+    }
     if (P->num_bfaces > 0 && !P->bface_normal) return fail("bface_normal is NULL");
     bool active = false;  // any boundary face other than no-flow
     if (P->bface_type)

@@ -1,0 +1,663 @@
+// Vertex-centred finite volumes (VcfvDiscretization) on the device: the
+// stencil geometry of 2D axis-aligned quadrilaterals and the AD
+// linearization of the immiscible model on it.
+//
+// Reference: VcfvStencil (vcfvstencil.hh:466-1015: corners, edge centres,
+// sub-control volumes as quadrilaterals, one sub-control-volume face per
+// edge from the edge centre to the element centre, boundary faces half an
+// intersection each), P1FeGradientCalculator (p1fegradientcalculator.hh:
+// 83-290) and FvBaseGradientCalculator (fvbasegradientcalculator.hh:
+// 200-318), the Darcy module (darcyfluxmodule.hh:183-525), the local
+// residual (fvbaselocalresidual.hh:158-191, 299-348, 419-626) and
+// FvBaseAdLocalLinearizer with one focus per element corner
+// (fvbaseadlocallinearizer.hh:173-292), scattered by FvBaseLinearizer::
+// linearizeElement_ (fvbaselinearizer.hh:595-626).
+//
+// GPU shape: the element pass runs one thread per (element, focus corner):
+// it evaluates the element's four corner residuals with the derivatives of
+// the focus corner's primary variables and writes them to a scratch buffer.
+// The gather pass runs one thread per vertex: it adds its (at most four)
+// elements' contributions in element order -- the reference's summation
+// order -- into the residual row and the nine Jacobian blocks of the row.
+// No atomics; the result does not depend on scheduling.  The geometry the
+// element pass needs (sub-control volumes, face normals and areas, P1
+// gradients at the integration points, mean permeabilities, gravity terms)
+// is computed once on the host in the reference's operation order.
+//
+// The intensive quantities of the immiscible model have constant densities,
+// so a corner's density carries no derivatives; every quantity of a corner
+// other than the focus one enters with its value only.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <type_traits>
+#include <utility>
+#include <vector>
+
+#include "../../include/gbfv.h"
+#include "gbfv_internal.cuh"
+#include "vcfv.cuh"
+
+namespace gbfv {
+
+void setLastError(const std::string& s);
+
+namespace {
+
+using D2 = Dual<2>;
+
+// corners of each edge of the 2D cube (dune-geometry numbering: corner c at
+// ((c & 1), (c >> 1) & 1)), the edges' local centres, and the boundary
+// intersections' corners
+const int EDGE_CORNER[4][2] = {{0, 2}, {1, 3}, {0, 1}, {2, 3}};
+const double EDGE_LOCAL[4][2] = {{0.0, 0.5}, {1.0, 0.5}, {0.5, 0.0}, {0.5, 1.0}};
+// sub-control-volume face k separates corner FI[k] (interior) and FJ[k]
+// (exterior): the edge's corners with corner 2 moved to the interior side
+// (vcfvstencil.hh:904-907)
+__constant__ int FI[4] = {2, 1, 0, 3};
+__constant__ int FJ[4] = {0, 3, 1, 2};
+
+struct ElemGeo {
+    int v[4];              // internal row of each corner
+    double scvVol[4];
+    double fa[4];          // face areas
+    double fn[4][2];       // unit normals, interior to exterior
+    double Kh[4][2];       // entry-wise harmonic mean of the two corners' K
+    double dTot[4][2];     // x_j - x_i
+    double absTot2[4];     // |x_j - x_i|^2
+    double gIn[4], gEx[4]; // g . (x_i - x_ip), g . (x_j - x_ip)
+    double w2p[4][2];      // two-point gradient weights (x_j - x_i) / |x_j - x_i|^2
+    double grad[4][4][2];  // P1: gradient of corner c's shape function at face k
+};
+
+struct BFaceV {
+    int c, type;
+    double area;
+    double n[2];
+    double w[2];           // (x_ip - x_scv) / |x_ip - x_scv|^2, the boundary gradient's weights
+    double dIn[2];         // x_vertex - x_ip
+    double gTimesDist, absDist2;
+    double K[2];           // the vertex's permeability
+    double pb[2], mobb[2], rhob[2];  // free-flow state
+    double rate[2];        // mass rate
+};
+
+struct VcfvArgs {
+    int E, ld;
+    const ElemGeo* geo;
+    const int* bfPtr;
+    const BFaceV* bf;
+    const int* inc;        // [k*ld + p] element*4 + corner of vertex p's k-th element, -1 none
+    const unsigned char* incSlot;  // [(k*4 + f)*ld + p] slot of the element's corner f in row p
+    double* R;             // [(e*4 + f)*2 + a] residual of corner f (focus f)
+    double* J;             // [((e*4 + f)*4 + j)*4 + a*2 + pv] d res_j,a / d x_f,pv
+    int p1;
+};
+
+double harmonicMeanV(double x, double y)
+{
+    if (x * y <= 0) return 0.0;
+    return (2 * x * y) / (x + y);
+}
+
+double quadArea(const double* p0, const double* p1, const double* p2, const double* p3)
+{
+    return 0.5 * std::abs((p3[0] - p1[0]) * (p2[1] - p0[1]) - (p3[1] - p1[1]) * (p2[0] - p0[0]));
+}
+
+// the geometry of one element (VcfvStencil::update, vcfvstencil.hh:864-
+// 1015), natural vertex indices; AxisAlignedCubeGeometry::global(x) =
+// lower + x .* (upper - lower)
+struct HostElem {
+    double lower[2], upper[2];
+    double vpos[4][2], scvVol[4], scvCenter[4][2];
+    int fi[4], fj[4];
+    double fn[4][2], fa[4], fip[4][2], grad[4][4][2];
+};
+
+HostElem hostElem(const gbfv_problem* P, const int* corner)
+{
+    HostElem E;
+    for (int d = 0; d < 2; ++d) {
+        E.lower[d] = P->center[3 * corner[0] + d];
+        E.upper[d] = P->center[3 * corner[3] + d];
+    }
+    auto global = [&](const double* l, double* x) {
+        for (int d = 0; d < 2; ++d) x[d] = E.lower[d] + l[d] * (E.upper[d] - E.lower[d]);
+    };
+    const double elemLocal[2] = {0.5, 0.5};
+    double elemGlobal[2], edgeCoord[4][2];
+    global(elemLocal, elemGlobal);
+    for (int c = 0; c < 4; ++c) {
+        const double l[2] = {double(c & 1), double((c >> 1) & 1)};
+        global(l, E.vpos[c]);
+    }
+    for (int k = 0; k < 4; ++k) global(EDGE_LOCAL[k], edgeCoord[k]);
+    E.scvVol[0] = quadArea(E.vpos[0], edgeCoord[2], elemGlobal, edgeCoord[0]);
+    E.scvVol[1] = quadArea(E.vpos[1], edgeCoord[1], elemGlobal, edgeCoord[2]);
+    E.scvVol[2] = quadArea(E.vpos[2], edgeCoord[0], elemGlobal, edgeCoord[3]);
+    E.scvVol[3] = quadArea(E.vpos[3], edgeCoord[3], elemGlobal, edgeCoord[1]);
+    // sub-control-volume centres: the mean of the local corners
+    for (int c = 0; c < 4; ++c) {
+        const double x0 = (c & 1) ? 0.5 : 0.0, y0 = ((c >> 1) & 1) ? 0.5 : 0.0;
+        const double loc[4][2] = {{x0, y0}, {x0 + 0.5, y0}, {x0, y0 + 0.5}, {x0 + 0.5, y0 + 0.5}};
+        double ctr[2] = {0.0, 0.0};
+        for (int q = 0; q < 4; ++q)
+            for (int d = 0; d < 2; ++d) ctr[d] += loc[q][d];
+        for (int d = 0; d < 2; ++d) ctr[d] /= 4;
+        global(ctr, E.scvCenter[c]);
+    }
+    const double jInv[2] = {1.0 / (E.upper[0] - E.lower[0]), 1.0 / (E.upper[1] - E.lower[1])};
+    for (int k = 0; k < 4; ++k) {
+        int i = EDGE_CORNER[k][0], j = EDGE_CORNER[k][1];
+        if (i == 2 || j == 2) std::swap(i, j);
+        E.fi[k] = i;
+        E.fj[k] = j;
+        const double ipLocal[2] = {(EDGE_LOCAL[k][0] + elemLocal[0]) * 0.5, (EDGE_LOCAL[k][1] + elemLocal[1]) * 0.5};
+        double diff[2] = {elemGlobal[0] - edgeCoord[k][0], elemGlobal[1] - edgeCoord[k][1]};
+        double n[2] = {diff[1], -diff[0]};
+        for (int d = 0; d < 2; ++d) diff[d] = E.vpos[j][d] - E.vpos[i][d];
+        if (n[0] * diff[0] + n[1] * diff[1] < 0) {
+            n[0] *= -1;
+            n[1] *= -1;
+        }
+        const double area = std::sqrt(n[0] * n[0] + n[1] * n[1]);
+        E.fa[k] = area;
+        E.fn[k][0] = n[0] / area;
+        E.fn[k][1] = n[1] / area;
+        global(ipLocal, E.fip[k]);
+        for (int c = 0; c < 4; ++c) {
+            const bool bx = c & 1, by = (c >> 1) & 1;
+            const double gx = (bx ? 1.0 : -1.0) * (by ? ipLocal[1] : 1.0 - ipLocal[1]);
+            const double gy = (bx ? ipLocal[0] : 1.0 - ipLocal[0]) * (by ? 1.0 : -1.0);
+            E.grad[k][c][0] = jInv[0] * gx;
+            E.grad[k][c][1] = jInv[1] * gy;
+        }
+    }
+    return E;
+}
+
+int slotOf(const double* a, const double* b)
+{
+    const int dx = b[0] > a[0] ? 1 : (b[0] < a[0] ? -1 : 0);
+    const int dy = b[1] > a[1] ? 1 : (b[1] < a[1] ? -1 : 0);
+    return (dy + 1) * 3 + (dx + 1);
+}
+
+// ---------------------------------------------------------------- kernels --
+// Element pass: thread (e, f) evaluates FvBaseLocalResidual::eval of element
+// e with the derivatives of corner f (fvbaselocalresidual.hh:158-191).
+template <bool P1>
+__global__ void __launch_bounds__(128) kVcfvElement(VcfvArgs a, DevMesh m, IqBuffers iq,
+                                                    const double* __restrict__ storageOld, int iter0, double dt)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.E * 4) return;
+    const int e = t >> 2, f = t & 3;
+    const ElemGeo& G = a.geo[e];
+    const int ld = m.ldN;
+    int v[4];
+    double cv[4][6];  // p0 p1 rho0 rho1 lam0 lam1 of each corner
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        v[c] = G.v[c];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) cv[c][k] = iq.val[k * ld + v[c]];
+    }
+    double fd[6][2];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        fd[k][0] = iq.der[(k * 2 + 0) * ld + v[f]];
+        fd[k][1] = iq.der[(k * 2 + 1) * ld + v[f]];
+    }
+    auto Q = [&](int c, int k) {
+        D2 r(cv[c][k]);
+        if (c == f) {
+            r.d[0] = fd[k][0];
+            r.d[1] = fd[k][1];
+        }
+        return r;
+    };
+    D2 res[4][2];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) res[c][0] = res[c][1] = D2(0.0);
+    // evalFluxes: the four sub-control-volume faces
+#pragma unroll 1
+    for (int k = 0; k < 4; ++k) {
+        const int i = FI[k], j = FJ[k];
+        D2 pg[2][2];
+#pragma unroll
+        for (int ph = 0; ph < 2; ++ph) {
+            if (P1) {
+                pg[ph][0] = D2(0.0);
+                pg[ph][1] = D2(0.0);
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    const D2 dv = Q(c, ph);
+                    pg[ph][0] = pg[ph][0] + dv * G.grad[k][c][0];
+                    pg[ph][1] = pg[ph][1] + dv * G.grad[k][c][1];
+                }
+            }
+            else {
+                const D2 deltay = Q(j, ph) - Q(i, ph);
+                pg[ph][0] = deltay * G.w2p[k][0];
+                pg[ph][1] = deltay * G.w2p[k][1];
+            }
+            // gravity correction (darcyfluxmodule.hh:214-283)
+            const D2 pStatIn = -(Q(i, 2 + ph) * G.gIn[k]);
+            const D2 pStatEx = -(Q(j, 2 + ph) * G.gEx[k]);
+            const D2 fs = (pStatEx - pStatIn) / G.absTot2[k];
+            pg[ph][0] = pg[ph][0] + G.dTot[k][0] * fs;
+            pg[ph][1] = pg[ph][1] + G.dTot[k][1] * fs;
+        }
+        D2 flux[2];
+#pragma unroll
+        for (int ph = 0; ph < 2; ++ph) {
+            D2 tmp(0.0);
+            tmp = tmp + pg[ph][0] * G.fn[k][0];
+            tmp = tmp + pg[ph][1] * G.fn[k][1];
+            const int up = tmp.v > 0 ? j : i;
+            const D2 mob = Q(up, 4 + ph);
+            D2 vf(0.0);
+#pragma unroll
+            for (int d = 0; d < 2; ++d) {
+                D2 fv = G.Kh[k][d] * pg[ph][d];
+                fv = fv * (-mob);
+                vf = vf + fv * G.fn[k][d];
+            }
+            flux[ph] = D2(0.0) + vf * Q(up, 2 + ph);
+            flux[ph] = flux[ph] * (1.0 * G.fa[k]);
+        }
+#pragma unroll
+        for (int ph = 0; ph < 2; ++ph) {
+            res[i][ph] = res[i][ph] + flux[ph];
+            res[j][ph] = res[j][ph] - flux[ph];
+        }
+    }
+    // evalVolumeTerms_: storage of the four sub-control volumes
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const double scvVolume = G.scvVol[c] * 1.0;
+#pragma unroll
+        for (int ph = 0; ph < 2; ++ph) {
+            D2 tmp(iq.sto[(ph * 3 + 0) * ld + v[c]]);
+            if (c == f) {
+                tmp.d[0] = iq.sto[(ph * 3 + 1) * ld + v[c]];
+                tmp.d[1] = iq.sto[(ph * 3 + 2) * ld + v[c]];
+            }
+            const double tmp2 = iter0 ? tmp.v : storageOld[ph * ld + v[c]];
+            tmp = tmp - tmp2;
+            tmp = tmp * (scvVolume / dt);
+            res[c][ph] = res[c][ph] + tmp;
+            res[c][ph] = res[c][ph] - 0.0 * scvVolume;
+        }
+    }
+    // evalBoundary_: this element's boundary sub-control-volume faces
+    for (int b = a.bfPtr[e]; b < a.bfPtr[e + 1]; ++b) {
+        const BFaceV B = a.bf[b];
+        D2 values[2] = {D2(0.0), D2(0.0)};
+        if (B.type == GBFV_BC_MASSRATE) {
+            values[0] = D2(B.rate[0]);
+            values[1] = D2(B.rate[1]);
+        }
+        else if (B.type == GBFV_BC_FREEFLOW) {
+#pragma unroll
+            for (int ph = 0; ph < 2; ++ph) {
+                const D2 pIn = Q(B.c, ph);
+                const D2 deltay = D2(B.pb[ph]) - pIn;
+                D2 pg[2];
+                pg[0] = deltay * B.w[0];
+                pg[1] = deltay * B.w[1];
+                const D2 pStatIn = (-B.gTimesDist) * Q(B.c, 2 + ph);
+                const D2 fsc = pStatIn / B.absDist2;
+                pg[0] = pg[0] + B.dIn[0] * fsc;
+                pg[1] = pg[1] + B.dIn[1] * fsc;
+                D2 tmp(0.0);
+                tmp = tmp + pg[0] * B.n[0];
+                tmp = tmp + pg[1] * B.n[1];
+                const D2 mob = tmp.v > 0.0 ? D2(B.mobb[ph]) : Q(B.c, 4 + ph);
+                D2 vf(0.0);
+#pragma unroll
+                for (int d = 0; d < 2; ++d) {
+                    D2 fv = B.K[d] * pg[d];
+                    fv = fv * (-mob);
+                    vf = vf + fv * B.n[d];
+                }
+                const D2 dens = B.pb[ph] > pIn.v ? D2(B.rhob[ph]) : Q(B.c, 2 + ph);
+                values[ph] = values[ph] + vf * dens;
+            }
+        }
+        const double aa = B.area * 1.0;
+#pragma unroll
+        for (int ph = 0; ph < 2; ++ph) res[B.c][ph] = res[B.c][ph] + values[ph] * aa;
+    }
+    // volumetric residual, then the scratch records
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const double V = m.volume[v[c]];
+        res[c][0] = res[c][0] / V;
+        res[c][1] = res[c][1] / V;
+    }
+    const size_t ef = (size_t)e * 4 + f;
+    a.R[ef * 2 + 0] = res[f][0].v;
+    a.R[ef * 2 + 1] = res[f][1].v;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int ph = 0; ph < 2; ++ph)
+#pragma unroll
+            for (int pv = 0; pv < 2; ++pv) a.J[(ef * 4 + j) * 4 + ph * 2 + pv] = res[j][ph].d[pv];
+}
+
+// Gather pass: vertex p's residual and Jacobian row, its elements' records
+// added in element order (residual_[globI] += ..., addToBlock(globJ, globI,
+// ...), fvbaselinearizer.hh:609-621); the storage cache at iteration 0.
+__global__ void __launch_bounds__(128) kVcfvGather(VcfvArgs a, DevMesh m, IqBuffers iq, double* __restrict__ storageOld,
+                                                   int iter0, double* __restrict__ residual, double* __restrict__ jval)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= m.N) return;
+    const int ld = m.ldN;
+    double r[2] = {0.0, 0.0};
+    double Jb[VCFV_SLOTS][4];
+#pragma unroll
+    for (int s = 0; s < VCFV_SLOTS; ++s)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) Jb[s][q] = 0.0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int ec = a.inc[k * ld + p];
+        if (ec < 0) break;
+        const size_t e = ec >> 2;
+        const int c = ec & 3;
+        r[0] += a.R[(e * 4 + c) * 2 + 0];
+        r[1] += a.R[(e * 4 + c) * 2 + 1];
+#pragma unroll
+        for (int f = 0; f < 4; ++f) {
+            const int s = a.incSlot[(k * 4 + f) * ld + p];
+            const double* src = &a.J[((e * 4 + f) * 4 + c) * 4];
+#pragma unroll
+            for (int sl = 0; sl < VCFV_SLOTS; ++sl)
+                if (sl == s)
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) Jb[sl][q] += src[q];
+        }
+    }
+    residual[2 * p + 0] = r[0];
+    residual[2 * p + 1] = r[1];
+#pragma unroll
+    for (int s = 0; s < VCFV_SLOTS; ++s)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) jval[((size_t)s * 4 + q) * ld + p] = Jb[s][q];
+    if (iter0) {
+        storageOld[0 * ld + p] = iq.sto[(0 * 3 + 0) * ld + p];
+        storageOld[1 * ld + p] = iq.sto[(1 * 3 + 0) * ld + p];
+    }
+}
+
+}  // namespace
+
+struct VcfvDev {
+    int E = 0, N = 0, ld = 0, p1 = 1, nbf = 0;
+    ElemGeo* geo = nullptr;
+    int* bfPtr = nullptr;
+    BFaceV* bf = nullptr;
+    int* inc = nullptr;
+    unsigned char* incSlot = nullptr;
+    double* R = nullptr;
+    double* J = nullptr;
+};
+
+int vcfvSetup(const gbfv_problem* P, VcfvSetup& s)
+{
+    auto fail = [](const std::string& w, int code) {
+        setLastError("vertex-centred grid: " + w);
+        return code;
+    };
+    if (P->model != GBFV_MODEL_IMMISCIBLE_2P) return fail("the immiscible model only", GBFV_ERR_UNSUPPORTED);
+    if (P->flux_module != GBFV_FLUX_DARCY) return fail("the Darcy flux module only", GBFV_ERR_UNSUPPORTED);
+    const int N = P->num_cells, E = P->num_elements;
+    for (int i = 0; P->constraint && i < N; ++i)
+        if (P->constraint[i] >= 0) return fail("constraints are not supported", GBFV_ERR_UNSUPPORTED);
+    for (int i = 0; i < N; ++i)
+        if (P->center[3 * i + 2] != 0.0) return fail("2D grids only (vertex z = 0)", GBFV_ERR_UNSUPPORTED);
+    s.N = N;
+    s.E = E;
+    s.totalVolume.assign(N, 0.0);
+    s.nbr.assign((size_t)N * VCFV_SLOTS, -1);
+    std::vector<char> used(N, 0);
+    for (int e = 0; e < E; ++e) {
+        const int* cn = &P->elem_corner[4 * e];
+        const double* x0 = &P->center[3 * cn[0]];
+        const double* x3 = &P->center[3 * cn[3]];
+        const double* x1 = &P->center[3 * cn[1]];
+        const double* x2 = &P->center[3 * cn[2]];
+        if (!(x3[0] > x0[0] && x3[1] > x0[1]) || x1[0] != x3[0] || x1[1] != x0[1] || x2[0] != x0[0] ||
+            x2[1] != x3[1])
+            return fail("element " + std::to_string(e) + " is not an axis-aligned box in corner order",
+                        GBFV_ERR_UNSUPPORTED);
+        const HostElem H = hostElem(P, cn);
+        for (int c = 0; c < 4; ++c) {
+            s.totalVolume[cn[c]] += H.scvVol[c];
+            used[cn[c]] = 1;
+        }
+        for (int a = 0; a < 4; ++a)
+            for (int c = 0; c < 4; ++c) {
+                const int sl = slotOf(&P->center[3 * cn[a]], &P->center[3 * cn[c]]);
+                int& q = s.nbr[(size_t)cn[a] * VCFV_SLOTS + sl];
+                if (q >= 0 && q != cn[c])
+                    return fail("two vertices in one neighbour direction of vertex " + std::to_string(cn[a]),
+                                GBFV_ERR_UNSUPPORTED);
+                q = cn[c];
+            }
+    }
+    for (int i = 0; i < N; ++i) {
+        if (!used[i]) return fail("vertex " + std::to_string(i) + " belongs to no element", GBFV_ERR_ARG);
+        int prev = -1;
+        for (int sl = 0; sl < VCFV_SLOTS; ++sl) {
+            const int q = s.nbr[(size_t)i * VCFV_SLOTS + sl];
+            if (q < 0) continue;
+            if (q <= prev)
+                return fail("vertex numbering is not the grid's natural order (x fastest)", GBFV_ERR_UNSUPPORTED);
+            prev = q;
+        }
+    }
+    return GBFV_OK;
+}
+
+VcfvDev* vcfvUpload(const gbfv_problem* P, const VcfvSetup& s, const DevPhysics& ph, const std::vector<int>& perm,
+                    int ld, int* status)
+{
+    VcfvDev* d = new VcfvDev();
+    auto fail = [&](int st) -> VcfvDev* {
+        if (status) *status = st;
+        vcfvDestroy(d);
+        return nullptr;
+    };
+    const int N = s.N, E = s.E;
+    d->E = E;
+    d->N = N;
+    d->ld = ld;
+    d->p1 = P->p1_gradients ? 1 : 0;
+    std::vector<ElemGeo> geo(E);
+    std::vector<int> bfPtr(E + 1, 0);
+    std::vector<BFaceV> bf;
+    const double* g = P->gravity;
+    for (int e = 0; e < E; ++e) {
+        const int* cn = &P->elem_corner[4 * e];
+        const HostElem H = hostElem(P, cn);
+        ElemGeo& G = geo[e];
+        std::memset(&G, 0, sizeof(G));
+        for (int c = 0; c < 4; ++c) {
+            G.v[c] = perm[cn[c]];
+            G.scvVol[c] = H.scvVol[c];
+        }
+        for (int k = 0; k < 4; ++k) {
+            const int i = H.fi[k], j = H.fj[k];
+            if (i != (k == 0 ? 2 : k == 1 ? 1 : k == 2 ? 0 : 3) || j != (k == 0 ? 0 : k == 1 ? 3 : k == 2 ? 1 : 2)) {
+                setLastError("vertex-centred grid: face corner table mismatch");
+                return fail(GBFV_ERR_UNSUPPORTED);
+            }
+            G.fa[k] = H.fa[k];
+            double distSq = 0.0;
+            for (int dd = 0; dd < 2; ++dd) {
+                G.fn[k][dd] = H.fn[k][dd];
+                G.Kh[k][dd] = harmonicMeanV(P->perm[3 * cn[i] + dd], P->perm[3 * cn[j] + dd]);
+                const double t = H.vpos[j][dd] - H.vpos[i][dd];
+                distSq += t * t;
+            }
+            double dIn[2], dEx[2];
+            for (int dd = 0; dd < 2; ++dd) {
+                dIn[dd] = H.vpos[i][dd] - H.fip[k][dd];
+                dEx[dd] = H.vpos[j][dd] - H.fip[k][dd];
+                G.dTot[k][dd] = H.vpos[j][dd] - H.vpos[i][dd];
+            }
+            G.absTot2[k] = G.dTot[k][0] * G.dTot[k][0] + G.dTot[k][1] * G.dTot[k][1];
+            double gIn = 0.0, gEx = 0.0;
+            for (int dd = 0; dd < 2; ++dd) gIn += g[dd] * dIn[dd];
+            for (int dd = 0; dd < 2; ++dd) gEx += g[dd] * dEx[dd];
+            G.gIn[k] = gIn;
+            G.gEx[k] = gEx;
+            for (int dd = 0; dd < 2; ++dd) G.w2p[k][dd] = (H.vpos[j][dd] - H.vpos[i][dd]) / distSq;
+            for (int c = 0; c < 4; ++c)
+                for (int dd = 0; dd < 2; ++dd) G.grad[k][c][dd] = H.grad[k][c][dd];
+        }
+        // boundary sub-control-volume faces, the free-flow states on the host
+        for (int b = P->bface_ptr[e]; b < P->bface_ptr[e + 1]; ++b) {
+            BFaceV B;
+            std::memset(&B, 0, sizeof(B));
+            const int c = P->bface_corner[b];
+            const int vn = cn[c];
+            B.c = c;
+            B.type = P->bface_type ? P->bface_type[b] : GBFV_BC_NOFLOW;
+            B.area = P->bface_area[b];
+            const double* xf = &P->bface_center[3 * b];
+            const double* xc = H.scvCenter[c];
+            double distSq = 0.0;
+            for (int dd = 0; dd < 2; ++dd) {
+                const double t = xf[dd] - xc[dd];
+                distSq += t * t;
+            }
+            for (int dd = 0; dd < 2; ++dd) {
+                B.n[dd] = P->bface_normal[3 * b + dd];
+                B.w[dd] = (xf[dd] - xc[dd]) / distSq;
+                B.dIn[dd] = H.vpos[c][dd] - xf[dd];
+                B.K[dd] = P->perm[3 * vn + dd];
+            }
+            double absDist2 = 0.0, gTimesDist = 0.0;
+            for (int dd = 0; dd < 2; ++dd) absDist2 += B.dIn[dd] * B.dIn[dd];
+            for (int dd = 0; dd < 2; ++dd) gTimesDist += g[dd] * B.dIn[dd];
+            B.absDist2 = absDist2;
+            B.gTimesDist = gTimesDist;
+            const double* val = &P->bface_value[4 * b];
+            if (B.type == GBFV_BC_MASSRATE) {
+                B.rate[0] = val[0];
+                B.rate[1] = val[1];
+            }
+            else if (B.type == GBFV_BC_FREEFLOW) {
+                const TwoPhaseLaw& L = ph.law[P->material[vn]];
+                const double pw = val[0], Swb = val[1];
+                const double sumRes = L.Swr + L.Snr;
+                const double SwE = (Swb - L.Swr) / (1.0 - sumRes);
+                const double SnE = ((1 - Swb) - L.Snr) / (1.0 - sumRes);
+                const double pcn = pcnw(L, SwE);
+                B.pb[0] = pw;
+                B.pb[1] = pw + pcn - 0.0;
+                const double krb[2] = {krw(L, SwE), krn(L, 1.0 - SnE)};
+                for (int a = 0; a < 2; ++a) {
+                    B.mobb[a] = krb[a] / P->mu[a];
+                    B.rhob[a] = P->rho[a];
+                }
+            }
+            else if (B.type != GBFV_BC_NOFLOW) {
+                setLastError("vertex-centred grid: unknown boundary type");
+                return fail(GBFV_ERR_ARG);
+            }
+            bf.push_back(B);
+        }
+        bfPtr[e + 1] = (int)bf.size();
+    }
+    // vertex -> (element, corner) in element order, and the slot of each of
+    // the element's corners in the vertex's row
+    std::vector<int> inc((size_t)4 * ld, -1);
+    std::vector<unsigned char> incSlot((size_t)16 * ld, 0);
+    std::vector<int> cnt(N, 0);
+    for (int e = 0; e < E; ++e) {
+        const int* cn = &P->elem_corner[4 * e];
+        for (int c = 0; c < 4; ++c) {
+            const int vn = cn[c], p = perm[vn];
+            const int k = cnt[vn]++;
+            if (k >= 4) {
+                setLastError("vertex-centred grid: a vertex in more than four elements");
+                return fail(GBFV_ERR_UNSUPPORTED);
+            }
+            inc[(size_t)k * ld + p] = e * 4 + c;
+            for (int f = 0; f < 4; ++f)
+                incSlot[((size_t)k * 4 + f) * ld + p] =
+                    (unsigned char)slotOf(&P->center[3 * vn], &P->center[3 * cn[f]]);
+        }
+    }
+    auto upload = [&](auto** dst, const auto& vec) -> bool {
+        using T = typename std::decay<decltype(vec)>::type::value_type;
+        const size_t bytes = sizeof(T) * std::max<size_t>(1, vec.size());
+        if (cudaMalloc((void**)dst, bytes) != cudaSuccess) return false;
+        return vec.empty() || cudaMemcpy(*dst, vec.data(), sizeof(T) * vec.size(), cudaMemcpyHostToDevice) == cudaSuccess;
+    };
+    if (!upload(&d->geo, geo) || !upload(&d->bfPtr, bfPtr) || !upload(&d->bf, bf) || !upload(&d->inc, inc) ||
+        !upload(&d->incSlot, incSlot))
+        return fail(GBFV_ERR_OOM);
+    d->nbf = (int)bf.size();
+    if (cudaMalloc((void**)&d->R, sizeof(double) * (size_t)E * 8) != cudaSuccess ||
+        cudaMalloc((void**)&d->J, sizeof(double) * (size_t)E * 64) != cudaSuccess)
+        return fail(GBFV_ERR_OOM);
+    if (status) *status = GBFV_OK;
+    return d;
+}
+
+void vcfvDestroy(VcfvDev* d)
+{
+    if (!d) return;
+    cudaFree(d->geo);
+    cudaFree(d->bfPtr);
+    cudaFree(d->bf);
+    cudaFree(d->inc);
+    cudaFree(d->incSlot);
+    cudaFree(d->R);
+    cudaFree(d->J);
+    delete d;
+}
+
+double vcfvLinearizeBytes(const VcfvDev* d)
+{
+    // element pass: geometry, 4 corners' values, the focus derivatives and
+    // storage, the scratch records; gather: incidence, scratch, the row
+    const double E = d->E, N = d->N;
+    const double elem = E * 4 * (sizeof(ElemGeo) / 4.0 + 4 * 6 * 8 + 12 * 8 + 4 * 6 * 8 + 72 * 8 / 4.0);
+    const double bnd = (double)d->nbf * sizeof(BFaceV) * 4;
+    const double gather = N * (4 * 4 + 16 + 4 * (8 * 2 + 4 * 32) + VCFV_SLOTS * 32 + 16);
+    return elem + bnd + gather;
+}
+
+void launchVcfvAssemble(const VcfvDev* d, const DevMesh& m, IqBuffers iq, double* storageOld, int iter0, double dt,
+                        double* residual, double* jval, cudaStream_t s)
+{
+    VcfvArgs a;
+    a.E = d->E;
+    a.ld = d->ld;
+    a.geo = d->geo;
+    a.bfPtr = d->bfPtr;
+    a.bf = d->bf;
+    a.inc = d->inc;
+    a.incSlot = d->incSlot;
+    a.R = d->R;
+    a.J = d->J;
+    a.p1 = d->p1;
+    const int nt = 4 * d->E;
+    if (d->p1) kVcfvElement<true><<<(nt + 127) / 128, 128, 0, s>>>(a, m, iq, storageOld, iter0, dt);
+    else kVcfvElement<false><<<(nt + 127) / 128, 128, 0, s>>>(a, m, iq, storageOld, iter0, dt);
+    kVcfvGather<<<(m.N + 127) / 128, 128, 0, s>>>(a, m, iq, storageOld, iter0, residual, jval);
+    countLaunch(2);
+}
+
+}  // namespace gbfv

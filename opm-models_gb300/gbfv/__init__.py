@@ -233,6 +233,14 @@ class LinearSolver:
         capi.check(self.lib.gbfv_linsolver_amg_apply(self.h, _d(d), _d(v)), "gbfv_linsolver_amg_apply")
         return v
 
+    def ilu0_apply(self, d):
+        """One FP64 application v = (LU)^-1 d of the general block ILU(0)
+        (patterns beyond the 5/7-point stencil's)."""
+        d = np.ascontiguousarray(d, float)
+        v = np.zeros(self.n * self.b)
+        capi.check(self.lib.gbfv_linsolver_ilu0_apply(self.h, _d(d), _d(v)), "gbfv_linsolver_ilu0_apply")
+        return v
+
     def close(self):
         if getattr(self, "h", None):
             self.lib.gbfv_linsolver_destroy(self.h)

@@ -91,6 +91,8 @@ class Problem(C.Structure):
         ("rho", C.c_double * 2), ("mu", C.c_double * 2),
         ("pvt", C.POINTER(BlackOilPvt)), ("temperature", C.c_double),
         ("flux_module", C.c_int32),
+        ("num_elements", C.c_int32), ("elem_corner", ip), ("bface_corner", ip),
+        ("p1_gradients", C.c_int32),
     ]
 
 
@@ -229,6 +231,7 @@ def load():
         "gbfv_linsolver_amg_levels": (C.c_int, [vp, ip, ip]),
         "gbfv_amg_levels": (C.c_int, [vp, ip, ip]),
         "gbfv_linsolver_amg_apply": (C.c_int, [vp, dp, dp]),
+        "gbfv_linsolver_ilu0_apply": (C.c_int, [vp, dp, dp]),
         "gbfv_kernel_launches": (C.c_int64, []),
         "gbfv_last_error": (C.c_char_p, []),
         "gbfv_phase_times": (C.c_int, [vp, dp]),

@@ -99,6 +99,12 @@ class ProblemData:
         s.mu = (C.c_double * 2)(*self.mu)
         s.temperature = self.temperature
         s.flux_module = self.flux_module
+        ec = getattr(self, "elem_corner", None)
+        if ec is not None:
+            s.num_elements = len(ec) // 4
+            s.elem_corner = capi.as_ptr(ec, I)
+            s.bface_corner = capi.as_ptr(self.bface_corner, I)
+            s.p1_gradients = self.p1_gradients
         if self.pvt_arrays is not None:
             a = self.pvt_arrays
             pv = capi.BlackOilPvt()
@@ -255,17 +261,34 @@ def lens(nx=48, ny=32, law="vg", dim=2, nz=16, flux="darcy"):
     p.gravity = tuple(grav)
     p.temperature = 273.15 + 20
     # boundary conditions (lensproblem.hh:468-537)
-    bc = g["bface_center"]
-    nb = len(bc)
+    ymax = ly if dim == 2 else lz
+    btype, bval = _lens_boundary(g["bface_center"], lx, ymax, vert, p.rho[0], grav[vert])
+    p.bface_type = btype
+    p.bface_value = np.ascontiguousarray(bval.ravel())
+    p.constraint = np.full(N, -1, np.int32)
+    # initial condition (lensproblem.hh:549-582)
+    p.init_pv = _lens_initial(c, ymax, vert, p.rho[0], grav[vert])
+    p.init_meaning = np.zeros(N, np.int32)
+    p.info = dict(name="lens", nx=nx, ny=ny, nz=(nz if dim == 3 else 1), dim=dim, flux=flux)
+    if flux == "trans":
+        p.flux_module = capi.FLUX_TRANS
+    elif flux != "darcy":
+        raise ValueError("flux must be 'darcy' or 'trans'")
+    return p
+
+
+def _lens_boundary(positions, xmax, ymax, vert, rho_w, gy, eps=3e-6):
+    """LensProblem::boundary (lensproblem.hh:468-537) at each boundary
+    integration point: free flow (hydrostatic p_w, S_w = 1; scaled by
+    1 + 1.5/height on the left) on the left and right, the NAPL inlet on the
+    top for 0.5 < lambda < 2/3, no flow elsewhere."""
+    nb = len(positions)
     btype = np.zeros(nb, np.int32)
     bval = np.zeros((nb, 4))
-    xmin, xmax = 0.0, lx
-    ymax = ly if dim == 2 else lz
+    xmin = 0.0
     height = ymax
-    rho_w = p.rho[0]
-    gy = grav[vert]
     for f in range(nb):
-        pos = bc[f]
+        pos = positions[f]
         on_left = pos[0] < xmin + eps
         on_right = pos[0] > xmax - eps
         on_upper = pos[vert] > ymax - eps
@@ -284,19 +307,123 @@ def lens(nx=48, ny=32, law="vg", dim=2, nz=16, flux="darcy"):
         elif on_upper and 0.5 < lam < 2.0 / 3.0:
             btype[f] = capi.BC_MASSRATE
             bval[f, 1] = -0.04
+    return btype, bval
+
+
+def _lens_initial(positions, ymax, vert, rho_w, gy):
+    """LensProblem::initial (lensproblem.hh:549-582): hydrostatic p_w, S_w = 1."""
+    depth = ymax - positions[:, vert]
+    pw = 1e5 - rho_w * gy * depth
+    return np.ascontiguousarray(np.stack([pw, np.ones(len(positions))], 1).ravel())
+
+
+def _quad_area(p0, p1, p2, p3):
+    """Area of the quadrilateral p0 p1 p2 p3 (VcfvStencil::quadrilateralArea,
+    vcfvstencil.hh:495-501)."""
+    return 0.5 * abs((p3[0] - p1[0]) * (p2[1] - p0[1]) - (p3[1] - p1[1]) * (p2[0] - p0[0]))
+
+
+# 2D cube reference element (dune-geometry numbering): corner c at
+# ((c & 1), (c >> 1) & 1); face f: 0 x = 0, 1 x = 1, 2 y = 0, 3 y = 1, with
+# corners FACE_CORNERS[f] and centre FACE_CENTER[f]
+FACE_CORNERS = ((0, 2), (1, 3), (0, 1), (2, 3))
+FACE_CENTER = ((0.0, 0.5), (1.0, 0.5), (0.5, 0.0), (0.5, 1.0))
+FACE_NORMAL = ((-1.0, 0.0), (1.0, 0.0), (0.0, -1.0), (0.0, 1.0))
+
+
+def lens_vcfv(nx=48, ny=32, law="vg", p1=True):
+    """LensProblem on the vertex-centred discretization
+    (lens_immiscible_vcfv_ad.cc / lens_immiscible_vcfv_fd.cc: 2D 48x32
+    elements over 6 m x 4 m, P1 finite-element gradients).  The degrees of
+    freedom are the (nx+1) x (ny+1) vertices, index i + (nx+1) j; element
+    ex + nx ey has corners (ex, ey), (ex+1, ey), (ex, ey+1), (ex+1, ey+1).
+    Material, permeability and the initial state are the problem's at each
+    vertex; boundary conditions at each boundary sub-control-volume face's
+    integration point (half way from the corner to the intersection's
+    centre, vcfvstencil.hh:966-1010)."""
+    lx, ly = 6.0, 4.0
+    hx, hy = lx / nx, ly / ny
+    mx, my = nx + 1, ny + 1
+    N = mx * my
+    vi = np.arange(N)
+    pos = np.zeros((N, 3))
+    pos[:, 0] = (vi % mx) * hx
+    pos[:, 1] = (vi // mx) * hy
+    p = ProblemData(capi.MODEL_IMMISCIBLE_2P)
+    p.center = np.ascontiguousarray(pos.ravel())
+    eps = 3e-6
+    lens_ll, lens_ur = (1.0, 2.0), (4.0, 3.0)
+    in_lens = np.ones(N, bool)
+    for d in range(2):
+        in_lens &= (pos[:, d] >= lens_ll[d] - eps) & (pos[:, d] <= lens_ur[d] + eps)
+    p.material = np.where(in_lens, 1, 0).astype(np.int32)
+    kl, ko = 9.05e-12, 4.6e-10
+    p.perm = np.ascontiguousarray(np.repeat(np.where(in_lens, kl, ko)[:, None], 3, 1).ravel())
+    p.porosity = np.full(N, 0.4)
+    if law == "vg":
+        mats = vg_params(0.05, 0.0, 0.0037, 4.7) + vg_params(0.18, 0.0, 0.00045, 7.3)
+    else:
+        mats = bc_params(0.05, 0.0, 500.0, 2.0) + bc_params(0.18, 0.0, 2000.0, 2.0)
+    p.material_params = np.array(mats, float)
+    p.rho = (1000.0, 1460.0)
+    p.mu = (1e-3, 5.7e-4)
+    p.gravity = (0.0, -9.81, 0.0)
+    p.temperature = 273.15 + 20
+    # elements and their boundary sub-control-volume faces
+    NE = nx * ny
+    ex, ey = np.arange(NE) % nx, np.arange(NE) // nx
+    v0 = ex + mx * ey
+    corners = np.stack([v0, v0 + 1, v0 + mx, v0 + mx + 1], 1)
+    p.elem_corner = np.ascontiguousarray(corners.ravel().astype(np.int32))
+    volume = np.zeros(N)
+    bptr, bcorner, bcenter, bnormal, barea = [0], [], [], [], []
+    for e in range(NE):
+        lower = np.array([ex[e] * hx, ey[e] * hy])
+        upper = np.array([(ex[e] + 1) * hx, (ey[e] + 1) * hy])
+        glob = lambda loc: lower + np.asarray(loc) * (upper - lower)
+        cg = [glob((c & 1, (c >> 1) & 1)) for c in range(4)]
+        edge = [glob(FACE_CENTER[f]) for f in range(4)]
+        mid = glob((0.5, 0.5))
+        scv = (_quad_area(cg[0], edge[2], mid, edge[0]), _quad_area(cg[1], edge[1], mid, edge[2]),
+               _quad_area(cg[2], edge[0], mid, edge[3]), _quad_area(cg[3], edge[3], mid, edge[1]))
+        for c in range(4):
+            volume[corners[e, c]] += scv[c]
+        for f in range(4):
+            on = (f == 0 and ex[e] == 0) or (f == 1 and ex[e] == nx - 1) or \
+                 (f == 2 and ey[e] == 0) or (f == 3 and ey[e] == ny - 1)
+            if not on:
+                continue
+            length = hy if f < 2 else hx
+            for c in FACE_CORNERS[f]:
+                loc = (np.array([c & 1, (c >> 1) & 1], float) + np.array(FACE_CENTER[f])) * 0.5
+                ip = glob(loc)
+                bcorner.append(c)
+                bcenter.append((ip[0], ip[1], 0.0))
+                bnormal.append((FACE_NORMAL[f][0], FACE_NORMAL[f][1], 0.0))
+                barea.append(0.5 * length)
+        bptr.append(len(bcorner))
+    p.volume = volume
+    p.conn_ptr = np.zeros(N + 1, np.int32)
+    p.conn_nbr = np.zeros(0, np.int32)
+    p.conn_dir = np.zeros(0, np.int32)
+    p.conn_normal = np.zeros(0)
+    p.conn_center = np.zeros(0)
+    p.conn_area = np.zeros(0)
+    p.bface_ptr = np.array(bptr, np.int32)
+    p.bface_corner = np.array(bcorner, np.int32)
+    bcenter = np.array(bcenter)
+    p.bface_center = np.ascontiguousarray(bcenter.ravel())
+    p.bface_normal = np.ascontiguousarray(np.array(bnormal).ravel())
+    p.bface_area = np.array(barea)
+    btype, bval = _lens_boundary(bcenter, lx, ly, 1, p.rho[0], -9.81)
     p.bface_type = btype
     p.bface_value = np.ascontiguousarray(bval.ravel())
+    p.p1_gradients = 1 if p1 else 0
     p.constraint = np.full(N, -1, np.int32)
-    # initial condition (lensproblem.hh:549-582)
-    depth = ymax - c[:, vert]
-    pw = 1e5 - rho_w * gy * depth
-    p.init_pv = np.ascontiguousarray(np.stack([pw, np.ones(N)], 1).ravel())
+    p.init_pv = _lens_initial(pos, ly, 1, p.rho[0], -9.81)
     p.init_meaning = np.zeros(N, np.int32)
-    p.info = dict(name="lens", nx=nx, ny=ny, nz=(nz if dim == 3 else 1), dim=dim, flux=flux)
-    if flux == "trans":
-        p.flux_module = capi.FLUX_TRANS
-    elif flux != "darcy":
-        raise ValueError("flux must be 'darcy' or 'trans'")
+    p.info = dict(name="lens-vcfv", nx=nx, ny=ny, nz=1, dim=2, flux="darcy", disc="vcfv",
+                  gradients="p1" if p1 else "two-point")
     return p
 
 

@@ -85,6 +85,9 @@ struct Prob {
     BlackOilPvt pvt;
     int fluxModule = GBFV_FLUX_DARCY;
     int dimWorld = 3;   // the highest coordinate axis the faces use, plus one
+    // vertex-centred grids: the cells are the vertices
+    int numElements = 0, p1Gradients = 0;
+    std::vector<int> elemCorner, bfCorner;
 };
 
 template <class T>
@@ -118,7 +121,14 @@ static Prob copyProblem(const gbfv_problem& q)
                 if (q.conn_normal[3 * c + d] != 0.0) maxAxis = std::max(maxAxis, d);
         P.dimWorld = maxAxis + 1;
     }
-    P.bfPtr = cp(q.bface_ptr, N + 1);
+    P.numElements = q.num_elements;
+    if (P.numElements > 0) {
+        P.elemCorner = cp(q.elem_corner, 4 * (size_t)P.numElements);
+        P.bfCorner = cp(q.bface_corner, q.num_bfaces);
+        P.p1Gradients = q.p1_gradients;
+        P.dimWorld = 2;
+    }
+    P.bfPtr = cp(q.bface_ptr, (P.numElements > 0 ? P.numElements : N) + 1);
     P.bfType = cp(q.bface_type, q.num_bfaces);
     P.bfNormal = cp(q.bface_normal, 3 * (size_t)q.num_bfaces);
     P.bfCenter = cp(q.bface_center, 3 * (size_t)q.num_bfaces);
@@ -410,6 +420,7 @@ struct Bcrs {
 };
 
 struct AmgHierarchy;  // amg.hh
+struct VcfvGrid;      // vcfv.hh
 
 struct Sim {
     Prob P;
@@ -431,6 +442,7 @@ struct Sim {
     int numIterations = 0;
     double refPressure = 1.0;  // ImmiscibleModel::referencePressure_ (immisciblemodel.hh:301-316)
     std::shared_ptr<AmgHierarchy> amg;  // ParallelAmgBackend's hierarchy (structure kept across solves)
+    std::shared_ptr<VcfvGrid> vcfv;  // vertex-centred stencils (vcfv.hh), else NULL
 };
 
 static void buildPattern(Sim& S)
@@ -963,6 +975,8 @@ static void applyConstraintsToLinearization(Sim& S)
     }
 }
 
+#include "vcfv.hh"
+
 // FvBaseLinearizer::linearizeDomain / linearize_ (fvbaselinearizer.hh:201-241,
 // 510-593): constraints, intensive quantities, element loop, constraints
 static void linearize(Sim& S)
@@ -971,7 +985,14 @@ static void linearize(Sim& S)
     std::fill(S.J.val.begin(), S.J.val.end(), 0.0);
     std::fill(S.residual.begin(), S.residual.end(), 0.0);
     const bool fd = S.prm.local_linearizer == GBFV_LIN_FD;
-    if (S.P.model == GBFV_MODEL_IMMISCIBLE_2P) {
+    if (S.vcfv) {
+        if (fd) throw NumericalProblem("vertex-centred grids take the AD local linearizer", GBFV_ERR_UNSUPPORTED);
+        std::vector<IQ2> iq(S.N);
+#pragma omp parallel for schedule(static)
+        for (int I = 0; I < S.N; ++I) iq[I] = immiscibleIQ(S.P, I, &S.x[I * 2]);
+        linearizeImmiscibleVcfv(S, iq);
+    }
+    else if (S.P.model == GBFV_MODEL_IMMISCIBLE_2P) {
         std::vector<IQ2> iq(S.N);
 #pragma omp parallel for schedule(static)
         for (int I = 0; I < S.N; ++I) iq[I] = immiscibleIQ(S.P, I, &S.x[I * 2]);
@@ -1558,7 +1579,22 @@ void* oracle_create(const gbfv_problem* prob, const gbfv_params* prm)
         S->storageOld.assign(S->N * S->b, 0.0);
         S->residual.assign(S->N * S->b, 0.0);
         S->rscale.assign(S->N * S->b, 0.0);
-        buildPattern(*S);
+        if (S->P.numElements > 0) {
+            // the vertex-centred discretization takes the immiscible model
+            // with the Darcy flux module and the AD local linearizer
+            if (S->P.model != GBFV_MODEL_IMMISCIBLE_2P || S->P.fluxModule != GBFV_FLUX_DARCY ||
+                prm->local_linearizer != GBFV_LIN_AD || prm->linearizer != GBFV_LINEARIZER_ELEMENT) {
+                delete S;
+                return nullptr;
+            }
+            S->vcfv = vcfvGrid(S->P);
+            S->P.volume = S->vcfv->totalVolume;
+            S->vcfv->bfPtr = S->P.bfPtr;
+            S->vcfv->bfCorner = S->P.bfCorner;
+            buildPatternVcfv(*S);
+        }
+        else
+            buildPattern(*S);
         return S;
     }
     catch (...) {
