@@ -1154,8 +1154,8 @@ static int buildPhysics(const gbfv_problem* P, DevPhysics& ph)
 // constraints, output fields) are the cell-centred ones.
 static int createVcfvImpl(gbfv_ctx* C, const gbfv_problem* P)
 {
-    if (C->prm.local_linearizer != GBFV_LIN_AD || C->prm.linearizer != GBFV_LINEARIZER_ELEMENT) {
-        setError("vertex-centred grids take the element linearizer with automatic differentiation");
+    if (C->prm.linearizer != GBFV_LINEARIZER_ELEMENT) {
+        setError("vertex-centred grids take the element linearizer");
         return GBFV_ERR_UNSUPPORTED;
     }
     VcfvSetup vs;
@@ -1874,10 +1874,6 @@ int gbfv_set_params(gbfv_ctx* C, const gbfv_params* p)
         setError("the linearizer is fixed when the context is created");
         return GBFV_ERR_UNSUPPORTED;
     }
-    if (C->vcfv && p->local_linearizer != GBFV_LIN_AD) {
-        setError("vertex-centred grids take the AD local linearizer");
-        return GBFV_ERR_UNSUPPORTED;
-    }
     C->prm = *p;
     return GBFV_OK;
 }
@@ -2023,8 +2019,12 @@ static int linearizeImpl(gbfv_ctx* C)
                 launchIq(C->mesh, C->dphys, C->fdX[b + pv], C->meaning, C->fd.minus[pv], C->stream);
             }
         }
-        launchAssembleFd(C->mesh, C->dphys, C->iq, C->fd, C->meaning, C->refP, method, C->storageOld,
-                         C->newtonIter == 0, C->dt, C->residual, C->jval, C->stream);
+        if (C->vcfv)
+            launchVcfvAssembleFd(C->vcfv, C->mesh, C->iq, C->fd, C->refP, method, C->storageOld, C->newtonIter == 0,
+                                 C->dt, C->residual, C->jval, C->stream);
+        else
+            launchAssembleFd(C->mesh, C->dphys, C->iq, C->fd, C->meaning, C->refP, method, C->storageOld,
+                             C->newtonIter == 0, C->dt, C->residual, C->jval, C->stream);
         cudaEventRecord(C->evL1, C->stream);
         C->linPending = 1;
         CK(cudaGetLastError());

@@ -186,87 +186,68 @@ int slotOf(const double* a, const double* b)
 }
 
 // ---------------------------------------------------------------- kernels --
-// Element pass: thread (e, f) evaluates FvBaseLocalResidual::eval of element
-// e with the derivatives of corner f (fvbaselocalresidual.hh:158-191).
-template <bool P1>
-__global__ void __launch_bounds__(128) kVcfvElement(VcfvArgs a, DevMesh m, IqBuffers iq,
-                                                    const double* __restrict__ storageOld, int iter0, double dt)
+__device__ __forceinline__ double valueOf(double x) { return x; }
+__device__ __forceinline__ double valueOf(const D2& x) { return x.v; }
+
+// FvBaseLocalResidual::eval of one element (fvbaselocalresidual.hh:158-191)
+// in the number type T (D2 for automatic differentiation, double for finite
+// differences).  Q(c, k): quantity k (p0 p1 rho0 rho1 lam0 lam1) of corner
+// c; Sto(c, ph): the storage of phase ph in corner c; sto0: the storage
+// values of the unperturbed state (the cache at iteration 0).
+template <class T, bool P1, class QF, class SF>
+__device__ __forceinline__ void elementEval(const VcfvArgs& a, const DevMesh& m, int e, const QF& Q, const SF& Sto,
+                                            const double* __restrict__ sto0, const double* __restrict__ storageOld,
+                                            int iter0, double dt, T (&res)[4][2])
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= a.E * 4) return;
-    const int e = t >> 2, f = t & 3;
     const ElemGeo& G = a.geo[e];
     const int ld = m.ldN;
-    int v[4];
-    double cv[4][6];  // p0 p1 rho0 rho1 lam0 lam1 of each corner
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
-        v[c] = G.v[c];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) cv[c][k] = iq.val[k * ld + v[c]];
-    }
-    double fd[6][2];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-        fd[k][0] = iq.der[(k * 2 + 0) * ld + v[f]];
-        fd[k][1] = iq.der[(k * 2 + 1) * ld + v[f]];
-    }
-    auto Q = [&](int c, int k) {
-        D2 r(cv[c][k]);
-        if (c == f) {
-            r.d[0] = fd[k][0];
-            r.d[1] = fd[k][1];
-        }
-        return r;
-    };
-    D2 res[4][2];
-#pragma unroll
-    for (int c = 0; c < 4; ++c) res[c][0] = res[c][1] = D2(0.0);
+    for (int c = 0; c < 4; ++c) res[c][0] = res[c][1] = T(0.0);
     // evalFluxes: the four sub-control-volume faces
 #pragma unroll 1
     for (int k = 0; k < 4; ++k) {
         const int i = FI[k], j = FJ[k];
-        D2 pg[2][2];
+        T pg[2][2];
 #pragma unroll
         for (int ph = 0; ph < 2; ++ph) {
             if (P1) {
-                pg[ph][0] = D2(0.0);
-                pg[ph][1] = D2(0.0);
+                pg[ph][0] = T(0.0);
+                pg[ph][1] = T(0.0);
 #pragma unroll
                 for (int c = 0; c < 4; ++c) {
-                    const D2 dv = Q(c, ph);
+                    const T dv = Q(c, ph);
                     pg[ph][0] = pg[ph][0] + dv * G.grad[k][c][0];
                     pg[ph][1] = pg[ph][1] + dv * G.grad[k][c][1];
                 }
             }
             else {
-                const D2 deltay = Q(j, ph) - Q(i, ph);
+                const T deltay = Q(j, ph) - Q(i, ph);
                 pg[ph][0] = deltay * G.w2p[k][0];
                 pg[ph][1] = deltay * G.w2p[k][1];
             }
             // gravity correction (darcyfluxmodule.hh:214-283)
-            const D2 pStatIn = -(Q(i, 2 + ph) * G.gIn[k]);
-            const D2 pStatEx = -(Q(j, 2 + ph) * G.gEx[k]);
-            const D2 fs = (pStatEx - pStatIn) / G.absTot2[k];
+            const T pStatIn = -(Q(i, 2 + ph) * G.gIn[k]);
+            const T pStatEx = -(Q(j, 2 + ph) * G.gEx[k]);
+            const T fs = (pStatEx - pStatIn) / G.absTot2[k];
             pg[ph][0] = pg[ph][0] + G.dTot[k][0] * fs;
             pg[ph][1] = pg[ph][1] + G.dTot[k][1] * fs;
         }
-        D2 flux[2];
+        T flux[2];
 #pragma unroll
         for (int ph = 0; ph < 2; ++ph) {
-            D2 tmp(0.0);
+            T tmp(0.0);
             tmp = tmp + pg[ph][0] * G.fn[k][0];
             tmp = tmp + pg[ph][1] * G.fn[k][1];
-            const int up = tmp.v > 0 ? j : i;
-            const D2 mob = Q(up, 4 + ph);
-            D2 vf(0.0);
+            const int up = valueOf(tmp) > 0 ? j : i;
+            const T mob = Q(up, 4 + ph);
+            T vf(0.0);
 #pragma unroll
             for (int d = 0; d < 2; ++d) {
-                D2 fv = G.Kh[k][d] * pg[ph][d];
+                T fv = G.Kh[k][d] * pg[ph][d];
                 fv = fv * (-mob);
                 vf = vf + fv * G.fn[k][d];
             }
-            flux[ph] = D2(0.0) + vf * Q(up, 2 + ph);
+            flux[ph] = T(0.0) + vf * Q(up, 2 + ph);
             flux[ph] = flux[ph] * (1.0 * G.fa[k]);
         }
 #pragma unroll
@@ -281,12 +262,8 @@ __global__ void __launch_bounds__(128) kVcfvElement(VcfvArgs a, DevMesh m, IqBuf
         const double scvVolume = G.scvVol[c] * 1.0;
 #pragma unroll
         for (int ph = 0; ph < 2; ++ph) {
-            D2 tmp(iq.sto[(ph * 3 + 0) * ld + v[c]]);
-            if (c == f) {
-                tmp.d[0] = iq.sto[(ph * 3 + 1) * ld + v[c]];
-                tmp.d[1] = iq.sto[(ph * 3 + 2) * ld + v[c]];
-            }
-            const double tmp2 = iter0 ? tmp.v : storageOld[ph * ld + v[c]];
+            T tmp = Sto(c, ph);
+            const double tmp2 = iter0 ? sto0[ph * 3 * ld + G.v[c]] : storageOld[ph * ld + G.v[c]];
             tmp = tmp - tmp2;
             tmp = tmp * (scvVolume / dt);
             res[c][ph] = res[c][ph] + tmp;
@@ -296,35 +273,35 @@ __global__ void __launch_bounds__(128) kVcfvElement(VcfvArgs a, DevMesh m, IqBuf
     // evalBoundary_: this element's boundary sub-control-volume faces
     for (int b = a.bfPtr[e]; b < a.bfPtr[e + 1]; ++b) {
         const BFaceV B = a.bf[b];
-        D2 values[2] = {D2(0.0), D2(0.0)};
+        T values[2] = {T(0.0), T(0.0)};
         if (B.type == GBFV_BC_MASSRATE) {
-            values[0] = D2(B.rate[0]);
-            values[1] = D2(B.rate[1]);
+            values[0] = T(B.rate[0]);
+            values[1] = T(B.rate[1]);
         }
         else if (B.type == GBFV_BC_FREEFLOW) {
 #pragma unroll
             for (int ph = 0; ph < 2; ++ph) {
-                const D2 pIn = Q(B.c, ph);
-                const D2 deltay = D2(B.pb[ph]) - pIn;
-                D2 pg[2];
+                const T pIn = Q(B.c, ph);
+                const T deltay = T(B.pb[ph]) - pIn;
+                T pg[2];
                 pg[0] = deltay * B.w[0];
                 pg[1] = deltay * B.w[1];
-                const D2 pStatIn = (-B.gTimesDist) * Q(B.c, 2 + ph);
-                const D2 fsc = pStatIn / B.absDist2;
+                const T pStatIn = (-B.gTimesDist) * Q(B.c, 2 + ph);
+                const T fsc = pStatIn / B.absDist2;
                 pg[0] = pg[0] + B.dIn[0] * fsc;
                 pg[1] = pg[1] + B.dIn[1] * fsc;
-                D2 tmp(0.0);
+                T tmp(0.0);
                 tmp = tmp + pg[0] * B.n[0];
                 tmp = tmp + pg[1] * B.n[1];
-                const D2 mob = tmp.v > 0.0 ? D2(B.mobb[ph]) : Q(B.c, 4 + ph);
-                D2 vf(0.0);
+                const T mob = valueOf(tmp) > 0.0 ? T(B.mobb[ph]) : Q(B.c, 4 + ph);
+                T vf(0.0);
 #pragma unroll
                 for (int d = 0; d < 2; ++d) {
-                    D2 fv = B.K[d] * pg[d];
+                    T fv = B.K[d] * pg[d];
                     fv = fv * (-mob);
                     vf = vf + fv * B.n[d];
                 }
-                const D2 dens = B.pb[ph] > pIn.v ? D2(B.rhob[ph]) : Q(B.c, 2 + ph);
+                const T dens = B.pb[ph] > valueOf(pIn) ? T(B.rhob[ph]) : Q(B.c, 2 + ph);
                 values[ph] = values[ph] + vf * dens;
             }
         }
@@ -332,13 +309,57 @@ __global__ void __launch_bounds__(128) kVcfvElement(VcfvArgs a, DevMesh m, IqBuf
 #pragma unroll
         for (int ph = 0; ph < 2; ++ph) res[B.c][ph] = res[B.c][ph] + values[ph] * aa;
     }
-    // volumetric residual, then the scratch records
+    // volumetric residual
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-        const double V = m.volume[v[c]];
+        const double V = m.volume[G.v[c]];
         res[c][0] = res[c][0] / V;
         res[c][1] = res[c][1] / V;
     }
+}
+
+// Element pass (automatic differentiation): thread (e, f) evaluates element
+// e with the derivatives of corner f (fvbaseadlocallinearizer.hh:173-292).
+template <bool P1>
+__global__ void __launch_bounds__(128) kVcfvElement(VcfvArgs a, DevMesh m, IqBuffers iq,
+                                                    const double* __restrict__ storageOld, int iter0, double dt)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.E * 4) return;
+    const int e = t >> 2, f = t & 3;
+    const ElemGeo& G = a.geo[e];
+    const int ld = m.ldN;
+    double cv[4][6];  // p0 p1 rho0 rho1 lam0 lam1 of each corner
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+        for (int k = 0; k < 6; ++k) cv[c][k] = iq.val[k * ld + G.v[c]];
+    const int vf = G.v[f];
+    double fd[6][2];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        fd[k][0] = iq.der[(k * 2 + 0) * ld + vf];
+        fd[k][1] = iq.der[(k * 2 + 1) * ld + vf];
+    }
+    auto Q = [&](int c, int k) {
+        D2 r(cv[c][k]);
+        if (c == f) {
+            r.d[0] = fd[k][0];
+            r.d[1] = fd[k][1];
+        }
+        return r;
+    };
+    auto Sto = [&](int c, int ph) {
+        const int v = G.v[c];
+        D2 r(iq.sto[(ph * 3 + 0) * ld + v]);
+        if (c == f) {
+            r.d[0] = iq.sto[(ph * 3 + 1) * ld + v];
+            r.d[1] = iq.sto[(ph * 3 + 2) * ld + v];
+        }
+        return r;
+    };
+    D2 res[4][2];
+    elementEval<D2, P1>(a, m, e, Q, Sto, iq.sto, storageOld, iter0, dt, res);
     const size_t ef = (size_t)e * 4 + f;
     a.R[ef * 2 + 0] = res[f][0].v;
     a.R[ef * 2 + 1] = res[f][1].v;
@@ -348,6 +369,77 @@ __global__ void __launch_bounds__(128) kVcfvElement(VcfvArgs a, DevMesh m, IqBuf
         for (int ph = 0; ph < 2; ++ph)
 #pragma unroll
             for (int pv = 0; pv < 2; ++pv) a.J[(ef * 4 + j) * 4 + ph * 2 + pv] = res[j][ph].d[pv];
+}
+
+// Element pass (finite differences, fvbasefdlocallinearizer.hh:236-510):
+// thread (e, f) evaluates element e unperturbed and with corner f's
+// primary variable pv deflected (the deflected states' intensive
+// quantities come from the per-vertex deflection passes, plus[pv] at
+// x + eps, minus[pv] at the second state), the columns of corner f being
+// the differences divided by the total deflection.
+template <bool P1>
+__global__ void __launch_bounds__(128) kVcfvElementFd(VcfvArgs a, DevMesh m, IqBuffers iq0, FdIq fdq,
+                                                      const double* __restrict__ refP, int method,
+                                                      const double* __restrict__ storageOld, int iter0, double dt)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.E * 4) return;
+    const int e = t >> 2, f = t & 3;
+    const ElemGeo& G = a.geo[e];
+    const int ld = m.ldN;
+    double cv[4][6];
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+        for (int k = 0; k < 6; ++k) cv[c][k] = iq0.val[k * ld + G.v[c]];
+    const int vf = G.v[f];
+    auto eval = [&](const IqBuffers* dq, int it0, double (&res)[4][2]) {
+        auto Q = [&](int c, int k) { return (dq && c == f) ? dq->val[k * ld + vf] : cv[c][k]; };
+        auto Sto = [&](int c, int ph) {
+            return (dq && c == f) ? dq->sto[(ph * 3) * ld + vf] : iq0.sto[(ph * 3) * ld + G.v[c]];
+        };
+        elementEval<double, P1>(a, m, e, Q, Sto, iq0.sto, storageOld, it0, dt, res);
+    };
+    double res0[4][2];
+    eval(nullptr, iter0, res0);
+    const size_t ef = (size_t)e * 4 + f;
+    a.R[ef * 2 + 0] = res0[f][0];
+    a.R[ef * 2 + 1] = res0[f][1];
+    // the deflection of this vertex's primary variable (the immiscible
+    // model's primaryVarWeight: 10 / reference pressure for the pressure)
+    const double baseEps = fmax(0.9123e-10, 2.220446049250313e-16 * 1.23e3);
+#pragma unroll 1
+    for (int pv = 0; pv < 2; ++pv) {
+        const double w = pv == 0 ? 10 / *refP : 1.0;
+        const double eps = baseEps / w;
+        double delta = 0.0;
+        double d[4][2], r1[4][2];
+        // the stashed state reads the storage cache: the unperturbed storage
+        if (method >= 0) {
+            delta += eps;
+            eval(&fdq.plus[pv], iter0, r1);
+#pragma unroll
+            for (int c = 0; c < 4; ++c) d[c][0] = r1[c][0], d[c][1] = r1[c][1];
+        }
+        else {
+#pragma unroll
+            for (int c = 0; c < 4; ++c) d[c][0] = res0[c][0], d[c][1] = res0[c][1];
+        }
+        if (method <= 0) {
+            delta += eps;
+            eval(&fdq.minus[pv], iter0, r1);
+#pragma unroll
+            for (int c = 0; c < 4; ++c) d[c][0] -= r1[c][0], d[c][1] -= r1[c][1];
+        }
+        else {
+#pragma unroll
+            for (int c = 0; c < 4; ++c) d[c][0] -= res0[c][0], d[c][1] -= res0[c][1];
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int ph = 0; ph < 2; ++ph) a.J[(ef * 4 + j) * 4 + ph * 2 + pv] = d[j][ph] / delta;
+    }
 }
 
 // Gather pass: vertex p's residual and Jacobian row, its elements' records
@@ -639,8 +731,8 @@ double vcfvLinearizeBytes(const VcfvDev* d)
     return elem + bnd + gather;
 }
 
-void launchVcfvAssemble(const VcfvDev* d, const DevMesh& m, IqBuffers iq, double* storageOld, int iter0, double dt,
-                        double* residual, double* jval, cudaStream_t s)
+namespace {
+VcfvArgs vcfvArgs(const VcfvDev* d)
 {
     VcfvArgs a;
     a.E = d->E;
@@ -653,6 +745,26 @@ void launchVcfvAssemble(const VcfvDev* d, const DevMesh& m, IqBuffers iq, double
     a.R = d->R;
     a.J = d->J;
     a.p1 = d->p1;
+    return a;
+}
+}  // namespace
+
+void launchVcfvAssembleFd(const VcfvDev* d, const DevMesh& m, IqBuffers iq0, const FdIq& fd, const double* refP,
+                          int method, double* storageOld, int iter0, double dt, double* residual, double* jval,
+                          cudaStream_t s)
+{
+    const VcfvArgs a = vcfvArgs(d);
+    const int nt = 4 * d->E;
+    if (d->p1) kVcfvElementFd<true><<<(nt + 127) / 128, 128, 0, s>>>(a, m, iq0, fd, refP, method, storageOld, iter0, dt);
+    else kVcfvElementFd<false><<<(nt + 127) / 128, 128, 0, s>>>(a, m, iq0, fd, refP, method, storageOld, iter0, dt);
+    kVcfvGather<<<(m.N + 127) / 128, 128, 0, s>>>(a, m, iq0, storageOld, iter0, residual, jval);
+    countLaunch(2);
+}
+
+void launchVcfvAssemble(const VcfvDev* d, const DevMesh& m, IqBuffers iq, double* storageOld, int iter0, double dt,
+                        double* residual, double* jval, cudaStream_t s)
+{
+    const VcfvArgs a = vcfvArgs(d);
     const int nt = 4 * d->E;
     if (d->p1) kVcfvElement<true><<<(nt + 127) / 128, 128, 0, s>>>(a, m, iq, storageOld, iter0, dt);
     else kVcfvElement<false><<<(nt + 127) / 128, 128, 0, s>>>(a, m, iq, storageOld, iter0, dt);

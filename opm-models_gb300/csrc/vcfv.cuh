@@ -42,4 +42,11 @@ double vcfvLinearizeBytes(const VcfvDev* d);
 void launchVcfvAssemble(const VcfvDev* d, const DevMesh& m, IqBuffers iq, double* storageOld, int iter0, double dt,
                         double* residual, double* jval, cudaStream_t s);
 
+// The same with the finite-difference local linearizer: iq0 the state's
+// intensive quantities, fd those of the per-vertex deflected states
+// (launchFdDeflect + launchIq), method the numeric difference method.
+void launchVcfvAssembleFd(const VcfvDev* d, const DevMesh& m, IqBuffers iq0, const FdIq& fd, const double* refP,
+                          int method, double* storageOld, int iter0, double dt, double* residual, double* jval,
+                          cudaStream_t s);
+
 }  // namespace gbfv

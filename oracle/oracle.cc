@@ -986,11 +986,13 @@ static void linearize(Sim& S)
     std::fill(S.residual.begin(), S.residual.end(), 0.0);
     const bool fd = S.prm.local_linearizer == GBFV_LIN_FD;
     if (S.vcfv) {
-        if (fd) throw NumericalProblem("vertex-centred grids take the AD local linearizer", GBFV_ERR_UNSUPPORTED);
         std::vector<IQ2> iq(S.N);
 #pragma omp parallel for schedule(static)
         for (int I = 0; I < S.N; ++I) iq[I] = immiscibleIQ(S.P, I, &S.x[I * 2]);
-        linearizeImmiscibleVcfv(S, iq);
+        if (fd)
+            linearizeImmiscibleVcfvFd(S, iq);
+        else
+            linearizeImmiscibleVcfv(S, iq);
     }
     else if (S.P.model == GBFV_MODEL_IMMISCIBLE_2P) {
         std::vector<IQ2> iq(S.N);
@@ -1581,9 +1583,9 @@ void* oracle_create(const gbfv_problem* prob, const gbfv_params* prm)
         S->rscale.assign(S->N * S->b, 0.0);
         if (S->P.numElements > 0) {
             // the vertex-centred discretization takes the immiscible model
-            // with the Darcy flux module and the AD local linearizer
+            // with the Darcy flux module and the element linearizer
             if (S->P.model != GBFV_MODEL_IMMISCIBLE_2P || S->P.fluxModule != GBFV_FLUX_DARCY ||
-                prm->local_linearizer != GBFV_LIN_AD || prm->linearizer != GBFV_LINEARIZER_ELEMENT) {
+                prm->linearizer != GBFV_LINEARIZER_ELEMENT) {
                 delete S;
                 return nullptr;
             }

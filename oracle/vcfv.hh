@@ -156,20 +156,19 @@ template <int N> static inline Dual<N> valueOnly(const Dual<N>& x) { return Dual
 // FvBaseLocalResidual::eval of element e with focus corner f: res[c][eq]
 // the corners' residuals (divided by their total volumes), derivatives
 // with respect to corner f's primary variables; sc[c][eq] the parity scale
-// (sum of |terms| / V).  iq: every vertex's intensive quantities, each with
-// the derivatives of its own primary variables.
-static void elementImmiscibleVcfv(Sim& S, const VcfvGrid& G, int e, int f, const std::vector<IQ2>& iq,
-                                  bool iter0, D2 (&res)[4][2], double (&sc)[4][2])
+// (sum of |terms| / V).  q: the corners' intensive quantities, each with
+// the derivatives of its own primary variables (f = -1: no focus, the
+// values only, as the finite-difference linearizer evaluates).
+static void elementImmiscibleVcfv(Sim& S, const VcfvGrid& G, int e, int f, const IQ2* const (&q)[4], bool iter0,
+                                  D2 (&res)[4][2], double (&sc)[4][2])
 {
     const Prob& P = S.P;
     const VcfvElement& E = G.el[e];
     for (int c = 0; c < 4; ++c)
-        for (int q = 0; q < 2; ++q) {
-            res[c][q] = D2(0.0);
-            sc[c][q] = 0.0;
+        for (int a = 0; a < 2; ++a) {
+            res[c][a] = D2(0.0);
+            sc[c][a] = 0.0;
         }
-    const IQ2* q[4];
-    for (int c = 0; c < 4; ++c) q[c] = &iq[E.v[c]];
     auto focus = [&](int c, const D2& x) { return c == f ? x : valueOnly(x); };
     // evalFluxes
     for (int k = 0; k < 4; ++k) {
@@ -345,7 +344,8 @@ static void linearizeImmiscibleVcfv(Sim& S, const std::vector<IQ2>& iq)
         const VcfvElement& E = G.el[e];
         D2 res[4][4][2];
         double sc[4][4][2];
-        for (int f = 0; f < 4; ++f) elementImmiscibleVcfv(S, G, e, f, iq, iter0, res[f], sc[f]);
+        const IQ2* q[4] = {&iq[E.v[0]], &iq[E.v[1]], &iq[E.v[2]], &iq[E.v[3]]};
+        for (int f = 0; f < 4; ++f) elementImmiscibleVcfv(S, G, e, f, q, iter0, res[f], sc[f]);
         for (int f = 0; f < 4; ++f) {
             const int gf = E.v[f];
             for (int a = 0; a < 2; ++a) {
@@ -356,6 +356,71 @@ static void linearizeImmiscibleVcfv(Sim& S, const std::vector<IQ2>& iq)
                 double* blk = &S.J.val[(size_t)S.J.find(E.v[j], gf) * 4];
                 for (int a = 0; a < 2; ++a)
                     for (int pv = 0; pv < 2; ++pv) blk[a * 2 + pv] += res[f][j][a].d[pv];
+            }
+        }
+    }
+}
+
+// FvBaseFdLocalLinearizer on the vertex-centred stencil
+// (fvbasefdlocallinearizer.hh:236-510): the element's four corner residuals
+// unperturbed, then per corner f and primary variable the residuals with
+// f's intensive quantities at the deflected state(s) -- the other corners
+// keep theirs, the storage of the old time level comes from the cache the
+// unperturbed evaluation filled -- their difference over the deflection
+// being column (., f) of the element's local Jacobian.
+static void linearizeImmiscibleVcfvFd(Sim& S, const std::vector<IQ2>& iq)
+{
+    const VcfvGrid& G = *S.vcfv;
+    const bool iter0 = S.newtonIter == 0;
+    const int method = S.prm.numeric_difference_method;
+    const double baseEps = std::max(0.9123e-10, std::numeric_limits<double>::epsilon() * 1.23e3);
+    std::fill(S.rscale.begin(), S.rscale.end(), 0.0);
+    for (int e = 0; e < (int)G.el.size(); ++e) {
+        const VcfvElement& E = G.el[e];
+        const IQ2* q[4] = {&iq[E.v[0]], &iq[E.v[1]], &iq[E.v[2]], &iq[E.v[3]]};
+        D2 res0[4][2], resD[4][2];
+        double sc[4][2], scD[4][2];
+        elementImmiscibleVcfv(S, G, e, -1, q, iter0, res0, sc);
+        for (int c = 0; c < 4; ++c)
+            for (int a = 0; a < 2; ++a) {
+                S.residual[E.v[c] * 2 + a] += res0[c][a].v;
+                S.rscale[E.v[c] * 2 + a] += sc[c][a];
+            }
+        for (int f = 0; f < 4; ++f) {
+            const int gf = E.v[f];
+            for (int pv = 0; pv < 2; ++pv) {
+                double xs[2] = {S.x[gf * 2], S.x[gf * 2 + 1]};
+                const double eps = baseEps / pvWeight(S, gf, pv);
+                double delta = 0.0, d[4][2];
+                const IQ2* qd[4] = {q[0], q[1], q[2], q[3]};
+                if (method >= 0) {
+                    xs[pv] += eps;
+                    delta += eps;
+                    const IQ2 dq = immiscibleIQ(S.P, gf, xs);
+                    qd[f] = &dq;
+                    elementImmiscibleVcfv(S, G, e, -1, qd, false, resD, scD);
+                    for (int c = 0; c < 4; ++c)
+                        for (int a = 0; a < 2; ++a) d[c][a] = resD[c][a].v;
+                }
+                else
+                    for (int c = 0; c < 4; ++c)
+                        for (int a = 0; a < 2; ++a) d[c][a] = res0[c][a].v;
+                if (method <= 0) {
+                    xs[pv] -= delta + eps;
+                    delta += eps;
+                    const IQ2 dq = immiscibleIQ(S.P, gf, xs);
+                    qd[f] = &dq;
+                    elementImmiscibleVcfv(S, G, e, -1, qd, false, resD, scD);
+                    for (int c = 0; c < 4; ++c)
+                        for (int a = 0; a < 2; ++a) d[c][a] -= resD[c][a].v;
+                }
+                else
+                    for (int c = 0; c < 4; ++c)
+                        for (int a = 0; a < 2; ++a) d[c][a] -= res0[c][a].v;
+                for (int j = 0; j < 4; ++j) {
+                    double* blk = &S.J.val[(size_t)S.J.find(E.v[j], gf) * 4];
+                    for (int a = 0; a < 2; ++a) blk[a * 2 + pv] += d[j][a] / delta;
+                }
             }
         }
     }

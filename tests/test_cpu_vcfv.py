@@ -138,7 +138,22 @@ def test_amg_backend_solves_the_vcfv_pattern():
     assert np.max(np.abs(x1 - x2)) <= 1e-5 * np.max(np.abs(x1))
 
 
-def test_refuses_what_it_does_not_model():
-    prob = problems.lens_vcfv(6, 4)
-    with pytest.raises(Exception):
-        O.Oracle(prob, _prm(local_linearizer=capi.LIN_FD))
+@pytest.mark.parametrize("method", [1, 0, -1])
+def test_fd_jacobian_approximates_the_ad_one(method):
+    """The finite-difference local linearizer on the vertex-centred stencil
+    (lens_immiscible_vcfv_fd): the same residual as the AD linearizer, a
+    Jacobian within the differencing error of the AD one."""
+    prob = problems.lens_vcfv(12, 8)
+    pv = _perturbed(prob)
+    out = []
+    for lin in (capi.LIN_AD, capi.LIN_FD):
+        o = O.Oracle(prob, _prm(local_linearizer=lin, numeric_difference_method=method))
+        assert o.linearize(250.0, 0) == 0
+        o.set_solution(pv, prob.init_meaning)
+        assert o.linearize(250.0, 1) == 0
+        out.append((o.residual(), o.jacobian()[2]))
+    (ra, ja), (rf, jf) = out
+    assert np.array_equal(ra, rf)
+    scale = np.max(np.abs(ja), axis=0)
+    # eps ~ 1e-10: the round-off of the residual over eps dominates
+    assert np.max(np.abs(jf - ja) / np.maximum(scale, 1e-300)) <= 2e-4

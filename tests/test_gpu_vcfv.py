@@ -3,7 +3,8 @@
 configuration) against the oracle's restatement (oracle/vcfv.hh): the
 residual and the 9-point Jacobian at the 1e-12 bar, the general block
 ILU(0) to the last bit, one solve, Newton through the lens time loop with
-ILU(0) and with AMG, and what it refuses."""
+ILU(0) and with AMG, the finite-difference linearizer, and what it
+refuses."""
 import numpy as np
 import pytest
 
@@ -142,11 +143,47 @@ def test_mixed_precision_meets_the_tolerance(built):
     assert np.max(np.abs(xg - x64)) <= 1e-6 * np.max(np.abs(x64))
 
 
+@pytest.mark.parametrize("method", [1, 0, -1])
+def test_fd_linearization_matches_the_oracle(built, method):
+    """The finite-difference local linearizer (lens_immiscible_vcfv_fd):
+    residual at 1e-12; the difference quotients at 1e-5 on the initial state
+    and 1e-3 on a randomly perturbed one -- the two sides' residuals differ
+    by rounding (the math library's pow in the material law, here up to
+    5e-14 of the summed terms), which the quotient divides by eps ~ 1e-10."""
+    prob = problems.lens_vcfv()
+    prm = _prm(local_linearizer=capi.LIN_FD, numeric_difference_method=method)
+    ctx = Context(prob, prm)
+    orc = O.Oracle(prob, prm)
+    er, ej = _compare(ctx, orc, 250.0, 0)
+    assert er <= RTOL_LIN and ej <= 1e-5, (er, ej)
+    pv = _perturbed(prob)
+    ctx.set_solution(pv, prob.init_meaning)
+    orc.set_solution(pv, prob.init_meaning)
+    er, ej = _compare(ctx, orc, 250.0, 1)
+    assert er <= RTOL_LIN and ej <= 1e-3, (er, ej)
+
+
+def test_fd_time_loop_matches_the_oracle(built):
+    prob = problems.lens_vcfv()
+    prm = _prm(local_linearizer=capi.LIN_FD, linear_tolerance=1e-10)
+    orc = O.Oracle(prob, prm)
+    ctx = Context(prob, prm)
+    so, dto, no, lo, _ = orc.time_integration(10, 250.0)
+    sg, dtg, ng, lg, _ = ctx.time_integration(10, 250.0)
+    assert so == 0 and sg == 0
+    assert np.array_equal(no, ng), (no, ng)
+    pvo, _ = orc.solution()
+    pvg, _ = ctx.solution()
+    assert rel_state_diff(pvg, pvo, 2) <= 1e-7
+
+
 def test_refuses_what_it_does_not_model(built):
     with pytest.raises(RuntimeError, match="ERR_UNSUPPORTED"):
-        Context(problems.lens_vcfv(6, 4), _prm(local_linearizer=capi.LIN_FD))
-    with pytest.raises(RuntimeError, match="ERR_UNSUPPORTED"):
         Context(problems.lens_vcfv(6, 4), _prm(linearizer=capi.LINEARIZER_TPFA))
-    ctx = Context(problems.lens_vcfv(6, 4), _prm())
-    import ctypes as C
-    assert ctx.lib.gbfv_set_params(ctx.h, C.byref(_prm(local_linearizer=capi.LIN_FD))) == capi.ERR_UNSUPPORTED
+    bad = problems.lens_vcfv(6, 4)
+    bad.elem_corner = bad.elem_corner.reshape(-1, 4)[:, [1, 0, 2, 3]].ravel().copy()
+    with pytest.raises(RuntimeError, match="ERR_UNSUPPORTED"):
+        Context(bad, _prm())
+    with pytest.raises(RuntimeError, match="ERR_UNSUPPORTED"):
+        from gbfv import Batch
+        Batch([problems.lens_vcfv(6, 4)], _prm())
