@@ -30,7 +30,7 @@ UNITS = {
     "vtk.cu": [],
     "problem.cu": [],
     "vcfv.cu": ["-fmad=false"],
-    "gilu.cu": ["-fmad=false"],
+    "gilu.cu": [],
 }
 
 

@@ -18,9 +18,12 @@
 // (block barriers) for systems whose levels fit a block, else a cooperative
 // grid with the bounded software barrier.  Block operations follow the
 // reference's order (FieldMatrix::rightmultiply, mmv, the cofactor
-// inverse), so with FMA contraction off the FP64 preconditioner is the
-// oracle's to the last bit.
+// inverse); the products are contracted to FMAs (on this GPU an FP64 warp
+// instruction is the scarce resource: contraction measured 1.6x faster
+// sweeps), so the FP64 preconditioner is the oracle's to rounding.
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -56,7 +59,13 @@ struct GiluArgs {
     DevStatus* st;
     double redTol, absTol, maxRes;
     int maxIter;
+    int warpSweep;       // one block, every level at most 32 rows, at most 4 lower / upper slots:
+                         // the narrow sweeps with the vectors in shared memory
+    unsigned long long* prof;  // optional phase timers (GBFV_GILU_PROFILE), 16 words
+    int localFactor;     // at most 9 slots and GILU_MAX_UPD updates per row: factorRowLocal
 };
+
+constexpr int WARP_SLOTS = 4;  // lower (and upper) slots the warp sweeps take
 
 template <class T, int B>
 __device__ __forceinline__ void ldBlk(const T* M, int s, int ld, int p, T (&o)[B * B])
@@ -125,11 +134,95 @@ __device__ bool factorRow(const GiluArgs<T>& a, int p)
     return true;
 }
 
+template <class T, int B>
+__device__ void narrowSweeps(const GiluArgs<T>& a, const T* d, T* v, unsigned char* smem);
+
+// row p of the factorization for patterns of at most 9 slots and 16
+// updates per row: the row's blocks, its lower neighbours' inverted pivots
+// and every upper block its updates read are loaded up front (one round of
+// independent loads), the row is factored in local arrays and stored once
+// -- the operations and their order are factorRow's
+constexpr int GILU_MAX_UPD = 16;
+template <class T, int B>
+__device__ bool factorRowLocal(const GiluArgs<T>& a, int p)
+{
+    const int ld = a.ld, ns = a.nslot, diag = a.diag;
+    const int q0 = a.updPtr[p], nu = a.updPtr[p + 1] - q0;
+    int k[9], up[GILU_MAX_UPD];
+#pragma unroll
+    for (int s = 0; s < 9; ++s) k[s] = s < ns ? a.col[(size_t)s * ld + p] : -1;
+#pragma unroll
+    for (int q = 0; q < GILU_MAX_UPD; ++q) up[q] = q < nu ? a.upd[q0 + q] : -1;
+    T Fr[9][B * B], Dk[WARP_SLOTS][B * B], U[GILU_MAX_UPD][B * B];
+#pragma unroll
+    for (int s = 0; s < 9; ++s)
+        if (s < ns)
+#pragma unroll
+            for (int e = 0; e < B * B; ++e) Fr[s][e] = a.A[((size_t)s * B * B + e) * ld + p];
+#pragma unroll
+    for (int s = 0; s < WARP_SLOTS; ++s)
+        if (s < diag && k[s] >= 0)
+#pragma unroll
+            for (int e = 0; e < B * B; ++e) Dk[s][e] = ldcg(&a.F[((size_t)diag * B * B + e) * ld + k[s]]);
+#pragma unroll
+    for (int q = 0; q < GILU_MAX_UPD; ++q)
+        if (up[q] >= 0) {
+            const int s = up[q] & 0xff, u = (up[q] >> 16) & 0xff;
+            const int kk = a.col[(size_t)s * ld + p];
+#pragma unroll
+            for (int e = 0; e < B * B; ++e) U[q][e] = ldcg(&a.F[((size_t)u * B * B + e) * ld + kk]);
+        }
+    int q = 0;
+#pragma unroll
+    for (int s = 0; s < WARP_SLOTS; ++s) {
+        if (s >= diag || k[s] < 0) continue;
+        T L[B * B];
+#pragma unroll
+        for (int i = 0; i < B; ++i)
+#pragma unroll
+            for (int j = 0; j < B; ++j) {
+                T t = T(0);
+#pragma unroll
+                for (int m = 0; m < B; ++m) t += Fr[s][i * B + m] * Dk[s][m * B + j];
+                L[i * B + j] = t;
+            }
+#pragma unroll
+        for (int e = 0; e < B * B; ++e) Fr[s][e] = L[e];
+        for (; q < nu && (up[q] & 0xff) == s; ++q) {
+            const int t = (up[q] >> 8) & 0xff;
+#pragma unroll
+            for (int i = 0; i < B; ++i)
+#pragma unroll
+                for (int j = 0; j < B; ++j) {
+                    T acc = T(0);
+#pragma unroll
+                    for (int m = 0; m < B; ++m) acc += L[i * B + m] * U[q][m * B + j];
+                    Fr[t][i * B + j] -= acc;
+                }
+        }
+    }
+    T R[B * B];
+    if (!invertBlock<T, B>(Fr[diag], R)) return false;
+#pragma unroll
+    for (int e = 0; e < B * B; ++e) Fr[diag][e] = R[e];
+#pragma unroll
+    for (int s = 0; s < 9; ++s)
+        if (s < ns)
+#pragma unroll
+            for (int e = 0; e < B * B; ++e) a.F[((size_t)s * B * B + e) * ld + p] = Fr[s][e];
+    return true;
+}
+
 // v = (LU)^-1 d: the forward sweep over the levels, then the backward one
 // (dune-istl's blockILUBacksolve)
 template <class T, int B, class Bar>
 __device__ bool iluApply(const GiluArgs<T>& a, const T* d, T* v, int gt, int gs, const Bar& bar)
 {
+    if (a.warpSweep) {
+        extern __shared__ __align__(16) unsigned char gsmem[];
+        narrowSweeps<T, B>(a, d, v, gsmem);
+        return bar();
+    }
     const int ld = a.ld;
     for (int l = 0; l < a.numLev; ++l) {
         for (int p = a.levPtr[l] + gt; p < a.levPtr[l + 1]; p += gs) {
@@ -181,12 +274,157 @@ __device__ bool iluApply(const GiluArgs<T>& a, const T* d, T* v, int gt, int gs,
     return true;
 }
 
+// ------------------------------------------------ narrow-system sweeps --
+// A system whose levels all have at most 32 rows sweeps with one warp: lane
+// r takes row r of every level (an FP64 warp instruction costs the same
+// with 5 active lanes as with 17, so spreading a level's rows over more
+// warps measured slower).  The sweep's input and output vectors live in
+// shared memory, and the block's other warps stream each level's column
+// indices and factor blocks into a shared-memory ring with cp.async,
+// GILU_AHEAD levels ahead of the sweep, so a level costs its FP64 work, a
+// few shared-memory round trips and one block barrier instead of a chain of
+// L2 loads (the sweeping warp staging its own copies measured slower).
+// Same operations in the same order as iluApply.
+constexpr int GILU_RING = 8;                // ring slots (levels in flight + 2)
+constexpr int GILU_AHEAD = GILU_RING - 2;   // a slot is refilled two levels after its use
+
+__device__ __forceinline__ void cpAsync(void* dst, const void* src, int bytes)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    if (bytes == 8) asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+    else asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cpCommit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cpWaitAhead() { asm volatile("cp.async.wait_group %0;\n" ::"n"(GILU_AHEAD) : "memory"); }
+__device__ __forceinline__ void cpWaitAll() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// planes of one ring slot: WARP_SLOTS blocks (and, backward, the inverted
+// pivot) of T per row, WARP_SLOTS column indices per row, 32 rows each
+template <class T, int B>
+struct Ring {
+    static constexpr int TP = (WARP_SLOTS + 1) * B * B;  // T planes
+    static constexpr int IP = WARP_SLOTS;                // int planes
+    static constexpr size_t bytes = (size_t)GILU_RING * 32 * (TP * sizeof(T) + IP * sizeof(int));
+    T* t;    // [slot][TP][32]
+    int* c;  // [slot][IP][32]
+};
+
+// shared-memory bytes of the narrow path: the ring, two vectors, the level pointers
+template <class T, int B>
+size_t narrowBytes(int N, int numLev)
+{
+    return Ring<T, B>::bytes + 2 * sizeof(T) * (size_t)N * B + sizeof(int) * (size_t)(numLev + 1);
+}
+
+// the staging warps: level l's data into ring slot l % GILU_RING (forward:
+// the lower slots in ascending order; backward: the upper slots in
+// descending order and the inverted pivot); one commit group per call,
+// empty past the ends
+template <class T, int B>
+__device__ __forceinline__ void stageLevel(const GiluArgs<T>& a, const Ring<T, B>& R, const int* lp, int l,
+                                           bool forward, int pt, int ps)
+{
+    if (l >= 0 && l < a.numLev) {
+        const int p0 = lp[l], rows = lp[l + 1] - p0, ld = a.ld, sl = l % GILU_RING;
+        T* rt = R.t + (size_t)sl * Ring<T, B>::TP * 32;
+        int* rc = R.c + (size_t)sl * Ring<T, B>::IP * 32;
+        const int nT = (forward ? WARP_SLOTS : WARP_SLOTS + 1) * B * B;
+        for (int q = pt; q < (nT + WARP_SLOTS) * rows; q += ps) {
+            const int plane = q / rows, r = q - plane * rows;
+            if (plane < nT) {
+                const int u = plane / (B * B), e = plane - u * B * B;
+                int slot;
+                if (forward) slot = u < a.diag ? u : -1;
+                else slot = u < WARP_SLOTS ? (a.nslot - 1 - u > a.diag ? a.nslot - 1 - u : -1) : a.diag;
+                if (slot >= 0) cpAsync(&rt[plane * 32 + r], &a.F[((size_t)slot * B * B + e) * ld + p0 + r], sizeof(T));
+            }
+            else {
+                const int u = plane - nT;
+                const int slot = forward ? u : a.nslot - 1 - u;
+                const bool ok = forward ? slot < a.diag : slot > a.diag;
+                if (ok) cpAsync(&rc[u * 32 + r], &a.col[(size_t)slot * ld + p0 + r], 4);
+                else rc[u * 32 + r] = -1;
+            }
+        }
+    }
+    cpCommit();
+}
+
+template <class T, int B>
+__device__ void narrowSweeps(const GiluArgs<T>& a, const T* d, T* v, unsigned char* smem)
+{
+    Ring<T, B> R;
+    R.t = reinterpret_cast<T*>(smem);
+    R.c = reinterpret_cast<int*>(smem + (size_t)GILU_RING * 32 * Ring<T, B>::TP * sizeof(T));
+    T* sd = reinterpret_cast<T*>(smem + Ring<T, B>::bytes);
+    T* sv = sd + (size_t)a.N * B;
+    int* lp = reinterpret_cast<int*>(sv + (size_t)a.N * B);  // the level pointers
+    const int lane = threadIdx.x & 31, nL = a.numLev;
+    const bool sweeper = threadIdx.x < 32;
+    const int pt = threadIdx.x - 32, ps = blockDim.x - 32;  // staging rank / count
+    for (int i = threadIdx.x; i < a.N * B; i += blockDim.x) sd[i] = ldcg(&d[i]);
+    for (int i = threadIdx.x; i <= nL; i += blockDim.x) lp[i] = a.levPtr[i];
+    __syncthreads();
+    for (int dir = 0; dir < 2; ++dir) {
+        const bool fw = dir == 0;
+        auto lev = [&](int step) { return fw ? step : nL - 1 - step; };
+        if (!sweeper)
+            for (int k = 0; k < GILU_AHEAD; ++k) stageLevel<T, B>(a, R, lp, lev(k), fw, pt, ps);
+        for (int step = 0; step < nL; ++step) {
+            if (!sweeper) {
+                stageLevel<T, B>(a, R, lp, lev(step + GILU_AHEAD), fw, pt, ps);
+                cpWaitAhead();  // the group of level `step` has landed
+            }
+            __syncthreads();
+            if (sweeper) {
+                const int l = lev(step), p0 = lp[l], rows = lp[l + 1] - p0, sl = l % GILU_RING;
+                if (lane < rows) {
+                    const int p = p0 + lane;
+                    const T* rt = R.t + (size_t)sl * Ring<T, B>::TP * 32;
+                    const int* rc = R.c + (size_t)sl * Ring<T, B>::IP * 32;
+                    T x[B];
+#pragma unroll
+                    for (int e = 0; e < B; ++e) x[e] = fw ? sd[p * B + e] : sv[p * B + e];
+#pragma unroll
+                    for (int u = 0; u < WARP_SLOTS; ++u) {
+                        const int k = rc[u * 32 + lane];
+                        if (k < 0) continue;
+#pragma unroll
+                        for (int i = 0; i < B; ++i)
+#pragma unroll
+                            for (int j = 0; j < B; ++j) x[i] -= rt[(u * B * B + i * B + j) * 32 + lane] * sv[k * B + j];
+                    }
+                    if (fw) {
+#pragma unroll
+                        for (int e = 0; e < B; ++e) sv[p * B + e] = x[e];
+                    }
+                    else {
+#pragma unroll
+                        for (int i = 0; i < B; ++i) {
+                            T t = T(0);
+#pragma unroll
+                            for (int j = 0; j < B; ++j) t += rt[(WARP_SLOTS * B * B + i * B + j) * 32 + lane] * x[j];
+                            sv[p * B + i] = t;
+                        }
+                    }
+                }
+            }
+        }
+        if (!sweeper) cpWaitAll();
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < a.N * B; i += blockDim.x) v[i] = sv[i];
+}
+
 template <class T, int B, class Bar>
 __device__ bool factorAll(const GiluArgs<T>& a, int gt, int gs, const Bar& bar)
 {
+    // one block: a level's rows round-robin over the warps, so its FP64 work
+    // spreads over the SM's sub-partitions
+    if (gridDim.x == 1) gt = (threadIdx.x & 31) * (blockDim.x >> 5) + (threadIdx.x >> 5);
     for (int l = 0; l < a.numLev; ++l) {
         for (int p = a.levPtr[l] + gt; p < a.levPtr[l + 1]; p += gs)
-            if (!factorRow<T, B>(a, p)) {
+            if (!(a.localFactor ? factorRowLocal<T, B>(a, p) : factorRow<T, B>(a, p))) {
                 atomicCAS(&a.st->code, 0, (int)GBFV_ERR_SINGULAR);
                 a.st->where = p;
             }
@@ -201,6 +439,30 @@ __device__ __forceinline__ void spmvRow(const GiluArgs<T>& a, const T* xin, int 
 {
 #pragma unroll
     for (int e = 0; e < B; ++e) acc[e] = T(0);
+    if (a.nslot <= 9) {
+        // up to nine slots: every column index, then every block and
+        // gathered value, issued before the first product
+        int k[9];
+#pragma unroll
+        for (int s = 0; s < 9; ++s) k[s] = s < a.nslot ? a.col[(size_t)s * a.ld + p] : -1;
+        T M[9][B * B], X[9][B];
+#pragma unroll
+        for (int s = 0; s < 9; ++s)
+            if (k[s] >= 0) {
+#pragma unroll
+                for (int e = 0; e < B * B; ++e) M[s][e] = a.A[((size_t)s * B * B + e) * a.ld + p];
+#pragma unroll
+                for (int j = 0; j < B; ++j) X[s][j] = ldcg(&xin[k[s] * B + j]);
+            }
+#pragma unroll
+        for (int s = 0; s < 9; ++s)
+            if (k[s] >= 0)
+#pragma unroll
+                for (int i = 0; i < B; ++i)
+#pragma unroll
+                    for (int j = 0; j < B; ++j) acc[i] += M[s][i * B + j] * X[s][j];
+        return;
+    }
     for (int s = 0; s < a.nslot; ++s) {
         const int k = a.col[(size_t)s * a.ld + p];
         if (k < 0) continue;
@@ -229,10 +491,15 @@ __global__ void __launch_bounds__(GILU_THREADS) kGiluBicgstab(const GiluArgs<T> 
     const int N = a.N;
     const GBar bar{&a.gs};
     const double eps = 2.2250738585072014e-308 * 1e10;  // numeric_limits<double>::min()*1e10
+    // optional timers: [0] factorization, [1] set-up, [2] p, [3] first
+    // preconditioner, [4] SpMV + dot, [5] x / r update, [6] second
+    // preconditioner, [7] SpMV + dots, [8] last update
+    PhaseClock clk(a.prof, gt);
     if (a.factor) {
         if (!factorAll<T, B>(a, gt, gs, bar)) goto timeout;
         if (*(volatile int*)&a.st->code != 0) return;
     }
+    clk.tick(0);
     {
         double mx[1] = {0.0};
         const bool isMax1[1] = {true};
@@ -292,6 +559,7 @@ __global__ void __launch_bounds__(GILU_THREADS) kGiluBicgstab(const GiluArgs<T> 
                 if (gt == 0) a.st->code = GBFV_ERR_BREAKDOWN;
                 break;
             }
+            clk.tick(1);
             const double beta = (rho_i / rho) * (alpha / omega);
             rho = rho_i;
             {
@@ -308,7 +576,9 @@ __global__ void __launch_bounds__(GILU_THREADS) kGiluBicgstab(const GiluArgs<T> 
                     }
                 if (!gridBarrier(a.gs)) goto timeout;
             }
+            clk.tick(2);
             if (!iluApply<T, B>(a, a.p, a.y, gt, gs, bar)) goto timeout;
+            clk.tick(3);
             {
                 double dd[1] = {0.0};
                 const bool isSum1[1] = {false};
@@ -334,6 +604,7 @@ __global__ void __launch_bounds__(GILU_THREADS) kGiluBicgstab(const GiluArgs<T> 
                     break;
                 }
                 alpha = rho_i / denom;
+                clk.tick(4);
                 if (fabs(alpha) <= eps) {
                     if (gt == 0) a.st->code = GBFV_ERR_BREAKDOWN;
                     break;
@@ -370,7 +641,9 @@ __global__ void __launch_bounds__(GILU_THREADS) kGiluBicgstab(const GiluArgs<T> 
                 }
                 if (stag || resErr > a.maxRes) break;
             }
+            clk.tick(5);
             if (!iluApply<T, B>(a, a.r, a.z, gt, gs, bar)) goto timeout;
+            clk.tick(6);
             {
                 double dd[2] = {0.0, 0.0};
                 const bool isSum2[2] = {false, false};
@@ -398,6 +671,7 @@ __global__ void __launch_bounds__(GILU_THREADS) kGiluBicgstab(const GiluArgs<T> 
                     break;
                 }
                 omega = tot2[1] / denom;
+                clk.tick(7);
                 if (fabs(omega) <= eps) {
                     if (gt == 0) a.st->code = GBFV_ERR_BREAKDOWN;
                     break;
@@ -425,6 +699,7 @@ __global__ void __launch_bounds__(GILU_THREADS) kGiluBicgstab(const GiluArgs<T> 
                 if (!gridBarrier(a.gs)) goto timeout;
                 double tot2[2];
                 allCombine<2, SYNC_GRID>(a.partial + 2 * tm.nblk * buf, kinds, tot2, tm);
+                clk.tick(8);
                 if (tot2[1] == 0.0) break;
             }
         }
@@ -457,6 +732,8 @@ __global__ void __launch_bounds__(GILU_THREADS) kGiluApply(const GiluArgs<T> a)
 
 struct GiluData {
     int N = 0, b = 0, nslot = 0, ld = 0, numLev = 0, blocks = 1, maxWidth = 0;
+    int warp = 0;  // narrow system: warp sweeps with the vector in shared memory
+    int localFactor = 0;  // rows factored in local arrays (factorRowLocal)
     const int* col = nullptr;  // not owned
     int* levPtr = nullptr;
     int* updPtr = nullptr;
@@ -469,6 +746,7 @@ struct GiluData {
     unsigned* bar = nullptr;
     cudaEvent_t evA = nullptr, evB = nullptr;
     size_t nnz = 0;
+    unsigned long long* prof = nullptr;  // GBFV_GILU_PROFILE phase timers
 };
 
 GiluData* giluCreate(int N, int b, int nslot, int ld, const std::vector<int>& colHost, const int* colDev,
@@ -522,6 +800,11 @@ GiluData* giluCreate(int N, int b, int nslot, int ld, const std::vector<int>& co
     }
     for (int s = 0; s < nslot; ++s)
         for (int p = 0; p < N; ++p) d->nnz += C(s, p) >= 0;
+    {
+        int maxUpd = 0;
+        for (int p = 0; p < N; ++p) maxUpd = std::max(maxUpd, updPtr[p + 1] - updPtr[p]);
+        d->localFactor = nslot <= 9 && diag <= WARP_SLOTS && maxUpd <= GILU_MAX_UPD;
+    }
     auto up = [&](int** dst, const std::vector<int>& v) {
         if (cudaMalloc((void**)dst, sizeof(int) * std::max<size_t>(1, v.size())) != cudaSuccess) return false;
         return v.empty() || cudaMemcpy(*dst, v.data(), sizeof(int) * v.size(), cudaMemcpyHostToDevice) == cudaSuccess;
@@ -543,6 +826,22 @@ GiluData* giluCreate(int N, int b, int nslot, int ld, const std::vector<int>& co
     int blocks = N <= 65536 ? 1 : std::min(maxCoop, std::max(1, (N + 4095) / 4096));
     if (const char* e = getenv("GBFV_GILU_BLOCKS")) blocks = std::max(1, std::min(maxCoop, atoi(e)));
     d->blocks = blocks;
+    // narrow systems: one block, every level within a warp, the ring and
+    // both sweep vectors (FP64) within 200 KB of shared memory
+    // (GBFV_GILU_WARP=0: off)
+    const int diagSlot = nslot / 2;
+    const size_t nb = b == 2 ? narrowBytes<double, 2>(N, d->numLev) : narrowBytes<double, 3>(N, d->numLev);
+    d->warp = blocks == 1 && d->maxWidth <= 32 && diagSlot <= WARP_SLOTS && nslot - 1 - diagSlot <= WARP_SLOTS &&
+              nb <= 200 * 1024;
+    if (const char* e = getenv("GBFV_GILU_WARP")) d->warp = d->warp && atoi(e) != 0;
+    if (d->warp) {
+        const int bytes = (int)nb;
+        for (const void* fn : {b == 2 ? (const void*)kGiluBicgstab<double, 2> : (const void*)kGiluBicgstab<double, 3>,
+                               b == 2 ? (const void*)kGiluBicgstab<float, 2> : (const void*)kGiluBicgstab<float, 3>,
+                               b == 2 ? (const void*)kGiluApply<double, 2> : (const void*)kGiluApply<double, 3>})
+            if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess)
+                d->warp = 0;
+    }
     const size_t nv = (size_t)N * b + 16;
     if (cudaMalloc((void**)&d->partial, sizeof(double) * 4 * (size_t)std::max(blocks, 16)) != cudaSuccess ||
         cudaMalloc((void**)&d->bar, 4 * sizeof(unsigned)) != cudaSuccess ||
@@ -568,6 +867,7 @@ void giluDestroy(GiluData* d)
     cudaFree(d->vec32);
     cudaFree(d->partial);
     cudaFree(d->bar);
+    cudaFree(d->prof);
     if (d->evA) cudaEventDestroy(d->evA);
     if (d->evB) cudaEventDestroy(d->evB);
     delete d;
@@ -616,14 +916,19 @@ int args(GiluData& d, GiluArgs<T>& a, const T* A, const T* rhs, DevStatus* st)
     a.gs.abort = (int*)(d.bar + 2);
     a.gs.perCluster = 0;
     a.st = st;
+    a.warpSweep = d.warp;
+    a.prof = d.prof;
+    a.localFactor = d.localFactor;
     return GBFV_OK;
 }
 
+// the sweep vector of the warp sweeps in shared memory: N * b values of T
 template <class T>
-int launch(const void* fn, GiluArgs<T>& a, int blocks, cudaStream_t s)
+int launch(const void* fn, GiluArgs<T>& a, int blocks, int b, cudaStream_t s)
 {
     void* argv[] = {(void*)&a};
-    const cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(GILU_THREADS), argv, 0, s);
+    const size_t smem = !a.warpSweep ? 0 : b == 2 ? narrowBytes<T, 2>(a.N, a.numLev) : narrowBytes<T, 3>(a.N, a.numLev);
+    const cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(GILU_THREADS), argv, smem, s);
     countLaunch();
     if (e != cudaSuccess) {
         setLastError(std::string("ILU(0) cooperative launch failed: ") + cudaGetErrorString(e));
@@ -646,12 +951,19 @@ int giluSolve(GiluData* d, const T* A, const T* rhs, T* x, int factor, double re
     a.absTol = absTol;
     a.maxRes = maxRes;
     a.maxIter = maxIter;
+    const char* profFile = getenv("GBFV_GILU_PROFILE");
+    if (profFile && !d->prof) {
+        if (cudaMalloc((void**)&d->prof, 16 * sizeof(unsigned long long)) != cudaSuccess) return GBFV_ERR_OOM;
+        a.prof = d->prof;
+    }
+    if (d->prof && cudaMemsetAsync(d->prof, 0, 16 * sizeof(unsigned long long), s) != cudaSuccess)
+        return GBFV_ERR_CUDA;
     if (cudaMemsetAsync(st, 0, sizeof(DevStatus), s) != cudaSuccess ||
         cudaMemsetAsync(d->bar, 0, 4 * sizeof(unsigned), s) != cudaSuccess)
         return GBFV_ERR_CUDA;
     cudaEventRecord(d->evA, s);
     const void* fn = d->b == 2 ? (const void*)kGiluBicgstab<T, 2> : (const void*)kGiluBicgstab<T, 3>;
-    if ((rs = launch<T>(fn, a, d->blocks, s))) return rs;
+    if ((rs = launch<T>(fn, a, d->blocks, d->b, s))) return rs;
     if (cudaMemcpyAsync(x, a.x, sizeof(T) * (size_t)d->N * d->b, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
         return GBFV_ERR_CUDA;
     cudaEventRecord(d->evB, s);
@@ -662,6 +974,18 @@ int giluSolve(GiluData* d, const T* A, const T* rhs, T* x, int factor, double re
     }
     iters = hst->iterations;
     if (ms) cudaEventElapsedTime(ms, d->evA, d->evB);
+    if (profFile && d->prof) {
+        // one JSON line per solve: nanoseconds per phase
+        unsigned long long h[16];
+        if (cudaMemcpy(h, d->prof, sizeof(h), cudaMemcpyDeviceToHost) == cudaSuccess)
+            if (FILE* f = std::fopen(profFile, "a")) {
+                std::fprintf(f, "{\"rows\": %d, \"levels\": %d, \"narrow\": %d, \"iterations\": %d, \"ns\": [", d->N,
+                             d->numLev, d->warp, iters);
+                for (int k = 0; k < 9; ++k) std::fprintf(f, "%s%llu", k ? ", " : "", h[k]);
+                std::fprintf(f, "]}\n");
+                std::fclose(f);
+            }
+    }
     if (bytes) {
         // per iteration: 2 sweeps over the factors (every stored block once
         // per application) and 2 SpMVs over A, plus the vector updates
@@ -684,7 +1008,7 @@ int giluApply64(GiluData* d, const double* A, const double* dv, double* v, cudaS
         cudaMemsetAsync(d->bar, 0, 4 * sizeof(unsigned), s) != cudaSuccess)
         return GBFV_ERR_CUDA;
     const void* fn = d->b == 2 ? (const void*)kGiluApply<double, 2> : (const void*)kGiluApply<double, 3>;
-    if ((rs = launch<double>(fn, a, d->blocks, s))) return rs;
+    if ((rs = launch<double>(fn, a, d->blocks, d->b, s))) return rs;
     if (cudaMemcpyAsync(v, a.x, sizeof(double) * (size_t)d->N * d->b, cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
         cudaMemcpyAsync(hst, st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)

@@ -2,7 +2,7 @@
 0: VcfvDiscretization with P1 or two-point gradients, the lens VCFV tests'
 configuration) against the oracle's restatement (oracle/vcfv.hh): the
 residual and the 9-point Jacobian at the 1e-12 bar, the general block
-ILU(0) to the last bit, one solve, Newton through the lens time loop with
+ILU(0) to rounding, one solve, Newton through the lens time loop with
 ILU(0) and with AMG, the finite-difference linearizer, and what it
 refuses."""
 import numpy as np
@@ -69,10 +69,11 @@ def test_residual_agrees_to_rounding(built):
     assert residual_mismatch(ctx.residual(), orc.residual(), orc.residual_scale()) <= 1e-14
 
 
-def test_general_ilu0_matches_the_oracle_to_the_last_bit(built):
+def test_general_ilu0_matches_the_oracle(built):
     """The block ILU(0) of the 9-point Jacobian (lower entries updating the
     whole shared part of the row) applied once, FP64: the oracle's
-    blockILU0Decomposition + back-solve in the same order."""
+    blockILU0Decomposition + back-solve in the same order, to rounding (the
+    device contracts products to FMAs)."""
     prob = problems.lens_vcfv()
     orc = O.Oracle(prob, _prm())
     assert orc.time_integration(2, 250.0)[0] == 0
@@ -86,7 +87,7 @@ def test_general_ilu0_matches_the_oracle_to_the_last_bit(built):
         st, _, vo = O.ilu0(rp, col, blk, d)
         assert st == 0
         vg = ls.ilu0_apply(d)
-        assert np.array_equal(vg, vo), np.max(np.abs(vg - vo))
+        assert np.max(np.abs(vg - vo)) <= 1e-13 * np.max(np.abs(vo)), np.max(np.abs(vg - vo))
 
 
 def test_one_solve_matches_the_oracle(built):
