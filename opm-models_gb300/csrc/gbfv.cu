@@ -144,8 +144,11 @@ struct SolverData {
     // first AMG solve; natural row of every internal row
     AmgData* amg = nullptr;
     std::vector<int> natural;
-    // block ILU(0) of a general pattern (vertex-centred grids), else NULL
+    // block ILU(0) of a general pattern (vertex-centred grids), or of a
+    // narrow structured system (giluRoute: every level at most 32 rows, see
+    // createImpl), else NULL
     GiluData* gilu = nullptr;
+    bool giluRoute = false;
     // max-norm residual reduction the last solve reached: the FP64 true
     // residual for the mixed form, BiCGStab's residual for the plain one
     double lastReduction = 0.0, lastResidual = 0.0;
@@ -1750,6 +1753,23 @@ static int createImpl(gbfv_ctx* C, const gbfv_problem* P)
     }
     if ((st = upload(&S.col, hCol)) || (st = upload(&S.levPtrD, levPtr))) return st;
     if ((st = allocSolver(S))) return st;
+    // Narrow systems (every wavefront level at most 32 rows, e.g. the 48 x 32
+    // lens; two-phase systems) solve faster with the general kernel's
+    // one-warp sweeps over shared memory than with the cluster sweeps: the
+    // same ILU(0) (no fill interactions here, so the same factors), one
+    // block.  A forced solver
+    // configuration (GBFV_SOLVER, gbfv_set_solver_config) or GBFV_NARROW=0
+    // keeps the structured solver.
+    {
+        int maxW = 0;
+        for (size_t l = 0; l + 1 < levPtr.size(); ++l) maxW = std::max(maxW, levPtr[l + 1] - levPtr[l]);
+        const char* nv = getenv("GBFV_NARROW");
+        if (b == 2 && maxW <= 32 && N <= 16384 && !getenv("GBFV_SOLVER") && !(nv && atoi(nv) == 0)) {
+            int gst = GBFV_OK;
+            S.gilu = giluCreate(N, b, nslot, ld, hCol, S.col, levPtr, &gst);
+            S.giluRoute = S.gilu != nullptr;
+        }
+    }
     if ((st = devAlloc(&C->st, 1))) return st;
     CK(cudaMallocHost((void**)&C->hst, sizeof(DevStatus)));
     CK(cudaMemset(C->st, 0, sizeof(DevStatus)));
@@ -2245,6 +2265,10 @@ int gbfv_set_solver_config(gbfv_ctx* C, int precision, int mode, int blocks)
         ((mode & SYNC_NARROW) && (base != SYNC_HYBRID || k != 1 || (mode & SYNC_TILES))))
         return GBFV_ERR_ARG;
     SolverData& S = C->S;
+    if (S.gilu && !S.giluRoute) {
+        setError("a vertex-centred context solves with the general block ILU(0) only");
+        return GBFV_ERR_UNSUPPORTED;
+    }
     const int maxH = (mode & SYNC_NARROW) ? S.maxHybridNarrow : S.maxHybrid[k];
     if (base == SYNC_CLUSTER && blocks > S.maxCluster[k]) return GBFV_ERR_UNSUPPORTED;
     if (base == SYNC_HYBRID && (blocks > maxH || blocks % HYBRID_CLUSTER || blocks <= HYBRID_CLUSTER))
@@ -2259,6 +2283,11 @@ int gbfv_set_solver_config(gbfv_ctx* C, int precision, int mode, int blocks)
     S.mode[k] = mode;
     S.nblk[k] = blocks;
     S.tuned[k] = 1;
+    if (S.giluRoute) {  // a forced configuration of the structured solver
+        giluDestroy(S.gilu);
+        S.gilu = nullptr;
+        S.giluRoute = false;
+    }
     return GBFV_OK;
 }
 
