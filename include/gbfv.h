@@ -576,9 +576,16 @@ typedef struct gbfv_restart_info {
     double time;
     int32_t vtk_section;         /* 1: with the VTKMultiWriter section       */
     int32_t vtk_writer_num;      /* its curWriterNum_                        */
+    int32_t entity_codim;        /* codimension of the entities: 0 elements
+                                    (ECFV), the grid dimension for vertices
+                                    (VCFV, vcfvdiscretization.hh:185-200)   */
+    int32_t num_elements;        /* gridView.size(0) (cookie) when the
+                                    entities are vertices; with codim 0 the
+                                    cells are the elements                   */
 } gbfv_restart_info;
-/* the file's text for num_cells cells of b primary variables (natural
- * order) and, for black-oil, their gas meanings (NULL: immiscible); *len =
+/* the file's text for num_cells entities (cells, or the vertices of a
+ * vertex-centred grid) of b primary variables (natural order) and, for
+ * black-oil, their gas meanings (NULL: immiscible); *len =
  * its size in bytes; buf NULL asks for the size only                      */
 int gbfv_format_restart(const gbfv_restart_info* info, int32_t num_cells, int32_t b, const double* pv,
                         const int32_t* gas_meaning, char* buf, size_t cap, size_t* len);
@@ -635,10 +642,16 @@ typedef struct gbfv_vtk_grid {
     const double* points;          /* [num_points*3]                      */
     int32_t vertices_per_cell;     /* 4 or 8                               */
     const int32_t* cell_vertices;  /* [num_cells*vertices_per_cell]        */
+    int32_t num_cells;             /* 0: the context's cells (cell data);
+                                      > 0: that many cells of a vertex-centred
+                                      grid whose num_points vertices are the
+                                      context's degrees of freedom (vertex
+                                      data, VcfvBaseOutputModule)           */
 } gbfv_vtk_grid;
 /* One time step's XML UnstructuredGrid file (.vtu, ASCII as the
  * reference's default VtkOutputFormat, fvbasediscretization.hh:237-238):
- * the selected fields as Float32 cell data, each value rounded to float as
+ * the selected fields as Float32 cell data (point data on a vertex-centred
+ * grid), each value rounded to float as
  * VtkScalarFunction::evaluate does (vtkscalarfunction.hh:76-110), in the
  * modules' order and with their names ("pressure_<phase>", ...,
  * "porosity", "PV_<primary variable>", "DOF index").                     */

@@ -320,6 +320,7 @@ struct gbfv_ctx {
     std::vector<void*> owned;
     // vertex-centred grid: element geometry, incidence and scratch (else NULL)
     VcfvDev* vcfv = nullptr;
+    int numElements = 0;
     // natural BCRS view
     std::vector<int> bcrsRowPtr, bcrsCol, bcrsSlot, bcrsRow;
     double dt = 1.0;
@@ -1250,6 +1251,7 @@ static int createVcfvImpl(gbfv_ctx* C, const gbfv_problem* P)
     CK(cudaMemcpy(C->dphys, &ph, sizeof(DevPhysics), cudaMemcpyHostToDevice));
     C->vcfv = vcfvUpload(P, vs, ph, perm, ld, &st);
     if (!C->vcfv) return st;
+    C->numElements = P->num_elements;
     // state
     const size_t nb = (size_t)N * b;
     if ((st = devAlloc(&C->x, nb)) || (st = devAlloc(&C->xOld, nb)) || (st = devAlloc(&C->residual, nb)) ||
@@ -2216,6 +2218,18 @@ int gbfv_newton_update(gbfv_ctx* C, int* switched)
 }
 
 void* gbfv_stream(gbfv_ctx* C) { return C ? (void*)C->stream : nullptr; }
+
+}  // extern "C"
+
+namespace gbfv {
+void entitiesOf(const gbfv_ctx* C, int32_t& codim, int32_t& numElements)
+{
+    codim = C->vcfv ? C->dim : 0;
+    numElements = C->vcfv ? C->numElements : 0;
+}
+}  // namespace gbfv
+
+extern "C" {
 
 int gbfv_save_state(gbfv_ctx* C)
 {

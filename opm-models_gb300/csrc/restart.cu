@@ -39,16 +39,31 @@
 
 namespace gbfv {
 void setLastError(const std::string& s);
+// the context's restart entities: codim 0 (cells) or, on a vertex-centred
+// grid, its dimension (vertices) and the element count
+void entitiesOf(const gbfv_ctx* ctx, int32_t& codim, int32_t& numElements);
 }
 
 namespace {
+
+// the entities are the cells (codim 0) or, on a vertex-centred grid, the
+// vertices; the cookie's element count follows
+int numElementsOf(const gbfv_restart_info& in, int numCells)
+{
+    return in.entity_codim > 0 ? in.num_elements : numCells;
+}
+
+std::string entitiesLine(const gbfv_restart_info& in)
+{
+    return "Entities: Codim " + std::to_string(in.entity_codim);
+}
 
 std::string cookie(const gbfv_restart_info& in, int numCells)
 {
     char buf[256];
     snprintf(buf, sizeof buf,
              "eWoms restart file: gridName='blubb' numCPUs=%d myRank=%d numElements=%d numEdges=%d numVertices=%d",
-             in.num_cpus, in.rank, numCells, in.num_edges, in.num_vertices);
+             in.num_cpus, in.rank, numElementsOf(in, numCells), in.num_edges, in.num_vertices);
     return buf;
 }
 
@@ -104,7 +119,7 @@ std::string formatRestart(const gbfv_restart_info& in, int numCells, int b, cons
         putI(s, in.vtk_writer_num);
         s += "\n0  0\n\n";
     }
-    s += "Entities: Codim 0\n";
+    s += entitiesLine(in) + "\n";
     const int nt = numCells < 65536 ? 1
                                     : (int)std::min<unsigned>(16u, std::max(1u, std::thread::hardware_concurrency()));
     std::vector<std::string> part(nt);
@@ -227,8 +242,8 @@ int parseRestart(const char* text, size_t len, const gbfv_restart_info& expect, 
         r.p += (size_t)metaLen;  // the meta file's bytes
         if (!sectionEnd(r, "the VTKMultiWriter section") || !r.line(l)) return GBFV_ERR_ARG;
     }
-    if (l != "Entities: Codim 0") {
-        gbfv::setLastError("restart file: expected section 'Entities: Codim 0'");
+    if (l != entitiesLine(expect)) {
+        gbfv::setLastError("restart file: expected section '" + entitiesLine(expect) + "'");
         return GBFV_ERR_ARG;
     }
     // the entity lines: located in one pass, parsed by several threads
@@ -321,7 +336,9 @@ extern "C" {
 int gbfv_format_restart(const gbfv_restart_info* info, int32_t num_cells, int32_t b, const double* pv,
                         const int32_t* gas_meaning, char* buf, size_t cap, size_t* len)
 {
-    if (!info || num_cells < 0 || b < 1 || b > 8 || (num_cells > 0 && !pv) || !len) return GBFV_ERR_ARG;
+    if (!info || num_cells < 0 || b < 1 || b > 8 || (num_cells > 0 && !pv) || !len || info->entity_codim < 0 ||
+        info->entity_codim > 3)
+        return GBFV_ERR_ARG;
     const std::string s = formatRestart(*info, num_cells, b, pv, gas_meaning);
     *len = s.size();
     if (buf) {
@@ -334,7 +351,9 @@ int gbfv_format_restart(const gbfv_restart_info* info, int32_t num_cells, int32_
 int gbfv_parse_restart(const char* text, size_t len, const gbfv_restart_info* expect, int32_t num_cells, int32_t b,
                        double* pv, int32_t* gas_meaning, gbfv_restart_info* out)
 {
-    if (!text || !expect || num_cells < 0 || b < 1 || b > 8 || (num_cells > 0 && !pv) || !out) return GBFV_ERR_ARG;
+    if (!text || !expect || num_cells < 0 || b < 1 || b > 8 || (num_cells > 0 && !pv) || !out ||
+        expect->entity_codim < 0 || expect->entity_codim > 3)
+        return GBFV_ERR_ARG;
     return parseRestart(text, len, *expect, num_cells, b, pv, gas_meaning, *out);
 }
 
@@ -357,12 +376,15 @@ int gbfv_restart_file_name(const char* output_dir, const char* sim_name, double 
     return GBFV_OK;
 }
 
-int gbfv_write_restart(gbfv_ctx* ctx, const char* path, const gbfv_restart_info* info)
+int gbfv_write_restart(gbfv_ctx* ctx, const char* path, const gbfv_restart_info* infoIn)
 {
-    if (!ctx || !path || !info) return GBFV_ERR_ARG;
+    if (!ctx || !path || !infoIn) return GBFV_ERR_ARG;
     int n = 0, b = 0, nnz = 0;
     int st = gbfv_dims(ctx, &n, &b, &nnz);
     if (st) return st;
+    gbfv_restart_info in = *infoIn;
+    gbfv::entitiesOf(ctx, in.entity_codim, in.num_elements);
+    const gbfv_restart_info* info = &in;
     std::vector<double> pv((size_t)n * b);
     std::vector<int32_t> gas(b == 3 ? n : 0);
     if ((st = gbfv_get_solution(ctx, pv.data(), b == 3 ? gas.data() : nullptr))) return st;
@@ -386,6 +408,7 @@ int gbfv_read_restart(gbfv_ctx* ctx, const char* path, gbfv_restart_info* info)
     int n = 0, b = 0, nnz = 0;
     int st = gbfv_dims(ctx, &n, &b, &nnz);
     if (st) return st;
+    gbfv::entitiesOf(ctx, info->entity_codim, info->num_elements);
     std::string text;
     if (!readFile(path, text)) {
         gbfv::setLastError(std::string("gbfv_read_restart: cannot read ") + path);

@@ -123,8 +123,16 @@ int gbfv_write_vtk(gbfv_ctx* ctx, const gbfv_vtk_grid* g, int32_t fields, const 
     int N = 0, b = 0, nnz = 0;
     int st = gbfv_dims(ctx, &N, &b, &nnz);
     if (st) return st;
+    // a vertex-centred grid: the degrees of freedom are the points
+    const bool pointData = g->num_cells > 0;
+    if (g->num_cells < 0 || (pointData && g->num_points != N)) {
+        gbfv::setLastError("gbfv_write_vtk: num_cells < 0, or vertex data with num_points other than the "
+                           "context's degrees of freedom");
+        return GBFV_ERR_ARG;
+    }
+    const int NC = pointData ? g->num_cells : N;
     const size_t vpc = (size_t)g->vertices_per_cell;
-    for (size_t k = 0; k < (size_t)N * vpc; ++k)
+    for (size_t k = 0; k < (size_t)NC * vpc; ++k)
         if (g->cell_vertices[k] < 0 || g->cell_vertices[k] >= g->num_points) {
             gbfv::setLastError("gbfv_write_vtk: cell vertex index out of range at entry " + std::to_string(k));
             return GBFV_ERR_ARG;
@@ -174,20 +182,22 @@ int gbfv_write_vtk(gbfv_ctx* ctx, const gbfv_vtk_grid* g, int32_t fields, const 
     }
     std::vector<float> pts((size_t)g->num_points * 3);
     for (size_t k = 0; k < pts.size(); ++k) pts[k] = (float)g->points[k];
-    std::vector<int32_t> offsets(N);
-    std::vector<uint8_t> types(N, (uint8_t)(vpc == 4 ? 9 : 12));  // VTK_QUAD, VTK_HEXAHEDRON
-    for (int i = 0; i < N; ++i) offsets[i] = (int32_t)((size_t)(i + 1) * vpc);
+    std::vector<int32_t> offsets(NC);
+    std::vector<uint8_t> types(NC, (uint8_t)(vpc == 4 ? 9 : 12));  // VTK_QUAD, VTK_HEXAHEDRON
+    for (int i = 0; i < NC; ++i) offsets[i] = (int32_t)((size_t)(i + 1) * vpc);
     std::string doc = "<?xml version=\"1.0\"?>\n"
                       "<VTKFile type=\"UnstructuredGrid\" version=\"0.1\" byte_order=\"LittleEndian\">\n"
                       "  <UnstructuredGrid>\n"
-                      "    <Piece NumberOfCells=\"" + std::to_string(N) + "\" NumberOfPoints=\"" +
+                      "    <Piece NumberOfCells=\"" + std::to_string(NC) + "\" NumberOfPoints=\"" +
                       std::to_string(g->num_points) + "\">\n";
-    if (!first.empty()) doc += "      <CellData Scalars=\"" + first + "\">\n" + cells + "      </CellData>\n";
+    const char* section = pointData ? "PointData" : "CellData";
+    if (!first.empty())
+        doc += std::string("      <") + section + " Scalars=\"" + first + "\">\n" + cells + "      </" + section + ">\n";
     doc += "      <Points>\n" + floatArray("Coordinates", 3, (size_t)g->num_points, pts.data()) + "      </Points>\n";
     doc += "      <Cells>\n";
-    doc += intArray("Int32", "connectivity", (size_t)N * vpc, g->cell_vertices);
-    doc += intArray("Int32", "offsets", (size_t)N, offsets.data());
-    doc += intArray("UInt8", "types", (size_t)N, types.data());
+    doc += intArray("Int32", "connectivity", (size_t)NC * vpc, g->cell_vertices);
+    doc += intArray("Int32", "offsets", (size_t)NC, offsets.data());
+    doc += intArray("UInt8", "types", (size_t)NC, types.data());
     doc += "      </Cells>\n    </Piece>\n  </UnstructuredGrid>\n</VTKFile>\n";
     if (!writeFile(path, doc)) {
         gbfv::setLastError(std::string("gbfv_write_vtk: cannot write ") + path);

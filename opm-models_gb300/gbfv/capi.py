@@ -186,7 +186,7 @@ class RestartInfo(C.Structure):
                 ("num_vertices", C.c_int32), ("episode_index", C.c_int32), ("time_step_index", C.c_int32),
                 ("episode_start_time", C.c_double), ("episode_length", C.c_double),
                 ("start_time", C.c_double), ("time", C.c_double), ("vtk_section", C.c_int32),
-                ("vtk_writer_num", C.c_int32)]
+                ("vtk_writer_num", C.c_int32), ("entity_codim", C.c_int32), ("num_elements", C.c_int32)]
 
 
 _LIB = None

@@ -10,12 +10,15 @@ from . import capi
 
 
 def info(num_edges, num_vertices, time=0.0, time_step_index=0, episode_index=0, episode_start_time=0.0,
-         episode_length=0.0, start_time=0.0, vtk_section=True, vtk_writer_num=0, num_cpus=1, rank=0):
+         episode_length=0.0, start_time=0.0, vtk_section=True, vtk_writer_num=0, num_cpus=1, rank=0,
+         entity_codim=0, num_elements=0):
     """gbfv_restart_info for a grid with the given edge and vertex counts
-    (gridView.size(dim-1), gridView.size(dim)) and the Simulator's clock."""
+    (gridView.size(dim-1), gridView.size(dim)) and the Simulator's clock;
+    entity_codim / num_elements for the vertices of a vertex-centred grid
+    (a context sets both itself when it writes or reads)."""
     return capi.RestartInfo(num_cpus, rank, num_edges, num_vertices, episode_index, time_step_index,
                             episode_start_time, episode_length, start_time, time, 1 if vtk_section else 0,
-                            vtk_writer_num)
+                            vtk_writer_num, entity_codim, num_elements)
 
 
 def cartesian_counts(shape):

@@ -16,12 +16,20 @@ DEFAULT_FIELDS = PRESSURE | DENSITY | SATURATION | RELPERM | POROSITY
 
 class VtkGrid(C.Structure):
     _fields_ = [("num_points", C.c_int32), ("points", C.POINTER(C.c_double)),
-                ("vertices_per_cell", C.c_int32), ("cell_vertices", C.POINTER(C.c_int32))]
+                ("vertices_per_cell", C.c_int32), ("cell_vertices", C.POINTER(C.c_int32)),
+                ("num_cells", C.c_int32)]
 
 
 def structured_points(problem):
     """Vertices and cells (VTK vertex order) of a problem built on
-    problems.structured_grid: (points [P, 3], cells [N, 4 or 8])."""
+    problems.structured_grid: (points [P, 3], cells [N, 4 or 8]).  For a
+    vertex-centred problem (problems.lens_vcfv) the points are its degrees
+    of freedom and the cells its elements (corners 0, 1, 3, 2 of the
+    reference element: counter-clockwise)."""
+    if getattr(problem, "elem_corner", None) is not None:
+        pts = np.ascontiguousarray(problem.center.reshape(-1, 3), float)
+        cells = problem.elem_corner.reshape(-1, 4)[:, [0, 1, 3, 2]]
+        return pts, np.ascontiguousarray(cells, np.int32)
     g = problem.grid
     nx, ny, dim = g["nx"], g["ny"], g["dim"]
     nz = g["nz"] if dim == 3 else 1
@@ -66,8 +74,10 @@ class MultiWriter:
 
     def __init__(self, problem, output_dir=".", sim_name="sim", fields=DEFAULT_FIELDS):
         self.pts, self.cells = structured_points(problem)
+        vertex_data = getattr(problem, "elem_corner", None) is not None
         self.grid = VtkGrid(len(self.pts), self.pts.ctypes.data_as(C.POINTER(C.c_double)), self.cells.shape[1],
-                            self.cells.ctypes.data_as(C.POINTER(C.c_int32)))
+                            self.cells.ctypes.data_as(C.POINTER(C.c_int32)),
+                            len(self.cells) if vertex_data else 0)
         self.dir, self.sim, self.fields = output_dir, sim_name or "sim", fields
         self.times, self.files = [], []
 

@@ -12,6 +12,8 @@ be built here); the layout follows the reference's source text:
                           fvbaseproblem.hh:755-760, vtkmultiwriter.hh:408-437
   EcfvDiscretization::serialize (codim 0)
                           ecfvdiscretization.hh:212-213
+  VcfvDiscretization::serialize (codim dim: the vertices)
+                          vcfvdiscretization.hh:185-200
   FvBaseDiscretization::serializeEntity
                           fvbasediscretization.hh:1440-1454
   BlackOilModel::serializeEntity
@@ -34,13 +36,16 @@ def cookie(num_cpus, rank, num_elements, num_edges, num_vertices):
 
 def format_restart(pv, gas_meaning=None, *, num_edges, num_vertices, num_cpus=1, rank=0, episode_index=0,
                    episode_start_time=0.0, episode_length=0.0, start_time=0.0, time=0.0, time_step_index=0,
-                   vtk_section=True, vtk_writer_num=0):
+                   vtk_section=True, vtk_writer_num=0, entity_codim=0, num_elements=None):
     """Text of the restart file of primary variables pv (num_cells x b,
     natural cell order); gas_meaning (black-oil) adds the meanings and the
-    PVT region after the variables (water Sw = 0, pressure Po = 0, region 0)."""
+    PVT region after the variables (water Sw = 0, pressure Po = 0, region 0).
+    entity_codim > 0: the entities are a vertex-centred grid's vertices and
+    num_elements its element count (the cookie's numElements)."""
     out = []
     # serializeBegin: the cookie section (no content)
-    out.append(cookie(num_cpus, rank, len(pv), num_edges, num_vertices) + "\n")
+    ne = len(pv) if entity_codim == 0 else num_elements
+    out.append(cookie(num_cpus, rank, ne, num_edges, num_vertices) + "\n")
     out.append("\n")
     # Simulator section: six values, each followed by a blank, then the end
     out.append("Simulator\n")
@@ -53,7 +58,7 @@ def format_restart(pv, gas_meaning=None, *, num_edges, num_vertices, num_cpus=1,
         out.append("%d\n" % vtk_writer_num)
         out.append("0  0\n")
         out.append("\n")
-    out.append("Entities: Codim 0\n")
+    out.append("Entities: Codim %d\n" % entity_codim)
     for c, row in enumerate(pv):
         line = "".join(_g(v) + " " for v in row)
         if gas_meaning is not None:

@@ -18,6 +18,11 @@
 // the context calls of gbfv_write_restart / gbfv_read_restart (not used here)
 namespace gbfv {
 void setLastError(const std::string&) {}
+void entitiesOf(const gbfv_ctx*, int32_t& codim, int32_t& numElements)
+{
+    codim = 0;
+    numElements = 0;
+}
 }
 extern "C" {
 int gbfv_dims(const gbfv_ctx*, int*, int*, int*) { return GBFV_ERR_ARG; }

@@ -62,3 +62,33 @@ def test_read_rejects_another_grid(built, tmp_path):
     with pytest.raises(Exception):
         ctx.read_restart(path, restart.info(edges, verts + 1))
     ctx.close()
+
+
+def test_vertex_centred_stop_write_read_continue(built, tmp_path):
+    """The vertex-centred lens: the context writes its vertices (codim 2,
+    the element count in the cookie) and a fresh context continues from the
+    file to the bits of the run that was not stopped."""
+    prob, dt = problems.lens_vcfv(), 250.0
+    prm = capi.default_params(linear_tolerance=1e-8)
+    edges, verts = restart.cartesian_counts((48, 32))
+    a = Context(prob, prm)
+    assert a.time_integration(4, dt, fixed_dt=True)[0] == 0
+    xa, _ = a.solution()
+    a.close()
+    b = Context(prob, prm)
+    assert b.time_integration(2, dt, fixed_dt=True)[0] == 0
+    path = str(tmp_path / "vcfv.ers")
+    b.write_restart(path, restart.info(edges, verts, time=2 * dt, time_step_index=2))
+    xb, _ = b.solution()
+    b.close()
+    with open(path, "rb") as f:
+        text = f.read()
+    assert text == R.format_restart(xb.reshape(-1, 2), None, num_edges=edges, num_vertices=verts, time=2 * dt,
+                                    time_step_index=2, entity_codim=2, num_elements=48 * 32)
+    c = Context(prob, prm)
+    out = c.read_restart(path, restart.info(edges, verts))
+    assert out.time == 2 * dt
+    assert c.time_integration(2, dt, fixed_dt=True)[0] == 0
+    xc, _ = c.solution()
+    c.close()
+    assert np.array_equal(xc, xa)

@@ -151,3 +151,26 @@ def test_large_state_formatted_and_parsed_by_threads():
     assert text == R.format_restart(pv, gm, num_edges=7, num_vertices=9, time=5.0)
     st, pv2, gm2, _ = restart.parse_restart(text, inf, n, 3, blackoil=True)
     assert st == 0 and np.array_equal(pv, pv2) and np.array_equal(gm, gm2)
+
+
+def test_vertex_centred_entities_are_the_vertices():
+    """A vertex-centred state (VcfvDiscretization::serialize writes the
+    entities of codimension dim): the section names codim 2, the cookie the
+    element count, one line per vertex; parsed back bit for bit."""
+    prob = problems.lens_vcfv(12, 8)
+    orc = O.Oracle(prob, capi.default_params(linear_tolerance=1e-6))
+    assert orc.time_integration(2, 250.0)[0] == 0
+    x, _ = orc.solution()
+    pv = x.reshape(-1, 2)
+    edges, verts = restart.cartesian_counts((12, 8))
+    inf = restart.info(edges, verts, time=500.0, time_step_index=2, entity_codim=2, num_elements=96)
+    got = restart.format_restart(inf, pv)
+    want = R.format_restart(pv, num_edges=edges, num_vertices=verts, time=500.0, time_step_index=2,
+                            entity_codim=2, num_elements=96)
+    assert got == want
+    assert b"numElements=96 " in got and b"\nEntities: Codim 2\n" in got
+    st, back, _, out = restart.parse_restart(got, inf, len(pv), 2)
+    assert st == 0 and np.array_equal(back, pv) and out.time == 500.0
+    # a file of the cells' entities is not the vertices' file
+    st0, *_ = restart.parse_restart(got, restart.info(edges, verts), len(pv), 2)
+    assert st0 != 0

@@ -119,3 +119,51 @@ def test_vtk_output_equals_the_oracle(built, tmp_path, kind):
     assert set(cells["types"].tolist()) == {9 if prob.b == 2 else 12}
     coll = ET.parse(os.path.join(str(tmp_path), kind + ".pvd")).getroot().find("Collection")
     assert [d.get("file") for d in coll.findall("DataSet")] == [kind + "-00000.vtu", kind + "-00001.vtu"]
+
+
+def test_vertex_centred_points_and_cells():
+    """A vertex-centred grid: the points are its degrees of freedom, the
+    cells its elements in VTK's counter-clockwise corner order."""
+    p = problems.lens_vcfv(4, 3)
+    pts, cells = vtk.structured_points(p)
+    assert pts.shape == (20, 3) and cells.shape == (12, 4)
+    assert np.allclose(pts[cells[0]][:, :2], [[0, 0], [1.5, 0], [1.5, 4 / 3], [0, 4 / 3]])
+    assert np.array_equal(pts, p.center.reshape(-1, 3))
+
+
+@pytest.mark.gpu
+def test_vertex_centred_vtk_output_is_vertex_data(built, tmp_path):
+    """VcfvBaseOutputModule writes vertex data: the fields of the vertex-
+    centred lens as PointData over the vertices, the elements as cells, the
+    values the oracle's output quantities rounded to float."""
+    prob = problems.lens_vcfv(12, 8)
+    prm = capi.default_params(linear_tolerance=1e-8)
+    ctx = Context(prob, prm)
+    st, *_ = ctx.time_integration(3, 250.0)
+    assert st == 0
+    w = vtk.MultiWriter(prob, str(tmp_path), "lensvcfv", fields=vtk.DEFAULT_FIELDS | vtk.PRIMARY_VARS)
+    path = w.write(ctx, 750.0)
+    x, m = ctx.solution()
+    ctx.close()
+    orc = O.Oracle(prob, prm)
+    orc.set_solution(x, m)
+    ref = orc.output_fields()
+    orc.close()
+    root = ET.parse(path).getroot()
+    piece = root.find("UnstructuredGrid").find("Piece")
+    assert piece.find("CellData") is None
+    pd = piece.find("PointData")
+    arrays = [(a.get("Name"), np.array(a.text.split(), np.float32)) for a in pd.findall("DataArray")]
+    assert int(piece.get("NumberOfPoints")) == prob.num_cells
+    assert int(piece.get("NumberOfCells")) == len(prob.elem_corner) // 4
+    names = [a[0] for a in arrays]
+    assert names[:2] == ["PV_pressure_w", "PV_saturation_w"]
+    got = dict(arrays)
+    assert np.allclose(got["PV_saturation_w"], x.reshape(-1, 2)[:, 1].astype(np.float32), rtol=0, atol=0)
+    for q, k in (("pressure", 0), ("density", 1), ("saturation", 2), ("relativePerm", 4)):
+        for a, ph in enumerate(("w", "n")):
+            want = ref[3 * k + a].astype(np.float32)
+            assert np.max(np.abs(got["%s_%s" % (q, ph)] - want)) <= 1e-6 * max(1.0, np.max(np.abs(want))), q
+    cells = {a.get("Name"): np.array(a.text.split(), np.int64) for a in piece.find("Cells").findall("DataArray")}
+    _, vc = vtk.structured_points(prob)
+    assert np.array_equal(cells["connectivity"], vc.ravel())
