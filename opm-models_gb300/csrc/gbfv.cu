@@ -1162,6 +1162,10 @@ static int createVcfvImpl(gbfv_ctx* C, const gbfv_problem* P)
         setError("vertex-centred grids take the element linearizer");
         return GBFV_ERR_UNSUPPORTED;
     }
+    if (P->model == GBFV_MODEL_BLACKOIL_3P && C->prm.local_linearizer != GBFV_LIN_AD) {
+        setError("vertex-centred black-oil grids take the AD local linearizer");
+        return GBFV_ERR_UNSUPPORTED;
+    }
     VcfvSetup vs;
     if (const int st = vcfvSetup(P, vs)) return st;
     int ndev = 0;
@@ -1169,7 +1173,7 @@ static int createVcfvImpl(gbfv_ctx* C, const gbfv_problem* P)
         setError("no CUDA device");
         return GBFV_ERR_NO_DEVICE;
     }
-    const int N = P->num_cells, b = 2, nslot = VCFV_SLOTS;
+    const int N = P->num_cells, b = P->model == GBFV_MODEL_BLACKOIL_3P ? 3 : 2, nslot = VCFV_SLOTS;
     C->N = N;
     C->model = P->model;
     C->b = b;
@@ -1218,7 +1222,17 @@ static int createVcfvImpl(gbfv_ctx* C, const gbfv_problem* P)
         hPor[p] = P->porosity[I];
         for (int d = 0; d < 3; ++d) hPerm[(size_t)d * ld + p] = P->perm[3 * I + d];
         hMat[p] = P->material[I];
+        hCflag[p] = P->constraint ? P->constraint[I] : -1;
     }
+    // constraint vertices (the problem's constraints(), e.g. wells)
+    std::vector<int> consCells, consOf;
+    for (int p = 0; p < N; ++p)
+        if (hCflag[p] >= 0) {
+            consCells.push_back(p);
+            consOf.push_back(hCflag[p]);
+        }
+    std::vector<double> consPv(P->constraint_pv, P->constraint_pv + 3 * (size_t)std::max(0, P->num_constraints));
+    std::vector<int> consMeaning(P->constraint_meaning, P->constraint_meaning + std::max(0, P->num_constraints));
     CK(cudaStreamCreateWithFlags(&C->stream, cudaStreamNonBlocking));
     for (auto& e : C->ev) CK(cudaEventCreate(&e));
     DevMesh& m = C->mesh;
@@ -1236,17 +1250,22 @@ static int createVcfvImpl(gbfv_ctx* C, const gbfv_problem* P)
         if (!s2) C->owned.push_back((void*)*dst);
         return s2;
     };
-    int *dMat, *dCflag;
-    double *dVol, *dPor, *dPerm;
+    int *dMat, *dCflag, *dConsCells, *dConsOf, *dConsMeaning;
+    double *dVol, *dPor, *dPerm, *dConsPv;
     if ((st = up(&dVol, hVol)) || (st = up(&dPor, hPor)) || (st = up(&dPerm, hPerm)) || (st = up(&dMat, hMat)) ||
-        (st = up(&dCflag, hCflag)))
+        (st = up(&dCflag, hCflag)) || (st = up(&dConsCells, consCells)) || (st = up(&dConsOf, consOf)) ||
+        (st = up(&dConsPv, consPv)) || (st = up(&dConsMeaning, consMeaning)))
         return st;
     m.volume = dVol;
     m.porosity = dPor;
     m.perm = dPerm;
     m.material = dMat;
     m.cflag = dCflag;
-    m.numConsCells = 0;
+    m.consCells = dConsCells;
+    m.consOf = dConsOf;
+    m.consPv = dConsPv;
+    m.consMeaning = dConsMeaning;
+    m.numConsCells = (int)consCells.size();
     if ((st = devAlloc(&C->dphys, 1))) return st;
     CK(cudaMemcpy(C->dphys, &ph, sizeof(DevPhysics), cudaMemcpyHostToDevice));
     C->vcfv = vcfvUpload(P, vs, ph, perm, ld, &st);

@@ -80,7 +80,7 @@ struct BFaceV {
     double gTimesDist, absDist2;
     double K[2];           // the vertex's permeability
     double pb[2], mobb[2], rhob[2];  // free-flow state
-    double rate[2];        // mass rate
+    double rate[3];        // mass rate per equation
 };
 
 struct VcfvArgs {
@@ -90,9 +90,10 @@ struct VcfvArgs {
     const BFaceV* bf;
     const int* inc;        // [k*ld + p] element*4 + corner of vertex p's k-th element, -1 none
     const unsigned char* incSlot;  // [(k*4 + f)*ld + p] slot of the element's corner f in row p
-    double* R;             // [(e*4 + f)*2 + a] residual of corner f (focus f)
-    double* J;             // [((e*4 + f)*4 + j)*4 + a*2 + pv] d res_j,a / d x_f,pv
+    double* R;             // [(e*4 + f)*b + a] residual of corner f (focus f)
+    double* J;             // [((e*4 + f)*4 + j)*b*b + a*b + pv] d res_j,a / d x_f,pv
     int p1;
+    double rhoRef[3];      // black-oil surface densities (water, oil, gas)
 };
 
 double harmonicMeanV(double x, double y)
@@ -186,60 +187,89 @@ int slotOf(const double* a, const double* b)
 }
 
 // ---------------------------------------------------------------- kernels --
+using D3 = Dual<3>;
 __device__ __forceinline__ double valueOf(double x) { return x; }
 __device__ __forceinline__ double valueOf(const D2& x) { return x.v; }
+__device__ __forceinline__ double valueOf(const D3& x) { return x.v; }
+
+// Intensive-quantity value planes of the two models (the IQ pass's layout):
+// two-phase p0 p1 rho0 rho1 lam0 lam1; black-oil p rho0..2 lam0..2
+// invB0..2 Rs (one pressure: zero capillary pressure)
+template <int B> struct Iq;
+template <> struct Iq<2> {
+    static constexpr int NV = 6;
+    static __device__ __forceinline__ int p(int a) { return a; }
+    static __device__ __forceinline__ int rho(int a) { return 2 + a; }
+    static __device__ __forceinline__ int lam(int a) { return 4 + a; }
+};
+template <> struct Iq<3> {
+    static constexpr int NV = 11;
+    static __device__ __forceinline__ int p(int) { return 0; }
+    static __device__ __forceinline__ int rho(int a) { return 1 + a; }
+    static __device__ __forceinline__ int lam(int a) { return 4 + a; }
+    static __device__ __forceinline__ int invB(int a) { return 7 + a; }
+    static __device__ __forceinline__ int rs() { return 10; }
+};
 
 // FvBaseLocalResidual::eval of one element (fvbaselocalresidual.hh:158-191)
-// in the number type T (D2 for automatic differentiation, double for finite
-// differences).  Q(c, k): quantity k (p0 p1 rho0 rho1 lam0 lam1) of corner
-// c; Sto(c, ph): the storage of phase ph in corner c; sto0: the storage
-// values of the unperturbed state (the cache at iteration 0).
-template <class T, bool P1, class QF, class SF>
+// for the model with B equations (2: immiscible two-phase; 3: black-oil,
+// blackoillocalresidual.hh:101-367) in the number type T (duals for
+// automatic differentiation, double for finite differences).  Q(c, k):
+// intensive-quantity value plane k of corner c; Sto(c, e): the storage of
+// equation e in corner c; sto0: the storage values of the unperturbed state
+// (the cache at iteration 0).
+template <class T, int B, bool P1, class QF, class SF>
 __device__ __forceinline__ void elementEval(const VcfvArgs& a, const DevMesh& m, int e, const QF& Q, const SF& Sto,
                                             const double* __restrict__ sto0, const double* __restrict__ storageOld,
-                                            int iter0, double dt, T (&res)[4][2])
+                                            int iter0, double dt, T (&res)[4][B])
 {
+    using I = Iq<B>;
+    constexpr int NP = B;  // phases
     const ElemGeo& G = a.geo[e];
     const int ld = m.ldN;
 #pragma unroll
-    for (int c = 0; c < 4; ++c) res[c][0] = res[c][1] = T(0.0);
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+        for (int q = 0; q < B; ++q) res[c][q] = T(0.0);
     // evalFluxes: the four sub-control-volume faces
 #pragma unroll 1
     for (int k = 0; k < 4; ++k) {
         const int i = FI[k], j = FJ[k];
-        T pg[2][2];
+        T pg[NP][2];
 #pragma unroll
-        for (int ph = 0; ph < 2; ++ph) {
+        for (int ph = 0; ph < NP; ++ph) {
             if (P1) {
                 pg[ph][0] = T(0.0);
                 pg[ph][1] = T(0.0);
 #pragma unroll
                 for (int c = 0; c < 4; ++c) {
-                    const T dv = Q(c, ph);
+                    const T dv = Q(c, I::p(ph));
                     pg[ph][0] = pg[ph][0] + dv * G.grad[k][c][0];
                     pg[ph][1] = pg[ph][1] + dv * G.grad[k][c][1];
                 }
             }
             else {
-                const T deltay = Q(j, ph) - Q(i, ph);
+                const T deltay = Q(j, I::p(ph)) - Q(i, I::p(ph));
                 pg[ph][0] = deltay * G.w2p[k][0];
                 pg[ph][1] = deltay * G.w2p[k][1];
             }
             // gravity correction (darcyfluxmodule.hh:214-283)
-            const T pStatIn = -(Q(i, 2 + ph) * G.gIn[k]);
-            const T pStatEx = -(Q(j, 2 + ph) * G.gEx[k]);
+            const T pStatIn = -(Q(i, I::rho(ph)) * G.gIn[k]);
+            const T pStatEx = -(Q(j, I::rho(ph)) * G.gEx[k]);
             const T fs = (pStatEx - pStatIn) / G.absTot2[k];
             pg[ph][0] = pg[ph][0] + G.dTot[k][0] * fs;
             pg[ph][1] = pg[ph][1] + G.dTot[k][1] * fs;
         }
-        T flux[2];
+        T flux[B];
 #pragma unroll
-        for (int ph = 0; ph < 2; ++ph) {
+        for (int q = 0; q < B; ++q) flux[q] = T(0.0);
+#pragma unroll
+        for (int ph = 0; ph < NP; ++ph) {
             T tmp(0.0);
             tmp = tmp + pg[ph][0] * G.fn[k][0];
             tmp = tmp + pg[ph][1] * G.fn[k][1];
             const int up = valueOf(tmp) > 0 ? j : i;
-            const T mob = Q(up, 4 + ph);
+            const T mob = Q(up, I::lam(ph));
             T vf(0.0);
 #pragma unroll
             for (int d = 0; d < 2; ++d) {
@@ -247,13 +277,23 @@ __device__ __forceinline__ void elementEval(const VcfvArgs& a, const DevMesh& m,
                 fv = fv * (-mob);
                 vf = vf + fv * G.fn[k][d];
             }
-            flux[ph] = T(0.0) + vf * Q(up, 2 + ph);
-            flux[ph] = flux[ph] * (1.0 * G.fa[k]);
+            if constexpr (B == 2) {
+                flux[ph] = T(0.0) + vf * Q(up, I::rho(ph));
+            }
+            else {
+                // component fluxes of the phase: water -> 1, oil -> 0 (and
+                // the gas dissolved in it -> 2), gas -> 2
+                const int comp = ph == 0 ? 1 : (ph == 1 ? 0 : 2);
+                const T svf = Q(up, Iq<3>::invB(ph)) * vf;
+                flux[comp] = flux[comp] + svf * a.rhoRef[ph];
+                if (ph == 1) flux[2] = flux[2] + Q(up, Iq<3>::rs()) * svf * a.rhoRef[2];
+            }
         }
 #pragma unroll
-        for (int ph = 0; ph < 2; ++ph) {
-            res[i][ph] = res[i][ph] + flux[ph];
-            res[j][ph] = res[j][ph] - flux[ph];
+        for (int q = 0; q < B; ++q) {
+            flux[q] = flux[q] * (1.0 * G.fa[k]);
+            res[i][q] = res[i][q] + flux[q];
+            res[j][q] = res[j][q] - flux[q];
         }
     }
     // evalVolumeTerms_: storage of the four sub-control volumes
@@ -261,119 +301,123 @@ __device__ __forceinline__ void elementEval(const VcfvArgs& a, const DevMesh& m,
     for (int c = 0; c < 4; ++c) {
         const double scvVolume = G.scvVol[c] * 1.0;
 #pragma unroll
-        for (int ph = 0; ph < 2; ++ph) {
-            T tmp = Sto(c, ph);
-            const double tmp2 = iter0 ? sto0[ph * 3 * ld + G.v[c]] : storageOld[ph * ld + G.v[c]];
+        for (int q = 0; q < B; ++q) {
+            T tmp = Sto(c, q);
+            const double tmp2 = iter0 ? sto0[q * (B + 1) * ld + G.v[c]] : storageOld[q * ld + G.v[c]];
             tmp = tmp - tmp2;
             tmp = tmp * (scvVolume / dt);
-            res[c][ph] = res[c][ph] + tmp;
-            res[c][ph] = res[c][ph] - 0.0 * scvVolume;
+            res[c][q] = res[c][q] + tmp;
+            res[c][q] = res[c][q] - 0.0 * scvVolume;
         }
     }
     // evalBoundary_: this element's boundary sub-control-volume faces
-    for (int b = a.bfPtr[e]; b < a.bfPtr[e + 1]; ++b) {
-        const BFaceV B = a.bf[b];
-        T values[2] = {T(0.0), T(0.0)};
-        if (B.type == GBFV_BC_MASSRATE) {
-            values[0] = T(B.rate[0]);
-            values[1] = T(B.rate[1]);
+    for (int bf = a.bfPtr[e]; bf < a.bfPtr[e + 1]; ++bf) {
+        const BFaceV Bf = a.bf[bf];
+        T values[B];
+#pragma unroll
+        for (int q = 0; q < B; ++q) values[q] = T(0.0);
+        if (Bf.type == GBFV_BC_MASSRATE) {
+#pragma unroll
+            for (int q = 0; q < B; ++q) values[q] = T(Bf.rate[q]);
         }
-        else if (B.type == GBFV_BC_FREEFLOW) {
+        else if (B == 2 && Bf.type == GBFV_BC_FREEFLOW) {
 #pragma unroll
             for (int ph = 0; ph < 2; ++ph) {
-                const T pIn = Q(B.c, ph);
-                const T deltay = T(B.pb[ph]) - pIn;
+                const T pIn = Q(Bf.c, I::p(ph));
+                const T deltay = T(Bf.pb[ph]) - pIn;
                 T pg[2];
-                pg[0] = deltay * B.w[0];
-                pg[1] = deltay * B.w[1];
-                const T pStatIn = (-B.gTimesDist) * Q(B.c, 2 + ph);
-                const T fsc = pStatIn / B.absDist2;
-                pg[0] = pg[0] + B.dIn[0] * fsc;
-                pg[1] = pg[1] + B.dIn[1] * fsc;
+                pg[0] = deltay * Bf.w[0];
+                pg[1] = deltay * Bf.w[1];
+                const T pStatIn = (-Bf.gTimesDist) * Q(Bf.c, I::rho(ph));
+                const T fsc = pStatIn / Bf.absDist2;
+                pg[0] = pg[0] + Bf.dIn[0] * fsc;
+                pg[1] = pg[1] + Bf.dIn[1] * fsc;
                 T tmp(0.0);
-                tmp = tmp + pg[0] * B.n[0];
-                tmp = tmp + pg[1] * B.n[1];
-                const T mob = valueOf(tmp) > 0.0 ? T(B.mobb[ph]) : Q(B.c, 4 + ph);
+                tmp = tmp + pg[0] * Bf.n[0];
+                tmp = tmp + pg[1] * Bf.n[1];
+                const T mob = valueOf(tmp) > 0.0 ? T(Bf.mobb[ph]) : Q(Bf.c, I::lam(ph));
                 T vf(0.0);
 #pragma unroll
                 for (int d = 0; d < 2; ++d) {
-                    T fv = B.K[d] * pg[d];
+                    T fv = Bf.K[d] * pg[d];
                     fv = fv * (-mob);
-                    vf = vf + fv * B.n[d];
+                    vf = vf + fv * Bf.n[d];
                 }
-                const T dens = B.pb[ph] > valueOf(pIn) ? T(B.rhob[ph]) : Q(B.c, 2 + ph);
+                const T dens = Bf.pb[ph] > valueOf(pIn) ? T(Bf.rhob[ph]) : Q(Bf.c, I::rho(ph));
                 values[ph] = values[ph] + vf * dens;
             }
         }
-        const double aa = B.area * 1.0;
+        const double aa = Bf.area * 1.0;
 #pragma unroll
-        for (int ph = 0; ph < 2; ++ph) res[B.c][ph] = res[B.c][ph] + values[ph] * aa;
+        for (int q = 0; q < B; ++q) res[Bf.c][q] = res[Bf.c][q] + values[q] * aa;
     }
     // volumetric residual
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
         const double V = m.volume[G.v[c]];
-        res[c][0] = res[c][0] / V;
-        res[c][1] = res[c][1] / V;
+#pragma unroll
+        for (int q = 0; q < B; ++q) res[c][q] = res[c][q] / V;
     }
 }
 
 // Element pass (automatic differentiation): thread (e, f) evaluates element
 // e with the derivatives of corner f (fvbaseadlocallinearizer.hh:173-292).
-template <bool P1>
+template <int B, bool P1>
 __global__ void __launch_bounds__(128) kVcfvElement(VcfvArgs a, DevMesh m, IqBuffers iq,
                                                     const double* __restrict__ storageOld, int iter0, double dt)
 {
+    using D = Dual<B>;
+    constexpr int NV = Iq<B>::NV;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= a.E * 4) return;
     const int e = t >> 2, f = t & 3;
     const ElemGeo& G = a.geo[e];
     const int ld = m.ldN;
-    double cv[4][6];  // p0 p1 rho0 rho1 lam0 lam1 of each corner
+    double cv[4][NV];  // the corners' intensive-quantity values
 #pragma unroll
     for (int c = 0; c < 4; ++c)
 #pragma unroll
-        for (int k = 0; k < 6; ++k) cv[c][k] = iq.val[k * ld + G.v[c]];
+        for (int k = 0; k < NV; ++k) cv[c][k] = iq.val[k * ld + G.v[c]];
     const int vf = G.v[f];
-    double fd[6][2];
+    double fd[NV][B];  // the focus corner's derivatives
 #pragma unroll
-    for (int k = 0; k < 6; ++k) {
-        fd[k][0] = iq.der[(k * 2 + 0) * ld + vf];
-        fd[k][1] = iq.der[(k * 2 + 1) * ld + vf];
-    }
+    for (int k = 0; k < NV; ++k)
+#pragma unroll
+        for (int d = 0; d < B; ++d) {
+            if (B == 2) fd[k][d] = iq.der[(k * 2 + d) * ld + vf];
+            else fd[k][d] = k == 0 ? (d == 1 ? 1.0 : 0.0) : iq.der[((k - 1) * 3 + d) * ld + vf];
+        }
     auto Q = [&](int c, int k) {
-        D2 r(cv[c][k]);
-        if (c == f) {
-            r.d[0] = fd[k][0];
-            r.d[1] = fd[k][1];
-        }
+        D r(cv[c][k]);
+        if (c == f)
+#pragma unroll
+            for (int d = 0; d < B; ++d) r.d[d] = fd[k][d];
         return r;
     };
-    auto Sto = [&](int c, int ph) {
+    auto Sto = [&](int c, int q) {
         const int v = G.v[c];
-        D2 r(iq.sto[(ph * 3 + 0) * ld + v]);
-        if (c == f) {
-            r.d[0] = iq.sto[(ph * 3 + 1) * ld + v];
-            r.d[1] = iq.sto[(ph * 3 + 2) * ld + v];
-        }
+        D r(iq.sto[(q * (B + 1) + 0) * ld + v]);
+        if (c == f)
+#pragma unroll
+            for (int d = 0; d < B; ++d) r.d[d] = iq.sto[(q * (B + 1) + 1 + d) * ld + v];
         return r;
     };
-    D2 res[4][2];
-    elementEval<D2, P1>(a, m, e, Q, Sto, iq.sto, storageOld, iter0, dt, res);
+    D res[4][B];
+    elementEval<D, B, P1>(a, m, e, Q, Sto, iq.sto, storageOld, iter0, dt, res);
     const size_t ef = (size_t)e * 4 + f;
-    a.R[ef * 2 + 0] = res[f][0].v;
-    a.R[ef * 2 + 1] = res[f][1].v;
+#pragma unroll
+    for (int q = 0; q < B; ++q) a.R[ef * B + q] = res[f][q].v;
 #pragma unroll
     for (int j = 0; j < 4; ++j)
 #pragma unroll
-        for (int ph = 0; ph < 2; ++ph)
+        for (int q = 0; q < B; ++q)
 #pragma unroll
-            for (int pv = 0; pv < 2; ++pv) a.J[(ef * 4 + j) * 4 + ph * 2 + pv] = res[j][ph].d[pv];
+            for (int pv = 0; pv < B; ++pv) a.J[(ef * 4 + j) * B * B + q * B + pv] = res[j][q].d[pv];
 }
 
-// Element pass (finite differences, fvbasefdlocallinearizer.hh:236-510):
-// thread (e, f) evaluates element e unperturbed and with corner f's
-// primary variable pv deflected (the deflected states' intensive
+// Element pass (finite differences, fvbasefdlocallinearizer.hh:236-510; the
+// two-phase model): thread (e, f) evaluates element e unperturbed and with
+// corner f's primary variable pv deflected (the deflected states' intensive
 // quantities come from the per-vertex deflection passes, plus[pv] at
 // x + eps, minus[pv] at the second state), the columns of corner f being
 // the differences divided by the total deflection.
@@ -398,7 +442,7 @@ __global__ void __launch_bounds__(128) kVcfvElementFd(VcfvArgs a, DevMesh m, IqB
         auto Sto = [&](int c, int ph) {
             return (dq && c == f) ? dq->sto[(ph * 3) * ld + vf] : iq0.sto[(ph * 3) * ld + G.v[c]];
         };
-        elementEval<double, P1>(a, m, e, Q, Sto, iq0.sto, storageOld, it0, dt, res);
+        elementEval<double, 2, P1>(a, m, e, Q, Sto, iq0.sto, storageOld, it0, dt, res);
     };
     double res0[4][2];
     eval(nullptr, iter0, res0);
@@ -444,54 +488,68 @@ __global__ void __launch_bounds__(128) kVcfvElementFd(VcfvArgs a, DevMesh m, IqB
 
 // Gather pass: vertex p's residual and Jacobian row, its elements' records
 // added in element order (residual_[globI] += ..., addToBlock(globJ, globI,
-// ...), fvbaselinearizer.hh:609-621); the storage cache at iteration 0.
+// ...), fvbaselinearizer.hh:609-621); a constrained vertex's row becomes the
+// identity with a zero residual (applyConstraintsToLinearization_,
+// fvbaselinearizer.hh:649-666); the storage cache at iteration 0.
+template <int B>
 __global__ void __launch_bounds__(128) kVcfvGather(VcfvArgs a, DevMesh m, IqBuffers iq, double* __restrict__ storageOld,
                                                    int iter0, double* __restrict__ residual, double* __restrict__ jval)
 {
+    constexpr int BB = B * B;
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= m.N) return;
     const int ld = m.ldN;
-    double r[2] = {0.0, 0.0};
-    double Jb[VCFV_SLOTS][4];
+    double r[B];
+#pragma unroll
+    for (int q = 0; q < B; ++q) r[q] = 0.0;
+    double Jb[VCFV_SLOTS][BB];
 #pragma unroll
     for (int s = 0; s < VCFV_SLOTS; ++s)
 #pragma unroll
-        for (int q = 0; q < 4; ++q) Jb[s][q] = 0.0;
+        for (int q = 0; q < BB; ++q) Jb[s][q] = 0.0;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         const int ec = a.inc[k * ld + p];
         if (ec < 0) break;
         const size_t e = ec >> 2;
         const int c = ec & 3;
-        r[0] += a.R[(e * 4 + c) * 2 + 0];
-        r[1] += a.R[(e * 4 + c) * 2 + 1];
+#pragma unroll
+        for (int q = 0; q < B; ++q) r[q] += a.R[(e * 4 + c) * B + q];
 #pragma unroll
         for (int f = 0; f < 4; ++f) {
             const int s = a.incSlot[(k * 4 + f) * ld + p];
-            const double* src = &a.J[((e * 4 + f) * 4 + c) * 4];
+            const double* src = &a.J[((e * 4 + f) * 4 + c) * BB];
 #pragma unroll
             for (int sl = 0; sl < VCFV_SLOTS; ++sl)
                 if (sl == s)
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) Jb[sl][q] += src[q];
+                    for (int q = 0; q < BB; ++q) Jb[sl][q] += src[q];
         }
     }
-    residual[2 * p + 0] = r[0];
-    residual[2 * p + 1] = r[1];
+    if (m.cflag[p] >= 0) {
+#pragma unroll
+        for (int q = 0; q < B; ++q) r[q] = 0.0;
+#pragma unroll
+        for (int s = 0; s < VCFV_SLOTS; ++s)
+#pragma unroll
+            for (int q = 0; q < BB; ++q) Jb[s][q] = (s == VCFV_DIAG && q % (B + 1) == 0) ? 1.0 : 0.0;
+    }
+#pragma unroll
+    for (int q = 0; q < B; ++q) residual[B * p + q] = r[q];
 #pragma unroll
     for (int s = 0; s < VCFV_SLOTS; ++s)
 #pragma unroll
-        for (int q = 0; q < 4; ++q) jval[((size_t)s * 4 + q) * ld + p] = Jb[s][q];
-    if (iter0) {
-        storageOld[0 * ld + p] = iq.sto[(0 * 3 + 0) * ld + p];
-        storageOld[1 * ld + p] = iq.sto[(1 * 3 + 0) * ld + p];
-    }
+        for (int q = 0; q < BB; ++q) jval[((size_t)s * BB + q) * ld + p] = Jb[s][q];
+    if (iter0)
+#pragma unroll
+        for (int q = 0; q < B; ++q) storageOld[q * ld + p] = iq.sto[(q * (B + 1) + 0) * ld + p];
 }
 
 }  // namespace
 
 struct VcfvDev {
-    int E = 0, N = 0, ld = 0, p1 = 1, nbf = 0;
+    int E = 0, N = 0, ld = 0, p1 = 1, nbf = 0, b = 2;
+    double rhoRef[3] = {0, 0, 0};
     ElemGeo* geo = nullptr;
     int* bfPtr = nullptr;
     BFaceV* bf = nullptr;
@@ -507,11 +565,12 @@ int vcfvSetup(const gbfv_problem* P, VcfvSetup& s)
         setLastError("vertex-centred grid: " + w);
         return code;
     };
-    if (P->model != GBFV_MODEL_IMMISCIBLE_2P) return fail("the immiscible model only", GBFV_ERR_UNSUPPORTED);
     if (P->flux_module != GBFV_FLUX_DARCY) return fail("the Darcy flux module only", GBFV_ERR_UNSUPPORTED);
     const int N = P->num_cells, E = P->num_elements;
-    for (int i = 0; P->constraint && i < N; ++i)
-        if (P->constraint[i] >= 0) return fail("constraints are not supported", GBFV_ERR_UNSUPPORTED);
+    if (P->model == GBFV_MODEL_BLACKOIL_3P && P->bface_type)
+        for (int f = 0; f < P->num_bfaces; ++f)
+            if (P->bface_type[f] == GBFV_BC_FREEFLOW)
+                return fail("free-flow boundaries are the two-phase model's", GBFV_ERR_UNSUPPORTED);
     for (int i = 0; i < N; ++i)
         if (P->center[3 * i + 2] != 0.0) return fail("2D grids only (vertex z = 0)", GBFV_ERR_UNSUPPORTED);
     s.N = N;
@@ -572,6 +631,10 @@ VcfvDev* vcfvUpload(const gbfv_problem* P, const VcfvSetup& s, const DevPhysics&
     d->N = N;
     d->ld = ld;
     d->p1 = P->p1_gradients ? 1 : 0;
+    d->b = P->model == GBFV_MODEL_BLACKOIL_3P ? 3 : 2;
+    d->rhoRef[0] = ph.pvt.rhoRefW;
+    d->rhoRef[1] = ph.pvt.rhoRefO;
+    d->rhoRef[2] = ph.pvt.rhoRefG;
     std::vector<ElemGeo> geo(E);
     std::vector<int> bfPtr(E + 1, 0);
     std::vector<BFaceV> bf;
@@ -644,8 +707,7 @@ VcfvDev* vcfvUpload(const gbfv_problem* P, const VcfvSetup& s, const DevPhysics&
             B.gTimesDist = gTimesDist;
             const double* val = &P->bface_value[4 * b];
             if (B.type == GBFV_BC_MASSRATE) {
-                B.rate[0] = val[0];
-                B.rate[1] = val[1];
+                for (int q = 0; q < d->b; ++q) B.rate[q] = val[q];
             }
             else if (B.type == GBFV_BC_FREEFLOW) {
                 const TwoPhaseLaw& L = ph.law[P->material[vn]];
@@ -700,8 +762,8 @@ VcfvDev* vcfvUpload(const gbfv_problem* P, const VcfvSetup& s, const DevPhysics&
         !upload(&d->incSlot, incSlot))
         return fail(GBFV_ERR_OOM);
     d->nbf = (int)bf.size();
-    if (cudaMalloc((void**)&d->R, sizeof(double) * (size_t)E * 8) != cudaSuccess ||
-        cudaMalloc((void**)&d->J, sizeof(double) * (size_t)E * 64) != cudaSuccess)
+    if (cudaMalloc((void**)&d->R, sizeof(double) * (size_t)E * 4 * d->b) != cudaSuccess ||
+        cudaMalloc((void**)&d->J, sizeof(double) * (size_t)E * 16 * d->b * d->b) != cudaSuccess)
         return fail(GBFV_ERR_OOM);
     if (status) *status = GBFV_OK;
     return d;
@@ -745,6 +807,7 @@ VcfvArgs vcfvArgs(const VcfvDev* d)
     a.R = d->R;
     a.J = d->J;
     a.p1 = d->p1;
+    for (int k = 0; k < 3; ++k) a.rhoRef[k] = d->rhoRef[k];
     return a;
 }
 }  // namespace
@@ -757,7 +820,7 @@ void launchVcfvAssembleFd(const VcfvDev* d, const DevMesh& m, IqBuffers iq0, con
     const int nt = 4 * d->E;
     if (d->p1) kVcfvElementFd<true><<<(nt + 127) / 128, 128, 0, s>>>(a, m, iq0, fd, refP, method, storageOld, iter0, dt);
     else kVcfvElementFd<false><<<(nt + 127) / 128, 128, 0, s>>>(a, m, iq0, fd, refP, method, storageOld, iter0, dt);
-    kVcfvGather<<<(m.N + 127) / 128, 128, 0, s>>>(a, m, iq0, storageOld, iter0, residual, jval);
+    kVcfvGather<2><<<(m.N + 127) / 128, 128, 0, s>>>(a, m, iq0, storageOld, iter0, residual, jval);
     countLaunch(2);
 }
 
@@ -766,9 +829,17 @@ void launchVcfvAssemble(const VcfvDev* d, const DevMesh& m, IqBuffers iq, double
 {
     const VcfvArgs a = vcfvArgs(d);
     const int nt = 4 * d->E;
-    if (d->p1) kVcfvElement<true><<<(nt + 127) / 128, 128, 0, s>>>(a, m, iq, storageOld, iter0, dt);
-    else kVcfvElement<false><<<(nt + 127) / 128, 128, 0, s>>>(a, m, iq, storageOld, iter0, dt);
-    kVcfvGather<<<(m.N + 127) / 128, 128, 0, s>>>(a, m, iq, storageOld, iter0, residual, jval);
+    const int nb = (nt + 127) / 128, ng = (m.N + 127) / 128;
+    if (d->b == 3) {
+        if (d->p1) kVcfvElement<3, true><<<nb, 128, 0, s>>>(a, m, iq, storageOld, iter0, dt);
+        else kVcfvElement<3, false><<<nb, 128, 0, s>>>(a, m, iq, storageOld, iter0, dt);
+        kVcfvGather<3><<<ng, 128, 0, s>>>(a, m, iq, storageOld, iter0, residual, jval);
+    }
+    else {
+        if (d->p1) kVcfvElement<2, true><<<nb, 128, 0, s>>>(a, m, iq, storageOld, iter0, dt);
+        else kVcfvElement<2, false><<<nb, 128, 0, s>>>(a, m, iq, storageOld, iter0, dt);
+        kVcfvGather<2><<<ng, 128, 0, s>>>(a, m, iq, storageOld, iter0, residual, jval);
+    }
     countLaunch(2);
 }
 

@@ -427,6 +427,89 @@ def lens_vcfv(nx=48, ny=32, law="vg", p1=True):
     return p
 
 
+def blackoil_vcfv(nx=40, ny=20, cell=(10.0, 5.0), sigma=1.0, seed=12345, corey_n=2.0, p_res=330e5,
+                  with_wells=True, pvt_rows=10):
+    """The black-oil benchmark on a vertex-centred 2D vertical section (the
+    reference's reservoir_blackoil_vcfv configuration has a 2D grid,
+    reservoirproblem.hh:78): (nx+1) x (ny+1) vertices, gravity along y,
+    lognormal permeability (vertical one tenth) and uniform porosity per
+    vertex, the PVT tables and Corey relperms of ``blackoil``, no-flow
+    boundaries, an injector at vertex (0, 0) and a producer at (nx, ny) as
+    constraint vertices."""
+    hx, hy = cell
+    mx, my = nx + 1, ny + 1
+    N = mx * my
+    vi = np.arange(N)
+    pos = np.zeros((N, 3))
+    pos[:, 0] = (vi % mx) * hx
+    pos[:, 1] = (vi // mx) * hy
+    p = ProblemData(capi.MODEL_BLACKOIL_3P)
+    p.center = np.ascontiguousarray(pos.ravel())
+    rng = np.random.Generator(np.random.Philox(seed))
+    z = rng.standard_normal(N)
+    kx = np.exp(math.log(1e-13) + sigma * z)
+    p.perm = np.ascontiguousarray(np.stack([kx, 0.1 * kx, np.zeros(N)], 1).ravel())
+    rng2 = np.random.Generator(np.random.Philox(seed + 1))
+    p.porosity = rng2.uniform(0.15, 0.30, N)
+    p.material = np.zeros(N, np.int32)
+    p.material_params = np.array([capi.LAW_COREY3P, 0, 0, 0, corey_n, 0, 0, 0], float)
+    p.gravity = (0.0, -9.81, 0.0)
+    pvt = blackoil_pvt(pvt_rows)
+    p.pvt_arrays = pvt
+    NE = nx * ny
+    ex, ey = np.arange(NE) % nx, np.arange(NE) // nx
+    v0 = ex + mx * ey
+    corners = np.stack([v0, v0 + 1, v0 + mx, v0 + mx + 1], 1)
+    p.elem_corner = np.ascontiguousarray(corners.ravel().astype(np.int32))
+    volume = np.zeros(N)
+    for c in range(4):
+        np.add.at(volume, corners[:, c], hx * hy / 4)
+    p.volume = volume
+    bptr, bcorner, bcenter, bnormal, barea = [0], [], [], [], []
+    for e in range(NE):
+        lower = np.array([ex[e] * hx, ey[e] * hy])
+        for f in range(4):
+            on = (f == 0 and ex[e] == 0) or (f == 1 and ex[e] == nx - 1) or \
+                 (f == 2 and ey[e] == 0) or (f == 3 and ey[e] == ny - 1)
+            if not on:
+                continue
+            length = hy if f < 2 else hx
+            for c in FACE_CORNERS[f]:
+                loc = (np.array([c & 1, (c >> 1) & 1], float) + np.array(FACE_CENTER[f])) * 0.5
+                ip = lower + loc * np.array([hx, hy])
+                bcorner.append(c)
+                bcenter.append((ip[0], ip[1], 0.0))
+                bnormal.append((FACE_NORMAL[f][0], FACE_NORMAL[f][1], 0.0))
+                barea.append(0.5 * length)
+        bptr.append(len(bcorner))
+    p.conn_ptr = np.zeros(N + 1, np.int32)
+    p.conn_nbr = np.zeros(0, np.int32)
+    p.conn_dir = np.zeros(0, np.int32)
+    p.conn_normal = np.zeros(0)
+    p.conn_center = np.zeros(0)
+    p.conn_area = np.zeros(0)
+    p.bface_ptr = np.array(bptr, np.int32)
+    p.bface_corner = np.array(bcorner, np.int32)
+    p.bface_center = np.ascontiguousarray(np.array(bcenter).ravel())
+    p.bface_normal = np.ascontiguousarray(np.array(bnormal).ravel())
+    p.bface_area = np.array(barea)
+    p.bface_type = np.zeros(len(barea), np.int32)
+    p.bface_value = np.zeros(4 * len(barea))
+    p.p1_gradients = 1
+    rs0 = 0.95 * rs_sat(pvt, p_res)
+    p.init_pv = np.ascontiguousarray(np.stack([np.zeros(N), np.full(N, p_res), np.full(N, rs0)], 1).ravel())
+    p.init_meaning = np.full(N, capi.GAS_RS, np.int32)
+    cons = np.full(N, -1, np.int32)
+    if with_wells:
+        cons[0] = 0
+        cons[N - 1] = 1
+        p.constraint_pv = np.array([1.0, 1.5 * p_res, 0.0, 0.0, p_res / 1.5, rs0], float)
+        p.constraint_meaning = np.array([capi.GAS_SG, capi.GAS_RS], np.int32)
+    p.constraint = cons
+    p.info = dict(name="blackoil-vcfv", nx=nx, ny=ny, nz=1, dim=2, sigma=sigma, seed=seed, disc="vcfv")
+    return p
+
+
 def _interp(table, x):
     xs = np.array([t[0] for t in table], float)
     ys = np.array([t[1] for t in table], float)

@@ -985,7 +985,14 @@ static void linearize(Sim& S)
     std::fill(S.J.val.begin(), S.J.val.end(), 0.0);
     std::fill(S.residual.begin(), S.residual.end(), 0.0);
     const bool fd = S.prm.local_linearizer == GBFV_LIN_FD;
-    if (S.vcfv) {
+    if (S.vcfv && S.P.model == GBFV_MODEL_BLACKOIL_3P) {
+        if (fd) throw NumericalProblem("vertex-centred black-oil grids take the AD local linearizer", GBFV_ERR_UNSUPPORTED);
+        std::vector<IQ3> iq(S.N);
+#pragma omp parallel for schedule(static)
+        for (int I = 0; I < S.N; ++I) iq[I] = blackoilIQ(S.P, I, &S.x[I * 3], S.meaning[I]);
+        linearizeBlackoilVcfv(S, iq);
+    }
+    else if (S.vcfv) {
         std::vector<IQ2> iq(S.N);
 #pragma omp parallel for schedule(static)
         for (int I = 0; I < S.N; ++I) iq[I] = immiscibleIQ(S.P, I, &S.x[I * 2]);
@@ -1584,8 +1591,7 @@ void* oracle_create(const gbfv_problem* prob, const gbfv_params* prm)
         if (S->P.numElements > 0) {
             // the vertex-centred discretization takes the immiscible model
             // with the Darcy flux module and the element linearizer
-            if (S->P.model != GBFV_MODEL_IMMISCIBLE_2P || S->P.fluxModule != GBFV_FLUX_DARCY ||
-                prm->linearizer != GBFV_LINEARIZER_ELEMENT) {
+            if (S->P.fluxModule != GBFV_FLUX_DARCY || prm->linearizer != GBFV_LINEARIZER_ELEMENT) {
                 delete S;
                 return nullptr;
             }

@@ -153,6 +153,79 @@ static std::shared_ptr<VcfvGrid> vcfvGrid(const Prob& P)
 
 template <int N> static inline Dual<N> valueOnly(const Dual<N>& x) { return Dual<N>(x.v); }
 
+// The Darcy volume fluxes of sub-control-volume face k for NP phases
+// (darcyfluxmodule.hh:183-322, 459-525 on the vertex-centred stencil): the
+// phase pressure gradients at the face's integration point (P1 or
+// two-point), the gravity correction from the two vertices, upwinding by
+// the sign of the potential gradient along the normal, the upstream
+// mobility; vf[a] the volume flux per unit area, up[a] the upstream corner.
+// f: the focus corner (-1: none).
+template <int NB, class IQ, int NP>
+static void vcfvPhaseFluxes(const Prob& P, const VcfvGrid& G, const VcfvElement& E, int k, int f,
+                            const IQ* const (&q)[4], Dual<NB> (&vf)[NP], int (&up)[NP])
+{
+    using D = Dual<NB>;
+    auto focus = [&](int c, const D& x) { return c == f ? x : valueOnly(x); };
+    const int i = E.fi[k], j = E.fj[k];
+    const double* n = E.fn[k];
+    D pg[NP][2];  // [phase][dim]
+    for (int a = 0; a < NP; ++a) {
+        if (G.p1) {
+            // P1FeGradientCalculator::calculateGradient
+            pg[a][0] = D(0.0);
+            pg[a][1] = D(0.0);
+            for (int c = 0; c < 4; ++c) {
+                const D dofVal = focus(c, q[c]->p[a]);
+                for (int d = 0; d < 2; ++d) pg[a][d] += dofVal * E.grad[k][c][d];
+            }
+        }
+        else {
+            // FvBaseGradientCalculator::calculateGradient (two-point)
+            D deltay;
+            if (i == f) deltay = valueOnly(q[j]->p[a]) - q[i]->p[a];
+            else if (j == f) deltay = q[j]->p[a] - valueOnly(q[i]->p[a]);
+            else deltay = valueOnly(q[j]->p[a]) - valueOnly(q[i]->p[a]);
+            double distSq = 0.0;
+            for (int d = 0; d < 2; ++d) {
+                const double t = E.vpos[j][d] - E.vpos[i][d];
+                distSq += t * t;
+            }
+            for (int d = 0; d < 2; ++d) pg[a][d] = deltay * ((E.vpos[j][d] - E.vpos[i][d]) / distSq);
+        }
+    }
+    // gravity (darcyfluxmodule.hh:214-283): posIn / posEx the vertices
+    double dIn[2], dEx[2], dTot[2];
+    for (int d = 0; d < 2; ++d) {
+        dIn[d] = E.vpos[i][d] - E.fip[k][d];
+        dEx[d] = E.vpos[j][d] - E.fip[k][d];
+        dTot[d] = E.vpos[j][d] - E.vpos[i][d];
+    }
+    const double absTot2 = dTot[0] * dTot[0] + dTot[1] * dTot[1];
+    double gIn = 0.0, gEx = 0.0;
+    for (int d = 0; d < 2; ++d) gIn += P.g[d] * dIn[d];
+    for (int d = 0; d < 2; ++d) gEx += P.g[d] * dEx[d];
+    for (int a = 0; a < NP; ++a) {
+        const D pStatIn = -(focus(i, q[i]->rho[a]) * gIn);
+        const D pStatEx = -(focus(j, q[j]->rho[a]) * gEx);
+        const D fs = (pStatEx - pStatIn) / absTot2;
+        for (int d = 0; d < 2; ++d) pg[a][d] += dTot[d] * fs;
+    }
+    double Kh[2];
+    for (int d = 0; d < 2; ++d) Kh[d] = harmonicMean(P.perm[3 * E.v[i] + d], P.perm[3 * E.v[j] + d]);
+    for (int a = 0; a < NP; ++a) {
+        D tmp(0.0);
+        for (int d = 0; d < 2; ++d) tmp += pg[a][d] * n[d];
+        up[a] = tmp > 0 ? j : i;
+        const D mob = focus(up[a], q[up[a]]->lam[a]);
+        vf[a] = D(0.0);
+        for (int d = 0; d < 2; ++d) {
+            D fv = Kh[d] * pg[a][d];
+            fv *= -mob;
+            vf[a] += fv * n[d];
+        }
+    }
+}
+
 // FvBaseLocalResidual::eval of element e with focus corner f: res[c][eq]
 // the corners' residuals (divided by their total volumes), derivatives
 // with respect to corner f's primary variables; sc[c][eq] the parity scale
@@ -173,65 +246,13 @@ static void elementImmiscibleVcfv(Sim& S, const VcfvGrid& G, int e, int f, const
     // evalFluxes
     for (int k = 0; k < 4; ++k) {
         const int i = E.fi[k], j = E.fj[k];
-        const double* n = E.fn[k];
-        D2 pg[2][2];  // [phase][dim]
-        for (int a = 0; a < 2; ++a) {
-            if (G.p1) {
-                // P1FeGradientCalculator::calculateGradient
-                pg[a][0] = D2(0.0);
-                pg[a][1] = D2(0.0);
-                for (int c = 0; c < 4; ++c) {
-                    const D2 dofVal = focus(c, q[c]->p[a]);
-                    for (int d = 0; d < 2; ++d) pg[a][d] += dofVal * E.grad[k][c][d];
-                }
-            }
-            else {
-                // FvBaseGradientCalculator::calculateGradient (two-point)
-                D2 deltay;
-                if (i == f) deltay = valueOnly(q[j]->p[a]) - q[i]->p[a];
-                else if (j == f) deltay = q[j]->p[a] - valueOnly(q[i]->p[a]);
-                else deltay = valueOnly(q[j]->p[a]) - valueOnly(q[i]->p[a]);
-                double distSq = 0.0;
-                for (int d = 0; d < 2; ++d) {
-                    const double t = E.vpos[j][d] - E.vpos[i][d];
-                    distSq += t * t;
-                }
-                for (int d = 0; d < 2; ++d) pg[a][d] = deltay * ((E.vpos[j][d] - E.vpos[i][d]) / distSq);
-            }
-        }
-        // gravity (darcyfluxmodule.hh:214-283): posIn / posEx the vertices
-        double dIn[2], dEx[2], dTot[2];
-        for (int d = 0; d < 2; ++d) {
-            dIn[d] = E.vpos[i][d] - E.fip[k][d];
-            dEx[d] = E.vpos[j][d] - E.fip[k][d];
-            dTot[d] = E.vpos[j][d] - E.vpos[i][d];
-        }
-        const double absTot2 = dTot[0] * dTot[0] + dTot[1] * dTot[1];
-        double gIn = 0.0, gEx = 0.0;
-        for (int d = 0; d < 2; ++d) gIn += P.g[d] * dIn[d];
-        for (int d = 0; d < 2; ++d) gEx += P.g[d] * dEx[d];
-        for (int a = 0; a < 2; ++a) {
-            const D2 pStatIn = -(focus(i, q[i]->rho[a]) * gIn);
-            const D2 pStatEx = -(focus(j, q[j]->rho[a]) * gEx);
-            const D2 fs = (pStatEx - pStatIn) / absTot2;
-            for (int d = 0; d < 2; ++d) pg[a][d] += dTot[d] * fs;
-        }
-        double Kh[2];
-        for (int d = 0; d < 2; ++d) Kh[d] = harmonicMean(P.perm[3 * E.v[i] + d], P.perm[3 * E.v[j] + d]);
+        D2 vf[2];
+        int up[2];
+        vcfvPhaseFluxes<2, IQ2, 2>(P, G, E, k, f, q, vf, up);
         D2 flux[2];
         for (int a = 0; a < 2; ++a) {
-            D2 tmp(0.0);
-            for (int d = 0; d < 2; ++d) tmp += pg[a][d] * n[d];
-            const int up = tmp > 0 ? j : i;
-            const D2 mob = focus(up, q[up]->lam[a]);
-            D2 vf(0.0);
-            for (int d = 0; d < 2; ++d) {
-                D2 fv = Kh[d] * pg[a][d];
-                fv *= -mob;
-                vf += fv * n[d];
-            }
             flux[a] = D2(0.0);
-            flux[a] += vf * focus(up, q[up]->rho[a]);
+            flux[a] += vf[a] * focus(up[a], q[up[a]]->rho[a]);
         }
         const double alpha = 1.0 * E.fa[k];
         for (int a = 0; a < 2; ++a) flux[a] *= alpha;
@@ -329,6 +350,126 @@ static void elementImmiscibleVcfv(Sim& S, const VcfvGrid& G, int e, int f, const
             res[c][a] /= G.totalVolume[E.v[c]];
             sc[c][a] /= G.totalVolume[E.v[c]];
         }
+}
+
+// The black-oil model on the vertex-centred stencil (blackoillocalresidual.hh:
+// 101-367: component storage phi S invB (+ Rs for the gas dissolved in oil),
+// component fluxes of the upstream invB (and Rs) times the phase volume
+// flux, both scaled by the surface densities); boundaries are no-flow or
+// mass rate.  Same conventions as elementImmiscibleVcfv.
+static void elementBlackoilVcfv(Sim& S, const VcfvGrid& G, int e, int f, const IQ3* const (&q)[4], bool iter0,
+                                D3 (&res)[4][3], double (&sc)[4][3])
+{
+    const Prob& P = S.P;
+    const BlackOilPvt& T = P.pvt;
+    const double rhoRef[3] = {T.rhoRefW, T.rhoRefO, T.rhoRefG};
+    const int compOfPhase[3] = {1, 0, 2};
+    const VcfvElement& E = G.el[e];
+    for (int c = 0; c < 4; ++c)
+        for (int a = 0; a < 3; ++a) {
+            res[c][a] = D3(0.0);
+            sc[c][a] = 0.0;
+        }
+    auto focus = [&](int c, const D3& x) { return c == f ? x : valueOnly(x); };
+    // evalFluxes
+    for (int k = 0; k < 4; ++k) {
+        const int i = E.fi[k], j = E.fj[k];
+        D3 vf[3];
+        int up[3];
+        vcfvPhaseFluxes<3, IQ3, 3>(P, G, E, k, f, q, vf, up);
+        D3 flux[3] = {D3(0.0), D3(0.0), D3(0.0)};
+        for (int a = 0; a < 3; ++a) {
+            D3 invB = focus(up[a], q[up[a]]->invB[a]);
+            D3 svf = invB * vf[a];
+            flux[compOfPhase[a]] += svf * rhoRef[a];
+            if (a == 1) {
+                D3 Rs = focus(up[a], q[up[a]]->Rs);
+                flux[2] += Rs * svf * T.rhoRefG;
+            }
+        }
+        const double alpha = 1.0 * E.fa[k];
+        for (int a = 0; a < 3; ++a) flux[a] *= alpha;
+        for (int a = 0; a < 3; ++a) {
+            res[i][a] += flux[a];
+            res[j][a] -= flux[a];
+            sc[i][a] += std::abs(flux[a].v);
+            sc[j][a] += std::abs(flux[a].v);
+        }
+    }
+    // evalVolumeTerms_
+    for (int c = 0; c < 4; ++c) {
+        const double scvVolume = E.scvVol[c] * 1.0;
+        const int v = E.v[c];
+        const IQ3& qc = *q[c];
+        D3 tmp[3] = {D3(0.0), D3(0.0), D3(0.0)};
+        D3 phi(qc.phi);
+        for (int a = 0; a < 3; ++a) {
+            D3 sv = qc.S[a] * qc.invB[a] * phi;
+            tmp[compOfPhase[a]] += sv;
+            if (a == 1) tmp[2] += qc.Rs * sv;
+        }
+        tmp[1] *= T.rhoRefW;
+        tmp[2] *= T.rhoRefG;
+        tmp[0] *= T.rhoRefO;
+        if (c != f)
+            for (int a = 0; a < 3; ++a) tmp[a] = valueOnly(tmp[a]);
+        double tmp2[3];
+        if (iter0) {
+            for (int a = 0; a < 3; ++a) tmp2[a] = tmp[a].v;
+            for (int a = 0; a < 3; ++a) S.storageOld[v * 3 + a] = tmp2[a];
+        }
+        else
+            for (int a = 0; a < 3; ++a) tmp2[a] = S.storageOld[v * 3 + a];
+        for (int a = 0; a < 3; ++a) {
+            sc[c][a] += std::abs(tmp[a].v) * (scvVolume / S.dt) + std::abs(tmp2[a]) * (scvVolume / S.dt);
+            tmp[a] -= tmp2[a];
+            tmp[a] *= scvVolume / S.dt;
+            res[c][a] += tmp[a];
+        }
+        for (int a = 0; a < 3; ++a) res[c][a] -= 0.0 * scvVolume;
+    }
+    // evalBoundary_: mass-rate boundary faces (no-flow adds nothing)
+    for (int b = G.bfPtr[e]; b < G.bfPtr[e + 1]; ++b) {
+        if (P.bfType[b] != GBFV_BC_MASSRATE) continue;
+        const int c = G.bfCorner[b];
+        const double aa = P.bfArea[b] * 1.0;
+        for (int a = 0; a < 3; ++a) {
+            const D3 val = D3(P.bfValue[4 * b + a]) * aa;
+            res[c][a] += val;
+            sc[c][a] += std::abs(val.v);
+        }
+    }
+    for (int c = 0; c < 4; ++c)
+        for (int a = 0; a < 3; ++a) {
+            res[c][a] /= G.totalVolume[E.v[c]];
+            sc[c][a] /= G.totalVolume[E.v[c]];
+        }
+}
+
+static void linearizeBlackoilVcfv(Sim& S, const std::vector<IQ3>& iq)
+{
+    const VcfvGrid& G = *S.vcfv;
+    const bool iter0 = S.newtonIter == 0;
+    std::fill(S.rscale.begin(), S.rscale.end(), 0.0);
+    for (int e = 0; e < (int)G.el.size(); ++e) {
+        const VcfvElement& E = G.el[e];
+        D3 res[4][4][3];
+        double sc[4][4][3];
+        const IQ3* q[4] = {&iq[E.v[0]], &iq[E.v[1]], &iq[E.v[2]], &iq[E.v[3]]};
+        for (int f = 0; f < 4; ++f) elementBlackoilVcfv(S, G, e, f, q, iter0, res[f], sc[f]);
+        for (int f = 0; f < 4; ++f) {
+            const int gf = E.v[f];
+            for (int a = 0; a < 3; ++a) {
+                S.residual[gf * 3 + a] += res[f][f][a].v;
+                S.rscale[gf * 3 + a] += sc[f][f][a];
+            }
+            for (int j = 0; j < 4; ++j) {
+                double* blk = &S.J.val[(size_t)S.J.find(E.v[j], gf) * 9];
+                for (int a = 0; a < 3; ++a)
+                    for (int pv = 0; pv < 3; ++pv) blk[a * 3 + pv] += res[f][j][a].d[pv];
+            }
+        }
+    }
 }
 
 // FvBaseLinearizer::linearizeElement_ over all elements in grid order

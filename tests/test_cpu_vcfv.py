@@ -157,3 +157,59 @@ def test_fd_jacobian_approximates_the_ad_one(method):
     scale = np.max(np.abs(ja), axis=0)
     # eps ~ 1e-10: the round-off of the residual over eps dominates
     assert np.max(np.abs(jf - ja) / np.maximum(scale, 1e-300)) <= 2e-4
+
+
+def _bo_state(prob, seed=3):
+    """Pressures, water saturations and both gas meanings perturbed."""
+    rng = np.random.default_rng(seed)
+    pv = prob.init_pv.reshape(-1, 3).copy()
+    pv[:, 1] *= 1.0 + 0.01 * rng.standard_normal(len(pv))
+    pv[:, 0] = rng.uniform(0.1, 0.3, len(pv))
+    m = prob.init_meaning.copy()
+    m[::3] = capi.GAS_SG
+    pv[::3, 2] = rng.uniform(0.0, 0.2, len(pv[::3]))
+    return pv.ravel(), m
+
+
+def test_blackoil_jacobian_is_the_derivative_of_the_residual():
+    """The black-oil model on the vertex-centred stencil (the reference's
+    reservoir_blackoil_vcfv): component fluxes with the upstream 1/B and
+    R_s, component storage, wells as constraint vertices."""
+    prob = problems.blackoil_vcfv(12, 8)
+    o = O.Oracle(prob, capi.default_params(linear_tolerance=1e-8, newton_tolerance=1e-6))
+    assert o.linearize(86400.0, 0) == 0
+    pv, m = _bo_state(prob)
+    o.set_solution(pv, m)
+    assert o.linearize(86400.0, 1) == 0
+    r0 = o.residual()
+    rp, col, blk = o.jacobian()
+    n = len(rp) - 1
+    for i in (5, 20, 50, 80, 100):
+        for v in range(3):
+            h = 1e-7 * max(1.0, abs(pv[3 * i + v]))
+            pv2 = pv.copy()
+            pv2[3 * i + v] += h
+            o.set_solution(pv2, m)
+            assert o.linearize(86400.0, 1) == 0
+            fd = (o.residual() - r0) / h
+            J = np.zeros(3 * n)
+            for row in range(n):
+                for k in range(rp[row], rp[row + 1]):
+                    if col[k] == i:
+                        J[3 * row:3 * row + 3] = blk[k][:, v]
+            assert np.max(np.abs(fd - J)) <= 1e-5 * np.max(np.abs(J)), (i, v)
+
+
+def test_blackoil_fluxes_cancel_and_newton_converges():
+    prob = problems.blackoil_vcfv(12, 8, with_wells=False)
+    o = O.Oracle(prob, capi.default_params(linear_tolerance=1e-8, newton_tolerance=1e-6))
+    pv, m = _bo_state(prob)
+    o.set_solution(pv, m)
+    assert o.linearize(86400.0, 0) == 0
+    r = o.residual().reshape(-1, 3) * prob.volume[:, None]
+    sc = o.residual_scale().reshape(-1, 3) * prob.volume[:, None]
+    assert np.all(np.abs(r.sum(axis=0)) <= 1e-12 * sc.sum(axis=0))
+    wells = problems.blackoil_vcfv(12, 8)
+    o2 = O.Oracle(wells, capi.default_params(linear_tolerance=1e-8, newton_tolerance=1e-6))
+    st, _, nn, _, _ = o2.time_integration(4, 86400.0, fixed_dt=True)
+    assert st == 0 and np.all(nn >= 1) and np.all(nn <= 12)
