@@ -8,7 +8,8 @@
 // be compiled here, and its tests pin no numbers.  The restatement follows
 // the reference source line by line where the reference holds the code
 // (citations below); the opm-common / dune-istl parts it relies on are
-// restated from their published algorithms and listed in UNPINNED.md.
+// restated from their published algorithms and listed in the oracle's table
+// of unpinned choices.
 //
 // Followed files (paths inside OPM/opm-models):
 //   element loop, scatter, constraints  fvbaselinearizer.hh:510-666

@@ -4,7 +4,7 @@ ctypes binding of the CPU restatement (oracle/oracle.cc).  Only tests/,
 __graft_entry__.smoke() and bench.py's cpu_baseline / reference legs may
 import this module; the product path never does.  Parity status: unpinned
 against the reference's own output (the reference cannot be built here);
-see oracle/UNPINNED.md.
+the oracle's table of unpinned choices lists what it restates.
 """
 import ctypes as C
 import os

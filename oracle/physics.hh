@@ -3,7 +3,7 @@
 // Material laws and PVT restated from their published mathematics.  The
 // reference takes them from opm-common, which is not vendored under the
 // reference tree; every choice below that could not be read from the
-// reference is listed in oracle/UNPINNED.md.
+// reference is listed in the oracle's table of unpinned choices.
 //   - EffToAbsLaw<RegularizedVanGenuchten>: lensproblem.hh:111-121 (law),
 //     lensproblem.hh:245-258 (parameters)
 //   - 3-phase Corey relperm through the updateRelperms hook:
@@ -171,7 +171,7 @@ struct BlackOilPvt {
     // (BlackOilFluidSystem::inverseFormationVolumeFactor), else the
     // undersaturated extension through the bubble-point pressure (LiveOilPvt
     // set up from saturated tables only, reservoirproblem.hh:297-304; the
-    // extension's form is a row of oracle/UNPINNED.md)
+    // extension's form is a row of the oracle's table of unpinned choices)
     template <class E>
     void oil(const E& p, const E& Rs, bool saturated, E& invB, E& mu) const
     {
