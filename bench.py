@@ -362,36 +362,49 @@ def mixed_solve_errors(ctx, w, torch):
     return errs
 
 
-def lens_line(torch, vcfv=False):
+def lens_line(torch, vcfv=False, blackoil=False):
     """The 48x32 lens (lensproblem.hh:227-627), 30 time steps from dt0 = 250 s
     with the reference's dt control, FP64, BiCGStab + ILU(0) to 1e-6: the GPU
     (device time of the whole run, after one untimed run) beside the oracle
     (all host threads, and one).  vcfv: the same problem on the vertex-
     centred discretization with P1 gradients (lens_immiscible_vcfv_ad.cc),
-    49x33 vertices, the 9-point Jacobian through the general block ILU(0)."""
+    49x33 vertices, the 9-point Jacobian through the general block ILU(0).
+    blackoil: the black-oil vertical section on the vertex-centred grid
+    (reservoir_blackoil_vcfv's 2D configuration, 41x21 vertices, wells as
+    constraint vertices), 10 daily steps."""
     from gbfv import Context, capi, problems
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
-    prob = problems.lens_vcfv(LENS["nx"], LENS["ny"]) if vcfv else problems.lens(LENS["nx"], LENS["ny"])
-    prm = capi.default_params(linear_tolerance=1e-6)
+    steps, dt0, fixed = LENS["steps"], LENS["dt"], False
+    if blackoil:
+        prob = problems.blackoil_vcfv(40, 20)
+        prm = capi.default_params(linear_tolerance=1e-6, newton_tolerance=1e-6)
+        steps, dt0, fixed = 10, 86400.0, True
+    else:
+        prob = problems.lens_vcfv(LENS["nx"], LENS["ny"]) if vcfv else problems.lens(LENS["nx"], LENS["ny"])
+        prm = capi.default_params(linear_tolerance=1e-6)
     ctx = Context(prob, prm)
     ctx.save_state()
     ext = torch.cuda.ExternalStream(ctx.stream())
-    ctx.time_integration(LENS["steps"], LENS["dt"])
+    ctx.time_integration(steps, dt0, fixed_dt=fixed)
     ctx.restore_state()
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(ext)
-    st, sdt, sn, sl, _ = ctx.time_integration(LENS["steps"], LENS["dt"])
+    st, sdt, sn, sl, _ = ctx.time_integration(steps, dt0, fixed_dt=fixed)
     e1.record(ext)
     e1.synchronize()
     ms = e0.elapsed_time(e1)
     ctx.close()
     cits = int(sn.sum()) * prob.num_cells
-    what = ("lens-vcfv-48x32 two-phase immiscible (VG), vertex-centred, P1 gradients, 1617 vertices"
-            if vcfv else "lens-48x32 two-phase immiscible (VG), 1536 cells")
-    out = {"workload": what + ", 30 time steps from 250 s, FP64, BiCGStab+ILU0 to 1e-6",
+    if blackoil:
+        what = ("blackoil-vcfv-40x20 three-phase black-oil vertical section, vertex-centred, P1 gradients, "
+                "861 vertices, wells as constraint vertices, 10 steps of 1 day")
+    else:
+        what = ("lens-vcfv-48x32 two-phase immiscible (VG), vertex-centred, P1 gradients, 1617 vertices"
+                if vcfv else "lens-48x32 two-phase immiscible (VG), 1536 cells") + ", 30 time steps from 250 s"
+    out = {"workload": what + ", FP64, BiCGStab+ILU0 to 1e-6",
            "unit": "dof-Newton-iters/s", "status": st, "value": cits / (ms / 1e3), "ms": ms,
            "newton_iterations": int(sn.sum()), "linear_iterations": int(sl.sum()), "final_dt": float(sdt[-1])}
     O.build()
@@ -399,7 +412,7 @@ def lens_line(torch, vcfv=False):
         O.set_threads(threads)
         orc = O.Oracle(prob, prm)
         t0 = time.perf_counter()
-        sto, _, sno, _, _ = orc.time_integration(LENS["steps"], LENS["dt"])
+        sto, _, sno, _, _ = orc.time_integration(steps, dt0, fixed_dt=fixed)
         dt = time.perf_counter() - t0
         orc.close()
         out[name] = {"value": int(sno.sum()) * prob.num_cells / dt, "s": dt, "cores": threads,
@@ -717,6 +730,7 @@ def run_ours(args):
     if not args.headline_only:
         line["lens-48x32"] = lens_line(torch)
         line["lens-vcfv-48x32"] = lens_line(torch, vcfv=True)
+        line["blackoil-vcfv-40x20"] = lens_line(torch, blackoil=True)
         line["ensemble-64"] = ensemble_leg(64, torch)
     if world == 1 and not args.no_cpu_baseline:
         v, dt, threads = cpu_sample(prob, iters=1)
