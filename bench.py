@@ -420,7 +420,16 @@ def lens_line(torch, vcfv=False, blackoil=False):
     return out
 
 
-def solver_traffic(wl, kst):
+def solver_kernel_name(cfg):
+    """The persistent solve kernel a solver configuration runs."""
+    if cfg["mode"].startswith("gilu"):
+        return ("kGiluBicgstab<float,3,%s> (persistent block ILU(0) + BiCGStab, %s sweeps, cooperative grid of "
+                "%d blocks)" % ("tagged" if "tagged" in cfg["mode"] else "level",
+                               "tagged" if "tagged" in cfg["mode"] else "level-barrier", cfg["blocks"]))
+    return "kBicgstab<float,3> (persistent ILU0 + BiCGStab, %s launch of %d blocks)" % (cfg["mode"], cfg["blocks"])
+
+
+def solver_traffic(wl, kst, kernel=None):
     """DRAM traffic of the solver per launch: the ratio of DRAM bytes
     (dram__bytes_read.sum + dram__bytes_write.sum) to algorithmic bytes of an
     ncu capture of this workload's solve (profiles/traffic.json), applied to
@@ -429,6 +438,9 @@ def solver_traffic(wl, kst):
     try:
         with open(tfile) as f:
             ent = json.load(f).get(wl)
+        # the capture of the kernel this run's solves used
+        if ent and kernel and ent.get("kernel", "").split("<")[0] != kernel.split("<")[0]:
+            ent = None
         if ent:
             kind = ent.get("traffic_kind", "scaled from a capture of the cluster launch of the same kernel body")
             return ent["dram_per_algorithmic_byte"] * kst["solve_bytes"] / max(1, kst["solve_launches"]), kind
@@ -672,7 +684,7 @@ def run_ours(args):
     kst = mixed["kst"]
     achieved = kst["solve_bytes"] / (kst["solve_ms"] / 1000.0) / 1e9 if kst["solve_ms"] > 0 else 0.0
     avg_launch_ms = kst["solve_ms"] / max(1, kst["solve_launches"])
-    traffic, traffic_kind = solver_traffic(args.workload, kst)
+    traffic, traffic_kind = solver_traffic(args.workload, kst, solver_kernel_name(mixed["cfg"]))
     lin_ach = kst["linearize_bytes"] / (kst["linearize_ms"] / 1000.0) / 1e9 if kst["linearize_ms"] > 0 else 0.0
     for name in ("mixed", "fp64"):
         head[name]["ctx"].close()
@@ -698,8 +710,7 @@ def run_ours(args):
         "e2e": {"value": e2e_cits / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(N * 3 * 8 + N * 4),
                 "d2h_bytes_per_step": int(N * 3 * 8 + N * 4)},
         "gpu_launches": int(mixed["launches"] / args.steps),
-        "roofline": {"bound": "hbm", "kernel": "kBicgstab<float,3> (persistent ILU0 + BiCGStab, %s launch of %d blocks)"
-                     % (mixed["cfg"]["mode"], mixed["cfg"]["blocks"]),
+        "roofline": {"bound": "hbm", "kernel": solver_kernel_name(mixed["cfg"]),
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "traffic_kind": traffic_kind, "peak_kind": peak_kind,
                      "avg_launch_ms": avg_launch_ms,

@@ -456,6 +456,13 @@ int gbfv_solver_config(const gbfv_ctx* ctx, int precision, int* mode, int* block
  * 256 threads instead of 512 (a cheaper level step where a level's share per
  * block fits 256 rows; one of the autotuner's candidates)                  */
 #define GBFV_SOLVER_NARROW 8
+/* reported by gbfv_solver_config only: the precision's solves run in the
+ * general block ILU(0) kernel (vertex-centred grids, narrow systems, and
+ * the FP32 inner solves of systems wider than one block), with
+ * GBFV_SOLVER_TAGGED where its sweeps publish every row's result with a tag
+ * its consumers wait for instead of a barrier per wavefront level          */
+#define GBFV_SOLVER_GILU 16
+#define GBFV_SOLVER_TAGGED 32
 int gbfv_set_solver_config(gbfv_ctx* ctx, int precision, int mode, int blocks);
 int gbfv_reset_kernel_stats(gbfv_ctx* ctx);
 /* with GBFV_PROFILE set in the environment at creation: nanoseconds spent

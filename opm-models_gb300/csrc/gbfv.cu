@@ -149,6 +149,12 @@ struct SolverData {
     // createImpl), else NULL
     GiluData* gilu = nullptr;
     bool giluRoute = false;
+    // wide structured system (giluWide): the general kernel's tagged sweeps
+    // (no barrier per wavefront level) are a candidate of the autotuner for
+    // the precisions in giluCand and serve the solves of those in giluUse
+    // (bit 1 FP64, bit 2 the FP32 inner solve of the mixed form)
+    bool giluWide = false;
+    int giluCand = 0, giluUse = 0;
     // max-norm residual reduction the last solve reached: the FP64 true
     // residual for the mixed form, BiCGStab's residual for the plain one
     double lastReduction = 0.0, lastResidual = 0.0;
@@ -248,6 +254,16 @@ double solveBytes(const SolverData& S, int iters, int factor, int s)
     if (factor) B += N * (Sl * bb + (d + 1) * bb) * s + 4.0 * N * d;
     B += (double)iters * (N * (2 * Sl * bb + 4 * d * bb + 2 * bb) * s + 4.0 * N * (2 * Sl + 4 * d) + 30.0 * N * b * s);
     return B;
+}
+
+// a batched or served system solves in the batch kernel: no general ILU(0)
+void dropWideGilu(SolverData& S)
+{
+    if (!S.giluWide) return;
+    giluDestroy(S.gilu);
+    S.gilu = nullptr;
+    S.giluWide = false;
+    S.giluCand = S.giluUse = 0;
 }
 
 void freeSolver(SolverData& S)
@@ -901,7 +917,27 @@ void tuneSolver(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hs
     }
     S.mode[k] = pick.mode;
     S.nblk[k] = pick.nb;
+    // the general kernel's tagged sweeps, timed the same way (last entry of
+    // the timings); kept for this precision when they are the fastest
+    const int bit = k ? 2 : 1;
+    if (S.giluWide && (S.giluCand & bit)) {
+        int it = 0;
+        float ms = 0;
+        const int rs = giluSolve<T>(S.gilu, A, rhs, vec[0], 1, 0.0, 0.0, 1e300, 12, stream, st, hst, it, &ms, nullptr);
+        if (rs != GBFV_OK && rs != GBFV_ERR_NOT_CONVERGED) {
+            cudaGetLastError();
+            ms = 1e30f;
+        }
+        else if (idx < 16)
+            S.tuneMs[k][idx++] = ms;
+        if (ms < best) S.giluUse |= bit;
+        else S.giluUse &= ~bit;
+    }
 }
+
+template <class T>
+int runGilu(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hst, const T* A, const T* rhs, T* x,
+            int factor, double redTol, double absTol, double maxRes, int maxIter, int& iters);
 
 template <class T>
 int runKrylov(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hst, const T* A, T* FL, T* FD,
@@ -910,6 +946,8 @@ int runKrylov(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hst,
 {
     const int k = sizeof(T) == 4 ? 1 : 0;
     if (!S.tuned[k]) tuneSolver<T>(S, stream, st, hst, A, FL, FD, rhs, vec);
+    if (S.giluWide && (S.giluUse & (k ? 2 : 1)))
+        return runGilu<T>(S, stream, st, hst, A, rhs, vec[0], factor, redTol, absTol, maxRes, maxIter, iters);
     return runKrylovCfg<T>(S, stream, st, hst, A, FL, FD, rhs, vec, factor, redTol, absTol, maxRes, maxIter,
                            S.mode[k], S.nblk[k], iters, nullptr, true);
 }
@@ -981,7 +1019,7 @@ int solvePlain(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hst
         rs = runAmg<double>(S, stream, st, hst, A, rhs, S.v64[0], prm.linear_tolerance, absTolOf(prm),
                             prm.linear_max_error, prm.linear_max_iterations, iters);
     }
-    else if (S.gilu)
+    else if (S.gilu && !S.giluWide)
         rs = runGilu<double>(S, stream, st, hst, A, rhs, S.v64[0], 1, prm.linear_tolerance, absTolOf(prm),
                              prm.linear_max_error, prm.linear_max_iterations, iters);
     else
@@ -1033,7 +1071,8 @@ int solveMixed(SolverData& S, cudaStream_t stream, DevStatus* st, DevStatus* hst
         float* vec[6] = {S.v32[1], S.v32[2], S.v32[3], S.v32[4], S.v32[5], S.v32[6]};
         const int ks = amg ? runAmg<float>(S, stream, st, hst, S.A32, S.v32[0], S.v32[1], innerTol, 0.0,
                                            prm.linear_max_error, prm.linear_max_iterations, it)
-                       : S.gilu ? runGilu<float>(S, stream, st, hst, S.A32, S.v32[0], S.v32[1], ref == 0, innerTol, 0.0,
+                       : S.gilu && !S.giluWide
+                           ? runGilu<float>(S, stream, st, hst, S.A32, S.v32[0], S.v32[1], ref == 0, innerTol, 0.0,
                                                  prm.linear_max_error, prm.linear_max_iterations, it)
                            : runKrylov<float>(S, stream, st, hst, S.A32, S.FL32, S.FD32, S.v32[0], vec, ref == 0,
                                               innerTol, 0.0, prm.linear_max_error, prm.linear_max_iterations, it);
@@ -1791,6 +1830,31 @@ static int createImpl(gbfv_ctx* C, const gbfv_problem* P)
             S.giluRoute = S.gilu != nullptr;
         }
     }
+    // Wide systems (more rows than one block of the general kernel takes):
+    // the general kernel's tagged sweeps publish every row's result with a
+    // tag that its consumers wait for, instead of a barrier per wavefront
+    // level, over every SM of the GPU -- measured 1.7x (FP32) and 1.5x
+    // (FP64) faster than the best structured launch on the 1M-cell system,
+    // slower on the 200k-cell one.  So they are one more candidate of the
+    // autotuner, per precision.  GBFV_SOLVER=tagged takes them without
+    // tuning; another GBFV_SOLVER, gbfv_set_solver_config of a precision or
+    // GBFV_GILU_TAGGED=0 / GBFV_GILU_TAGGED64=0 leave them out.
+    const char* forced = getenv("GBFV_SOLVER");
+    const bool forceTagged = forced && strcmp(forced, "tagged") == 0;
+    if (!S.gilu && N > 65536 && (!forced || forceTagged)) {
+        int gst = GBFV_OK;
+        S.gilu = giluCreate(N, b, nslot, ld, hCol, S.col, levPtr, &gst);
+        S.giluCand = S.gilu ? (giluTagged(S.gilu, 0) ? 2 : 0) | (giluTagged(S.gilu, 1) ? 1 : 0) : 0;
+        S.giluWide = S.giluCand != 0;
+        if (!S.giluWide) {
+            giluDestroy(S.gilu);
+            S.gilu = nullptr;
+        }
+        else if (forceTagged) {  // GBFV_SOLVER=tagged: no autotuning
+            S.giluUse = S.giluCand;
+            S.tuned[0] = S.tuned[1] = 1;
+        }
+    }
     if ((st = devAlloc(&C->st, 1))) return st;
     CK(cudaMallocHost((void**)&C->hst, sizeof(DevStatus)));
     CK(cudaMemset(C->st, 0, sizeof(DevStatus)));
@@ -2298,7 +2362,7 @@ int gbfv_set_solver_config(gbfv_ctx* C, int precision, int mode, int blocks)
         ((mode & SYNC_NARROW) && (base != SYNC_HYBRID || k != 1 || (mode & SYNC_TILES))))
         return GBFV_ERR_ARG;
     SolverData& S = C->S;
-    if (S.gilu && !S.giluRoute) {
+    if (S.gilu && !S.giluRoute && !S.giluWide) {
         setError("a vertex-centred context solves with the general block ILU(0) only");
         return GBFV_ERR_UNSUPPORTED;
     }
@@ -2316,10 +2380,14 @@ int gbfv_set_solver_config(gbfv_ctx* C, int precision, int mode, int blocks)
     S.mode[k] = mode;
     S.nblk[k] = blocks;
     S.tuned[k] = 1;
-    if (S.giluRoute) {  // a forced configuration of the structured solver
+    if (S.giluWide) {  // this precision now solves with the structured kernel
+        S.giluUse &= ~(k ? 2 : 1);
+        S.giluCand &= ~(k ? 2 : 1);
+    }
+    if (S.giluRoute || (S.giluWide && !S.giluCand)) {  // a forced configuration of the structured solver
         giluDestroy(S.gilu);
         S.gilu = nullptr;
-        S.giluRoute = false;
+        S.giluRoute = S.giluWide = false;
     }
     return GBFV_OK;
 }
@@ -2328,6 +2396,14 @@ int gbfv_solver_config(const gbfv_ctx* C, int precision, int* mode, int* blocks,
 {
     if (!C) return GBFV_ERR_ARG;
     const int k = precision == GBFV_PREC_MIXED ? 1 : 0;
+    const SolverData& S = C->S;
+    if (S.gilu && (!S.giluWide || (S.giluUse & (k ? 2 : 1)))) {
+        // the general block ILU(0) kernel
+        if (mode) *mode = GBFV_SOLVER_GILU | (giluTagged(S.gilu, !k) ? GBFV_SOLVER_TAGGED : 0);
+        if (blocks) *blocks = giluBlocks(S.gilu);
+        if (nt) *nt = 0;
+        return GBFV_OK;
+    }
     if (mode) *mode = C->S.mode[k];
     if (blocks) *blocks = C->S.nblk[k];
     int n = 0;
@@ -3577,6 +3653,7 @@ gbfv_batch* gbfv_batch_create(const gbfv_problem* probs, int num_systems, const 
         int st = GBFV_OK;
         gbfv_ctx* C = gbfv_create(&probs[i], &B->prm, &st);
         if (!C) return fail(B, st ? st : GBFV_ERR_ARG);
+        dropWideGilu(C->S);
         B->ctx.push_back(C);
         if (i == 0) {
             B->b = C->b;
@@ -3805,6 +3882,7 @@ int gbfv_serve_admit(gbfv_batch* B, const gbfv_problem* prob, const double* pv, 
     C->S.mode[k] = SYNC_CLUSTER;
     C->S.nblk[k] = B->cluster;
     C->S.tuned[k] = 1;
+    dropWideGilu(C->S);
     B->ctx[i] = C;
     LinJob lj;
     SolveJob sj;

@@ -63,6 +63,12 @@ struct GiluArgs {
                          // the narrow sweeps with the vectors in shared memory
     unsigned long long* prof;  // optional phase timers (GBFV_GILU_PROFILE), 16 words
     int localFactor;     // at most 9 slots and GILU_MAX_UPD updates per row: factorRowLocal
+    // tagged sweeps (several blocks): row chunks of at most 32 rows inside
+    // one level, and the tagged words of every row component (one for
+    // FP32, two for FP64), zeroed before the launch
+    int tagged, numChunks;
+    const int* chunkPtr;      // [numChunks + 1]
+    unsigned long long* tw;   // [N * b * words]: tag << 32 | value bits
 };
 
 constexpr int WARP_SLOTS = 4;  // lower (and upper) slots the warp sweeps take
@@ -215,9 +221,189 @@ __device__ bool factorRowLocal(const GiluArgs<T>& a, int p)
 
 // v = (LU)^-1 d: the forward sweep over the levels, then the backward one
 // (dune-istl's blockILUBacksolve)
-template <class T, int B, class Bar>
-__device__ bool iluApply(const GiluArgs<T>& a, const T* d, T* v, int gt, int gs, const Bar& bar)
+// ------------------------------------------------------ tagged sweeps --
+// The FP32 sweeps of a system too wide for one block, without a barrier per
+// level: a row publishes each component of its result as one 64-bit word
+// {tag, value bits} (single-copy atomic: the value arrives with its tag),
+// and a row reads the words of the rows it depends on until they carry the
+// current sweep's tag.  The tags of one launch are 1, 2, 3, ... (forward
+// and backward sweep of every application); the words are zeroed before
+// the launch.  Rows are dealt to warps in chunks of at most 32 rows of one
+// level, chunk c to warp c mod W, the forward sweep in ascending and the
+// backward sweep in descending chunk order.  Every dependency lies in an
+// earlier level (later, backward), so the lowest unfinished chunk can
+// always proceed: the cooperative launch keeps every warp resident, and no
+// wait closes a cycle.  Every wait is bounded and gives up with the grid's
+// abort word.  Same operations in the same order as iluApply: the same
+// results to the bit.
+constexpr int TAG_SLOTS = 4;  // lower (upper) slots a tagged row takes
+
+// words per value: an FP32 value rides in one word, an FP64 value in two
+// (low and high half, each with the tag)
+template <class T>
+__host__ __device__ constexpr int tagWords() { return sizeof(T) / 4; }
+
+__device__ __forceinline__ void stWord(unsigned long long* p, unsigned tag, unsigned bits)
 {
+    const unsigned long long w = ((unsigned long long)tag << 32) | bits;
+    asm volatile("st.relaxed.gpu.global.b64 [%0], %1;\n" ::"l"(p), "l"(w) : "memory");
+}
+
+__device__ __forceinline__ unsigned long long ldWord(const unsigned long long* p)
+{
+    unsigned long long w;
+    asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];\n" : "=l"(w) : "l"(p) : "memory");
+    return w;
+}
+
+__device__ __forceinline__ void stTagged(unsigned long long* p, unsigned tag, float v) { stWord(p, tag, __float_as_uint(v)); }
+__device__ __forceinline__ void stTagged(unsigned long long* p, unsigned tag, double v)
+{
+    const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+    stWord(p, tag, (unsigned)u);
+    stWord(p + 1, tag, (unsigned)(u >> 32));
+}
+
+// the B components of the rows k[0..TAG_SLOTS) (k < 0: none) once every
+// word carries `tag`; false when the wait gave up
+template <class T, int B>
+__device__ __forceinline__ bool waitTagged(const unsigned long long* tw, const int (&k)[TAG_SLOTS], unsigned tag,
+                                           T (&x)[TAG_SLOTS][B], int* abort)
+{
+    constexpr int NW = tagWords<T>(), RW = B * NW;  // words per component, per row
+    static_assert(TAG_SLOTS * RW <= 32, "pending mask");
+    unsigned pending = 0;
+#pragma unroll
+    for (int s = 0; s < TAG_SLOTS; ++s)
+        if (k[s] >= 0) pending |= ((1u << RW) - 1u) << (s * RW);
+    unsigned lo[TAG_SLOTS][RW];
+    long long t0 = 0;
+    for (int round = 0; pending; ++round) {
+        unsigned long long w[TAG_SLOTS][RW];
+#pragma unroll
+        for (int s = 0; s < TAG_SLOTS; ++s)
+#pragma unroll
+            for (int q = 0; q < RW; ++q)
+                if (pending & (1u << (s * RW + q))) w[s][q] = ldWord(&tw[(size_t)k[s] * RW + q]);
+#pragma unroll
+        for (int s = 0; s < TAG_SLOTS; ++s)
+#pragma unroll
+            for (int q = 0; q < RW; ++q)
+                if ((pending & (1u << (s * RW + q))) && (unsigned)(w[s][q] >> 32) == tag) {
+                    lo[s][q] = (unsigned)w[s][q];
+                    pending &= ~(1u << (s * RW + q));
+                }
+        if (!pending) break;
+        if (round == 0) t0 = clock64();
+        else if ((round & 15) == 0) {
+            if (*(volatile int*)abort) return false;
+            if (clock64() - t0 > GB_TIMEOUT_CYCLES) {
+                atomicExch(abort, 1);
+                return false;
+            }
+        }
+        if (round >= 2) __nanosleep(32);
+    }
+#pragma unroll
+    for (int s = 0; s < TAG_SLOTS; ++s)
+#pragma unroll
+        for (int e = 0; e < B; ++e) {
+            if constexpr (NW == 1)
+                x[s][e] = __uint_as_float(lo[s][e]);
+            else
+                x[s][e] = __longlong_as_double(
+                    (long long)(((unsigned long long)lo[s][2 * e + 1] << 32) | lo[s][2 * e]));
+        }
+    return true;
+}
+
+template <class T, int B>
+__device__ __noinline__ bool taggedApply(const GiluArgs<T>& a, const T* d, T* v, unsigned& tag)
+{
+    constexpr int RW = B * tagWords<T>();
+    const unsigned tf = ++tag, tb = ++tag;
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, W = (gridDim.x * blockDim.x) >> 5;
+    const int ld = a.ld;
+    unsigned long long* tw = a.tw;
+    bool ok = true;
+    for (int c = gw; c < a.numChunks; c += W) {
+        const int p = a.chunkPtr[c] + lane;
+        if (ok && p < a.chunkPtr[c + 1]) {
+            T rhs[B];
+#pragma unroll
+            for (int e = 0; e < B; ++e) rhs[e] = ldcg(&d[p * B + e]);
+            int k[TAG_SLOTS];
+            T L[TAG_SLOTS][B * B];
+#pragma unroll
+            for (int s = 0; s < TAG_SLOTS; ++s) {
+                k[s] = s < a.diag ? a.col[(size_t)s * ld + p] : -1;
+                if (k[s] >= 0) ldBlk<T, B>(a.F, s, ld, p, L[s]);
+            }
+            T x[TAG_SLOTS][B];
+            if (!waitTagged<T, B>(tw, k, tf, x, a.gs.abort)) ok = false;
+#pragma unroll
+            for (int s = 0; s < TAG_SLOTS; ++s)
+                if (k[s] >= 0)
+#pragma unroll
+                    for (int i = 0; i < B; ++i)
+#pragma unroll
+                        for (int j = 0; j < B; ++j) rhs[i] -= L[s][i * B + j] * x[s][j];
+#pragma unroll
+            for (int e = 0; e < B; ++e) {
+                v[p * B + e] = rhs[e];
+                stTagged(&tw[(size_t)p * RW + e * tagWords<T>()], tf, rhs[e]);
+            }
+        }
+        __syncwarp();  // the warp's lanes move to the next chunk together
+    }
+    if (gw < a.numChunks) {
+        for (int c = gw + ((a.numChunks - 1 - gw) / W) * W; c >= 0; c -= W) {
+            const int p = a.chunkPtr[c] + lane;
+            if (ok && p < a.chunkPtr[c + 1]) {
+                T rhs[B];
+#pragma unroll
+                for (int e = 0; e < B; ++e) rhs[e] = v[p * B + e];
+                // upper slots in descending order, as iluApply takes them
+                int k[TAG_SLOTS];
+                T U[TAG_SLOTS][B * B];
+#pragma unroll
+                for (int q = 0; q < TAG_SLOTS; ++q) {
+                    const int s = a.nslot - 1 - q;
+                    k[q] = s > a.diag ? a.col[(size_t)s * ld + p] : -1;
+                    if (k[q] >= 0) ldBlk<T, B>(a.F, s, ld, p, U[q]);
+                }
+                T Di[B * B];
+                ldBlk<T, B>(a.F, a.diag, ld, p, Di);
+                T x[TAG_SLOTS][B];
+                if (!waitTagged<T, B>(tw, k, tb, x, a.gs.abort)) ok = false;
+#pragma unroll
+                for (int q = 0; q < TAG_SLOTS; ++q)
+                    if (k[q] >= 0)
+#pragma unroll
+                        for (int i = 0; i < B; ++i)
+#pragma unroll
+                            for (int j = 0; j < B; ++j) rhs[i] -= U[q][i * B + j] * x[q][j];
+#pragma unroll
+                for (int i = 0; i < B; ++i) {
+                    T t = T(0);
+#pragma unroll
+                    for (int j = 0; j < B; ++j) t += Di[i * B + j] * rhs[j];
+                    v[p * B + i] = t;
+                    stTagged(&tw[(size_t)p * RW + i * tagWords<T>()], tb, t);
+                }
+            }
+            __syncwarp();
+        }
+    }
+    // the grid barrier after the sweeps makes v visible to every block
+    return gridBarrier(a.gs) && ok;
+}
+
+template <class T, int B, bool TG, class Bar>
+__device__ bool iluApply(const GiluArgs<T>& a, const T* d, T* v, int gt, int gs, const Bar& bar, unsigned& tag)
+{
+    if constexpr (TG) return taggedApply<T, B>(a, d, v, tag);
     if (a.warpSweep) {
         extern __shared__ __align__(16) unsigned char gsmem[];
         narrowSweeps<T, B>(a, d, v, gsmem);
@@ -483,7 +669,7 @@ struct GBar {
 
 // BiCGStabSolver::apply (bicgstabsolver.hh:120-330) with the block ILU(0)
 // preconditioner, factorization included, in one cooperative launch
-template <class T, int B>
+template <class T, int B, bool TG>
 __global__ void __launch_bounds__(GILU_THREADS) kGiluBicgstab(const GiluArgs<T> a)
 {
     const Team<SYNC_GRID> tm;
@@ -495,6 +681,7 @@ __global__ void __launch_bounds__(GILU_THREADS) kGiluBicgstab(const GiluArgs<T> 
     // preconditioner, [4] SpMV + dot, [5] x / r update, [6] second
     // preconditioner, [7] SpMV + dots, [8] last update
     PhaseClock clk(a.prof, gt);
+    unsigned tag = 0;  // tagged sweeps: the last tag used
     if (a.factor) {
         if (!factorAll<T, B>(a, gt, gs, bar)) goto timeout;
         if (*(volatile int*)&a.st->code != 0) return;
@@ -577,7 +764,7 @@ __global__ void __launch_bounds__(GILU_THREADS) kGiluBicgstab(const GiluArgs<T> 
                 if (!gridBarrier(a.gs)) goto timeout;
             }
             clk.tick(2);
-            if (!iluApply<T, B>(a, a.p, a.y, gt, gs, bar)) goto timeout;
+            if (!iluApply<T, B, TG>(a, a.p, a.y, gt, gs, bar, tag)) goto timeout;
             clk.tick(3);
             {
                 double dd[1] = {0.0};
@@ -642,7 +829,7 @@ __global__ void __launch_bounds__(GILU_THREADS) kGiluBicgstab(const GiluArgs<T> 
                 if (stag || resErr > a.maxRes) break;
             }
             clk.tick(5);
-            if (!iluApply<T, B>(a, a.r, a.z, gt, gs, bar)) goto timeout;
+            if (!iluApply<T, B, TG>(a, a.r, a.z, gt, gs, bar, tag)) goto timeout;
             clk.tick(6);
             {
                 double dd[2] = {0.0, 0.0};
@@ -715,17 +902,18 @@ timeout:
 }
 
 // factorization and one preconditioner application alone (tests)
-template <class T, int B>
+template <class T, int B, bool TG>
 __global__ void __launch_bounds__(GILU_THREADS) kGiluApply(const GiluArgs<T> a)
 {
     const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
     const GBar bar{&a.gs};
+    unsigned tag = 0;
     if (!factorAll<T, B>(a, gt, gs, bar)) {
         if (gt == 0) a.st->code = GBFV_ERR_TIMEOUT;
         return;
     }
     if (*(volatile int*)&a.st->code != 0) return;
-    if (!iluApply<T, B>(a, a.rhs, a.x, gt, gs, bar) && gt == 0) a.st->code = GBFV_ERR_TIMEOUT;
+    if (!iluApply<T, B, TG>(a, a.rhs, a.x, gt, gs, bar, tag) && gt == 0) a.st->code = GBFV_ERR_TIMEOUT;
 }
 
 }  // namespace
@@ -747,6 +935,10 @@ struct GiluData {
     cudaEvent_t evA = nullptr, evB = nullptr;
     size_t nnz = 0;
     unsigned long long* prof = nullptr;  // GBFV_GILU_PROFILE phase timers
+    int tagged = 0, tagged64 = 0;  // tagged sweeps of FP32 / FP64 solves (several blocks)
+    int numChunks = 0;
+    int* chunkPtr = nullptr;
+    unsigned long long* tw = nullptr;
 };
 
 GiluData* giluCreate(int N, int b, int nslot, int ld, const std::vector<int>& colHost, const int* colDev,
@@ -815,9 +1007,12 @@ GiluData* giluCreate(int N, int b, int nslot, int ld, const std::vector<int>& co
     int dev = 0, nsm = 1, occ = 1 << 20;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    for (const void* fn : {b == 2 ? (const void*)kGiluBicgstab<double, 2> : (const void*)kGiluBicgstab<double, 3>,
-                           b == 2 ? (const void*)kGiluBicgstab<float, 2> : (const void*)kGiluBicgstab<float, 3>,
-                           b == 2 ? (const void*)kGiluApply<double, 2> : (const void*)kGiluApply<double, 3>}) {
+    for (const void* fn : {b == 2 ? (const void*)kGiluBicgstab<double, 2, false> : (const void*)kGiluBicgstab<double, 3, false>,
+                           b == 2 ? (const void*)kGiluBicgstab<float, 2, false> : (const void*)kGiluBicgstab<float, 3, false>,
+                           b == 2 ? (const void*)kGiluApply<double, 2, false> : (const void*)kGiluApply<double, 3, false>,
+                           b == 2 ? (const void*)kGiluBicgstab<double, 2, true> : (const void*)kGiluBicgstab<double, 3, true>,
+                           b == 2 ? (const void*)kGiluBicgstab<float, 2, true> : (const void*)kGiluBicgstab<float, 3, true>,
+                           b == 2 ? (const void*)kGiluApply<double, 2, true> : (const void*)kGiluApply<double, 3, true>}) {
         int o = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, fn, GILU_THREADS, 0);
         occ = std::min(occ, o);
@@ -836,17 +1031,33 @@ GiluData* giluCreate(int N, int b, int nslot, int ld, const std::vector<int>& co
     if (const char* e = getenv("GBFV_GILU_WARP")) d->warp = d->warp && atoi(e) != 0;
     if (d->warp) {
         const int bytes = (int)nb;
-        for (const void* fn : {b == 2 ? (const void*)kGiluBicgstab<double, 2> : (const void*)kGiluBicgstab<double, 3>,
-                               b == 2 ? (const void*)kGiluBicgstab<float, 2> : (const void*)kGiluBicgstab<float, 3>,
-                               b == 2 ? (const void*)kGiluApply<double, 2> : (const void*)kGiluApply<double, 3>})
+        for (const void* fn : {b == 2 ? (const void*)kGiluBicgstab<double, 2, false> : (const void*)kGiluBicgstab<double, 3, false>,
+                               b == 2 ? (const void*)kGiluBicgstab<float, 2, false> : (const void*)kGiluBicgstab<float, 3, false>,
+                               b == 2 ? (const void*)kGiluApply<double, 2, false> : (const void*)kGiluApply<double, 3, false>})
             if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess)
                 d->warp = 0;
     }
-    const size_t nv = (size_t)N * b + 16;
+    // tagged sweeps for systems on several blocks whose rows have at most
+    // TAG_SLOTS lower and upper entries: FP32 (GBFV_GILU_TAGGED=0: off) and
+    // FP64 (GBFV_GILU_TAGGED64=0: off); chunks of at most 32 rows inside
+    // one level
+    d->tagged = d->tagged64 = blocks > 1 && diagSlot <= TAG_SLOTS && nslot - 1 - diagSlot <= TAG_SLOTS;
+    if (const char* e = getenv("GBFV_GILU_TAGGED64")) d->tagged64 = d->tagged64 && atoi(e) != 0;
+    if (const char* e = getenv("GBFV_GILU_TAGGED")) d->tagged = d->tagged && atoi(e) != 0;
+    // the tagged sweeps take every SM (more warps in flight per level: 139
+    // against 158 ms for a 200k-cell FP32 solve on 152 against 49 blocks)
+    if ((d->tagged || d->tagged64) && !getenv("GBFV_GILU_BLOCKS")) d->blocks = blocks = maxCoop;
+    if (d->tagged || d->tagged64) {
+        std::vector<int> chunks;
+        for (int l = 0; l < d->numLev; ++l)
+            for (int p = levPtr[l]; p < levPtr[l + 1]; p += 32) chunks.push_back(p);
+        chunks.push_back(N);
+        d->numChunks = (int)chunks.size() - 1;
+        if (!up(&d->chunkPtr, chunks)) return fail(GBFV_ERR_OOM, "");
+    }
+    // the factors and vectors of a precision are allocated at its first solve
     if (cudaMalloc((void**)&d->partial, sizeof(double) * 4 * (size_t)std::max(blocks, 16)) != cudaSuccess ||
-        cudaMalloc((void**)&d->bar, 4 * sizeof(unsigned)) != cudaSuccess ||
-        cudaMalloc((void**)&d->vec64, sizeof(double) * 6 * nv) != cudaSuccess ||
-        cudaMalloc((void**)&d->F64, sizeof(double) * (size_t)nslot * b * b * ld) != cudaSuccess)
+        cudaMalloc((void**)&d->bar, 4 * sizeof(unsigned)) != cudaSuccess)
         return fail(GBFV_ERR_OOM, "");
     cudaMemset(d->bar, 0, 4 * sizeof(unsigned));
     cudaEventCreate(&d->evA);
@@ -854,6 +1065,9 @@ GiluData* giluCreate(int N, int b, int nslot, int ld, const std::vector<int>& co
     if (status) *status = GBFV_OK;
     return d;
 }
+
+int giluTagged(const GiluData* d, int fp64) { return d ? (fp64 ? d->tagged64 : d->tagged) : 0; }
+int giluBlocks(const GiluData* d) { return d ? d->blocks : 0; }
 
 void giluDestroy(GiluData* d)
 {
@@ -868,6 +1082,8 @@ void giluDestroy(GiluData* d)
     cudaFree(d->partial);
     cudaFree(d->bar);
     cudaFree(d->prof);
+    cudaFree(d->chunkPtr);
+    cudaFree(d->tw);
     if (d->evA) cudaEventDestroy(d->evA);
     if (d->evB) cudaEventDestroy(d->evB);
     delete d;
@@ -882,6 +1098,9 @@ int args(GiluData& d, GiluArgs<T>& a, const T* A, const T* rhs, DevStatus* st)
     T* vec;
     T* F;
     if (sizeof(T) == 8) {
+        if (!d.vec64 && (cudaMalloc((void**)&d.vec64, sizeof(double) * 6 * nv) != cudaSuccess ||
+                         cudaMalloc((void**)&d.F64, sizeof(double) * (size_t)d.nslot * d.b * d.b * d.ld) != cudaSuccess))
+            return GBFV_ERR_OOM;
         vec = (T*)d.vec64;
         F = (T*)d.F64;
     }
@@ -892,6 +1111,10 @@ int args(GiluData& d, GiluArgs<T>& a, const T* A, const T* rhs, DevStatus* st)
         vec = (T*)d.vec32;
         F = (T*)d.F32;
     }
+    const bool tagged = sizeof(T) == 4 ? d.tagged : d.tagged64;
+    // tagged words: two per component (enough for FP64)
+    if (tagged && !d.tw && cudaMalloc((void**)&d.tw, sizeof(unsigned long long) * 2 * (size_t)d.N * d.b) != cudaSuccess)
+        return GBFV_ERR_OOM;
     a.N = d.N;
     a.ld = d.ld;
     a.nslot = d.nslot;
@@ -919,6 +1142,10 @@ int args(GiluData& d, GiluArgs<T>& a, const T* A, const T* rhs, DevStatus* st)
     a.warpSweep = d.warp;
     a.prof = d.prof;
     a.localFactor = d.localFactor;
+    a.tagged = tagged;
+    a.numChunks = d.numChunks;
+    a.chunkPtr = d.chunkPtr;
+    a.tw = d.tw;
     return GBFV_OK;
 }
 
@@ -961,8 +1188,11 @@ int giluSolve(GiluData* d, const T* A, const T* rhs, T* x, int factor, double re
     if (cudaMemsetAsync(st, 0, sizeof(DevStatus), s) != cudaSuccess ||
         cudaMemsetAsync(d->bar, 0, 4 * sizeof(unsigned), s) != cudaSuccess)
         return GBFV_ERR_CUDA;
+    if (a.tagged && cudaMemsetAsync(d->tw, 0, sizeof(T) * 2 * (size_t)d->N * d->b, s) != cudaSuccess)
+        return GBFV_ERR_CUDA;
     cudaEventRecord(d->evA, s);
-    const void* fn = d->b == 2 ? (const void*)kGiluBicgstab<T, 2> : (const void*)kGiluBicgstab<T, 3>;
+    const void* fn = a.tagged ? (d->b == 2 ? (const void*)kGiluBicgstab<T, 2, true> : (const void*)kGiluBicgstab<T, 3, true>)
+                              : (d->b == 2 ? (const void*)kGiluBicgstab<T, 2, false> : (const void*)kGiluBicgstab<T, 3, false>);
     if ((rs = launch<T>(fn, a, d->blocks, d->b, s))) return rs;
     if (cudaMemcpyAsync(x, a.x, sizeof(T) * (size_t)d->N * d->b, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
         return GBFV_ERR_CUDA;
@@ -1005,9 +1235,11 @@ int giluApply64(GiluData* d, const double* A, const double* dv, double* v, cudaS
     if ((rs = args<double>(*d, a, A, dv, st))) return rs;
     a.factor = 1;
     if (cudaMemsetAsync(st, 0, sizeof(DevStatus), s) != cudaSuccess ||
-        cudaMemsetAsync(d->bar, 0, 4 * sizeof(unsigned), s) != cudaSuccess)
+        cudaMemsetAsync(d->bar, 0, 4 * sizeof(unsigned), s) != cudaSuccess ||
+        (a.tagged && cudaMemsetAsync(d->tw, 0, sizeof(double) * 2 * (size_t)d->N * d->b, s) != cudaSuccess))
         return GBFV_ERR_CUDA;
-    const void* fn = d->b == 2 ? (const void*)kGiluApply<double, 2> : (const void*)kGiluApply<double, 3>;
+    const void* fn = a.tagged ? (d->b == 2 ? (const void*)kGiluApply<double, 2, true> : (const void*)kGiluApply<double, 3, true>)
+                              : (d->b == 2 ? (const void*)kGiluApply<double, 2, false> : (const void*)kGiluApply<double, 3, false>);
     if ((rs = launch<double>(fn, a, d->blocks, d->b, s))) return rs;
     if (cudaMemcpyAsync(v, a.x, sizeof(double) * (size_t)d->N * d->b, cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
         cudaMemcpyAsync(hst, st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s) != cudaSuccess ||

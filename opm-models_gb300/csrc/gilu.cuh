@@ -23,6 +23,10 @@ struct GiluData;
 GiluData* giluCreate(int N, int b, int nslot, int ld, const std::vector<int>& colHost, const int* colDev,
                      const std::vector<int>& levPtr, int* status);
 void giluDestroy(GiluData* d);
+// whether the solves of a precision sweep with tagged words (no barrier per
+// level), and the blocks of the launch
+int giluTagged(const GiluData* d, int fp64);
+int giluBlocks(const GiluData* d);
 
 // BiCGStab + block ILU(0) (the reference's ParallelBiCGStabSolverBackend
 // with Dune::SeqILU<..., 0> in natural order) in one persistent launch: the

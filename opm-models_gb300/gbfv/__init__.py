@@ -164,6 +164,9 @@ class Context:
         mode, nb, nt = C.c_int(), C.c_int(), C.c_int()
         ms = np.zeros(16)
         self.lib.gbfv_solver_config(self.h, precision, C.byref(mode), C.byref(nb), _d(ms), C.byref(nt))
+        if mode.value & capi.SOLVER_GILU:
+            name = "gilu+tagged" if mode.value & capi.SOLVER_TAGGED else "gilu"
+            return {"mode": name, "blocks": nb.value, "tune_ms": []}
         name = {0: "grid", 1: "cluster", 2: "hybrid"}.get(mode.value & 3, "?")
         if mode.value & capi.SOLVER_NARROW:
             name += "-256"

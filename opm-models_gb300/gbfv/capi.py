@@ -50,6 +50,8 @@ SOLVER_CLUSTER = 1
 SOLVER_HYBRID = 2
 SOLVER_TILES = 4   # or-ed into SOLVER_CLUSTER / SOLVER_HYBRID: spatial-tile sweeps
 SOLVER_NARROW = 8  # or-ed into SOLVER_HYBRID (mixed precision): 256-thread blocks
+SOLVER_GILU = 16   # reported: the general block ILU(0) kernel
+SOLVER_TAGGED = 32  # reported with SOLVER_GILU: tagged sweeps, no barrier per level
 LIN_AD = 0         # local linearizer: automatic differentiation
 LIN_FD = 1         # finite differences (FvBaseFdLocalLinearizer)
 LINSOLVER_ILU0 = 0  # linear solver: BiCGStab + block ILU(0)

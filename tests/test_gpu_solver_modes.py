@@ -103,3 +103,37 @@ def test_narrow_hybrid_mixed_keeps_the_fp64_newton_counts(built):
     assert np.array_equal(n, n64), (n, n64)
     assert np.array_equal(m, m64)
     assert rel_state_diff(x, x64, 3) <= 2e-5
+
+
+@pytest.mark.parametrize("prec", [capi.PREC_MIXED, capi.PREC_FP64])
+def test_tagged_sweeps_equal_the_cluster_sweeps(built, monkeypatch, prec):
+    """A system wider than one block of the general kernel (72,000 cells)
+    solved with its tagged sweeps (GBFV_SOLVER=tagged: every row publishes
+    its result with a tag that its consumers wait for; no barrier per
+    wavefront level) against the structured cluster sweeps forced on the
+    same system.  FP32 inner solves: the same operations, so the same
+    iteration counts and states.  FP64: the general kernel contracts its
+    products to FMAs and the structured one does not, so the solves (here to
+    1e-10) differ by rounding -- the same Newton counts and gas meanings,
+    linear iteration counts within 10 %, states within 1e-8."""
+    monkeypatch.setenv("GBFV_SOLVER", "tagged")
+    prob = problems.blackoil(60, 60, 20, seed=7)
+    fp32 = prec == capi.PREC_MIXED
+    prm = capi.default_params(linear_tolerance=1e-6 if fp32 else 1e-10, newton_tolerance=1e-6, precision=prec,
+                              inner_tolerance=1e-6)
+    ctx = Context(prob, prm)
+    assert ctx.solver_config(prec)["mode"] == "gilu+tagged"
+    st, _, sn, sl, _ = ctx.time_integration(2, 86400.0, fixed_dt=True)
+    x, m = ctx.solution()
+    assert ctx.solver_config(prec)["mode"] == "gilu+tagged"
+    ctx.close()
+    monkeypatch.delenv("GBFV_SOLVER")
+    st2, sn2, sl2, x2, m2, cfg = _run(prob, prm, prec, capi.SOLVER_CLUSTER, 16, 2, 86400.0)
+    assert st == 0 and st2 == 0 and cfg["mode"] == "cluster"
+    assert np.array_equal(sn, sn2) and np.array_equal(m, m2)
+    sl, sl2 = np.asarray(sl), np.asarray(sl2)
+    if fp32:
+        assert np.abs(sl - sl2).max() <= 2, (sl, sl2)
+    else:
+        assert np.all(np.abs(sl - sl2) <= 0.1 * sl2), (sl, sl2)
+    assert rel_state_diff(x, x2, 3) <= 1e-8

@@ -234,3 +234,27 @@ def test_blackoil_time_loop_matches_the_oracle(built):
     pvg, mg = ctx.solution()
     assert np.array_equal(mo, mg)
     assert rel_state_diff(pvg, pvo, 3) <= 1e-8
+
+
+@pytest.mark.parametrize("prec", [capi.PREC_MIXED, capi.PREC_FP64])
+def test_tagged_sweeps_equal_level_sweeps(built, monkeypatch, prec):
+    """The general kernel on 8 blocks (the narrow path off): its tagged
+    sweeps (rows publish tagged results, no barrier per level) give the
+    level-barrier sweeps' solution to the bit, iteration count included."""
+    prob = problems.lens_vcfv()
+    prm = _prm(precision=prec)
+    monkeypatch.setenv("GBFV_GILU_BLOCKS", "8")
+    monkeypatch.setenv("GBFV_GILU_WARP", "0")
+    out = []
+    for tagged in ("0", "1"):
+        monkeypatch.setenv("GBFV_GILU_TAGGED", tagged)
+        monkeypatch.setenv("GBFV_GILU_TAGGED64", tagged)
+        ctx = Context(prob, prm)
+        mode = ctx.solver_config(prec)["mode"]
+        assert mode == ("gilu+tagged" if tagged == "1" else "gilu"), mode
+        assert ctx.linearize(250.0, 0) == 0
+        out.append(ctx.solve())
+        ctx.close()
+    (s0, x0, i0), (s1, x1, i1) = out
+    assert s0 == 0 and s1 == 0 and i0 == i1
+    assert np.array_equal(x0, x1)
