@@ -66,7 +66,7 @@ struct GiluArgs {
     // tagged sweeps (several blocks): row chunks of at most 32 rows inside
     // one level, and the tagged words of every row component (one for
     // FP32, two for FP64), zeroed before the launch
-    int tagged, numChunks;
+    int tagged, numChunks, pollNs;  // pollNs: back-off between polls after the second
     const int* chunkPtr;      // [numChunks + 1]
     unsigned long long* tw;   // [N * b * words]: tag << 32 | value bits
 };
@@ -268,7 +268,7 @@ __device__ __forceinline__ void stTagged(unsigned long long* p, unsigned tag, do
 // word carries `tag`; false when the wait gave up
 template <class T, int B>
 __device__ __forceinline__ bool waitTagged(const unsigned long long* tw, const int (&k)[TAG_SLOTS], unsigned tag,
-                                           T (&x)[TAG_SLOTS][B], int* abort)
+                                           T (&x)[TAG_SLOTS][B], int* abort, int pollNs)
 {
     constexpr int NW = tagWords<T>(), RW = B * NW;  // words per component, per row
     static_assert(TAG_SLOTS * RW <= 32, "pending mask");
@@ -302,7 +302,7 @@ __device__ __forceinline__ bool waitTagged(const unsigned long long* tw, const i
                 return false;
             }
         }
-        if (round >= 2) __nanosleep(32);
+        if (round >= 2 && pollNs > 0) __nanosleep(pollNs);
     }
 #pragma unroll
     for (int s = 0; s < TAG_SLOTS; ++s)
@@ -341,7 +341,7 @@ __device__ __noinline__ bool taggedApply(const GiluArgs<T>& a, const T* d, T* v,
                 if (k[s] >= 0) ldBlk<T, B>(a.F, s, ld, p, L[s]);
             }
             T x[TAG_SLOTS][B];
-            if (!waitTagged<T, B>(tw, k, tf, x, a.gs.abort)) ok = false;
+            if (!waitTagged<T, B>(tw, k, tf, x, a.gs.abort, a.pollNs)) ok = false;
 #pragma unroll
             for (int s = 0; s < TAG_SLOTS; ++s)
                 if (k[s] >= 0)
@@ -376,7 +376,7 @@ __device__ __noinline__ bool taggedApply(const GiluArgs<T>& a, const T* d, T* v,
                 T Di[B * B];
                 ldBlk<T, B>(a.F, a.diag, ld, p, Di);
                 T x[TAG_SLOTS][B];
-                if (!waitTagged<T, B>(tw, k, tb, x, a.gs.abort)) ok = false;
+                if (!waitTagged<T, B>(tw, k, tb, x, a.gs.abort, a.pollNs)) ok = false;
 #pragma unroll
                 for (int q = 0; q < TAG_SLOTS; ++q)
                     if (k[q] >= 0)
@@ -936,6 +936,11 @@ struct GiluData {
     size_t nnz = 0;
     unsigned long long* prof = nullptr;  // GBFV_GILU_PROFILE phase timers
     int tagged = 0, tagged64 = 0;  // tagged sweeps of FP32 / FP64 solves (several blocks)
+    // back-off of a waiting row between polls (GBFV_GILU_POLL_NS): none --
+    // on the 1M-cell FP32 solve 0 / 16 / 32 / 100 / 250 ns measured 295 /
+    // 304 / 309 / 310 / 310 ms, so the polls' L2 traffic does not slow the
+    // producers and a sleep only adds latency
+    int pollNs = 0;
     int numChunks = 0;
     int* chunkPtr = nullptr;
     unsigned long long* tw = nullptr;
@@ -1044,6 +1049,7 @@ GiluData* giluCreate(int N, int b, int nslot, int ld, const std::vector<int>& co
     d->tagged = d->tagged64 = blocks > 1 && diagSlot <= TAG_SLOTS && nslot - 1 - diagSlot <= TAG_SLOTS;
     if (const char* e = getenv("GBFV_GILU_TAGGED64")) d->tagged64 = d->tagged64 && atoi(e) != 0;
     if (const char* e = getenv("GBFV_GILU_TAGGED")) d->tagged = d->tagged && atoi(e) != 0;
+    if (const char* e = getenv("GBFV_GILU_POLL_NS")) d->pollNs = std::max(0, std::min(1000, atoi(e)));
     // the tagged sweeps take every SM (more warps in flight per level: 139
     // against 158 ms for a 200k-cell FP32 solve on 152 against 49 blocks)
     if ((d->tagged || d->tagged64) && !getenv("GBFV_GILU_BLOCKS")) d->blocks = blocks = maxCoop;
@@ -1143,6 +1149,7 @@ int args(GiluData& d, GiluArgs<T>& a, const T* A, const T* rhs, DevStatus* st)
     a.prof = d.prof;
     a.localFactor = d.localFactor;
     a.tagged = tagged;
+    a.pollNs = d.pollNs;
     a.numChunks = d.numChunks;
     a.chunkPtr = d.chunkPtr;
     a.tw = d.tw;
