@@ -483,8 +483,11 @@ def latency_floor(w, kst, clocks):
     wavefront level count (nx + ny + nz - 2 on these grids), every BiCGStab
     iteration runs two preconditioner applications of a forward and a
     backward sweep over all levels, and no level step can be shorter than
-    one hop of its result to the next level's CTA.  floor_ms = iterations x
-    4 x levels x hop; frac = floor_ms / the solver's measured time."""
+    one hop of its result to the next level's CTA.  The hop is the
+    cluster's distributed-shared-memory hop; the tagged sweeps pass a
+    result through L2, which takes longer, so the floor bounds both.
+    floor_ms = iterations x 4 x levels x hop; frac = floor_ms / the
+    solver's measured time."""
     levels = w["nx"] + w["ny"] + w["nz"] - 2
     mhz = (clocks or {}).get("sm_mhz") or 2070.0
     hop_us = LEVEL_HOP_CYCLES / mhz
