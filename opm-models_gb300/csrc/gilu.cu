@@ -16,7 +16,8 @@
 // sweeps and BiCGStab (bicgstabsolver.hh:120-330, the structured solver's
 // iteration and criterion) run in the same persistent launch: one block
 // (block barriers) for systems whose levels fit a block, else a cooperative
-// grid with the bounded software barrier.  Block operations follow the
+// grid with the bounded software barrier -- or, for such wide systems,
+// tagged sweeps with no barrier per level (see the tagged-sweep section).  Block operations follow the
 // reference's order (FieldMatrix::rightmultiply, mmv, the cofactor
 // inverse); the products are contracted to FMAs (on this GPU an FP64 warp
 // instruction is the scarce resource: contraction measured 1.6x faster
