@@ -543,9 +543,13 @@ void* gbfv_batch_stream(gbfv_batch* batch);
  * gbfv_batch_system) until gbfv_serve_release frees its device memory.
  * Admission by HBM footprint is the caller's policy, with
  * gbfv_footprint_bytes as the estimate of one system.                    */
-/* estimated device bytes of one system (context + solver buffers); -1 for
- * a size no context takes (num_cells outside 1..GBFV_MAX_CELLS, block size
- * other than 2 or 3, dim other than 2 or 3)                               */
+/* estimated device bytes of one system (context + solver buffers) as a
+ * batch or a server holds it; -1 for a size no context takes (num_cells
+ * outside 1..GBFV_MAX_CELLS, block size other than 2 or 3, dim other than
+ * 2 or 3).  A stand-alone context of more than 65,536 cells whose
+ * autotuner picks the tagged sweeps also holds their copy of the factors
+ * and vectors (about 320 B per cell in FP32, 650 B in FP64 at b = 3, dim = 3, plus
+ * 48 B of tagged words), not counted here.                                */
 int64_t gbfv_footprint_bytes(int num_cells, int block_size, int dim);
 gbfv_batch* gbfv_serve_create(int capacity, int model, const gbfv_params* params,
                               int cluster_size, int max_cells, int* status);
